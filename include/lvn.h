@@ -1,0 +1,228 @@
+/*
+ * lvn.h -- C ABI of the GB300-native chunk-meshing library (liblvn.so).
+ *
+ * Drop-in replacement for the OpenCL compute layer of the leven voxel engine
+ * (leven/src/compute.h:35-77).  Every entry point below names the reference
+ * interface it replaces.  Conventions carried over from the reference:
+ *   - int return: 0 on success, a negative code on failure (compute.h:12);
+ *   - chunk `min` and `size` are world units, 1 voxel = 4 world units at
+ *     LOD0; the density-space offset is min / 4 and sampleScale is
+ *     size / (voxels_per_chunk * 4) (compute.cpp:569-577);
+ *   - not thread-safe: global state (noise seed, stored CSG operations) is
+ *     shared, and one mesh-generation context is driven from one thread
+ *     (compute.cpp:168-191).
+ * Struct layouts are byte-identical to the reference's CSGOperationInfo,
+ * MeshVertex, MeshTriangle and SeamNodeInfo.
+ *
+ * No torch or CUDA types appear in the signatures; a CUDA stream is passed as
+ * an opaque pointer.
+ */
+#ifndef LVN_H
+#define LVN_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- error codes (negative, like the reference's CL codes) ------------- */
+#define LVN_OK                  0
+#define LVN_ERR_NO_DEVICE      (-1)     /* CL_DEVICE_NOT_FOUND analogue          */
+#define LVN_ERR_OUT_OF_MEMORY  (-5)     /* CL_OUT_OF_RESOURCES analogue          */
+#define LVN_ERR_INVALID        (-30)    /* CL_INVALID_VALUE analogue             */
+#define LVN_ERR_CAPACITY       (-100)   /* caller buffer too small; counts set   */
+#define LVN_ERR_NOT_INITIALISED (-101)
+#define LVN_ERR_HASH           (-102)   /* cuckoo insert failed after retries    */
+#define LVN_ERR_DEVICE_STATUS  (-103)   /* a kernel reported an internal limit   */
+#define LVN_ERR_CUDA           (-99999) /* LVN_CL_ERROR (compute.h:12) analogue  */
+
+/* ---- density selector (new; the reference hard-codes Terrain) ---------- */
+#define LVN_DENSITY_REFERENCE 0   /* Terrain: ridged x billow + fBm (noise.cl:205-268) */
+#define LVN_DENSITY_FBM2D     1   /* y - amp2 * fBm2D(xz)                              */
+#define LVN_DENSITY_CAVES     2   /* y - amp2 * fBm2D(xz) + amp3 * fBm3D(xyz)           */
+
+#define LVN_MEMORY_HOST   0
+#define LVN_MEMORY_DEVICE 1
+
+/* mesh-generation options (lvn_meshgen_set_option) */
+#define LVN_OPT_CROSSING_MODE 1   /* 0 = 17-sample search (reference), 1 = linear     */
+#define LVN_OPT_CACHE         2   /* 1 = keep density-field / octree caches (default) */
+#define LVN_OPT_PROFILE       3   /* 1 = record per-stage CUDA events                 */
+
+/* CSGOperationInfo (leven/src/compute.h:16-24; apply_csg_operation.cl:5-14), 48 B */
+typedef struct lvn_csg_op {
+    int32_t type;          /* 0 = add (union), 1 = subtract           */
+    int32_t brush_shape;   /* RenderShape: 0 = cube, 1 = sphere       */
+    int32_t material;      /* 0..255                                  */
+    float   rotate_y;      /* radians, cube brushes                   */
+    float   origin[4];     /* density units                           */
+    float   dimensions[4]; /* half extents (cube) / radius in [0]     */
+} lvn_csg_op;
+
+/* MeshVertex (leven/src/render_types.h:24-38), 48 B */
+typedef struct lvn_mesh_vertex {
+    float position[4];
+    float normal[4];
+    float colour[4];       /* rgb = LOD colour, a = dominant material */
+} lvn_mesh_vertex;
+
+/* MeshTriangle (leven/src/render_types.h:42-58), 12 B, chunk-local indices */
+typedef struct lvn_mesh_triangle {
+    int32_t indices[3];
+} lvn_mesh_triangle;
+
+/* SeamNodeInfo (leven/src/compute.h:26-31), 48 B */
+typedef struct lvn_seam_node {
+    int32_t localspace_min[4]; /* voxel xyz, w = material << 8 | corners */
+    float   position[4];
+    float   normal[4];
+} lvn_seam_node;
+
+/* density parameters (new) */
+typedef struct lvn_density_params {
+    int32_t mode;          /* LVN_DENSITY_*                             */
+    int32_t octaves2;      /* 2D fBm: octaves, base frequency (1/voxel), */
+    float   freq2;         /*   lacunarity, gain, amplitude (voxels)     */
+    float   lacunarity2;
+    float   gain2;
+    float   amp2;
+    int32_t octaves3;      /* 3D cave fBm, same parameters               */
+    float   freq3;
+    float   lacunarity3;
+    float   gain3;
+    float   amp3;
+} lvn_density_params;
+
+/* Output of one generateChunkMesh call.  The caller owns the arrays (host or
+ * device memory per `memory`) and sets the capacities; the callee fills the
+ * counts.  When an array is too small nothing is written to it,
+ * LVN_ERR_CAPACITY is returned and the counts give the required sizes.  The
+ * reference's fixed MeshBuffer arrays (render_types.h:62-90) become these
+ * caller-sized arrays; the 14,336-vertex cap is lifted. */
+typedef struct lvn_mesh_out {
+    int32_t            memory;
+    lvn_mesh_vertex*   vertices;
+    int32_t            vertex_capacity;
+    int32_t            num_vertices;
+    lvn_mesh_triangle* triangles;
+    int32_t            triangle_capacity;
+    int32_t            num_triangles;
+    lvn_seam_node*     seams;
+    int32_t            seam_capacity;
+    int32_t            num_seams;
+} lvn_mesh_out;
+
+/* one chunk of a batch: world-space min and size (as generateChunkMesh) */
+typedef struct lvn_chunk_desc {
+    int32_t min[3];
+    int32_t size;
+} lvn_chunk_desc;
+
+/* per-chunk result of a batch; offsets index the batch arrays */
+typedef struct lvn_chunk_result {
+    int32_t vertex_offset;
+    int32_t num_vertices;     /* 0 when the chunk has no triangles (compute_octree.cpp:227-232) */
+    int32_t triangle_offset;
+    int32_t num_triangles;
+    int32_t seam_offset;
+    int32_t num_seams;
+    int32_t num_edges;        /* active field edges after CSG */
+    int32_t num_nodes;        /* active voxels (leaf nodes)   */
+} lvn_chunk_result;
+
+typedef struct lvn_batch_out {
+    int32_t            memory;          /* LVN_MEMORY_HOST / LVN_MEMORY_DEVICE */
+    lvn_mesh_vertex*   vertices;
+    int64_t            vertex_capacity;
+    int64_t            total_vertices;  /* vertex slots used (all leaves)      */
+    lvn_mesh_triangle* triangles;
+    int64_t            triangle_capacity;
+    int64_t            total_triangles;
+    lvn_seam_node*     seams;
+    int64_t            seam_capacity;
+    int64_t            total_seams;
+    lvn_chunk_result*  chunks;          /* host array, one entry per chunk     */
+} lvn_batch_out;
+
+typedef struct lvn_meshgen lvn_meshgen;
+
+/* ---- global compute state --------------------------------------------- */
+
+/* Compute_Initialise (compute.h:35; compute.cpp:195-232): selects device 0,
+ * builds the noise permutation image for `noise_seed`. */
+int lvn_initialise(int32_t noise_seed, uint32_t default_material, int32_t num_csg_brushes);
+/* Compute_Shutdown (compute.h:36; compute.cpp:236-239) */
+int lvn_shutdown(void);
+/* Compute_SetNoiseSeed (compute.h:38; compute_density_field.cpp:129-134) */
+int lvn_set_noise_seed(int32_t noise_seed);
+/* Compute_StoreCSGOperation (compute.h:39; compute_density_field.cpp:312-317);
+ * aabb_min/aabb_max are the AABB fields of the reference's AABB (aabb.h:168-259) */
+int lvn_store_csg_operation(const lvn_csg_op* op, const int32_t aabb_min[3], const int32_t aabb_max[3]);
+/* Compute_ClearCSGOperations (compute.h:40; compute_density_field.cpp:321-326) */
+int lvn_clear_csg_operations(void);
+/* CalcCSGOperationBounds (clipmap.cpp:1638-1643): the AABB the engine stores
+ * with an operation */
+int lvn_csg_operation_bounds(const lvn_csg_op* op, int32_t aabb_min[3], int32_t aabb_max[3]);
+/* new: density function selector (the reference's DensityFunc, noise.cl:225-268,
+ * is mode LVN_DENSITY_REFERENCE) */
+int lvn_set_density(const lvn_density_params* params);
+/* GetCLErrorString (compute.h:81) */
+const char* lvn_error_string(int32_t code);
+
+/* ---- mesh-generation context (class Compute_MeshGenContext, compute.h:46-77) */
+
+/* Compute_MeshGenContext::create (compute.h:50; compute.cpp:605-610,
+ * 245-312); NULL on failure.  voxels_per_chunk: 8, 16, 32 or 64. */
+lvn_meshgen* lvn_meshgen_create(int32_t voxels_per_chunk);
+void         lvn_meshgen_destroy(lvn_meshgen* ctx);
+/* Compute_MeshGenContext::voxelsPerChunk (compute.h:52; compute.cpp:612-615) */
+int lvn_meshgen_voxels_per_chunk(const lvn_meshgen* ctx);
+/* Compute_MeshGenContext::applyCSGOperations (compute.h:54-57; compute_csg.cpp:224-242) */
+int lvn_meshgen_apply_csg_operations(lvn_meshgen* ctx, const lvn_csg_op* ops, int32_t num_ops,
+                                     const int32_t min[3], int32_t size);
+/* Compute_MeshGenContext::freeChunkOctree (compute.h:59-61; compute_octree.cpp:379-387) */
+int lvn_meshgen_free_chunk_octree(lvn_meshgen* ctx, const int32_t min[3], int32_t size);
+/* Compute_MeshGenContext::isChunkEmpty (compute.h:63-66; compute_density_field.cpp:278-299).
+ * *is_empty = 1 when the chunk's field has no active edge (the reference
+ * returns the inverse, numEdges > 0; that call site is unreachable). */
+int lvn_meshgen_is_chunk_empty(lvn_meshgen* ctx, const int32_t min[3], int32_t size, int32_t* is_empty);
+/* Compute_MeshGenContext::generateChunkMesh (compute.h:68-72; compute_octree.cpp:351-375) */
+int lvn_meshgen_generate_chunk_mesh(lvn_meshgen* ctx, const int32_t min[3], int32_t size, lvn_mesh_out* out);
+
+/* new: mesh `num_chunks` chunks in one batched pass on the GPU.  Each chunk is
+ * generated exactly as generateChunkMesh would on a cold cache (fresh field,
+ * stored CSG operations whose AABB overlaps the chunk replayed in store
+ * order); the caches are neither read nor written. */
+int lvn_meshgen_generate_chunks(lvn_meshgen* ctx, const lvn_chunk_desc* chunks, int32_t num_chunks,
+                                lvn_batch_out* out);
+
+/* new: execution control */
+int   lvn_meshgen_set_stream(lvn_meshgen* ctx, void* cuda_stream);
+void* lvn_meshgen_get_stream(lvn_meshgen* ctx);
+int   lvn_meshgen_set_option(lvn_meshgen* ctx, int32_t option, int32_t value);
+/* per-stage device times (ms) accumulated while LVN_OPT_PROFILE is on;
+ * returns the number of stages, names via lvn_meshgen_stage_name */
+int         lvn_meshgen_stage_times(lvn_meshgen* ctx, float* ms, int32_t* launches, int32_t capacity);
+const char* lvn_meshgen_stage_name(int32_t stage);
+int         lvn_meshgen_reset_stage_times(lvn_meshgen* ctx);
+
+/* new: intermediate buffers of chunk `chunk` of the last batch, for
+ * stage-level parity checks (what = LVN_DEBUG_*).  Returns the element count,
+ * or LVN_ERR_CAPACITY when cap_bytes is too small. */
+#define LVN_DEBUG_MATERIALS    0  /* uint8[F]   final field materials           */
+#define LVN_DEBUG_EDGE_KEYS    1  /* int32[E]   edge keys, final list order     */
+#define LVN_DEBUG_EDGE_INFO    2  /* float4[E]  (normal.xyz, t)                 */
+#define LVN_DEBUG_NODE_CODES   3  /* uint32[V]                                  */
+#define LVN_DEBUG_NODE_INFO    4  /* int32[V]   edges << 16 | material << 8 | corners */
+#define LVN_DEBUG_EDGE_TABLE   5  /* uint64[prime] edge cuckoo table            */
+#define LVN_DEBUG_EDGE_STASH   6  /* uint64[101]                                */
+#define LVN_DEBUG_NODE_TABLE   7  /* uint64[prime] node cuckoo table            */
+#define LVN_DEBUG_NODE_STASH   8  /* uint64[101]                                */
+#define LVN_DEBUG_PLAIN_EDGES  9  /* int32       number of plain (non-CSG) edges */
+int64_t lvn_meshgen_debug_fetch(lvn_meshgen* ctx, int32_t what, int32_t chunk, void* host, int64_t cap_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LVN_H */

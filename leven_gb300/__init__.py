@@ -1,0 +1,302 @@
+"""Python binding of liblvn, the GB300-native chunk-meshing library.
+
+Mirrors the reference engine's compute interface (leven/src/compute.h:35-77):
+module functions for the global state (initialise, set_noise_seed,
+store_csg_operation, clear_csg_operations) and `MeshGen` for the
+Compute_MeshGenContext methods (apply_csg_operations, free_chunk_octree,
+is_chunk_empty, generate_chunk_mesh), plus the batched `generate_chunks`.
+Errors surface as `LvnError` carrying the library's negative code.
+
+The compute path is liblvn.so only: if the library is missing this module
+raises on first use; nothing falls back to a CPU implementation.
+"""
+import ctypes as C
+import pathlib
+
+import numpy as np
+
+_PKG = pathlib.Path(__file__).resolve().parent
+LIB_PATH = _PKG / "liblvn.so"
+
+LVN_OK = 0
+LVN_ERR_CAPACITY = -100
+LVN_MEMORY_HOST = 0
+LVN_MEMORY_DEVICE = 1
+LVN_DENSITY_REFERENCE, LVN_DENSITY_FBM2D, LVN_DENSITY_CAVES = 0, 1, 2
+LVN_OPT_CROSSING_MODE, LVN_OPT_CACHE, LVN_OPT_PROFILE = 1, 2, 3
+(DEBUG_MATERIALS, DEBUG_EDGE_KEYS, DEBUG_EDGE_INFO, DEBUG_NODE_CODES, DEBUG_NODE_INFO, DEBUG_EDGE_TABLE,
+ DEBUG_EDGE_STASH, DEBUG_NODE_TABLE, DEBUG_NODE_STASH, DEBUG_PLAIN_EDGES) = range(10)
+
+
+class LvnError(RuntimeError):
+    def __init__(self, code, what=""):
+        self.code = code
+        super().__init__(f"{what}: {error_string(code)} ({code})")
+
+
+class CsgOp(C.Structure):
+    """CSGOperationInfo (leven/src/compute.h:16-24)."""
+    _fields_ = [("type", C.c_int32), ("brush_shape", C.c_int32), ("material", C.c_int32),
+                ("rotate_y", C.c_float), ("origin", C.c_float * 4), ("dimensions", C.c_float * 4)]
+
+
+class DensityParams(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("octaves2", C.c_int32), ("freq2", C.c_float), ("lacunarity2", C.c_float),
+                ("gain2", C.c_float), ("amp2", C.c_float), ("octaves3", C.c_int32), ("freq3", C.c_float),
+                ("lacunarity3", C.c_float), ("gain3", C.c_float), ("amp3", C.c_float)]
+
+
+class MeshOut(C.Structure):
+    _fields_ = [("memory", C.c_int32), ("vertices", C.c_void_p), ("vertex_capacity", C.c_int32),
+                ("num_vertices", C.c_int32), ("triangles", C.c_void_p), ("triangle_capacity", C.c_int32),
+                ("num_triangles", C.c_int32), ("seams", C.c_void_p), ("seam_capacity", C.c_int32),
+                ("num_seams", C.c_int32)]
+
+
+class ChunkDesc(C.Structure):
+    _fields_ = [("min", C.c_int32 * 3), ("size", C.c_int32)]
+
+
+class ChunkResult(C.Structure):
+    _fields_ = [("vertex_offset", C.c_int32), ("num_vertices", C.c_int32), ("triangle_offset", C.c_int32),
+                ("num_triangles", C.c_int32), ("seam_offset", C.c_int32), ("num_seams", C.c_int32),
+                ("num_edges", C.c_int32), ("num_nodes", C.c_int32)]
+
+
+class BatchOut(C.Structure):
+    _fields_ = [("memory", C.c_int32), ("vertices", C.c_void_p), ("vertex_capacity", C.c_int64),
+                ("total_vertices", C.c_int64), ("triangles", C.c_void_p), ("triangle_capacity", C.c_int64),
+                ("total_triangles", C.c_int64), ("seams", C.c_void_p), ("seam_capacity", C.c_int64),
+                ("total_seams", C.c_int64), ("chunks", C.POINTER(ChunkResult))]
+
+
+# every symbol include/lvn.h declares
+EXPORTS = [
+    "lvn_initialise", "lvn_shutdown", "lvn_set_noise_seed", "lvn_store_csg_operation", "lvn_clear_csg_operations",
+    "lvn_csg_operation_bounds", "lvn_set_density", "lvn_error_string", "lvn_meshgen_create", "lvn_meshgen_destroy",
+    "lvn_meshgen_voxels_per_chunk", "lvn_meshgen_apply_csg_operations", "lvn_meshgen_free_chunk_octree",
+    "lvn_meshgen_is_chunk_empty", "lvn_meshgen_generate_chunk_mesh", "lvn_meshgen_generate_chunks",
+    "lvn_meshgen_set_stream", "lvn_meshgen_get_stream", "lvn_meshgen_set_option", "lvn_meshgen_stage_times",
+    "lvn_meshgen_stage_name", "lvn_meshgen_reset_stage_times", "lvn_meshgen_debug_fetch",
+]
+
+_lib = None
+
+
+def lib():
+    """Loads liblvn.so (built in-tree by leven_gb300.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} is missing: run `python -c 'import __graft_entry__ as g; g.build()'`")
+    L = C.CDLL(str(LIB_PATH))
+    i32p = C.POINTER(C.c_int32)
+    L.lvn_initialise.argtypes = [C.c_int32, C.c_uint32, C.c_int32]
+    L.lvn_set_noise_seed.argtypes = [C.c_int32]
+    L.lvn_store_csg_operation.argtypes = [C.POINTER(CsgOp), i32p, i32p]
+    L.lvn_csg_operation_bounds.argtypes = [C.POINTER(CsgOp), i32p, i32p]
+    L.lvn_set_density.argtypes = [C.POINTER(DensityParams)]
+    L.lvn_error_string.argtypes = [C.c_int32]
+    L.lvn_error_string.restype = C.c_char_p
+    L.lvn_meshgen_create.argtypes = [C.c_int32]
+    L.lvn_meshgen_create.restype = C.c_void_p
+    L.lvn_meshgen_destroy.argtypes = [C.c_void_p]
+    L.lvn_meshgen_destroy.restype = None
+    L.lvn_meshgen_voxels_per_chunk.argtypes = [C.c_void_p]
+    L.lvn_meshgen_apply_csg_operations.argtypes = [C.c_void_p, C.POINTER(CsgOp), C.c_int32, i32p, C.c_int32]
+    L.lvn_meshgen_free_chunk_octree.argtypes = [C.c_void_p, i32p, C.c_int32]
+    L.lvn_meshgen_is_chunk_empty.argtypes = [C.c_void_p, i32p, C.c_int32, i32p]
+    L.lvn_meshgen_generate_chunk_mesh.argtypes = [C.c_void_p, i32p, C.c_int32, C.POINTER(MeshOut)]
+    L.lvn_meshgen_generate_chunks.argtypes = [C.c_void_p, C.POINTER(ChunkDesc), C.c_int32, C.POINTER(BatchOut)]
+    L.lvn_meshgen_set_stream.argtypes = [C.c_void_p, C.c_void_p]
+    L.lvn_meshgen_get_stream.argtypes = [C.c_void_p]
+    L.lvn_meshgen_get_stream.restype = C.c_void_p
+    L.lvn_meshgen_set_option.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
+    L.lvn_meshgen_stage_times.argtypes = [C.c_void_p, C.POINTER(C.c_float), i32p, C.c_int32]
+    L.lvn_meshgen_stage_name.argtypes = [C.c_int32]
+    L.lvn_meshgen_stage_name.restype = C.c_char_p
+    L.lvn_meshgen_reset_stage_times.argtypes = [C.c_void_p]
+    L.lvn_meshgen_debug_fetch.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int64]
+    L.lvn_meshgen_debug_fetch.restype = C.c_int64
+    _lib = L
+    return L
+
+
+def error_string(code):
+    try:
+        return lib().lvn_error_string(code).decode()
+    except ImportError:
+        return "liblvn unavailable"
+
+
+def _check(rc, what):
+    if rc < 0:
+        raise LvnError(rc, what)
+    return rc
+
+
+def _ivec3(v):
+    return (C.c_int32 * 3)(*[int(x) for x in v])
+
+
+def make_op(type_, brush_shape, material, origin, dimensions, rotate_y=0.0):
+    op = CsgOp()
+    op.type, op.brush_shape, op.material, op.rotate_y = type_, brush_shape, material, rotate_y
+    op.origin = (C.c_float * 4)(origin[0], origin[1], origin[2], 0.0)
+    op.dimensions = (C.c_float * 4)(dimensions[0], dimensions[1], dimensions[2], 0.0)
+    return op
+
+
+def initialise(noise_seed, default_material=0, num_csg_brushes=2):
+    """Compute_Initialise (compute.h:35)."""
+    return _check(lib().lvn_initialise(noise_seed, default_material, num_csg_brushes), "lvn_initialise")
+
+
+def shutdown():
+    return _check(lib().lvn_shutdown(), "lvn_shutdown")
+
+
+def set_noise_seed(seed):
+    return _check(lib().lvn_set_noise_seed(seed), "lvn_set_noise_seed")
+
+
+def set_density(mode=LVN_DENSITY_REFERENCE, octaves2=8, freq2=1.0 / 256, lacunarity2=2.0, gain2=0.5, amp2=48.0,
+                octaves3=6, freq3=1.0 / 64, lacunarity3=2.0, gain3=0.5, amp3=12.0):
+    p = DensityParams(mode, octaves2, freq2, lacunarity2, gain2, amp2, octaves3, freq3, lacunarity3, gain3, amp3)
+    return _check(lib().lvn_set_density(C.byref(p)), "lvn_set_density")
+
+
+def csg_operation_bounds(op):
+    lo, hi = (C.c_int32 * 3)(), (C.c_int32 * 3)()
+    _check(lib().lvn_csg_operation_bounds(C.byref(op), lo, hi), "lvn_csg_operation_bounds")
+    return list(lo), list(hi)
+
+
+def store_csg_operation(op, aabb=None):
+    """Compute_StoreCSGOperation (compute.h:39); the AABB defaults to the
+    engine's CalcCSGOperationBounds."""
+    lo, hi = aabb if aabb is not None else csg_operation_bounds(op)
+    return _check(lib().lvn_store_csg_operation(C.byref(op), _ivec3(lo), _ivec3(hi)), "lvn_store_csg_operation")
+
+
+def clear_csg_operations():
+    return _check(lib().lvn_clear_csg_operations(), "lvn_clear_csg_operations")
+
+
+class Mesh:
+    """Host copy of one chunk's generateChunkMesh output."""
+
+    def __init__(self, vertices, triangles, seams):
+        self.vertices = vertices    # float32 (V, 12): position, normal, colour
+        self.triangles = triangles  # int32 (T, 3)
+        self.seams = seams          # int32 (S, 12): localspaceMin (4 int), position, normal (as float bits)
+
+
+class MeshGen:
+    """Compute_MeshGenContext (compute.h:46-77) over liblvn."""
+
+    def __init__(self, voxels_per_chunk=64):
+        self._h = lib().lvn_meshgen_create(voxels_per_chunk)
+        if not self._h:
+            raise LvnError(-1, "lvn_meshgen_create")
+        self.voxels_per_chunk = voxels_per_chunk
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().lvn_meshgen_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_option(self, option, value):
+        return _check(lib().lvn_meshgen_set_option(self._h, option, value), "lvn_meshgen_set_option")
+
+    def stream(self):
+        return lib().lvn_meshgen_get_stream(self._h)
+
+    def set_stream(self, ptr):
+        return _check(lib().lvn_meshgen_set_stream(self._h, ptr), "lvn_meshgen_set_stream")
+
+    def apply_csg_operations(self, ops, min_xyz, size):
+        arr = (CsgOp * max(1, len(ops)))(*ops)
+        return _check(lib().lvn_meshgen_apply_csg_operations(self._h, arr, len(ops), _ivec3(min_xyz), size),
+                      "lvn_meshgen_apply_csg_operations")
+
+    def free_chunk_octree(self, min_xyz, size):
+        return _check(lib().lvn_meshgen_free_chunk_octree(self._h, _ivec3(min_xyz), size),
+                      "lvn_meshgen_free_chunk_octree")
+
+    def is_chunk_empty(self, min_xyz, size):
+        out = C.c_int32(0)
+        _check(lib().lvn_meshgen_is_chunk_empty(self._h, _ivec3(min_xyz), size, C.byref(out)),
+               "lvn_meshgen_is_chunk_empty")
+        return bool(out.value)
+
+    def generate_chunk_mesh(self, min_xyz, size, capacity=1 << 16):
+        while True:
+            v = np.zeros((capacity, 12), np.float32)
+            t = np.zeros((2 * capacity, 3), np.int32)
+            s = np.zeros((capacity, 12), np.int32)
+            out = MeshOut(LVN_MEMORY_HOST, v.ctypes.data, capacity, 0, t.ctypes.data, 2 * capacity, 0,
+                          s.ctypes.data, capacity, 0)
+            rc = lib().lvn_meshgen_generate_chunk_mesh(self._h, _ivec3(min_xyz), size, C.byref(out))
+            if rc == LVN_ERR_CAPACITY:
+                capacity = max(out.num_vertices, out.num_triangles, out.num_seams, capacity) * 2
+                continue
+            _check(rc, "lvn_meshgen_generate_chunk_mesh")
+            return Mesh(v[:out.num_vertices].copy(), t[:out.num_triangles].copy(), s[:out.num_seams].copy())
+
+    def generate_chunks(self, chunks, out=None):
+        """Batched generation.  `chunks`: iterable of (min_xyz, size).  Returns
+        (vertices, triangles, seams, results) as host arrays, results being a
+        numpy structured array of lvn_chunk_result."""
+        n = len(chunks)
+        descs = (ChunkDesc * max(1, n))()
+        for i, (mn, size) in enumerate(chunks):
+            descs[i] = ChunkDesc((C.c_int32 * 3)(*mn), size)
+        results = (ChunkResult * max(1, n))()
+        cap = 1 << 20
+        while True:
+            v = np.zeros((cap, 12), np.float32)
+            t = np.zeros((2 * cap, 3), np.int32)
+            s = np.zeros((cap, 12), np.int32)
+            bo = BatchOut(LVN_MEMORY_HOST, v.ctypes.data, cap, 0, t.ctypes.data, 2 * cap, 0, s.ctypes.data, cap, 0,
+                          C.cast(results, C.POINTER(ChunkResult)))
+            rc = lib().lvn_meshgen_generate_chunks(self._h, descs, n, C.byref(bo))
+            if rc == LVN_ERR_CAPACITY:
+                cap = int(max(bo.total_vertices, bo.total_triangles, bo.total_seams, cap) * 2)
+                continue
+            _check(rc, "lvn_meshgen_generate_chunks")
+            res = np.ctypeslib.as_array(C.cast(results, C.POINTER(C.c_int32)), shape=(max(1, n), 8))[:n].copy()
+            return (v[:bo.total_vertices].copy(), t[:bo.total_triangles].copy(), s[:bo.total_seams].copy(), res)
+
+    def generate_chunks_raw(self, descs, n, batch_out):
+        """Direct C-ABI call with caller-prepared ctypes structures."""
+        return lib().lvn_meshgen_generate_chunks(self._h, descs, n, C.byref(batch_out))
+
+    def debug_fetch(self, what, chunk, dtype, width=1, max_elems=1 << 22):
+        buf = np.zeros(max_elems * width, dtype=dtype)
+        n = lib().lvn_meshgen_debug_fetch(self._h, what, chunk, buf.ctypes.data, buf.nbytes)
+        _check(int(n), "lvn_meshgen_debug_fetch")
+        if what == DEBUG_PLAIN_EDGES:
+            return int(n)
+        out = buf[: n * width]
+        return out.reshape(n, width) if width > 1 else out
+
+    def stage_times(self):
+        ms = (C.c_float * 32)()
+        launches = (C.c_int32 * 32)()
+        n = lib().lvn_meshgen_stage_times(self._h, ms, launches, 32)
+        return {lib().lvn_meshgen_stage_name(i).decode(): (ms[i], launches[i]) for i in range(n)}
+
+    def reset_stage_times(self):
+        return lib().lvn_meshgen_reset_stage_times(self._h)

@@ -1,0 +1,1118 @@
+// lvn_api.cu -- host orchestration and the C ABI of liblvn (include/lvn.h).
+//
+// Replaces the reference's OpenCL host layer (leven/src/compute.cpp,
+// compute_density_field.cpp, compute_octree.cpp, compute_csg.cpp,
+// compute_cuckoo.cpp).  One CUDA stream per mesh-generation context; a batch
+// of chunks is enqueued as a fixed sequence of kernels with no host round
+// trip, then one small device-to-host read returns the per-chunk counts.
+// Device pools grow on demand and are reused across calls.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <random>
+#include <tuple>
+#include <vector>
+
+#include "lvn_kernels.cuh"
+
+using namespace lvn;
+
+namespace {
+
+#define LVN_CK(call)                                                                 \
+    do {                                                                             \
+        cudaError_t err__ = (call);                                                  \
+        if (err__ != cudaSuccess) {                                                  \
+            std::fprintf(stderr, "liblvn: %s failed: %s\n", #call, cudaGetErrorString(err__)); \
+            return err__ == cudaErrorMemoryAllocation ? LVN_ERR_OUT_OF_MEMORY : LVN_ERR_CUDA; \
+        }                                                                            \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// buffers
+// ---------------------------------------------------------------------------
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t need) {
+        if (need <= bytes && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        const size_t alloc = std::max<size_t>(need, 256);
+        cudaError_t e = cudaMalloc(&p, alloc);
+        if (e == cudaSuccess) bytes = alloc;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <typename T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+struct HostBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t need) {
+        if (need <= bytes && p) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+        const size_t alloc = std::max<size_t>(need, 256);
+        cudaError_t e = cudaMallocHost(&p, alloc);
+        if (e == cudaSuccess) bytes = alloc;
+        return e;
+    }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <typename T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+// ---------------------------------------------------------------------------
+// global compute state (compute.cpp:168-232, compute_density_field.cpp:23-24)
+// ---------------------------------------------------------------------------
+
+struct StoredOp {
+    lvn_csg_op op;
+    int32_t lo[3], hi[3];
+};
+
+struct Global {
+    bool initialised = false;
+    int device = 0;
+    int num_sms = 0;
+    int32_t default_material = 0;
+    int32_t seed = 0;
+    DevBuf perm, grad;
+    DensityParams density{LVN_DENSITY_REFERENCE, 8, 1.f / 256.f, 2.f, 0.5f, 48.f, 6, 1.f / 64.f, 2.f, 0.5f, 12.f};
+    std::vector<StoredOp> ops;
+    std::mt19937 hash_gen;  // default-seeded, drawn in call order (compute_cuckoo.cpp:46-47)
+} g;
+
+// Ken Perlin's reference permutation (public domain).
+const uint8_t kPerlin[256] = {
+    151, 160, 137, 91,  90,  15,  131, 13,  201, 95,  96,  53,  194, 233, 7,   225, 140, 36,  103, 30,  69,  142,
+    8,   99,  37,  240, 21,  10,  23,  190, 6,   148, 247, 120, 234, 75,  0,   26,  197, 62,  94,  252, 219, 203,
+    117, 35,  11,  32,  57,  177, 33,  88,  237, 149, 56,  87,  174, 20,  125, 136, 171, 168, 68,  175, 74,  165,
+    71,  134, 139, 48,  27,  166, 77,  146, 158, 231, 83,  111, 229, 122, 60,  211, 133, 230, 220, 105, 92,  41,
+    55,  46,  245, 40,  244, 102, 143, 54,  65,  25,  63,  161, 1,   216, 80,  73,  209, 76,  132, 187, 208, 89,
+    18,  169, 200, 196, 135, 130, 116, 188, 159, 86,  164, 100, 109, 198, 173, 186, 3,   64,  52,  217, 226, 250,
+    124, 123, 5,   202, 38,  147, 118, 126, 255, 82,  85,  212, 207, 206, 59,  227, 47,  16,  58,  17,  182, 189,
+    28,  42,  223, 183, 170, 213, 119, 248, 152, 2,   44,  154, 163, 70,  221, 153, 101, 155, 167, 43,  172, 9,
+    129, 22,  39,  253, 19,  98,  108, 110, 79,  113, 224, 232, 178, 185, 112, 104, 218, 246, 97,  228, 251, 34,
+    242, 193, 238, 210, 144, 12,  191, 179, 162, 241, 81,  51,  145, 235, 249, 14,  239, 107, 49,  192, 214, 31,
+    181, 199, 106, 157, 184, 84,  204, 176, 115, 121, 50,  45,  127, 4,   150, 254, 138, 236, 205, 93,  222, 114,
+    67,  29,  24,  72,  243, 141, 128, 195, 78,  66,  215, 61,  156, 180};
+
+// gradient directions (compute_density_field.cpp:60-63)
+const int8_t kGrad3[16][3] = {{0, 1, 1},  {0, 1, -1},  {0, -1, 1}, {0, -1, -1}, {1, 0, 1},  {1, 0, -1},
+                              {-1, 0, 1}, {-1, 0, -1}, {1, 1, 0},  {1, -1, 0},  {-1, 1, 0}, {-1, -1, 0},
+                              {1, 0, -1}, {-1, 0, -1}, {0, -1, 1}, {0, 1, 1}};
+
+// Jenkins one-at-a-time over the key's little-endian bytes (compute_density_field.cpp:68-86)
+uint32_t noise_hash(int x, int y, int seed) {
+    const uint32_t key = (((uint32_t)x << 24) | ((uint32_t)y << 16)) ^ (uint32_t)seed;
+    uint32_t h = 0;
+    for (int i = 0; i < 4; i++) {
+        h += (key >> (8 * i)) & 0xffu;
+        h += h << 10;
+        h ^= h >> 6;
+    }
+    h += h << 3;
+    h ^= h >> 11;
+    h += h << 15;
+    return h;
+}
+
+// CreateNoisePermutationLookupImage (compute_density_field.cpp:90-125): the
+// 512-entry literal there holds Perlin's 256 values, then the same list
+// without its first six, then six zeros; it is shuffled with the seeded
+// default engine and sampled per texel by the Jenkins hash.
+int upload_perm(int seed) {
+    std::array<int, 512> perm{};
+    for (int i = 0; i < 256; i++) perm[i] = kPerlin[i];
+    for (int k = 0; k < 250; k++) perm[256 + k] = kPerlin[6 + k];
+    std::shuffle(perm.begin(), perm.end(), std::default_random_engine(seed));
+    std::vector<uint8_t> v(65536);
+    for (int i = 0; i < 256; i++)
+        for (int j = 0; j < 256; j++) v[i * 256 + j] = (uint8_t)perm[noise_hash(i, j, seed) & 0x1ff];
+    // RGB as read_imagef returns UNORM8: (b / 255) * 4 - 1
+    float grad[64];
+    for (int k = 0; k < 16; k++) {
+        for (int c = 0; c < 3; c++) {
+            const unsigned char b = (unsigned char)(kGrad3[k][c] * 64 + 64);
+            grad[4 * k + c] = ((float)b / 255.0f) * 4.0f - 1.0f;
+        }
+        grad[4 * k + 3] = 0.f;
+    }
+    LVN_CK(g.perm.ensure(65536));
+    LVN_CK(g.grad.ensure(sizeof(grad)));
+    LVN_CK(cudaMemcpy(g.perm.p, v.data(), 65536, cudaMemcpyHostToDevice));
+    LVN_CK(cudaMemcpy(g.grad.p, grad, sizeof(grad), cudaMemcpyHostToDevice));
+    g.seed = seed;
+    return LVN_OK;
+}
+
+// CalcCSGOperationBounds (clipmap.cpp:1638-1643): CSG_OFFSET 0.5, fudge 2,
+// ivec3(float) truncation
+void op_bounds(const lvn_csg_op& op, int32_t lo[3], int32_t hi[3]) {
+    for (int i = 0; i < 3; i++) {
+        const int half = (int)(op.dimensions[i] * (float)LEAF_SIZE_SCALE) + 2;
+        const int origin = (int)((op.origin[i] - 0.5f) * (float)LEAF_SIZE_SCALE);
+        lo[i] = origin - half;
+        hi[i] = origin + half;
+    }
+}
+
+// AABB::overlaps (aabb.h:26-35), inclusive bounds
+bool overlaps(const int32_t alo[3], const int32_t ahi[3], const int32_t blo[3], const int32_t bhi[3]) {
+    return !(ahi[0] < blo[0] || ahi[1] < blo[1] || ahi[2] < blo[2] || alo[0] > bhi[0] || alo[1] > bhi[1] ||
+             alo[2] > bhi[2]);
+}
+
+Brush make_brush(const lvn_csg_op& op) {
+    Brush b;
+    for (int i = 0; i < 3; i++) {
+        b.origin[i] = op.origin[i];
+        b.dimensions[i] = op.dimensions[i];
+    }
+    b.type = op.type;
+    b.brush = op.brush_shape;
+    b.cos_y = (float)std::cos((double)op.rotate_y);
+    b.sin_y = (float)std::sin((double)op.rotate_y);
+    b.material = op.material;
+    b.pad = 0;
+    return b;
+}
+
+bool valid_op(const lvn_csg_op& op) {
+    return (op.type == 0 || op.type == 1) && (op.brush_shape == 0 || op.brush_shape == 1) && op.material >= 0 &&
+           op.material <= 255;
+}
+
+// ColourForMinLeafSize (clipmap.cpp:329-353)
+void lod_colour(int s, float c[3]) {
+    switch (s) {
+        case 1: c[0] = 0.3f; c[1] = 0.1f; c[2] = 0.f; break;
+        case 2: c[0] = 0.f; c[1] = 0.f; c[2] = 0.5f; break;
+        case 4: c[0] = 0.f; c[1] = 0.5f; c[2] = 0.5f; break;
+        case 8: c[0] = 0.5f; c[1] = 0.f; c[2] = 0.5f; break;
+        case 16: c[0] = 0.f; c[1] = 0.5f; c[2] = 0.f; break;
+        default: c[0] = 0.5f; c[1] = 0.f; c[2] = 0.f; break;
+    }
+}
+
+void draw_params(uint32_t* p) {
+    std::uniform_int_distribution<uint32_t> dist(1u << 15, 1u << 30);
+    for (int i = 0; i < CUCKOO_HASH_FN_COUNT * 2; i++) p[i] = dist(g.hash_gen);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// mesh-generation context
+// ---------------------------------------------------------------------------
+
+typedef std::tuple<int32_t, int32_t, int32_t, int32_t> ChunkKey;
+
+struct FieldEntry {  // GPUDensityField (compute_local.h:28-37)
+    DevBuf corners;
+    DevBuf keys, info;
+    int32_t num_edges = 0;
+    int32_t last_op = 0;
+};
+
+struct OctreeEntry {  // the mesh a cached GPUOctree (compute_local.h:43-49) regenerates
+    std::vector<lvn_mesh_vertex> vertices;
+    std::vector<lvn_mesh_triangle> triangles;
+    std::vector<lvn_seam_node> seams;
+    int32_t num_vertices = 0;
+};
+
+struct lvn_meshgen {
+    int vpc = 64;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int crossing_mode = 0;
+    bool cache = true;
+    bool profile = false;
+
+    // pools
+    DevBuf desc, cs, bs, brushes, corners, edge_tiles, vox_tiles;
+    DevBuf edge_keys, edge_chunk, edge_info, node_codes, node_info, node_chunk;
+    DevBuf edge_slots, node_slots, quad_scratch, node_tile_counts, chunk_tile_off;
+    DevBuf vertices, triangles, seams;
+    HostBuf h_desc, h_brushes, h_cs, h_bs;
+    int64_t ecap = 0, vcap = 0, eslot_cap = 0, nslot_cap = 0, ntile_cap = 0;
+    int64_t vert_cap = 0, tri_cap = 0, seam_cap = 0;
+    int chunk_cap = 0;
+
+    // last batch, for debug fetch
+    int last_n = 0;
+    std::vector<ChunkState> last_cs;
+
+    // profiling
+    cudaEvent_t ev[ST_COUNT + 1] = {};
+    double stage_ms[ST_COUNT] = {};
+    int stage_launches[ST_COUNT] = {};
+
+    std::map<ChunkKey, FieldEntry> fields;
+    std::map<ChunkKey, OctreeEntry> octrees;
+};
+
+namespace {
+
+struct Capacity {
+    int64_t ecap, vcap;
+};
+
+// Size every pool for `n` chunks with at least the given edge / node capacity.
+int ensure_pools(lvn_meshgen* m, int n, Capacity want) {
+    const int F = field_size(m->vpc);
+    const int C = m->vpc * m->vpc * m->vpc;
+    const int64_t ecap = std::max<int64_t>(want.ecap, 1024);
+    const int64_t vcap = std::max<int64_t>(want.vcap, 1024);
+    LVN_CK(m->desc.ensure(sizeof(ChunkDesc) * n));
+    LVN_CK(m->cs.ensure(sizeof(ChunkState) * n));
+    LVN_CK(m->bs.ensure(sizeof(BatchState)));
+    LVN_CK(m->corners.ensure(sizeof(uint16_t) * (size_t)F * n));
+    LVN_CK(m->edge_tiles.ensure(sizeof(int2) * (size_t)edge_tiles_per_chunk(m->vpc) * n));
+    LVN_CK(m->vox_tiles.ensure(sizeof(int) * (size_t)vox_tiles_per_chunk(m->vpc) * n));
+    LVN_CK(m->chunk_tile_off.ensure(sizeof(int) * (size_t)(n + 1)));
+    LVN_CK(m->h_desc.ensure(sizeof(ChunkDesc) * n));
+    LVN_CK(m->h_cs.ensure(sizeof(ChunkState) * n));
+    LVN_CK(m->h_bs.ensure(sizeof(BatchState)));
+    if (ecap > m->ecap) {
+        LVN_CK(m->edge_keys.ensure(sizeof(int32_t) * ecap));
+        LVN_CK(m->edge_chunk.ensure(sizeof(int32_t) * ecap));
+        LVN_CK(m->edge_info.ensure(sizeof(float4) * ecap));
+        m->ecap = ecap;
+    }
+    const int64_t eslots = 2 * m->ecap + (int64_t)n * (CUCKOO_MIN_TABLE_SIZE + CUCKOO_STASH_SIZE + 512);
+    if (eslots > m->eslot_cap) {
+        LVN_CK(m->edge_slots.ensure(sizeof(unsigned long long) * eslots));
+        m->eslot_cap = eslots;
+    }
+    if (vcap > m->vcap) {
+        LVN_CK(m->node_codes.ensure(sizeof(uint32_t) * vcap));
+        LVN_CK(m->node_info.ensure(sizeof(int32_t) * vcap));
+        LVN_CK(m->node_chunk.ensure(sizeof(int32_t) * vcap));
+        LVN_CK(m->quad_scratch.ensure(sizeof(int4) * 3 * vcap));
+        LVN_CK(m->vertices.ensure(sizeof(lvn_mesh_vertex) * vcap));
+        LVN_CK(m->triangles.ensure(sizeof(lvn_mesh_triangle) * 6 * vcap));
+        LVN_CK(m->seams.ensure(sizeof(lvn_seam_node) * vcap));
+        m->vcap = vcap;
+        m->vert_cap = vcap;
+        m->tri_cap = 6 * vcap;
+        m->seam_cap = vcap;
+    }
+    const int64_t nslots = 2 * m->vcap + (int64_t)n * (CUCKOO_MIN_TABLE_SIZE + CUCKOO_STASH_SIZE + 512);
+    if (nslots > m->nslot_cap) {
+        LVN_CK(m->node_slots.ensure(sizeof(unsigned long long) * nslots));
+        m->nslot_cap = nslots;
+    }
+    const int64_t ntiles = m->vcap / kNodeTile + n + 1;
+    if (ntiles > m->ntile_cap) {
+        LVN_CK(m->node_tile_counts.ensure(sizeof(int2) * ntiles));
+        m->ntile_cap = ntiles;
+    }
+    (void)C;
+    m->chunk_cap = std::max(m->chunk_cap, n);
+    return LVN_OK;
+}
+
+Capacity default_capacity(const lvn_meshgen* m, int n) {
+    const int F = field_size(m->vpc);
+    const int C = m->vpc * m->vpc * m->vpc;
+    // per-chunk averages sized for surface chunks; one chunk's worst case always fits
+    return Capacity{(int64_t)n * (int64_t)std::min(3 * F, 48 * 1024) + 3 * (int64_t)F,
+                    (int64_t)n * (int64_t)std::min(C, 24 * 1024) + (int64_t)C};
+}
+
+BatchPtrs make_ptrs(lvn_meshgen* m, int n) {
+    BatchPtrs b;
+    std::memset(&b, 0, sizeof(b));
+    b.n = n;
+    b.vpc = m->vpc;
+    b.crossing_mode = m->crossing_mode;
+    b.plain_class = 1;
+    b.num_sms = g.num_sms;
+    b.density = g.density;
+    b.default_material = g.default_material;
+    b.desc = m->desc.as<ChunkDesc>();
+    b.cs = m->cs.as<ChunkState>();
+    b.bs = m->bs.as<BatchState>();
+    b.brushes = m->brushes.as<Brush>();
+    b.perm = g.perm.as<uint8_t>();
+    b.grad = g.grad.as<float>();
+    b.corners = m->corners.as<uint16_t>();
+    b.edge_tiles = m->edge_tiles.as<int2>();
+    b.vox_tiles = m->vox_tiles.as<int>();
+    b.edge_keys = m->edge_keys.as<int32_t>();
+    b.edge_chunk = m->edge_chunk.as<int32_t>();
+    b.edge_info = m->edge_info.as<float4>();
+    b.ecap = m->ecap;
+    b.node_codes = m->node_codes.as<uint32_t>();
+    b.node_info = m->node_info.as<int32_t>();
+    b.node_chunk = m->node_chunk.as<int32_t>();
+    b.vcap = m->vcap;
+    b.edge_slots = m->edge_slots.as<unsigned long long>();
+    b.edge_slot_cap = m->eslot_cap;
+    b.node_slots = m->node_slots.as<unsigned long long>();
+    b.node_slot_cap = m->nslot_cap;
+    b.quad_scratch = m->quad_scratch.as<int4>();
+    b.node_tile_counts = m->node_tile_counts.as<int2>();
+    b.chunk_tile_off = m->chunk_tile_off.as<int>();
+    b.node_tile_cap = m->ntile_cap;
+    b.vertices = m->vertices.as<lvn_mesh_vertex>();
+    b.vertex_cap = m->vert_cap;
+    b.triangles = m->triangles.as<lvn_mesh_triangle>();
+    b.triangle_cap = m->tri_cap;
+    b.seams = m->seams.as<lvn_seam_node>();
+    b.seam_cap = m->seam_cap;
+    return b;
+}
+
+typedef cudaError_t (*Launcher)(const BatchPtrs&, cudaStream_t);
+
+int stage(lvn_meshgen* m, int st, Launcher fn, const BatchPtrs& b) {
+    if (m->profile) LVN_CK(cudaEventRecord(m->ev[st], m->stream));
+    LVN_CK(fn(b, m->stream));
+    if (m->profile) {
+        LVN_CK(cudaEventRecord(m->ev[ST_COUNT], m->stream));
+        LVN_CK(cudaEventSynchronize(m->ev[ST_COUNT]));
+        float ms = 0.f;
+        LVN_CK(cudaEventElapsedTime(&ms, m->ev[st], m->ev[ST_COUNT]));
+        m->stage_ms[st] += ms;
+        m->stage_launches[st] += 1;
+    }
+    return LVN_OK;
+}
+
+#define LVN_STAGE(ST, FN)                        \
+    do {                                         \
+        const int rc__ = stage(m, ST, FN, b);    \
+        if (rc__ != LVN_OK) return rc__;         \
+    } while (0)
+
+// Field, CSG and edge stages for fresh fields (LoadDensityField on a cache
+// miss followed by the replay of stored operations).
+int enqueue_field_stages(lvn_meshgen* m, const BatchPtrs& b, bool any_ops) {
+    LVN_CK(launch_reset(b, m->stream));
+    LVN_STAGE(ST_FIELD, launch_field);
+    if (any_ops) LVN_STAGE(ST_CSG, launch_csg);
+    LVN_STAGE(ST_EDGE_COUNT, launch_edge_count);
+    LVN_STAGE(ST_EDGE_PLAN, launch_edge_plan);
+    LVN_STAGE(ST_EDGE_SCATTER, launch_edge_scatter);
+    LVN_STAGE(ST_HERMITE, launch_hermite);
+    return LVN_OK;
+}
+
+// ConstructOctreeFromField + GenerateMeshFromOctree + GatherSeamNodesFromOctree
+int enqueue_octree_stages(lvn_meshgen* m, const BatchPtrs& b) {
+    LVN_STAGE(ST_VOX_COUNT, launch_vox_count);
+    LVN_STAGE(ST_VOX_PLAN, launch_vox_plan);
+    LVN_STAGE(ST_VOX_SCATTER, launch_vox_scatter);
+    LVN_STAGE(ST_HASH_FILL, launch_hash_fill);
+    LVN_STAGE(ST_EDGE_INSERT, launch_edge_insert);
+    LVN_STAGE(ST_LEAF, launch_leaf);
+    LVN_STAGE(ST_NODE_INSERT, launch_node_insert);
+    LVN_STAGE(ST_MESH_COUNT, launch_mesh_count);
+    LVN_STAGE(ST_MESH_PLAN, launch_mesh_plan);
+    LVN_STAGE(ST_MESH_SCATTER, launch_mesh_scatter);
+    return LVN_OK;
+}
+
+int read_states(lvn_meshgen* m, int n) {
+    LVN_CK(cudaMemcpyAsync(m->h_cs.p, m->cs.p, sizeof(ChunkState) * n, cudaMemcpyDeviceToHost, m->stream));
+    LVN_CK(cudaMemcpyAsync(m->h_bs.p, m->bs.p, sizeof(BatchState), cudaMemcpyDeviceToHost, m->stream));
+    LVN_CK(cudaStreamSynchronize(m->stream));
+    m->last_n = n;
+    m->last_cs.assign(m->h_cs.as<ChunkState>(), m->h_cs.as<ChunkState>() + n);
+    return LVN_OK;
+}
+
+// Build the chunk descriptors of a batch of fresh chunks: density offset and
+// sample scale (compute_density_field.cpp:146-149), LOD colour, the stored
+// operations whose AABB overlaps the chunk (compute_density_field.cpp:255-265),
+// and cuckoo parameters for its two tables.
+int build_descs(lvn_meshgen* m, const lvn_chunk_desc* chunks, int n, std::vector<ChunkDesc>& descs,
+                std::vector<Brush>& brushes, bool with_stored_ops) {
+    descs.resize(n);
+    brushes.clear();
+    for (int c = 0; c < n; c++) {
+        const lvn_chunk_desc& in = chunks[c];
+        const int scale = in.size / (m->vpc * LEAF_SIZE_SCALE);
+        if (scale <= 0 || in.size % (m->vpc * LEAF_SIZE_SCALE) != 0) return LVN_ERR_INVALID;
+        ChunkDesc& d = descs[c];
+        std::memset(&d, 0, sizeof(d));
+        for (int i = 0; i < 3; i++) {
+            d.off[i] = in.min[i] / LEAF_SIZE_SCALE;
+            d.min[i] = in.min[i];
+        }
+        d.scale = scale;
+        d.size = in.size;
+        lod_colour(in.size / CLIPMAP_LEAF_SIZE, d.colour);
+        d.op_begin = (int32_t)brushes.size();
+        if (with_stored_ops) {
+            const int32_t lo[3] = {in.min[0], in.min[1], in.min[2]};
+            const int32_t hi[3] = {in.min[0] + in.size, in.min[1] + in.size, in.min[2] + in.size};
+            for (const StoredOp& s : g.ops)
+                if (overlaps(lo, hi, s.lo, s.hi)) brushes.push_back(make_brush(s.op));
+        }
+        d.op_count = (int32_t)brushes.size() - d.op_begin;
+        draw_params(d.edge_params);
+        draw_params(d.node_params);
+    }
+    return LVN_OK;
+}
+
+int upload(lvn_meshgen* m, const std::vector<ChunkDesc>& descs, const std::vector<Brush>& brushes) {
+    const int n = (int)descs.size();
+    std::memcpy(m->h_desc.p, descs.data(), sizeof(ChunkDesc) * n);
+    LVN_CK(cudaMemcpyAsync(m->desc.p, m->h_desc.p, sizeof(ChunkDesc) * n, cudaMemcpyHostToDevice, m->stream));
+    if (!brushes.empty()) {
+        LVN_CK(m->h_brushes.ensure(sizeof(Brush) * brushes.size()));
+        LVN_CK(m->brushes.ensure(sizeof(Brush) * brushes.size()));
+        std::memcpy(m->h_brushes.p, brushes.data(), sizeof(Brush) * brushes.size());
+        LVN_CK(cudaMemcpyAsync(m->brushes.p, m->h_brushes.p, sizeof(Brush) * brushes.size(), cudaMemcpyHostToDevice,
+                               m->stream));
+    } else {
+        LVN_CK(m->brushes.ensure(sizeof(Brush)));
+    }
+    return LVN_OK;
+}
+
+// Redraw cuckoo parameters for chunks whose insert failed (the reference
+// retries with fresh parameters, compute_cuckoo.cpp:89-132).
+bool redraw_failed(lvn_meshgen* m, std::vector<ChunkDesc>& descs) {
+    bool any = false;
+    const ChunkState* cs = m->h_cs.as<ChunkState>();
+    for (size_t c = 0; c < descs.size(); c++) {
+        if (cs[c].edge_insert_failed) { draw_params(descs[c].edge_params); any = true; }
+        if (cs[c].node_insert_failed) { draw_params(descs[c].node_params); any = true; }
+    }
+    return any;
+}
+
+constexpr int kMaxHashRetries = 16;
+
+// Run fresh chunks end to end into the internal pools (or the caller's device
+// buffers when `dev_out` is given).  Grows the pools and reruns once when a
+// pool overflowed; retries the hash with new parameters when an insert failed.
+int run_fresh_batch(lvn_meshgen* m, std::vector<ChunkDesc>& descs, const std::vector<Brush>& brushes,
+                    const lvn_batch_out* dev_out) {
+    const int n = (int)descs.size();
+    Capacity cap = default_capacity(m, n);
+    cap.ecap = std::max(cap.ecap, m->ecap);
+    cap.vcap = std::max(cap.vcap, m->vcap);
+    for (int attempt = 0; attempt < kMaxHashRetries + 2; attempt++) {
+        int rc = ensure_pools(m, n, cap);
+        if (rc) return rc;
+        rc = upload(m, descs, brushes);
+        if (rc) return rc;
+        BatchPtrs b = make_ptrs(m, n);
+        if (dev_out) {
+            b.vertices = dev_out->vertices;
+            b.vertex_cap = dev_out->vertex_capacity;
+            b.triangles = dev_out->triangles;
+            b.triangle_cap = dev_out->triangle_capacity;
+            b.seams = dev_out->seams;
+            b.seam_cap = dev_out->seam_capacity;
+        }
+        rc = enqueue_field_stages(m, b, !brushes.empty());
+        if (rc) return rc;
+        rc = enqueue_octree_stages(m, b);
+        if (rc) return rc;
+        rc = read_states(m, n);
+        if (rc) return rc;
+        const BatchState& bs = *m->h_bs.as<BatchState>();
+        if (bs.overflow) {
+            const bool user_short = dev_out && ((bs.overflow & (OVF_QUADS | OVF_SEAMS)) ||
+                                                ((bs.overflow & OVF_NODES) && bs.total_nodes > b.vertex_cap &&
+                                                 bs.total_nodes <= b.vcap));
+            if (user_short) return LVN_ERR_CAPACITY;
+            // grow to the sizes this run reported and try again
+            cap.ecap = std::max<int64_t>(cap.ecap, (int64_t)bs.total_edges + 1024);
+            if (bs.overflow & OVF_EDGE_SLOTS) cap.ecap = std::max<int64_t>(cap.ecap, bs.total_edge_slots);
+            if (bs.overflow & (OVF_NODES | OVF_NODE_SLOTS | OVF_QUADS | OVF_SEAMS))
+                cap.vcap = std::max<int64_t>(cap.vcap * 2, (int64_t)bs.total_nodes + 1024);
+            if (bs.overflow & OVF_EDGES) cap.ecap = std::max<int64_t>(cap.ecap * 2, (int64_t)bs.total_edges + 1024);
+            continue;
+        }
+        if (redraw_failed(m, descs)) continue;
+        return LVN_OK;
+    }
+    return LVN_ERR_HASH;
+}
+
+void fill_results(lvn_meshgen* m, int n, lvn_chunk_result* r) {
+    const ChunkState* cs = m->h_cs.as<ChunkState>();
+    for (int c = 0; c < n; c++) {
+        r[c].vertex_offset = cs[c].node_off;
+        r[c].num_vertices = cs[c].quads > 0 ? cs[c].nodes : 0;
+        r[c].triangle_offset = 2 * cs[c].quad_off;
+        r[c].num_triangles = 2 * cs[c].quads;
+        r[c].seam_offset = cs[c].seam_off;
+        r[c].num_seams = cs[c].seams;
+        r[c].num_edges = cs[c].num_edges;
+        r[c].num_nodes = cs[c].nodes;
+    }
+}
+
+int copy_out(lvn_meshgen* m, void* dst, const void* src, size_t bytes, int memory) {
+    if (bytes == 0) return LVN_OK;
+    LVN_CK(cudaMemcpyAsync(dst, src, bytes, memory == LVN_MEMORY_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                           m->stream));
+    return LVN_OK;
+}
+
+// ---- cached single-chunk path ---------------------------------------------
+
+ChunkKey key_of(const int32_t min[3], int32_t size) { return ChunkKey(min[0], min[1], min[2], size); }
+
+int one_desc(lvn_meshgen* m, const int32_t min[3], int32_t size, std::vector<ChunkDesc>& descs) {
+    lvn_chunk_desc cd;
+    for (int i = 0; i < 3; i++) cd.min[i] = min[i];
+    cd.size = size;
+    std::vector<Brush> none;
+    return build_descs(m, &cd, 1, descs, none, false);
+}
+
+// Copy the pool state of chunk 0 (corners + edge list) into a field entry.
+int save_field(lvn_meshgen* m, FieldEntry& f) {
+    const ChunkState& cs = m->last_cs[0];
+    const size_t F = (size_t)field_size(m->vpc);
+    LVN_CK(f.corners.ensure(sizeof(uint16_t) * F));
+    LVN_CK(cudaMemcpyAsync(f.corners.p, m->corners.p, sizeof(uint16_t) * F, cudaMemcpyDeviceToDevice, m->stream));
+    f.num_edges = cs.num_edges;
+    LVN_CK(f.keys.ensure(sizeof(int32_t) * std::max(1, cs.num_edges)));
+    LVN_CK(f.info.ensure(sizeof(float4) * std::max(1, cs.num_edges)));
+    LVN_CK(cudaMemcpyAsync(f.keys.p, m->edge_keys.p, sizeof(int32_t) * cs.num_edges, cudaMemcpyDeviceToDevice,
+                           m->stream));
+    LVN_CK(cudaMemcpyAsync(f.info.p, m->edge_info.p, sizeof(float4) * cs.num_edges, cudaMemcpyDeviceToDevice,
+                           m->stream));
+    LVN_CK(cudaStreamSynchronize(m->stream));
+    return LVN_OK;
+}
+
+// GenerateDefaultDensityField + FindDefaultEdges (compute_density_field.cpp:138-231)
+int generate_field(lvn_meshgen* m, const int32_t min[3], int32_t size, FieldEntry& f) {
+    std::vector<ChunkDesc> descs;
+    int rc = one_desc(m, min, size, descs);
+    if (rc) return rc;
+    Capacity cap = default_capacity(m, 1);
+    cap.ecap = std::max(cap.ecap, m->ecap);
+    cap.vcap = std::max(cap.vcap, m->vcap);
+    if ((rc = ensure_pools(m, 1, cap))) return rc;
+    std::vector<Brush> none;
+    if ((rc = upload(m, descs, none))) return rc;
+    BatchPtrs b = make_ptrs(m, 1);
+    if ((rc = enqueue_field_stages(m, b, false))) return rc;
+    if ((rc = read_states(m, 1))) return rc;
+    if (m->h_bs.as<BatchState>()->overflow) return LVN_ERR_DEVICE_STATUS;
+    f.last_op = 0;
+    return save_field(m, f);
+}
+
+// ApplyCSGOperations on a cached field (compute_csg.cpp:11-219)
+int apply_csg_to_field(lvn_meshgen* m, const int32_t min[3], int32_t size, FieldEntry& f,
+                       const std::vector<lvn_csg_op>& ops) {
+    if (ops.empty()) return LVN_OK;
+    std::vector<ChunkDesc> descs;
+    int rc = one_desc(m, min, size, descs);
+    if (rc) return rc;
+    std::vector<Brush> brushes;
+    for (const lvn_csg_op& op : ops) brushes.push_back(make_brush(op));
+    descs[0].op_begin = 0;
+    descs[0].op_count = (int32_t)brushes.size();
+    Capacity cap = default_capacity(m, 1);
+    cap.ecap = std::max<int64_t>(std::max(cap.ecap, m->ecap), (int64_t)f.num_edges + 3 * field_size(m->vpc));
+    cap.vcap = std::max(cap.vcap, m->vcap);
+    if ((rc = ensure_pools(m, 1, cap))) return rc;
+    if ((rc = upload(m, descs, brushes))) return rc;
+    const size_t F = (size_t)field_size(m->vpc);
+    LVN_CK(cudaMemcpyAsync(m->corners.p, f.corners.p, sizeof(uint16_t) * F, cudaMemcpyDeviceToDevice, m->stream));
+    BatchPtrs b = make_ptrs(m, 1);
+    b.plain_class = 0;
+    b.prev_keys = f.keys.as<int32_t>();
+    b.prev_info = f.info.as<float4>();
+    b.prev_count = f.num_edges;
+    LVN_CK(launch_reset(b, m->stream));
+    if ((rc = stage(m, ST_CSG, launch_csg, b))) return rc;
+    LVN_CK(launch_prune_edges(b, m->stream));
+    if ((rc = stage(m, ST_EDGE_COUNT, launch_edge_count, b))) return rc;
+    if ((rc = stage(m, ST_EDGE_PLAN, launch_edge_plan, b))) return rc;
+    if ((rc = stage(m, ST_EDGE_SCATTER, launch_edge_scatter, b))) return rc;
+    if ((rc = stage(m, ST_HERMITE, launch_hermite, b))) return rc;
+    if ((rc = read_states(m, 1))) return rc;
+    if (m->h_bs.as<BatchState>()->overflow) return LVN_ERR_DEVICE_STATUS;
+    return save_field(m, f);
+}
+
+// LoadDensityField (compute_density_field.cpp:235-274)
+int load_field(lvn_meshgen* m, const int32_t min[3], int32_t size, FieldEntry** out) {
+    const ChunkKey k = key_of(min, size);
+    auto it = m->fields.find(k);
+    FieldEntry* f;
+    if (it != m->fields.end()) {
+        f = &it->second;
+    } else {
+        FieldEntry fresh;
+        int rc = generate_field(m, min, size, fresh);
+        if (rc) {
+            fresh.corners.release();
+            fresh.keys.release();
+            fresh.info.release();
+            return rc;
+        }
+        f = &m->fields.emplace(k, std::move(fresh)).first->second;
+    }
+    const int32_t lo[3] = {min[0], min[1], min[2]};
+    const int32_t hi[3] = {min[0] + size, min[1] + size, min[2] + size};
+    std::vector<lvn_csg_op> replay;
+    for (size_t i = (size_t)std::max(0, f->last_op); i < g.ops.size(); i++)
+        if (overlaps(lo, hi, g.ops[i].lo, g.ops[i].hi)) replay.push_back(g.ops[i].op);
+    f->last_op = (int32_t)g.ops.size();
+    *out = f;
+    if (!replay.empty()) return apply_csg_to_field(m, min, size, *f, replay);
+    return LVN_OK;
+}
+
+// ConstructOctreeFromField + mesh + seams for one cached field
+int mesh_from_field(lvn_meshgen* m, const int32_t min[3], int32_t size, FieldEntry& f) {
+    std::vector<ChunkDesc> descs;
+    int rc = one_desc(m, min, size, descs);
+    if (rc) return rc;
+    std::vector<Brush> none;
+    Capacity cap = default_capacity(m, 1);
+    cap.ecap = std::max<int64_t>(std::max(cap.ecap, m->ecap), (int64_t)f.num_edges + 1024);
+    cap.vcap = std::max(cap.vcap, m->vcap);
+    for (int attempt = 0; attempt < kMaxHashRetries; attempt++) {
+        if ((rc = ensure_pools(m, 1, cap))) return rc;
+        if ((rc = upload(m, descs, none))) return rc;
+        const size_t F = (size_t)field_size(m->vpc);
+        LVN_CK(cudaMemcpyAsync(m->corners.p, f.corners.p, sizeof(uint16_t) * F, cudaMemcpyDeviceToDevice, m->stream));
+        LVN_CK(cudaMemcpyAsync(m->edge_keys.p, f.keys.p, sizeof(int32_t) * f.num_edges, cudaMemcpyDeviceToDevice,
+                               m->stream));
+        LVN_CK(cudaMemcpyAsync(m->edge_info.p, f.info.p, sizeof(float4) * f.num_edges, cudaMemcpyDeviceToDevice,
+                               m->stream));
+        LVN_CK(cudaMemsetAsync(m->edge_chunk.p, 0, sizeof(int32_t) * std::max(1, f.num_edges), m->stream));
+        ChunkState cs;
+        std::memset(&cs, 0, sizeof(cs));
+        cs.plain_edges = f.num_edges;
+        cs.num_edges = f.num_edges;
+        cs.edge_prime = 0;
+        if (f.num_edges > 0) {
+            // FindNextPrime (primes.cpp:32-58) on the host for the cached path
+            auto is_prime = [](int x) {
+                int o = 4, i = 5;
+                for (;;) {
+                    const int q = x / i;
+                    if (q < i) return true;
+                    if (x == q * i) return false;
+                    o ^= 6;
+                    i += o;
+                }
+            };
+            const int nn = std::max((int)CUCKOO_MIN_TABLE_SIZE, f.num_edges * 2);
+            int x;
+            if (nn <= 5) x = nn <= 2 ? 2 : nn == 3 ? 3 : 5;
+            else {
+                const int k = nn / 6;
+                int i = nn - 6 * k;
+                const int o = i < 2 ? 1 : 5;
+                x = 6 * k + o;
+                for (i = (3 + o) / 2; !is_prime(x); x += i) i ^= 6;
+            }
+            cs.edge_prime = (uint32_t)x;
+        }
+        BatchState bs;
+        std::memset(&bs, 0, sizeof(bs));
+        bs.total_edges = f.num_edges;
+        bs.total_edge_slots = cs.edge_prime ? cs.edge_prime + CUCKOO_STASH_SIZE : 0;
+        if (bs.total_edge_slots > m->eslot_cap) {
+            cap.ecap = std::max<int64_t>(cap.ecap, bs.total_edge_slots);
+            continue;
+        }
+        std::memcpy(m->h_cs.p, &cs, sizeof(cs));
+        std::memcpy(m->h_bs.p, &bs, sizeof(bs));
+        LVN_CK(cudaMemcpyAsync(m->cs.p, m->h_cs.p, sizeof(cs), cudaMemcpyHostToDevice, m->stream));
+        LVN_CK(cudaMemcpyAsync(m->bs.p, m->h_bs.p, sizeof(bs), cudaMemcpyHostToDevice, m->stream));
+        BatchPtrs b = make_ptrs(m, 1);
+        if ((rc = enqueue_octree_stages(m, b))) return rc;
+        if ((rc = read_states(m, 1))) return rc;
+        const BatchState& hb = *m->h_bs.as<BatchState>();
+        if (hb.overflow) {
+            cap.vcap = std::max<int64_t>(cap.vcap * 2, (int64_t)hb.total_nodes + 1024);
+            continue;
+        }
+        if (redraw_failed(m, descs)) continue;
+        return LVN_OK;
+    }
+    return LVN_ERR_HASH;
+}
+
+int export_chunk(lvn_meshgen* m, const OctreeEntry& o, lvn_mesh_out* out) {
+    out->num_vertices = o.num_vertices;
+    out->num_triangles = (int32_t)o.triangles.size();
+    out->num_seams = (int32_t)o.seams.size();
+    if (out->num_vertices > out->vertex_capacity || out->num_triangles > out->triangle_capacity ||
+        out->num_seams > out->seam_capacity)
+        return LVN_ERR_CAPACITY;
+    const cudaMemcpyKind kind = out->memory == LVN_MEMORY_DEVICE ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost;
+    if (out->num_vertices)
+        LVN_CK(cudaMemcpy(out->vertices, o.vertices.data(), sizeof(lvn_mesh_vertex) * out->num_vertices, kind));
+    if (out->num_triangles)
+        LVN_CK(cudaMemcpy(out->triangles, o.triangles.data(), sizeof(lvn_mesh_triangle) * out->num_triangles, kind));
+    if (out->num_seams) LVN_CK(cudaMemcpy(out->seams, o.seams.data(), sizeof(lvn_seam_node) * out->num_seams, kind));
+    return LVN_OK;
+}
+
+// Pull chunk 0's mesh out of the pools into host vectors.
+int pull_chunk(lvn_meshgen* m, OctreeEntry& o) {
+    const ChunkState& cs = m->last_cs[0];
+    o.num_vertices = cs.quads > 0 ? cs.nodes : 0;
+    o.vertices.resize(o.num_vertices);
+    o.triangles.resize(2 * (size_t)cs.quads);
+    o.seams.resize(cs.seams);
+    if (o.num_vertices)
+        LVN_CK(cudaMemcpyAsync(o.vertices.data(), m->vertices.as<lvn_mesh_vertex>() + cs.node_off,
+                               sizeof(lvn_mesh_vertex) * o.num_vertices, cudaMemcpyDeviceToHost, m->stream));
+    if (cs.quads)
+        LVN_CK(cudaMemcpyAsync(o.triangles.data(), m->triangles.as<lvn_mesh_triangle>() + 2 * (size_t)cs.quad_off,
+                               sizeof(lvn_mesh_triangle) * o.triangles.size(), cudaMemcpyDeviceToHost, m->stream));
+    if (cs.seams)
+        LVN_CK(cudaMemcpyAsync(o.seams.data(), m->seams.as<lvn_seam_node>() + cs.seam_off,
+                               sizeof(lvn_seam_node) * cs.seams, cudaMemcpyDeviceToHost, m->stream));
+    LVN_CK(cudaStreamSynchronize(m->stream));
+    return LVN_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+
+extern "C" {
+
+int lvn_initialise(int32_t noise_seed, uint32_t default_material, int32_t num_csg_brushes) {
+    (void)num_csg_brushes;  // the brush set is fixed: cube and sphere (apply_csg_operation.cl:76-78)
+    if (default_material > 255) return LVN_ERR_INVALID;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return LVN_ERR_NO_DEVICE;
+    LVN_CK(cudaGetDevice(&g.device));
+    LVN_CK(cudaDeviceGetAttribute(&g.num_sms, cudaDevAttrMultiProcessorCount, g.device));
+    g.default_material = (int32_t)default_material;
+    g.hash_gen = std::mt19937();
+    const int rc = upload_perm(noise_seed);
+    if (rc) return rc;
+    g.initialised = true;
+    return LVN_OK;
+}
+
+int lvn_shutdown(void) {
+    g.perm.release();
+    g.grad.release();
+    g.ops.clear();
+    g.initialised = false;
+    return LVN_OK;
+}
+
+int lvn_set_noise_seed(int32_t noise_seed) {
+    if (!g.initialised) return LVN_ERR_NOT_INITIALISED;
+    return upload_perm(noise_seed);
+}
+
+int lvn_store_csg_operation(const lvn_csg_op* op, const int32_t aabb_min[3], const int32_t aabb_max[3]) {
+    if (!op || !aabb_min || !aabb_max || !valid_op(*op)) return LVN_ERR_INVALID;
+    StoredOp s;
+    s.op = *op;
+    for (int i = 0; i < 3; i++) {
+        s.lo[i] = aabb_min[i];
+        s.hi[i] = aabb_max[i];
+    }
+    g.ops.push_back(s);
+    return LVN_OK;
+}
+
+int lvn_clear_csg_operations(void) {
+    g.ops.clear();
+    return LVN_OK;
+}
+
+int lvn_csg_operation_bounds(const lvn_csg_op* op, int32_t aabb_min[3], int32_t aabb_max[3]) {
+    if (!op || !aabb_min || !aabb_max) return LVN_ERR_INVALID;
+    op_bounds(*op, aabb_min, aabb_max);
+    return LVN_OK;
+}
+
+int lvn_set_density(const lvn_density_params* p) {
+    if (!p || p->mode < LVN_DENSITY_REFERENCE || p->mode > LVN_DENSITY_CAVES || p->octaves2 < 0 || p->octaves2 > 32 ||
+        p->octaves3 < 0 || p->octaves3 > 32)
+        return LVN_ERR_INVALID;
+    g.density = *p;
+    return LVN_OK;
+}
+
+const char* lvn_error_string(int32_t code) {
+    switch (code) {
+        case LVN_OK: return "LVN_OK";
+        case LVN_ERR_NO_DEVICE: return "LVN_ERR_NO_DEVICE";
+        case LVN_ERR_OUT_OF_MEMORY: return "LVN_ERR_OUT_OF_MEMORY";
+        case LVN_ERR_INVALID: return "LVN_ERR_INVALID";
+        case LVN_ERR_CAPACITY: return "LVN_ERR_CAPACITY";
+        case LVN_ERR_NOT_INITIALISED: return "LVN_ERR_NOT_INITIALISED";
+        case LVN_ERR_HASH: return "LVN_ERR_HASH";
+        case LVN_ERR_DEVICE_STATUS: return "LVN_ERR_DEVICE_STATUS";
+        case LVN_ERR_CUDA: return "LVN_ERR_CUDA";
+        default: return "unknown liblvn error code";
+    }
+}
+
+lvn_meshgen* lvn_meshgen_create(int32_t voxels_per_chunk) {
+    if (!g.initialised) return nullptr;
+    if (voxels_per_chunk != 8 && voxels_per_chunk != 16 && voxels_per_chunk != 32 && voxels_per_chunk != 64)
+        return nullptr;
+    lvn_meshgen* m = new lvn_meshgen();
+    m->vpc = voxels_per_chunk;
+    if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete m;
+        return nullptr;
+    }
+    m->own_stream = true;
+    for (int i = 0; i <= ST_COUNT; i++) cudaEventCreate(&m->ev[i]);
+    return m;
+}
+
+void lvn_meshgen_destroy(lvn_meshgen* m) {
+    if (!m) return;
+    cudaStreamSynchronize(m->stream);
+    DevBuf* bufs[] = {&m->desc,       &m->cs,         &m->bs,         &m->brushes,      &m->corners,
+                      &m->edge_tiles, &m->vox_tiles,  &m->edge_keys,  &m->edge_chunk,   &m->edge_info,
+                      &m->node_codes, &m->node_info,  &m->node_chunk, &m->edge_slots,   &m->node_slots,
+                      &m->quad_scratch, &m->node_tile_counts, &m->chunk_tile_off, &m->vertices, &m->triangles,
+                      &m->seams};
+    for (DevBuf* b : bufs) b->release();
+    m->h_desc.release();
+    m->h_brushes.release();
+    m->h_cs.release();
+    m->h_bs.release();
+    for (auto& kv : m->fields) {
+        kv.second.corners.release();
+        kv.second.keys.release();
+        kv.second.info.release();
+    }
+    for (int i = 0; i <= ST_COUNT; i++)
+        if (m->ev[i]) cudaEventDestroy(m->ev[i]);
+    if (m->own_stream) cudaStreamDestroy(m->stream);
+    delete m;
+}
+
+int lvn_meshgen_voxels_per_chunk(const lvn_meshgen* m) { return m ? m->vpc : 0; }
+
+int lvn_meshgen_set_stream(lvn_meshgen* m, void* stream) {
+    if (!m) return LVN_ERR_INVALID;
+    LVN_CK(cudaStreamSynchronize(m->stream));
+    if (m->own_stream) cudaStreamDestroy(m->stream);
+    m->stream = static_cast<cudaStream_t>(stream);
+    m->own_stream = false;
+    return LVN_OK;
+}
+
+void* lvn_meshgen_get_stream(lvn_meshgen* m) { return m ? (void*)m->stream : nullptr; }
+
+int lvn_meshgen_set_option(lvn_meshgen* m, int32_t option, int32_t value) {
+    if (!m) return LVN_ERR_INVALID;
+    switch (option) {
+        case LVN_OPT_CROSSING_MODE:
+            if (value != 0 && value != 1) return LVN_ERR_INVALID;
+            m->crossing_mode = value;
+            return LVN_OK;
+        case LVN_OPT_CACHE: m->cache = value != 0; return LVN_OK;
+        case LVN_OPT_PROFILE: m->profile = value != 0; return LVN_OK;
+        default: return LVN_ERR_INVALID;
+    }
+}
+
+int lvn_meshgen_stage_times(lvn_meshgen* m, float* ms, int32_t* launches, int32_t capacity) {
+    if (!m) return LVN_ERR_INVALID;
+    for (int i = 0; i < ST_COUNT && i < capacity; i++) {
+        if (ms) ms[i] = (float)m->stage_ms[i];
+        if (launches) launches[i] = m->stage_launches[i];
+    }
+    return ST_COUNT;
+}
+
+const char* lvn_meshgen_stage_name(int32_t s) { return stage_name(s); }
+
+int lvn_meshgen_reset_stage_times(lvn_meshgen* m) {
+    if (!m) return LVN_ERR_INVALID;
+    for (int i = 0; i < ST_COUNT; i++) {
+        m->stage_ms[i] = 0.0;
+        m->stage_launches[i] = 0;
+    }
+    return LVN_OK;
+}
+
+int lvn_meshgen_generate_chunks(lvn_meshgen* m, const lvn_chunk_desc* chunks, int32_t n, lvn_batch_out* out) {
+    if (!g.initialised) return LVN_ERR_NOT_INITIALISED;
+    if (!m || !out || n < 0 || (n > 0 && !chunks)) return LVN_ERR_INVALID;
+    if (n > 65535) return LVN_ERR_INVALID;
+    if (n == 0) {
+        out->total_vertices = out->total_triangles = out->total_seams = 0;
+        return LVN_OK;
+    }
+    std::vector<ChunkDesc> descs;
+    std::vector<Brush> brushes;
+    int rc = build_descs(m, chunks, n, descs, brushes, true);
+    if (rc) return rc;
+    const bool dev = out->memory == LVN_MEMORY_DEVICE;
+    rc = run_fresh_batch(m, descs, brushes, dev ? out : nullptr);
+    const BatchState& bs = *m->h_bs.as<BatchState>();
+    out->total_vertices = bs.total_nodes;
+    out->total_triangles = 2 * (int64_t)bs.total_quads;
+    out->total_seams = bs.total_seams;
+    if (rc) return rc;
+    if (out->chunks) fill_results(m, n, out->chunks);
+    if (!dev) {
+        if (out->total_vertices > out->vertex_capacity || out->total_triangles > out->triangle_capacity ||
+            out->total_seams > out->seam_capacity)
+            return LVN_ERR_CAPACITY;
+        if ((rc = copy_out(m, out->vertices, m->vertices.p, sizeof(lvn_mesh_vertex) * out->total_vertices, 0))) return rc;
+        if ((rc = copy_out(m, out->triangles, m->triangles.p, sizeof(lvn_mesh_triangle) * out->total_triangles, 0)))
+            return rc;
+        if ((rc = copy_out(m, out->seams, m->seams.p, sizeof(lvn_seam_node) * out->total_seams, 0))) return rc;
+        LVN_CK(cudaStreamSynchronize(m->stream));
+    }
+    return LVN_OK;
+}
+
+int lvn_meshgen_generate_chunk_mesh(lvn_meshgen* m, const int32_t min[3], int32_t size, lvn_mesh_out* out) {
+    if (!g.initialised) return LVN_ERR_NOT_INITIALISED;
+    if (!m || !min || !out) return LVN_ERR_INVALID;
+    if (size <= 0 || size % (m->vpc * LEAF_SIZE_SCALE) != 0) return LVN_ERR_INVALID;
+    if (!m->cache) {
+        // cold path: one fresh chunk with the stored operations replayed
+        lvn_chunk_desc cd;
+        for (int i = 0; i < 3; i++) cd.min[i] = min[i];
+        cd.size = size;
+        std::vector<ChunkDesc> descs;
+        std::vector<Brush> brushes;
+        int rc = build_descs(m, &cd, 1, descs, brushes, true);
+        if (rc) return rc;
+        if ((rc = run_fresh_batch(m, descs, brushes, nullptr))) return rc;
+        OctreeEntry o;
+        if ((rc = pull_chunk(m, o))) return rc;
+        return export_chunk(m, o, out);
+    }
+    // LoadOctree (compute_octree.cpp:154-181)
+    const ChunkKey k = key_of(min, size);
+    auto it = m->octrees.find(k);
+    if (it == m->octrees.end()) {
+        FieldEntry* f = nullptr;
+        int rc = load_field(m, min, size, &f);
+        if (rc) return rc;
+        f = &m->fields[k];
+        OctreeEntry o;
+        if (f->num_edges > 0) {
+            if ((rc = mesh_from_field(m, min, size, *f))) return rc;
+            if ((rc = pull_chunk(m, o))) return rc;
+        }
+        it = m->octrees.emplace(k, std::move(o)).first;
+    }
+    return export_chunk(m, it->second, out);
+}
+
+int lvn_meshgen_apply_csg_operations(lvn_meshgen* m, const lvn_csg_op* ops, int32_t num_ops, const int32_t min[3],
+                                     int32_t size) {
+    if (!g.initialised) return LVN_ERR_NOT_INITIALISED;
+    if (!m || !min || num_ops < 0 || (num_ops > 0 && !ops)) return LVN_ERR_INVALID;
+    if (size <= 0 || size % (m->vpc * LEAF_SIZE_SCALE) != 0) return LVN_ERR_INVALID;
+    for (int i = 0; i < num_ops; i++)
+        if (!valid_op(ops[i])) return LVN_ERR_INVALID;
+    FieldEntry* f = nullptr;
+    int rc = load_field(m, min, size, &f);
+    if (rc) return rc;
+    f = &m->fields[key_of(min, size)];
+    std::vector<lvn_csg_op> v(ops, ops + num_ops);
+    if ((rc = apply_csg_to_field(m, min, size, *f, v))) return rc;
+    f->last_op += num_ops;  // compute_csg.cpp:237
+    return LVN_OK;
+}
+
+int lvn_meshgen_free_chunk_octree(lvn_meshgen* m, const int32_t min[3], int32_t size) {
+    if (!m || !min) return LVN_ERR_INVALID;
+    m->octrees.erase(key_of(min, size));
+    return LVN_OK;
+}
+
+int lvn_meshgen_is_chunk_empty(lvn_meshgen* m, const int32_t min[3], int32_t size, int32_t* is_empty) {
+    if (!g.initialised) return LVN_ERR_NOT_INITIALISED;
+    if (!m || !min || !is_empty) return LVN_ERR_INVALID;
+    if (size <= 0 || size % (m->vpc * LEAF_SIZE_SCALE) != 0) return LVN_ERR_INVALID;
+    const ChunkKey k = key_of(min, size);
+    auto it = m->fields.find(k);
+    if (it == m->fields.end()) {
+        FieldEntry fresh;
+        const int rc = generate_field(m, min, size, fresh);
+        if (rc) return rc;
+        it = m->fields.emplace(k, std::move(fresh)).first;
+    }
+    *is_empty = it->second.num_edges == 0 ? 1 : 0;
+    return LVN_OK;
+}
+
+int64_t lvn_meshgen_debug_fetch(lvn_meshgen* m, int32_t what, int32_t chunk, void* host, int64_t cap) {
+    if (!m || chunk < 0 || chunk >= m->last_n) return LVN_ERR_INVALID;
+    const ChunkState& cs = m->last_cs[chunk];
+    const size_t F = (size_t)field_size(m->vpc);
+    const void* src = nullptr;
+    int64_t count = 0, elem = 0;
+    std::vector<uint8_t> mats;
+    switch (what) {
+        case LVN_DEBUG_MATERIALS: {
+            std::vector<uint16_t> cw(F);
+            if (cudaMemcpy(cw.data(), m->corners.as<uint16_t>() + F * chunk, F * 2, cudaMemcpyDeviceToHost) != cudaSuccess)
+                return LVN_ERR_CUDA;
+            if (cap < (int64_t)F) return LVN_ERR_CAPACITY;
+            for (size_t i = 0; i < F; i++) static_cast<uint8_t*>(host)[i] = (uint8_t)(cw[i] & 0xff);
+            return (int64_t)F;
+        }
+        case LVN_DEBUG_EDGE_KEYS: src = m->edge_keys.as<int32_t>() + cs.edge_off; count = cs.num_edges; elem = 4; break;
+        case LVN_DEBUG_EDGE_INFO: src = m->edge_info.as<float4>() + cs.edge_off; count = cs.num_edges; elem = 16; break;
+        case LVN_DEBUG_NODE_CODES: src = m->node_codes.as<uint32_t>() + cs.node_off; count = cs.nodes; elem = 4; break;
+        case LVN_DEBUG_NODE_INFO: src = m->node_info.as<int32_t>() + cs.node_off; count = cs.nodes; elem = 4; break;
+        case LVN_DEBUG_EDGE_TABLE:
+            src = m->edge_slots.as<unsigned long long>() + cs.edge_table_off; count = cs.edge_prime; elem = 8; break;
+        case LVN_DEBUG_EDGE_STASH:
+            src = m->edge_slots.as<unsigned long long>() + cs.edge_table_off + cs.edge_prime;
+            count = cs.edge_prime ? CUCKOO_STASH_SIZE : 0; elem = 8; break;
+        case LVN_DEBUG_NODE_TABLE:
+            src = m->node_slots.as<unsigned long long>() + cs.node_table_off; count = cs.node_prime; elem = 8; break;
+        case LVN_DEBUG_NODE_STASH:
+            src = m->node_slots.as<unsigned long long>() + cs.node_table_off + cs.node_prime;
+            count = cs.node_prime ? CUCKOO_STASH_SIZE : 0; elem = 8; break;
+        case LVN_DEBUG_PLAIN_EDGES: return cs.plain_edges;
+        default: return LVN_ERR_INVALID;
+    }
+    if (count * elem > cap) return LVN_ERR_CAPACITY;
+    if (count && cudaMemcpy(host, src, count * elem, cudaMemcpyDeviceToHost) != cudaSuccess) return LVN_ERR_CUDA;
+    return count;
+}
+
+}  // extern "C"

@@ -1,0 +1,1319 @@
+// lvn_kernels.cu -- the sm_103a kernels of the chunk-meshing pipeline.
+//
+// A batch of chunks flows through these stages (one launch each, all on one
+// stream, no host round trip):
+//
+//   field      density per corner of each 66^3 field (heightfield modes reuse
+//              the height term down each y column)      density_field.cl:11-37
+//   csg        stored brush operations applied to the corner materials
+//                                                       apply_csg_operation.cl:179-241
+//   edge_*     count / plan / scatter of active field edges in the reference's
+//              (hermite index, axis) order; plain edges touched by CSG are
+//              dropped and CSG-created edges appended     density_field.cl:41-92,
+//                                                       apply_csg_operation.cl:253-437
+//   hermite    17-sample zero crossing + central-difference normal per edge
+//                                                       density_field.cl:96-151,
+//                                                       apply_csg_operation.cl:443-477
+//   vox_*      count / plan / scatter of active voxels (leaf codes, edge
+//              masks, dominant material)                octree.cl:142-223
+//   hash_fill, edge_insert, node_insert
+//              cuckoo tables, one per chunk and key set   cuckoo.cl:26-71
+//   leaf       12 edge lookups, QEF accumulate + 10-sweep Jacobi solve,
+//              MeshVertex written in place              octree.cl:236-331,475-487
+//   mesh_*     quad emission with 3 node lookups per axis, seam nodes
+//                                                       octree.cl:385-464,506-551
+//
+// Compactions are tile based: a CTA owns a tile of a chunk's dense domain,
+// counts in one pass, and after a single-CTA plan kernel has scanned the tile
+// counts it scatters with warp-shuffle block scans, which keeps the
+// reference's linear-index order exactly.
+#include "lvn_kernels.cuh"
+#include "lvn_noise.cuh"
+
+#include <cfloat>
+
+namespace lvn {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int kThreads = 256;
+
+// ---------------------------------------------------------------------------
+// geometry
+// ---------------------------------------------------------------------------
+
+template <int VPC>
+struct Geo {
+    static constexpr int FD = VPC + 2;           // FIELD_DIM
+    static constexpr int HD = VPC + 1;           // HERMITE_INDEX_SIZE
+    static constexpr int F = FD * FD * FD;
+    static constexpr int C = VPC * VPC * VPC;
+    static constexpr int DEPTH = VPC == 8 ? 3 : VPC == 16 ? 4 : VPC == 32 ? 5 : 6;  // MAX_OCTREE_DEPTH
+    static constexpr int SHIFT = DEPTH + 1;      // VOXEL_INDEX_SHIFT
+    static constexpr int MASK = (1 << SHIFT) - 1;
+    static constexpr int NBE = (F + kTilePoints - 1) / kTilePoints;
+    static constexpr int NBV = (C + kTilePoints - 1) / kTilePoints;
+};
+
+// EDGE_MAP / EDGE_VERTEX_MAP (shared_constants.cl:4-9, octree.cl:227-232) as
+// nibble tables: {0,4},{1,5},{2,6},{3,7},{0,2},{1,3},{4,6},{5,7},{0,1},{2,3},{4,5},{6,7}
+__device__ __forceinline__ int edge_c0(int i) { return (int)((0x642054103210ull >> (4 * i)) & 0xfull); }
+__device__ __forceinline__ int edge_c1(int i) { return (int)((0x753176327654ull >> (4 * i)) & 0xfull); }
+
+template <int VPC>
+__device__ __forceinline__ uint32_t code_for_position(int x, int y, int z) {  // octree.cl:34-47
+    uint32_t code = 1;
+#pragma unroll
+    for (int depth = Geo<VPC>::DEPTH - 1; depth >= 0; depth--) {
+        const uint32_t c = (uint32_t)((((x >> depth) & 1) << 2) | (((y >> depth) & 1) << 1) | ((z >> depth) & 1));
+        code = (code << 3) | c;
+    }
+    return code;
+}
+
+template <int VPC>
+__device__ __forceinline__ void position_for_code(uint32_t code, int& x, int& y, int& z) {  // octree.cl:51-72
+    x = y = z = 0;
+#pragma unroll
+    for (int i = 0; i < Geo<VPC>::DEPTH; i++) {
+        const uint32_t c = code & 7u;
+        code >>= 3;
+        x |= (int)((c >> 2) & 1u) << i;
+        y |= (int)((c >> 1) & 1u) << i;
+        z |= (int)(c & 1u) << i;
+    }
+}
+
+template <int VPC>
+__device__ __forceinline__ int edge_key(int x, int y, int z, int axis) {
+    return ((x | (y << Geo<VPC>::SHIFT) | (z << (2 * Geo<VPC>::SHIFT))) << 2) | axis;
+}
+
+// ---------------------------------------------------------------------------
+// scans
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ int warp_inclusive(int v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int n = __shfl_up_sync(FULL, v, o);
+        if (lane >= o) v += n;
+    }
+    return v;
+}
+
+// Exclusive scan over the CTA; `sm` holds NT/32 + 1 ints.  Safe to call
+// back to back (ends with a barrier).
+template <int NT>
+__device__ __forceinline__ int block_exclusive(int v, int& total, int* sm) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int inc = warp_inclusive(v);
+    if (lane == 31) sm[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        const int w = lane < NT / 32 ? sm[lane] : 0;
+        const int wi = warp_inclusive(w);
+        if (lane < NT / 32) sm[lane] = wi - w;
+        if (lane == NT / 32 - 1) sm[NT / 32] = wi;
+    }
+    __syncthreads();
+    const int r = inc - v + sm[warp];
+    total = sm[NT / 32];
+    __syncthreads();
+    return r;
+}
+
+template <int NT>
+__device__ __forceinline__ int block_sum(int v, int* sm) {
+    int total;
+    block_exclusive<NT>(v, total, sm);
+    return total;
+}
+
+// Exclusive scan of `n` ints in place by one warp; returns the total.
+__device__ __forceinline__ int warp_scan_array(int* a, int n) {
+    const int lane = threadIdx.x & 31;
+    int carry = 0;
+    for (int base = 0; base < n; base += 32) {
+        const int i = base + lane;
+        const int v = i < n ? a[i] : 0;
+        const int inc = warp_inclusive(v);
+        if (i < n) a[i] = carry + inc - v;
+        carry += __shfl_sync(FULL, inc, 31);
+    }
+    return carry;
+}
+
+// Exclusive scan over n values held in global memory by one 1024-thread CTA.
+// val(i) supplies the value; out(i, excl) receives the result.  Returns the total.
+template <typename Val, typename Out>
+__device__ __forceinline__ long long cta_scan(int n, Val val, Out out, long long* sm_carry, int* sm) {
+    long long carry = 0;
+    for (int base = 0; base < n; base += 1024) {
+        const int i = base + threadIdx.x;
+        const int v = i < n ? val(i) : 0;
+        int total;
+        const int ex = block_exclusive<1024>(v, total, sm);
+        if (i < n) out(i, carry + ex);
+        carry += total;
+    }
+    (void)sm_carry;
+    return carry;
+}
+
+// ---------------------------------------------------------------------------
+// FindNextPrime (primes.cpp:9-58)
+// ---------------------------------------------------------------------------
+
+__device__ bool is_prime_d(int x) {
+    int o = 4, i = 5;
+    for (;;) {
+        const int q = x / i;
+        if (q < i) return true;
+        if (x == q * i) return false;
+        o ^= 6;
+        i += o;
+    }
+}
+
+__device__ int find_next_prime_d(int n) {
+    if (n <= 2) return 2;
+    if (n == 3) return 3;
+    if (n <= 5) return 5;
+    const int k = n / 6;
+    int i = n - 6 * k;
+    const int o = i < 2 ? 1 : 5;
+    int x = 6 * k + o;
+    for (i = (3 + o) / 2; !is_prime_d(x); x += i) i ^= 6;
+    return x;
+}
+
+// ---------------------------------------------------------------------------
+// cuckoo hash (cuckoo.cl:1-105)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t cuckoo_hash(uint32_t key, uint32_t a, uint32_t b, uint32_t mod) {
+    const unsigned long long h = (uint32_t)(a * key);  // 32-bit product (cuckoo.cl:21)
+    return (uint32_t)(((h + b) % 4294967291ull) % mod);
+}
+
+struct HashView {
+    const unsigned long long* table;
+    const unsigned long long* stash;
+    uint32_t prime;
+    int stash_used;
+    uint32_t p[10];
+
+    // Cuckoo_Find (cuckoo.cl:73-104); the stash probe reads the stash
+    __device__ __forceinline__ uint32_t find(uint32_t key) const {
+#pragma unroll
+        for (int i = 0; i < CUCKOO_STASH_HASH_INDEX; i++) {
+            const unsigned long long e = table[cuckoo_hash(key, p[2 * i], p[2 * i + 1], prime)];
+            if ((uint32_t)e == key) return (uint32_t)(e >> 32);
+        }
+        if (stash_used) {
+            const unsigned long long e = stash[cuckoo_hash(key, p[8], p[9], CUCKOO_STASH_SIZE)];
+            if ((uint32_t)e == key) return (uint32_t)(e >> 32);
+        }
+        return ~0u;
+    }
+};
+
+// Cuckoo_InsertKeys (cuckoo.cl:26-71) for one key.  Returns 0 on success,
+// 1 when the key went to the stash, -1 when the stash slot was taken.
+__device__ __forceinline__ int cuckoo_insert(unsigned long long* table, unsigned long long* stash, uint32_t prime,
+                                             const uint32_t* p, uint32_t key, uint32_t value) {
+    unsigned long long entry = ((unsigned long long)value << 32) | key;
+    uint32_t h = cuckoo_hash(key, p[0], p[1], prime);
+    for (int i = 0; i < CUCKOO_MAX_ITERATIONS; i++) {
+        entry = atomicExch(&table[h], entry);
+        if (entry == CUCKOO_EMPTY) return 0;
+        key = (uint32_t)entry;
+        const uint32_t h0 = cuckoo_hash(key, p[0], p[1], prime);
+        const uint32_t h1 = cuckoo_hash(key, p[2], p[3], prime);
+        const uint32_t h2 = cuckoo_hash(key, p[4], p[5], prime);
+        const uint32_t h3 = cuckoo_hash(key, p[6], p[7], prime);
+        if (h == h0) h = h1;
+        else if (h == h1) h = h2;
+        else if (h == h2) h = h3;
+        else if (h == h3) h = h0;
+    }
+    key = (uint32_t)entry;
+    const uint32_t hs = cuckoo_hash(key, p[8], p[9], CUCKOO_STASH_SIZE);
+    const unsigned long long prev = atomicCAS(&stash[hs], CUCKOO_EMPTY, entry);
+    return prev == CUCKOO_EMPTY ? 1 : -1;
+}
+
+// ---------------------------------------------------------------------------
+// QEF (qef.cl), identical operation order to the restatement
+// ---------------------------------------------------------------------------
+
+struct Qef {
+    float ata[6];
+    float atb[3];
+    float mp[4];
+};
+
+__device__ __forceinline__ float dot4(float ax, float ay, float az, float aw, float bx, float by, float bz, float bw) {
+    return fmaf(aw, bw, fmaf(az, bz, fmaf(ay, by, ax * bx)));
+}
+
+__device__ __forceinline__ void givens_coeffs_sym(float a_pp, float a_pq, float a_qq, float& c, float& s) {
+    if (a_pq == 0.f) { c = 1.f; s = 0.f; return; }
+    const float tau = (a_qq - a_pp) / (2.f * a_pq);
+    const float stt = sqrtf(fmaf(tau, tau, 1.f));
+    const float tn = 1.f / ((tau >= 0.f) ? (tau + stt) : (tau - stt));
+    c = 1.f / sqrtf(fmaf(tn, tn, 1.f));
+    s = tn * c;
+}
+
+__device__ __forceinline__ void rot_xy(float& x, float& y, float c, float s) {
+    const float u = x, v = y;
+    x = c * u - s * v;
+    y = s * u + c * v;
+}
+
+__device__ __forceinline__ void rotq_xy(float& x, float& y, float a, float c, float s) {
+    const float cc = c * c, ss = s * s;
+    const float mx = 2.f * c * s * a;
+    const float u = x, v = y;
+    x = cc * u - mx + ss * v;
+    y = ss * u + mx + cc * v;
+}
+
+// svd_rotate (qef.cl:58-86) on the upper triangle vtav and V
+template <int A, int B>
+__device__ __forceinline__ void svd_rotate(float (&vt)[3][3], float (&v)[3][3]) {
+    if (vt[A][B] == 0.f) return;
+    float c, s;
+    givens_coeffs_sym(vt[A][A], vt[A][B], vt[B][B], c, s);
+    float x = vt[A][A], y = vt[B][B];
+    rotq_xy(x, y, vt[A][B], c, s);
+    vt[A][A] = x;
+    vt[B][B] = y;
+    x = vt[0][3 - B];
+    y = vt[1 - A][2];
+    rot_xy(x, y, c, s);
+    vt[0][3 - B] = x;
+    vt[1 - A][2] = y;
+    vt[A][B] = 0.f;
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+        x = v[r][A];
+        y = v[r][B];
+        rot_xy(x, y, c, s);
+        v[r][A] = x;
+        v[r][B] = y;
+    }
+}
+
+__device__ __forceinline__ float svd_invdet(float x, float tol) {
+    return (fabsf(x) < tol || fabsf(1.f / x) < tol) ? 0.f : (1.f / x);
+}
+
+// qef_solve (qef.cl:239-256); returns the solved position (w = masspoint w)
+__device__ __forceinline__ void qef_solve(const Qef& q, float& ox, float& oy, float& oz) {
+    const float w = fmaxf(q.mp[3], 1.f);
+    const float mx = q.mp[0] / w, my = q.mp[1] / w, mz = q.mp[2] / w, mw = q.mp[3] / w;
+    const float* A = q.ata;
+    float ax = dot4(A[0], A[1], A[2], 0.f, mx, my, mz, mw);
+    float ay = A[1] * mx + A[3] * my + A[4] * mz;
+    float az = A[2] * mx + A[4] * my + A[5] * mz;
+    ax = q.atb[0] - ax;
+    ay = q.atb[1] - ay;
+    az = q.atb[2] - az;
+    const float aw = 0.f - 0.f;
+    float V[3][3] = {{1.f, 0.f, 0.f}, {0.f, 1.f, 0.f}, {0.f, 0.f, 1.f}};
+    float vt[3][3] = {{A[0], A[1], A[2]}, {0.f, A[3], A[4]}, {0.f, 0.f, A[5]}};
+#pragma unroll 1
+    for (int i = 0; i < 10; i++) {
+        svd_rotate<0, 1>(vt, V);
+        svd_rotate<0, 2>(vt, V);
+        svd_rotate<1, 2>(vt, V);
+    }
+    const float d0 = svd_invdet(vt[0][0], 0.1f);
+    const float d1 = svd_invdet(vt[1][1], 0.1f);
+    const float d2 = svd_invdet(vt[2][2], 0.1f);
+    float o[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) o[r][c] = V[r][0] * d0 * V[c][0] + V[r][1] * d1 * V[c][1] + V[r][2] * d2 * V[c][2];
+    float x = dot4(o[0][0], o[0][1], o[0][2], 0.f, ax, ay, az, aw);
+    float y = dot4(o[1][0], o[1][1], o[1][2], 0.f, ax, ay, az, aw);
+    float z = dot4(o[2][0], o[2][1], o[2][2], 0.f, ax, ay, az, aw);
+    ox = x + mx;
+    oy = y + my;
+    oz = z + mz;
+}
+
+// ---------------------------------------------------------------------------
+// stage 0: reset per-chunk state
+// ---------------------------------------------------------------------------
+
+__global__ void k_reset(BatchPtrs b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < b.n) {
+        ChunkState z;
+        memset(&z, 0, sizeof(z));
+        b.cs[i] = z;
+    }
+    if (i == 0) {
+        BatchState z;
+        memset(&z, 0, sizeof(z));
+        *b.bs = z;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// stage 1: density field (GenerateDefaultField, density_field.cl:11-37)
+// One thread per (x, z) column; heightfield modes evaluate the height term
+// once per column (the density is y - amp * h(x, z) [+ caves]).
+// ---------------------------------------------------------------------------
+
+template <int VPC>
+__global__ void __launch_bounds__(128) k_field(BatchPtrs b) {
+    using G = Geo<VPC>;
+    __shared__ float sg[64];
+    if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
+    __syncthreads();
+    const int c = blockIdx.y;
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= G::FD * G::FD) return;
+    const int x = col % G::FD, z = col / G::FD;
+    const ChunkDesc& d = b.desc[c];
+    const int scale = d.scale;
+    const Noise nz{b.perm, sg};
+    const float wx = (float)(x * scale + d.off[0]);
+    const float wz = (float)(z * scale + d.off[2]);
+    const float h = nz.height(b.density, wx, wz);
+    const int dm = b.default_material;
+    const uint16_t solid = (uint16_t)(dm | (dm != MATERIAL_AIR ? CORNER_PLAIN_SOLID : 0));
+    uint16_t* out = b.corners + (size_t)c * G::F + x + G::FD * G::FD * z;
+#pragma unroll 2
+    for (int y = 0; y < G::FD; y++) {
+        const float wy = (float)(y * scale + d.off[1]);
+        const float dv = nz.density_h(b.density, h, wx, wy, wz);
+        out[G::FD * y] = dv < 0.f ? solid : (uint16_t)MATERIAL_AIR;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// stage 2: CSG materials (CSG_HermiteIndices + UpdateFieldMaterials,
+// apply_csg_operation.cl:179-241); marks corners this batch changed.
+// ---------------------------------------------------------------------------
+
+template <int VPC>
+__global__ void __launch_bounds__(kThreads) k_csg(BatchPtrs b) {
+    using G = Geo<VPC>;
+    const int c = blockIdx.y;
+    const ChunkDesc& d = b.desc[c];
+    const int nops = d.op_count;
+    if (nops == 0) return;
+    const int L = blockIdx.x * blockDim.x + threadIdx.x;
+    if (L >= G::F) return;
+    const int x = L % G::FD, y = (L / G::FD) % G::FD, z = L / (G::FD * G::FD);
+    uint16_t* cw = b.corners + (size_t)c * G::F + L;
+    const uint16_t w = *cw;
+    const int m = w & 0xff;
+    const float wx = (float)(d.off[0] + d.scale * x);
+    const float wy = (float)(d.off[1] + d.scale * y);
+    const float wz = (float)(d.off[2] + d.scale * z);
+    int nm = m;
+    const Brush* ops = b.brushes + d.op_begin;
+    for (int i = 0; i < nops; i++) {
+        const Brush& br = ops[i];
+        if (brush_density(br, wx, wy, wz) <= 0.f) nm = br.type == 0 ? br.material : MATERIAL_AIR;
+    }
+    const uint16_t plain = w & CORNER_PLAIN_SOLID;
+    *cw = (uint16_t)(nm | plain | (nm != m ? CORNER_CHANGED : 0));
+}
+
+// ---------------------------------------------------------------------------
+// Cached-field CSG (compute_csg.cpp:140-175): the field's existing edges that
+// no changed corner touches are kept, in order, ahead of the created edges.
+// One CTA, chunk 0 of a one-chunk batch.
+// ---------------------------------------------------------------------------
+
+template <int VPC>
+__global__ void __launch_bounds__(1024) k_prune_edges(BatchPtrs b) {
+    using G = Geo<VPC>;
+    __shared__ int sm[1024 / 32 + 1];
+    const uint16_t* cw = b.corners;
+    const int n = b.prev_count;
+    int base = 0;
+    for (int r = 0; r < n; r += 1024) {
+        const int i = r + threadIdx.x;
+        int keep = 0;
+        int key = 0;
+        if (i < n) {
+            key = b.prev_keys[i];
+            const int a = key & 3, h = key >> 2;
+            const int x = h & G::MASK, y = (h >> G::SHIFT) & G::MASK, z = (h >> (2 * G::SHIFT)) & G::MASK;
+            const int L = x + G::FD * y + G::FD * G::FD * z;
+            const int coord = a == 0 ? x : a == 1 ? y : z;
+            const int stride = a == 0 ? 1 : a == 1 ? G::FD : G::FD * G::FD;
+            const bool touched = (L < G::F && (cw[L] & CORNER_CHANGED)) ||
+                                 (coord + 1 < G::FD && L + stride < G::F && (cw[L + stride] & CORNER_CHANGED));
+            keep = touched ? 0 : 1;
+        }
+        int total;
+        const int ex = block_exclusive<1024>(keep, total, sm);
+        if (keep && base + ex < b.ecap) {
+            b.edge_keys[base + ex] = key;
+            b.edge_info[base + ex] = b.prev_info[i];
+            b.edge_chunk[base + ex] = 0;
+        }
+        base += total;
+    }
+    if (threadIdx.x == 0) b.cs[0].kept_edges = base;
+}
+
+// ---------------------------------------------------------------------------
+// stage 3-5: field edges.  For field point q and axis a:
+//   plain-kept = q in the hermite grid, the plain field changes sign along a,
+//                and no CSG-changed corner touches the edge;
+//   created    = the edge is touched (FindUpdatedEdges) and the final
+//                materials change sign along it (FilterValidEdges, with the
+//                PARANOID linear-index guard).
+// Returns plain bits 0-2 and created bits 3-5.
+// ---------------------------------------------------------------------------
+
+template <int VPC>
+__device__ __forceinline__ int edge_flags(const uint16_t* __restrict__ cw, int L, bool plain_class) {
+    using G = Geo<VPC>;
+    const int x = L % G::FD, y = (L / G::FD) % G::FD, z = L / (G::FD * G::FD);
+    const uint16_t w0 = cw[L];
+    const bool herm = plain_class && x < G::HD && y < G::HD && z < G::HD;
+    const bool air0 = (w0 & 0xff) == MATERIAL_AIR;
+    int flags = 0;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const int stride = a == 0 ? 1 : a == 1 ? G::FD : G::FD * G::FD;
+        const int coord = a == 0 ? x : a == 1 ? y : z;
+        const int L1 = L + stride;
+        const bool inb = coord + 1 < G::FD;
+        const uint16_t w1 = L1 < G::F ? cw[L1] : (uint16_t)MATERIAL_AIR;
+        const bool touched = (w0 & CORNER_CHANGED) || (inb && (w1 & CORNER_CHANGED));
+        const bool plain_sc = herm && ((w0 ^ w1) & CORNER_PLAIN_SOLID);
+        const bool air1 = (w1 & 0xff) == MATERIAL_AIR;
+        if (plain_sc && !touched) flags |= 1 << a;
+        if (touched && air0 != air1) flags |= 8 << a;
+    }
+    return flags;
+}
+
+template <int VPC>
+__global__ void __launch_bounds__(kThreads) k_edge_count(BatchPtrs b) {
+    using G = Geo<VPC>;
+    __shared__ int sm[kThreads / 32 + 1];
+    const int c = blockIdx.y, tile = blockIdx.x;
+    const uint16_t* cw = b.corners + (size_t)c * G::F;
+    int packed = 0;
+#pragma unroll 2
+    for (int r = 0; r < kTilePoints / kThreads; r++) {
+        const int L = tile * kTilePoints + r * kThreads + threadIdx.x;
+        if (L < G::F) {
+            const int f = edge_flags<VPC>(cw, L, b.plain_class != 0);
+            packed += __popc(f & 7) | (__popc(f >> 3) << 16);
+        }
+    }
+    const int total = block_sum<kThreads>(packed, sm);
+    if (threadIdx.x == 0) b.edge_tiles[(size_t)c * G::NBE + tile] = make_int2(total & 0xffff, total >> 16);
+}
+
+// Single CTA: per-chunk tile offsets, per-chunk edge offsets, edge-table plan.
+template <int VPC>
+__global__ void __launch_bounds__(1024) k_edge_plan(BatchPtrs b) {
+    using G = Geo<VPC>;
+    __shared__ int sm[1024 / 32 + 1];
+    __shared__ long long carry;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // per-chunk: exclusive scan of the chunk's tile counts (both classes)
+    for (int c = warp; c < b.n; c += 32) {
+        int2* t = b.edge_tiles + (size_t)c * G::NBE;
+        int cp = 0, cc = 0;
+        for (int base = 0; base < G::NBE; base += 32) {
+            const int i = base + lane;
+            const int2 v = i < G::NBE ? t[i] : make_int2(0, 0);
+            const int ip = warp_inclusive(v.x), ic = warp_inclusive(v.y);
+            if (i < G::NBE) t[i] = make_int2(cp + ip - v.x, cc + ic - v.y);
+            cp += __shfl_sync(FULL, ip, 31);
+            cc += __shfl_sync(FULL, ic, 31);
+        }
+        if (lane == 0) {
+            // edges kept from a cached field precede the plain class
+            cp += b.cs[c].kept_edges;
+            b.cs[c].plain_edges = cp;
+            b.cs[c].created_edges = cc;
+            b.cs[c].num_edges = cp + cc;
+            // Cuckoo_InitialiseTable (compute_cuckoo.cpp:53)
+            const int e = cp + cc;
+            b.cs[c].edge_prime = e > 0 ? (uint32_t)find_next_prime_d(max((int)CUCKOO_MIN_TABLE_SIZE, e * 2)) : 0u;
+        }
+    }
+    __syncthreads();
+    (void)carry;
+    const long long total = cta_scan(
+        b.n, [&](int c) { return b.cs[c].num_edges; }, [&](int c, long long ex) { b.cs[c].edge_off = (int)ex; },
+        nullptr, sm);
+    const long long slots = cta_scan(
+        b.n, [&](int c) { return b.cs[c].edge_prime ? (int)b.cs[c].edge_prime + CUCKOO_STASH_SIZE : 0; },
+        [&](int c, long long ex) { b.cs[c].edge_table_off = (int)ex; }, nullptr, sm);
+    if (threadIdx.x == 0) {
+        b.bs->total_edges = (int)total;
+        b.bs->total_edge_slots = slots;
+        int ovf = 0;
+        if (total > b.ecap) ovf |= OVF_EDGES;
+        if (slots > b.edge_slot_cap) ovf |= OVF_EDGE_SLOTS;
+        b.bs->overflow |= ovf;
+    }
+}
+
+template <int VPC>
+__global__ void __launch_bounds__(kThreads) k_edge_scatter(BatchPtrs b) {
+    using G = Geo<VPC>;
+    __shared__ int sm[kThreads / 32 + 1];
+    if (b.bs->overflow) return;
+    const int c = blockIdx.y, tile = blockIdx.x;
+    const uint16_t* cw = b.corners + (size_t)c * G::F;
+    const ChunkState st = b.cs[c];
+    const int2 toff = b.edge_tiles[(size_t)c * G::NBE + tile];
+    int base_p = st.edge_off + st.kept_edges + toff.x;
+    int base_c = st.edge_off + st.plain_edges + toff.y;
+    for (int r = 0; r < kTilePoints / kThreads; r++) {
+        const int L = tile * kTilePoints + r * kThreads + threadIdx.x;
+        const int f = L < G::F ? edge_flags<VPC>(cw, L, b.plain_class != 0) : 0;
+        const int packed = __popc(f & 7) | (__popc(f >> 3) << 16);
+        int total;
+        const int ex = block_exclusive<kThreads>(packed, total, sm);
+        if (f) {
+            const int x = L % G::FD, y = (L / G::FD) % G::FD, z = L / (G::FD * G::FD);
+            int pp = base_p + (ex & 0xffff);
+            int pc = base_c + (ex >> 16);
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                if (f & (1 << a)) {
+                    b.edge_keys[pp] = edge_key<VPC>(x, y, z, a);
+                    b.edge_chunk[pp] = c;
+                    pp++;
+                }
+            }
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                if (f & (8 << a)) {
+                    b.edge_keys[pc] = edge_key<VPC>(x, y, z, a);
+                    b.edge_chunk[pc] = c;
+                    pc++;
+                }
+            }
+        }
+        base_p += total & 0xffff;
+        base_c += total >> 16;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// stage 6: hermite data per edge
+// ---------------------------------------------------------------------------
+
+template <int VPC>
+__device__ __forceinline__ float4 hermite_density(const BatchPtrs& b, const Noise& nz, const ChunkDesc& d, int key) {
+    using G = Geo<VPC>;
+    const int axis = key & 3;
+    const int hidx = key >> 2;
+    const int lx = hidx & G::MASK, ly = (hidx >> G::SHIFT) & G::MASK, lz = (hidx >> (2 * G::SHIFT)) & G::MASK;
+    const int s = d.scale;
+    const int wx = s * lx + d.off[0], wy = s * ly + d.off[1], wz = s * lz + d.off[2];
+    const float p0x = (float)wx, p0y = (float)wy, p0z = (float)wz;
+    const float p1x = (float)(wx + (axis == 0 ? s : 0));
+    const float p1y = (float)(wy + (axis == 1 ? s : 0));
+    const float p1z = (float)(wz + (axis == 2 ? s : 0));
+    const DensityParams& dp = b.density;
+    float t = 0.f;
+    float hbest;
+    if (b.crossing_mode == 0) {
+        // 17-sample search for min |d| (density_field.cl:122-136); first minimum wins
+        float minv = FLT_MAX;
+        float cur = 0.f;
+        if (axis == 1) {
+            const float h = nz.height(dp, p0x, p0z);  // x and z are fixed along a y edge
+            hbest = h;
+            for (int i = 0; i <= 16; i++) {
+                const float py = fmaf(p1y - p0y, cur, p0y);
+                const float dv = fabsf(nz.density_h(dp, h, p0x, py, p0z));
+                if (dv < minv) { t = cur; minv = dv; }
+                cur += 0.0625f;
+            }
+        } else {
+            hbest = 0.f;
+            for (int i = 0; i <= 16; i++) {
+                const float px = fmaf(p1x - p0x, cur, p0x);
+                const float pz = fmaf(p1z - p0z, cur, p0z);
+                const float h = nz.height(dp, px, pz);
+                const float dv = fabsf(nz.density_h(dp, h, px, p0y, pz));
+                if (dv < minv) { t = cur; minv = dv; hbest = h; }
+                cur += 0.0625f;
+            }
+        }
+    } else {
+        const float d0 = nz.density(dp, p0x, p0y, p0z);
+        const float d1 = nz.density(dp, p1x, p1y, p1z);
+        const float den = d0 - d1;
+        t = den != 0.f ? d0 / den : 0.5f;
+        t = fminf(fmaxf(t, 0.f), 1.f);
+        hbest = nz.height(dp, fmaf(p1x - p0x, t, p0x), fmaf(p1z - p0z, t, p0z));
+    }
+    const float px = fmaf(p1x - p0x, t, p0x);
+    const float py = fmaf(p1y - p0y, t, p0y);
+    const float pz = fmaf(p1z - p0z, t, p0z);
+    const float h = 0.001f;
+    float nx = nz.density(dp, px + h, py, pz) - nz.density(dp, px - h, py, pz);
+    float ny = nz.density_h(dp, hbest, px, py + h, pz) - nz.density_h(dp, hbest, px, py - h, pz);
+    float nzv = nz.density(dp, px, py, pz + h) - nz.density(dp, px, py, pz - h);
+    normalize3(nx, ny, nzv);
+    return make_float4(nx, ny, nzv, t);
+}
+
+// CSG FindEdgeIntersectionInfo (apply_csg_operation.cl:443-477)
+template <int VPC>
+__device__ __forceinline__ float4 hermite_brush(const BatchPtrs& b, const ChunkDesc& d, int key) {
+    using G = Geo<VPC>;
+    const int axis = key & 3;
+    const int hidx = key >> 2;
+    const int lx = hidx & G::MASK, ly = (hidx >> G::SHIFT) & G::MASK, lz = (hidx >> (2 * G::SHIFT)) & G::MASK;
+    const int s = d.scale;
+    const int wx = s * lx + d.off[0], wy = s * ly + d.off[1], wz = s * lz + d.off[2];
+    const float p0x = (float)wx, p0y = (float)wy, p0z = (float)wz;
+    const float p1x = (float)(wx + (axis == 0 ? s : 0));
+    const float p1y = (float)(wy + (axis == 1 ? s : 0));
+    const float p1z = (float)(wz + (axis == 2 ? s : 0));
+    const Brush* ops = b.brushes + d.op_begin;
+    const int nops = d.op_count;
+    // BrushZeroCrossing (apply_csg_operation.cl:86-110)
+    float mind = FLT_MAX, t = 0.f;
+    for (float tt = 0.f; tt <= 1.f; tt += (1.f / 16.f)) {
+        const float px = fmaf(p1x - p0x, tt, p0x);
+        const float py = fmaf(p1y - p0y, tt, p0y);
+        const float pz = fmaf(p1z - p0z, tt, p0z);
+        for (int i = 0; i < nops; i++) {
+            const float dv = fabsf(brush_density(ops[i], px, py, pz));
+            if (dv < mind) { t = tt; mind = dv; }
+        }
+    }
+    const float px = fmaf(p1x - p0x, t, p0x);
+    const float py = fmaf(p1y - p0y, t, p0y);
+    const float pz = fmaf(p1z - p0z, t, p0z);
+    // BrushNormal (apply_csg_operation.cl:144-175): the last containing op wins
+    float nx = 0.f, ny = 0.f, nzv = 0.f;
+    const float h = 0.001f;
+    for (int i = 0; i < nops; i++) {
+        const Brush& br = ops[i];
+        if (brush_density(br, px, py, pz) > 0.f) continue;
+        float gx = brush_density(br, px + h, py, pz) - brush_density(br, px - h, py, pz);
+        float gy = brush_density(br, px, py + h, pz) - brush_density(br, px, py - h, pz);
+        float gz = brush_density(br, px, py, pz + h) - brush_density(br, px, py, pz - h);
+        normalize3(gx, gy, gz);
+        const float flip = br.type == 0 ? 1.f : -1.f;
+        nx = flip * gx;
+        ny = flip * gy;
+        nzv = flip * gz;
+    }
+    return make_float4(nx, ny, nzv, t);
+}
+
+template <int VPC>
+__global__ void __launch_bounds__(kThreads) k_hermite(BatchPtrs b) {
+    __shared__ float sg[64];
+    if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
+    __syncthreads();
+    if (b.bs->overflow) return;
+    const Noise nz{b.perm, sg};
+    const int total = b.bs->total_edges;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int c = b.edge_chunk[i];
+        const ChunkDesc& d = b.desc[c];
+        const int key = b.edge_keys[i];
+        const ChunkState& st = b.cs[c];
+        const bool created = (i - st.edge_off) >= st.plain_edges;
+        if (created) b.edge_info[i] = hermite_brush<VPC>(b, d, key);
+        else if ((i - st.edge_off) >= st.kept_edges) b.edge_info[i] = hermite_density<VPC>(b, nz, d, key);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// stage 7-9: active voxels (FindActiveVoxels + CompactVoxels, octree.cl:142-223)
+// ---------------------------------------------------------------------------
+
+// FindDominantMaterial (octree.cl:96-138)
+__device__ __forceinline__ int dominant_material(int (&m)[8]) {
+#pragma unroll
+    for (int i = 1; i < 8; i++) {
+        const int tmp = m[i];
+        int j = i;
+        for (; j >= 1 && tmp < m[j - 1]; j--) m[j] = m[j - 1];
+        m[j] = tmp;
+    }
+    int current = m[0], count = 1, max_count = 0, max_material = 0;
+#pragma unroll
+    for (int i = 1; i < 8; i++) {
+        const int v = m[i];
+        if (v == MATERIAL_AIR || v == MATERIAL_NONE) continue;
+        if (current != v) {
+            if (count > max_count) { max_count = count; max_material = current; }
+            current = v;
+            count = 1;
+        } else {
+            count++;
+        }
+    }
+    if (count > max_count) max_material = current;
+    return max_material;
+}
+
+// corner mask of voxel (x, y, z); bit i = corner CHILD_MIN_OFFSETS[i] is not air
+template <int VPC>
+__device__ __forceinline__ int voxel_corners(const uint16_t* __restrict__ cw, int x, int y, int z, int (&mats)[8]) {
+    using G = Geo<VPC>;
+    int corners = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int cx = x + (i >> 2), cy = y + ((i >> 1) & 1), cz = z + (i & 1);
+        const int m = cw[cx + G::FD * cy + G::FD * G::FD * cz] & 0xff;
+        mats[i] = m;
+        corners |= (m == MATERIAL_AIR ? 0 : 1) << i;
+    }
+    return corners;
+}
+
+template <int VPC>
+__global__ void __launch_bounds__(kThreads) k_vox_count(BatchPtrs b) {
+    using G = Geo<VPC>;
+    __shared__ int sm[kThreads / 32 + 1];
+    const int c = blockIdx.y, tile = blockIdx.x;
+    const uint16_t* cw = b.corners + (size_t)c * G::F;
+    int cnt = 0;
+    for (int r = 0; r < kTilePoints / kThreads; r++) {
+        const int v = tile * kTilePoints + r * kThreads + threadIdx.x;
+        if (v < G::C) {
+            const int x = v % VPC, y = (v / VPC) % VPC, z = v / (VPC * VPC);
+            int mats[8];
+            const int corners = voxel_corners<VPC>(cw, x, y, z, mats);
+            cnt += (corners != 0 && corners != 255) ? 1 : 0;
+        }
+    }
+    const int total = block_sum<kThreads>(cnt, sm);
+    if (threadIdx.x == 0) b.vox_tiles[(size_t)c * G::NBV + tile] = total;
+}
+
+template <int VPC>
+__global__ void __launch_bounds__(1024) k_vox_plan(BatchPtrs b) {
+    using G = Geo<VPC>;
+    __shared__ int sm[1024 / 32 + 1];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int c = warp; c < b.n; c += 32) {
+        // a chunk without field edges builds no octree (compute_octree.cpp:167-171)
+        int v = warp_scan_array(b.vox_tiles + (size_t)c * G::NBV, G::NBV);
+        if (b.cs[c].num_edges == 0) v = 0;
+        if (lane == 0) {
+            b.cs[c].nodes = v;
+            b.cs[c].node_prime = v > 0 ? (uint32_t)find_next_prime_d(max((int)CUCKOO_MIN_TABLE_SIZE, v * 2)) : 0u;
+        }
+    }
+    __syncthreads();
+    const long long total = cta_scan(
+        b.n, [&](int c) { return b.cs[c].nodes; }, [&](int c, long long ex) { b.cs[c].node_off = (int)ex; }, nullptr, sm);
+    const long long slots = cta_scan(
+        b.n, [&](int c) { return b.cs[c].node_prime ? (int)b.cs[c].node_prime + CUCKOO_STASH_SIZE : 0; },
+        [&](int c, long long ex) { b.cs[c].node_table_off = (int)ex; }, nullptr, sm);
+    const long long tiles = cta_scan(
+        b.n, [&](int c) { return (b.cs[c].nodes + kNodeTile - 1) / kNodeTile; },
+        [&](int c, long long ex) { b.chunk_tile_off[c] = (int)ex; }, nullptr, sm);
+    if (threadIdx.x == 0) {
+        b.chunk_tile_off[b.n] = (int)tiles;
+        b.bs->total_nodes = (int)total;
+        b.bs->total_node_slots = slots;
+        int ovf = 0;
+        if (total > b.vcap || total > b.vertex_cap) ovf |= OVF_NODES;
+        if (slots > b.node_slot_cap) ovf |= OVF_NODE_SLOTS;
+        if (tiles > b.node_tile_cap) ovf |= OVF_NODES;
+        b.bs->overflow |= ovf;
+    }
+}
+
+template <int VPC>
+__global__ void __launch_bounds__(kThreads) k_vox_scatter(BatchPtrs b) {
+    using G = Geo<VPC>;
+    __shared__ int sm[kThreads / 32 + 1];
+    if (b.bs->overflow) return;
+    const int c = blockIdx.y, tile = blockIdx.x;
+    const ChunkState st = b.cs[c];
+    if (st.nodes == 0) return;
+    const uint16_t* cw = b.corners + (size_t)c * G::F;
+    int base = st.node_off + b.vox_tiles[(size_t)c * G::NBV + tile];
+    for (int r = 0; r < kTilePoints / kThreads; r++) {
+        const int v = tile * kTilePoints + r * kThreads + threadIdx.x;
+        int corners = 0, x = 0, y = 0, z = 0;
+        int mats[8];
+        bool active = false;
+        if (v < G::C) {
+            x = v % VPC;
+            y = (v / VPC) % VPC;
+            z = v / (VPC * VPC);
+            corners = voxel_corners<VPC>(cw, x, y, z, mats);
+            active = corners != 0 && corners != 255;
+        }
+        int total;
+        const int ex = block_exclusive<kThreads>(active ? 1 : 0, total, sm);
+        if (active) {
+            int edges = 0;
+#pragma unroll
+            for (int i = 0; i < 12; i++) {
+                const int s0 = (corners >> edge_c0(i)) & 1, s1 = (corners >> edge_c1(i)) & 1;
+                edges |= (s0 != s1 ? 1 : 0) << i;
+            }
+            const int dom = dominant_material(mats);
+            const int pos = base + ex;
+            b.node_codes[pos] = code_for_position<VPC>(x, y, z);
+            b.node_info[pos] = (edges << 16) | (dom << 8) | corners;
+            b.node_chunk[pos] = c;
+        }
+        base += total;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// stage 10-13: cuckoo tables, leaves
+// ---------------------------------------------------------------------------
+
+__global__ void k_hash_fill(BatchPtrs b) {
+    if (b.bs->overflow) return;
+    const long long ne = b.bs->total_edge_slots, nn = b.bs->total_node_slots;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < ne + nn; i += stride) {
+        if (i < ne) b.edge_slots[i] = CUCKOO_EMPTY;
+        else b.node_slots[i - ne] = CUCKOO_EMPTY;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_edge_insert(BatchPtrs b) {
+    if (b.bs->overflow) return;
+    const int total = b.bs->total_edges;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int c = b.edge_chunk[i];
+        ChunkState* st = b.cs + c;
+        const uint32_t prime = st->edge_prime;
+        unsigned long long* table = b.edge_slots + st->edge_table_off;
+        uint32_t p[10];
+#pragma unroll
+        for (int k = 0; k < 10; k++) p[k] = b.desc[c].edge_params[k];
+        const int r = cuckoo_insert(table, table + prime, prime, p, (uint32_t)b.edge_keys[i], (uint32_t)(i - st->edge_off));
+        if (r == 1) st->edge_stash_used = 1;
+        if (r < 0) st->edge_insert_failed = 1;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_node_insert(BatchPtrs b) {
+    if (b.bs->overflow) return;
+    const int total = b.bs->total_nodes;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int c = b.node_chunk[i];
+        ChunkState* st = b.cs + c;
+        const uint32_t prime = st->node_prime;
+        unsigned long long* table = b.node_slots + st->node_table_off;
+        uint32_t p[10];
+#pragma unroll
+        for (int k = 0; k < 10; k++) p[k] = b.desc[c].node_params[k];
+        const int r = cuckoo_insert(table, table + prime, prime, p, b.node_codes[i], (uint32_t)(i - st->node_off));
+        if (r == 1) st->node_stash_used = 1;
+        if (r < 0) st->node_insert_failed = 1;
+    }
+}
+
+// CreateLeafNodes + SolveQEFs + GenerateMeshVertexBuffer (octree.cl:236-331, 475-487)
+template <int VPC>
+__global__ void __launch_bounds__(kThreads) k_leaf(BatchPtrs b) {
+    if (b.bs->overflow) return;
+    const int total = b.bs->total_nodes;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int c = b.node_chunk[i];
+        const ChunkState& st = b.cs[c];
+        const ChunkDesc& d = b.desc[c];
+        HashView hv;
+        hv.prime = st.edge_prime;
+        hv.table = b.edge_slots + st.edge_table_off;
+        hv.stash = hv.table + hv.prime;
+        hv.stash_used = st.edge_stash_used;
+#pragma unroll
+        for (int k = 0; k < 10; k++) hv.p[k] = d.edge_params[k];
+        const float4* info = b.edge_info + st.edge_off;
+        int x, y, z;
+        position_for_code<VPC>(b.node_codes[i], x, y, z);
+        const int ni = b.node_info[i];
+        const int edge_list = ni >> 16;
+        const float fs = (float)d.scale;
+        Qef q;
+#pragma unroll
+        for (int k = 0; k < 6; k++) q.ata[k] = 0.f;
+        q.atb[0] = q.atb[1] = q.atb[2] = 0.f;
+        q.mp[0] = q.mp[1] = q.mp[2] = q.mp[3] = 0.f;
+        float sx = 0.f, sy = 0.f, sz = 0.f, sw = 0.f;
+        for (int e = 0; e < 12; e++) {
+            if (!((edge_list >> e) & 1)) continue;
+            const int e0 = edge_c0(e), e1 = edge_c1(e);
+            const int o0x = e0 >> 2, o0y = (e0 >> 1) & 1, o0z = e0 & 1;
+            const int o1x = e1 >> 2, o1y = (e1 >> 1) & 1, o1z = e1 & 1;
+            const int axis = e / 4;
+            const uint32_t di = hv.find((uint32_t)edge_key<VPC>(x + o0x, y + o0y, z + o0z, axis));
+            if (di == ~0u) continue;
+            const float4 ed = info[di];
+            const float p0x = (float)x + (float)o0x, p0y = (float)y + (float)o0y, p0z = (float)z + (float)o0z;
+            const float p1x = (float)x + (float)o1x, p1y = (float)y + (float)o1y, p1z = (float)z + (float)o1z;
+            const float px = fs * fmaf(p1x - p0x, ed.w, p0x);
+            const float py = fs * fmaf(p1y - p0y, ed.w, p0y);
+            const float pz = fs * fmaf(p1z - p0z, ed.w, p0z);
+            const float pw = fs * fmaf(0.f - 0.f, ed.w, 0.f);
+            // qef_add_point (qef.cl:170-191)
+            const float nx = ed.x, ny = ed.y, nzv = ed.z;
+            q.ata[0] += nx * nx;
+            q.ata[1] += nx * ny;
+            q.ata[2] += nx * nzv;
+            q.ata[3] += ny * ny;
+            q.ata[4] += ny * nzv;
+            q.ata[5] += nzv * nzv;
+            const float bb = dot4(px, py, pz, pw, nx, ny, nzv, 0.f);
+            q.atb[0] += nx * bb;
+            q.atb[1] += ny * bb;
+            q.atb[2] += nzv * bb;
+            q.mp[0] += px;
+            q.mp[1] += py;
+            q.mp[2] += pz;
+            q.mp[3] += 1.f;
+            sx += nx;
+            sy += ny;
+            sz += nzv;
+            sw += 1.f;
+        }
+        // qef_create_from_points divides the mass point by its count (qef.cl:302)
+        const float mw = q.mp[3];
+        q.mp[0] = q.mp[0] / mw;
+        q.mp[1] = q.mp[1] / mw;
+        q.mp[2] = q.mp[2] / mw;
+        q.mp[3] = q.mp[3] / mw;
+        float ox, oy, oz;
+        qef_solve(q, ox, oy, oz);
+        lvn_mesh_vertex vtx;
+        vtx.position[0] = fmaf(ox, (float)LEAF_SIZE_SCALE, (float)d.min[0]);
+        vtx.position[1] = fmaf(oy, (float)LEAF_SIZE_SCALE, (float)d.min[1]);
+        vtx.position[2] = fmaf(oz, (float)LEAF_SIZE_SCALE, (float)d.min[2]);
+        vtx.position[3] = 1.f;
+        vtx.normal[0] = sx / sw;
+        vtx.normal[1] = sy / sw;
+        vtx.normal[2] = sz / sw;
+        vtx.normal[3] = 0.f;
+        vtx.colour[0] = d.colour[0];
+        vtx.colour[1] = d.colour[1];
+        vtx.colour[2] = d.colour[2];
+        vtx.colour[3] = (float)((ni & 0xffff) >> 8);
+        float4* dst = reinterpret_cast<float4*>(b.vertices + i);
+        dst[0] = make_float4(vtx.position[0], vtx.position[1], vtx.position[2], vtx.position[3]);
+        dst[1] = make_float4(vtx.normal[0], vtx.normal[1], vtx.normal[2], vtx.normal[3]);
+        dst[2] = make_float4(vtx.colour[0], vtx.colour[1], vtx.colour[2], vtx.colour[3]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// stage 14-16: quads and seams (GenerateMesh, CompactMeshTriangles,
+// FindSeamNodes, ExtractSeamNodeInfo: octree.cl:385-464, 506-551)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ int chunk_of_tile(const int* off, int n, int vt) {
+    int lo = 0, hi = n;  // largest c in [0, n) with off[c] <= vt
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (off[mid] <= vt) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <int VPC>
+__global__ void __launch_bounds__(kNodeTile) k_mesh_count(BatchPtrs b) {
+    __shared__ int sm[kNodeTile / 32 + 1];
+    if (b.bs->overflow) return;
+    const int ntiles = b.chunk_tile_off[b.n];
+    for (int vt = blockIdx.x; vt < ntiles; vt += gridDim.x) {
+        const int c = chunk_of_tile(b.chunk_tile_off, b.n, vt);
+        const ChunkState& st = b.cs[c];
+        const int local = (vt - b.chunk_tile_off[c]) * kNodeTile + threadIdx.x;
+        int packed = 0;
+        if (local < st.nodes) {
+            const int i = st.node_off + local;
+            HashView hv;
+            hv.prime = st.node_prime;
+            hv.table = b.node_slots + st.node_table_off;
+            hv.stash = hv.table + hv.prime;
+            hv.stash_used = st.node_stash_used;
+#pragma unroll
+            for (int k = 0; k < 10; k++) hv.p[k] = b.desc[c].node_params[k];
+            int pos[3];
+            position_for_code<VPC>(b.node_codes[i], pos[0], pos[1], pos[2]);
+            const int corners = b.node_info[i] & 0xff;
+            int quads = 0;
+#pragma unroll
+            for (int axis = 0; axis < 3; axis++) {
+                int4 q = make_int4(-1, -1, -1, 0);
+                const int aa = pos[(axis + 1) % 3], bb = pos[(axis + 2) % 3];
+                if (aa != VPC - 1 && bb != VPC - 1) {
+                    // EDGE_NODE_OFFSETS (octree.cl:376-381)
+                    int nb[3];
+#pragma unroll
+                    for (int k = 1; k < 4; k++) {
+                        int ox = 0, oy = 0, oz = 0;
+                        if (axis == 0) { oy = (k >> 1) & 1; oz = k & 1; }
+                        else if (axis == 1) { ox = k & 1; oz = (k >> 1) & 1; }
+                        else { oy = k & 1; ox = (k >> 1) & 1; }
+                        nb[k - 1] = (int)hv.find(code_for_position<VPC>(pos[0] + ox, pos[1] + oy, pos[2] + oz));
+                    }
+                    if (nb[0] != -1 && nb[1] != -1 && nb[2] != -1) {
+                        // ProcessEdge (octree.cl:335-372)
+                        const int edge = axis * 4 + 3;
+                        const int m1 = (corners >> edge_c0(edge)) & 1, m2 = (corners >> edge_c1(edge)) & 1;
+                        if (m1 != m2) {
+                            q = make_int4(nb[0], nb[1], nb[2], 1 | (m1 != 0 ? 2 : 0));
+                            quads++;
+                        }
+                    }
+                }
+                b.quad_scratch[3 * (size_t)i + axis] = q;
+            }
+            const bool seam = pos[0] == 0 || pos[0] == VPC - 1 || pos[1] == 0 || pos[1] == VPC - 1 || pos[2] == 0 ||
+                              pos[2] == VPC - 1;
+            packed = quads | (seam ? 1 << 16 : 0);
+        }
+        const int total = block_sum<kNodeTile>(packed, sm);
+        if (threadIdx.x == 0) b.node_tile_counts[vt] = make_int2(total & 0xffff, total >> 16);
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_mesh_plan(BatchPtrs b) {
+    __shared__ int sm[1024 / 32 + 1];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (b.bs->overflow) return;
+    for (int c = warp; c < b.n; c += 32) {
+        const int t0 = b.chunk_tile_off[c], nt = b.chunk_tile_off[c + 1] - t0;
+        int2* t = b.node_tile_counts + t0;
+        int cq = 0, cs = 0;
+        for (int base = 0; base < nt; base += 32) {
+            const int i = base + lane;
+            const int2 v = i < nt ? t[i] : make_int2(0, 0);
+            const int iq = warp_inclusive(v.x), is = warp_inclusive(v.y);
+            if (i < nt) t[i] = make_int2(cq + iq - v.x, cs + is - v.y);
+            cq += __shfl_sync(FULL, iq, 31);
+            cs += __shfl_sync(FULL, is, 31);
+        }
+        if (lane == 0) {
+            b.cs[c].quads = cq;
+            b.cs[c].seams = cs;
+        }
+    }
+    __syncthreads();
+    const long long tq = cta_scan(
+        b.n, [&](int c) { return b.cs[c].quads; }, [&](int c, long long ex) { b.cs[c].quad_off = (int)ex; }, nullptr, sm);
+    const long long ts = cta_scan(
+        b.n, [&](int c) { return b.cs[c].seams; }, [&](int c, long long ex) { b.cs[c].seam_off = (int)ex; }, nullptr, sm);
+    if (threadIdx.x == 0) {
+        b.bs->total_quads = (int)tq;
+        b.bs->total_seams = (int)ts;
+        int ovf = 0;
+        if (2 * tq > b.triangle_cap) ovf |= OVF_QUADS;
+        if (ts > b.seam_cap) ovf |= OVF_SEAMS;
+        b.bs->overflow |= ovf;
+    }
+}
+
+template <int VPC>
+__global__ void __launch_bounds__(kNodeTile) k_mesh_scatter(BatchPtrs b) {
+    __shared__ int sm[kNodeTile / 32 + 1];
+    if (b.bs->overflow) return;
+    const int ntiles = b.chunk_tile_off[b.n];
+    // winding orders by sign-change direction (octree.cl:357-362)
+    const int w0[6] = {0, 1, 3, 0, 3, 2};
+    const int w1[6] = {0, 3, 1, 0, 2, 3};
+    for (int vt = blockIdx.x; vt < ntiles; vt += gridDim.x) {
+        const int c = chunk_of_tile(b.chunk_tile_off, b.n, vt);
+        const ChunkState& st = b.cs[c];
+        const int local = (vt - b.chunk_tile_off[c]) * kNodeTile + threadIdx.x;
+        const bool valid = local < st.nodes;
+        const int i = st.node_off + local;
+        int4 q[3];
+        int quads = 0;
+        bool seam = false;
+        int pos[3] = {0, 0, 0};
+        if (valid) {
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                q[a] = b.quad_scratch[3 * (size_t)i + a];
+                quads += q[a].w & 1;
+            }
+            position_for_code<VPC>(b.node_codes[i], pos[0], pos[1], pos[2]);
+            seam = pos[0] == 0 || pos[0] == VPC - 1 || pos[1] == 0 || pos[1] == VPC - 1 || pos[2] == 0 ||
+                   pos[2] == VPC - 1;
+        }
+        int total;
+        const int ex = block_exclusive<kNodeTile>(quads | (seam ? 1 << 16 : 0), total, sm);
+        if (valid) {
+            const int2 toff = b.node_tile_counts[vt];
+            int qp = st.quad_off + toff.x + (ex & 0xffff);
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                if (!(q[a].w & 1)) continue;
+                const int idx[4] = {local, q[a].x, q[a].y, q[a].z};
+                const int* w = (q[a].w & 2) ? w1 : w0;
+                lvn_mesh_triangle* tri = b.triangles + 2 * (size_t)qp;
+                tri[0].indices[0] = idx[w[0]];
+                tri[0].indices[1] = idx[w[1]];
+                tri[0].indices[2] = idx[w[2]];
+                tri[1].indices[0] = idx[w[3]];
+                tri[1].indices[1] = idx[w[4]];
+                tri[1].indices[2] = idx[w[5]];
+                qp++;
+            }
+            if (seam) {
+                const int sp = st.seam_off + toff.y + (ex >> 16);
+                const float4* v = reinterpret_cast<const float4*>(b.vertices + i);
+                int4* dst = reinterpret_cast<int4*>(b.seams + sp);
+                dst[0] = make_int4(pos[0], pos[1], pos[2], b.node_info[i] & 0xffff);
+                const float4 p = v[0], nrm = v[1];
+                reinterpret_cast<float4*>(dst)[1] = p;
+                reinterpret_cast<float4*>(dst)[2] = nrm;
+            }
+        }
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+
+const char* stage_name(int s) {
+    static const char* names[ST_COUNT] = {"field",      "csg",        "edge_count", "edge_plan",   "edge_scatter",
+                                          "hermite",    "vox_count",  "vox_plan",   "vox_scatter", "hash_fill",
+                                          "edge_insert", "leaf",      "node_insert", "mesh_count", "mesh_plan",
+                                          "mesh_scatter"};
+    return s >= 0 && s < ST_COUNT ? names[s] : "?";
+}
+
+#define LVN_VPC_DISPATCH(VPCVAR, CALL) \
+    switch (VPCVAR) {                   \
+        case 8: { constexpr int V = 8; CALL; } break;   \
+        case 16: { constexpr int V = 16; CALL; } break; \
+        case 32: { constexpr int V = 32; CALL; } break; \
+        case 64: { constexpr int V = 64; CALL; } break; \
+        default: return cudaErrorInvalidValue;          \
+    }
+
+static inline int persistent_grid(const BatchPtrs& b, int per_sm) { return b.num_sms * per_sm; }
+
+cudaError_t launch_reset(const BatchPtrs& b, cudaStream_t s) {
+    k_reset<<<(b.n + 255) / 256, 256, 0, s>>>(b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_field(const BatchPtrs& b, cudaStream_t s) {
+    const int fd = b.vpc + 2;
+    dim3 grid((fd * fd + 127) / 128, b.n);
+    LVN_VPC_DISPATCH(b.vpc, (k_field<V><<<grid, 128, 0, s>>>(b)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_csg(const BatchPtrs& b, cudaStream_t s) {
+    dim3 grid((field_size(b.vpc) + kThreads - 1) / kThreads, b.n);
+    LVN_VPC_DISPATCH(b.vpc, (k_csg<V><<<grid, kThreads, 0, s>>>(b)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prune_edges(const BatchPtrs& b, cudaStream_t s) {
+    LVN_VPC_DISPATCH(b.vpc, (k_prune_edges<V><<<1, 1024, 0, s>>>(b)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_edge_count(const BatchPtrs& b, cudaStream_t s) {
+    dim3 grid(edge_tiles_per_chunk(b.vpc), b.n);
+    LVN_VPC_DISPATCH(b.vpc, (k_edge_count<V><<<grid, kThreads, 0, s>>>(b)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_edge_plan(const BatchPtrs& b, cudaStream_t s) {
+    LVN_VPC_DISPATCH(b.vpc, (k_edge_plan<V><<<1, 1024, 0, s>>>(b)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_edge_scatter(const BatchPtrs& b, cudaStream_t s) {
+    dim3 grid(edge_tiles_per_chunk(b.vpc), b.n);
+    LVN_VPC_DISPATCH(b.vpc, (k_edge_scatter<V><<<grid, kThreads, 0, s>>>(b)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_hermite(const BatchPtrs& b, cudaStream_t s) {
+    LVN_VPC_DISPATCH(b.vpc, (k_hermite<V><<<persistent_grid(b, 8), kThreads, 0, s>>>(b)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_vox_count(const BatchPtrs& b, cudaStream_t s) {
+    dim3 grid(vox_tiles_per_chunk(b.vpc), b.n);
+    LVN_VPC_DISPATCH(b.vpc, (k_vox_count<V><<<grid, kThreads, 0, s>>>(b)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_vox_plan(const BatchPtrs& b, cudaStream_t s) {
+    LVN_VPC_DISPATCH(b.vpc, (k_vox_plan<V><<<1, 1024, 0, s>>>(b)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_vox_scatter(const BatchPtrs& b, cudaStream_t s) {
+    dim3 grid(vox_tiles_per_chunk(b.vpc), b.n);
+    LVN_VPC_DISPATCH(b.vpc, (k_vox_scatter<V><<<grid, kThreads, 0, s>>>(b)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_hash_fill(const BatchPtrs& b, cudaStream_t s) {
+    k_hash_fill<<<persistent_grid(b, 4), 256, 0, s>>>(b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_edge_insert(const BatchPtrs& b, cudaStream_t s) {
+    k_edge_insert<<<persistent_grid(b, 8), kThreads, 0, s>>>(b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_leaf(const BatchPtrs& b, cudaStream_t s) {
+    LVN_VPC_DISPATCH(b.vpc, (k_leaf<V><<<persistent_grid(b, 8), kThreads, 0, s>>>(b)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_node_insert(const BatchPtrs& b, cudaStream_t s) {
+    k_node_insert<<<persistent_grid(b, 8), kThreads, 0, s>>>(b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mesh_count(const BatchPtrs& b, cudaStream_t s) {
+    LVN_VPC_DISPATCH(b.vpc, (k_mesh_count<V><<<persistent_grid(b, 8), kNodeTile, 0, s>>>(b)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mesh_plan(const BatchPtrs& b, cudaStream_t s) {
+    k_mesh_plan<<<1, 1024, 0, s>>>(b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mesh_scatter(const BatchPtrs& b, cudaStream_t s) {
+    LVN_VPC_DISPATCH(b.vpc, (k_mesh_scatter<V><<<persistent_grid(b, 8), kNodeTile, 0, s>>>(b)));
+    return cudaGetLastError();
+}
+
+}  // namespace lvn

@@ -1,0 +1,119 @@
+// lvn_kernels.cuh -- device pointers of one batch and the launcher interface
+// of the chunk-meshing kernels (implemented in lvn_kernels.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "lvn_types.h"
+
+namespace lvn {
+
+// Every device buffer a batch touches.  Pools are chunk-major: chunk c's
+// edges, nodes, quads and seams are contiguous and in the reference's
+// compaction order, at offsets recorded in ChunkState.
+struct BatchPtrs {
+    int n;                       // chunks in the batch
+    int vpc;                     // voxels per chunk
+    int crossing_mode;           // 0 = 17-sample search, 1 = linear
+    int plain_class;             // 1: plain field edges are generated (fresh fields)
+    int num_sms;
+    DensityParams density;
+    int32_t default_material;
+
+    const ChunkDesc* desc;       // [n]
+    ChunkState* cs;              // [n]
+    BatchState* bs;              // [1]
+    const Brush* brushes;        // per-chunk op lists, flattened
+
+    const uint8_t* perm;         // 65536 B permutation image (alpha channel)
+    const float* grad;           // 16 x 4 gradient table
+
+    uint16_t* corners;           // [n][F]
+    int2* edge_tiles;            // [n][NBE] (plain, created) counts, then in-chunk offsets
+    int* vox_tiles;              // [n][NBV]
+
+    int32_t* edge_keys;          // [ecap]
+    int32_t* edge_chunk;         // [ecap]
+    float4* edge_info;           // [ecap]
+    int64_t ecap;
+
+    uint32_t* node_codes;        // [vcap]
+    int32_t* node_info;          // [vcap] edges << 16 | material << 8 | corners
+    int32_t* node_chunk;         // [vcap]
+    int64_t vcap;
+
+    unsigned long long* edge_slots;  // [edge_slot_cap]
+    int64_t edge_slot_cap;
+    unsigned long long* node_slots;  // [node_slot_cap]
+    int64_t node_slot_cap;
+
+    int4* quad_scratch;          // [3 * vcap] (n1, n2, n3, flags) per (node, axis)
+    int2* node_tile_counts;      // [node tile cap] (quads, seams) per node tile, then offsets
+    int* chunk_tile_off;         // [n + 1] first node tile of each chunk
+    int64_t node_tile_cap;
+
+    lvn_mesh_vertex* vertices;   // [vertex_cap]
+    int64_t vertex_cap;
+    lvn_mesh_triangle* triangles;// [triangle_cap]
+    int64_t triangle_cap;
+    lvn_seam_node* seams;        // [seam_cap]
+    int64_t seam_cap;
+
+    // cached-field CSG: the field's current edge list (chunk 0 only)
+    const int32_t* prev_keys;
+    const float4* prev_info;
+    int prev_count;
+};
+
+constexpr int kTilePoints = 2048;   // dense tile (field points / voxels) per CTA
+constexpr int kNodeTile = 256;      // sparse node tile per CTA iteration
+
+inline int field_dim(int vpc) { return vpc + 2; }
+inline int field_size(int vpc) { return (vpc + 2) * (vpc + 2) * (vpc + 2); }
+inline int edge_tiles_per_chunk(int vpc) { return (field_size(vpc) + kTilePoints - 1) / kTilePoints; }
+inline int vox_tiles_per_chunk(int vpc) { return (vpc * vpc * vpc + kTilePoints - 1) / kTilePoints; }
+
+// Stage identifiers for profiling (order of execution).
+enum Stage {
+    ST_FIELD = 0,
+    ST_CSG,
+    ST_EDGE_COUNT,
+    ST_EDGE_PLAN,
+    ST_EDGE_SCATTER,
+    ST_HERMITE,
+    ST_VOX_COUNT,
+    ST_VOX_PLAN,
+    ST_VOX_SCATTER,
+    ST_HASH_FILL,
+    ST_EDGE_INSERT,
+    ST_LEAF,
+    ST_NODE_INSERT,
+    ST_MESH_COUNT,
+    ST_MESH_PLAN,
+    ST_MESH_SCATTER,
+    ST_COUNT
+};
+const char* stage_name(int s);
+
+// Launchers: each enqueues one kernel of the pipeline on `stream`.
+cudaError_t launch_reset(const BatchPtrs& b, cudaStream_t stream);
+cudaError_t launch_field(const BatchPtrs& b, cudaStream_t stream);
+cudaError_t launch_csg(const BatchPtrs& b, cudaStream_t stream);
+cudaError_t launch_prune_edges(const BatchPtrs& b, cudaStream_t stream);
+cudaError_t launch_edge_count(const BatchPtrs& b, cudaStream_t stream);
+cudaError_t launch_edge_plan(const BatchPtrs& b, cudaStream_t stream);
+cudaError_t launch_edge_scatter(const BatchPtrs& b, cudaStream_t stream);
+cudaError_t launch_hermite(const BatchPtrs& b, cudaStream_t stream);
+cudaError_t launch_vox_count(const BatchPtrs& b, cudaStream_t stream);
+cudaError_t launch_vox_plan(const BatchPtrs& b, cudaStream_t stream);
+cudaError_t launch_vox_scatter(const BatchPtrs& b, cudaStream_t stream);
+cudaError_t launch_hash_fill(const BatchPtrs& b, cudaStream_t stream);
+cudaError_t launch_edge_insert(const BatchPtrs& b, cudaStream_t stream);
+cudaError_t launch_leaf(const BatchPtrs& b, cudaStream_t stream);
+cudaError_t launch_node_insert(const BatchPtrs& b, cudaStream_t stream);
+cudaError_t launch_mesh_count(const BatchPtrs& b, cudaStream_t stream);
+cudaError_t launch_mesh_plan(const BatchPtrs& b, cudaStream_t stream);
+cudaError_t launch_mesh_scatter(const BatchPtrs& b, cudaStream_t stream);
+
+}  // namespace lvn

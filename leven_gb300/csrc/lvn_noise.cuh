@@ -1,0 +1,236 @@
+// lvn_noise.cuh -- device simplex noise, fractals, terrain densities and CSG
+// brushes for the chunk-meshing path.
+//
+// Semantics follow the reference's OpenCL (leven/cl/simplex.cl, noise.cl,
+// apply_csg_operation.cl, hg_sdf.glsl fBox/pR).  The library is compiled with
+// -fmad=false: a multiply-add is fused only where this file calls fmaf, so the
+// result of every density evaluation is a fixed sequence of IEEE single
+// precision operations:
+//   * dot(a,b) = fma(a.z,b.z, fma(a.y,b.y, a.x*b.x))  (2D drops the z term)
+//   * octave accumulation `noise += s * amplitude` = fma(s, amplitude, noise)
+//   * mix(a,b,t) = fma(b-a, t, a)
+//   * the image sampler (nearest, repeat, normalised coordinates) resolves an
+//     integer lattice coordinate i to texel i & 255; the 3D second lookup
+//     uses u = A/255, i.e. column A for A < 255 and column 0 for A == 255
+//   * snoise3's falloff constant 0.6 is single precision
+//   * pow(frequency, -1) in the ridged fractal is 1.f / frequency
+#pragma once
+#include <cstdint>
+#include <cfloat>
+
+#include "lvn_types.h"
+
+namespace lvn {
+
+// Permutation image in the layout the kernels read: v[row*256 + col] is the
+// alpha channel (shuffled permutation value), grad[k] the RGB channel of a
+// texel whose alpha has low nibble k, as read_imagef returns it.
+struct PermTable {
+    const uint8_t* v;   // 65536 bytes, device
+    const float* grad;  // 16 x 4 floats, device (xyz used)
+};
+
+__device__ __forceinline__ int texel(int row, int col) { return ((row & 255) << 8) | (col & 255); }
+__device__ __forceinline__ int alpha_column(int a) { return a == 255 ? 0 : a; }
+
+__device__ __forceinline__ float dot2(float ax, float ay, float bx, float by) { return fmaf(ay, by, ax * bx); }
+__device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, float by, float bz) {
+    return fmaf(az, bz, fmaf(ay, by, ax * bx));
+}
+
+struct Noise {
+    const uint8_t* __restrict__ v;
+    const float* __restrict__ g;  // in shared memory when staged
+
+    __device__ __forceinline__ int perm(int idx) const { return __ldg(v + idx); }
+
+    // snoise2 (simplex.cl:158-216)
+    __device__ __forceinline__ float snoise2(float px, float py) const {
+        const float F2 = 0.366025403784f;
+        const float G2 = 0.211324865405f;
+        const float C2 = 1.f - 2.f * G2;
+        const float s = (px + py) * F2;
+        const float pix = floorf(px + s);
+        const float piy = floorf(py + s);
+        const float t = (pix + piy) * G2;
+        const float x0 = px - (pix - t);
+        const float y0 = py - (piy - t);
+        const int ix = (int)pix, iy = (int)piy;
+        const int o1x = x0 > y0 ? 1 : 0;
+        const int o1y = 1 - o1x;
+        const int k0 = perm(texel(iy, ix)) & 15;
+        const int k1 = perm(texel(iy + o1y, ix + o1x)) & 15;
+        const int k2 = perm(texel(iy + 1, ix + 1)) & 15;
+
+        float n0 = 0.f, n1 = 0.f, n2 = 0.f;
+        float t0 = 0.5f - dot2(x0, y0, x0, y0);
+        if (!(t0 < 0.f)) { t0 = t0 * t0; n0 = (t0 * t0) * dot2(g[4 * k0], g[4 * k0 + 1], x0, y0); }
+        const float x1 = (x0 - (float)o1x) + G2, y1 = (y0 - (float)o1y) + G2;
+        float t1 = 0.5f - dot2(x1, y1, x1, y1);
+        if (!(t1 < 0.f)) { t1 = t1 * t1; n1 = (t1 * t1) * dot2(g[4 * k1], g[4 * k1 + 1], x1, y1); }
+        const float x2 = x0 - C2, y2 = y0 - C2;
+        float t2 = 0.5f - dot2(x2, y2, x2, y2);
+        if (!(t2 < 0.f)) { t2 = t2 * t2; n2 = (t2 * t2) * dot2(g[4 * k2], g[4 * k2 + 1], x2, y2); }
+        return 70.f * ((n0 + n1) + n2);
+    }
+
+    __device__ __forceinline__ float corner3(int ix, int iy, int iz, float x, float y, float z) const {
+        const int a = perm(texel(iy, ix));
+        const int k = perm(texel(iz, alpha_column(a))) & 15;
+        float tt = 0.6f - dot3(x, y, z, x, y, z);
+        if (tt < 0.f) return 0.f;
+        tt = tt * tt;
+        return (tt * tt) * dot3(g[4 * k], g[4 * k + 1], g[4 * k + 2], x, y, z);
+    }
+
+    // snoise3 (simplex.cl:218-289) with simplex() ranking (simplex.cl:133-156)
+    __device__ __forceinline__ float snoise3(float px, float py, float pz) const {
+        const float F3 = 0.333333333333f;
+        const float G3 = 0.166666666667f;
+        const float C2 = 2.f * G3;
+        const float C3 = 1.f - 3.f * G3;
+        const float s = ((px + py) + pz) * F3;
+        const float pix = floorf(px + s);
+        const float piy = floorf(py + s);
+        const float piz = floorf(pz + s);
+        const float t = ((pix + piy) + piz) * G3;
+        const float x0 = px - (pix - t);
+        const float y0 = py - (piy - t);
+        const float z0 = pz - (piz - t);
+        const int ix = (int)pix, iy = (int)piy, iz = (int)piz;
+        const int isx_y = x0 >= y0 ? 1 : 0;
+        const int isx_z = x0 >= z0 ? 1 : 0;
+        const int isy_z = y0 >= z0 ? 1 : 0;
+        const int off_x = isx_y + isx_z;
+        const int off_y = (1 - isx_y) + isy_z;
+        const int off_z = (1 - isx_z) + (1 - isy_z);
+        const int o2x = min(max(off_x, 0), 1), o2y = min(max(off_y, 0), 1), o2z = min(max(off_z, 0), 1);
+        const int o1x = min(max(off_x - 1, 0), 1), o1y = min(max(off_y - 1, 0), 1), o1z = min(max(off_z - 1, 0), 1);
+        const float n0 = corner3(ix, iy, iz, x0, y0, z0);
+        const float n1 = corner3(ix + o1x, iy + o1y, iz + o1z, (x0 - (float)o1x) + G3, (y0 - (float)o1y) + G3,
+                                 (z0 - (float)o1z) + G3);
+        const float n2 = corner3(ix + o2x, iy + o2y, iz + o2z, (x0 - (float)o2x) + C2, (y0 - (float)o2y) + C2,
+                                 (z0 - (float)o2z) + C2);
+        const float n3 = corner3(ix + 1, iy + 1, iz + 1, x0 - C3, y0 - C3, z0 - C3);
+        return 32.f * (((n0 + n1) + n2) + n3);
+    }
+
+    // BasicFractal (noise.cl:8-36), NOISE_SCALE == 1
+    __device__ __forceinline__ float fbm2(int octaves, float frequency, float lacunarity, float persistence, float x,
+                                          float y) const {
+        float px = x * 1.f, py = y * 1.f;
+        float noise = 0.f, amplitude = 1.f;
+        px = px * frequency;
+        py = py * frequency;
+        for (int i = 0; i < octaves; i++) {
+            noise = fmaf(snoise2(px, py), amplitude, noise);
+            px = px * lacunarity;
+            py = py * lacunarity;
+            amplitude = amplitude * persistence;
+        }
+        return noise;
+    }
+
+    // 3D analogue of BasicFractal (the cave term)
+    __device__ __forceinline__ float fbm3(int octaves, float frequency, float lacunarity, float persistence, float x,
+                                          float y, float z) const {
+        float px = x * frequency, py = y * frequency, pz = z * frequency;
+        float noise = 0.f, amplitude = 1.f;
+        for (int i = 0; i < octaves; i++) {
+            noise = fmaf(snoise3(px, py, pz), amplitude, noise);
+            px = px * lacunarity;
+            py = py * lacunarity;
+            pz = pz * lacunarity;
+            amplitude = amplitude * persistence;
+        }
+        return noise;
+    }
+
+    // RidgedMultiFractal (noise.cl:42-81), RIDGED_MULTI_H == 1
+    __device__ __forceinline__ float ridged(int octaves, float lacunarity, float gain, float offset, float x,
+                                            float y) const {
+        float px = x * 1.f, py = y * 1.f;
+        float signal = snoise2(px, py);
+        signal = fabsf(signal);
+        signal = offset - signal;
+        signal = signal * signal;
+        float noise = signal;
+        float weight = 1.f;
+        float frequency = 1.f;
+        for (int i = 0; i < octaves; i++) {
+            px = px * lacunarity;
+            py = py * lacunarity;
+            weight = signal * gain;
+            weight = fminf(fmaxf(weight, 0.f), 1.f);
+            signal = snoise2(px, py);
+            signal = fabsf(signal);
+            signal = offset - signal;
+            signal = signal * weight;
+            const float exponent = 1.f / frequency;
+            frequency = frequency * lacunarity;
+            noise = fmaf(signal, exponent, noise);
+        }
+        noise = noise * (1.f / (float)octaves);
+        return noise;
+    }
+
+    // Terrain (noise.cl:205-223)
+    __device__ __forceinline__ float terrain(float x, float z) const {
+        const float px = x * (1.f / 2000.f);
+        const float pz = z * (1.f / 2000.f);
+        float r = 0.8f * ridged(7, 2.114352f, 1.5241f, 1.f, px, pz);
+        r = fminf(fmaxf(r, 0.f), 1.f);
+        float billow = 0.6f * fbm2(4, 0.24f, 1.8754f, 0.433f, -4.33f * px, 7.98f * pz);
+        billow = fmaf(0.5f, billow, 0.5f);
+        float b2 = 0.6f * fbm2(2, 0.63f, 2.2f, 0.15f, px, pz);
+        b2 = fmaf(b2, 0.5f, 0.5f);
+        return fmaf(billow, r, b2);
+    }
+
+    // The height term h(x,z) of a heightfield density d = y - amp*h (+ caves)
+    __device__ __forceinline__ float height(const DensityParams& d, float x, float z) const {
+        if (d.mode == LVN_DENSITY_REFERENCE) return terrain(x, z);
+        return fbm2(d.octaves2, d.freq2, d.lacunarity2, d.gain2, x, z);
+    }
+    __device__ __forceinline__ float height_amp(const DensityParams& d) const {
+        return d.mode == LVN_DENSITY_REFERENCE ? 900.f : d.amp2;  // MAX_TERRAIN_HEIGHT
+    }
+    // density from a precomputed height term: DensityFunc (noise.cl:225-268)
+    __device__ __forceinline__ float density_h(const DensityParams& d, float h, float x, float y, float z) const {
+        const float base = fmaf(-height_amp(d), h, y);
+        if (d.mode != LVN_DENSITY_CAVES) return base;
+        return fmaf(d.amp3, fbm3(d.octaves3, d.freq3, d.lacunarity3, d.gain3, x, y, z), base);
+    }
+    __device__ __forceinline__ float density(const DensityParams& d, float x, float y, float z) const {
+        return density_h(d, height(d, x, z), x, y, z);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// CSG brushes: apply_csg_operation.cl:42-175, hg_sdf.glsl fBox (218-221), pR (460-463)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ float length3(float x, float y, float z) { return sqrtf(dot3(x, y, z, x, y, z)); }
+
+__device__ __forceinline__ float brush_density(const Brush& b, float wx, float wy, float wz) {
+    const float lx = wx - b.origin[0], ly = wy - b.origin[1], lz = wz - b.origin[2];
+    if (b.brush != 0) return length3(lx, ly, lz) - b.dimensions[0];  // Density_Sphere
+    const float rx = fmaf(b.sin_y, lz, b.cos_y * lx);                 // pR(p.xz, rotateY)
+    const float rz = fmaf(b.sin_y, -lx, b.cos_y * lz);
+    const float dx = fabsf(rx) - b.dimensions[0];
+    const float dy = fabsf(ly) - b.dimensions[1];
+    const float dz = fabsf(rz) - b.dimensions[2];
+    const float outside = length3(fmaxf(dx, 0.f), fmaxf(dy, 0.f), fmaxf(dz, 0.f));
+    const float inside = fmaxf(fmaxf(fminf(dx, 0.f), fminf(dy, 0.f)), fminf(dz, 0.f));
+    return outside + inside;
+}
+
+__device__ __forceinline__ void normalize3(float& x, float& y, float& z) {
+    const float len = sqrtf(dot3(x, y, z, x, y, z));
+    if (len == 0.f) { x = y = z = 0.f; return; }
+    x = x / len;
+    y = y / len;
+    z = z / len;
+}
+
+}  // namespace lvn

@@ -1,0 +1,103 @@
+// lvn_types.h -- plain structs shared by the host orchestration and the
+// device kernels of liblvn.  No CUDA or torch types; includable from C++.
+#pragma once
+#include <cstdint>
+
+#include "../../include/lvn.h"
+
+namespace lvn {
+
+constexpr int MATERIAL_NONE = 200;  // leven/src/volume_materials.h:7
+constexpr int MATERIAL_AIR = 201;   // leven/src/volume_materials.h:8
+constexpr int LEAF_SIZE_SCALE = 4;  // leven/src/volume_constants.h:7-8
+constexpr int CLIPMAP_LEAF_SIZE = 256;  // volume_constants.h:15
+
+// cuckoo constants (leven/src/compute_cuckoo.h:6-10)
+constexpr uint64_t CUCKOO_EMPTY = ~0ull;
+constexpr int CUCKOO_STASH_HASH_INDEX = 4;
+constexpr int CUCKOO_HASH_FN_COUNT = 5;
+constexpr int CUCKOO_STASH_SIZE = 101;
+constexpr int CUCKOO_MAX_ITERATIONS = 32;
+constexpr uint32_t CUCKOO_MIN_TABLE_SIZE = 2048u;  // compute_cuckoo.cpp:15
+
+// corner word in the field array: material | plain-solid << 8 | changed << 9
+constexpr uint16_t CORNER_PLAIN_SOLID = 1u << 8;
+constexpr uint16_t CORNER_CHANGED = 1u << 9;
+
+typedef lvn_density_params DensityParams;
+
+// A CSG operation as the kernels read it (48 B): the reference's
+// CSGOperationInfo plus cos/sin of rotate_y evaluated once on the host.
+struct Brush {
+    float origin[3];
+    int32_t type;
+    float dimensions[3];
+    int32_t brush;
+    float cos_y, sin_y;
+    int32_t material;
+    int32_t pad;
+};
+static_assert(sizeof(Brush) == 48, "Brush layout");
+
+// Per-chunk descriptor uploaded with each batch (host -> device).
+struct ChunkDesc {
+    int32_t off[3];      // density-space origin = min / LEAF_SIZE_SCALE
+    int32_t scale;       // sampleScale
+    int32_t min[3];      // world min
+    int32_t size;        // world size
+    float colour[3];     // ColourForMinLeafSize(size / 256)
+    int32_t op_begin;    // into the batch brush array
+    int32_t op_count;
+    int32_t pad[3];
+    uint32_t edge_params[CUCKOO_HASH_FN_COUNT * 2];
+    uint32_t node_params[CUCKOO_HASH_FN_COUNT * 2];
+};
+
+// Per-chunk counters and offsets produced on the device.
+struct ChunkState {
+    int32_t plain_edges;     // plain edges kept (not touched by CSG)
+    int32_t created_edges;   // CSG-created edges
+    int32_t edge_off;        // first edge in the batch edge pool
+    int32_t num_edges;
+    int32_t nodes;           // active voxels
+    int32_t node_off;
+    int32_t quads;
+    int32_t quad_off;
+    int32_t seams;
+    int32_t seam_off;
+    uint32_t edge_prime;
+    int32_t edge_table_off;  // slots; the stash follows the table
+    uint32_t node_prime;
+    int32_t node_table_off;
+    int32_t edge_stash_used;
+    int32_t node_stash_used;
+    int32_t edge_insert_failed;
+    int32_t node_insert_failed;
+    int32_t kept_edges;      // edges kept from a cached field (cached-field CSG)
+    int32_t pad;
+};
+static_assert(sizeof(ChunkState) == 80, "ChunkState layout");
+
+// Batch-wide totals and status (device).
+struct BatchState {
+    int32_t total_edges;
+    int32_t total_nodes;
+    int32_t total_quads;
+    int32_t total_seams;
+    int64_t total_edge_slots;
+    int64_t total_node_slots;
+    int32_t overflow;        // bitmask of pools that ran out of capacity
+    int32_t status;          // device-side internal status (0 = ok)
+    int32_t pad[6];
+};
+
+enum OverflowBits : int32_t {
+    OVF_EDGES = 1,
+    OVF_NODES = 2,
+    OVF_QUADS = 4,
+    OVF_SEAMS = 8,
+    OVF_EDGE_SLOTS = 16,
+    OVF_NODE_SLOTS = 32,
+};
+
+}  // namespace lvn

@@ -1,0 +1,135 @@
+"""Seeded synthetic workloads for the chunk-meshing path.
+
+Chunk lists are world-space (min, size) pairs as the engine passes them to
+generateChunkMesh (1 voxel = 4 world units at LOD0, a 64^3 chunk at LOD k has
+size 256 * 2^k).  CSG operations are in density units, as
+Clipmap::queueCSGOperation produces them (leven/src/clipmap.cpp:1618-1636).
+
+Random numbers come from a 32-bit Mersenne twister with std::mt19937's
+seeding, so the same seed gives the same operations in C++ and Python;
+floats are (x >> 8) * 2^-24, uniform in [0, 1).
+"""
+from dataclasses import dataclass
+
+MATERIAL_AIR = 201
+
+
+class MT19937:
+    """std::mt19937 (seed_seq-free constructor semantics)."""
+
+    def __init__(self, seed=5489):
+        self.mt = [0] * 624
+        self.mt[0] = seed & 0xFFFFFFFF
+        for i in range(1, 624):
+            self.mt[i] = (1812433253 * (self.mt[i - 1] ^ (self.mt[i - 1] >> 30)) + i) & 0xFFFFFFFF
+        self.index = 624
+
+    def _twist(self):
+        mt = self.mt
+        for i in range(624):
+            y = (mt[i] & 0x80000000) | (mt[(i + 1) % 624] & 0x7FFFFFFF)
+            v = mt[(i + 397) % 624] ^ (y >> 1)
+            if y & 1:
+                v ^= 0x9908B0DF
+            mt[i] = v
+        self.index = 0
+
+    def u32(self):
+        if self.index >= 624:
+            self._twist()
+        y = self.mt[self.index]
+        self.index += 1
+        y ^= y >> 11
+        y ^= (y << 7) & 0x9D2C5680
+        y ^= (y << 15) & 0xEFC60000
+        y ^= y >> 18
+        return y & 0xFFFFFFFF
+
+    def uniform(self, lo, hi):
+        return lo + (hi - lo) * ((self.u32() >> 8) * (1.0 / 16777216.0))
+
+
+@dataclass
+class Op:
+    type: int          # 0 add (union), 1 subtract
+    brush_shape: int   # 0 cube, 1 sphere
+    material: int
+    origin: tuple      # density units
+    dimensions: tuple  # half extents / radius in [0]
+    rotate_y: float = 0.0
+
+    def as_tuple(self):
+        return (self.type, self.brush_shape, self.material, self.rotate_y, self.origin, self.dimensions)
+
+
+@dataclass
+class Workload:
+    name: str
+    chunks: list       # [((x, y, z), size)]
+    ops: list          # [Op]
+    density: dict      # keyword arguments of leven_gb300.set_density
+    noise_seed: int = 1
+    voxels_per_chunk: int = 64
+
+
+FBM2D = dict(mode=1, octaves2=8, freq2=1.0 / 256.0, lacunarity2=2.0, gain2=0.5, amp2=48.0)
+CAVES = dict(mode=2, octaves2=8, freq2=1.0 / 256.0, lacunarity2=2.0, gain2=0.5, amp2=48.0,
+             octaves3=6, freq3=1.0 / 64.0, lacunarity3=2.0, gain3=0.5, amp3=12.0)
+
+
+def plain_one_chunk():
+    """One LOD0 64^3 chunk, density-space origin (0, 32, 0), 2D fBm terrain
+    (8 octaves, 1/256, lacunarity 2, gain 0.5, amplitude 48), seed 1."""
+    return Workload("plain-one-chunk-64", [((0, 128, 0), 256)], [], FBM2D)
+
+
+def csg_ops(n, seed, region_lo, region_hi, rmin=2.0, rmax=12.0):
+    """n operations, half sphere-subtract (type 1, sphere, AIR) and half
+    box-union (type 0, cube, material 1), centres uniform in the region,
+    radius / half extents uniform in [rmin, rmax] voxels, no rotation."""
+    rng = MT19937(seed)
+    ops = []
+    for _ in range(n):
+        subtract = (rng.u32() & 1) == 1
+        c = tuple(rng.uniform(region_lo[i], region_hi[i]) for i in range(3))
+        if subtract:
+            r = rng.uniform(rmin, rmax)
+            ops.append(Op(1, 1, MATERIAL_AIR, c, (r, r, r)))
+        else:
+            ops.append(Op(0, 0, 1, c, tuple(rng.uniform(rmin, rmax) for _ in range(3))))
+    return ops
+
+
+def tiled_csg(nx=8, ny=2, nz=8, n_ops=32, seed=1):
+    """LOD0 64^3 chunks tiling a (64 nx) x (64 ny) x (64 nz) voxel region,
+    y centred on 0 so that the fBm surface is inside, with n_ops seeded CSG
+    operations.  The default is 8 x 2 x 8 = 128 chunks over 512 x 128 x 512
+    voxels and 32 operations."""
+    y0 = -(64 * ny) // 2
+    chunks = [((256 * i, 4 * y0 + 256 * j, 256 * k), 256) for k in range(nz) for j in range(ny) for i in range(nx)]
+    ops = csg_ops(n_ops, seed, (0.0, float(y0), 0.0), (64.0 * nx, float(y0 + 64 * ny), 64.0 * nz))
+    return Workload(f"tiled-csg-{len(chunks)}x64^3-{n_ops}ops", chunks, ops, FBM2D)
+
+
+def op_bounds(op):
+    """CalcCSGOperationBounds (clipmap.cpp:1638-1643)."""
+    import numpy as np
+
+    lo, hi = [], []
+    for i in range(3):
+        half = int(np.float32(op.dimensions[i]) * np.float32(4.0)) + 2
+        origin = int((np.float32(op.origin[i]) - np.float32(0.5)) * np.float32(4.0))
+        lo.append(origin - half)
+        hi.append(origin + half)
+    return lo, hi
+
+
+def ops_for_chunk(ops, mn, size):
+    """Stored operations whose AABB overlaps the chunk (compute_density_field.cpp:255-263)."""
+    out = []
+    for op in ops:
+        lo, hi = op_bounds(op)
+        if not (mn[0] + size < lo[0] or mn[1] + size < lo[1] or mn[2] + size < lo[2] or mn[0] > hi[0] or
+                mn[1] > hi[1] or mn[2] > hi[2]):
+            out.append(op)
+    return out

@@ -1,0 +1,1314 @@
+// lvn_oracle.cpp -- CPU restatement of the leven chunk-meshing path.
+//
+// TEST INFRASTRUCTURE ONLY (see lvn_oracle.h).  Plain sequential C++17,
+// compiled with -O2 -ffp-contract=off and no fast-math, so that every
+// floating-point operation is the IEEE single-precision operation written
+// here.  Fused multiply-adds appear only where this file calls std::fmaf;
+// the CUDA product path performs the same operations in the same order.
+//
+// Floating-point conventions of this restatement (the reference was compiled
+// with -cl-fast-relaxed-math, leven/src/compute.cpp:258, so its own bits are
+// implementation-defined; these rules fix one admissible choice):
+//   * dot(a,b) = fma(a.z,b.z, fma(a.y,b.y, a.x*b.x))   (2D: fma(a.y,b.y,a.x*b.x))
+//   * a += b*c in fBm / octave accumulation loops = fma(b, c, a)
+//   * mix(a,b,t) = fma(b-a, t, a)
+//   * snoise3's `0.6 - dot` (a double literal in simplex.cl:243) is single
+//     precision here; snoise2's `0.5 - dot` is exact either way.
+//   * pow(frequency, -1) in RidgedMultiFractal (noise.cl:73) = 1.f / frequency
+//   * normalize(v) = v / sqrt(dot(v,v)); a zero vector stays zero.
+//   * rsqrt in givens_coeffs_sym (qef.cl:40) = 1.f / sqrtf(x); the double
+//     expressions of svd_rotateq_xy (`2.0 * c * s * a`, qef.cl:52) and
+//     svd_invdet (`1.0 / x`, qef.cl:108) are evaluated in single precision.
+//   * Image reads (simplex.cl:59, nearest + repeat + normalised coordinates)
+//     resolve an integer lattice coordinate i to texel (i & 255); the 3D
+//     second lookup uses u = A/255, which selects column A for A < 255 and
+//     column 0 for A == 255 (u == 1.0 wraps to 0).
+#include "lvn_oracle.h"
+
+#include <algorithm>
+#include <array>
+#include <atomic>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <random>
+#include <thread>
+#include <unordered_set>
+#include <vector>
+
+namespace {
+
+constexpr int MATERIAL_NONE = 200;   // leven/src/volume_materials.h:7
+constexpr int MATERIAL_AIR = 201;    // leven/src/volume_materials.h:8
+constexpr int LEAF_SIZE_SCALE = 4;   // leven/src/volume_constants.h:7-8
+
+// ---------------------------------------------------------------------------
+// Permutation lookup image: compute_density_field.cpp:28-125
+// ---------------------------------------------------------------------------
+
+// Ken Perlin's reference permutation (public domain).
+const int kPerlin[256] = {
+    151, 160, 137, 91,  90,  15,  131, 13,  201, 95,  96,  53,  194, 233, 7,   225,
+    140, 36,  103, 30,  69,  142, 8,   99,  37,  240, 21,  10,  23,  190, 6,   148,
+    247, 120, 234, 75,  0,   26,  197, 62,  94,  252, 219, 203, 117, 35,  11,  32,
+    57,  177, 33,  88,  237, 149, 56,  87,  174, 20,  125, 136, 171, 168, 68,  175,
+    74,  165, 71,  134, 139, 48,  27,  166, 77,  146, 158, 231, 83,  111, 229, 122,
+    60,  211, 133, 230, 220, 105, 92,  41,  55,  46,  245, 40,  244, 102, 143, 54,
+    65,  25,  63,  161, 1,   216, 80,  73,  209, 76,  132, 187, 208, 89,  18,  169,
+    200, 196, 135, 130, 116, 188, 159, 86,  164, 100, 109, 198, 173, 186, 3,   64,
+    52,  217, 226, 250, 124, 123, 5,   202, 38,  147, 118, 126, 255, 82,  85,  212,
+    207, 206, 59,  227, 47,  16,  58,  17,  182, 189, 28,  42,  223, 183, 170, 213,
+    119, 248, 152, 2,   44,  154, 163, 70,  221, 153, 101, 155, 167, 43,  172, 9,
+    129, 22,  39,  253, 19,  98,  108, 110, 79,  113, 224, 232, 178, 185, 112, 104,
+    218, 246, 97,  228, 251, 34,  242, 193, 238, 210, 144, 12,  191, 179, 162, 241,
+    81,  51,  145, 235, 249, 14,  239, 107, 49,  192, 214, 31,  181, 199, 106, 157,
+    184, 84,  204, 176, 115, 121, 50,  45,  127, 4,   150, 254, 138, 236, 205, 93,
+    222, 114, 67,  29,  24,  72,  243, 141, 128, 195, 78,  66,  215, 61,  156, 180,
+};
+
+// Perlin's 16 gradient directions (compute_density_field.cpp:60-63).
+const int kGrad3[16][3] = {{0, 1, 1},  {0, 1, -1},  {0, -1, 1}, {0, -1, -1},
+                           {1, 0, 1},  {1, 0, -1},  {-1, 0, 1}, {-1, 0, -1},
+                           {1, 1, 0},  {1, -1, 0},  {-1, 1, 0}, {-1, -1, 0},
+                           {1, 0, -1}, {-1, 0, -1}, {0, -1, 1}, {0, 1, 1}};
+
+// The reference's `int perm[512]` literal (compute_density_field.cpp:28-52)
+// holds 506 values: Perlin's 256, then the same list without its first six
+// entries; aggregate initialisation zero-fills the last six.
+std::array<int, 512> reference_perm512() {
+    std::array<int, 512> p{};
+    for (int i = 0; i < 256; i++) p[i] = kPerlin[i];
+    for (int k = 0; k < 250; k++) p[256 + k] = kPerlin[6 + k];
+    for (int i = 506; i < 512; i++) p[i] = 0;
+    return p;
+}
+
+// Jenkins one-at-a-time over the four little-endian bytes of the key
+// (compute_density_field.cpp:68-86).
+uint32_t noise_hash(int x, int y, int seed) {
+    const uint32_t key = (uint32_t)(((uint32_t)x << 24) | ((uint32_t)y << 16)) ^ (uint32_t)seed;
+    uint32_t hash = 0;
+    for (int i = 0; i < 4; i++) {
+        hash += (key >> (8 * i)) & 0xffu;
+        hash += (hash << 10);
+        hash ^= (hash >> 6);
+    }
+    hash += (hash << 3);
+    hash ^= (hash >> 11);
+    hash += (hash << 15);
+    return hash;
+}
+
+struct PermLut {
+    uint8_t v[65536];   // alpha channel: shuffled permutation value per texel
+    float g[16][3];     // RGB channel as read_imagef returns it: (b/255)*4-1
+};
+
+PermLut g_lut;
+bool g_lut_ready = false;
+
+// CreateNoisePermutationLookupImage (compute_density_field.cpp:90-125)
+void build_lut(int seed, PermLut* L) {
+    std::array<int, 512> shuffled = reference_perm512();
+    std::shuffle(shuffled.begin(), shuffled.end(), std::default_random_engine(seed));
+    for (int i = 0; i < 256; i++) {
+        for (int j = 0; j < 256; j++) {
+            const uint8_t value = (uint8_t)shuffled[noise_hash(i, j, seed) & 0x1ff];
+            L->v[i * 256 + j] = value;  // row i (v coordinate), column j (u)
+        }
+    }
+    for (int k = 0; k < 16; k++) {
+        for (int c = 0; c < 3; c++) {
+            const unsigned char b = (unsigned char)(kGrad3[k][c] * 64 + 64);
+            L->g[k][c] = ((float)b / 255.0f) * 4.0f - 1.0f;
+        }
+    }
+}
+
+inline int texel(int row, int col) { return ((row & 255) << 8) | (col & 255); }
+// u = A/255 as a normalised coordinate: column A, except A == 255 -> 1.0 -> 0
+inline int alpha_column(int a) { return a == 255 ? 0 : a; }
+
+// ---------------------------------------------------------------------------
+// Simplex noise: simplex.cl:158-289 (Gustavson, public domain)
+// ---------------------------------------------------------------------------
+
+inline float dot2(float ax, float ay, float bx, float by) { return std::fmaf(ay, by, ax * bx); }
+inline float dot3(float ax, float ay, float az, float bx, float by, float bz) {
+    return std::fmaf(az, bz, std::fmaf(ay, by, ax * bx));
+}
+
+const float F2 = 0.366025403784f;
+const float G2 = 0.211324865405f;
+const float F3 = 0.333333333333f;
+const float G3 = 0.166666666667f;
+
+float snoise2(float px, float py, const PermLut& L) {
+    const float c2 = 1.f - 2.f * G2;
+    const float s = (px + py) * F2;
+    const float pix = std::floor(px + s);
+    const float piy = std::floor(py + s);
+    const float t = (pix + piy) * G2;
+    const float x0 = px - (pix - t);
+    const float y0 = py - (piy - t);
+    const int ix = (int)pix, iy = (int)piy;
+    const int o1x = x0 > y0 ? 1 : 0;
+    const int o1y = 1 - o1x;
+
+    float n0 = 0.f, n1 = 0.f, n2 = 0.f;
+    {
+        const float* g = L.g[L.v[texel(iy, ix)] & 15];
+        float t0 = 0.5f - dot2(x0, y0, x0, y0);
+        if (!(t0 < 0.f)) { t0 = t0 * t0; n0 = (t0 * t0) * dot2(g[0], g[1], x0, y0); }
+    }
+    const float x1 = (x0 - (float)o1x) + G2, y1 = (y0 - (float)o1y) + G2;
+    {
+        const float* g = L.g[L.v[texel(iy + o1y, ix + o1x)] & 15];
+        float t1 = 0.5f - dot2(x1, y1, x1, y1);
+        if (!(t1 < 0.f)) { t1 = t1 * t1; n1 = (t1 * t1) * dot2(g[0], g[1], x1, y1); }
+    }
+    const float x2 = x0 - c2, y2 = y0 - c2;
+    {
+        const float* g = L.g[L.v[texel(iy + 1, ix + 1)] & 15];
+        float t2 = 0.5f - dot2(x2, y2, x2, y2);
+        if (!(t2 < 0.f)) { t2 = t2 * t2; n2 = (t2 * t2) * dot2(g[0], g[1], x2, y2); }
+    }
+    return 70.f * ((n0 + n1) + n2);
+}
+
+float snoise3(float px, float py, float pz, const PermLut& L) {
+    const float c2 = 2.f * G3;
+    const float c3 = 1.f - 3.f * G3;
+    const float s = ((px + py) + pz) * F3;
+    const float pix = std::floor(px + s);
+    const float piy = std::floor(py + s);
+    const float piz = std::floor(pz + s);
+    const float t = ((pix + piy) + piz) * G3;
+    const float x0 = px - (pix - t);
+    const float y0 = py - (piy - t);
+    const float z0 = pz - (piz - t);
+    const int ix = (int)pix, iy = (int)piy, iz = (int)piz;
+
+    // simplex() (simplex.cl:133-156): rank the components of Pf0
+    const int isx_y = x0 >= y0 ? 1 : 0;  // step(P.y, P.x)
+    const int isx_z = x0 >= z0 ? 1 : 0;  // step(P.z, P.x)
+    const int isy_z = y0 >= z0 ? 1 : 0;  // step(P.z, P.y)
+    const int off_x = isx_y + isx_z;
+    const int off_y = (1 - isx_y) + isy_z;
+    const int off_z = (1 - isx_z) + (1 - isy_z);
+    const int o2x = std::min(std::max(off_x, 0), 1), o2y = std::min(std::max(off_y, 0), 1),
+              o2z = std::min(std::max(off_z, 0), 1);
+    const int o1x = std::min(std::max(off_x - 1, 0), 1), o1y = std::min(std::max(off_y - 1, 0), 1),
+              o1z = std::min(std::max(off_z - 1, 0), 1);
+
+    auto corner = [&](int dx, int dy, int dz, float x, float y, float z) -> float {
+        const int a = L.v[texel(iy + dy, ix + dx)];
+        const float* g = L.g[L.v[texel(iz + dz, alpha_column(a))] & 15];
+        float tt = 0.6f - dot3(x, y, z, x, y, z);
+        if (tt < 0.f) return 0.f;
+        tt = tt * tt;
+        return (tt * tt) * dot3(g[0], g[1], g[2], x, y, z);
+    };
+
+    const float n0 = corner(0, 0, 0, x0, y0, z0);
+    const float x1 = (x0 - (float)o1x) + G3, y1 = (y0 - (float)o1y) + G3, z1 = (z0 - (float)o1z) + G3;
+    const float n1 = corner(o1x, o1y, o1z, x1, y1, z1);
+    const float x2 = (x0 - (float)o2x) + c2, y2 = (y0 - (float)o2y) + c2, z2 = (z0 - (float)o2z) + c2;
+    const float n2 = corner(o2x, o2y, o2z, x2, y2, z2);
+    const float x3 = x0 - c3, y3 = y0 - c3, z3 = z0 - c3;
+    const float n3 = corner(1, 1, 1, x3, y3, z3);
+    return 32.f * (((n0 + n1) + n2) + n3);
+}
+
+// ---------------------------------------------------------------------------
+// Fractals and density: noise.cl:8-81, 205-268
+// ---------------------------------------------------------------------------
+
+// BasicFractal (noise.cl:8-36); NOISE_SCALE == 1
+float basic_fractal(int octaves, float frequency, float lacunarity, float persistence, float x, float y,
+                    const PermLut& L) {
+    float px = x * 1.f, py = y * 1.f;
+    float noise = 0.f, amplitude = 1.f;
+    px = px * frequency;
+    py = py * frequency;
+    for (int i = 0; i < octaves; i++) {
+        noise = std::fmaf(snoise2(px, py, L), amplitude, noise);
+        px = px * lacunarity;
+        py = py * lacunarity;
+        amplitude = amplitude * persistence;
+    }
+    return noise;
+}
+
+// 3D analogue of BasicFractal for the cave term of the caves density mode
+float basic_fractal3(int octaves, float frequency, float lacunarity, float persistence, float x, float y,
+                     float z, const PermLut& L) {
+    float px = x * frequency, py = y * frequency, pz = z * frequency;
+    float noise = 0.f, amplitude = 1.f;
+    for (int i = 0; i < octaves; i++) {
+        noise = std::fmaf(snoise3(px, py, pz, L), amplitude, noise);
+        px = px * lacunarity;
+        py = py * lacunarity;
+        pz = pz * lacunarity;
+        amplitude = amplitude * persistence;
+    }
+    return noise;
+}
+
+// RidgedMultiFractal (noise.cl:42-81) with RIDGED_MULTI_H == 1
+float ridged_multi_fractal(int octaves, float lacunarity, float gain, float offset, float x, float y,
+                           const PermLut& L) {
+    float px = x * 1.f, py = y * 1.f;
+    float signal = snoise2(px, py, L);
+    signal = std::fabs(signal);
+    signal = offset - signal;
+    signal = signal * signal;
+    float noise = signal;
+    float weight = 1.f;
+    float frequency = 1.f;
+    for (int i = 0; i < octaves; i++) {
+        px = px * lacunarity;
+        py = py * lacunarity;
+        weight = signal * gain;
+        weight = std::min(std::max(weight, 0.f), 1.f);
+        signal = snoise2(px, py, L);
+        signal = std::fabs(signal);
+        signal = offset - signal;
+        signal = signal * weight;
+        const float exponent = 1.f / frequency;
+        frequency = frequency * lacunarity;
+        noise = std::fmaf(signal, exponent, noise);
+    }
+    noise = noise * (1.f / (float)octaves);
+    return noise;
+}
+
+// Terrain (noise.cl:205-223)
+float terrain(float x, float z, const PermLut& L) {
+    const float px = x * (1.f / 2000.f);
+    const float pz = z * (1.f / 2000.f);
+    float ridged = 0.8f * ridged_multi_fractal(7, 2.114352f, 1.5241f, 1.f, px, pz, L);
+    ridged = std::min(std::max(ridged, 0.f), 1.f);
+    float billow = 0.6f * basic_fractal(4, 0.24f, 1.8754f, 0.433f, -4.33f * px, 7.98f * pz, L);
+    billow = std::fmaf(0.5f, billow, 0.5f);
+    float b2 = 0.6f * basic_fractal(2, 0.63f, 2.2f, 0.15f, px, pz, L);
+    b2 = std::fmaf(b2, 0.5f, 0.5f);
+    return std::fmaf(billow, ridged, b2);
+}
+
+// DensityFunc (noise.cl:225-268) and the two heightfield modes
+float density(const orc_density& d, float x, float y, float z, const PermLut& L) {
+    switch (d.mode) {
+        case 0:
+            return std::fmaf(-900.f, terrain(x, z, L), y);  // MAX_TERRAIN_HEIGHT = 900
+        case 1: {
+            const float h = basic_fractal(d.octaves2, d.freq2, d.lacunarity2, d.gain2, x, z, L);
+            return std::fmaf(-d.amp2, h, y);
+        }
+        default: {
+            const float h = basic_fractal(d.octaves2, d.freq2, d.lacunarity2, d.gain2, x, z, L);
+            const float base = std::fmaf(-d.amp2, h, y);
+            const float c = basic_fractal3(d.octaves3, d.freq3, d.lacunarity3, d.gain3, x, y, z, L);
+            return std::fmaf(d.amp3, c, base);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Chunk geometry (compute.cpp:245-282)
+// ---------------------------------------------------------------------------
+
+struct Dims {
+    int vpc;      // VOXELS_PER_CHUNK
+    int hdim;     // HERMITE_INDEX_SIZE = vpc + 1
+    int fdim;     // FIELD_DIM = vpc + 2
+    int shift;    // VOXEL_INDEX_SHIFT = log2(vpc) + 1
+    int mask;     // VOXEL_INDEX_MASK
+    int depth;    // MAX_OCTREE_DEPTH = log2(vpc)
+    explicit Dims(int v) : vpc(v), hdim(v + 1), fdim(v + 2) {
+        int l = 0;
+        while ((1 << l) < v) l++;
+        depth = l;
+        shift = l + 1;
+        mask = (1 << shift) - 1;
+    }
+    int field_index(int x, int y, int z) const { return x + y * fdim + z * fdim * fdim; }
+    int field_size() const { return fdim * fdim * fdim; }
+};
+
+const int kChildMinOffsets[8][3] = {{0, 0, 0}, {0, 0, 1}, {0, 1, 0}, {0, 1, 1},
+                                    {1, 0, 0}, {1, 0, 1}, {1, 1, 0}, {1, 1, 1}};  // shared_constants.cl:11-22
+const int kEdgeMap[12][2] = {{0, 4}, {1, 5}, {2, 6}, {3, 7}, {0, 2}, {1, 3},
+                             {4, 6}, {5, 7}, {0, 1}, {2, 3}, {4, 5}, {6, 7}};  // shared_constants.cl:4-9
+const int kEdgeNodeOffsets[3][4][3] = {  // octree.cl:376-381
+    {{0, 0, 0}, {0, 0, 1}, {0, 1, 0}, {0, 1, 1}},
+    {{0, 0, 0}, {1, 0, 0}, {0, 0, 1}, {1, 0, 1}},
+    {{0, 0, 0}, {0, 1, 0}, {1, 0, 0}, {1, 1, 0}}};
+const int kAxisOffset[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+
+struct F4 {
+    float x, y, z, w;
+};
+
+// ---------------------------------------------------------------------------
+// FindNextPrime: primes.cpp:9-58
+// ---------------------------------------------------------------------------
+
+bool is_prime(int x) {
+    int o = 4;
+    int i = 5;
+    while (true) {
+        const int q = x / i;
+        if (q < i) return true;
+        if (x == q * i) return false;
+        o ^= 6;
+        i += o;
+    }
+}
+
+int find_next_prime(int n) {
+    if (n <= 2) return 2;
+    if (n == 3) return 3;
+    if (n <= 5) return 5;
+    const int k = n / 6;
+    int i = n - 6 * k;
+    const int o = i < 2 ? 1 : 5;
+    int x = 6 * k + o;
+    for (i = (3 + o) / 2; !is_prime(x); x += i) i ^= 6;
+    return x;
+}
+
+// ---------------------------------------------------------------------------
+// Cuckoo hash: cuckoo.cl:1-105, compute_cuckoo.cpp:46-139, compute_cuckoo.h:6-10
+// ---------------------------------------------------------------------------
+
+constexpr uint64_t CUCKOO_EMPTY = ~0ull;
+constexpr int CUCKOO_STASH_HASH_INDEX = 4;
+constexpr int CUCKOO_HASH_FN_COUNT = 5;
+constexpr int CUCKOO_STASH_SIZE = 101;
+constexpr int CUCKOO_MAX_ITERATIONS = 32;
+constexpr uint32_t CUCKOO_MIN_TABLE_SIZE = 2048u;
+
+// Cuckoo_Hash (cuckoo.cl:18-24): the product a*key wraps at 32 bits
+inline uint32_t cuckoo_hash(int which, uint32_t key, uint32_t a, uint32_t b, uint32_t prime) {
+    const uint64_t p = 4294967291ull;
+    const uint64_t h = (uint32_t)(a * key);
+    const uint64_t mod = which < CUCKOO_STASH_HASH_INDEX ? prime : (uint64_t)CUCKOO_STASH_SIZE;
+    return (uint32_t)(((h + b) % p) % mod);
+}
+
+struct Cuckoo {
+    uint32_t prime = 0;
+    std::vector<uint64_t> table;
+    uint64_t stash[CUCKOO_STASH_SIZE];
+    uint32_t params[CUCKOO_HASH_FN_COUNT * 2];
+    bool stash_used = false;
+
+    // one pass of Cuckoo_InsertKeys (cuckoo.cl:26-71) executed key by key;
+    // the stash slot is the stash hash mod STASH_SIZE (the reference passes
+    // whichHash 0 there, which indexes the 101-entry stash modulo the table
+    // prime -- an out-of-bounds write; the intent is restated).
+    bool insert_all(const uint32_t* keys, int n, bool* used_stash) {
+        bool ok = true;
+        *used_stash = false;
+        for (int index = 0; index < n; index++) {
+            uint32_t key = keys[index];
+            uint64_t entry = ((uint64_t)(uint32_t)index << 32) | key;
+            uint32_t h = cuckoo_hash(0, key, params[0], params[1], prime);
+            bool done = false;
+            for (int i = 0; i < CUCKOO_MAX_ITERATIONS; i++) {
+                std::swap(table[h], entry);
+                if (entry == CUCKOO_EMPTY) { done = true; break; }
+                key = (uint32_t)(entry & 0xffffffffu);
+                const uint32_t h0 = cuckoo_hash(0, key, params[0], params[1], prime);
+                const uint32_t h1 = cuckoo_hash(1, key, params[2], params[3], prime);
+                const uint32_t h2 = cuckoo_hash(2, key, params[4], params[5], prime);
+                const uint32_t h3 = cuckoo_hash(3, key, params[6], params[7], prime);
+                if (h == h0) h = h1;
+                else if (h == h1) h = h2;
+                else if (h == h2) h = h3;
+                else if (h == h3) h = h0;
+            }
+            if (done) continue;
+            *used_stash = true;
+            key = (uint32_t)(entry & 0xffffffffu);
+            const uint32_t hs = cuckoo_hash(CUCKOO_STASH_HASH_INDEX, key, params[8], params[9], prime);
+            if (stash[hs] == CUCKOO_EMPTY) stash[hs] = entry;
+            else ok = false;
+        }
+        return ok;
+    }
+
+    // Cuckoo_Find (cuckoo.cl:73-104) with the stash probe reading the stash
+    // (the reference reads data[h] there).
+    uint32_t find(uint32_t key) const {
+        for (int i = 0; i < CUCKOO_STASH_HASH_INDEX; i++) {
+            const uint32_t h = cuckoo_hash(i, key, params[2 * i], params[2 * i + 1], prime);
+            const uint64_t e = table[h];
+            if ((uint32_t)(e & 0xffffffffu) == key) return (uint32_t)(e >> 32);
+        }
+        if (stash_used) {
+            const uint32_t h = cuckoo_hash(CUCKOO_STASH_HASH_INDEX, key, params[8], params[9], prime);
+            const uint64_t e = stash[h];
+            if ((uint32_t)(e & 0xffffffffu) == key) return (uint32_t)(e >> 32);
+        }
+        return ~0u;
+    }
+};
+
+// Cuckoo_InitialiseTable + Cuckoo_InsertKeys host loop (compute_cuckoo.cpp:49-139):
+// a fresh parameter set is drawn until every key inserts.
+void cuckoo_build(Cuckoo* c, const uint32_t* keys, int n, std::mt19937& gen, int* retries) {
+    std::uniform_int_distribution<uint32_t> dist(1u << 15, 1u << 30);
+    c->prime = (uint32_t)find_next_prime((int)std::max(CUCKOO_MIN_TABLE_SIZE, (uint32_t)n * 2u));
+    int attempts = 0;
+    for (;;) {
+        for (int i = 0; i < CUCKOO_HASH_FN_COUNT * 2; i++) c->params[i] = dist(gen);
+        c->table.assign(c->prime, CUCKOO_EMPTY);
+        for (int i = 0; i < CUCKOO_STASH_SIZE; i++) c->stash[i] = CUCKOO_EMPTY;
+        bool used = false;
+        const bool ok = c->insert_all(keys, n, &used);
+        if (ok) {
+            c->stash_used = used;
+            break;
+        }
+        attempts++;
+    }
+    if (retries) *retries = attempts;
+}
+
+// ---------------------------------------------------------------------------
+// RemoveDuplicates: compute.cpp:450-543, duplicate.cl:4-114
+// ---------------------------------------------------------------------------
+
+// MurmurHash (duplicate.cl:4-28); the seed argument is unused by the reference
+inline uint32_t murmur(uint32_t value) {
+    const uint32_t c1 = 0xcc9e2d51u, c2 = 0x1b873593u;
+    uint32_t hash = value;
+    hash *= c1;
+    hash = (hash << 15) | (hash >> 17);
+    hash *= c2;
+    hash ^= value;
+    hash = ((hash << 13) | (hash >> 19)) * 5u + 0xe6546b64u;
+    hash ^= (hash >> 16);
+    hash *= 0x85ebca6bu;
+    hash ^= (hash >> 13);
+    hash *= 0xc2b2ae35u;
+    hash ^= (hash >> 16);
+    return hash;
+}
+
+// The reference's racy `table[hash] = id` (MapSequenceIndices) is restated
+// as a sequential loop, i.e. the highest sequence index wins a slot.
+std::vector<int32_t> remove_duplicates(const std::vector<int32_t>& input) {
+    std::vector<int32_t> result;
+    const int n0 = (int)input.size();
+    if (n0 == 0) return result;
+    const uint32_t prime = (uint32_t)find_next_prime(n0 * 2);
+    std::vector<int32_t> table(prime);
+    std::vector<int32_t> sequence = input;
+    while (!sequence.empty()) {
+        std::fill(table.begin(), table.end(), -1);
+        for (int id = 0; id < (int)sequence.size(); id++) table[murmur((uint32_t)sequence[id]) % prime] = id;
+        std::vector<int32_t> winners;
+        for (uint32_t s = 0; s < prime; s++)
+            if (table[s] != -1) winners.push_back(sequence[table[s]]);
+        result.insert(result.end(), winners.begin(), winners.end());
+        for (int32_t w : winners) table[murmur((uint32_t)w) % prime] = w;
+        std::vector<int32_t> losers;
+        for (int32_t v : sequence)
+            if (table[murmur((uint32_t)v) % prime] != v) losers.push_back(v);
+        if (losers.empty()) break;
+        sequence.swap(losers);
+    }
+    return result;
+}
+
+// ---------------------------------------------------------------------------
+// CSG brushes: apply_csg_operation.cl:42-175, hg_sdf.glsl fBox / pR
+// ---------------------------------------------------------------------------
+
+struct Brush {
+    orc_csg_op op;
+    float c, s;  // cos / sin of rotate_y, evaluated once in double on the host
+};
+
+inline float length3(float x, float y, float z) { return std::sqrt(dot3(x, y, z, x, y, z)); }
+
+// Density_Cuboid (apply_csg_operation.cl:49-68): pR rotation then fBox
+float density_cuboid(float wx, float wy, float wz, const Brush& b) {
+    const float lx = wx - b.op.origin[0], ly = wy - b.op.origin[1], lz = wz - b.op.origin[2];
+    // pR(p.xz, a): p = cos(a)*p + sin(a)*(p.y, -p.x)   (hg_sdf.glsl:460-463)
+    const float rx = std::fmaf(b.s, lz, b.c * lx);
+    const float rz = std::fmaf(b.s, -lx, b.c * lz);
+    // fBox (hg_sdf.glsl:218-221)
+    const float dx = std::fabs(rx) - b.op.dimensions[0];
+    const float dy = std::fabs(ly) - b.op.dimensions[1];
+    const float dz = std::fabs(rz) - b.op.dimensions[2];
+    const float outside = length3(std::max(dx, 0.f), std::max(dy, 0.f), std::max(dz, 0.f));
+    const float inside = std::max(std::max(std::min(dx, 0.f), std::min(dy, 0.f)), std::min(dz, 0.f));
+    return outside + inside;
+}
+
+// Density_Sphere (apply_csg_operation.cl:42-45)
+float density_sphere(float wx, float wy, float wz, const Brush& b) {
+    return length3(wx - b.op.origin[0], wy - b.op.origin[1], wz - b.op.origin[2]) - b.op.dimensions[0];
+}
+
+// BrushDensity (apply_csg_operation.cl:72-81)
+inline float brush_density(float x, float y, float z, const Brush& b) {
+    return b.op.brush == 0 ? density_cuboid(x, y, z, b) : density_sphere(x, y, z, b);
+}
+
+// BrushMaterial (apply_csg_operation.cl:114-140)
+int brush_material(float x, float y, float z, const std::vector<Brush>& ops, int material) {
+    int m = material;
+    for (const Brush& b : ops)
+        if (brush_density(x, y, z, b) <= 0.f) m = b.op.type == 0 ? b.op.material : MATERIAL_AIR;
+    return m;
+}
+
+inline void normalize3(float& x, float& y, float& z) {
+    const float len = std::sqrt(dot3(x, y, z, x, y, z));
+    if (len == 0.f) { x = y = z = 0.f; return; }
+    x = x / len;
+    y = y / len;
+    z = z / len;
+}
+
+// BrushZeroCrossing (apply_csg_operation.cl:86-110)
+float brush_zero_crossing(const F4& p0, const F4& p1, const std::vector<Brush>& ops) {
+    float min_density = FLT_MAX;
+    float crossing = 0.f;
+    for (float t = 0.f; t <= 1.f; t += (1.f / 16.f)) {
+        const float px = std::fmaf(p1.x - p0.x, t, p0.x);
+        const float py = std::fmaf(p1.y - p0.y, t, p0.y);
+        const float pz = std::fmaf(p1.z - p0.z, t, p0.z);
+        for (const Brush& b : ops) {
+            const float d = std::fabs(brush_density(px, py, pz, b));
+            if (d < min_density) { crossing = t; min_density = d; }
+        }
+    }
+    return crossing;
+}
+
+// BrushNormal (apply_csg_operation.cl:144-175)
+void brush_normal(float px, float py, float pz, const std::vector<Brush>& ops, float n[3]) {
+    n[0] = n[1] = n[2] = 0.f;
+    const float h = 0.001f;
+    for (const Brush& b : ops) {
+        if (brush_density(px, py, pz, b) > 0.f) continue;
+        float gx = brush_density(px + h, py, pz, b) - brush_density(px - h, py, pz, b);
+        float gy = brush_density(px, py + h, pz, b) - brush_density(px, py - h, pz, b);
+        float gz = brush_density(px, py, pz + h, b) - brush_density(px, py, pz - h, b);
+        normalize3(gx, gy, gz);
+        const float flip = b.op.type == 0 ? 1.f : -1.f;
+        n[0] = flip * gx;
+        n[1] = flip * gy;
+        n[2] = flip * gz;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// QEF: qef.cl:1-305
+// ---------------------------------------------------------------------------
+
+struct QEF {
+    float ata[6];
+    float pad[2];
+    F4 atb;
+    F4 masspoint;
+};
+static_assert(sizeof(QEF) == 64, "QEFData layout (qef.cl:7-14): 8 floats + 2 float4");
+
+inline float dot4(const F4& a, const F4& b) {
+    return std::fmaf(a.w, b.w, std::fmaf(a.z, b.z, std::fmaf(a.y, b.y, a.x * b.x)));
+}
+
+// qef_add_point (qef.cl:170-191)
+void qef_add_point(QEF& q, const F4& n, const F4& p) {
+    q.ata[0] += n.x * n.x;
+    q.ata[1] += n.x * n.y;
+    q.ata[2] += n.x * n.z;
+    q.ata[3] += n.y * n.y;
+    q.ata[4] += n.y * n.z;
+    q.ata[5] += n.z * n.z;
+    const float b = dot4(p, n);
+    q.atb.x += n.x * b;
+    q.atb.y += n.y * b;
+    q.atb.z += n.z * b;
+    q.masspoint.x += p.x;
+    q.masspoint.y += p.y;
+    q.masspoint.z += p.z;
+    q.masspoint.w += 1.f;
+}
+
+typedef float Mat3[3][3];
+
+// givens_coeffs_sym (qef.cl:31-42)
+void givens_coeffs_sym(float a_pp, float a_pq, float a_qq, float* c, float* s) {
+    if (a_pq == 0.f) { *c = 1.f; *s = 0.f; return; }
+    const float tau = (a_qq - a_pp) / (2.f * a_pq);
+    const float stt = std::sqrt(std::fmaf(tau, tau, 1.f));
+    const float tn = 1.f / ((tau >= 0.f) ? (tau + stt) : (tau - stt));
+    *c = 1.f / std::sqrt(std::fmaf(tn, tn, 1.f));
+    *s = tn * (*c);
+}
+
+inline void svd_rotate_xy(float& x, float& y, float c, float s) {
+    const float u = x, v = y;
+    x = c * u - s * v;
+    y = s * u + c * v;
+}
+
+inline void svd_rotateq_xy(float& x, float& y, float a, float c, float s) {
+    const float cc = c * c, ss = s * s;
+    const float mx = 2.f * c * s * a;
+    const float u = x, v = y;
+    x = cc * u - mx + ss * v;
+    y = ss * u + mx + cc * v;
+}
+
+// svd_rotate (qef.cl:58-86)
+void svd_rotate(Mat3 vtav, Mat3 v, int a, int b) {
+    if (vtav[a][b] == 0.f) return;
+    float c, s;
+    givens_coeffs_sym(vtav[a][a], vtav[a][b], vtav[b][b], &c, &s);
+    float x = vtav[a][a], y = vtav[b][b];
+    svd_rotateq_xy(x, y, vtav[a][b], c, s);
+    vtav[a][a] = x;
+    vtav[b][b] = y;
+    x = vtav[0][3 - b];
+    y = vtav[1 - a][2];
+    svd_rotate_xy(x, y, c, s);
+    vtav[0][3 - b] = x;
+    vtav[1 - a][2] = y;
+    vtav[a][b] = 0.f;
+    for (int r = 0; r < 3; r++) {
+        x = v[r][a];
+        y = v[r][b];
+        svd_rotate_xy(x, y, c, s);
+        v[r][a] = x;
+        v[r][b] = y;
+    }
+}
+
+inline float svd_invdet(float x, float tol) {
+    return (std::fabs(x) < tol || std::fabs(1.f / x) < tol) ? 0.f : (1.f / x);
+}
+
+// qef_solve (qef.cl:239-256) via svd_solve_ATA_ATb (qef.cl:127-144), 10 sweeps
+F4 qef_solve(QEF q) {
+    const float w = std::max(q.masspoint.w, 1.f);
+    q.masspoint.x /= w;
+    q.masspoint.y /= w;
+    q.masspoint.z /= w;
+    q.masspoint.w /= w;
+    const float* A = q.ata;
+    const F4 mp = q.masspoint;
+    // svd_vmul_sym (qef.cl:146-152)
+    F4 amp;
+    amp.x = dot4(F4{A[0], A[1], A[2], 0.f}, mp);
+    amp.y = A[1] * mp.x + A[3] * mp.y + A[4] * mp.z;
+    amp.z = A[2] * mp.x + A[4] * mp.y + A[5] * mp.z;
+    amp.w = 0.f;
+    amp.x = q.atb.x - amp.x;
+    amp.y = q.atb.y - amp.y;
+    amp.z = q.atb.z - amp.z;
+    amp.w = q.atb.w - amp.w;
+
+    Mat3 V = {{1.f, 0.f, 0.f}, {0.f, 1.f, 0.f}, {0.f, 0.f, 1.f}};
+    Mat3 vtav = {{A[0], A[1], A[2]}, {0.f, A[3], A[4]}, {0.f, 0.f, A[5]}};
+    for (int i = 0; i < 10; i++) {
+        svd_rotate(vtav, V, 0, 1);
+        svd_rotate(vtav, V, 0, 2);
+        svd_rotate(vtav, V, 1, 2);
+    }
+    const float d0 = svd_invdet(vtav[0][0], 0.1f);
+    const float d1 = svd_invdet(vtav[1][1], 0.1f);
+    const float d2 = svd_invdet(vtav[2][2], 0.1f);
+    Mat3 o;
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++)
+            o[r][c] = V[r][0] * d0 * V[c][0] + V[r][1] * d1 * V[c][1] + V[r][2] * d2 * V[c][2];
+    F4 x;
+    x.x = dot4(F4{o[0][0], o[0][1], o[0][2], 0.f}, amp);
+    x.y = dot4(F4{o[1][0], o[1][1], o[1][2], 0.f}, amp);
+    x.z = dot4(F4{o[2][0], o[2][1], o[2][2], 0.f}, amp);
+    x.w = 0.f;
+    x.x += mp.x;
+    x.y += mp.y;
+    x.z += mp.z;
+    x.w += mp.w;
+    return x;
+}
+
+// ---------------------------------------------------------------------------
+// Octree codes: octree.cl:3-72
+// ---------------------------------------------------------------------------
+
+uint32_t code_for_position(int x, int y, int z, int depth_max) {
+    uint32_t code = 1;
+    for (int depth = depth_max - 1; depth >= 0; depth--) {
+        const uint32_t c = (uint32_t)((((x >> depth) & 1) << 2) | (((y >> depth) & 1) << 1) | ((z >> depth) & 1));
+        code = (code << 3) | c;
+    }
+    return code;
+}
+
+void position_for_code(uint32_t code, int depth_max, int p[3]) {
+    int msb = 0;
+    for (uint32_t c = code; c; c >>= 1) msb++;
+    const int node_depth = msb / 3;
+    p[0] = p[1] = p[2] = 0;
+    for (int i = depth_max - node_depth; i < depth_max; i++) {
+        const uint32_t c = code & 7u;
+        code >>= 3;
+        p[0] |= (int)((c >> 2) & 1u) << i;
+        p[1] |= (int)((c >> 1) & 1u) << i;
+        p[2] |= (int)(c & 1u) << i;
+    }
+}
+
+// FindDominantMaterial (octree.cl:96-138)
+int dominant_material(const int m[8]) {
+    int data[8];
+    for (int i = 0; i < 8; i++) data[i] = m[i];
+    for (int i = 1; i < 8; i++) {
+        const int tmp = data[i];
+        int j = i;
+        for (; j >= 1 && tmp < data[j - 1]; j--) data[j] = data[j - 1];
+        data[j] = tmp;
+    }
+    int current = data[0], count = 1, max_count = 0, max_material = 0;
+    for (int i = 1; i < 8; i++) {
+        const int v = data[i];
+        if (v == MATERIAL_AIR || v == MATERIAL_NONE) continue;
+        if (current != v) {
+            if (count > max_count) { max_count = count; max_material = current; }
+            current = v;
+            count = 1;
+        } else {
+            count++;
+        }
+    }
+    if (count > max_count) max_material = current;
+    return max_material;
+}
+
+// ColourForMinLeafSize (clipmap.cpp:329-353)
+void colour_for_min_leaf_size(int s, float c[3]) {
+    switch (s) {
+        case 1: c[0] = 0.3f; c[1] = 0.1f; c[2] = 0.f; break;
+        case 2: c[0] = 0.f; c[1] = 0.f; c[2] = 0.5f; break;
+        case 4: c[0] = 0.f; c[1] = 0.5f; c[2] = 0.5f; break;
+        case 8: c[0] = 0.5f; c[1] = 0.f; c[2] = 0.5f; break;
+        case 16: c[0] = 0.f; c[1] = 0.5f; c[2] = 0.f; break;
+        default: c[0] = 0.5f; c[1] = 0.f; c[2] = 0.f; break;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The per-chunk pipeline
+// ---------------------------------------------------------------------------
+
+struct Chunk {
+    std::vector<int32_t> materials;
+    std::vector<int32_t> plain_edge_keys;
+    std::vector<int32_t> edge_keys;
+    std::vector<F4> edge_info;
+    std::vector<int32_t> created_keys;
+    std::vector<uint32_t> node_codes;
+    std::vector<int32_t> node_edges;
+    std::vector<int32_t> node_materials;
+    std::vector<QEF> qefs;
+    std::vector<F4> positions, normals;
+    std::vector<int32_t> triangles;  // 3 ints per triangle
+    std::vector<float> vertices;     // 12 floats per MeshVertex
+    std::vector<int32_t> seams;      // 12 x 4-byte words per SeamNodeInfo
+    int mesh_vertex_count = 0;
+};
+
+inline int edge_key(const Dims& D, int x, int y, int z, int axis) {
+    return ((x | (y << D.shift) | (z << (2 * D.shift))) << 2) | axis;
+}
+inline void decode_edge(const Dims& D, int key, int p[3], int* axis) {
+    *axis = key & 3;
+    const int h = key >> 2;
+    p[0] = h & D.mask;
+    p[1] = (h >> D.shift) & D.mask;
+    p[2] = (h >> (2 * D.shift)) & D.mask;
+}
+
+// FindEdgeIntersectionInfo (density_field.cl:96-151); crossing_mode 1
+// replaces the 17-sample search by linear interpolation of the end densities.
+F4 edge_info_density(const Dims& D, const orc_density& dn, const PermLut& L, int key, const int off[3],
+                     int scale, int crossing_mode) {
+    int lp[3], axis;
+    decode_edge(D, key, lp, &axis);
+    const int wx = scale * lp[0] + off[0], wy = scale * lp[1] + off[1], wz = scale * lp[2] + off[2];
+    const F4 p0{(float)wx, (float)wy, (float)wz, 0.f};
+    const F4 p1{(float)(wx + scale * kAxisOffset[axis][0]), (float)(wy + scale * kAxisOffset[axis][1]),
+                (float)(wz + scale * kAxisOffset[axis][2]), 0.f};
+    float t = 0.f;
+    if (crossing_mode == 0) {
+        float min_value = FLT_MAX;
+        float current = 0.f;
+        for (int i = 0; i <= 16; i++) {
+            const float px = std::fmaf(p1.x - p0.x, current, p0.x);
+            const float py = std::fmaf(p1.y - p0.y, current, p0.y);
+            const float pz = std::fmaf(p1.z - p0.z, current, p0.z);
+            const float d = std::fabs(density(dn, px, py, pz, L));
+            if (d < min_value) { t = current; min_value = d; }
+            current += 0.0625f;
+        }
+    } else {
+        const float d0 = density(dn, p0.x, p0.y, p0.z, L);
+        const float d1 = density(dn, p1.x, p1.y, p1.z, L);
+        const float den = d0 - d1;
+        t = den != 0.f ? d0 / den : 0.5f;
+        t = std::min(std::max(t, 0.f), 1.f);
+    }
+    const float px = std::fmaf(p1.x - p0.x, t, p0.x);
+    const float py = std::fmaf(p1.y - p0.y, t, p0.y);
+    const float pz = std::fmaf(p1.z - p0.z, t, p0.z);
+    const float h = 0.001f;
+    float nx = density(dn, px + h, py, pz, L) - density(dn, px - h, py, pz, L);
+    float ny = density(dn, px, py + h, pz, L) - density(dn, px, py - h, pz, L);
+    float nz = density(dn, px, py, pz + h, L) - density(dn, px, py, pz - h, L);
+    normalize3(nx, ny, nz);
+    return F4{nx, ny, nz, t};
+}
+
+// CSG FindEdgeIntersectionInfo (apply_csg_operation.cl:443-477)
+F4 edge_info_brush(const Dims& D, int key, const int off[3], int scale, const std::vector<Brush>& ops) {
+    int lp[3], axis;
+    decode_edge(D, key, lp, &axis);
+    const int wx = scale * lp[0] + off[0], wy = scale * lp[1] + off[1], wz = scale * lp[2] + off[2];
+    const F4 p0{(float)wx, (float)wy, (float)wz, 0.f};
+    const F4 p1{(float)(wx + scale * kAxisOffset[axis][0]), (float)(wy + scale * kAxisOffset[axis][1]),
+                (float)(wz + scale * kAxisOffset[axis][2]), 0.f};
+    const float t = brush_zero_crossing(p0, p1, ops);
+    const float px = std::fmaf(p1.x - p0.x, t, p0.x);
+    const float py = std::fmaf(p1.y - p0.y, t, p0.y);
+    const float pz = std::fmaf(p1.z - p0.z, t, p0.z);
+    float n[3];
+    brush_normal(px, py, pz, ops, n);
+    return F4{n[0], n[1], n[2], t};
+}
+
+std::vector<Brush> make_brushes(const orc_csg_op* ops, int n) {
+    std::vector<Brush> out;
+    for (int i = 0; i < n; i++) {
+        Brush b;
+        b.op = ops[i];
+        b.c = (float)std::cos((double)ops[i].rotate_y);
+        b.s = (float)std::sin((double)ops[i].rotate_y);
+        out.push_back(b);
+    }
+    return out;
+}
+
+// ApplyCSGOperations (compute_csg.cpp:11-219)
+void apply_csg(const Dims& D, Chunk& ch, const std::vector<Brush>& ops, const int off[3], int scale) {
+    if (ops.empty()) return;
+    const int F = D.field_size();
+    // CSG_HermiteIndices + scan + CompactPoints + UpdateFieldMaterials
+    std::vector<int> updated_points;  // field linear indices, ascending
+    std::vector<int32_t> new_materials = ch.materials;
+    for (int z = 0; z < D.fdim; z++)
+        for (int y = 0; y < D.fdim; y++)
+            for (int x = 0; x < D.fdim; x++) {
+                const int idx = D.field_index(x, y, z);
+                const int old = ch.materials[idx];
+                const int m = brush_material((float)(off[0] + scale * x), (float)(off[1] + scale * y),
+                                             (float)(off[2] + scale * z), ops, old);
+                if (m != old) {
+                    updated_points.push_back(idx);
+                    new_materials[idx] = m;
+                }
+            }
+    if (updated_points.empty()) return;
+    ch.materials = new_materials;
+
+    // FindUpdatedEdges + RemoveInvalidIndices + CompactIndexArray
+    std::vector<int32_t> generated;
+    for (int idx : updated_points) {
+        const int x = idx % D.fdim, y = (idx / D.fdim) % D.fdim, z = idx / (D.fdim * D.fdim);
+        const int base = (x | (y << D.shift) | (z << (2 * D.shift))) << 2;
+        generated.push_back(base | 0);
+        generated.push_back(base | 1);
+        generated.push_back(base | 2);
+        if (x > 0) generated.push_back(edge_key(D, x - 1, y, z, 0));
+        if (y > 0) generated.push_back(edge_key(D, x, y - 1, z, 1));
+        if (z > 0) generated.push_back(edge_key(D, x, y, z - 1, 2));
+    }
+    const std::vector<int32_t> invalidated = remove_duplicates(generated);
+
+    // FilterValidEdges (with the PARANOID guard, apply_csg_operation.cl:363-365)
+    std::vector<int32_t> created;
+    for (int32_t e : invalidated) {
+        int p[3], axis;
+        decode_edge(D, e, p, &axis);
+        const int i0 = D.field_index(p[0], p[1], p[2]);
+        const int i1 = D.field_index(p[0] + kAxisOffset[axis][0], p[1] + kAxisOffset[axis][1],
+                                     p[2] + kAxisOffset[axis][2]);
+        const int m0 = i0 < F ? ch.materials[i0] : MATERIAL_AIR;
+        const int m1 = i1 < F ? ch.materials[i1] : MATERIAL_AIR;
+        const bool sign_change = (m0 == MATERIAL_AIR && m1 != MATERIAL_AIR) || (m1 == MATERIAL_AIR && m0 != MATERIAL_AIR);
+        if (sign_change && e != -1) created.push_back(e);
+    }
+
+    // PruneFieldEdges + CompactFieldEdges.  When every field edge is pruned
+    // the reference keeps the unpruned list (compute_csg.cpp:156); the
+    // restatement replaces it by the empty list.
+    if (!invalidated.empty() && !ch.edge_keys.empty()) {
+        std::unordered_set<int32_t> inv(invalidated.begin(), invalidated.end());
+        std::vector<int32_t> keys;
+        std::vector<F4> info;
+        for (size_t i = 0; i < ch.edge_keys.size(); i++) {
+            if (inv.count(ch.edge_keys[i])) continue;
+            keys.push_back(ch.edge_keys[i]);
+            info.push_back(ch.edge_info[i]);
+        }
+        ch.edge_keys.swap(keys);
+        ch.edge_info.swap(info);
+    }
+
+    // CSG FindEdgeIntersectionInfo for the created edges, appended
+    for (int32_t e : created) {
+        ch.edge_keys.push_back(e);
+        ch.edge_info.push_back(edge_info_brush(D, e, off, scale, ops));
+    }
+    ch.created_keys.insert(ch.created_keys.end(), created.begin(), created.end());
+}
+
+int run_chunk(Chunk& ch, const orc_density& dn, const orc_chunk_args& a, const PermLut& L) {
+    const Dims D(a.voxels_per_chunk);
+    ch = Chunk();
+    const int scale = a.size / (D.vpc * LEAF_SIZE_SCALE);
+    if (scale <= 0) return -1;
+    const int off[3] = {a.min[0] / LEAF_SIZE_SCALE, a.min[1] / LEAF_SIZE_SCALE, a.min[2] / LEAF_SIZE_SCALE};
+
+    // GenerateDefaultField (density_field.cl:11-37)
+    const int F = D.field_size();
+    ch.materials.assign(F, 0);
+    for (int z = 0; z < D.fdim; z++)
+        for (int y = 0; y < D.fdim; y++)
+            for (int x = 0; x < D.fdim; x++) {
+                const float d = density(dn, (float)(x * scale + off[0]), (float)(y * scale + off[1]),
+                                        (float)(z * scale + off[2]), L);
+                ch.materials[D.field_index(x, y, z)] = d < 0.f ? a.default_material : MATERIAL_AIR;
+            }
+
+    // FindFieldEdges + ExclusiveScan + CompactEdges (density_field.cl:41-92)
+    for (int z = 0; z < D.hdim; z++)
+        for (int y = 0; y < D.hdim; y++)
+            for (int x = 0; x < D.hdim; x++) {
+                const int c0 = ch.materials[D.field_index(x, y, z)];
+                for (int i = 0; i < 3; i++) {
+                    const int ce = ch.materials[D.field_index(x + kAxisOffset[i][0], y + kAxisOffset[i][1],
+                                                              z + kAxisOffset[i][2])];
+                    const bool sc = (c0 != MATERIAL_AIR && ce == MATERIAL_AIR) || (c0 == MATERIAL_AIR && ce != MATERIAL_AIR);
+                    if (sc) ch.edge_keys.push_back(edge_key(D, x, y, z, i));
+                }
+            }
+    ch.plain_edge_keys = ch.edge_keys;
+    for (int32_t k : ch.edge_keys) ch.edge_info.push_back(edge_info_density(D, dn, L, k, off, scale, a.crossing_mode));
+
+    // stored CSG operations replayed as one batch (compute_density_field.cpp:255-271)
+    if (a.num_ops > 0) apply_csg(D, ch, make_brushes(a.ops, a.num_ops), off, scale);
+
+    if (ch.edge_keys.empty()) return 0;
+
+    // FindActiveVoxels + CompactVoxels (octree.cl:142-223)
+    for (int z = 0; z < D.vpc; z++)
+        for (int y = 0; y < D.vpc; y++)
+            for (int x = 0; x < D.vpc; x++) {
+                int cm[8];
+                int corners = 0;
+                for (int i = 0; i < 8; i++) {
+                    cm[i] = ch.materials[D.field_index(x + kChildMinOffsets[i][0], y + kChildMinOffsets[i][1],
+                                                       z + kChildMinOffsets[i][2])];
+                    corners |= (cm[i] == MATERIAL_AIR ? 0 : 1) << i;
+                }
+                if (corners == 0 || corners == 255) continue;
+                int edges = 0;
+                for (int i = 0; i < 12; i++) {
+                    const int s0 = (corners >> kEdgeMap[i][0]) & 1, s1 = (corners >> kEdgeMap[i][1]) & 1;
+                    edges |= (s0 != s1 ? 1 : 0) << i;
+                }
+                ch.node_codes.push_back(code_for_position(x, y, z, D.depth));
+                ch.node_edges.push_back(edges);
+                ch.node_materials.push_back((dominant_material(cm) << 8) | corners);
+            }
+    const int V = (int)ch.node_codes.size();
+    if (V == 0) return 0;
+
+    std::mt19937 gen(a.hash_seed);
+
+    // edge hash + CreateLeafNodes (octree.cl:236-312)
+    Cuckoo edge_hash;
+    cuckoo_build(&edge_hash, reinterpret_cast<const uint32_t*>(ch.edge_keys.data()), (int)ch.edge_keys.size(), gen,
+                 nullptr);
+    ch.qefs.resize(V);
+    ch.normals.resize(V);
+    ch.positions.resize(V);
+    for (int v = 0; v < V; v++) {
+        int pos[3];
+        position_for_code(ch.node_codes[v], D.depth, pos);
+        const int edge_list = ch.node_edges[v];
+        F4 ep[12], en[12];
+        int count = 0;
+        for (int i = 0; i < 12; i++) {
+            if (!((edge_list >> i) & 1)) continue;
+            const int e0 = kEdgeMap[i][0], e1 = kEdgeMap[i][1];
+            const F4 p0{(float)pos[0] + (float)kChildMinOffsets[e0][0], (float)pos[1] + (float)kChildMinOffsets[e0][1],
+                        (float)pos[2] + (float)kChildMinOffsets[e0][2], 0.f};
+            const F4 p1{(float)pos[0] + (float)kChildMinOffsets[e1][0], (float)pos[1] + (float)kChildMinOffsets[e1][1],
+                        (float)pos[2] + (float)kChildMinOffsets[e1][2], 0.f};
+            const int axis = i / 4;
+            const int key = edge_key(D, pos[0] + kChildMinOffsets[e0][0], pos[1] + kChildMinOffsets[e0][1],
+                                     pos[2] + kChildMinOffsets[e0][2], axis);
+            const uint32_t di = edge_hash.find((uint32_t)key);
+            if (di == ~0u) continue;
+            const F4 e = ch.edge_info[di];
+            const float fs = (float)scale;
+            ep[count] = F4{fs * std::fmaf(p1.x - p0.x, e.w, p0.x), fs * std::fmaf(p1.y - p0.y, e.w, p0.y),
+                           fs * std::fmaf(p1.z - p0.z, e.w, p0.z), fs * std::fmaf(p1.w - p0.w, e.w, p0.w)};
+            en[count] = F4{e.x, e.y, e.z, 0.f};
+            count++;
+        }
+        // qef_create_from_points (qef.cl:283-303)
+        QEF q;
+        std::memset(&q, 0, sizeof(q));
+        for (int i = 0; i < count; i++) qef_add_point(q, en[i], ep[i]);
+        q.masspoint.x /= q.masspoint.w;
+        q.masspoint.y /= q.masspoint.w;
+        q.masspoint.z /= q.masspoint.w;
+        q.masspoint.w /= q.masspoint.w;
+        ch.qefs[v] = q;
+        F4 n{0.f, 0.f, 0.f, 0.f};
+        for (int i = 0; i < count; i++) {
+            n.x += en[i].x;
+            n.y += en[i].y;
+            n.z += en[i].z;
+            n.w += 1.f;
+        }
+        n.x /= n.w;
+        n.y /= n.w;
+        n.z /= n.w;
+        n.w = 0.f;
+        ch.normals[v] = n;
+        // SolveQEFs (octree.cl:316-331)
+        F4 x = qef_solve(q);
+        x.x = std::fmaf(x.x, (float)LEAF_SIZE_SCALE, (float)a.min[0]);
+        x.y = std::fmaf(x.y, (float)LEAF_SIZE_SCALE, (float)a.min[1]);
+        x.z = std::fmaf(x.z, (float)LEAF_SIZE_SCALE, (float)a.min[2]);
+        x.w = 1.f;
+        ch.positions[v] = x;
+    }
+
+    // node hash (compute_octree.cpp:143-144) + GenerateMesh (octree.cl:385-442)
+    Cuckoo node_hash;
+    cuckoo_build(&node_hash, ch.node_codes.data(), V, gen, nullptr);
+    for (int v = 0; v < V; v++) {
+        int pos[3];
+        position_for_code(ch.node_codes[v], D.depth, pos);
+        for (int axis = 0; axis < 3; axis++) {
+            const int aa = pos[(axis + 1) % 3], bb = pos[(axis + 2) % 3];
+            if (aa == D.vpc - 1 || bb == D.vpc - 1) continue;
+            int idx[4];
+            idx[0] = v;
+            bool all = true;
+            for (int n = 1; n < 4; n++) {
+                const uint32_t c = code_for_position(pos[0] + kEdgeNodeOffsets[axis][n][0],
+                                                     pos[1] + kEdgeNodeOffsets[axis][n][1],
+                                                     pos[2] + kEdgeNodeOffsets[axis][n][2], D.depth);
+                const uint32_t f = node_hash.find(c);
+                idx[n] = (int)f;
+                if (f == ~0u) all = false;
+            }
+            if (!all) continue;
+            // ProcessEdge (octree.cl:335-372)
+            const int edge = axis * 4 + 3;
+            const int corners = ch.node_materials[v] & 0xff;
+            const int m1 = (corners >> kEdgeMap[edge][0]) & 1, m2 = (corners >> kEdgeMap[edge][1]) & 1;
+            if (m1 == m2) continue;
+            static const int kWinding[2][6] = {{0, 1, 3, 0, 3, 2}, {0, 3, 1, 0, 2, 3}};
+            const int flip = m1 != 0 ? 1 : 0;
+            for (int k = 0; k < 6; k++) ch.triangles.push_back(idx[kWinding[flip][k]]);
+        }
+    }
+
+    // GenerateMeshVertexBuffer (octree.cl:475-487); the vertex count is
+    // exported only when triangles exist (compute_octree.cpp:227-232, 331-337)
+    float col[3];
+    colour_for_min_leaf_size(a.size / 256, col);  // CLIPMAP_LEAF_SIZE (volume_constants.h:15)
+    const int T = (int)ch.triangles.size() / 3;
+    ch.mesh_vertex_count = T > 0 ? V : 0;
+    ch.vertices.resize((size_t)V * 12);
+    for (int v = 0; v < V; v++) {
+        float* o = &ch.vertices[(size_t)v * 12];
+        o[0] = ch.positions[v].x; o[1] = ch.positions[v].y; o[2] = ch.positions[v].z; o[3] = ch.positions[v].w;
+        o[4] = ch.normals[v].x; o[5] = ch.normals[v].y; o[6] = ch.normals[v].z; o[7] = ch.normals[v].w;
+        o[8] = col[0]; o[9] = col[1]; o[10] = col[2]; o[11] = (float)(ch.node_materials[v] >> 8);
+    }
+
+    // FindSeamNodes + ExtractSeamNodeInfo (octree.cl:506-551)
+    for (int v = 0; v < V; v++) {
+        int pos[3];
+        position_for_code(ch.node_codes[v], D.depth, pos);
+        bool seam = false;
+        for (int i = 0; i < 3; i++) seam = seam || pos[i] == 0 || pos[i] == D.vpc - 1;
+        if (!seam) continue;
+        int32_t rec[12];
+        rec[0] = pos[0]; rec[1] = pos[1]; rec[2] = pos[2]; rec[3] = ch.node_materials[v];
+        std::memcpy(&rec[4], &ch.positions[v], 16);
+        std::memcpy(&rec[8], &ch.normals[v], 16);
+        ch.seams.insert(ch.seams.end(), rec, rec + 12);
+    }
+    return 0;
+}
+
+template <typename T>
+int copy_out(const std::vector<T>& v, void* out, int64_t cap) {
+    const int64_t bytes = (int64_t)(v.size() * sizeof(T));
+    if (out == nullptr || cap < bytes) return -2;
+    if (bytes) std::memcpy(out, v.data(), (size_t)bytes);
+    return (int)v.size();
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+
+extern "C" {
+
+int orc_set_seed(int32_t seed) {
+    build_lut(seed, &g_lut);
+    g_lut_ready = true;
+    return 0;
+}
+
+void orc_perm_lut(uint8_t* out) { std::memcpy(out, g_lut.v, sizeof(g_lut.v)); }
+
+float orc_density_at(const orc_density* d, float x, float y, float z) { return density(*d, x, y, z, g_lut); }
+float orc_snoise2(float x, float y) { return snoise2(x, y, g_lut); }
+float orc_snoise3(float x, float y, float z) { return snoise3(x, y, z, g_lut); }
+int orc_find_next_prime(int32_t n) { return find_next_prime(n); }
+
+void* orc_chunk_new(void) { return new Chunk(); }
+void orc_chunk_free(void* h) { delete static_cast<Chunk*>(h); }
+
+int orc_chunk_run(void* h, const orc_density* d, const orc_chunk_args* a) {
+    if (!g_lut_ready) return -3;
+    const int v = a->voxels_per_chunk;
+    if (v < 8 || v > 64 || (v & (v - 1))) return -1;
+    return run_chunk(*static_cast<Chunk*>(h), *d, *a, g_lut);
+}
+
+int orc_chunk_count(void* hp, int what) {
+    const Chunk& c = *static_cast<Chunk*>(hp);
+    switch (what) {
+        case ORC_MATERIALS: return (int)c.materials.size();
+        case ORC_EDGE_KEYS: case ORC_EDGE_INFO: return (int)c.edge_keys.size();
+        case ORC_NODE_CODES: case ORC_NODE_EDGES: case ORC_NODE_MATERIALS: case ORC_VERTICES: case ORC_QEFS:
+            return (int)c.node_codes.size();
+        case ORC_TRIANGLES: return (int)c.triangles.size() / 3;
+        case ORC_SEAMS: return (int)c.seams.size() / 12;
+        case ORC_PLAIN_EDGE_KEYS: return (int)c.plain_edge_keys.size();
+        case ORC_MESH_VERTEX_COUNT: return c.mesh_vertex_count;
+        case ORC_CREATED_EDGE_KEYS: return (int)c.created_keys.size();
+        default: return -1;
+    }
+}
+
+int orc_chunk_get(void* hp, int what, void* out, int64_t cap) {
+    const Chunk& c = *static_cast<Chunk*>(hp);
+    switch (what) {
+        case ORC_MATERIALS: return copy_out(c.materials, out, cap);
+        case ORC_EDGE_KEYS: return copy_out(c.edge_keys, out, cap);
+        case ORC_EDGE_INFO: return copy_out(c.edge_info, out, cap);
+        case ORC_NODE_CODES: return copy_out(c.node_codes, out, cap);
+        case ORC_NODE_EDGES: return copy_out(c.node_edges, out, cap);
+        case ORC_NODE_MATERIALS: return copy_out(c.node_materials, out, cap);
+        case ORC_VERTICES: return copy_out(c.vertices, out, cap) < 0 ? -2 : (int)c.node_codes.size();
+        case ORC_TRIANGLES: return copy_out(c.triangles, out, cap) < 0 ? -2 : (int)c.triangles.size() / 3;
+        case ORC_SEAMS: return copy_out(c.seams, out, cap) < 0 ? -2 : (int)c.seams.size() / 12;
+        case ORC_PLAIN_EDGE_KEYS: return copy_out(c.plain_edge_keys, out, cap);
+        case ORC_QEFS: return copy_out(c.qefs, out, cap);
+        case ORC_CREATED_EDGE_KEYS: return copy_out(c.created_keys, out, cap);
+        default: return -1;
+    }
+}
+
+struct orc_cuckoo {
+    Cuckoo c;
+};
+
+orc_cuckoo* orc_cuckoo_build(const uint32_t* keys, int32_t n, uint32_t seed, int32_t* retries) {
+    auto* h = new orc_cuckoo();
+    std::mt19937 gen(seed);
+    int r = 0;
+    cuckoo_build(&h->c, keys, n, gen, &r);
+    if (retries) *retries = r;
+    return h;
+}
+
+int orc_cuckoo_find(const orc_cuckoo* c, uint32_t key, uint32_t* value) {
+    const uint32_t v = c->c.find(key);
+    if (value) *value = v;
+    return v != ~0u ? 1 : 0;
+}
+
+int orc_cuckoo_prime(const orc_cuckoo* c) { return (int)c->c.prime; }
+void orc_cuckoo_free(orc_cuckoo* c) { delete c; }
+
+int orc_remove_duplicates(const int32_t* in, int32_t n, int32_t* out) {
+    std::vector<int32_t> v(in, in + n);
+    const std::vector<int32_t> r = remove_duplicates(v);
+    std::memcpy(out, r.data(), r.size() * sizeof(int32_t));
+    return (int)r.size();
+}
+
+void orc_csg_op_bounds(const orc_csg_op* op, int32_t out_min[3], int32_t out_max[3]) {
+    // CalcCSGOperationBounds (clipmap.cpp:1638-1643): CSG_OFFSET = 0.5,
+    // CSG_BOUNDS_FUDGE = 2; ivec3(float) truncates toward zero
+    for (int i = 0; i < 3; i++) {
+        const int half = (int)(op->dimensions[i] * (float)LEAF_SIZE_SCALE) + 2;
+        const int origin = (int)((op->origin[i] - 0.5f) * (float)LEAF_SIZE_SCALE);
+        out_min[i] = origin - half;
+        out_max[i] = origin + half;
+    }
+}
+
+int orc_aabb_overlaps(const int32_t amin[3], const int32_t amax[3], const int32_t bmin[3], const int32_t bmax[3]) {
+    return !(amax[0] < bmin[0] || amax[1] < bmin[1] || amax[2] < bmin[2] || amin[0] > bmax[0] ||
+             amin[1] > bmax[1] || amin[2] > bmax[2]);
+}
+
+int64_t orc_mesh_chunks(const orc_density* d, const orc_chunk_args* chunks, int32_t n, int32_t threads) {
+    if (!g_lut_ready || n <= 0) return -1;
+    if (threads < 1) threads = 1;
+    std::atomic<int> next{0};
+    std::atomic<int64_t> total{0};
+    auto worker = [&]() {
+        Chunk ch;
+        for (;;) {
+            const int i = next.fetch_add(1);
+            if (i >= n) break;
+            if (run_chunk(ch, *d, chunks[i], g_lut) == 0)
+                total += (int64_t)ch.mesh_vertex_count + (int64_t)ch.triangles.size() / 3;
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; t++) pool.emplace_back(worker);
+    for (auto& t : pool) t.join();
+    return total.load();
+}
+
+}  // extern "C"

@@ -1,0 +1,110 @@
+/*
+ * lvn_oracle.h -- C ABI of the CPU oracle for the leven chunk-meshing path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker: tests/, the smoke
+ * entry point and the bench's CPU-baseline leg load it.  The product library
+ * (leven_gb300/csrc) never includes, links or calls anything in oracle/.
+ *
+ * The oracle is a plain, sequential C++17 restatement of the reference's
+ * OpenCL kernels (the .cl files under leven/cl) and their host orchestration
+ * (leven/src/compute*.cpp).  Every function in lvn_oracle.cpp cites the
+ * reference file:line it follows.  Parity is pinned only where the reference
+ * ships known answers (cuckoo fixtures, RemoveDuplicates, FindNextPrime);
+ * field / edge / QEF / mesh results are the restatement's own and are pinned
+ * by nothing in the reference ("parity unpinned" for those stages).
+ */
+#ifndef LVN_ORACLE_H
+#define LVN_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* byte-identical to CSGOperationInfo (leven/src/compute.h:16-24), 48 B */
+typedef struct orc_csg_op {
+    int32_t type;        /* 0 = add (union), 1 = subtract */
+    int32_t brush;       /* 0 = cuboid, 1 = sphere */
+    int32_t material;
+    float   rotate_y;
+    float   origin[4];
+    float   dimensions[4];
+} orc_csg_op;
+
+/* density selector; mode 0 = reference Terrain (noise.cl:205-268),
+ * 1 = 2D fBm heightfield, 2 = 2D fBm heightfield + 3D fBm caves */
+typedef struct orc_density {
+    int32_t mode;
+    int32_t octaves2;
+    float   freq2, lacunarity2, gain2, amp2;
+    int32_t octaves3;
+    float   freq3, lacunarity3, gain3, amp3;
+} orc_density;
+
+typedef struct orc_chunk_args {
+    int32_t min[3];          /* world units (1 voxel = 4 at LOD0) */
+    int32_t size;            /* world units; sampleScale = size / (vpc*4) */
+    int32_t voxels_per_chunk;/* power of two, 8..64 */
+    int32_t default_material;
+    int32_t crossing_mode;   /* 0 = 17-sample search (reference), 1 = linear */
+    int32_t num_ops;
+    const orc_csg_op* ops;   /* applied as ONE batch after the plain edges */
+    uint32_t hash_seed;      /* seeds the hash-parameter generator */
+} orc_chunk_args;
+
+/* what orc_chunk_get / orc_chunk_count fetch */
+enum {
+    ORC_MATERIALS = 0,      /* int32[F]   final field materials             */
+    ORC_EDGE_KEYS = 1,      /* int32[E]   field edge keys (final list order) */
+    ORC_EDGE_INFO = 2,      /* float4[E]  (normal.xyz, t)                    */
+    ORC_NODE_CODES = 3,     /* uint32[V]  leaf codes, linear voxel order     */
+    ORC_NODE_EDGES = 4,     /* int32[V]   12-bit edge masks                  */
+    ORC_NODE_MATERIALS = 5, /* int32[V]   material<<8 | corners              */
+    ORC_VERTICES = 6,       /* MeshVertex[V]  (48 B)                         */
+    ORC_TRIANGLES = 7,      /* int32[3 * 2T]                                 */
+    ORC_SEAMS = 8,          /* SeamNodeInfo[S] (48 B)                        */
+    ORC_PLAIN_EDGE_KEYS = 9,/* int32[E0]  edges before CSG                   */
+    ORC_QEFS = 10,          /* QEFData[V] (64 B)                             */
+    ORC_MESH_VERTEX_COUNT = 11, /* reported vertex count (0 when no tris)     */
+    ORC_CREATED_EDGE_KEYS = 12, /* int32[]   CSG-created edge keys           */
+    ORC_NUM_WHAT = 13
+};
+
+int   orc_set_seed(int32_t seed);
+void  orc_perm_lut(uint8_t* out65536);
+float orc_density_at(const orc_density* d, float x, float y, float z);
+float orc_snoise2(float x, float y);
+float orc_snoise3(float x, float y, float z);
+int   orc_find_next_prime(int32_t n);
+
+void* orc_chunk_new(void);
+void  orc_chunk_free(void* h);
+int   orc_chunk_run(void* h, const orc_density* d, const orc_chunk_args* a);
+int   orc_chunk_count(void* h, int what);
+int   orc_chunk_get(void* h, int what, void* out, int64_t cap_bytes);
+
+/* cuckoo restatement (cuckoo.cl + compute_cuckoo.cpp), sequential insert */
+typedef struct orc_cuckoo orc_cuckoo;
+orc_cuckoo* orc_cuckoo_build(const uint32_t* keys, int32_t n, uint32_t seed, int32_t* retries);
+int      orc_cuckoo_find(const orc_cuckoo* c, uint32_t key, uint32_t* value);
+int      orc_cuckoo_prime(const orc_cuckoo* c);
+void     orc_cuckoo_free(orc_cuckoo* c);
+
+/* RemoveDuplicates restatement (compute.cpp:450-543, duplicate.cl) */
+int orc_remove_duplicates(const int32_t* in, int32_t n, int32_t* out);
+
+/* CSG op AABB (clipmap.cpp:1638-1643) and overlap (aabb.h:26-35) */
+void orc_csg_op_bounds(const orc_csg_op* op, int32_t out_min[3], int32_t out_max[3]);
+int  orc_aabb_overlaps(const int32_t amin[3], const int32_t amax[3],
+                       const int32_t bmin[3], const int32_t bmax[3]);
+
+/* CPU baseline: mesh n chunks (each a fresh field with its ops) on `threads`
+ * host threads; returns total vertices + triangles for sanity */
+int64_t orc_mesh_chunks(const orc_density* d, const orc_chunk_args* chunks, int32_t n,
+                        int32_t threads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

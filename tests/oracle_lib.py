@@ -1,0 +1,192 @@
+"""ctypes binding of the CPU oracle (oracle/_build/liboracle.so).
+
+The oracle is the checker: tests, the smoke entry point and the bench's CPU
+baseline load it; the product never does.
+"""
+import ctypes as C
+import pathlib
+import subprocess
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parents[1]
+ORACLE_SO = ROOT / "oracle" / "_build" / "liboracle.so"
+REF_SO = ROOT / "oracle" / "_ref" / "libref.so"
+
+(ORC_MATERIALS, ORC_EDGE_KEYS, ORC_EDGE_INFO, ORC_NODE_CODES, ORC_NODE_EDGES, ORC_NODE_MATERIALS,
+ ORC_VERTICES, ORC_TRIANGLES, ORC_SEAMS, ORC_PLAIN_EDGE_KEYS, ORC_QEFS, ORC_MESH_VERTEX_COUNT,
+ ORC_CREATED_EDGE_KEYS) = range(13)
+
+
+class CsgOp(C.Structure):
+    _fields_ = [("type", C.c_int32), ("brush", C.c_int32), ("material", C.c_int32),
+                ("rotate_y", C.c_float), ("origin", C.c_float * 4), ("dimensions", C.c_float * 4)]
+
+
+class Density(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("octaves2", C.c_int32), ("freq2", C.c_float),
+                ("lacunarity2", C.c_float), ("gain2", C.c_float), ("amp2", C.c_float),
+                ("octaves3", C.c_int32), ("freq3", C.c_float), ("lacunarity3", C.c_float),
+                ("gain3", C.c_float), ("amp3", C.c_float)]
+
+
+class ChunkArgs(C.Structure):
+    _fields_ = [("min", C.c_int32 * 3), ("size", C.c_int32), ("voxels_per_chunk", C.c_int32),
+                ("default_material", C.c_int32), ("crossing_mode", C.c_int32), ("num_ops", C.c_int32),
+                ("ops", C.POINTER(CsgOp)), ("hash_seed", C.c_uint32)]
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "all"], check=True)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not ORACLE_SO.exists():
+            build()
+        L = C.CDLL(str(ORACLE_SO))
+        L.orc_set_seed.argtypes = [C.c_int32]
+        L.orc_perm_lut.argtypes = [C.c_void_p]
+        L.orc_density_at.argtypes = [C.POINTER(Density), C.c_float, C.c_float, C.c_float]
+        L.orc_density_at.restype = C.c_float
+        L.orc_snoise2.argtypes = [C.c_float, C.c_float]
+        L.orc_snoise2.restype = C.c_float
+        L.orc_snoise3.argtypes = [C.c_float, C.c_float, C.c_float]
+        L.orc_snoise3.restype = C.c_float
+        L.orc_find_next_prime.argtypes = [C.c_int32]
+        L.orc_chunk_new.restype = C.c_void_p
+        L.orc_chunk_free.argtypes = [C.c_void_p]
+        L.orc_chunk_run.argtypes = [C.c_void_p, C.POINTER(Density), C.POINTER(ChunkArgs)]
+        L.orc_chunk_count.argtypes = [C.c_void_p, C.c_int]
+        L.orc_chunk_get.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int64]
+        L.orc_cuckoo_build.argtypes = [C.c_void_p, C.c_int32, C.c_uint32, C.POINTER(C.c_int32)]
+        L.orc_cuckoo_build.restype = C.c_void_p
+        L.orc_cuckoo_find.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32)]
+        L.orc_cuckoo_prime.argtypes = [C.c_void_p]
+        L.orc_cuckoo_free.argtypes = [C.c_void_p]
+        L.orc_remove_duplicates.argtypes = [C.c_void_p, C.c_int32, C.c_void_p]
+        L.orc_csg_op_bounds.argtypes = [C.POINTER(CsgOp), C.c_int32 * 3, C.c_int32 * 3]
+        L.orc_aabb_overlaps.argtypes = [C.c_int32 * 3] * 4
+        L.orc_mesh_chunks.argtypes = [C.POINTER(Density), C.POINTER(ChunkArgs), C.c_int32, C.c_int32]
+        L.orc_mesh_chunks.restype = C.c_int64
+        _lib = L
+    return _lib
+
+
+def density(mode=1, octaves2=8, freq2=1.0 / 256.0, lac2=2.0, gain2=0.5, amp2=48.0,
+            octaves3=6, freq3=1.0 / 64.0, lac3=2.0, gain3=0.5, amp3=12.0):
+    return Density(mode, octaves2, freq2, lac2, gain2, amp2, octaves3, freq3, lac3, gain3, amp3)
+
+
+def make_ops(ops):
+    """ops: list of (type, brush, material, rotate_y, origin[3], dims[3])."""
+    arr = (CsgOp * max(1, len(ops)))()
+    for i, (t, b, m, r, o, d) in enumerate(ops):
+        arr[i] = CsgOp(t, b, m, r, (C.c_float * 4)(o[0], o[1], o[2], 0.0), (C.c_float * 4)(d[0], d[1], d[2], 0.0))
+    return arr
+
+
+class OracleChunk:
+    """Runs the oracle pipeline for one chunk and exposes every stage."""
+
+    def __init__(self, dens, min_xyz, size, vpc=64, default_material=0, crossing_mode=0, ops=(), hash_seed=5489):
+        L = lib()
+        self._h = L.orc_chunk_new()
+        self._ops = make_ops(list(ops))
+        a = ChunkArgs((C.c_int32 * 3)(*min_xyz), size, vpc, default_material, crossing_mode, len(ops),
+                      C.cast(self._ops, C.POINTER(CsgOp)), hash_seed)
+        rc = L.orc_chunk_run(self._h, C.byref(dens), C.byref(a))
+        if rc != 0:
+            raise RuntimeError(f"orc_chunk_run failed: {rc}")
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc_chunk_free(self._h)
+            self._h = None
+
+    def count(self, what):
+        return lib().orc_chunk_count(self._h, what)
+
+    def get(self, what, dtype, width=1):
+        n = self.count(what if what != ORC_VERTICES else ORC_NODE_CODES)
+        if what == ORC_TRIANGLES:
+            n = self.count(ORC_TRIANGLES)
+        out = np.zeros((max(n, 1), width), dtype=dtype)
+        got = lib().orc_chunk_get(self._h, what, out.ctypes.data, out.nbytes)
+        if got < 0:
+            raise RuntimeError(f"orc_chunk_get({what}) failed: {got}")
+        out = out[:n]
+        return out[:, 0] if width == 1 else out
+
+    # convenience accessors
+    def materials(self):
+        return self.get(ORC_MATERIALS, np.int32)
+
+    def edge_keys(self):
+        return self.get(ORC_EDGE_KEYS, np.int32)
+
+    def plain_edge_keys(self):
+        return self.get(ORC_PLAIN_EDGE_KEYS, np.int32)
+
+    def created_edge_keys(self):
+        return self.get(ORC_CREATED_EDGE_KEYS, np.int32)
+
+    def edge_info(self):
+        return self.get(ORC_EDGE_INFO, np.float32, 4)
+
+    def node_codes(self):
+        return self.get(ORC_NODE_CODES, np.uint32)
+
+    def node_edges(self):
+        return self.get(ORC_NODE_EDGES, np.int32)
+
+    def node_materials(self):
+        return self.get(ORC_NODE_MATERIALS, np.int32)
+
+    def vertices(self):
+        return self.get(ORC_VERTICES, np.float32, 12)
+
+    def triangles(self):
+        return self.get(ORC_TRIANGLES, np.int32, 3)
+
+    def seams(self):
+        return self.get(ORC_SEAMS, np.int32, 12)
+
+    def qefs(self):
+        return self.get(ORC_QEFS, np.float32, 16)
+
+    def mesh_vertex_count(self):
+        return self.count(ORC_MESH_VERTEX_COUNT)
+
+
+def set_seed(seed):
+    lib().orc_set_seed(seed)
+
+
+def perm_lut():
+    out = np.zeros(65536, dtype=np.uint8)
+    lib().orc_perm_lut(out.ctypes.data)
+    return out
+
+
+def find_next_prime(n):
+    return lib().orc_find_next_prime(n)
+
+
+def remove_duplicates(values):
+    v = np.ascontiguousarray(values, dtype=np.int32)
+    out = np.zeros(max(1, v.size), dtype=np.int32)
+    n = lib().orc_remove_duplicates(v.ctypes.data, v.size, out.ctypes.data)
+    return out[:n]
+
+
+def op_bounds(op_tuple):
+    ops = make_ops([op_tuple])
+    lo = (C.c_int32 * 3)()
+    hi = (C.c_int32 * 3)()
+    lib().orc_csg_op_bounds(ops, lo, hi)
+    return list(lo), list(hi)

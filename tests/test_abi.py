@@ -1,0 +1,81 @@
+"""The C-ABI library loads and exports every entry point include/lvn.h
+declares; host-side argument checks work without a GPU (no compute calls)."""
+import ctypes as C
+import pathlib
+import re
+
+import pytest
+
+import leven_gb300 as lvn
+
+ROOT = pathlib.Path(__file__).resolve().parents[1]
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from leven_gb300 import build
+
+    build.build()
+    return lvn.lib()
+
+
+def header_functions():
+    text = (ROOT / "include" / "lvn.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(lvn_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_exports_every_declared_symbol(lib):
+    names = header_functions()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert sorted(lvn.EXPORTS) == names
+
+
+def test_struct_layouts():
+    # byte-identical to CSGOperationInfo, MeshVertex, MeshTriangle, SeamNodeInfo
+    assert C.sizeof(lvn.CsgOp) == 48
+    assert C.sizeof(lvn.ChunkDesc) == 16
+    assert C.sizeof(lvn.ChunkResult) == 32
+
+
+def test_error_strings(lib):
+    assert lvn.error_string(0) == "LVN_OK"
+    assert lvn.error_string(-100) == "LVN_ERR_CAPACITY"
+    assert lvn.error_string(-99999) == "LVN_ERR_CUDA"
+
+
+def test_host_checks_without_device(lib):
+    # before lvn_initialise nothing computes
+    assert lib.lvn_meshgen_create(64) is None
+    mn = (C.c_int32 * 3)(0, 0, 0)
+    out = lvn.BatchOut()
+    assert lib.lvn_meshgen_generate_chunks(None, None, 0, C.byref(out)) in (-101, -30)
+    # operation bounds are host logic (CalcCSGOperationBounds, clipmap.cpp:1638-1643)
+    op = lvn.make_op(1, 1, 201, (10.5, 20.5, -3.5), (3.0, 3.0, 3.0))
+    lo, hi = lvn.csg_operation_bounds(op)
+    assert lo == [26, 66, -30] and hi == [54, 94, -2]
+    assert lib.lvn_store_csg_operation(C.byref(lvn.make_op(2, 0, 1, (0, 0, 0), (1, 1, 1))), mn, mn) == -30
+    assert lib.lvn_store_csg_operation(C.byref(lvn.make_op(0, 0, 300, (0, 0, 0), (1, 1, 1))), mn, mn) == -30
+    assert lib.lvn_clear_csg_operations() == 0
+    p = lvn.DensityParams(7, 8, 0.1, 2.0, 0.5, 48.0, 6, 0.1, 2.0, 0.5, 12.0)
+    assert lib.lvn_set_density(C.byref(p)) == -30
+
+
+def test_workload_generator():
+    from leven_gb300 import workloads as W
+
+    # std::mt19937 default seed: the 10000th output is 4123659995
+    rng = W.MT19937(5489)
+    for _ in range(9999):
+        rng.u32()
+    assert rng.u32() == 4123659995
+    wl = W.tiled_csg()
+    assert len(wl.chunks) == 128 and len(wl.ops) == 32
+    kinds = {(o.type, o.brush_shape) for o in wl.ops}
+    assert kinds == {(1, 1), (0, 0)}
+    for o in wl.ops:
+        assert 0 <= o.origin[0] < 512 and -64 <= o.origin[1] < 64 and 0 <= o.origin[2] < 512
+        assert all(2 <= d <= 12 for d in o.dimensions)
+    assert W.op_bounds(W.Op(1, 1, 201, (10.5, 20.5, -3.5), (3.0, 3.0, 3.0))) == ([26, 66, -30], [54, 94, -2])
