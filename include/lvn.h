@@ -222,6 +222,29 @@ int         lvn_meshgen_reset_stage_times(lvn_meshgen* ctx);
 #define LVN_DEBUG_PLAIN_EDGES  9  /* int32       number of plain (non-CSG) edges */
 int64_t lvn_meshgen_debug_fetch(lvn_meshgen* ctx, int32_t what, int32_t chunk, void* host, int64_t cap_bytes);
 
+/* No counterpart in the reference.  Meshes one chunk exactly as
+ * lvn_meshgen_generate_chunk_mesh does with caching off, but allocates no
+ * memory: for engine threads that cannot call cudaMalloc / cudaFree (a
+ * frame-locked render or streaming thread, where cudaFree would synchronise
+ * the device; engines that reserve all GPU memory at start-up; recording
+ * into a CUDA graph).  The caller passes the chunk and its output arrays
+ * (host or device per out->memory); the stored CSG operations and the noise
+ * seed come from the global state as usual.  All intermediate buffers live
+ * in one static device array of LVN_NOALLOC_SCRATCH_BYTES that every GPU
+ * loading the library keeps until exit.  The first call on a device looks up
+ * that array's address (cudaGetSymbolAddress), so make it before any stream
+ * capture.  Chunks beyond the LVN_NOALLOC_MAX_* limits are rejected with
+ * LVN_ERR_CAPACITY.  Calls share the array: two calls in flight on the GPU at
+ * the same time (different streams or threads) race; serialise them.
+ * cuda_stream may be NULL (the legacy default stream). */
+#define LVN_NOALLOC_SCRATCH_BYTES        (12 * 1024 * 1024)
+#define LVN_NOALLOC_MAX_VOXELS_PER_CHUNK 64
+#define LVN_NOALLOC_MAX_EDGES            65536   /* active field edges after CSG */
+#define LVN_NOALLOC_MAX_NODES            32768   /* leaves (active voxels)       */
+#define LVN_NOALLOC_MAX_CSG_OPS          64      /* stored operations per chunk  */
+int lvn_generate_chunk_mesh_noalloc(const int32_t min[3], int32_t size, int32_t voxels_per_chunk, lvn_mesh_out* out,
+                                    void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

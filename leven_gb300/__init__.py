@@ -78,6 +78,7 @@ EXPORTS = [
     "lvn_meshgen_is_chunk_empty", "lvn_meshgen_generate_chunk_mesh", "lvn_meshgen_generate_chunks",
     "lvn_meshgen_set_stream", "lvn_meshgen_get_stream", "lvn_meshgen_set_option", "lvn_meshgen_stage_times",
     "lvn_meshgen_stage_name", "lvn_meshgen_reset_stage_times", "lvn_meshgen_debug_fetch",
+    "lvn_generate_chunk_mesh_noalloc",
 ]
 
 _lib = None
@@ -119,6 +120,7 @@ def lib():
     L.lvn_meshgen_reset_stage_times.argtypes = [C.c_void_p]
     L.lvn_meshgen_debug_fetch.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int64]
     L.lvn_meshgen_debug_fetch.restype = C.c_int64
+    L.lvn_generate_chunk_mesh_noalloc.argtypes = [i32p, C.c_int32, C.c_int32, C.POINTER(MeshOut), C.c_void_p]
     _lib = L
     return L
 

@@ -1116,3 +1116,40 @@ int64_t lvn_meshgen_debug_fetch(lvn_meshgen* m, int32_t what, int32_t chunk, voi
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// read-only state access for other translation units (lvn_state.h)
+// ---------------------------------------------------------------------------
+
+#include "lvn_state.h"
+
+namespace lvn {
+
+GlobalView global_view() {
+    GlobalView v;
+    v.initialised = g.initialised;
+    v.num_sms = g.num_sms;
+    v.default_material = g.default_material;
+    v.perm = g.perm.as<uint8_t>();
+    v.grad = g.grad.as<float>();
+    v.density = g.density;
+    return v;
+}
+
+int stored_ops_for_chunk(const int32_t min[3], int32_t size, Brush* out, int cap) {
+    const int32_t lo[3] = {min[0], min[1], min[2]};
+    const int32_t hi[3] = {min[0] + size, min[1] + size, min[2] + size};
+    int n = 0;
+    for (const StoredOp& s : g.ops) {
+        if (!overlaps(lo, hi, s.lo, s.hi)) continue;
+        if (n >= cap) return -1;
+        out[n++] = make_brush(s.op);
+    }
+    return n;
+}
+
+void draw_hash_params(uint32_t* p) { draw_params(p); }
+
+void lod_colour_for(int s, float c[3]) { lod_colour(s, c); }
+
+}  // namespace lvn

@@ -1,0 +1,28 @@
+// lvn_state.h -- read-only access to liblvn's global compute state for
+// translation units other than lvn_api.cu (defined at the end of lvn_api.cu).
+#pragma once
+#include <cstdint>
+
+#include "lvn_types.h"
+
+namespace lvn {
+
+struct GlobalView {
+    bool initialised;
+    int num_sms;
+    int32_t default_material;
+    const uint8_t* perm;   // device permutation image (65536 B)
+    const float* grad;     // device gradient table (16 x 4)
+    DensityParams density;
+};
+
+GlobalView global_view();
+// The stored operations whose AABB overlaps [min, min + size], in store
+// order, written to out[0..cap); returns their count, or -1 when more than cap.
+int stored_ops_for_chunk(const int32_t min[3], int32_t size, Brush* out, int cap);
+// Draws one cuckoo parameter set (10 words) from the shared generator.
+void draw_hash_params(uint32_t* p);
+// ColourForMinLeafSize (clipmap.cpp:329-353)
+void lod_colour_for(int min_leaf_size, float c[3]);
+
+}  // namespace lvn
