@@ -198,6 +198,39 @@ Brush make_brush(const lvn_csg_op& op) {
     return b;
 }
 
+// Field-index box holding every point the operations can change: a sphere's
+// points with d <= 0 lie within its radius, a cube's (rotated about y) within
+// sqrt(hx^2 + hz^2) in x/z and hy in y; one density unit of margin.
+void csg_box(const Brush* ops, int n, const int32_t off[3], int scale, int fd, int32_t lo[3], int32_t hi[3]) {
+    for (int i = 0; i < 3; i++) {
+        lo[i] = fd;
+        hi[i] = -1;
+    }
+    for (int k = 0; k < n; k++) {
+        const Brush& b = ops[k];
+        double ext[3];
+        if (b.brush != 0) {
+            ext[0] = ext[1] = ext[2] = std::fabs((double)b.dimensions[0]);
+        } else {
+            const double r = std::sqrt((double)b.dimensions[0] * b.dimensions[0] + (double)b.dimensions[2] * b.dimensions[2]);
+            ext[0] = ext[2] = r;
+            ext[1] = std::fabs((double)b.dimensions[1]);
+        }
+        for (int i = 0; i < 3; i++) {
+            const double l = ((double)b.origin[i] - ext[i] - 1.0 - off[i]) / scale;
+            const double h = ((double)b.origin[i] + ext[i] + 1.0 - off[i]) / scale;
+            int li = 0, hi_ = fd - 1;
+            if (std::isfinite(l) && std::isfinite(h)) {
+                li = (int)std::max(0.0, std::min((double)fd - 1, std::floor(l)));
+                hi_ = (int)std::max(0.0, std::min((double)fd - 1, std::ceil(h)));
+                if (h < 0.0 || l > fd - 1) { li = fd; hi_ = -1; }  // entirely outside the field
+            }
+            lo[i] = std::min(lo[i], li);
+            hi[i] = std::max(hi[i], hi_);
+        }
+    }
+}
+
 bool valid_op(const lvn_csg_op& op) {
     return (op.type == 0 || op.type == 1) && (op.brush_shape == 0 || op.brush_shape == 1) && op.material >= 0 &&
            op.material <= 255;
@@ -229,7 +262,7 @@ void draw_params(uint32_t* p) {
 typedef std::tuple<int32_t, int32_t, int32_t, int32_t> ChunkKey;
 
 struct FieldEntry {  // GPUDensityField (compute_local.h:28-37)
-    DevBuf corners;
+    DevBuf mats, planes;
     DevBuf keys, info;
     int32_t num_edges = 0;
     int32_t last_op = 0;
@@ -251,7 +284,7 @@ struct lvn_meshgen {
     bool profile = false;
 
     // pools
-    DevBuf desc, cs, bs, brushes, corners, edge_tiles, vox_tiles;
+    DevBuf desc, cs, bs, brushes, mats, planes, edge_tiles, vox_tiles;
     DevBuf edge_keys, edge_chunk, edge_info, node_codes, node_info, node_chunk;
     DevBuf edge_slots, node_slots, quad_scratch, node_tile_counts, chunk_tile_off;
     DevBuf vertices, triangles, seams;
@@ -288,7 +321,8 @@ int ensure_pools(lvn_meshgen* m, int n, Capacity want) {
     LVN_CK(m->desc.ensure(sizeof(ChunkDesc) * n));
     LVN_CK(m->cs.ensure(sizeof(ChunkState) * n));
     LVN_CK(m->bs.ensure(sizeof(BatchState)));
-    LVN_CK(m->corners.ensure(sizeof(uint16_t) * (size_t)F * n));
+    LVN_CK(m->mats.ensure((size_t)F * n));
+    LVN_CK(m->planes.ensure(sizeof(uint4) * 3 * (size_t)field_rows(m->vpc) * n));
     LVN_CK(m->edge_tiles.ensure(sizeof(int2) * (size_t)edge_tiles_per_chunk(m->vpc) * n));
     LVN_CK(m->vox_tiles.ensure(sizeof(int) * (size_t)vox_tiles_per_chunk(m->vpc) * n));
     LVN_CK(m->chunk_tile_off.ensure(sizeof(int) * (size_t)(n + 1)));
@@ -358,7 +392,8 @@ BatchPtrs make_ptrs(lvn_meshgen* m, int n) {
     b.brushes = m->brushes.as<Brush>();
     b.perm = g.perm.as<uint8_t>();
     b.grad = g.grad.as<float>();
-    b.corners = m->corners.as<uint16_t>();
+    b.mats = m->mats.as<uint8_t>();
+    b.planes = m->planes.as<uint4>();
     b.edge_tiles = m->edge_tiles.as<int2>();
     b.vox_tiles = m->vox_tiles.as<int>();
     b.edge_keys = m->edge_keys.as<int32_t>();
@@ -474,6 +509,7 @@ int build_descs(lvn_meshgen* m, const lvn_chunk_desc* chunks, int n, std::vector
                 if (overlaps(lo, hi, s.lo, s.hi)) brushes.push_back(make_brush(s.op));
         }
         d.op_count = (int32_t)brushes.size() - d.op_begin;
+        csg_box(brushes.data() + d.op_begin, d.op_count, d.off, scale, m->vpc + 2, d.csg_lo, d.csg_hi);
         draw_params(d.edge_params);
         draw_params(d.node_params);
     }
@@ -596,8 +632,11 @@ int one_desc(lvn_meshgen* m, const int32_t min[3], int32_t size, std::vector<Chu
 int save_field(lvn_meshgen* m, FieldEntry& f) {
     const ChunkState& cs = m->last_cs[0];
     const size_t F = (size_t)field_size(m->vpc);
-    LVN_CK(f.corners.ensure(sizeof(uint16_t) * F));
-    LVN_CK(cudaMemcpyAsync(f.corners.p, m->corners.p, sizeof(uint16_t) * F, cudaMemcpyDeviceToDevice, m->stream));
+    const size_t PB = sizeof(uint4) * 3 * (size_t)field_rows(m->vpc);
+    LVN_CK(f.mats.ensure(F));
+    LVN_CK(f.planes.ensure(PB));
+    LVN_CK(cudaMemcpyAsync(f.mats.p, m->mats.p, F, cudaMemcpyDeviceToDevice, m->stream));
+    LVN_CK(cudaMemcpyAsync(f.planes.p, m->planes.p, PB, cudaMemcpyDeviceToDevice, m->stream));
     f.num_edges = cs.num_edges;
     LVN_CK(f.keys.ensure(sizeof(int32_t) * std::max(1, cs.num_edges)));
     LVN_CK(f.info.ensure(sizeof(float4) * std::max(1, cs.num_edges)));
@@ -639,13 +678,19 @@ int apply_csg_to_field(lvn_meshgen* m, const int32_t min[3], int32_t size, Field
     for (const lvn_csg_op& op : ops) brushes.push_back(make_brush(op));
     descs[0].op_begin = 0;
     descs[0].op_count = (int32_t)brushes.size();
+    csg_box(brushes.data(), descs[0].op_count, descs[0].off, descs[0].scale, m->vpc + 2, descs[0].csg_lo,
+            descs[0].csg_hi);
     Capacity cap = default_capacity(m, 1);
     cap.ecap = std::max<int64_t>(std::max(cap.ecap, m->ecap), (int64_t)f.num_edges + 3 * field_size(m->vpc));
     cap.vcap = std::max(cap.vcap, m->vcap);
     if ((rc = ensure_pools(m, 1, cap))) return rc;
     if ((rc = upload(m, descs, brushes))) return rc;
     const size_t F = (size_t)field_size(m->vpc);
-    LVN_CK(cudaMemcpyAsync(m->corners.p, f.corners.p, sizeof(uint16_t) * F, cudaMemcpyDeviceToDevice, m->stream));
+    const size_t R = (size_t)field_rows(m->vpc);
+    LVN_CK(cudaMemcpyAsync(m->mats.p, f.mats.p, F, cudaMemcpyDeviceToDevice, m->stream));
+    LVN_CK(cudaMemcpyAsync(m->planes.p, f.planes.p, sizeof(uint4) * 2 * R, cudaMemcpyDeviceToDevice, m->stream));
+    // no corner is changed by this batch until the CSG kernel says so
+    LVN_CK(cudaMemsetAsync(m->planes.as<uint4>() + 2 * R, 0, sizeof(uint4) * R, m->stream));
     BatchPtrs b = make_ptrs(m, 1);
     b.plain_class = 0;
     b.prev_keys = f.keys.as<int32_t>();
@@ -674,7 +719,8 @@ int load_field(lvn_meshgen* m, const int32_t min[3], int32_t size, FieldEntry** 
         FieldEntry fresh;
         int rc = generate_field(m, min, size, fresh);
         if (rc) {
-            fresh.corners.release();
+            fresh.mats.release();
+            fresh.planes.release();
             fresh.keys.release();
             fresh.info.release();
             return rc;
@@ -705,7 +751,9 @@ int mesh_from_field(lvn_meshgen* m, const int32_t min[3], int32_t size, FieldEnt
         if ((rc = ensure_pools(m, 1, cap))) return rc;
         if ((rc = upload(m, descs, none))) return rc;
         const size_t F = (size_t)field_size(m->vpc);
-        LVN_CK(cudaMemcpyAsync(m->corners.p, f.corners.p, sizeof(uint16_t) * F, cudaMemcpyDeviceToDevice, m->stream));
+        LVN_CK(cudaMemcpyAsync(m->mats.p, f.mats.p, F, cudaMemcpyDeviceToDevice, m->stream));
+        LVN_CK(cudaMemcpyAsync(m->planes.p, f.planes.p, sizeof(uint4) * 3 * (size_t)field_rows(m->vpc),
+                               cudaMemcpyDeviceToDevice, m->stream));
         LVN_CK(cudaMemcpyAsync(m->edge_keys.p, f.keys.p, sizeof(int32_t) * f.num_edges, cudaMemcpyDeviceToDevice,
                                m->stream));
         LVN_CK(cudaMemcpyAsync(m->edge_info.p, f.info.p, sizeof(float4) * f.num_edges, cudaMemcpyDeviceToDevice,
@@ -902,7 +950,7 @@ lvn_meshgen* lvn_meshgen_create(int32_t voxels_per_chunk) {
 void lvn_meshgen_destroy(lvn_meshgen* m) {
     if (!m) return;
     cudaStreamSynchronize(m->stream);
-    DevBuf* bufs[] = {&m->desc,       &m->cs,         &m->bs,         &m->brushes,      &m->corners,
+    DevBuf* bufs[] = {&m->desc,       &m->cs,         &m->bs,         &m->brushes,      &m->mats,  &m->planes,
                       &m->edge_tiles, &m->vox_tiles,  &m->edge_keys,  &m->edge_chunk,   &m->edge_info,
                       &m->node_codes, &m->node_info,  &m->node_chunk, &m->edge_slots,   &m->node_slots,
                       &m->quad_scratch, &m->node_tile_counts, &m->chunk_tile_off, &m->vertices, &m->triangles,
@@ -913,7 +961,8 @@ void lvn_meshgen_destroy(lvn_meshgen* m) {
     m->h_cs.release();
     m->h_bs.release();
     for (auto& kv : m->fields) {
-        kv.second.corners.release();
+        kv.second.mats.release();
+        kv.second.planes.release();
         kv.second.keys.release();
         kv.second.info.release();
     }
@@ -1085,14 +1134,8 @@ int64_t lvn_meshgen_debug_fetch(lvn_meshgen* m, int32_t what, int32_t chunk, voi
     int64_t count = 0, elem = 0;
     std::vector<uint8_t> mats;
     switch (what) {
-        case LVN_DEBUG_MATERIALS: {
-            std::vector<uint16_t> cw(F);
-            if (cudaMemcpy(cw.data(), m->corners.as<uint16_t>() + F * chunk, F * 2, cudaMemcpyDeviceToHost) != cudaSuccess)
-                return LVN_ERR_CUDA;
-            if (cap < (int64_t)F) return LVN_ERR_CAPACITY;
-            for (size_t i = 0; i < F; i++) static_cast<uint8_t*>(host)[i] = (uint8_t)(cw[i] & 0xff);
-            return (int64_t)F;
-        }
+        case LVN_DEBUG_MATERIALS:
+            src = m->mats.as<uint8_t>() + F * chunk; count = (int64_t)F; elem = 1; break;
         case LVN_DEBUG_EDGE_KEYS: src = m->edge_keys.as<int32_t>() + cs.edge_off; count = cs.num_edges; elem = 4; break;
         case LVN_DEBUG_EDGE_INFO: src = m->edge_info.as<float4>() + cs.edge_off; count = cs.num_edges; elem = 16; break;
         case LVN_DEBUG_NODE_CODES: src = m->node_codes.as<uint32_t>() + cs.node_off; count = cs.nodes; elem = 4; break;
@@ -1151,5 +1194,9 @@ int stored_ops_for_chunk(const int32_t min[3], int32_t size, Brush* out, int cap
 void draw_hash_params(uint32_t* p) { draw_params(p); }
 
 void lod_colour_for(int s, float c[3]) { lod_colour(s, c); }
+
+void csg_box_for(const Brush* ops, int n, const int32_t off[3], int scale, int fd, int32_t lo[3], int32_t hi[3]) {
+    csg_box(ops, n, off, scale, fd, lo, hi);
+}
 
 }  // namespace lvn

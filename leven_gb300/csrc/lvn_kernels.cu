@@ -48,12 +48,11 @@ struct Geo {
     static constexpr int FD = VPC + 2;           // FIELD_DIM
     static constexpr int HD = VPC + 1;           // HERMITE_INDEX_SIZE
     static constexpr int F = FD * FD * FD;
-    static constexpr int C = VPC * VPC * VPC;
     static constexpr int DEPTH = VPC == 8 ? 3 : VPC == 16 ? 4 : VPC == 32 ? 5 : 6;  // MAX_OCTREE_DEPTH
     static constexpr int SHIFT = DEPTH + 1;      // VOXEL_INDEX_SHIFT
     static constexpr int MASK = (1 << SHIFT) - 1;
-    static constexpr int NBE = (F + kTilePoints - 1) / kTilePoints;
-    static constexpr int NBV = (C + kTilePoints - 1) / kTilePoints;
+    static constexpr int NBE = (FD * FD + kThreads - 1) / kThreads;   // field-row tiles
+    static constexpr int NBV = (VPC * VPC + kThreads - 1) / kThreads; // voxel-row tiles
 };
 
 // EDGE_MAP / EDGE_VERTEX_MAP (shared_constants.cl:4-9, octree.cl:227-232) as
@@ -164,7 +163,7 @@ __device__ __forceinline__ long long cta_scan(int n, Val val, Out out, long long
 }
 
 // ---------------------------------------------------------------------------
-// FindNextPrime (primes.cpp:9-58)
+// IsPrime (primes.cpp:9-28)
 // ---------------------------------------------------------------------------
 
 __device__ bool is_prime_d(int x) {
@@ -178,17 +177,6 @@ __device__ bool is_prime_d(int x) {
     }
 }
 
-__device__ int find_next_prime_d(int n) {
-    if (n <= 2) return 2;
-    if (n == 3) return 3;
-    if (n <= 5) return 5;
-    const int k = n / 6;
-    int i = n - 6 * k;
-    const int o = i < 2 ? 1 : 5;
-    int x = 6 * k + o;
-    for (i = (3 + o) / 2; !is_prime_d(x); x += i) i ^= 6;
-    return x;
-}
 
 // ---------------------------------------------------------------------------
 // cuckoo hash (cuckoo.cl:1-105)
@@ -368,67 +356,142 @@ __global__ void k_reset(BatchPtrs b) {
 }
 
 // ---------------------------------------------------------------------------
-// stage 1: density field (GenerateDefaultField, density_field.cl:11-37)
-// One thread per (x, z) column; heightfield modes evaluate the height term
-// once per column (the density is y - amp * h(x, z) [+ caves]).
+// Field bit planes.  Row (y, z) of a chunk's field packs x = 0..65 into a
+// uint4 (bits 0-31, 32-63, 64-65).  Plane 0: plain solid (material != AIR
+// before CSG); plane 1: final air (material == AIR after CSG); plane 2:
+// changed by this CSG batch.  Row index r = y + FD * z, so the linear
+// successor of field point (FD-1, y, z) is bit 0 of row r + 1, as in the
+// reference's linear field index.
 // ---------------------------------------------------------------------------
 
 template <int VPC>
-__global__ void __launch_bounds__(128) k_field(BatchPtrs b) {
+__device__ __forceinline__ uint4* plane_ptr(const BatchPtrs& b, int c, int plane) {
+    constexpr int R = (VPC + 2) * (VPC + 2);
+    return b.planes + ((size_t)c * 3 + plane) * R;
+}
+
+// x + 1 neighbour: shift right by one bit across the row
+__device__ __forceinline__ uint4 shr1(uint4 r) {
+    return make_uint4((r.x >> 1) | (r.y << 31), (r.y >> 1) | (r.z << 31), (r.z >> 1) | (r.w << 31), r.w >> 1);
+}
+__device__ __forceinline__ uint4 and4(uint4 a, uint4 b) { return make_uint4(a.x & b.x, a.y & b.y, a.z & b.z, a.w & b.w); }
+__device__ __forceinline__ uint4 or4(uint4 a, uint4 b) { return make_uint4(a.x | b.x, a.y | b.y, a.z | b.z, a.w | b.w); }
+__device__ __forceinline__ uint4 xor4(uint4 a, uint4 b) { return make_uint4(a.x ^ b.x, a.y ^ b.y, a.z ^ b.z, a.w ^ b.w); }
+__device__ __forceinline__ uint4 not4(uint4 a) { return make_uint4(~a.x, ~a.y, ~a.z, ~a.w); }
+__device__ __forceinline__ int popc4(uint4 a) { return __popc(a.x) + __popc(a.y) + __popc(a.z) + __popc(a.w); }
+__device__ __forceinline__ bool bit4(uint4 a, int x) {
+    const unsigned w = x < 32 ? a.x : x < 64 ? a.y : x < 96 ? a.z : a.w;
+    return (w >> (x & 31)) & 1u;
+}
+// low `n` bits set (n <= 128)
+__device__ __forceinline__ uint4 low_bits(int n) {
+    auto m = [](int k) { return k <= 0 ? 0u : k >= 32 ? ~0u : ((1u << k) - 1u); };
+    return make_uint4(m(n), m(n - 32), m(n - 64), m(n - 96));
+}
+
+// ---------------------------------------------------------------------------
+// stage 1: density field (GenerateDefaultField, density_field.cl:11-37)
+// One CTA per (z slice, chunk), one thread per x; heightfield modes evaluate
+// the height term once per (x, z) column.  Writes the byte materials and the
+// three bit planes (warp ballots along x).
+// ---------------------------------------------------------------------------
+
+template <int VPC>
+__global__ void __launch_bounds__(96) k_field(BatchPtrs b) {
     using G = Geo<VPC>;
     __shared__ float sg[64];
+    __shared__ unsigned words[3];
     if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
     __syncthreads();
-    const int c = blockIdx.y;
-    const int col = blockIdx.x * blockDim.x + threadIdx.x;
-    if (col >= G::FD * G::FD) return;
-    const int x = col % G::FD, z = col / G::FD;
+    const int c = blockIdx.y, z = blockIdx.x;
+    const int x = threadIdx.x;
+    const bool valid = x < G::FD;
     const ChunkDesc& d = b.desc[c];
     const int scale = d.scale;
     const Noise nz{b.perm, sg};
     const float wx = (float)(x * scale + d.off[0]);
     const float wz = (float)(z * scale + d.off[2]);
-    const float h = nz.height(b.density, wx, wz);
+    const float h = valid ? nz.height(b.density, wx, wz) : 0.f;
     const int dm = b.default_material;
-    const uint16_t solid = (uint16_t)(dm | (dm != MATERIAL_AIR ? CORNER_PLAIN_SOLID : 0));
-    uint16_t* out = b.corners + (size_t)c * G::F + x + G::FD * G::FD * z;
-#pragma unroll 2
+    uint8_t* mats = b.mats + (size_t)c * G::F + x + G::FD * G::FD * z;
+    uint4* P = plane_ptr<VPC>(b, c, 0) + G::FD * z;
+    uint4* A = plane_ptr<VPC>(b, c, 1) + G::FD * z;
+    uint4* X = plane_ptr<VPC>(b, c, 2) + G::FD * z;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint4 V = low_bits(G::FD);
     for (int y = 0; y < G::FD; y++) {
-        const float wy = (float)(y * scale + d.off[1]);
-        const float dv = nz.density_h(b.density, h, wx, wy, wz);
-        out[G::FD * y] = dv < 0.f ? solid : (uint16_t)MATERIAL_AIR;
+        bool solid = false;
+        if (valid) {
+            const float wy = (float)(y * scale + d.off[1]);
+            const float dv = nz.density_h(b.density, h, wx, wy, wz);
+            const int m = dv < 0.f ? dm : MATERIAL_AIR;
+            mats[G::FD * y] = (uint8_t)m;
+            solid = m != MATERIAL_AIR;
+        }
+        const unsigned s = __ballot_sync(FULL, solid);
+        if (lane == 0) words[warp] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const uint4 p = make_uint4(words[0], words[1], words[2], 0u);
+            P[y] = p;
+            A[y] = and4(not4(p), V);
+            X[y] = make_uint4(0u, 0u, 0u, 0u);
+        }
+        __syncthreads();
     }
 }
 
 // ---------------------------------------------------------------------------
 // stage 2: CSG materials (CSG_HermiteIndices + UpdateFieldMaterials,
-// apply_csg_operation.cl:179-241); marks corners this batch changed.
+// apply_csg_operation.cl:179-241) inside the chunk's operation bounding box;
+// rows there get their final-air and changed bits rewritten.
 // ---------------------------------------------------------------------------
 
 template <int VPC>
-__global__ void __launch_bounds__(kThreads) k_csg(BatchPtrs b) {
+__global__ void __launch_bounds__(96) k_csg(BatchPtrs b) {
     using G = Geo<VPC>;
-    const int c = blockIdx.y;
+    __shared__ unsigned air_w[3], chg_w[3];
+    const int c = blockIdx.y, z = blockIdx.x;
     const ChunkDesc& d = b.desc[c];
     const int nops = d.op_count;
-    if (nops == 0) return;
-    const int L = blockIdx.x * blockDim.x + threadIdx.x;
-    if (L >= G::F) return;
-    const int x = L % G::FD, y = (L / G::FD) % G::FD, z = L / (G::FD * G::FD);
-    uint16_t* cw = b.corners + (size_t)c * G::F + L;
-    const uint16_t w = *cw;
-    const int m = w & 0xff;
-    const float wx = (float)(d.off[0] + d.scale * x);
-    const float wy = (float)(d.off[1] + d.scale * y);
-    const float wz = (float)(d.off[2] + d.scale * z);
-    int nm = m;
+    if (nops == 0 || z < d.csg_lo[2] || z > d.csg_hi[2]) return;
+    const int x = threadIdx.x;
+    const bool inx = x < G::FD && x >= d.csg_lo[0] && x <= d.csg_hi[0];
     const Brush* ops = b.brushes + d.op_begin;
-    for (int i = 0; i < nops; i++) {
-        const Brush& br = ops[i];
-        if (brush_density(br, wx, wy, wz) <= 0.f) nm = br.type == 0 ? br.material : MATERIAL_AIR;
+    uint8_t* mats = b.mats + (size_t)c * G::F + G::FD * G::FD * z;
+    uint4* A = plane_ptr<VPC>(b, c, 1) + G::FD * z;
+    uint4* X = plane_ptr<VPC>(b, c, 2) + G::FD * z;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const float wx = (float)(d.off[0] + d.scale * x);
+    const float wz = (float)(d.off[2] + d.scale * z);
+    for (int y = d.csg_lo[1]; y <= d.csg_hi[1]; y++) {
+        bool air = false, changed = false;
+        if (x < G::FD) {
+            const int m = mats[x + G::FD * y];
+            int nm = m;
+            if (inx) {
+                const float wy = (float)(d.off[1] + d.scale * y);
+                for (int i = 0; i < nops; i++) {
+                    const Brush& br = ops[i];
+                    if (brush_density(br, wx, wy, wz) <= 0.f) nm = br.type == 0 ? br.material : MATERIAL_AIR;
+                }
+                if (nm != m) mats[x + G::FD * y] = (uint8_t)nm;
+            }
+            air = nm == MATERIAL_AIR;
+            changed = nm != m;
+        }
+        const unsigned aw = __ballot_sync(FULL, air), cw = __ballot_sync(FULL, changed);
+        if (lane == 0) {
+            air_w[warp] = aw;
+            chg_w[warp] = cw;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            A[y] = make_uint4(air_w[0], air_w[1], air_w[2], 0u);
+            X[y] = make_uint4(chg_w[0], chg_w[1], chg_w[2], 0u);
+        }
+        __syncthreads();
     }
-    const uint16_t plain = w & CORNER_PLAIN_SOLID;
-    *cw = (uint16_t)(nm | plain | (nm != m ? CORNER_CHANGED : 0));
 }
 
 // ---------------------------------------------------------------------------
@@ -441,7 +504,7 @@ template <int VPC>
 __global__ void __launch_bounds__(1024) k_prune_edges(BatchPtrs b) {
     using G = Geo<VPC>;
     __shared__ int sm[1024 / 32 + 1];
-    const uint16_t* cw = b.corners;
+    const uint4* X = plane_ptr<VPC>(b, 0, 2);
     const int n = b.prev_count;
     int base = 0;
     for (int r = 0; r < n; r += 1024) {
@@ -452,11 +515,11 @@ __global__ void __launch_bounds__(1024) k_prune_edges(BatchPtrs b) {
             key = b.prev_keys[i];
             const int a = key & 3, h = key >> 2;
             const int x = h & G::MASK, y = (h >> G::SHIFT) & G::MASK, z = (h >> (2 * G::SHIFT)) & G::MASK;
-            const int L = x + G::FD * y + G::FD * G::FD * z;
-            const int coord = a == 0 ? x : a == 1 ? y : z;
-            const int stride = a == 0 ? 1 : a == 1 ? G::FD : G::FD * G::FD;
-            const bool touched = (L < G::F && (cw[L] & CORNER_CHANGED)) ||
-                                 (coord + 1 < G::FD && L + stride < G::F && (cw[L + stride] & CORNER_CHANGED));
+            const int row = y + G::FD * z;
+            bool touched = bit4(X[row], x);
+            if (a == 0 && x + 1 < G::FD) touched = touched || bit4(X[row], x + 1);
+            if (a == 1 && y + 1 < G::FD) touched = touched || bit4(X[row + 1], x);
+            if (a == 2 && z + 1 < G::FD) touched = touched || bit4(X[row + G::FD], x);
             keep = touched ? 0 : 1;
         }
         int total;
@@ -472,37 +535,54 @@ __global__ void __launch_bounds__(1024) k_prune_edges(BatchPtrs b) {
 }
 
 // ---------------------------------------------------------------------------
-// stage 3-5: field edges.  For field point q and axis a:
-//   plain-kept = q in the hermite grid, the plain field changes sign along a,
+// stage 3-5: field edges, one thread per field row.  For point q, axis a:
+//   plain-kept = q in the hermite grid, the plain field changes sign along a
 //                and no CSG-changed corner touches the edge;
-//   created    = the edge is touched (FindUpdatedEdges) and the final
-//                materials change sign along it (FilterValidEdges, with the
-//                PARANOID linear-index guard).
-// Returns plain bits 0-2 and created bits 3-5.
+//   created    = the edge is touched (FindUpdatedEdges: a changed end point,
+//                the far end only when it is a real field point) and the
+//                final materials change sign along it (FilterValidEdges,
+//                reading the linear successor with the PARANOID guard).
 // ---------------------------------------------------------------------------
 
+struct RowEdges {
+    uint4 kept[3];
+    uint4 created[3];
+};
+
 template <int VPC>
-__device__ __forceinline__ int edge_flags(const uint16_t* __restrict__ cw, int L, bool plain_class) {
+__device__ __forceinline__ RowEdges row_edges(const BatchPtrs& b, int c, int row) {
     using G = Geo<VPC>;
-    const int x = L % G::FD, y = (L / G::FD) % G::FD, z = L / (G::FD * G::FD);
-    const uint16_t w0 = cw[L];
-    const bool herm = plain_class && x < G::HD && y < G::HD && z < G::HD;
-    const bool air0 = (w0 & 0xff) == MATERIAL_AIR;
-    int flags = 0;
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-        const int stride = a == 0 ? 1 : a == 1 ? G::FD : G::FD * G::FD;
-        const int coord = a == 0 ? x : a == 1 ? y : z;
-        const int L1 = L + stride;
-        const bool inb = coord + 1 < G::FD;
-        const uint16_t w1 = L1 < G::F ? cw[L1] : (uint16_t)MATERIAL_AIR;
-        const bool touched = (w0 & CORNER_CHANGED) || (inb && (w1 & CORNER_CHANGED));
-        const bool plain_sc = herm && ((w0 ^ w1) & CORNER_PLAIN_SOLID);
-        const bool air1 = (w1 & 0xff) == MATERIAL_AIR;
-        if (plain_sc && !touched) flags |= 1 << a;
-        if (touched && air0 != air1) flags |= 8 << a;
+    constexpr int R = G::FD * G::FD;
+    const int y = row % G::FD, z = row / G::FD;
+    const uint4* P = plane_ptr<VPC>(b, c, 0);
+    const uint4* A = plane_ptr<VPC>(b, c, 1);
+    const uint4* X = plane_ptr<VPC>(b, c, 2);
+    const uint4 V = low_bits(G::FD);
+    const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+    const uint4 a0 = A[row], x0 = X[row];
+    const bool has_y = row + 1 < R, has_z = row + G::FD < R;
+    const uint4 a_next = has_y ? A[row + 1] : V;
+    const uint4 a_up = has_z ? A[row + G::FD] : V;
+    const uint4 x_y = (y + 1 < G::FD) ? X[row + 1] : zero;
+    const uint4 x_z = (z + 1 < G::FD) ? X[row + G::FD] : zero;
+    // final-air neighbours: x + 1 (linear successor at x = FD-1), y + 1, z + 1
+    uint4 ax = shr1(a0);
+    if (bit4(a_next, 0)) ax = or4(ax, xor4(low_bits(G::FD), low_bits(G::FD - 1)));
+    const uint4 t0 = or4(x0, shr1(x0)), t1 = or4(x0, x_y), t2 = or4(x0, x_z);
+    RowEdges e;
+    e.created[0] = and4(and4(t0, xor4(a0, ax)), V);
+    e.created[1] = and4(and4(t1, xor4(a0, a_next)), V);
+    e.created[2] = and4(and4(t2, xor4(a0, a_up)), V);
+    if (b.plain_class && y < G::HD && z < G::HD) {
+        const uint4 H = low_bits(G::HD);
+        const uint4 p0 = P[row];
+        e.kept[0] = and4(and4(H, xor4(p0, shr1(p0))), not4(t0));
+        e.kept[1] = and4(and4(H, xor4(p0, P[row + 1])), not4(t1));
+        e.kept[2] = and4(and4(H, xor4(p0, P[row + G::FD])), not4(t2));
+    } else {
+        e.kept[0] = e.kept[1] = e.kept[2] = zero;
     }
-    return flags;
+    return e;
 }
 
 template <int VPC>
@@ -510,18 +590,33 @@ __global__ void __launch_bounds__(kThreads) k_edge_count(BatchPtrs b) {
     using G = Geo<VPC>;
     __shared__ int sm[kThreads / 32 + 1];
     const int c = blockIdx.y, tile = blockIdx.x;
-    const uint16_t* cw = b.corners + (size_t)c * G::F;
+    const int row = tile * kThreads + threadIdx.x;
     int packed = 0;
-#pragma unroll 2
-    for (int r = 0; r < kTilePoints / kThreads; r++) {
-        const int L = tile * kTilePoints + r * kThreads + threadIdx.x;
-        if (L < G::F) {
-            const int f = edge_flags<VPC>(cw, L, b.plain_class != 0);
-            packed += __popc(f & 7) | (__popc(f >> 3) << 16);
-        }
+    if (row < G::FD * G::FD) {
+        const RowEdges e = row_edges<VPC>(b, c, row);
+        packed = (popc4(e.kept[0]) + popc4(e.kept[1]) + popc4(e.kept[2])) |
+                 ((popc4(e.created[0]) + popc4(e.created[1]) + popc4(e.created[2])) << 16);
     }
     const int total = block_sum<kThreads>(packed, sm);
     if (threadIdx.x == 0) b.edge_tiles[(size_t)c * G::NBE + tile] = make_int2(total & 0xffff, total >> 16);
+}
+
+// Exclusive scan over one warp; the smallest prime >= n (FindNextPrime,
+// primes.cpp:32-58: candidates 6k +- 1, trial division), 32 candidates at a time.
+__device__ __forceinline__ int warp_find_next_prime(int n) {
+    if (n <= 2) return 2;
+    if (n == 3) return 3;
+    if (n <= 5) return 5;
+    const int lane = threadIdx.x & 31;
+    const int k = n / 6;
+    const int o = (n - 6 * k) < 2 ? 1 : 5;
+    const int x0 = 6 * k + o;
+    for (int base = 0;; base += 32) {
+        const int j = base + lane;
+        const int cand = x0 + 6 * (j >> 1) + ((j & 1) ? (o == 1 ? 4 : 2) : 0);
+        const unsigned m = __ballot_sync(FULL, is_prime_d(cand));
+        if (m) return __shfl_sync(FULL, cand, __ffs(m) - 1);
+    }
 }
 
 // Single CTA: per-chunk tile offsets, per-chunk edge offsets, edge-table plan.
@@ -529,9 +624,7 @@ template <int VPC>
 __global__ void __launch_bounds__(1024) k_edge_plan(BatchPtrs b) {
     using G = Geo<VPC>;
     __shared__ int sm[1024 / 32 + 1];
-    __shared__ long long carry;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    // per-chunk: exclusive scan of the chunk's tile counts (both classes)
     for (int c = warp; c < b.n; c += 32) {
         int2* t = b.edge_tiles + (size_t)c * G::NBE;
         int cp = 0, cc = 0;
@@ -543,19 +636,19 @@ __global__ void __launch_bounds__(1024) k_edge_plan(BatchPtrs b) {
             cp += __shfl_sync(FULL, ip, 31);
             cc += __shfl_sync(FULL, ic, 31);
         }
+        // edges kept from a cached field precede the plain class
+        cp += b.cs[c].kept_edges;
+        const int e = cp + cc;
+        // Cuckoo_InitialiseTable (compute_cuckoo.cpp:53)
+        const int prime = e > 0 ? warp_find_next_prime(max((int)CUCKOO_MIN_TABLE_SIZE, e * 2)) : 0;
         if (lane == 0) {
-            // edges kept from a cached field precede the plain class
-            cp += b.cs[c].kept_edges;
             b.cs[c].plain_edges = cp;
             b.cs[c].created_edges = cc;
-            b.cs[c].num_edges = cp + cc;
-            // Cuckoo_InitialiseTable (compute_cuckoo.cpp:53)
-            const int e = cp + cc;
-            b.cs[c].edge_prime = e > 0 ? (uint32_t)find_next_prime_d(max((int)CUCKOO_MIN_TABLE_SIZE, e * 2)) : 0u;
+            b.cs[c].num_edges = e;
+            b.cs[c].edge_prime = (uint32_t)prime;
         }
     }
     __syncthreads();
-    (void)carry;
     const long long total = cta_scan(
         b.n, [&](int c) { return b.cs[c].num_edges; }, [&](int c, long long ex) { b.cs[c].edge_off = (int)ex; },
         nullptr, sm);
@@ -578,40 +671,49 @@ __global__ void __launch_bounds__(kThreads) k_edge_scatter(BatchPtrs b) {
     __shared__ int sm[kThreads / 32 + 1];
     if (b.bs->overflow) return;
     const int c = blockIdx.y, tile = blockIdx.x;
-    const uint16_t* cw = b.corners + (size_t)c * G::F;
+    const int row = tile * kThreads + threadIdx.x;
+    const bool valid = row < G::FD * G::FD;
+    RowEdges e;
+    int np = 0, nc = 0;
+    if (valid) {
+        e = row_edges<VPC>(b, c, row);
+        np = popc4(e.kept[0]) + popc4(e.kept[1]) + popc4(e.kept[2]);
+        nc = popc4(e.created[0]) + popc4(e.created[1]) + popc4(e.created[2]);
+    }
+    int total;
+    const int ex = block_exclusive<kThreads>(np | (nc << 16), total, sm);
+    if (!valid || (np | nc) == 0) return;
     const ChunkState st = b.cs[c];
     const int2 toff = b.edge_tiles[(size_t)c * G::NBE + tile];
-    int base_p = st.edge_off + st.kept_edges + toff.x;
-    int base_c = st.edge_off + st.plain_edges + toff.y;
-    for (int r = 0; r < kTilePoints / kThreads; r++) {
-        const int L = tile * kTilePoints + r * kThreads + threadIdx.x;
-        const int f = L < G::F ? edge_flags<VPC>(cw, L, b.plain_class != 0) : 0;
-        const int packed = __popc(f & 7) | (__popc(f >> 3) << 16);
-        int total;
-        const int ex = block_exclusive<kThreads>(packed, total, sm);
-        if (f) {
-            const int x = L % G::FD, y = (L / G::FD) % G::FD, z = L / (G::FD * G::FD);
-            int pp = base_p + (ex & 0xffff);
-            int pc = base_c + (ex >> 16);
+    int pp = st.edge_off + st.kept_edges + toff.x + (ex & 0xffff);
+    int pc = st.edge_off + st.plain_edges + toff.y + (ex >> 16);
+    const int y = row % G::FD, z = row / G::FD;
+    // emit in (x, axis) order: the reference's (hermite index, axis) order
+    uint4 any = or4(or4(e.kept[0], e.kept[1]), e.kept[2]);
+    while (popc4(any)) {
+        const int x = any.x ? __ffs(any.x) - 1 : any.y ? 31 + __ffs(any.y) : any.z ? 63 + __ffs(any.z) : 95 + __ffs(any.w);
 #pragma unroll
-            for (int a = 0; a < 3; a++) {
-                if (f & (1 << a)) {
-                    b.edge_keys[pp] = edge_key<VPC>(x, y, z, a);
-                    b.edge_chunk[pp] = c;
-                    pp++;
-                }
-            }
-#pragma unroll
-            for (int a = 0; a < 3; a++) {
-                if (f & (8 << a)) {
-                    b.edge_keys[pc] = edge_key<VPC>(x, y, z, a);
-                    b.edge_chunk[pc] = c;
-                    pc++;
-                }
+        for (int a = 0; a < 3; a++) {
+            if (bit4(e.kept[a], x)) {
+                b.edge_keys[pp] = edge_key<VPC>(x, y, z, a);
+                b.edge_chunk[pp] = c;
+                pp++;
             }
         }
-        base_p += total & 0xffff;
-        base_c += total >> 16;
+        any = and4(any, not4(low_bits(x + 1)));
+    }
+    any = or4(or4(e.created[0], e.created[1]), e.created[2]);
+    while (popc4(any)) {
+        const int x = any.x ? __ffs(any.x) - 1 : any.y ? 31 + __ffs(any.y) : any.z ? 63 + __ffs(any.z) : 95 + __ffs(any.w);
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            if (bit4(e.created[a], x)) {
+                b.edge_keys[pc] = edge_key<VPC>(x, y, z, a);
+                b.edge_chunk[pc] = c;
+                pc++;
+            }
+        }
+        any = and4(any, not4(low_bits(x + 1)));
     }
 }
 
@@ -744,7 +846,8 @@ __global__ void __launch_bounds__(kThreads) k_hermite(BatchPtrs b) {
 }
 
 // ---------------------------------------------------------------------------
-// stage 7-9: active voxels (FindActiveVoxels + CompactVoxels, octree.cl:142-223)
+// stage 7-9: active voxels (FindActiveVoxels + CompactVoxels, octree.cl:142-223),
+// one thread per voxel row (y, z) over the final-air plane.
 // ---------------------------------------------------------------------------
 
 // FindDominantMaterial (octree.cl:96-138)
@@ -773,19 +876,33 @@ __device__ __forceinline__ int dominant_material(int (&m)[8]) {
     return max_material;
 }
 
-// corner mask of voxel (x, y, z); bit i = corner CHILD_MIN_OFFSETS[i] is not air
+struct VoxRow {
+    uint4 s[4];    // solid rows (y,z), (y,z+1), (y+1,z), (y+1,z+1): corner bits i & 3
+    uint4 active;
+};
+
+// corner i = CHILD_MIN_OFFSETS[i] = (i >> 2, (i >> 1) & 1, i & 1)
 template <int VPC>
-__device__ __forceinline__ int voxel_corners(const uint16_t* __restrict__ cw, int x, int y, int z, int (&mats)[8]) {
+__device__ __forceinline__ VoxRow vox_row(const BatchPtrs& b, int c, int vrow) {
     using G = Geo<VPC>;
-    int corners = 0;
+    const int y = vrow % VPC, z = vrow / VPC;
+    const int r = y + G::FD * z;
+    const uint4* A = plane_ptr<VPC>(b, c, 1);
+    const uint4 V = low_bits(G::FD);
+    VoxRow v;
+    const uint4 a00 = A[r], a01 = A[r + G::FD], a10 = A[r + 1], a11 = A[r + G::FD + 1];
+    v.s[0] = and4(not4(a00), V);
+    v.s[1] = and4(not4(a01), V);
+    v.s[2] = and4(not4(a10), V);
+    v.s[3] = and4(not4(a11), V);
+    uint4 all_s = make_uint4(~0u, ~0u, ~0u, ~0u), all_a = all_s;
 #pragma unroll
-    for (int i = 0; i < 8; i++) {
-        const int cx = x + (i >> 2), cy = y + ((i >> 1) & 1), cz = z + (i & 1);
-        const int m = cw[cx + G::FD * cy + G::FD * G::FD * cz] & 0xff;
-        mats[i] = m;
-        corners |= (m == MATERIAL_AIR ? 0 : 1) << i;
+    for (int i = 0; i < 4; i++) {
+        all_s = and4(all_s, and4(v.s[i], shr1(v.s[i])));
     }
-    return corners;
+    all_a = and4(and4(and4(a00, shr1(a00)), and4(a01, shr1(a01))), and4(and4(a10, shr1(a10)), and4(a11, shr1(a11))));
+    v.active = and4(not4(or4(all_s, all_a)), low_bits(VPC));
+    return v;
 }
 
 template <int VPC>
@@ -793,17 +910,9 @@ __global__ void __launch_bounds__(kThreads) k_vox_count(BatchPtrs b) {
     using G = Geo<VPC>;
     __shared__ int sm[kThreads / 32 + 1];
     const int c = blockIdx.y, tile = blockIdx.x;
-    const uint16_t* cw = b.corners + (size_t)c * G::F;
+    const int vrow = tile * kThreads + threadIdx.x;
     int cnt = 0;
-    for (int r = 0; r < kTilePoints / kThreads; r++) {
-        const int v = tile * kTilePoints + r * kThreads + threadIdx.x;
-        if (v < G::C) {
-            const int x = v % VPC, y = (v / VPC) % VPC, z = v / (VPC * VPC);
-            int mats[8];
-            const int corners = voxel_corners<VPC>(cw, x, y, z, mats);
-            cnt += (corners != 0 && corners != 255) ? 1 : 0;
-        }
-    }
+    if (vrow < VPC * VPC) cnt = popc4(vox_row<VPC>(b, c, vrow).active);
     const int total = block_sum<kThreads>(cnt, sm);
     if (threadIdx.x == 0) b.vox_tiles[(size_t)c * G::NBV + tile] = total;
 }
@@ -817,9 +926,10 @@ __global__ void __launch_bounds__(1024) k_vox_plan(BatchPtrs b) {
         // a chunk without field edges builds no octree (compute_octree.cpp:167-171)
         int v = warp_scan_array(b.vox_tiles + (size_t)c * G::NBV, G::NBV);
         if (b.cs[c].num_edges == 0) v = 0;
+        const int prime = v > 0 ? warp_find_next_prime(max((int)CUCKOO_MIN_TABLE_SIZE, v * 2)) : 0;
         if (lane == 0) {
             b.cs[c].nodes = v;
-            b.cs[c].node_prime = v > 0 ? (uint32_t)find_next_prime_d(max((int)CUCKOO_MIN_TABLE_SIZE, v * 2)) : 0u;
+            b.cs[c].node_prime = (uint32_t)prime;
         }
     }
     __syncthreads();
@@ -849,38 +959,45 @@ __global__ void __launch_bounds__(kThreads) k_vox_scatter(BatchPtrs b) {
     __shared__ int sm[kThreads / 32 + 1];
     if (b.bs->overflow) return;
     const int c = blockIdx.y, tile = blockIdx.x;
-    const ChunkState st = b.cs[c];
+    const ChunkState& st = b.cs[c];
     if (st.nodes == 0) return;
-    const uint16_t* cw = b.corners + (size_t)c * G::F;
-    int base = st.node_off + b.vox_tiles[(size_t)c * G::NBV + tile];
-    for (int r = 0; r < kTilePoints / kThreads; r++) {
-        const int v = tile * kTilePoints + r * kThreads + threadIdx.x;
-        int corners = 0, x = 0, y = 0, z = 0;
-        int mats[8];
-        bool active = false;
-        if (v < G::C) {
-            x = v % VPC;
-            y = (v / VPC) % VPC;
-            z = v / (VPC * VPC);
-            corners = voxel_corners<VPC>(cw, x, y, z, mats);
-            active = corners != 0 && corners != 255;
-        }
-        int total;
-        const int ex = block_exclusive<kThreads>(active ? 1 : 0, total, sm);
-        if (active) {
-            int edges = 0;
+    const int vrow = tile * kThreads + threadIdx.x;
+    const bool valid = vrow < VPC * VPC;
+    VoxRow v;
+    int cnt = 0;
+    if (valid) {
+        v = vox_row<VPC>(b, c, vrow);
+        cnt = popc4(v.active);
+    }
+    int total;
+    const int ex = block_exclusive<kThreads>(cnt, total, sm);
+    if (!cnt) return;
+    int pos = st.node_off + b.vox_tiles[(size_t)c * G::NBV + tile] + ex;
+    const int y = vrow % VPC, z = vrow / VPC;
+    const uint8_t* mats = b.mats + (size_t)c * G::F;
+    uint4 act = v.active;
+    while (popc4(act)) {
+        const int x = act.x ? __ffs(act.x) - 1 : act.y ? 31 + __ffs(act.y) : 63 + __ffs(act.z);
+        int corners = 0;
+        int m[8];
 #pragma unroll
-            for (int i = 0; i < 12; i++) {
-                const int s0 = (corners >> edge_c0(i)) & 1, s1 = (corners >> edge_c1(i)) & 1;
-                edges |= (s0 != s1 ? 1 : 0) << i;
-            }
-            const int dom = dominant_material(mats);
-            const int pos = base + ex;
-            b.node_codes[pos] = code_for_position<VPC>(x, y, z);
-            b.node_info[pos] = (edges << 16) | (dom << 8) | corners;
-            b.node_chunk[pos] = c;
+        for (int i = 0; i < 8; i++) {
+            const int dx = i >> 2, dy = (i >> 1) & 1, dz = i & 1;
+            corners |= (bit4(v.s[dz | (dy << 1)], x + dx) ? 1 : 0) << i;
+            m[i] = mats[(x + dx) + G::FD * (y + dy) + G::FD * G::FD * (z + dz)];
         }
-        base += total;
+        int edges = 0;
+#pragma unroll
+        for (int i = 0; i < 12; i++) {
+            const int s0 = (corners >> edge_c0(i)) & 1, s1 = (corners >> edge_c1(i)) & 1;
+            edges |= (s0 != s1 ? 1 : 0) << i;
+        }
+        const int dom = dominant_material(m);
+        b.node_codes[pos] = code_for_position<VPC>(x, y, z);
+        b.node_info[pos] = (edges << 16) | (dom << 8) | corners;
+        b.node_chunk[pos] = c;
+        pos++;
+        act = and4(act, not4(low_bits(x + 1)));
     }
 }
 
@@ -1225,15 +1342,14 @@ cudaError_t launch_reset(const BatchPtrs& b, cudaStream_t s) {
 }
 
 cudaError_t launch_field(const BatchPtrs& b, cudaStream_t s) {
-    const int fd = b.vpc + 2;
-    dim3 grid((fd * fd + 127) / 128, b.n);
-    LVN_VPC_DISPATCH(b.vpc, (k_field<V><<<grid, 128, 0, s>>>(b)));
+    dim3 grid(b.vpc + 2, b.n);
+    LVN_VPC_DISPATCH(b.vpc, (k_field<V><<<grid, 96, 0, s>>>(b)));
     return cudaGetLastError();
 }
 
 cudaError_t launch_csg(const BatchPtrs& b, cudaStream_t s) {
-    dim3 grid((field_size(b.vpc) + kThreads - 1) / kThreads, b.n);
-    LVN_VPC_DISPATCH(b.vpc, (k_csg<V><<<grid, kThreads, 0, s>>>(b)));
+    dim3 grid(b.vpc + 2, b.n);
+    LVN_VPC_DISPATCH(b.vpc, (k_csg<V><<<grid, 96, 0, s>>>(b)));
     return cudaGetLastError();
 }
 

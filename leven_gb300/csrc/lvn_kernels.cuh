@@ -29,7 +29,8 @@ struct BatchPtrs {
     const uint8_t* perm;         // 65536 B permutation image (alpha channel)
     const float* grad;           // 16 x 4 gradient table
 
-    uint16_t* corners;           // [n][F]
+    uint8_t* mats;               // [n][F] field materials, index x + FD*y + FD*FD*z
+    uint4* planes;               // [n][3][FD*FD] bit rows: plain solid, final air, changed
     int2* edge_tiles;            // [n][NBE] (plain, created) counts, then in-chunk offsets
     int* vox_tiles;              // [n][NBV]
 
@@ -66,13 +67,15 @@ struct BatchPtrs {
     int prev_count;
 };
 
-constexpr int kTilePoints = 2048;   // dense tile (field points / voxels) per CTA
+constexpr int kRowTile = 256;       // field / voxel rows per CTA in the dense stages
+constexpr int kTilePoints = 2048;
 constexpr int kNodeTile = 256;      // sparse node tile per CTA iteration
 
 inline int field_dim(int vpc) { return vpc + 2; }
 inline int field_size(int vpc) { return (vpc + 2) * (vpc + 2) * (vpc + 2); }
-inline int edge_tiles_per_chunk(int vpc) { return (field_size(vpc) + kTilePoints - 1) / kTilePoints; }
-inline int vox_tiles_per_chunk(int vpc) { return (vpc * vpc * vpc + kTilePoints - 1) / kTilePoints; }
+inline int field_rows(int vpc) { return (vpc + 2) * (vpc + 2); }
+inline int edge_tiles_per_chunk(int vpc) { return (field_rows(vpc) + kRowTile - 1) / kRowTile; }
+inline int vox_tiles_per_chunk(int vpc) { return (vpc * vpc + kRowTile - 1) / kRowTile; }
 
 // Stage identifiers for profiling (order of execution).
 enum Stage {

@@ -36,8 +36,8 @@ constexpr int kMaxOps = LVN_NOALLOC_MAX_CSG_OPS;
 
 constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 constexpr size_t kF = (size_t)(kMaxVpc + 2) * (kMaxVpc + 2) * (kMaxVpc + 2);
-constexpr size_t kNbe = (kF + kTilePoints - 1) / kTilePoints;
-constexpr size_t kNbv = ((size_t)kMaxVpc * kMaxVpc * kMaxVpc + kTilePoints - 1) / kTilePoints;
+constexpr size_t kNbe = ((size_t)(kMaxVpc + 2) * (kMaxVpc + 2) + kRowTile - 1) / kRowTile;
+constexpr size_t kNbv = ((size_t)kMaxVpc * kMaxVpc + kRowTile - 1) / kRowTile;
 constexpr int64_t kEdgeSlots = 2 * kMaxEdges + CUCKOO_MIN_TABLE_SIZE + CUCKOO_STASH_SIZE + 512;
 constexpr int64_t kNodeSlots = 2 * kMaxNodes + CUCKOO_MIN_TABLE_SIZE + CUCKOO_STASH_SIZE + 512;
 constexpr int64_t kNodeTiles = kMaxNodes / kNodeTile + 2;
@@ -47,8 +47,10 @@ constexpr size_t OFF_DESC = 0;
 constexpr size_t OFF_CS = OFF_DESC + align256(sizeof(ChunkDesc));
 constexpr size_t OFF_BS = OFF_CS + align256(sizeof(ChunkState));
 constexpr size_t OFF_BRUSH = OFF_BS + align256(sizeof(BatchState));
-constexpr size_t OFF_CORNERS = OFF_BRUSH + align256(sizeof(Brush) * kMaxOps);
-constexpr size_t OFF_ETILES = OFF_CORNERS + align256(sizeof(uint16_t) * kF);
+constexpr size_t kRows = (size_t)(kMaxVpc + 2) * (kMaxVpc + 2);
+constexpr size_t OFF_MATS = OFF_BRUSH + align256(sizeof(Brush) * kMaxOps);
+constexpr size_t OFF_PLANES = OFF_MATS + align256(kF);
+constexpr size_t OFF_ETILES = OFF_PLANES + align256(16 * 3 * kRows);
 constexpr size_t OFF_VTILES = OFF_ETILES + align256(8 * kNbe);
 constexpr size_t OFF_CTILE = OFF_VTILES + align256(4 * kNbv);
 constexpr size_t OFF_EKEYS = OFF_CTILE + align256(4 * 2);
@@ -135,6 +137,7 @@ extern "C" int lvn_generate_chunk_mesh_noalloc(const int32_t min[3], int32_t siz
     }
     desc.op_begin = 0;
     desc.op_count = nops;
+    csg_box_for(brushes, nops, desc.off, desc.scale, vpc + 2, desc.csg_lo, desc.csg_hi);
 
     BatchPtrs b;
     std::memset(&b, 0, sizeof(b));
@@ -151,7 +154,8 @@ extern "C" int lvn_generate_chunk_mesh_noalloc(const int32_t min[3], int32_t siz
     b.cs = reinterpret_cast<ChunkState*>(base + OFF_CS);
     b.bs = reinterpret_cast<BatchState*>(base + OFF_BS);
     b.brushes = reinterpret_cast<Brush*>(base + OFF_BRUSH);
-    b.corners = reinterpret_cast<uint16_t*>(base + OFF_CORNERS);
+    b.mats = reinterpret_cast<uint8_t*>(base + OFF_MATS);
+    b.planes = reinterpret_cast<uint4*>(base + OFF_PLANES);
     b.edge_tiles = reinterpret_cast<int2*>(base + OFF_ETILES);
     b.vox_tiles = reinterpret_cast<int*>(base + OFF_VTILES);
     b.chunk_tile_off = reinterpret_cast<int*>(base + OFF_CTILE);

@@ -24,5 +24,7 @@ int stored_ops_for_chunk(const int32_t min[3], int32_t size, Brush* out, int cap
 void draw_hash_params(uint32_t* p);
 // ColourForMinLeafSize (clipmap.cpp:329-353)
 void lod_colour_for(int min_leaf_size, float c[3]);
+// Field-index box holding every point the operations can change.
+void csg_box_for(const Brush* ops, int n, const int32_t off[3], int scale, int fd, int32_t lo[3], int32_t hi[3]);
 
 }  // namespace lvn

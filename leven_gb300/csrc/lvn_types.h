@@ -20,9 +20,6 @@ constexpr int CUCKOO_STASH_SIZE = 101;
 constexpr int CUCKOO_MAX_ITERATIONS = 32;
 constexpr uint32_t CUCKOO_MIN_TABLE_SIZE = 2048u;  // compute_cuckoo.cpp:15
 
-// corner word in the field array: material | plain-solid << 8 | changed << 9
-constexpr uint16_t CORNER_PLAIN_SOLID = 1u << 8;
-constexpr uint16_t CORNER_CHANGED = 1u << 9;
 
 typedef lvn_density_params DensityParams;
 
@@ -48,6 +45,8 @@ struct ChunkDesc {
     float colour[3];     // ColourForMinLeafSize(size / 256)
     int32_t op_begin;    // into the batch brush array
     int32_t op_count;
+    int32_t csg_lo[3];   // field-index box that holds every point the operations can change
+    int32_t csg_hi[3];
     int32_t pad[3];
     uint32_t edge_params[CUCKOO_HASH_FN_COUNT * 2];
     uint32_t node_params[CUCKOO_HASH_FN_COUNT * 2];
