@@ -285,7 +285,7 @@ struct lvn_meshgen {
 
     // pools
     DevBuf desc, cs, bs, brushes, mats, planes, edge_tiles, vox_tiles;
-    DevBuf edge_keys, edge_chunk, edge_info, node_codes, node_info, node_chunk;
+    DevBuf edge_keys, edge_chunk, edge_info, edge_work, node_codes, node_info, node_chunk;
     DevBuf edge_slots, node_slots, quad_scratch, node_tile_counts, chunk_tile_off;
     DevBuf vertices, triangles, seams;
     HostBuf h_desc, h_brushes, h_cs, h_bs;
@@ -323,7 +323,7 @@ int ensure_pools(lvn_meshgen* m, int n, Capacity want) {
     LVN_CK(m->bs.ensure(sizeof(BatchState)));
     LVN_CK(m->mats.ensure((size_t)F * n));
     LVN_CK(m->planes.ensure(sizeof(uint4) * 3 * (size_t)field_rows(m->vpc) * n));
-    LVN_CK(m->edge_tiles.ensure(sizeof(int2) * (size_t)edge_tiles_per_chunk(m->vpc) * n));
+    LVN_CK(m->edge_tiles.ensure(sizeof(int4) * (size_t)edge_tiles_per_chunk(m->vpc) * n));
     LVN_CK(m->vox_tiles.ensure(sizeof(int) * (size_t)vox_tiles_per_chunk(m->vpc) * n));
     LVN_CK(m->chunk_tile_off.ensure(sizeof(int) * (size_t)(n + 1)));
     LVN_CK(m->h_desc.ensure(sizeof(ChunkDesc) * n));
@@ -333,6 +333,7 @@ int ensure_pools(lvn_meshgen* m, int n, Capacity want) {
         LVN_CK(m->edge_keys.ensure(sizeof(int32_t) * ecap));
         LVN_CK(m->edge_chunk.ensure(sizeof(int32_t) * ecap));
         LVN_CK(m->edge_info.ensure(sizeof(float4) * ecap));
+        LVN_CK(m->edge_work.ensure(sizeof(int32_t) * ecap));
         m->ecap = ecap;
     }
     const int64_t eslots = 2 * m->ecap + (int64_t)n * (CUCKOO_MIN_TABLE_SIZE + CUCKOO_STASH_SIZE + 512);
@@ -383,6 +384,7 @@ BatchPtrs make_ptrs(lvn_meshgen* m, int n) {
     b.vpc = m->vpc;
     b.crossing_mode = m->crossing_mode;
     b.plain_class = 1;
+    b.derive_mats = 1;
     b.num_sms = g.num_sms;
     b.density = g.density;
     b.default_material = g.default_material;
@@ -394,11 +396,12 @@ BatchPtrs make_ptrs(lvn_meshgen* m, int n) {
     b.grad = g.grad.as<float>();
     b.mats = m->mats.as<uint8_t>();
     b.planes = m->planes.as<uint4>();
-    b.edge_tiles = m->edge_tiles.as<int2>();
+    b.edge_tiles = m->edge_tiles.as<int4>();
     b.vox_tiles = m->vox_tiles.as<int>();
     b.edge_keys = m->edge_keys.as<int32_t>();
     b.edge_chunk = m->edge_chunk.as<int32_t>();
     b.edge_info = m->edge_info.as<float4>();
+    b.edge_work = m->edge_work.as<int32_t>();
     b.ecap = m->ecap;
     b.node_codes = m->node_codes.as<uint32_t>();
     b.node_info = m->node_info.as<int32_t>();
@@ -461,6 +464,7 @@ int enqueue_octree_stages(lvn_meshgen* m, const BatchPtrs& b) {
     LVN_STAGE(ST_VOX_COUNT, launch_vox_count);
     LVN_STAGE(ST_VOX_PLAN, launch_vox_plan);
     LVN_STAGE(ST_VOX_SCATTER, launch_vox_scatter);
+    LVN_STAGE(ST_PRIMES, launch_primes);
     LVN_STAGE(ST_HASH_FILL, launch_hash_fill);
     LVN_STAGE(ST_EDGE_INSERT, launch_edge_insert);
     LVN_STAGE(ST_LEAF, launch_leaf);
@@ -801,6 +805,7 @@ int mesh_from_field(lvn_meshgen* m, const int32_t min[3], int32_t size, FieldEnt
         LVN_CK(cudaMemcpyAsync(m->cs.p, m->h_cs.p, sizeof(cs), cudaMemcpyHostToDevice, m->stream));
         LVN_CK(cudaMemcpyAsync(m->bs.p, m->h_bs.p, sizeof(bs), cudaMemcpyHostToDevice, m->stream));
         BatchPtrs b = make_ptrs(m, 1);
+        b.derive_mats = 0;  // the cached field may hold CSG materials
         if ((rc = enqueue_octree_stages(m, b))) return rc;
         if ((rc = read_states(m, 1))) return rc;
         const BatchState& hb = *m->h_bs.as<BatchState>();
@@ -951,7 +956,7 @@ void lvn_meshgen_destroy(lvn_meshgen* m) {
     if (!m) return;
     cudaStreamSynchronize(m->stream);
     DevBuf* bufs[] = {&m->desc,       &m->cs,         &m->bs,         &m->brushes,      &m->mats,  &m->planes,
-                      &m->edge_tiles, &m->vox_tiles,  &m->edge_keys,  &m->edge_chunk,   &m->edge_info,
+                      &m->edge_tiles, &m->vox_tiles,  &m->edge_keys,  &m->edge_chunk,   &m->edge_info, &m->edge_work,
                       &m->node_codes, &m->node_info,  &m->node_chunk, &m->edge_slots,   &m->node_slots,
                       &m->quad_scratch, &m->node_tile_counts, &m->chunk_tile_off, &m->vertices, &m->triangles,
                       &m->seams};

@@ -182,15 +182,30 @@ __device__ bool is_prime_d(int x) {
 // cuckoo hash (cuckoo.cl:1-105)
 // ---------------------------------------------------------------------------
 
-__device__ __forceinline__ uint32_t cuckoo_hash(uint32_t key, uint32_t a, uint32_t b, uint32_t mod) {
-    const unsigned long long h = (uint32_t)(a * key);  // 32-bit product (cuckoo.cl:21)
-    return (uint32_t)(((h + b) % 4294967291ull) % mod);
+// ((a * key mod 2^32) + b) mod 4294967291 mod m (cuckoo.cl:18-24).  h + b is
+// below 2 * 4294967291, so the first remainder is one conditional subtract;
+// the second uses magic = floor((2^32 - 1) / m), whose quotient estimate is
+// at most two below the true quotient.
+__device__ __forceinline__ uint32_t cuckoo_hash(uint32_t key, uint32_t a, uint32_t b, uint32_t mod, uint32_t magic) {
+    unsigned long long s = (unsigned long long)(uint32_t)(a * key) + b;
+    if (s >= 4294967291ull) s -= 4294967291ull;
+    const uint32_t x = (uint32_t)s;
+    uint32_t r = x - __umulhi(x, magic) * mod;
+    if (r >= mod) r -= mod;
+    if (r >= mod) r -= mod;
+    return r;
+}
+__device__ __forceinline__ uint32_t stash_hash(uint32_t key, uint32_t a, uint32_t b) {
+    unsigned long long s = (unsigned long long)(uint32_t)(a * key) + b;
+    if (s >= 4294967291ull) s -= 4294967291ull;
+    return (uint32_t)s % (uint32_t)CUCKOO_STASH_SIZE;
 }
 
 struct HashView {
     const unsigned long long* table;
     const unsigned long long* stash;
     uint32_t prime;
+    uint32_t magic;
     int stash_used;
     uint32_t p[10];
 
@@ -198,11 +213,11 @@ struct HashView {
     __device__ __forceinline__ uint32_t find(uint32_t key) const {
 #pragma unroll
         for (int i = 0; i < CUCKOO_STASH_HASH_INDEX; i++) {
-            const unsigned long long e = table[cuckoo_hash(key, p[2 * i], p[2 * i + 1], prime)];
+            const unsigned long long e = table[cuckoo_hash(key, p[2 * i], p[2 * i + 1], prime, magic)];
             if ((uint32_t)e == key) return (uint32_t)(e >> 32);
         }
         if (stash_used) {
-            const unsigned long long e = stash[cuckoo_hash(key, p[8], p[9], CUCKOO_STASH_SIZE)];
+            const unsigned long long e = stash[stash_hash(key, p[8], p[9])];
             if ((uint32_t)e == key) return (uint32_t)(e >> 32);
         }
         return ~0u;
@@ -212,24 +227,24 @@ struct HashView {
 // Cuckoo_InsertKeys (cuckoo.cl:26-71) for one key.  Returns 0 on success,
 // 1 when the key went to the stash, -1 when the stash slot was taken.
 __device__ __forceinline__ int cuckoo_insert(unsigned long long* table, unsigned long long* stash, uint32_t prime,
-                                             const uint32_t* p, uint32_t key, uint32_t value) {
+                                             uint32_t magic, const uint32_t* p, uint32_t key, uint32_t value) {
     unsigned long long entry = ((unsigned long long)value << 32) | key;
-    uint32_t h = cuckoo_hash(key, p[0], p[1], prime);
+    uint32_t h = cuckoo_hash(key, p[0], p[1], prime, magic);
     for (int i = 0; i < CUCKOO_MAX_ITERATIONS; i++) {
         entry = atomicExch(&table[h], entry);
         if (entry == CUCKOO_EMPTY) return 0;
         key = (uint32_t)entry;
-        const uint32_t h0 = cuckoo_hash(key, p[0], p[1], prime);
-        const uint32_t h1 = cuckoo_hash(key, p[2], p[3], prime);
-        const uint32_t h2 = cuckoo_hash(key, p[4], p[5], prime);
-        const uint32_t h3 = cuckoo_hash(key, p[6], p[7], prime);
+        const uint32_t h0 = cuckoo_hash(key, p[0], p[1], prime, magic);
+        const uint32_t h1 = cuckoo_hash(key, p[2], p[3], prime, magic);
+        const uint32_t h2 = cuckoo_hash(key, p[4], p[5], prime, magic);
+        const uint32_t h3 = cuckoo_hash(key, p[6], p[7], prime, magic);
         if (h == h0) h = h1;
         else if (h == h1) h = h2;
         else if (h == h2) h = h3;
         else if (h == h3) h = h0;
     }
     key = (uint32_t)entry;
-    const uint32_t hs = cuckoo_hash(key, p[8], p[9], CUCKOO_STASH_SIZE);
+    const uint32_t hs = stash_hash(key, p[8], p[9]);
     const unsigned long long prev = atomicCAS(&stash[hs], CUCKOO_EMPTY, entry);
     return prev == CUCKOO_EMPTY ? 1 : -1;
 }
@@ -400,7 +415,6 @@ template <int VPC>
 __global__ void __launch_bounds__(96) k_field(BatchPtrs b) {
     using G = Geo<VPC>;
     __shared__ float sg[64];
-    __shared__ unsigned words[3];
     if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
     __syncthreads();
     const int c = blockIdx.y, z = blockIdx.x;
@@ -414,11 +428,13 @@ __global__ void __launch_bounds__(96) k_field(BatchPtrs b) {
     const float h = valid ? nz.height(b.density, wx, wz) : 0.f;
     const int dm = b.default_material;
     uint8_t* mats = b.mats + (size_t)c * G::F + x + G::FD * G::FD * z;
-    uint4* P = plane_ptr<VPC>(b, c, 0) + G::FD * z;
-    uint4* A = plane_ptr<VPC>(b, c, 1) + G::FD * z;
-    uint4* X = plane_ptr<VPC>(b, c, 2) + G::FD * z;
+    // word `warp` of each row of the three planes (rows are 4 words)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint4 V = low_bits(G::FD);
+    uint32_t* P = reinterpret_cast<uint32_t*>(plane_ptr<VPC>(b, c, 0) + G::FD * z);
+    uint32_t* A = reinterpret_cast<uint32_t*>(plane_ptr<VPC>(b, c, 1) + G::FD * z);
+    uint32_t* X = reinterpret_cast<uint32_t*>(plane_ptr<VPC>(b, c, 2) + G::FD * z);
+    const uint4 V4 = low_bits(G::FD);
+    const uint32_t vmask = warp == 0 ? V4.x : warp == 1 ? V4.y : V4.z;
     for (int y = 0; y < G::FD; y++) {
         bool solid = false;
         if (valid) {
@@ -429,15 +445,15 @@ __global__ void __launch_bounds__(96) k_field(BatchPtrs b) {
             solid = m != MATERIAL_AIR;
         }
         const unsigned s = __ballot_sync(FULL, solid);
-        if (lane == 0) words[warp] = s;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            const uint4 p = make_uint4(words[0], words[1], words[2], 0u);
-            P[y] = p;
-            A[y] = and4(not4(p), V);
-            X[y] = make_uint4(0u, 0u, 0u, 0u);
+        if (lane == 0) {
+            P[4 * y + warp] = s;
+            A[4 * y + warp] = ~s & vmask;
+            X[4 * y + warp] = 0u;
+        } else if (lane == 1 && warp == 0) {
+            P[4 * y + 3] = 0u;
+            A[4 * y + 3] = 0u;
+            X[4 * y + 3] = 0u;
         }
-        __syncthreads();
     }
 }
 
@@ -450,7 +466,6 @@ __global__ void __launch_bounds__(96) k_field(BatchPtrs b) {
 template <int VPC>
 __global__ void __launch_bounds__(96) k_csg(BatchPtrs b) {
     using G = Geo<VPC>;
-    __shared__ unsigned air_w[3], chg_w[3];
     const int c = blockIdx.y, z = blockIdx.x;
     const ChunkDesc& d = b.desc[c];
     const int nops = d.op_count;
@@ -459,9 +474,9 @@ __global__ void __launch_bounds__(96) k_csg(BatchPtrs b) {
     const bool inx = x < G::FD && x >= d.csg_lo[0] && x <= d.csg_hi[0];
     const Brush* ops = b.brushes + d.op_begin;
     uint8_t* mats = b.mats + (size_t)c * G::F + G::FD * G::FD * z;
-    uint4* A = plane_ptr<VPC>(b, c, 1) + G::FD * z;
-    uint4* X = plane_ptr<VPC>(b, c, 2) + G::FD * z;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t* A = reinterpret_cast<uint32_t*>(plane_ptr<VPC>(b, c, 1) + G::FD * z);
+    uint32_t* X = reinterpret_cast<uint32_t*>(plane_ptr<VPC>(b, c, 2) + G::FD * z);
     const float wx = (float)(d.off[0] + d.scale * x);
     const float wz = (float)(d.off[2] + d.scale * z);
     for (int y = d.csg_lo[1]; y <= d.csg_hi[1]; y++) {
@@ -482,15 +497,9 @@ __global__ void __launch_bounds__(96) k_csg(BatchPtrs b) {
         }
         const unsigned aw = __ballot_sync(FULL, air), cw = __ballot_sync(FULL, changed);
         if (lane == 0) {
-            air_w[warp] = aw;
-            chg_w[warp] = cw;
+            A[4 * y + warp] = aw;
+            X[4 * y + warp] = cw;
         }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            A[y] = make_uint4(air_w[0], air_w[1], air_w[2], 0u);
-            X[y] = make_uint4(chg_w[0], chg_w[1], chg_w[2], 0u);
-        }
-        __syncthreads();
     }
 }
 
@@ -591,14 +600,15 @@ __global__ void __launch_bounds__(kThreads) k_edge_count(BatchPtrs b) {
     __shared__ int sm[kThreads / 32 + 1];
     const int c = blockIdx.y, tile = blockIdx.x;
     const int row = tile * kThreads + threadIdx.x;
-    int packed = 0;
+    int plain = 0, created = 0;
     if (row < G::FD * G::FD) {
         const RowEdges e = row_edges<VPC>(b, c, row);
-        packed = (popc4(e.kept[0]) + popc4(e.kept[1]) + popc4(e.kept[2])) |
-                 ((popc4(e.created[0]) + popc4(e.created[1]) + popc4(e.created[2])) << 16);
+        plain = (popc4(e.kept[0]) + popc4(e.kept[2])) | (popc4(e.kept[1]) << 16);
+        created = popc4(e.created[0]) + popc4(e.created[1]) + popc4(e.created[2]);
     }
-    const int total = block_sum<kThreads>(packed, sm);
-    if (threadIdx.x == 0) b.edge_tiles[(size_t)c * G::NBE + tile] = make_int2(total & 0xffff, total >> 16);
+    const int tp = block_sum<kThreads>(plain, sm);
+    const int tc = block_sum<kThreads>(created, sm);
+    if (threadIdx.x == 0) b.edge_tiles[(size_t)c * G::NBE + tile] = make_int4(tp & 0xffff, tp >> 16, tc, 0);
 }
 
 // Exclusive scan over one warp; the smallest prime >= n (FindNextPrime,
@@ -619,6 +629,30 @@ __device__ __forceinline__ int warp_find_next_prime(int n) {
     }
 }
 
+// Slots reserved for a chunk's cuckoo table of k keys: its prime
+// (nextprime(max(2048, 2k)), compute_cuckoo.cpp:53) is below that bound plus
+// 512 (prime gaps below 2^31 are under 300), then the 101-entry stash.
+__device__ __forceinline__ int table_slot_bound(int k) {
+    return k > 0 ? max((int)CUCKOO_MIN_TABLE_SIZE, 2 * k) + 512 + CUCKOO_STASH_SIZE : 0;
+}
+
+// The two cuckoo primes of every chunk, one warp per chunk.
+__global__ void __launch_bounds__(256) k_primes(BatchPtrs b) {
+    if (b.bs->overflow) return;
+    const int c = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (c >= b.n) return;
+    ChunkState& st = b.cs[c];
+    const int e = st.num_edges, v = st.nodes;
+    const int pe = e > 0 ? warp_find_next_prime(max((int)CUCKOO_MIN_TABLE_SIZE, 2 * e)) : 0;
+    const int pv = v > 0 ? warp_find_next_prime(max((int)CUCKOO_MIN_TABLE_SIZE, 2 * v)) : 0;
+    if ((threadIdx.x & 31) == 0) {
+        st.edge_prime = (uint32_t)pe;
+        st.node_prime = (uint32_t)pv;
+        st.edge_magic = pe ? 0xffffffffu / (uint32_t)pe : 0u;
+        st.node_magic = pv ? 0xffffffffu / (uint32_t)pv : 0u;
+    }
+}
+
 // Single CTA: per-chunk tile offsets, per-chunk edge offsets, edge-table plan.
 template <int VPC>
 __global__ void __launch_bounds__(1024) k_edge_plan(BatchPtrs b) {
@@ -626,35 +660,50 @@ __global__ void __launch_bounds__(1024) k_edge_plan(BatchPtrs b) {
     __shared__ int sm[1024 / 32 + 1];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int c = warp; c < b.n; c += 32) {
-        int2* t = b.edge_tiles + (size_t)c * G::NBE;
-        int cp = 0, cc = 0;
+        int4* t = b.edge_tiles + (size_t)c * G::NBE;
+        int cx = 0, cy = 0, cc = 0;
         for (int base = 0; base < G::NBE; base += 32) {
             const int i = base + lane;
-            const int2 v = i < G::NBE ? t[i] : make_int2(0, 0);
-            const int ip = warp_inclusive(v.x), ic = warp_inclusive(v.y);
-            if (i < G::NBE) t[i] = make_int2(cp + ip - v.x, cc + ic - v.y);
-            cp += __shfl_sync(FULL, ip, 31);
+            const int4 v = i < G::NBE ? t[i] : make_int4(0, 0, 0, 0);
+            const int ix = warp_inclusive(v.x), iy = warp_inclusive(v.y), ic = warp_inclusive(v.z);
+            if (i < G::NBE) t[i] = make_int4(cx + ix - v.x, cy + iy - v.y, cc + ic - v.z, 0);
+            cx += __shfl_sync(FULL, ix, 31);
+            cy += __shfl_sync(FULL, iy, 31);
             cc += __shfl_sync(FULL, ic, 31);
         }
-        // edges kept from a cached field precede the plain class
-        cp += b.cs[c].kept_edges;
-        const int e = cp + cc;
-        // Cuckoo_InitialiseTable (compute_cuckoo.cpp:53)
-        const int prime = e > 0 ? warp_find_next_prime(max((int)CUCKOO_MIN_TABLE_SIZE, e * 2)) : 0;
         if (lane == 0) {
+            // edges kept from a cached field precede the plain class
+            const int cp = b.cs[c].kept_edges + cx + cy;
+            b.cs[c].edges_xz = cx;
+            b.cs[c].edges_y = cy;
             b.cs[c].plain_edges = cp;
             b.cs[c].created_edges = cc;
-            b.cs[c].num_edges = e;
-            b.cs[c].edge_prime = (uint32_t)prime;
+            b.cs[c].num_edges = cp + cc;
         }
     }
     __syncthreads();
     const long long total = cta_scan(
         b.n, [&](int c) { return b.cs[c].num_edges; }, [&](int c, long long ex) { b.cs[c].edge_off = (int)ex; },
         nullptr, sm);
+    // table slots are reserved for the largest prime the chunk can need; the
+    // prime itself is found later by k_primes
     const long long slots = cta_scan(
-        b.n, [&](int c) { return b.cs[c].edge_prime ? (int)b.cs[c].edge_prime + CUCKOO_STASH_SIZE : 0; },
+        b.n, [&](int c) { return table_slot_bound(b.cs[c].num_edges); },
         [&](int c, long long ex) { b.cs[c].edge_table_off = (int)ex; }, nullptr, sm);
+    const long long txz = cta_scan(
+        b.n, [&](int c) { return b.cs[c].edges_xz; }, [&](int c, long long ex) { b.cs[c].wl_xz_off = (int)ex; },
+        nullptr, sm);
+    const long long ty = cta_scan(
+        b.n, [&](int c) { return b.cs[c].edges_y; }, [&](int c, long long ex) { b.cs[c].wl_y_off = (int)ex; },
+        nullptr, sm);
+    const long long tcr = cta_scan(
+        b.n, [&](int c) { return b.cs[c].created_edges; }, [&](int c, long long ex) { b.cs[c].wl_c_off = (int)ex; },
+        nullptr, sm);
+    if (threadIdx.x == 0) {
+        b.bs->total_xz = (int)txz;
+        b.bs->total_y = (int)ty;
+        b.bs->total_created = (int)tcr;
+    }
     if (threadIdx.x == 0) {
         b.bs->total_edges = (int)total;
         b.bs->total_edge_slots = slots;
@@ -674,19 +723,26 @@ __global__ void __launch_bounds__(kThreads) k_edge_scatter(BatchPtrs b) {
     const int row = tile * kThreads + threadIdx.x;
     const bool valid = row < G::FD * G::FD;
     RowEdges e;
-    int np = 0, nc = 0;
+    int nxz = 0, ny = 0, nc = 0;
     if (valid) {
         e = row_edges<VPC>(b, c, row);
-        np = popc4(e.kept[0]) + popc4(e.kept[1]) + popc4(e.kept[2]);
+        nxz = popc4(e.kept[0]) + popc4(e.kept[2]);
+        ny = popc4(e.kept[1]);
         nc = popc4(e.created[0]) + popc4(e.created[1]) + popc4(e.created[2]);
     }
-    int total;
-    const int ex = block_exclusive<kThreads>(np | (nc << 16), total, sm);
-    if (!valid || (np | nc) == 0) return;
+    int tp, tc;
+    const int exp = block_exclusive<kThreads>(nxz | (ny << 16), tp, sm);
+    const int exc = block_exclusive<kThreads>(nc, tc, sm);
+    if (!valid || (nxz | ny | nc) == 0) return;
     const ChunkState st = b.cs[c];
-    const int2 toff = b.edge_tiles[(size_t)c * G::NBE + tile];
-    int pp = st.edge_off + st.kept_edges + toff.x + (ex & 0xffff);
-    int pc = st.edge_off + st.plain_edges + toff.y + (ex >> 16);
+    const BatchState& bs = *b.bs;
+    const int4 toff = b.edge_tiles[(size_t)c * G::NBE + tile];
+    const int exz = exp & 0xffff, ey = exp >> 16;
+    int pp = st.edge_off + st.kept_edges + toff.x + toff.y + exz + ey;
+    int pc = st.edge_off + st.plain_edges + toff.z + exc;
+    int wxz = st.wl_xz_off + toff.x + exz;
+    int wy = bs.total_xz + st.wl_y_off + toff.y + ey;
+    int wc = bs.total_xz + bs.total_y + st.wl_c_off + toff.z + exc;
     const int y = row % G::FD, z = row / G::FD;
     // emit in (x, axis) order: the reference's (hermite index, axis) order
     uint4 any = or4(or4(e.kept[0], e.kept[1]), e.kept[2]);
@@ -697,6 +753,8 @@ __global__ void __launch_bounds__(kThreads) k_edge_scatter(BatchPtrs b) {
             if (bit4(e.kept[a], x)) {
                 b.edge_keys[pp] = edge_key<VPC>(x, y, z, a);
                 b.edge_chunk[pp] = c;
+                if (a == 1) b.edge_work[wy++] = pp;
+                else b.edge_work[wxz++] = pp;
                 pp++;
             }
         }
@@ -710,6 +768,7 @@ __global__ void __launch_bounds__(kThreads) k_edge_scatter(BatchPtrs b) {
             if (bit4(e.created[a], x)) {
                 b.edge_keys[pc] = edge_key<VPC>(x, y, z, a);
                 b.edge_chunk[pc] = c;
+                b.edge_work[wc++] = pc;
                 pc++;
             }
         }
@@ -833,15 +892,16 @@ __global__ void __launch_bounds__(kThreads) k_hermite(BatchPtrs b) {
     __syncthreads();
     if (b.bs->overflow) return;
     const Noise nz{b.perm, sg};
-    const int total = b.bs->total_edges;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    // work list segments: plain x/z edges, plain y edges, CSG-created edges, so
+    // that a warp's 32 edges take the same path
+    const int nplain = b.bs->total_xz + b.bs->total_y;
+    const int total = nplain + b.bs->total_created;
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < total; w += gridDim.x * blockDim.x) {
+        const int i = b.edge_work[w];
         const int c = b.edge_chunk[i];
         const ChunkDesc& d = b.desc[c];
         const int key = b.edge_keys[i];
-        const ChunkState& st = b.cs[c];
-        const bool created = (i - st.edge_off) >= st.plain_edges;
-        if (created) b.edge_info[i] = hermite_brush<VPC>(b, d, key);
-        else if ((i - st.edge_off) >= st.kept_edges) b.edge_info[i] = hermite_density<VPC>(b, nz, d, key);
+        b.edge_info[i] = w >= nplain ? hermite_brush<VPC>(b, d, key) : hermite_density<VPC>(b, nz, d, key);
     }
 }
 
@@ -926,17 +986,13 @@ __global__ void __launch_bounds__(1024) k_vox_plan(BatchPtrs b) {
         // a chunk without field edges builds no octree (compute_octree.cpp:167-171)
         int v = warp_scan_array(b.vox_tiles + (size_t)c * G::NBV, G::NBV);
         if (b.cs[c].num_edges == 0) v = 0;
-        const int prime = v > 0 ? warp_find_next_prime(max((int)CUCKOO_MIN_TABLE_SIZE, v * 2)) : 0;
-        if (lane == 0) {
-            b.cs[c].nodes = v;
-            b.cs[c].node_prime = (uint32_t)prime;
-        }
+        if (lane == 0) b.cs[c].nodes = v;
     }
     __syncthreads();
     const long long total = cta_scan(
         b.n, [&](int c) { return b.cs[c].nodes; }, [&](int c, long long ex) { b.cs[c].node_off = (int)ex; }, nullptr, sm);
     const long long slots = cta_scan(
-        b.n, [&](int c) { return b.cs[c].node_prime ? (int)b.cs[c].node_prime + CUCKOO_STASH_SIZE : 0; },
+        b.n, [&](int c) { return table_slot_bound(b.cs[c].nodes); },
         [&](int c, long long ex) { b.cs[c].node_table_off = (int)ex; }, nullptr, sm);
     const long long tiles = cta_scan(
         b.n, [&](int c) { return (b.cs[c].nodes + kNodeTile - 1) / kNodeTile; },
@@ -975,6 +1031,10 @@ __global__ void __launch_bounds__(kThreads) k_vox_scatter(BatchPtrs b) {
     int pos = st.node_off + b.vox_tiles[(size_t)c * G::NBV + tile] + ex;
     const int y = vrow % VPC, z = vrow / VPC;
     const uint8_t* mats = b.mats + (size_t)c * G::F;
+    // a fresh field without CSG holds the default material or AIR only, so the
+    // corner materials follow from the solid bits
+    const bool derive = b.derive_mats && b.desc[c].op_count == 0;
+    const int dm = b.default_material;
     uint4 act = v.active;
     while (popc4(act)) {
         const int x = act.x ? __ffs(act.x) - 1 : act.y ? 31 + __ffs(act.y) : 63 + __ffs(act.z);
@@ -983,8 +1043,9 @@ __global__ void __launch_bounds__(kThreads) k_vox_scatter(BatchPtrs b) {
 #pragma unroll
         for (int i = 0; i < 8; i++) {
             const int dx = i >> 2, dy = (i >> 1) & 1, dz = i & 1;
-            corners |= (bit4(v.s[dz | (dy << 1)], x + dx) ? 1 : 0) << i;
-            m[i] = mats[(x + dx) + G::FD * (y + dy) + G::FD * G::FD * (z + dz)];
+            const bool solid = bit4(v.s[dz | (dy << 1)], x + dx);
+            corners |= (solid ? 1 : 0) << i;
+            m[i] = derive ? (solid ? dm : MATERIAL_AIR) : mats[(x + dx) + G::FD * (y + dy) + G::FD * G::FD * (z + dz)];
         }
         int edges = 0;
 #pragma unroll
@@ -1026,7 +1087,8 @@ __global__ void __launch_bounds__(kThreads) k_edge_insert(BatchPtrs b) {
         uint32_t p[10];
 #pragma unroll
         for (int k = 0; k < 10; k++) p[k] = b.desc[c].edge_params[k];
-        const int r = cuckoo_insert(table, table + prime, prime, p, (uint32_t)b.edge_keys[i], (uint32_t)(i - st->edge_off));
+        const int r = cuckoo_insert(table, table + prime, prime, st->edge_magic, p, (uint32_t)b.edge_keys[i],
+                                    (uint32_t)(i - st->edge_off));
         if (r == 1) st->edge_stash_used = 1;
         if (r < 0) st->edge_insert_failed = 1;
     }
@@ -1043,7 +1105,8 @@ __global__ void __launch_bounds__(kThreads) k_node_insert(BatchPtrs b) {
         uint32_t p[10];
 #pragma unroll
         for (int k = 0; k < 10; k++) p[k] = b.desc[c].node_params[k];
-        const int r = cuckoo_insert(table, table + prime, prime, p, b.node_codes[i], (uint32_t)(i - st->node_off));
+        const int r = cuckoo_insert(table, table + prime, prime, st->node_magic, p, b.node_codes[i],
+                                    (uint32_t)(i - st->node_off));
         if (r == 1) st->node_stash_used = 1;
         if (r < 0) st->node_insert_failed = 1;
     }
@@ -1060,6 +1123,7 @@ __global__ void __launch_bounds__(kThreads) k_leaf(BatchPtrs b) {
         const ChunkDesc& d = b.desc[c];
         HashView hv;
         hv.prime = st.edge_prime;
+        hv.magic = st.edge_magic;
         hv.table = b.edge_slots + st.edge_table_off;
         hv.stash = hv.table + hv.prime;
         hv.stash_used = st.edge_stash_used;
@@ -1170,6 +1234,7 @@ __global__ void __launch_bounds__(kNodeTile) k_mesh_count(BatchPtrs b) {
             const int i = st.node_off + local;
             HashView hv;
             hv.prime = st.node_prime;
+            hv.magic = st.node_magic;
             hv.table = b.node_slots + st.node_table_off;
             hv.stash = hv.table + hv.prime;
             hv.stash_used = st.node_stash_used;
@@ -1319,7 +1384,7 @@ __global__ void __launch_bounds__(kNodeTile) k_mesh_scatter(BatchPtrs b) {
 
 const char* stage_name(int s) {
     static const char* names[ST_COUNT] = {"field",      "csg",        "edge_count", "edge_plan",   "edge_scatter",
-                                          "hermite",    "vox_count",  "vox_plan",   "vox_scatter", "hash_fill",
+                                          "hermite",    "vox_count",  "vox_plan",   "vox_scatter", "primes", "hash_fill",
                                           "edge_insert", "leaf",      "node_insert", "mesh_count", "mesh_plan",
                                           "mesh_scatter"};
     return s >= 0 && s < ST_COUNT ? names[s] : "?";
@@ -1394,6 +1459,11 @@ cudaError_t launch_vox_plan(const BatchPtrs& b, cudaStream_t s) {
 cudaError_t launch_vox_scatter(const BatchPtrs& b, cudaStream_t s) {
     dim3 grid(vox_tiles_per_chunk(b.vpc), b.n);
     LVN_VPC_DISPATCH(b.vpc, (k_vox_scatter<V><<<grid, kThreads, 0, s>>>(b)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_primes(const BatchPtrs& b, cudaStream_t s) {
+    k_primes<<<(b.n + 7) / 8, 256, 0, s>>>(b);
     return cudaGetLastError();
 }
 

@@ -17,6 +17,7 @@ struct BatchPtrs {
     int vpc;                     // voxels per chunk
     int crossing_mode;           // 0 = 17-sample search, 1 = linear
     int plain_class;             // 1: plain field edges are generated (fresh fields)
+    int derive_mats;             // 1: a chunk without operations holds only default / AIR materials
     int num_sms;
     DensityParams density;
     int32_t default_material;
@@ -31,12 +32,13 @@ struct BatchPtrs {
 
     uint8_t* mats;               // [n][F] field materials, index x + FD*y + FD*FD*z
     uint4* planes;               // [n][3][FD*FD] bit rows: plain solid, final air, changed
-    int2* edge_tiles;            // [n][NBE] (plain, created) counts, then in-chunk offsets
+    int4* edge_tiles;            // [n][NBE] (plain x/z, plain y, created) counts, then in-chunk offsets
     int* vox_tiles;              // [n][NBV]
 
     int32_t* edge_keys;          // [ecap]
     int32_t* edge_chunk;         // [ecap]
     float4* edge_info;           // [ecap]
+    int32_t* edge_work;          // [ecap] hermite work list: plain x/z, plain y, created segments
     int64_t ecap;
 
     uint32_t* node_codes;        // [vcap]
@@ -88,6 +90,7 @@ enum Stage {
     ST_VOX_COUNT,
     ST_VOX_PLAN,
     ST_VOX_SCATTER,
+    ST_PRIMES,
     ST_HASH_FILL,
     ST_EDGE_INSERT,
     ST_LEAF,
@@ -111,6 +114,7 @@ cudaError_t launch_hermite(const BatchPtrs& b, cudaStream_t stream);
 cudaError_t launch_vox_count(const BatchPtrs& b, cudaStream_t stream);
 cudaError_t launch_vox_plan(const BatchPtrs& b, cudaStream_t stream);
 cudaError_t launch_vox_scatter(const BatchPtrs& b, cudaStream_t stream);
+cudaError_t launch_primes(const BatchPtrs& b, cudaStream_t stream);
 cudaError_t launch_hash_fill(const BatchPtrs& b, cudaStream_t stream);
 cudaError_t launch_edge_insert(const BatchPtrs& b, cudaStream_t stream);
 cudaError_t launch_leaf(const BatchPtrs& b, cudaStream_t stream);

@@ -51,12 +51,13 @@ constexpr size_t kRows = (size_t)(kMaxVpc + 2) * (kMaxVpc + 2);
 constexpr size_t OFF_MATS = OFF_BRUSH + align256(sizeof(Brush) * kMaxOps);
 constexpr size_t OFF_PLANES = OFF_MATS + align256(kF);
 constexpr size_t OFF_ETILES = OFF_PLANES + align256(16 * 3 * kRows);
-constexpr size_t OFF_VTILES = OFF_ETILES + align256(8 * kNbe);
+constexpr size_t OFF_VTILES = OFF_ETILES + align256(16 * kNbe);
 constexpr size_t OFF_CTILE = OFF_VTILES + align256(4 * kNbv);
 constexpr size_t OFF_EKEYS = OFF_CTILE + align256(4 * 2);
 constexpr size_t OFF_ECHUNK = OFF_EKEYS + align256(4 * kMaxEdges);
 constexpr size_t OFF_EINFO = OFF_ECHUNK + align256(4 * kMaxEdges);
-constexpr size_t OFF_NCODES = OFF_EINFO + align256(16 * kMaxEdges);
+constexpr size_t OFF_EWORK = OFF_EINFO + align256(16 * kMaxEdges);
+constexpr size_t OFF_NCODES = OFF_EWORK + align256(4 * kMaxEdges);
 constexpr size_t OFF_NINFO = OFF_NCODES + align256(4 * kMaxNodes);
 constexpr size_t OFF_NCHUNK = OFF_NINFO + align256(4 * kMaxNodes);
 constexpr size_t OFF_ESLOTS = OFF_NCHUNK + align256(4 * kMaxNodes);
@@ -145,6 +146,7 @@ extern "C" int lvn_generate_chunk_mesh_noalloc(const int32_t min[3], int32_t siz
     b.vpc = vpc;
     b.crossing_mode = 0;
     b.plain_class = 1;
+    b.derive_mats = 1;
     b.num_sms = gv.num_sms;
     b.density = gv.density;
     b.default_material = gv.default_material;
@@ -156,12 +158,13 @@ extern "C" int lvn_generate_chunk_mesh_noalloc(const int32_t min[3], int32_t siz
     b.brushes = reinterpret_cast<Brush*>(base + OFF_BRUSH);
     b.mats = reinterpret_cast<uint8_t*>(base + OFF_MATS);
     b.planes = reinterpret_cast<uint4*>(base + OFF_PLANES);
-    b.edge_tiles = reinterpret_cast<int2*>(base + OFF_ETILES);
+    b.edge_tiles = reinterpret_cast<int4*>(base + OFF_ETILES);
     b.vox_tiles = reinterpret_cast<int*>(base + OFF_VTILES);
     b.chunk_tile_off = reinterpret_cast<int*>(base + OFF_CTILE);
     b.edge_keys = reinterpret_cast<int32_t*>(base + OFF_EKEYS);
     b.edge_chunk = reinterpret_cast<int32_t*>(base + OFF_ECHUNK);
     b.edge_info = reinterpret_cast<float4*>(base + OFF_EINFO);
+    b.edge_work = reinterpret_cast<int32_t*>(base + OFF_EWORK);
     b.ecap = kMaxEdges;
     b.node_codes = reinterpret_cast<uint32_t*>(base + OFF_NCODES);
     b.node_info = reinterpret_cast<int32_t*>(base + OFF_NINFO);
@@ -204,6 +207,7 @@ extern "C" int lvn_generate_chunk_mesh_noalloc(const int32_t min[3], int32_t siz
         NA_CK(launch_vox_count(b, stream));
         NA_CK(launch_vox_plan(b, stream));
         NA_CK(launch_vox_scatter(b, stream));
+        NA_CK(launch_primes(b, stream));
         NA_CK(launch_hash_fill(b, stream));
         NA_CK(launch_edge_insert(b, stream));
         NA_CK(launch_leaf(b, stream));

@@ -115,9 +115,27 @@ struct Noise {
         return 32.f * (((n0 + n1) + n2) + n3);
     }
 
-    // BasicFractal (noise.cl:8-36), NOISE_SCALE == 1
+    // BasicFractal (noise.cl:8-36), NOISE_SCALE == 1; the octave loop is
+    // fully unrolled for the common 8-octave case
+    template <int OCT>
+    __device__ __forceinline__ float fbm2_fixed(float frequency, float lacunarity, float persistence, float x,
+                                                float y) const {
+        float px = x * 1.f, py = y * 1.f;
+        float noise = 0.f, amplitude = 1.f;
+        px = px * frequency;
+        py = py * frequency;
+#pragma unroll
+        for (int i = 0; i < OCT; i++) {
+            noise = fmaf(snoise2(px, py), amplitude, noise);
+            px = px * lacunarity;
+            py = py * lacunarity;
+            amplitude = amplitude * persistence;
+        }
+        return noise;
+    }
     __device__ __forceinline__ float fbm2(int octaves, float frequency, float lacunarity, float persistence, float x,
                                           float y) const {
+        if (octaves == 8) return fbm2_fixed<8>(frequency, lacunarity, persistence, x, y);
         float px = x * 1.f, py = y * 1.f;
         float noise = 0.f, amplitude = 1.f;
         px = px * frequency;

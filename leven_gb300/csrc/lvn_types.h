@@ -73,9 +73,16 @@ struct ChunkState {
     int32_t edge_insert_failed;
     int32_t node_insert_failed;
     int32_t kept_edges;      // edges kept from a cached field (cached-field CSG)
-    int32_t pad;
+    int32_t edges_xz;        // new plain edges along x or z
+    int32_t edges_y;         // new plain edges along y
+    int32_t wl_xz_off;       // chunk's first entry in each hermite work-list segment
+    int32_t wl_y_off;
+    int32_t wl_c_off;
+    uint32_t edge_magic;     // floor((2^32 - 1) / edge_prime), for the table modulo
+    uint32_t node_magic;
+    int32_t pad[2];
 };
-static_assert(sizeof(ChunkState) == 80, "ChunkState layout");
+static_assert(sizeof(ChunkState) == 112, "ChunkState layout");
 
 // Batch-wide totals and status (device).
 struct BatchState {
@@ -87,7 +94,10 @@ struct BatchState {
     int64_t total_node_slots;
     int32_t overflow;        // bitmask of pools that ran out of capacity
     int32_t status;          // device-side internal status (0 = ok)
-    int32_t pad[6];
+    int32_t total_xz;        // hermite work-list segment sizes
+    int32_t total_y;
+    int32_t total_created;
+    int32_t pad[3];
 };
 
 enum OverflowBits : int32_t {
