@@ -96,7 +96,7 @@ struct Global {
     int num_sms = 0;
     int32_t default_material = 0;
     int32_t seed = 0;
-    DevBuf perm, grad;
+    DevBuf perm, perm_k2, grad;
     DensityParams density{LVN_DENSITY_REFERENCE, 8, 1.f / 256.f, 2.f, 0.5f, 48.f, 6, 1.f / 64.f, 2.f, 0.5f, 12.f};
     std::vector<StoredOp> ops;
     std::mt19937 hash_gen;  // default-seeded, drawn in call order (compute_cuckoo.cpp:46-47)
@@ -158,9 +158,13 @@ int upload_perm(int seed) {
         }
         grad[4 * k + 3] = 0.f;
     }
+    std::vector<uint8_t> k2(65536);
+    for (int i = 0; i < 65536; i++) k2[i] = v[i] & 15;
     LVN_CK(g.perm.ensure(65536));
+    LVN_CK(g.perm_k2.ensure(65536));
     LVN_CK(g.grad.ensure(sizeof(grad)));
     LVN_CK(cudaMemcpy(g.perm.p, v.data(), 65536, cudaMemcpyHostToDevice));
+    LVN_CK(cudaMemcpy(g.perm_k2.p, k2.data(), 65536, cudaMemcpyHostToDevice));
     LVN_CK(cudaMemcpy(g.grad.p, grad, sizeof(grad), cudaMemcpyHostToDevice));
     g.seed = seed;
     return LVN_OK;
@@ -295,7 +299,13 @@ struct lvn_meshgen {
 
     // last batch, for debug fetch
     int last_n = 0;
+    bool last_fresh = true;
     std::vector<ChunkState> last_cs;
+    std::vector<ChunkDesc> last_desc;
+
+    // export of pinned host outputs: a side stream and its events
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_leaf = nullptr, ev_side = nullptr;
 
     // profiling
     cudaEvent_t ev[ST_COUNT + 1] = {};
@@ -385,6 +395,7 @@ BatchPtrs make_ptrs(lvn_meshgen* m, int n) {
     b.crossing_mode = m->crossing_mode;
     b.plain_class = 1;
     b.derive_mats = 1;
+    b.need_mats = 0;
     b.num_sms = g.num_sms;
     b.density = g.density;
     b.default_material = g.default_material;
@@ -393,6 +404,7 @@ BatchPtrs make_ptrs(lvn_meshgen* m, int n) {
     b.bs = m->bs.as<BatchState>();
     b.brushes = m->brushes.as<Brush>();
     b.perm = g.perm.as<uint8_t>();
+    b.perm_k2 = g.perm_k2.as<uint8_t>();
     b.grad = g.grad.as<float>();
     b.mats = m->mats.as<uint8_t>();
     b.planes = m->planes.as<uint4>();
@@ -459,8 +471,17 @@ int enqueue_field_stages(lvn_meshgen* m, const BatchPtrs& b, bool any_ops) {
     return LVN_OK;
 }
 
-// ConstructOctreeFromField + GenerateMeshFromOctree + GatherSeamNodesFromOctree
-int enqueue_octree_stages(lvn_meshgen* m, const BatchPtrs& b) {
+// Caller arrays the export kernels write directly (pinned host memory).
+struct DirectOut {
+    void* dst[3];
+    int64_t cap[3];
+};
+
+// ConstructOctreeFromField + GenerateMeshFromOctree + GatherSeamNodesFromOctree.
+// With `direct`, the vertices are exported on a side stream as soon as the
+// leaves are written, overlapping the mesh stages, and the triangles and
+// seams after the last stage.
+int enqueue_octree_stages(lvn_meshgen* m, const BatchPtrs& b, const DirectOut* direct = nullptr) {
     LVN_STAGE(ST_VOX_COUNT, launch_vox_count);
     LVN_STAGE(ST_VOX_PLAN, launch_vox_plan);
     LVN_STAGE(ST_VOX_SCATTER, launch_vox_scatter);
@@ -468,11 +489,46 @@ int enqueue_octree_stages(lvn_meshgen* m, const BatchPtrs& b) {
     LVN_STAGE(ST_HASH_FILL, launch_hash_fill);
     LVN_STAGE(ST_EDGE_INSERT, launch_edge_insert);
     LVN_STAGE(ST_LEAF, launch_leaf);
+    if (direct) {
+        LVN_CK(cudaEventRecord(m->ev_leaf, m->stream));
+        LVN_CK(cudaStreamWaitEvent(m->side, m->ev_leaf, 0));
+        LVN_CK(launch_export(b, 0, direct->dst[0], direct->cap[0], m->side));
+        LVN_CK(cudaEventRecord(m->ev_side, m->side));
+    }
     LVN_STAGE(ST_NODE_INSERT, launch_node_insert);
     LVN_STAGE(ST_MESH_COUNT, launch_mesh_count);
     LVN_STAGE(ST_MESH_PLAN, launch_mesh_plan);
     LVN_STAGE(ST_MESH_SCATTER, launch_mesh_scatter);
+    if (direct) {
+        LVN_CK(launch_export(b, 1, direct->dst[1], direct->cap[1], m->stream));
+        LVN_CK(launch_export(b, 2, direct->dst[2], direct->cap[2], m->stream));
+        LVN_CK(cudaStreamWaitEvent(m->stream, m->ev_side, 0));
+    }
     return LVN_OK;
+}
+
+// Device addresses of caller arrays that are pinned (or registered) host
+// memory, or of device memory; false when any array is pageable.
+bool direct_addresses(const lvn_batch_out* out, DirectOut* d) {
+    void* src[3] = {out->vertices, out->triangles, out->seams};
+    const int64_t cap[3] = {out->vertex_capacity, out->triangle_capacity, out->seam_capacity};
+    for (int i = 0; i < 3; i++) {
+        d->cap[i] = cap[i];
+        d->dst[i] = nullptr;
+        if (!src[i]) {
+            if (cap[i] > 0) return false;
+            continue;
+        }
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, src[i]) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        if (a.type != cudaMemoryTypeHost && a.type != cudaMemoryTypeDevice) return false;
+        if (!a.devicePointer) return false;
+        d->dst[i] = a.devicePointer;
+    }
+    return true;
 }
 
 int read_states(lvn_meshgen* m, int n) {
@@ -554,7 +610,7 @@ constexpr int kMaxHashRetries = 16;
 // buffers when `dev_out` is given).  Grows the pools and reruns once when a
 // pool overflowed; retries the hash with new parameters when an insert failed.
 int run_fresh_batch(lvn_meshgen* m, std::vector<ChunkDesc>& descs, const std::vector<Brush>& brushes,
-                    const lvn_batch_out* dev_out) {
+                    const lvn_batch_out* dev_out, const DirectOut* direct = nullptr) {
     const int n = (int)descs.size();
     Capacity cap = default_capacity(m, n);
     cap.ecap = std::max(cap.ecap, m->ecap);
@@ -575,11 +631,14 @@ int run_fresh_batch(lvn_meshgen* m, std::vector<ChunkDesc>& descs, const std::ve
         }
         rc = enqueue_field_stages(m, b, !brushes.empty());
         if (rc) return rc;
-        rc = enqueue_octree_stages(m, b);
+        rc = enqueue_octree_stages(m, b, direct);
         if (rc) return rc;
         rc = read_states(m, n);
         if (rc) return rc;
+        m->last_fresh = true;
+        m->last_desc = descs;
         const BatchState& bs = *m->h_bs.as<BatchState>();
+        if (direct && bs.status) return LVN_ERR_CAPACITY;  // a caller array was too small
         if (bs.overflow) {
             const bool user_short = dev_out && ((bs.overflow & (OVF_QUADS | OVF_SEAMS)) ||
                                                 ((bs.overflow & OVF_NODES) && bs.total_nodes > b.vertex_cap &&
@@ -664,8 +723,11 @@ int generate_field(lvn_meshgen* m, const int32_t min[3], int32_t size, FieldEntr
     std::vector<Brush> none;
     if ((rc = upload(m, descs, none))) return rc;
     BatchPtrs b = make_ptrs(m, 1);
+    b.need_mats = 1;  // a cached field keeps every byte material
+    b.derive_mats = 0;
     if ((rc = enqueue_field_stages(m, b, false))) return rc;
     if ((rc = read_states(m, 1))) return rc;
+    m->last_fresh = false;
     if (m->h_bs.as<BatchState>()->overflow) return LVN_ERR_DEVICE_STATUS;
     f.last_op = 0;
     return save_field(m, f);
@@ -697,6 +759,8 @@ int apply_csg_to_field(lvn_meshgen* m, const int32_t min[3], int32_t size, Field
     LVN_CK(cudaMemsetAsync(m->planes.as<uint4>() + 2 * R, 0, sizeof(uint4) * R, m->stream));
     BatchPtrs b = make_ptrs(m, 1);
     b.plain_class = 0;
+    b.need_mats = 1;
+    b.derive_mats = 0;
     b.prev_keys = f.keys.as<int32_t>();
     b.prev_info = f.info.as<float4>();
     b.prev_count = f.num_edges;
@@ -708,6 +772,7 @@ int apply_csg_to_field(lvn_meshgen* m, const int32_t min[3], int32_t size, Field
     if ((rc = stage(m, ST_EDGE_SCATTER, launch_edge_scatter, b))) return rc;
     if ((rc = stage(m, ST_HERMITE, launch_hermite, b))) return rc;
     if ((rc = read_states(m, 1))) return rc;
+    m->last_fresh = false;
     if (m->h_bs.as<BatchState>()->overflow) return LVN_ERR_DEVICE_STATUS;
     return save_field(m, f);
 }
@@ -808,6 +873,7 @@ int mesh_from_field(lvn_meshgen* m, const int32_t min[3], int32_t size, FieldEnt
         b.derive_mats = 0;  // the cached field may hold CSG materials
         if ((rc = enqueue_octree_stages(m, b))) return rc;
         if ((rc = read_states(m, 1))) return rc;
+        m->last_fresh = false;
         const BatchState& hb = *m->h_bs.as<BatchState>();
         if (hb.overflow) {
             cap.vcap = std::max<int64_t>(cap.vcap * 2, (int64_t)hb.total_nodes + 1024);
@@ -880,6 +946,7 @@ int lvn_initialise(int32_t noise_seed, uint32_t default_material, int32_t num_cs
 
 int lvn_shutdown(void) {
     g.perm.release();
+    g.perm_k2.release();
     g.grad.release();
     g.ops.clear();
     g.initialised = false;
@@ -973,6 +1040,9 @@ void lvn_meshgen_destroy(lvn_meshgen* m) {
     }
     for (int i = 0; i <= ST_COUNT; i++)
         if (m->ev[i]) cudaEventDestroy(m->ev[i]);
+    if (m->ev_leaf) cudaEventDestroy(m->ev_leaf);
+    if (m->ev_side) cudaEventDestroy(m->ev_side);
+    if (m->side) cudaStreamDestroy(m->side);
     if (m->own_stream) cudaStreamDestroy(m->stream);
     delete m;
 }
@@ -1036,14 +1106,21 @@ int lvn_meshgen_generate_chunks(lvn_meshgen* m, const lvn_chunk_desc* chunks, in
     int rc = build_descs(m, chunks, n, descs, brushes, true);
     if (rc) return rc;
     const bool dev = out->memory == LVN_MEMORY_DEVICE;
-    rc = run_fresh_batch(m, descs, brushes, dev ? out : nullptr);
+    DirectOut direct;
+    const bool use_direct = !dev && direct_addresses(out, &direct);
+    if (use_direct && !m->side) {
+        LVN_CK(cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking));
+        LVN_CK(cudaEventCreateWithFlags(&m->ev_leaf, cudaEventDisableTiming));
+        LVN_CK(cudaEventCreateWithFlags(&m->ev_side, cudaEventDisableTiming));
+    }
+    rc = run_fresh_batch(m, descs, brushes, dev ? out : nullptr, use_direct ? &direct : nullptr);
     const BatchState& bs = *m->h_bs.as<BatchState>();
     out->total_vertices = bs.total_nodes;
     out->total_triangles = 2 * (int64_t)bs.total_quads;
     out->total_seams = bs.total_seams;
     if (rc) return rc;
     if (out->chunks) fill_results(m, n, out->chunks);
-    if (!dev) {
+    if (!dev && !use_direct) {
         if (out->total_vertices > out->vertex_capacity || out->total_triangles > out->triangle_capacity ||
             out->total_seams > out->seam_capacity)
             return LVN_ERR_CAPACITY;
@@ -1139,8 +1216,36 @@ int64_t lvn_meshgen_debug_fetch(lvn_meshgen* m, int32_t what, int32_t chunk, voi
     int64_t count = 0, elem = 0;
     std::vector<uint8_t> mats;
     switch (what) {
-        case LVN_DEBUG_MATERIALS:
-            src = m->mats.as<uint8_t>() + F * chunk; count = (int64_t)F; elem = 1; break;
+        case LVN_DEBUG_MATERIALS: {
+            if (cap < (int64_t)F) return LVN_ERR_CAPACITY;
+            uint8_t* out = static_cast<uint8_t*>(host);
+            if (cudaMemcpy(out, m->mats.as<uint8_t>() + F * chunk, F, cudaMemcpyDeviceToHost) != cudaSuccess)
+                return LVN_ERR_CUDA;
+            if (m->last_fresh && chunk < (int)m->last_desc.size()) {
+                // fresh fields hold byte materials only inside the CSG box; the
+                // rest are the default material or AIR by the final-air bits
+                const int fd = m->vpc + 2;
+                const size_t R = (size_t)fd * fd;
+                std::vector<uint4> air(R);
+                if (cudaMemcpy(air.data(), m->planes.as<uint4>() + (3 * (size_t)chunk + 1) * R, R * sizeof(uint4),
+                               cudaMemcpyDeviceToHost) != cudaSuccess)
+                    return LVN_ERR_CUDA;
+                const ChunkDesc& d = m->last_desc[chunk];
+                for (int z = 0; z < fd; z++)
+                    for (int y = 0; y < fd; y++)
+                        for (int x = 0; x < fd; x++) {
+                            const bool in_box = d.op_count > 0 && x >= d.csg_lo[0] && x <= d.csg_hi[0] &&
+                                                y >= d.csg_lo[1] && y <= d.csg_hi[1] && z >= d.csg_lo[2] &&
+                                                z <= d.csg_hi[2];
+                            if (in_box) continue;
+                            const uint4 r = air[y + fd * z];
+                            const unsigned w = x < 32 ? r.x : x < 64 ? r.y : r.z;
+                            const bool is_air = (w >> (x & 31)) & 1u;
+                            out[x + fd * y + (size_t)fd * fd * z] = is_air ? MATERIAL_AIR : (uint8_t)g.default_material;
+                        }
+            }
+            return (int64_t)F;
+        }
         case LVN_DEBUG_EDGE_KEYS: src = m->edge_keys.as<int32_t>() + cs.edge_off; count = cs.num_edges; elem = 4; break;
         case LVN_DEBUG_EDGE_INFO: src = m->edge_info.as<float4>() + cs.edge_off; count = cs.num_edges; elem = 16; break;
         case LVN_DEBUG_NODE_CODES: src = m->node_codes.as<uint32_t>() + cs.node_off; count = cs.nodes; elem = 4; break;
@@ -1179,6 +1284,7 @@ GlobalView global_view() {
     v.num_sms = g.num_sms;
     v.default_material = g.default_material;
     v.perm = g.perm.as<uint8_t>();
+    v.perm_k2 = g.perm_k2.as<uint8_t>();
     v.grad = g.grad.as<float>();
     v.density = g.density;
     return v;

@@ -210,12 +210,15 @@ struct HashView {
     uint32_t p[10];
 
     // Cuckoo_Find (cuckoo.cl:73-104); the stash probe reads the stash
+    // All four probes are issued before any is tested: a key occupies at most
+    // one slot, so testing them in order gives the sequential probe's answer.
     __device__ __forceinline__ uint32_t find(uint32_t key) const {
+        unsigned long long e[CUCKOO_STASH_HASH_INDEX];
 #pragma unroll
-        for (int i = 0; i < CUCKOO_STASH_HASH_INDEX; i++) {
-            const unsigned long long e = table[cuckoo_hash(key, p[2 * i], p[2 * i + 1], prime, magic)];
-            if ((uint32_t)e == key) return (uint32_t)(e >> 32);
-        }
+        for (int i = 0; i < CUCKOO_STASH_HASH_INDEX; i++) e[i] = table[cuckoo_hash(key, p[2 * i], p[2 * i + 1], prime, magic)];
+#pragma unroll
+        for (int i = 0; i < CUCKOO_STASH_HASH_INDEX; i++)
+            if ((uint32_t)e[i] == key) return (uint32_t)(e[i] >> 32);
         if (stash_used) {
             const unsigned long long e = stash[stash_hash(key, p[8], p[9])];
             if ((uint32_t)e == key) return (uint32_t)(e >> 32);
@@ -404,6 +407,21 @@ __device__ __forceinline__ uint4 low_bits(int n) {
     return make_uint4(m(n), m(n - 32), m(n - 64), m(n - 96));
 }
 
+// Height term and density for a density mode fixed at compile time, so a
+// kernel carries one density's code (DensityFunc, noise.cl:225-268).
+template <int MODE>
+__device__ __forceinline__ float height_m(const Noise& nz, const DensityParams& dp, float x, float z) {
+    if (MODE == LVN_DENSITY_REFERENCE) return nz.terrain(x, z);
+    return nz.fbm2(dp.octaves2, dp.freq2, dp.lacunarity2, dp.gain2, x, z);
+}
+template <int MODE>
+__device__ __forceinline__ float dens_h(const Noise& nz, const DensityParams& dp, float h, float x, float y, float z) {
+    const float amp = MODE == LVN_DENSITY_REFERENCE ? 900.f : dp.amp2;  // MAX_TERRAIN_HEIGHT
+    const float base = fmaf(-amp, h, y);
+    if (MODE != LVN_DENSITY_CAVES) return base;
+    return fmaf(dp.amp3, nz.fbm3(dp.octaves3, dp.freq3, dp.lacunarity3, dp.gain3, x, y, z), base);
+}
+
 // ---------------------------------------------------------------------------
 // stage 1: density field (GenerateDefaultField, density_field.cl:11-37)
 // One CTA per (z slice, chunk), one thread per x; heightfield modes evaluate
@@ -411,49 +429,80 @@ __device__ __forceinline__ uint4 low_bits(int n) {
 // three bit planes (warp ballots along x).
 // ---------------------------------------------------------------------------
 
-template <int VPC>
+template <int VPC, int MODE>
 __global__ void __launch_bounds__(96) k_field(BatchPtrs b) {
     using G = Geo<VPC>;
     __shared__ float sg[64];
+    __shared__ uint32_t words[3][G::FD];  // solid-bit word of each warp, per row y
     if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
     __syncthreads();
     const int c = blockIdx.y, z = blockIdx.x;
     const int x = threadIdx.x;
     const bool valid = x < G::FD;
-    const ChunkDesc& d = b.desc[c];
-    const int scale = d.scale;
-    const Noise nz{b.perm, sg};
-    const float wx = (float)(x * scale + d.off[0]);
-    const float wz = (float)(z * scale + d.off[2]);
-    const float h = valid ? nz.height(b.density, wx, wz) : 0.f;
+    // descriptor fields in registers: the byte stores below may alias them
+    const int scale = b.desc[c].scale;
+    const int ox = b.desc[c].off[0], oy = b.desc[c].off[1], oz = b.desc[c].off[2];
+    const Noise nz{b.perm, b.perm_k2, sg};
+    const DensityParams& dp = b.density;
+    const float wx = (float)(x * scale + ox);
+    const float wz = (float)(z * scale + oz);
+    const float h = valid ? height_m<MODE>(nz, dp, wx, wz) : 0.f;
     const int dm = b.default_material;
+    const bool write_mats = b.need_mats != 0;
     uint8_t* mats = b.mats + (size_t)c * G::F + x + G::FD * G::FD * z;
-    // word `warp` of each row of the three planes (rows are 4 words)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    uint32_t* P = reinterpret_cast<uint32_t*>(plane_ptr<VPC>(b, c, 0) + G::FD * z);
-    uint32_t* A = reinterpret_cast<uint32_t*>(plane_ptr<VPC>(b, c, 1) + G::FD * z);
-    uint32_t* X = reinterpret_cast<uint32_t*>(plane_ptr<VPC>(b, c, 2) + G::FD * z);
-    const uint4 V4 = low_bits(G::FD);
-    const uint32_t vmask = warp == 0 ? V4.x : warp == 1 ? V4.y : V4.z;
-    for (int y = 0; y < G::FD; y++) {
-        bool solid = false;
-        if (valid) {
-            const float wy = (float)(y * scale + d.off[1]);
-            const float dv = nz.density_h(b.density, h, wx, wy, wz);
-            const int m = dv < 0.f ? dm : MATERIAL_AIR;
-            mats[G::FD * y] = (uint8_t)m;
-            solid = m != MATERIAL_AIR;
+    uint32_t pw = 0;  // lane l keeps the ballot of row (y & ~31) + l
+    if (MODE != LVN_DENSITY_CAVES) {
+        // y - amp * h rounds monotonically in y, so the column is solid below
+        // the first y whose density is >= 0 and air from there up
+        int ycross = 0;
+        if (valid && dm != MATERIAL_AIR) {
+            int lo = 0, hi = G::FD;  // first y in [lo, hi) with density >= 0, hi if none
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (dens_h<MODE>(nz, dp, h, wx, (float)(mid * scale + oy), wz) < 0.f) lo = mid + 1;
+                else hi = mid;
+            }
+            ycross = lo;
         }
-        const unsigned s = __ballot_sync(FULL, solid);
-        if (lane == 0) {
-            P[4 * y + warp] = s;
-            A[4 * y + warp] = ~s & vmask;
-            X[4 * y + warp] = 0u;
-        } else if (lane == 1 && warp == 0) {
-            P[4 * y + 3] = 0u;
-            A[4 * y + 3] = 0u;
-            X[4 * y + 3] = 0u;
+        for (int y = 0; y < G::FD; y++) {
+            const bool solid = y < ycross;
+            if (valid && write_mats) mats[G::FD * y] = (uint8_t)(solid ? dm : MATERIAL_AIR);
+            const unsigned sb = __ballot_sync(FULL, solid);
+            pw = (y & 31) == lane ? sb : pw;
+            if ((y & 31) == 31 || y == G::FD - 1) {
+                const int yy = (y & ~31) + lane;
+                if (yy <= y) words[warp][yy] = pw;
+            }
         }
+    } else {
+        for (int y = 0; y < G::FD; y++) {
+            bool solid = false;
+            if (valid) {
+                const float dv = dens_h<MODE>(nz, dp, h, wx, (float)(y * scale + oy), wz);
+                const int m = dv < 0.f ? dm : MATERIAL_AIR;
+                if (write_mats) mats[G::FD * y] = (uint8_t)m;
+                solid = m != MATERIAL_AIR;
+            }
+            const unsigned sb = __ballot_sync(FULL, solid);
+            pw = (y & 31) == lane ? sb : pw;
+            if ((y & 31) == 31 || y == G::FD - 1) {
+                const int yy = (y & ~31) + lane;
+                if (yy <= y) words[warp][yy] = pw;
+            }
+        }
+    }
+    __syncthreads();
+    // one thread per row writes the three 16-byte plane rows
+    const uint4 V = low_bits(G::FD);
+    uint4* P = plane_ptr<VPC>(b, c, 0) + G::FD * z;
+    uint4* A = plane_ptr<VPC>(b, c, 1) + G::FD * z;
+    uint4* X = plane_ptr<VPC>(b, c, 2) + G::FD * z;
+    for (int y = threadIdx.x; y < G::FD; y += blockDim.x) {
+        const uint4 p = make_uint4(words[0][y], words[1][y], words[2][y], 0u);
+        P[y] = p;
+        A[y] = and4(not4(p), V);
+        X[y] = make_uint4(0u, 0u, 0u, 0u);
     }
 }
 
@@ -467,7 +516,7 @@ template <int VPC>
 __global__ void __launch_bounds__(96) k_csg(BatchPtrs b) {
     using G = Geo<VPC>;
     const int c = blockIdx.y, z = blockIdx.x;
-    const ChunkDesc& d = b.desc[c];
+    const ChunkDesc d = b.desc[c];  // a copy: the byte stores below may alias the descriptor
     const int nops = d.op_count;
     if (nops == 0 || z < d.csg_lo[2] || z > d.csg_hi[2]) return;
     const int x = threadIdx.x;
@@ -482,7 +531,11 @@ __global__ void __launch_bounds__(96) k_csg(BatchPtrs b) {
     for (int y = d.csg_lo[1]; y <= d.csg_hi[1]; y++) {
         bool air = false, changed = false;
         if (x < G::FD) {
-            const int m = mats[x + G::FD * y];
+            // a fresh field's materials are the default or AIR, given by its
+            // plain-solid bits; a cached field's are in the byte array
+            const int m = b.need_mats ? mats[x + G::FD * y]
+                                      : (bit4(plane_ptr<VPC>(b, c, 0)[y + G::FD * z], x) ? b.default_material
+                                                                                        : MATERIAL_AIR);
             int nm = m;
             if (inx) {
                 const float wy = (float)(d.off[1] + d.scale * y);
@@ -490,7 +543,8 @@ __global__ void __launch_bounds__(96) k_csg(BatchPtrs b) {
                     const Brush& br = ops[i];
                     if (brush_density(br, wx, wy, wz) <= 0.f) nm = br.type == 0 ? br.material : MATERIAL_AIR;
                 }
-                if (nm != m) mats[x + G::FD * y] = (uint8_t)nm;
+                // inside the box the byte array holds the final material
+                if (nm != m || !b.need_mats) mats[x + G::FD * y] = (uint8_t)nm;
             }
             air = nm == MATERIAL_AIR;
             changed = nm != m;
@@ -780,7 +834,11 @@ __global__ void __launch_bounds__(kThreads) k_edge_scatter(BatchPtrs b) {
 // stage 6: hermite data per edge
 // ---------------------------------------------------------------------------
 
-template <int VPC>
+// FindEdgeIntersectionInfo (density_field.cl:96-151).  A y edge keeps x and z
+// fixed, so its height term is evaluated once; the other edges evaluate it
+// per sample.  Each density evaluation has one call site in a loop, which
+// keeps the kernel small enough for the instruction cache.
+template <int VPC, int MODE>
 __device__ __forceinline__ float4 hermite_density(const BatchPtrs& b, const Noise& nz, const ChunkDesc& d, int key) {
     using G = Geo<VPC>;
     const int axis = key & 3;
@@ -793,47 +851,61 @@ __device__ __forceinline__ float4 hermite_density(const BatchPtrs& b, const Nois
     const float p1y = (float)(wy + (axis == 1 ? s : 0));
     const float p1z = (float)(wz + (axis == 2 ? s : 0));
     const DensityParams& dp = b.density;
+    const bool yedge = axis == 1;
     float t = 0.f;
-    float hbest;
+    float hbest = 0.f;
     if (b.crossing_mode == 0) {
         // 17-sample search for min |d| (density_field.cl:122-136); first minimum wins
         float minv = FLT_MAX;
         float cur = 0.f;
-        if (axis == 1) {
-            const float h = nz.height(dp, p0x, p0z);  // x and z are fixed along a y edge
-            hbest = h;
-            for (int i = 0; i <= 16; i++) {
-                const float py = fmaf(p1y - p0y, cur, p0y);
-                const float dv = fabsf(nz.density_h(dp, h, p0x, py, p0z));
-                if (dv < minv) { t = cur; minv = dv; }
-                cur += 0.0625f;
-            }
-        } else {
-            hbest = 0.f;
-            for (int i = 0; i <= 16; i++) {
-                const float px = fmaf(p1x - p0x, cur, p0x);
-                const float pz = fmaf(p1z - p0z, cur, p0z);
-                const float h = nz.height(dp, px, pz);
-                const float dv = fabsf(nz.density_h(dp, h, px, p0y, pz));
-                if (dv < minv) { t = cur; minv = dv; hbest = h; }
-                cur += 0.0625f;
-            }
+        const float hy = yedge ? height_m<MODE>(nz, dp, p0x, p0z) : 0.f;
+        for (int i = 0; i <= 16; i++) {
+            const float px = fmaf(p1x - p0x, cur, p0x);
+            const float py = fmaf(p1y - p0y, cur, p0y);
+            const float pz = fmaf(p1z - p0z, cur, p0z);
+            const float h = yedge ? hy : height_m<MODE>(nz, dp, px, pz);
+            const float dv = fabsf(dens_h<MODE>(nz, dp, h, px, py, pz));
+            if (dv < minv) { t = cur; minv = dv; hbest = h; }
+            cur += 0.0625f;
         }
     } else {
-        const float d0 = nz.density(dp, p0x, p0y, p0z);
-        const float d1 = nz.density(dp, p1x, p1y, p1z);
-        const float den = d0 - d1;
-        t = den != 0.f ? d0 / den : 0.5f;
+        float e0 = 0.f, e1 = 0.f;
+        for (int j = 0; j < 2; j++) {
+            const float qx = j ? p1x : p0x, qy = j ? p1y : p0y, qz = j ? p1z : p0z;
+            const float v = dens_h<MODE>(nz, dp, height_m<MODE>(nz, dp, qx, qz), qx, qy, qz);
+            e0 = j == 0 ? v : e0;
+            e1 = j == 1 ? v : e1;
+        }
+        const float den = e0 - e1;
+        t = den != 0.f ? e0 / den : 0.5f;
         t = fminf(fmaxf(t, 0.f), 1.f);
-        hbest = nz.height(dp, fmaf(p1x - p0x, t, p0x), fmaf(p1z - p0z, t, p0z));
+        hbest = height_m<MODE>(nz, dp, fmaf(p1x - p0x, t, p0x), fmaf(p1z - p0z, t, p0z));
     }
     const float px = fmaf(p1x - p0x, t, p0x);
     const float py = fmaf(p1y - p0y, t, p0y);
     const float pz = fmaf(p1z - p0z, t, p0z);
     const float h = 0.001f;
-    float nx = nz.density(dp, px + h, py, pz) - nz.density(dp, px - h, py, pz);
-    float ny = nz.density_h(dp, hbest, px, py + h, pz) - nz.density_h(dp, hbest, px, py - h, pz);
-    float nzv = nz.density(dp, px, py, pz + h) - nz.density(dp, px, py, pz - h);
+    // central differences: x+h, x-h, z+h, z-h need their own height term;
+    // y+h and y-h share the one at (px, pz)
+    float d0 = 0.f, d1 = 0.f, d2 = 0.f, d3 = 0.f;  // registers, not an indexed array
+    for (int j = 0; j < 4; j++) {
+        const float qx = j == 0 ? px + h : j == 1 ? px - h : px;
+        const float qz = j == 2 ? pz + h : j == 3 ? pz - h : pz;
+        const float v = dens_h<MODE>(nz, dp, height_m<MODE>(nz, dp, qx, qz), qx, py, qz);
+        d0 = j == 0 ? v : d0;
+        d1 = j == 1 ? v : d1;
+        d2 = j == 2 ? v : d2;
+        d3 = j == 3 ? v : d3;
+    }
+    float ny0 = 0.f, ny1 = 0.f;
+    for (int j = 0; j < 2; j++) {
+        const float v = dens_h<MODE>(nz, dp, hbest, px, j ? py - h : py + h, pz);
+        ny0 = j == 0 ? v : ny0;
+        ny1 = j == 1 ? v : ny1;
+    }
+    float nx = d0 - d1;
+    float ny = ny0 - ny1;
+    float nzv = d2 - d3;
     normalize3(nx, ny, nzv);
     return make_float4(nx, ny, nzv, t);
 }
@@ -885,13 +957,13 @@ __device__ __forceinline__ float4 hermite_brush(const BatchPtrs& b, const ChunkD
     return make_float4(nx, ny, nzv, t);
 }
 
-template <int VPC>
+template <int VPC, int MODE>
 __global__ void __launch_bounds__(kThreads) k_hermite(BatchPtrs b) {
     __shared__ float sg[64];
     if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
     __syncthreads();
     if (b.bs->overflow) return;
-    const Noise nz{b.perm, sg};
+    const Noise nz{b.perm, b.perm_k2, sg};
     // work list segments: plain x/z edges, plain y edges, CSG-created edges, so
     // that a warp's 32 edges take the same path
     const int nplain = b.bs->total_xz + b.bs->total_y;
@@ -901,7 +973,7 @@ __global__ void __launch_bounds__(kThreads) k_hermite(BatchPtrs b) {
         const int c = b.edge_chunk[i];
         const ChunkDesc& d = b.desc[c];
         const int key = b.edge_keys[i];
-        b.edge_info[i] = w >= nplain ? hermite_brush<VPC>(b, d, key) : hermite_density<VPC>(b, nz, d, key);
+        b.edge_info[i] = w >= nplain ? hermite_brush<VPC>(b, d, key) : hermite_density<VPC, MODE>(b, nz, d, key);
     }
 }
 
@@ -1019,33 +1091,60 @@ __global__ void __launch_bounds__(kThreads) k_vox_scatter(BatchPtrs b) {
     if (st.nodes == 0) return;
     const int vrow = tile * kThreads + threadIdx.x;
     const bool valid = vrow < VPC * VPC;
-    VoxRow v;
-    int cnt = 0;
-    if (valid) {
-        v = vox_row<VPC>(b, c, vrow);
-        cnt = popc4(v.active);
-    }
+    uint4 act = make_uint4(0u, 0u, 0u, 0u);
+    if (valid) act = vox_row<VPC>(b, c, vrow).active;
+    const int cnt = popc4(act);
     int total;
     const int ex = block_exclusive<kThreads>(cnt, total, sm);
-    if (!cnt) return;
-    int pos = st.node_off + b.vox_tiles[(size_t)c * G::NBV + tile] + ex;
-    const int y = vrow % VPC, z = vrow / VPC;
+    // the warp's active voxels, in row order then x order, are spread over
+    // its lanes: voxel j of the warp goes to lane j % 32
+    const int lane = threadIdx.x & 31;
+    const int winc = warp_inclusive(cnt);
+    const int wexcl = winc - cnt;
+    const int wtotal = __shfl_sync(FULL, winc, 31);
+    if (wtotal == 0) return;
+    const int base = st.node_off + b.vox_tiles[(size_t)c * G::NBV + tile] + __shfl_sync(FULL, ex, 0);
+    const uint4* A = plane_ptr<VPC>(b, c, 1);
     const uint8_t* mats = b.mats + (size_t)c * G::F;
     // a fresh field without CSG holds the default material or AIR only, so the
     // corner materials follow from the solid bits
-    const bool derive = b.derive_mats && b.desc[c].op_count == 0;
+    const bool fresh = b.derive_mats != 0;
+    const bool has_ops = b.desc[c].op_count > 0;
+    const int bx0 = b.desc[c].csg_lo[0], bx1 = b.desc[c].csg_hi[0], by0 = b.desc[c].csg_lo[1],
+              by1 = b.desc[c].csg_hi[1], bz0 = b.desc[c].csg_lo[2], bz1 = b.desc[c].csg_hi[2];
     const int dm = b.default_material;
-    uint4 act = v.active;
-    while (popc4(act)) {
-        const int x = act.x ? __ffs(act.x) - 1 : act.y ? 31 + __ffs(act.y) : 63 + __ffs(act.z);
+    for (int j0 = 0; j0 < wtotal; j0 += 32) {
+        const int j = j0 + lane;
+        // source lane: the last lane whose exclusive count is <= j
+        int src = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+            const int e = __shfl_sync(FULL, wexcl, (src + step) & 31);
+            if (src + step < 32 && e <= j) src += step;
+        }
+        const int k = j - __shfl_sync(FULL, wexcl, src);
+        const unsigned w0 = __shfl_sync(FULL, act.x, src), w1 = __shfl_sync(FULL, act.y, src);
+        const int row = __shfl_sync(FULL, vrow, src);
+        if (j >= wtotal) continue;
+        // x of the k-th set bit of the source row
+        unsigned w = w0;
+        int kk = k, off = 0;
+        if (kk >= __popc(w0)) { kk -= __popc(w0); w = w1; off = 32; }
+        for (int i = 0; i < kk; i++) w &= w - 1;
+        const int x = off + __ffs(w) - 1;
+        const int y = row % VPC, z = row / VPC;
+        const int r = y + G::FD * z;
         int corners = 0;
         int m[8];
 #pragma unroll
         for (int i = 0; i < 8; i++) {
             const int dx = i >> 2, dy = (i >> 1) & 1, dz = i & 1;
-            const bool solid = bit4(v.s[dz | (dy << 1)], x + dx);
-            corners |= (solid ? 1 : 0) << i;
-            m[i] = derive ? (solid ? dm : MATERIAL_AIR) : mats[(x + dx) + G::FD * (y + dy) + G::FD * G::FD * (z + dz)];
+            const bool air = bit4(A[r + dy + G::FD * dz], x + dx);
+            corners |= (air ? 0 : 1) << i;
+            // a fresh field holds byte materials only inside its CSG box
+            const int cx = x + dx, cy = y + dy, cz = z + dz;
+            const bool in_box = has_ops && cx >= bx0 && cx <= bx1 && cy >= by0 && cy <= by1 && cz >= bz0 && cz <= bz1;
+            m[i] = (fresh && !in_box) ? (air ? MATERIAL_AIR : dm) : mats[cx + G::FD * cy + G::FD * G::FD * cz];
         }
         int edges = 0;
 #pragma unroll
@@ -1054,11 +1153,10 @@ __global__ void __launch_bounds__(kThreads) k_vox_scatter(BatchPtrs b) {
             edges |= (s0 != s1 ? 1 : 0) << i;
         }
         const int dom = dominant_material(m);
+        const int pos = base + j;
         b.node_codes[pos] = code_for_position<VPC>(x, y, z);
         b.node_info[pos] = (edges << 16) | (dom << 8) | corners;
         b.node_chunk[pos] = c;
-        pos++;
-        act = and4(act, not4(low_bits(x + 1)));
     }
 }
 
@@ -1379,6 +1477,44 @@ __global__ void __launch_bounds__(kNodeTile) k_mesh_scatter(BatchPtrs b) {
 }  // namespace
 
 // ---------------------------------------------------------------------------
+// export: copy one output pool (vertices, triangles or seams) to the caller's
+// array, which may be pinned host memory reached over NVLink-C2C.  The element
+// count is read on the device; an array too small is not written and the
+// batch is flagged.
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(256) k_export(BatchPtrs b, int which, void* dst, int64_t capacity) {
+    const BatchState& bs = *b.bs;
+    if (bs.overflow) return;
+    const void* src;
+    int64_t count, elem;
+    if (which == 0) { src = b.vertices; count = bs.total_nodes; elem = sizeof(lvn_mesh_vertex); }
+    else if (which == 1) { src = b.triangles; count = 2 * (int64_t)bs.total_quads; elem = sizeof(lvn_mesh_triangle); }
+    else { src = b.seams; count = bs.total_seams; elem = sizeof(lvn_seam_node); }
+    if (count > capacity) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&b.bs->status, 1 << which);
+        return;
+    }
+    const int64_t nbytes = count * elem;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15) == 0) {
+        const int64_t n16 = nbytes >> 4;
+        const uint4* s4 = static_cast<const uint4*>(src);
+        uint4* d4 = static_cast<uint4*>(dst);
+        for (int64_t i = t0; i < n16; i += stride) d4[i] = s4[i];
+        const int64_t done = n16 << 4;
+        const uint32_t* s1 = static_cast<const uint32_t*>(src);
+        uint32_t* d1 = static_cast<uint32_t*>(dst);
+        for (int64_t i = (done >> 2) + t0; i < (nbytes >> 2); i += stride) d1[i] = s1[i];
+    } else {
+        const uint32_t* s1 = static_cast<const uint32_t*>(src);
+        uint32_t* d1 = static_cast<uint32_t*>(dst);
+        for (int64_t i = t0; i < (nbytes >> 2); i += stride) d1[i] = s1[i];
+    }
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 
@@ -1408,7 +1544,11 @@ cudaError_t launch_reset(const BatchPtrs& b, cudaStream_t s) {
 
 cudaError_t launch_field(const BatchPtrs& b, cudaStream_t s) {
     dim3 grid(b.vpc + 2, b.n);
-    LVN_VPC_DISPATCH(b.vpc, (k_field<V><<<grid, 96, 0, s>>>(b)));
+    switch (b.density.mode) {
+        case LVN_DENSITY_REFERENCE: LVN_VPC_DISPATCH(b.vpc, (k_field<V, LVN_DENSITY_REFERENCE><<<grid, 96, 0, s>>>(b))); break;
+        case LVN_DENSITY_FBM2D: LVN_VPC_DISPATCH(b.vpc, (k_field<V, LVN_DENSITY_FBM2D><<<grid, 96, 0, s>>>(b))); break;
+        default: LVN_VPC_DISPATCH(b.vpc, (k_field<V, LVN_DENSITY_CAVES><<<grid, 96, 0, s>>>(b))); break;
+    }
     return cudaGetLastError();
 }
 
@@ -1441,7 +1581,12 @@ cudaError_t launch_edge_scatter(const BatchPtrs& b, cudaStream_t s) {
 }
 
 cudaError_t launch_hermite(const BatchPtrs& b, cudaStream_t s) {
-    LVN_VPC_DISPATCH(b.vpc, (k_hermite<V><<<persistent_grid(b, 8), kThreads, 0, s>>>(b)));
+    const int g = persistent_grid(b, 8);
+    switch (b.density.mode) {
+        case LVN_DENSITY_REFERENCE: LVN_VPC_DISPATCH(b.vpc, (k_hermite<V, LVN_DENSITY_REFERENCE><<<g, kThreads, 0, s>>>(b))); break;
+        case LVN_DENSITY_FBM2D: LVN_VPC_DISPATCH(b.vpc, (k_hermite<V, LVN_DENSITY_FBM2D><<<g, kThreads, 0, s>>>(b))); break;
+        default: LVN_VPC_DISPATCH(b.vpc, (k_hermite<V, LVN_DENSITY_CAVES><<<g, kThreads, 0, s>>>(b))); break;
+    }
     return cudaGetLastError();
 }
 
@@ -1494,6 +1639,11 @@ cudaError_t launch_mesh_count(const BatchPtrs& b, cudaStream_t s) {
 
 cudaError_t launch_mesh_plan(const BatchPtrs& b, cudaStream_t s) {
     k_mesh_plan<<<1, 1024, 0, s>>>(b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_export(const BatchPtrs& b, int which, void* dst, int64_t capacity, cudaStream_t s) {
+    k_export<<<persistent_grid(b, 4), 256, 0, s>>>(b, which, dst, capacity);
     return cudaGetLastError();
 }
 

@@ -17,7 +17,9 @@ struct BatchPtrs {
     int vpc;                     // voxels per chunk
     int crossing_mode;           // 0 = 17-sample search, 1 = linear
     int plain_class;             // 1: plain field edges are generated (fresh fields)
-    int derive_mats;             // 1: a chunk without operations holds only default / AIR materials
+    int derive_mats;             // 1: fresh fields: byte materials exist only inside a chunk's CSG box,
+                                 //    elsewhere they are the default material or AIR by the solid bits
+    int need_mats;               // 1: the field kernel writes every byte material (cached fields)
     int num_sms;
     DensityParams density;
     int32_t default_material;
@@ -28,6 +30,7 @@ struct BatchPtrs {
     const Brush* brushes;        // per-chunk op lists, flattened
 
     const uint8_t* perm;         // 65536 B permutation image (alpha channel)
+    const uint8_t* perm_k2;      // 65536 B: alpha & 15 (2D gradient index) per texel
     const float* grad;           // 16 x 4 gradient table
 
     uint8_t* mats;               // [n][F] field materials, index x + FD*y + FD*FD*z
@@ -122,5 +125,7 @@ cudaError_t launch_node_insert(const BatchPtrs& b, cudaStream_t stream);
 cudaError_t launch_mesh_count(const BatchPtrs& b, cudaStream_t stream);
 cudaError_t launch_mesh_plan(const BatchPtrs& b, cudaStream_t stream);
 cudaError_t launch_mesh_scatter(const BatchPtrs& b, cudaStream_t stream);
+// which: 0 vertices, 1 triangles, 2 seams; dst must be device-addressable
+cudaError_t launch_export(const BatchPtrs& b, int which, void* dst, int64_t capacity, cudaStream_t stream);
 
 }  // namespace lvn

@@ -39,12 +39,15 @@ __device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, fl
 }
 
 struct Noise {
-    const uint8_t* __restrict__ v;
-    const float* __restrict__ g;  // in shared memory when staged
+    const uint8_t* __restrict__ v;   // alpha channel (shuffled permutation value) per texel
+    const uint8_t* __restrict__ k2;  // low nibble of the alpha channel per texel (2D gradient index)
+    const float* __restrict__ g;     // 16 x 4 gradient table, staged in shared memory
 
     __device__ __forceinline__ int perm(int idx) const { return __ldg(v + idx); }
 
-    // snoise2 (simplex.cl:158-216)
+    // snoise2 (simplex.cl:158-216).  Texel (row, col) of corner 1 is (iy, ix+1)
+    // when x0 > y0 and (iy+1, ix) otherwise, so the three lookups share the
+    // wrapped row / column indices.
     __device__ __forceinline__ float snoise2(float px, float py) const {
         const float F2 = 0.366025403784f;
         const float G2 = 0.211324865405f;
@@ -56,21 +59,35 @@ struct Noise {
         const float x0 = px - (pix - t);
         const float y0 = py - (piy - t);
         const int ix = (int)pix, iy = (int)piy;
-        const int o1x = x0 > y0 ? 1 : 0;
-        const int o1y = 1 - o1x;
-        const int k0 = perm(texel(iy, ix)) & 15;
-        const int k1 = perm(texel(iy + o1y, ix + o1x)) & 15;
-        const int k2 = perm(texel(iy + 1, ix + 1)) & 15;
+        const bool xgt = x0 > y0;
+        const int r0 = (iy & 255) << 8, r1 = ((iy + 1) & 255) << 8;
+        const int c0 = ix & 255, c1 = (ix + 1) & 255;
+        const int k0 = __ldg(k2 + (r0 | c0));
+        const int k1 = __ldg(k2 + (xgt ? (r0 | c1) : (r1 | c0)));
+        const int kk2 = __ldg(k2 + (r1 | c1));
+        const float2* g2 = reinterpret_cast<const float2*>(g);
 
         float n0 = 0.f, n1 = 0.f, n2 = 0.f;
         float t0 = 0.5f - dot2(x0, y0, x0, y0);
-        if (!(t0 < 0.f)) { t0 = t0 * t0; n0 = (t0 * t0) * dot2(g[4 * k0], g[4 * k0 + 1], x0, y0); }
-        const float x1 = (x0 - (float)o1x) + G2, y1 = (y0 - (float)o1y) + G2;
+        if (!(t0 < 0.f)) {
+            const float2 gg = g2[2 * k0];
+            t0 = t0 * t0;
+            n0 = (t0 * t0) * dot2(gg.x, gg.y, x0, y0);
+        }
+        const float x1 = (x0 - (xgt ? 1.f : 0.f)) + G2, y1 = (y0 - (xgt ? 0.f : 1.f)) + G2;
         float t1 = 0.5f - dot2(x1, y1, x1, y1);
-        if (!(t1 < 0.f)) { t1 = t1 * t1; n1 = (t1 * t1) * dot2(g[4 * k1], g[4 * k1 + 1], x1, y1); }
+        if (!(t1 < 0.f)) {
+            const float2 gg = g2[2 * k1];
+            t1 = t1 * t1;
+            n1 = (t1 * t1) * dot2(gg.x, gg.y, x1, y1);
+        }
         const float x2 = x0 - C2, y2 = y0 - C2;
         float t2 = 0.5f - dot2(x2, y2, x2, y2);
-        if (!(t2 < 0.f)) { t2 = t2 * t2; n2 = (t2 * t2) * dot2(g[4 * k2], g[4 * k2 + 1], x2, y2); }
+        if (!(t2 < 0.f)) {
+            const float2 gg = g2[2 * kk2];
+            t2 = t2 * t2;
+            n2 = (t2 * t2) * dot2(gg.x, gg.y, x2, y2);
+        }
         return 70.f * ((n0 + n1) + n2);
     }
 

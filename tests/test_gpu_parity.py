@@ -344,3 +344,35 @@ def test_two_csg_batches_on_cached_field(lvn_gpu):
         assert m.vertices.shape[0] == ref.mesh_vertex_count()
     finally:
         g.close()
+
+
+def test_pinned_host_outputs(lvn_gpu, mg):
+    """Pinned host arrays are written by export kernels over the C2C link; the
+    result equals the pageable path byte for byte, and an array that is too
+    small is reported as a capacity error."""
+    torch = pytest.importorskip("torch")
+    lvn = lvn_gpu
+    lvn.set_density(**W.FBM2D)
+    wl = W.tiled_csg(2, 2, 2, n_ops=8, seed=5)
+    for op in wl.ops:
+        lvn.store_csg_operation(lvn.make_op(op.type, op.brush_shape, op.material, op.origin, op.dimensions))
+    V, T, S, res = mg.generate_chunks(wl.chunks)      # pageable numpy arrays
+    n = len(wl.chunks)
+    descs = (lvn.ChunkDesc * n)(*[lvn.ChunkDesc((C.c_int32 * 3)(*mn), s) for mn, s in wl.chunks])
+    results = (lvn.ChunkResult * n)()
+    cap_v, cap_t, cap_s = V.shape[0] + 7, T.shape[0] + 5, S.shape[0] + 3
+    hv = torch.zeros(cap_v * 12, dtype=torch.float32).pin_memory()
+    ht = torch.zeros(cap_t * 3, dtype=torch.int32).pin_memory()
+    hs = torch.zeros(cap_s * 12, dtype=torch.int32).pin_memory()
+    bo = lvn.BatchOut(lvn.LVN_MEMORY_HOST, hv.data_ptr(), cap_v, 0, ht.data_ptr(), cap_t, 0, hs.data_ptr(), cap_s, 0,
+                      C.cast(results, C.POINTER(lvn.ChunkResult)))
+    assert mg.generate_chunks_raw(descs, n, bo) == 0
+    assert (bo.total_vertices, bo.total_triangles, bo.total_seams) == (V.shape[0], T.shape[0], S.shape[0])
+    assert np.array_equal(hv.numpy().reshape(-1, 12)[:V.shape[0]].view(np.int32), V.view(np.int32))
+    assert np.array_equal(ht.numpy().reshape(-1, 3)[:T.shape[0]], T)
+    assert np.array_equal(hs.numpy().reshape(-1, 12)[:S.shape[0]], S)
+    small = lvn.BatchOut(lvn.LVN_MEMORY_HOST, hv.data_ptr(), cap_v, 0, ht.data_ptr(), 10, 0, hs.data_ptr(), cap_s, 0,
+                         C.cast(results, C.POINTER(lvn.ChunkResult)))
+    assert mg.generate_chunks_raw(descs, n, small) == lvn.LVN_ERR_CAPACITY
+    assert small.total_triangles == T.shape[0]
+    lvn.clear_csg_operations()
