@@ -43,6 +43,9 @@ def parse():
     p.add_argument("--impl", default="lvn", choices=["lvn", "reference"])
     p.add_argument("--cpu-sample", type=int, default=0, help="chunks in the CPU-baseline sample (0 = auto)")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--workload", default="tiled", choices=["tiled", "clipmap", "one"],
+                   help="tiled: 128 LOD0 chunks + 32 CSG ops (default); clipmap: 1024 chunks over LOD 0-4 with "
+                        "3D caves; one: a single LOD0 chunk")
     return p.parse_args()
 
 
@@ -107,10 +110,31 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+WORKLOAD = "tiled"
+
+
 def workload():
     from leven_gb300 import workloads as W
 
+    if WORKLOAD == "clipmap":
+        return W.clipmap_caves()
+    if WORKLOAD == "one":
+        return W.plain_one_chunk()
     return W.tiled_csg()
+
+
+def density_name(wl):
+    d = wl.density
+    if d["mode"] == 2:
+        return f"fbm2d-{d['octaves2']}oct + caves fbm3d-{d['octaves3']}oct, seed {wl.noise_seed}"
+    if d["mode"] == 1:
+        return f"fbm2d-{d['octaves2']}oct, seed {wl.noise_seed}"
+    return f"reference terrain, seed {wl.noise_seed}"
+
+
+def lod_range(wl):
+    lods = sorted({(s // 256).bit_length() - 1 for _, s in wl.chunks})
+    return lods[0] if len(lods) == 1 else f"{lods[0]}-{lods[-1]}"
 
 
 def cpu_baseline(wl, sample_chunks, threads):
@@ -124,7 +148,8 @@ def cpu_baseline(wl, sample_chunks, threads):
     O.set_seed(wl.noise_seed)
     d = wl.density
     dens = O.density(mode=d["mode"], octaves2=d["octaves2"], freq2=d["freq2"], lac2=d["lacunarity2"],
-                     gain2=d["gain2"], amp2=d["amp2"])
+                     gain2=d["gain2"], amp2=d["amp2"], octaves3=d.get("octaves3", 6), freq3=d.get("freq3", 1.0 / 64),
+                     lac3=d.get("lacunarity3", 2.0), gain3=d.get("gain3", 0.5), amp3=d.get("amp3", 12.0))
     # chunks spread over the workload (both y layers, with and without operations)
     idx = [int(i * len(wl.chunks) / sample_chunks) for i in range(sample_chunks)]
     args = (O.ChunkArgs * len(idx))()
@@ -168,7 +193,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * sample / value, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": wl.name, "chunks_per_step": sample, "voxels_per_chunk": 64, "csg_ops": len(wl.ops),
-                   "density": "fbm2d-8oct", "sample": f"{sample} of {len(wl.chunks)} chunks per step"},
+                   "density": density_name(wl), "sample": f"{sample} of {len(wl.chunks)} chunks per step"},
         "cpu_baseline": {"value": round(value, 3), "unit": "chunks/s", "cores": threads, "kind": "port",
                          "sample": f"{sample} chunks of the {len(wl.chunks)}-chunk workload per step"},
         "e2e": {"value": round(value, 3), "unit": "chunks/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -316,20 +341,25 @@ def run_lvn(args):
     dom_ms = stages[dominant][0] / stages[dominant][1]
     stage_ms = {k: round(v[0] / v[1], 4) for k, v in stages.items() if v[1]}
     E = int(res_np[:, 6].sum())
+    traffic = committed_traffic(dominant)
     if dominant == "hermite":
         # FP32 issue-rate roofline: SMs x 128 lanes x 2 flop x clock
         sms = torch.cuda.get_device_properties(dev).multi_processor_count
         clk = (clocks.summary()["sm_mhz"] or peaks.get("clocks_under_load", {}).get("sm_mhz_median", 1477.0))
         fp32_peak = sms * 128 * 2 * clk * 1e6 / 1e12
-        flops = hermite_flops(E, res_np)
-        roof = {"bound": "fp32", "achieved": round(flops / (dom_ms / 1e3) / 1e12, 3), "peak": round(fp32_peak, 2),
-                "unit": "TFLOP/s", "frac": round(flops / (dom_ms / 1e3) / 1e12 / fp32_peak, 4), "traffic": None,
+        if wl.density["mode"] != 1:
+            flops = None  # the per-evaluation count above is for the 2D fBm terrain
+        else:
+            flops = hermite_flops(*edge_axis_counts(mg, lvn, n))
+        ach = flops / (dom_ms / 1e3) / 1e12 if flops else None
+        roof = {"bound": "fp32", "achieved": round(ach, 3) if ach else None, "peak": round(fp32_peak, 2),
+                "unit": "TFLOP/s", "frac": round(ach / fp32_peak, 4) if ach else None, "traffic": traffic,
                 "kernel": dominant, "ms_per_launch": round(dom_ms, 4), "peak_source": f"SMs x 128 x 2 x {clk} MHz"}
     else:
         b = stage_work(dominant, res_np, n)
         ach = b / (dom_ms / 1e3) / 1e9 if b else None
         roof = {"bound": "hbm", "achieved": round(ach, 1) if ach else None, "peak": hbm_peak, "unit": "GB/s",
-                "frac": round(ach / hbm_peak, 4) if ach else None, "traffic": None, "kernel": dominant,
+                "frac": round(ach / hbm_peak, 4) if ach else None, "traffic": traffic, "kernel": dominant,
                 "ms_per_launch": round(dom_ms, 4), "peak_source": peak_src}
 
     bo = bo_host
@@ -341,7 +371,7 @@ def run_lvn(args):
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": wl.name, "chunks_per_step": n, "voxels_per_chunk": wl.voxels_per_chunk,
-                   "csg_ops": len(wl.ops), "density": "fbm2d-8oct seed 1", "lod": 0,
+                   "csg_ops": len(wl.ops), "density": density_name(wl), "lod": lod_range(wl),
                    "parallelism": f"replicas x{world}", "l2": "flushed between steps (256 MiB write)",
                    "vertices": int(bo.total_vertices), "triangles": int(bo.total_triangles),
                    "edges": E, "seams": int(bo.total_seams)},
@@ -365,20 +395,52 @@ def run_lvn(args):
         torch.distributed.destroy_process_group()
 
 
-def hermite_flops(E, res):
-    """Algorithmic FP32 operations of the hermite stage: per plain edge, the
-    density evaluations it needs (x/z edges: 17 search + 4 normal height
-    evaluations; y edges: 1 + 4) times the flops of one 8-octave 2D fBm
-    height evaluation (counted in the restatement: 8 x 56 per snoise2 plus
-    the octave update)."""
-    per_height = 8 * (56 + 4)
-    # edge axes are not reported per chunk; two thirds of terrain edges lie on x / z
-    per_edge = (2 * 21 + 1 * 5) / 3.0
-    return E * per_edge * per_height
+def committed_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary
+    (profiles/<kernel>_tiled_csg_128.md, line `dram_bytes_per_launch`)."""
+    path = ROOT / "profiles" / f"{kernel}_tiled_csg_128.md"
+    try:
+        for line in path.read_text().splitlines():
+            if "dram_bytes_per_launch" in line:
+                return int(line.split("|")[2].strip())
+    except (OSError, ValueError, IndexError):
+        pass
+    return None
+
+
+# FP32 operations of the restated density arithmetic (an fma counts 2):
+# one simplex2 evaluation with its three corners inside the kernel radius 51,
+# one octave of fBm 51 + 5, an 8-octave height term 8 * 56 + 4 = 452.
+FLOP_HEIGHT8 = 452
+# x / z edge: 17 search samples (height + density fma + 3 mix fmas) and 4
+# normal samples (height + density + offset), y normal pair, normalise;
+# y edge: one height, 17 cheap samples, the same normal work.
+FLOP_XZ_EDGE = 17 * (FLOP_HEIGHT8 + 2 + 6) + 4 * (FLOP_HEIGHT8 + 3) + 6 + 9 + 6
+FLOP_Y_EDGE = FLOP_HEIGHT8 + 17 * (2 + 6) + 4 * (FLOP_HEIGHT8 + 3) + 6 + 9 + 6
+
+
+def edge_axis_counts(mg, lvn, n):
+    """Plain x/z and y edge counts of the last batch (CSG-created edges excluded)."""
+    import numpy as np
+
+    nxz = ny = 0
+    for c in range(n):
+        keys = mg.debug_fetch(lvn.DEBUG_EDGE_KEYS, c, np.int32)
+        plain = mg.debug_fetch(lvn.DEBUG_PLAIN_EDGES, c, np.int32, max_elems=1)
+        axes = keys[:plain] & 3
+        ny += int((axes == 1).sum())
+        nxz += int(plain - (axes == 1).sum())
+    return nxz, ny
+
+
+def hermite_flops(nxz, ny):
+    return nxz * FLOP_XZ_EDGE + ny * FLOP_Y_EDGE
+
 
 
 if __name__ == "__main__":
     a = parse()
+    WORKLOAD = a.workload
     if a.impl == "reference":
         run_reference(a)
     else:

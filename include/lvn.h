@@ -49,6 +49,7 @@ extern "C" {
 #define LVN_OPT_CROSSING_MODE 1   /* 0 = 17-sample search (reference), 1 = linear     */
 #define LVN_OPT_CACHE         2   /* 1 = keep density-field / octree caches (default) */
 #define LVN_OPT_PROFILE       3   /* 1 = record per-stage CUDA events                 */
+#define LVN_OPT_GRAPHS        4   /* 1 = run batches as one captured CUDA graph (default) */
 
 /* CSGOperationInfo (leven/src/compute.h:16-24; apply_csg_operation.cl:5-14), 48 B */
 typedef struct lvn_csg_op {

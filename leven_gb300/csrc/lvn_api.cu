@@ -96,7 +96,7 @@ struct Global {
     int num_sms = 0;
     int32_t default_material = 0;
     int32_t seed = 0;
-    DevBuf perm, perm_k2, grad;
+    DevBuf perm, perm_k4, grad;
     DensityParams density{LVN_DENSITY_REFERENCE, 8, 1.f / 256.f, 2.f, 0.5f, 48.f, 6, 1.f / 64.f, 2.f, 0.5f, 12.f};
     std::vector<StoredOp> ops;
     std::mt19937 hash_gen;  // default-seeded, drawn in call order (compute_cuckoo.cpp:46-47)
@@ -158,13 +158,19 @@ int upload_perm(int seed) {
         }
         grad[4 * k + 3] = 0.f;
     }
-    std::vector<uint8_t> k2(65536);
-    for (int i = 0; i < 65536; i++) k2[i] = v[i] & 15;
+    // packed gradient indices of texel (j, i) and its wrapped +x, +y, +xy neighbours
+    std::vector<uint16_t> k4(65536);
+    for (int j = 0; j < 256; j++)
+        for (int i = 0; i < 256; i++) {
+            const int i1 = (i + 1) & 255, j1 = (j + 1) & 255;
+            k4[j * 256 + i] = (uint16_t)((v[j * 256 + i] & 15) | ((v[j * 256 + i1] & 15) << 4) |
+                                         ((v[j1 * 256 + i] & 15) << 8) | ((v[j1 * 256 + i1] & 15) << 12));
+        }
     LVN_CK(g.perm.ensure(65536));
-    LVN_CK(g.perm_k2.ensure(65536));
+    LVN_CK(g.perm_k4.ensure(sizeof(uint16_t) * 65536));
     LVN_CK(g.grad.ensure(sizeof(grad)));
     LVN_CK(cudaMemcpy(g.perm.p, v.data(), 65536, cudaMemcpyHostToDevice));
-    LVN_CK(cudaMemcpy(g.perm_k2.p, k2.data(), 65536, cudaMemcpyHostToDevice));
+    LVN_CK(cudaMemcpy(g.perm_k4.p, k4.data(), sizeof(uint16_t) * 65536, cudaMemcpyHostToDevice));
     LVN_CK(cudaMemcpy(g.grad.p, grad, sizeof(grad), cudaMemcpyHostToDevice));
     g.seed = seed;
     return LVN_OK;
@@ -303,6 +309,11 @@ struct lvn_meshgen {
     std::vector<ChunkState> last_cs;
     std::vector<ChunkDesc> last_desc;
 
+    // batch graph: the whole fresh-batch sequence captured once per key
+    cudaGraphExec_t graph_exec = nullptr;
+    std::vector<uintptr_t> graph_key;
+    bool use_graphs = true;
+
     // export of pinned host outputs: a side stream and its events
     cudaStream_t side = nullptr;
     cudaEvent_t ev_leaf = nullptr, ev_side = nullptr;
@@ -404,7 +415,7 @@ BatchPtrs make_ptrs(lvn_meshgen* m, int n) {
     b.bs = m->bs.as<BatchState>();
     b.brushes = m->brushes.as<Brush>();
     b.perm = g.perm.as<uint8_t>();
-    b.perm_k2 = g.perm_k2.as<uint8_t>();
+    b.perm_k4 = g.perm_k4.as<uint16_t>();
     b.grad = g.grad.as<float>();
     b.mats = m->mats.as<uint8_t>();
     b.planes = m->planes.as<uint4>();
@@ -531,13 +542,23 @@ bool direct_addresses(const lvn_batch_out* out, DirectOut* d) {
     return true;
 }
 
-int read_states(lvn_meshgen* m, int n) {
+int enqueue_state_readback(lvn_meshgen* m, int n) {
     LVN_CK(cudaMemcpyAsync(m->h_cs.p, m->cs.p, sizeof(ChunkState) * n, cudaMemcpyDeviceToHost, m->stream));
     LVN_CK(cudaMemcpyAsync(m->h_bs.p, m->bs.p, sizeof(BatchState), cudaMemcpyDeviceToHost, m->stream));
+    return LVN_OK;
+}
+
+int finish_states(lvn_meshgen* m, int n) {
     LVN_CK(cudaStreamSynchronize(m->stream));
     m->last_n = n;
     m->last_cs.assign(m->h_cs.as<ChunkState>(), m->h_cs.as<ChunkState>() + n);
     return LVN_OK;
+}
+
+int read_states(lvn_meshgen* m, int n) {
+    int rc = enqueue_state_readback(m, n);
+    if (rc) return rc;
+    return finish_states(m, n);
 }
 
 // Build the chunk descriptors of a batch of fresh chunks: density offset and
@@ -576,20 +597,29 @@ int build_descs(lvn_meshgen* m, const lvn_chunk_desc* chunks, int n, std::vector
     return LVN_OK;
 }
 
-int upload(lvn_meshgen* m, const std::vector<ChunkDesc>& descs, const std::vector<Brush>& brushes) {
-    const int n = (int)descs.size();
-    std::memcpy(m->h_desc.p, descs.data(), sizeof(ChunkDesc) * n);
-    LVN_CK(cudaMemcpyAsync(m->desc.p, m->h_desc.p, sizeof(ChunkDesc) * n, cudaMemcpyHostToDevice, m->stream));
-    if (!brushes.empty()) {
-        LVN_CK(m->h_brushes.ensure(sizeof(Brush) * brushes.size()));
-        LVN_CK(m->brushes.ensure(sizeof(Brush) * brushes.size()));
-        std::memcpy(m->h_brushes.p, brushes.data(), sizeof(Brush) * brushes.size());
-        LVN_CK(cudaMemcpyAsync(m->brushes.p, m->h_brushes.p, sizeof(Brush) * brushes.size(), cudaMemcpyHostToDevice,
-                               m->stream));
-    } else {
-        LVN_CK(m->brushes.ensure(sizeof(Brush)));
-    }
+// Host staging of a batch's descriptors and operations (pinned buffers).
+int stage_inputs(lvn_meshgen* m, const std::vector<ChunkDesc>& descs, const std::vector<Brush>& brushes) {
+    std::memcpy(m->h_desc.p, descs.data(), sizeof(ChunkDesc) * descs.size());
+    const size_t nb = std::max<size_t>(brushes.size(), 1);
+    LVN_CK(m->h_brushes.ensure(sizeof(Brush) * nb));
+    LVN_CK(m->brushes.ensure(sizeof(Brush) * nb));
+    if (!brushes.empty()) std::memcpy(m->h_brushes.p, brushes.data(), sizeof(Brush) * brushes.size());
     return LVN_OK;
+}
+
+// The copies of the staged inputs to the device (captured into batch graphs).
+int enqueue_inputs(lvn_meshgen* m, int n, size_t n_brushes) {
+    LVN_CK(cudaMemcpyAsync(m->desc.p, m->h_desc.p, sizeof(ChunkDesc) * n, cudaMemcpyHostToDevice, m->stream));
+    if (n_brushes)
+        LVN_CK(cudaMemcpyAsync(m->brushes.p, m->h_brushes.p, sizeof(Brush) * n_brushes, cudaMemcpyHostToDevice,
+                               m->stream));
+    return LVN_OK;
+}
+
+int upload(lvn_meshgen* m, const std::vector<ChunkDesc>& descs, const std::vector<Brush>& brushes) {
+    int rc = stage_inputs(m, descs, brushes);
+    if (rc) return rc;
+    return enqueue_inputs(m, (int)descs.size(), brushes.size());
 }
 
 // Redraw cuckoo parameters for chunks whose insert failed (the reference
@@ -618,7 +648,7 @@ int run_fresh_batch(lvn_meshgen* m, std::vector<ChunkDesc>& descs, const std::ve
     for (int attempt = 0; attempt < kMaxHashRetries + 2; attempt++) {
         int rc = ensure_pools(m, n, cap);
         if (rc) return rc;
-        rc = upload(m, descs, brushes);
+        rc = stage_inputs(m, descs, brushes);
         if (rc) return rc;
         BatchPtrs b = make_ptrs(m, n);
         if (dev_out) {
@@ -629,11 +659,57 @@ int run_fresh_batch(lvn_meshgen* m, std::vector<ChunkDesc>& descs, const std::ve
             b.seams = dev_out->seams;
             b.seam_cap = dev_out->seam_capacity;
         }
-        rc = enqueue_field_stages(m, b, !brushes.empty());
-        if (rc) return rc;
-        rc = enqueue_octree_stages(m, b, direct);
-        if (rc) return rc;
-        rc = read_states(m, n);
+        auto enqueue_all = [&]() -> int {
+            int r = enqueue_inputs(m, n, brushes.size());
+            if (!r) r = enqueue_field_stages(m, b, !brushes.empty());
+            if (!r) r = enqueue_octree_stages(m, b, direct);
+            if (!r) r = enqueue_state_readback(m, n);
+            return r;
+        };
+        if (m->use_graphs && !m->profile) {
+            // N3: the batch is one graph launch; re-captured only when a
+            // buffer, a capacity or the shape of the batch changes
+            std::vector<uintptr_t> key = {(uintptr_t)n, (uintptr_t)brushes.size(), (uintptr_t)m->crossing_mode,
+                                          (uintptr_t)g.density.mode, (uintptr_t)b.vertices, (uintptr_t)b.vertex_cap,
+                                          (uintptr_t)b.triangles, (uintptr_t)b.triangle_cap, (uintptr_t)b.seams,
+                                          (uintptr_t)b.seam_cap, (uintptr_t)b.ecap, (uintptr_t)b.vcap,
+                                          (uintptr_t)b.edge_slot_cap, (uintptr_t)b.node_slot_cap,
+                                          (uintptr_t)b.node_tile_cap, (uintptr_t)m->desc.p, (uintptr_t)m->brushes.p,
+                                          (uintptr_t)m->mats.p, (uintptr_t)m->edge_keys.p, (uintptr_t)m->node_codes.p,
+                                          (uintptr_t)m->edge_slots.p, (uintptr_t)m->node_slots.p,
+                                          (uintptr_t)m->h_desc.p, (uintptr_t)m->h_brushes.p, (uintptr_t)m->h_cs.p,
+                                          (uintptr_t)g.perm.p, (uintptr_t)(direct ? direct->dst[0] : nullptr),
+                                          (uintptr_t)(direct ? direct->dst[1] : nullptr),
+                                          (uintptr_t)(direct ? direct->dst[2] : nullptr),
+                                          (uintptr_t)(direct ? direct->cap[0] : 0), (uintptr_t)(direct ? direct->cap[1] : 0),
+                                          (uintptr_t)(direct ? direct->cap[2] : 0), (uintptr_t)g.default_material};
+            const uint32_t* dk = reinterpret_cast<const uint32_t*>(&g.density);
+            for (size_t i = 0; i < sizeof(g.density) / 4; i++) key.push_back(dk[i]);
+            if (!m->graph_exec || key != m->graph_key) {
+                if (m->graph_exec) {
+                    cudaGraphExecDestroy(m->graph_exec);
+                    m->graph_exec = nullptr;
+                }
+                cudaGraph_t graph = nullptr;
+                LVN_CK(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
+                const int r = enqueue_all();
+                const cudaError_t ce = cudaStreamEndCapture(m->stream, &graph);
+                if (r) {
+                    if (graph) cudaGraphDestroy(graph);
+                    return r;
+                }
+                LVN_CK(ce);
+                const cudaError_t ie = cudaGraphInstantiate(&m->graph_exec, graph, 0);
+                cudaGraphDestroy(graph);
+                LVN_CK(ie);
+                m->graph_key = key;
+            }
+            LVN_CK(cudaGraphLaunch(m->graph_exec, m->stream));
+        } else {
+            rc = enqueue_all();
+            if (rc) return rc;
+        }
+        rc = finish_states(m, n);
         if (rc) return rc;
         m->last_fresh = true;
         m->last_desc = descs;
@@ -946,7 +1022,7 @@ int lvn_initialise(int32_t noise_seed, uint32_t default_material, int32_t num_cs
 
 int lvn_shutdown(void) {
     g.perm.release();
-    g.perm_k2.release();
+    g.perm_k4.release();
     g.grad.release();
     g.ops.clear();
     g.initialised = false;
@@ -1040,6 +1116,7 @@ void lvn_meshgen_destroy(lvn_meshgen* m) {
     }
     for (int i = 0; i <= ST_COUNT; i++)
         if (m->ev[i]) cudaEventDestroy(m->ev[i]);
+    if (m->graph_exec) cudaGraphExecDestroy(m->graph_exec);
     if (m->ev_leaf) cudaEventDestroy(m->ev_leaf);
     if (m->ev_side) cudaEventDestroy(m->ev_side);
     if (m->side) cudaStreamDestroy(m->side);
@@ -1069,6 +1146,7 @@ int lvn_meshgen_set_option(lvn_meshgen* m, int32_t option, int32_t value) {
             return LVN_OK;
         case LVN_OPT_CACHE: m->cache = value != 0; return LVN_OK;
         case LVN_OPT_PROFILE: m->profile = value != 0; return LVN_OK;
+        case LVN_OPT_GRAPHS: m->use_graphs = value != 0; return LVN_OK;
         default: return LVN_ERR_INVALID;
     }
 }
@@ -1284,7 +1362,7 @@ GlobalView global_view() {
     v.num_sms = g.num_sms;
     v.default_material = g.default_material;
     v.perm = g.perm.as<uint8_t>();
-    v.perm_k2 = g.perm_k2.as<uint8_t>();
+    v.perm_k4 = g.perm_k4.as<uint16_t>();
     v.grad = g.grad.as<float>();
     v.density = g.density;
     return v;

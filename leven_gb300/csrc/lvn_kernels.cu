@@ -442,7 +442,7 @@ __global__ void __launch_bounds__(96) k_field(BatchPtrs b) {
     // descriptor fields in registers: the byte stores below may alias them
     const int scale = b.desc[c].scale;
     const int ox = b.desc[c].off[0], oy = b.desc[c].off[1], oz = b.desc[c].off[2];
-    const Noise nz{b.perm, b.perm_k2, sg};
+    const Noise nz{b.perm, b.perm_k4, sg};
     const DensityParams& dp = b.density;
     const float wx = (float)(x * scale + ox);
     const float wz = (float)(z * scale + oz);
@@ -963,7 +963,7 @@ __global__ void __launch_bounds__(kThreads) k_hermite(BatchPtrs b) {
     if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
     __syncthreads();
     if (b.bs->overflow) return;
-    const Noise nz{b.perm, b.perm_k2, sg};
+    const Noise nz{b.perm, b.perm_k4, sg};
     // work list segments: plain x/z edges, plain y edges, CSG-created edges, so
     // that a warp's 32 edges take the same path
     const int nplain = b.bs->total_xz + b.bs->total_y;

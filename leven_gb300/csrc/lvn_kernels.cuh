@@ -30,7 +30,8 @@ struct BatchPtrs {
     const Brush* brushes;        // per-chunk op lists, flattened
 
     const uint8_t* perm;         // 65536 B permutation image (alpha channel)
-    const uint8_t* perm_k2;      // 65536 B: alpha & 15 (2D gradient index) per texel
+    const uint16_t* perm_k4;     // 65536 x 16 bit: the 2D gradient indices of a texel and its +x, +y, +xy
+                                 // neighbours (wrapping), 4 bits each
     const float* grad;           // 16 x 4 gradient table
 
     uint8_t* mats;               // [n][F] field materials, index x + FD*y + FD*FD*z

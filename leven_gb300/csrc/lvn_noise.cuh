@@ -39,15 +39,16 @@ __device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, fl
 }
 
 struct Noise {
-    const uint8_t* __restrict__ v;   // alpha channel (shuffled permutation value) per texel
-    const uint8_t* __restrict__ k2;  // low nibble of the alpha channel per texel (2D gradient index)
-    const float* __restrict__ g;     // 16 x 4 gradient table, staged in shared memory
+    const uint8_t* __restrict__ v;    // alpha channel (shuffled permutation value) per texel
+    const uint16_t* __restrict__ k4;  // per texel (row j, col i): the 2D gradient indices (alpha & 15) of
+                                      // texels (j, i), (j, i+1), (j+1, i), (j+1, i+1), 4 bits each
+    const float* __restrict__ g;      // 16 x 4 gradient table, staged in shared memory
 
     __device__ __forceinline__ int perm(int idx) const { return __ldg(v + idx); }
 
-    // snoise2 (simplex.cl:158-216).  Texel (row, col) of corner 1 is (iy, ix+1)
-    // when x0 > y0 and (iy+1, ix) otherwise, so the three lookups share the
-    // wrapped row / column indices.
+    // snoise2 (simplex.cl:158-216).  The three corners' texels are (iy, ix),
+    // (iy, ix+1) or (iy+1, ix) by the x0 > y0 test, and (iy+1, ix+1): one
+    // 16-bit load holds all their gradient indices.
     __device__ __forceinline__ float snoise2(float px, float py) const {
         const float F2 = 0.366025403784f;
         const float G2 = 0.211324865405f;
@@ -60,11 +61,10 @@ struct Noise {
         const float y0 = py - (piy - t);
         const int ix = (int)pix, iy = (int)piy;
         const bool xgt = x0 > y0;
-        const int r0 = (iy & 255) << 8, r1 = ((iy + 1) & 255) << 8;
-        const int c0 = ix & 255, c1 = (ix + 1) & 255;
-        const int k0 = __ldg(k2 + (r0 | c0));
-        const int k1 = __ldg(k2 + (xgt ? (r0 | c1) : (r1 | c0)));
-        const int kk2 = __ldg(k2 + (r1 | c1));
+        const unsigned q = __ldg(k4 + (((iy & 255) << 8) | (ix & 255)));
+        const int k0 = q & 15;
+        const int k1 = (q >> (xgt ? 4 : 8)) & 15;
+        const int kk2 = q >> 12;
         const float2* g2 = reinterpret_cast<const float2*>(g);
 
         float n0 = 0.f, n1 = 0.f, n2 = 0.f;

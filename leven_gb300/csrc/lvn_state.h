@@ -12,7 +12,7 @@ struct GlobalView {
     int num_sms;
     int32_t default_material;
     const uint8_t* perm;   // device permutation image (65536 B)
-    const uint8_t* perm_k2;  // device alpha & 15 per texel (65536 B)
+    const uint16_t* perm_k4;  // device packed 2D gradient indices per texel (65536 x 16 bit)
     const float* grad;     // device gradient table (16 x 4)
     DensityParams density;
 };

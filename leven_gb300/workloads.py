@@ -133,3 +133,72 @@ def ops_for_chunk(ops, mn, size):
                 mn[1] > hi[1] or mn[2] > hi[2]):
             out.append(op)
     return out
+
+
+# Clipmap LOD selection (leven/src/clipmap.cpp:28-41, 1056-1128)
+CLIPMAP_LEAF_SIZE = 256
+NUM_LODS = 6
+LOD_MAX_NODE_SIZE = CLIPMAP_LEAF_SIZE * (1 << (NUM_LODS - 1))
+LOD_ACTIVE_DISTANCES = [0.0, CLIPMAP_LEAF_SIZE * 1.5, CLIPMAP_LEAF_SIZE * 3.5, CLIPMAP_LEAF_SIZE * 5.5,
+                        CLIPMAP_LEAF_SIZE * 7.5, CLIPMAP_LEAF_SIZE * 13.5]
+
+
+def distance_to_node(mn, size, cam):
+    """DistanceToNode (clipmap.cpp:1056-1064): distance from the camera to the node's box."""
+    d2 = 0.0
+    for i in range(3):
+        lo, hi = mn[i], mn[i] + size
+        d = max(lo - cam[i], 0.0, cam[i] - hi)
+        d2 += d * d
+    return d2 ** 0.5
+
+
+def select_clipmap_nodes(root_min, root_size, cam):
+    """SelectActiveClipmapNodes (clipmap.cpp:1084-1128) over a complete clipmap
+    octree whose leaves are CLIPMAP_LEAF_SIZE nodes: a node no larger than
+    LOD_MAX_NODE_SIZE is selected when its distance to the camera is at least
+    its LOD's active distance and no ancestor was selected."""
+    out = []
+
+    def visit(mn, size, parent_active):
+        active = False
+        if not parent_active and size <= LOD_MAX_NODE_SIZE:
+            lod = (size // CLIPMAP_LEAF_SIZE).bit_length() - 1
+            if distance_to_node(mn, size, cam) >= LOD_ACTIVE_DISTANCES[lod]:
+                out.append((tuple(mn), size))
+                active = True
+        if size == CLIPMAP_LEAF_SIZE or parent_active or active:
+            return  # nothing below a selected node is selected
+        half = size // 2
+        for i in range(8):
+            off = ((i >> 2) & 1, (i >> 1) & 1, i & 1)  # CHILD_MIN_OFFSETS order
+            visit(tuple(mn[k] + off[k] * half for k in range(3)), half, parent_active or active)
+
+    visit(tuple(root_min), root_size, False)
+    return out
+
+
+def clipmap_caves(n_chunks=1024, max_lod=4, seed=1):
+    """configs[2]: n_chunks chunks over clipmap LODs 0..max_lod, density = 2D
+    fBm heightfield + 3D fBm caves (6 octaves, 1/64, amplitude 12).  One
+    camera selects about 370 nodes of LOD <= 4 (SelectActiveClipmapNodes over
+    a 2^15-unit world centred on the origin), so the chunks are the union of
+    the selections of a camera moving along a seeded straight path, as the
+    engine re-meshes while the camera travels, nearest-first to the starting
+    camera."""
+    rng = MT19937(seed)
+    cam0 = (rng.uniform(-2048.0, 2048.0), rng.uniform(-64.0, 64.0), rng.uniform(-2048.0, 2048.0))
+    step = (rng.uniform(-1.0, 1.0) * 512.0, 0.0, rng.uniform(-1.0, 1.0) * 512.0)
+    root_size = 1 << 15
+    root_min = (-root_size // 2, -root_size // 2, -root_size // 2)
+    chosen = {}
+    for k in range(64):
+        cam = tuple(cam0[i] + k * step[i] for i in range(3))
+        for mn, size in select_clipmap_nodes(root_min, root_size, cam):
+            if size <= CLIPMAP_LEAF_SIZE << max_lod:
+                chosen[(mn, size)] = True
+        if len(chosen) >= 2 * n_chunks:
+            break
+    nodes = sorted(chosen, key=lambda nd: (distance_to_node(nd[0], nd[1], cam0), nd[1], nd[0]))[:n_chunks]
+    return Workload(f"clipmap-caves-{len(nodes)}chunks-lod0-{max_lod}", [(tuple(mn), size) for mn, size in nodes], [],
+                    CAVES)

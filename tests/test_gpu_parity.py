@@ -376,3 +376,26 @@ def test_pinned_host_outputs(lvn_gpu, mg):
     assert mg.generate_chunks_raw(descs, n, small) == lvn.LVN_ERR_CAPACITY
     assert small.total_triangles == T.shape[0]
     lvn.clear_csg_operations()
+
+
+def test_graph_and_stream_paths_agree(lvn_gpu):
+    """A batch replayed from its captured CUDA graph equals the same batch
+    enqueued kernel by kernel, and a re-capture follows a change of shape."""
+    lvn = lvn_gpu
+    lvn.set_density(**W.FBM2D)
+    wl = W.tiled_csg(3, 2, 3, n_ops=12, seed=9)
+    lvn.clear_csg_operations()
+    for op in wl.ops:
+        lvn.store_csg_operation(lvn.make_op(op.type, op.brush_shape, op.material, op.origin, op.dimensions))
+    a, b = lvn.MeshGen(64), lvn.MeshGen(64)
+    try:
+        b.set_option(lvn.LVN_OPT_GRAPHS, 0)
+        for chunks in (wl.chunks, wl.chunks[:7], wl.chunks):
+            ra = a.generate_chunks(chunks)
+            rb = b.generate_chunks(chunks)
+            for x, y in zip(ra, rb):
+                assert np.array_equal(np.asarray(x).view(np.uint8), np.asarray(y).view(np.uint8))
+    finally:
+        a.close()
+        b.close()
+        lvn.clear_csg_operations()
