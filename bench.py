@@ -16,6 +16,13 @@ hermite data, leaves + QEF, cuckoo tables, mesh, seams.
 `--impl reference` times the CPU restatement of the reference algorithm
 (oracle/, the reference's OpenCL cannot run here) on all host threads over
 a bounded sample of the same workload.
+
+`--workload clipmap`: 1024 chunks over clipmap LODs 0-4 around a moving
+seeded camera, 2D fBm heightfield + 3D fBm caves, followed by the octree
+simplification at QEF error 0.05 (CPU baseline: the same, simplification
+included).  `--surrogate`: trains the learned density surrogate on the GPU
+and meshes the clipmap chunk set with the 2D fBm density plain and through
+the surrogate (its own JSON line, impl "lvn-surrogate").
 """
 import argparse
 import ctypes as C
@@ -41,8 +48,17 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="lvn", choices=["lvn", "reference"])
-    p.add_argument("--cpu-sample", type=int, default=0, help="chunks in the CPU-baseline sample (0 = auto)")
+    p.add_argument("--cpu-sample", type=int, default=0, help="chunks per CPU-baseline sample (0 = whole-workload passes for >= 10 s; reference arm: about 2 s per step)")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-autotune", action="store_true", help="keep the built-in persistent-grid shapes")
+    p.add_argument("--surrogate", action="store_true",
+                   help="learned-density run: train the surrogate (2^24 samples of the 2D fBm density, Adam), then "
+                        "mesh the 1024-chunk clipmap set plain and with the surrogate")
+    p.add_argument("--train-steps", type=int, default=20000)
+    p.add_argument("--gate", type=float, default=0.5, help="surrogate probe gate (density units)")
+    p.add_argument("--simplify", type=float, default=None,
+                   help="octree simplification QEF-error threshold (voxel^2); default 0.05 for the clipmap "
+                        "workload, off otherwise; < 0 = off")
     p.add_argument("--workload", default="tiled", choices=["tiled", "clipmap", "one"],
                    help="tiled: 128 LOD0 chunks + 32 CSG ops (default); clipmap: 1024 chunks over LOD 0-4 with "
                         "3D caves; one: a single LOD0 chunk")
@@ -113,6 +129,16 @@ class ClockSampler:
 WORKLOAD = "tiled"
 
 
+def simplify_threshold(args):
+    if args.simplify is not None:
+        return args.simplify
+    return 0.05 if WORKLOAD == "clipmap" else -1.0
+
+
+def simp_name(thr):
+    return f"octree QEF error <= {thr} voxel^2" if thr >= 0 else None
+
+
 def workload():
     from leven_gb300 import workloads as W
 
@@ -137,34 +163,58 @@ def lod_range(wl):
     return lods[0] if len(lods) == 1 else f"{lods[0]}-{lods[-1]}"
 
 
-def cpu_baseline(wl, sample_chunks, threads):
-    """The oracle (CPU restatement of the reference algorithm) meshing a bounded
-    sample of the workload's chunks on `threads` host threads."""
-    sys.path.insert(0, str(ROOT / "tests"))
-    import oracle_lib as O
-    from leven_gb300 import workloads as W
+class CpuBaseline:
+    """The oracle (CPU restatement of the reference algorithm) meshing chunks of
+    the workload on `threads` host threads, one orc_mesh_chunks call per pass."""
 
-    O.build()
-    O.set_seed(wl.noise_seed)
-    d = wl.density
-    dens = O.density(mode=d["mode"], octaves2=d["octaves2"], freq2=d["freq2"], lac2=d["lacunarity2"],
-                     gain2=d["gain2"], amp2=d["amp2"], octaves3=d.get("octaves3", 6), freq3=d.get("freq3", 1.0 / 64),
-                     lac3=d.get("lacunarity3", 2.0), gain3=d.get("gain3", 0.5), amp3=d.get("amp3", 12.0))
-    # chunks spread over the workload (both y layers, with and without operations)
-    idx = [int(i * len(wl.chunks) / sample_chunks) for i in range(sample_chunks)]
-    args = (O.ChunkArgs * len(idx))()
-    keep = []
-    for j, c in enumerate(idx):
-        mn, size = wl.chunks[c]
-        ops = O.make_ops([op.as_tuple() for op in W.ops_for_chunk(wl.ops, mn, size)])
-        keep.append(ops)
-        n_ops = len(W.ops_for_chunk(wl.ops, mn, size))
-        args[j] = O.ChunkArgs((C.c_int32 * 3)(*mn), size, wl.voxels_per_chunk, 0, 0, n_ops,
-                              C.cast(ops, C.POINTER(O.CsgOp)), 5489)
-    t0 = time.perf_counter()
-    O.lib().orc_mesh_chunks(C.byref(dens), args, len(idx), threads)
-    dt = time.perf_counter() - t0
-    return len(idx) / dt, dt, len(idx)
+    def __init__(self, wl, threads, simplify=-1.0):
+        sys.path.insert(0, str(ROOT / "tests"))
+        import oracle_lib as O
+        from leven_gb300 import workloads as W
+
+        O.build()
+        O.set_seed(wl.noise_seed)
+        self.O, self.threads, self.n, self.simplify = O, threads, len(wl.chunks), simplify
+        d = wl.density
+        self.dens = O.density(mode=d["mode"], octaves2=d["octaves2"], freq2=d["freq2"], lac2=d["lacunarity2"],
+                              gain2=d["gain2"], amp2=d["amp2"], octaves3=d.get("octaves3", 6),
+                              freq3=d.get("freq3", 1.0 / 64), lac3=d.get("lacunarity3", 2.0),
+                              gain3=d.get("gain3", 0.5), amp3=d.get("amp3", 12.0))
+        self.args = (O.ChunkArgs * self.n)()
+        self.keep = []
+        for j, (mn, size) in enumerate(wl.chunks):
+            mine = W.ops_for_chunk(wl.ops, mn, size)
+            ops = O.make_ops([op.as_tuple() for op in mine])
+            self.keep.append(ops)
+            self.args[j] = O.ChunkArgs((C.c_int32 * 3)(*mn), size, wl.voxels_per_chunk, 0, 0, len(mine),
+                                       C.cast(ops, C.POINTER(O.CsgOp)), 5489)
+
+    def run(self, count):
+        """Mesh `count` chunks spread evenly over the workload; returns seconds."""
+        if count >= self.n:
+            arr, m = self.args, self.n
+        else:
+            arr = (self.O.ChunkArgs * count)()
+            for j in range(count):
+                arr[j] = self.args[int(j * self.n / count)]
+            m = count
+        t0 = time.perf_counter()
+        self.O.lib().orc_mesh_chunks_simplified(C.byref(self.dens), arr, m, self.threads, self.simplify)
+        return time.perf_counter() - t0
+
+    def rate(self, target_s):
+        """Whole-workload passes until at least target_s seconds of CPU work."""
+        done, total = 0, 0.0
+        while total < target_s:
+            total += self.run(self.n)
+            done += self.n
+        return done / total, total, done
+
+    def step_chunks(self, step_s):
+        """Chunks one step of about step_s seconds meshes (calibrated on a small sample)."""
+        m = min(self.n, max(self.threads, 16))
+        r = m / self.run(m)
+        return int(min(self.n, max(self.threads, r * step_s)))
 
 
 def host_threads():
@@ -180,20 +230,21 @@ def run_reference(args):
         return
     wl = workload()
     threads = host_threads()
-    sample = args.cpu_sample or max(threads, 16)
+    cb = CpuBaseline(wl, threads, simplify_threshold(args))
+    sample = args.cpu_sample or cb.step_chunks(2.0)
     vals = []
     for _ in range(args.warmup):
-        cpu_baseline(wl, min(sample, threads), threads)
+        cb.run(min(sample, threads))
     for _ in range(args.steps):
-        v, dt, n = cpu_baseline(wl, sample, threads)
-        vals.append(v)
+        vals.append(sample / cb.run(sample))
     value = statistics.median(vals)
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "chunks/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * sample / value, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": wl.name, "chunks_per_step": sample, "voxels_per_chunk": 64, "csg_ops": len(wl.ops),
-                   "density": density_name(wl), "sample": f"{sample} of {len(wl.chunks)} chunks per step"},
+                   "density": density_name(wl), "simplify": simp_name(simplify_threshold(args)),
+                   "sample": f"{sample} of {len(wl.chunks)} chunks per step"},
         "cpu_baseline": {"value": round(value, 3), "unit": "chunks/s", "cores": threads, "kind": "port",
                          "sample": f"{sample} chunks of the {len(wl.chunks)}-chunk workload per step"},
         "e2e": {"value": round(value, 3), "unit": "chunks/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -247,6 +298,9 @@ def run_lvn(args):
         lvn.store_csg_operation(lvn.make_op(op.type, op.brush_shape, op.material, op.origin, op.dimensions))
     mg = lvn.MeshGen(wl.voxels_per_chunk)
     mg.set_option(lvn.LVN_OPT_CACHE, 0)
+    simp = simplify_threshold(args)
+    if simp >= 0:
+        mg.set_simplify(simp)
     stream = torch.cuda.ExternalStream(mg.stream(), device=dev)
     n = len(wl.chunks)
     descs = (lvn.ChunkDesc * n)()
@@ -254,6 +308,8 @@ def run_lvn(args):
         descs[i] = lvn.ChunkDesc((C.c_int32 * 3)(*mn), size)
     results = (lvn.ChunkResult * n)()
 
+    # launch shapes for this batch (outside the timed region, like a compile)
+    tuned = None if args.no_autotune else mg.autotune(wl.chunks)
     # size the outputs once from a first run
     _, _, _, res = mg.generate_chunks(wl.chunks)
     tot_v = int(res[:, 7].sum())
@@ -342,19 +398,24 @@ def run_lvn(args):
     stage_ms = {k: round(v[0] / v[1], 4) for k, v in stages.items() if v[1]}
     E = int(res_np[:, 6].sum())
     traffic = committed_traffic(dominant)
-    if dominant == "hermite":
+    df = density_flops(wl)
+    if dominant in ("hermite", "field") and df is not None and (dominant == "hermite" or wl.density["mode"] == 2):
         # FP32 issue-rate roofline: SMs x 128 lanes x 2 flop x clock
         sms = torch.cuda.get_device_properties(dev).multi_processor_count
         clk = (clocks.summary()["sm_mhz"] or peaks.get("clocks_under_load", {}).get("sm_mhz_median", 1477.0))
         fp32_peak = sms * 128 * 2 * clk * 1e6 / 1e12
-        if wl.density["mode"] != 1:
-            flops = None  # the per-evaluation count above is for the 2D fBm terrain
-        else:
-            flops = hermite_flops(*edge_axis_counts(mg, lvn, n))
-        ach = flops / (dom_ms / 1e3) / 1e12 if flops else None
-        roof = {"bound": "fp32", "achieved": round(ach, 3) if ach else None, "peak": round(fp32_peak, 2),
-                "unit": "TFLOP/s", "frac": round(ach / fp32_peak, 4) if ach else None, "traffic": traffic,
-                "kernel": dominant, "ms_per_launch": round(dom_ms, 4), "peak_source": f"SMs x 128 x 2 x {clk} MHz"}
+        if dominant == "hermite":
+            fxz, fy = hermite_edge_flops(*df)
+            nxz, ny = edge_axis_counts(mg, lvn, n)
+            flops = nxz * fxz + ny * fy
+        else:  # every field point of every chunk: the height per column, the cave term per point
+            fd = wl.voxels_per_chunk + 2
+            flops = n * (fd * fd * df[0] + fd ** 3 * df[1])
+        ach = flops / (dom_ms / 1e3) / 1e12
+        roof = {"bound": "fp32", "achieved": round(ach, 3), "peak": round(fp32_peak, 2),
+                "unit": "TFLOP/s", "frac": round(ach / fp32_peak, 4), "traffic": traffic,
+                "kernel": dominant, "ms_per_launch": round(dom_ms, 4), "peak_source": f"SMs x 128 x 2 x {clk} MHz",
+                "flop_per_launch": int(flops)}
     else:
         b = stage_work(dominant, res_np, n)
         ach = b / (dom_ms / 1e3) / 1e9 if b else None
@@ -372,6 +433,8 @@ def run_lvn(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": wl.name, "chunks_per_step": n, "voxels_per_chunk": wl.voxels_per_chunk,
                    "csg_ops": len(wl.ops), "density": density_name(wl), "lod": lod_range(wl),
+                   "simplify": simp_name(simp), "leaf_vertices": int(res_np[:, 7].sum()),
+                   "launch_shapes": {"autotuned_ctas_per_sm": tuned} if tuned else "built-in",
                    "parallelism": f"replicas x{world}", "l2": "flushed between steps (256 MiB write)",
                    "vertices": int(bo.total_vertices), "triangles": int(bo.total_triangles),
                    "edges": E, "seams": int(bo.total_seams)},
@@ -384,10 +447,17 @@ def run_lvn(args):
     }
     if rank == 0 and not args.no_cpu_baseline:
         threads = host_threads()
-        sample = args.cpu_sample or max(threads, 16)
-        v, dt, m = cpu_baseline(wl, sample, threads)
+        cb = CpuBaseline(wl, threads, simp)
+        if args.cpu_sample:
+            dt = cb.run(args.cpu_sample)
+            m = min(args.cpu_sample, n)
+            v = m / dt
+            what = f"{m} chunks spread over the {n}-chunk workload, {dt:.1f} s"
+        else:
+            v, dt, m = cb.rate(10.0)
+            what = f"{m // n} passes over the {n}-chunk workload ({m} chunks), {dt:.1f} s"
         line["cpu_baseline"] = {"value": round(v, 3), "unit": "chunks/s", "cores": threads, "kind": "port",
-                                "sample": f"{m} chunks of the {n}-chunk workload, {dt:.1f} s"}
+                                "sample": what}
     if rank == 0:
         print(json.dumps(line), flush=True)
     mg.close()
@@ -410,13 +480,30 @@ def committed_traffic(kernel):
 
 # FP32 operations of the restated density arithmetic (an fma counts 2):
 # one simplex2 evaluation with its three corners inside the kernel radius 51,
-# one octave of fBm 51 + 5, an 8-octave height term 8 * 56 + 4 = 452.
+# one octave of fBm 51 + 5, an 8-octave height term 8 * 56 + 4 = 452;
+# one simplex3 evaluation 102, one octave of 3D fBm 108, the 6-octave cave
+# term 6 * 108 + 3 = 651 plus its fma.
 FLOP_HEIGHT8 = 452
-# x / z edge: 17 search samples (height + density fma + 3 mix fmas) and 4
-# normal samples (height + density + offset), y normal pair, normalise;
-# y edge: one height, 17 cheap samples, the same normal work.
-FLOP_XZ_EDGE = 17 * (FLOP_HEIGHT8 + 2 + 6) + 4 * (FLOP_HEIGHT8 + 3) + 6 + 9 + 6
-FLOP_Y_EDGE = FLOP_HEIGHT8 + 17 * (2 + 6) + 4 * (FLOP_HEIGHT8 + 3) + 6 + 9 + 6
+FLOP_CAVES6 = 651 + 2
+
+
+def density_flops(wl):
+    """(per-column height term, per-point rest) FP32 operations, or None."""
+    d = wl.density
+    if d["mode"] == 1 and d["octaves2"] == 8:
+        return FLOP_HEIGHT8, 2
+    if d["mode"] == 2 and d["octaves2"] == 8 and d["octaves3"] == 6:
+        return FLOP_HEIGHT8, 2 + FLOP_CAVES6
+    return None
+
+
+def hermite_edge_flops(h, p):
+    """x / z edge: 17 search samples (height + point + 3 mix fmas) and 4
+    normal samples with their own height; y edge: the height once.  Both add
+    the y normal pair (shared height) and the normalisation (21)."""
+    xz = 17 * (h + p + 6) + 4 * (h + p + 3) + 2 * p + 21
+    y = h + 17 * (p + 6) + 4 * (h + p + 3) + 2 * p + 21
+    return xz, y
 
 
 def edge_axis_counts(mg, lvn, n):
@@ -433,9 +520,116 @@ def edge_axis_counts(mg, lvn, n):
     return nxz, ny
 
 
-def hermite_flops(nxz, ny):
-    return nxz * FLOP_XZ_EDGE + ny * FLOP_Y_EDGE
+def hausdorff_voxels(va, vb, voxel):
+    """Symmetric Hausdorff distance between two vertex sets, in voxels."""
+    from scipy.spatial import cKDTree
 
+    if len(va) == 0 or len(vb) == 0:
+        return None
+    d1 = cKDTree(vb).query(va)[0].max()
+    d2 = cKDTree(va).query(vb)[0].max()
+    return float(max(d1, d2)) / voxel
+
+
+def run_surrogate(args):
+    """Plain vs learned-density meshing of the clipmap chunk set (LOD 0-4)
+    with the 2D fBm density the surrogate is trained on."""
+    import numpy as np
+    import torch
+
+    import leven_gb300 as lvn
+    from leven_gb300 import workloads as W
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    chunks = W.clipmap_caves().chunks
+    lvn.initialise(1, 0, 2)
+    lvn.set_density(**W.FBM2D)
+    lvn.clear_csg_operations()
+    lo, hi = (-1024.0, -128.0, -1024.0), (1024.0, 128.0, 1024.0)
+    sur = lvn.Surrogate(lo, hi, seed=1)
+    t0 = time.perf_counter()
+    sur.sample(1 << 24, seed=1)
+    t_sample = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    losses = sur.train(args.train_steps, batch=65536, lr=1e-3)
+    t_train = time.perf_counter() - t0
+    train_flop = 3 * 2 * (96 * 128 + 3 * 128 * 128 + 128) * 65536 * args.train_steps
+
+    n = len(chunks)
+    descs = (lvn.ChunkDesc * n)()
+    for i, (mn, size) in enumerate(chunks):
+        descs[i] = lvn.ChunkDesc((C.c_int32 * 3)(*mn), size)
+    results = (lvn.ChunkResult * n)()
+    mg = lvn.MeshGen(64)
+    mg.set_option(lvn.LVN_OPT_CACHE, 0)
+    stream = torch.cuda.ExternalStream(mg.stream(), device=dev)
+    Vp, Tp, Sp, resp = mg.generate_chunks(chunks)
+    cap_v, cap_t, cap_s = int(resp[:, 7].sum()) + 1024, 2 * Tp.shape[0] + 4096, Sp.shape[0] + 1024
+    d_vert = torch.empty(cap_v * 12, dtype=torch.float32, device=dev)
+    d_tri = torch.empty(cap_t * 3, dtype=torch.int32, device=dev)
+    d_seam = torch.empty(cap_s * 12, dtype=torch.int32, device=dev)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.int32, device=dev)
+
+    def timed(steps, warmup):
+        bo = lvn.BatchOut(lvn.LVN_MEMORY_DEVICE, d_vert.data_ptr(), cap_v, 0, d_tri.data_ptr(), cap_t, 0,
+                          d_seam.data_ptr(), cap_s, 0, C.cast(results, C.POINTER(lvn.ChunkResult)))
+        for _ in range(warmup):
+            assert mg.generate_chunks_raw(descs, n, bo) == 0
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            assert mg.generate_chunks_raw(descs, n, bo) == 0
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return sum(ts) / len(ts)
+
+    with ClockSampler(local) as clocks:
+        ms_plain = timed(args.steps, args.warmup)
+        mg.set_surrogate(sur, args.gate)
+        ms_sur = timed(args.steps, args.warmup)
+    use = mg.surrogate_chunks(n)
+    Vs, Ts, Ss, ress = mg.generate_chunks(chunks)
+    hd = []
+    for c in np.flatnonzero(use):
+        rp, rs = resp[c], ress[c]
+        voxel = 4.0 * chunks[c][1] / 256  # world units per voxel of this chunk
+        h = hausdorff_voxels(Vp[rp[0]:rp[0] + rp[1], :3], Vs[rs[0]:rs[0] + rs[1], :3], voxel)
+        if h is not None:
+            hd.append(h)
+    # density error of the surrogate against the plain FP32 density on fresh samples
+    pts = sur.sample(1 << 16, seed=99, fetch=True)
+    err = np.abs(sur.eval(pts) - pts[:, 3])
+    line = {
+        "metric": "64^3 chunks meshed/sec on 1 GB300, plain vs learned density", "impl": "lvn-surrogate",
+        "value": round(n / (ms_sur / 1e3), 2), "plain": round(n / (ms_plain / 1e3), 2), "unit": "chunks/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_sur, 3),
+        "plain_ms_per_step": round(ms_plain, 3), "higher_is_better": True, "dtype": "bf16/f32",
+        "data": "synthetic", "clocks": clocks.summary(),
+        "config": {"workload": f"clipmap-{n}chunks-lod0-4 with the 2D fBm density", "train_samples": 1 << 24,
+                   "train_steps": args.train_steps, "batch": 65536, "lr": 1e-3, "gate": args.gate,
+                   "domain": [lo, hi]},
+        "surrogate": {"chunks_on_surrogate": int(use.sum()), "fallback_rate": round(1 - use.sum() / n, 4),
+                      "train_s": round(t_train, 2), "sample_s": round(t_sample, 2),
+                      "train_tflops": round(train_flop / t_train / 1e12, 2),
+                      "loss_first": float(losses[0]) if len(losses) else None,
+                      "loss_last100": float(np.mean(losses[-100:])) if len(losses) else None,
+                      "density_abs_err_mean": float(err.mean()), "density_abs_err_p99": float(np.quantile(err, 0.99)),
+                      "hausdorff_voxels_mean": round(float(np.mean(hd)), 4) if hd else None,
+                      "hausdorff_voxels_max": round(float(np.max(hd)), 4) if hd else None,
+                      "chunks_within_0.05_mean_0.5_max": int(sum(h <= 0.5 for h in hd))},
+    }
+    print(json.dumps(line), flush=True)
+    mg.close()
+    sur.close()
 
 
 if __name__ == "__main__":
@@ -443,5 +637,7 @@ if __name__ == "__main__":
     WORKLOAD = a.workload
     if a.impl == "reference":
         run_reference(a)
+    elif a.surrogate:
+        run_surrogate(a)
     else:
         run_lvn(a)

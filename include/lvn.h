@@ -208,6 +208,26 @@ int         lvn_meshgen_stage_times(lvn_meshgen* ctx, float* ms, int32_t* launch
 const char* lvn_meshgen_stage_name(int32_t stage);
 int         lvn_meshgen_reset_stage_times(lvn_meshgen* ctx);
 
+/* new (not in the reference): bottom-up octree simplification of every mesh
+ * this context makes from now on.  Classic dual contouring collapse (Ju et al.
+ * 2002): an octree node replaces its subtree when all of its children did
+ * (leaves count, voxels on the chunk's faces never collapse, so seams are
+ * unchanged) and the QEF error of its summed crossings, solved with the
+ * reference's qef_solve (qef.cl:239-256), is at most `threshold` (voxel^2,
+ * the chunk's own voxel as unit).  The mesh is re-expressed over the collapsed
+ * nodes; lvn_chunk_result and the totals then describe the simplified mesh.
+ * threshold < 0 turns it off (the default). */
+int lvn_meshgen_set_simplify(lvn_meshgen* ctx, float threshold);
+
+/* new: launch-shape autotuner.  Runs the batch `chunks` (as
+ * lvn_meshgen_generate_chunks would, outputs discarded) with each stage's
+ * persistent grid at 2, 4, 8, 16 and 32 CTAs per SM, and keeps the fastest
+ * shape of every stage for later batches with the same density mode,
+ * crossing mode, simplification setting and power-of-two batch size.  The
+ * chosen CTAs per SM, indexed by stage (0 = built-in default), go to
+ * grid_per_sm[0 .. lvn_meshgen_stage_times' count) when it is not NULL. */
+int lvn_meshgen_autotune(lvn_meshgen* ctx, const lvn_chunk_desc* chunks, int32_t num_chunks, int32_t* grid_per_sm);
+
 /* new: intermediate buffers of chunk `chunk` of the last batch, for
  * stage-level parity checks (what = LVN_DEBUG_*).  Returns the element count,
  * or LVN_ERR_CAPACITY when cap_bytes is too small. */
@@ -221,6 +241,8 @@ int         lvn_meshgen_reset_stage_times(lvn_meshgen* ctx);
 #define LVN_DEBUG_NODE_TABLE   7  /* uint64[prime] node cuckoo table            */
 #define LVN_DEBUG_NODE_STASH   8  /* uint64[101]                                */
 #define LVN_DEBUG_PLAIN_EDGES  9  /* int32       number of plain (non-CSG) edges */
+#define LVN_DEBUG_SIMP_REPS   10  /* int32[V]   simplification: representative of each leaf,
+                                     first leaf below it | octree level << 20   */
 int64_t lvn_meshgen_debug_fetch(lvn_meshgen* ctx, int32_t what, int32_t chunk, void* host, int64_t cap_bytes);
 
 /* No counterpart in the reference.  Meshes one chunk exactly as
@@ -245,6 +267,55 @@ int64_t lvn_meshgen_debug_fetch(lvn_meshgen* ctx, int32_t what, int32_t chunk, v
 #define LVN_NOALLOC_MAX_CSG_OPS          64      /* stored operations per chunk  */
 int lvn_generate_chunk_mesh_noalloc(const int32_t min[3], int32_t size, int32_t voxels_per_chunk, lvn_mesh_out* out,
                                     void* cuda_stream);
+
+/* ---- learned density surrogate (new; not in the reference) ------------
+ * An MLP from a density-space position to the density: 16 frequencies per
+ * axis of sin / cos Fourier features over the domain (96 inputs), 4 hidden
+ * layers of 128 with SiLU, a linear output; 62,081 parameters.  BF16 weights
+ * and activations with FP32 accumulation on the tensor cores (tcgen05), FP32
+ * master weights and Adam (beta 0.9 / 0.999, eps 1e-8).  All functions return
+ * LVN_OK or a negative error code unless noted. */
+typedef struct lvn_surrogate lvn_surrogate;
+
+/* a surrogate over [domain_min, domain_max] (density units), weights drawn
+ * as PyTorch's Linear does from `seed`; NULL on failure */
+lvn_surrogate* lvn_surrogate_create(const float domain_min[3], const float domain_max[3], uint64_t seed);
+void    lvn_surrogate_destroy(lvn_surrogate* s);
+int32_t lvn_surrogate_num_params(void);
+/* parameters as one float array: W0[128][96] b0[128] W1[128][128] b1 W2 b2 W3 b3 w4[128] b4 */
+int     lvn_surrogate_set_params(lvn_surrogate* s, const float* params, int64_t n);
+int     lvn_surrogate_get_params(lvn_surrogate* s, float* params, int64_t capacity);
+/* generate the training pool: n samples (x, y, z, plain density) of the
+ * density set by lvn_set_density, 70% within 4 voxels of the heightfield
+ * surface and 30% uniform in the domain; copied to host_out when not NULL */
+int     lvn_surrogate_sample(lvn_surrogate* s, int64_t n, uint64_t seed, float* host_out);
+/* `steps` Adam steps on consecutive batches of the pool; losses[steps] (MSE
+ * of density / 8) when not NULL.  batch is a multiple of 128. */
+int     lvn_surrogate_train(lvn_surrogate* s, int32_t steps, int32_t batch, float lr, float* losses);
+/* one forward + backward on n host samples (x, y, z, target), n a multiple of
+ * 128: the gradient of the loss into grad[lvn_surrogate_num_params()] */
+int     lvn_surrogate_grad(lvn_surrogate* s, const float* samples, int32_t n, float* grad, float* loss);
+/* densities of n points (x, y, z, unused) in `memory` (LVN_MEMORY_HOST or
+ * LVN_MEMORY_DEVICE) */
+int     lvn_surrogate_eval(lvn_surrogate* s, const float* points, int64_t n, float* density, int32_t memory);
+/* densities of `count` lattices of dim^3 points in device memory: lattice l
+ * is lattices[4l .. 4l+3] = (x0, y0, z0, step), points x0 + step (i, j, k)
+ * with i fastest; density[l dim^3 + i + dim (j + dim k)] (device) */
+int     lvn_surrogate_eval_lattices(lvn_surrogate* s, const float* lattices, int32_t count, int32_t dim,
+                                    float* density);
+int     lvn_surrogate_domain(const lvn_surrogate* s, float domain_min[3], float domain_max[3]);
+void*   lvn_surrogate_get_stream(lvn_surrogate* s);
+
+/* Mesh with the surrogate: every fresh chunk of this context is probed at
+ * 8 x 8 x 8 of its field points; when the surrogate lies inside the domain
+ * for the whole chunk and within `gate` (density units) of the plain density
+ * at every probe, the chunk's field is the surrogate's (signs from its
+ * densities, crossings by linear interpolation, normals from central
+ * differences of its field), else the plain path (fallback).  NULL turns it
+ * off.  The surrogate must outlive its use by this context. */
+int lvn_meshgen_set_surrogate(lvn_meshgen* ctx, lvn_surrogate* s, float gate);
+/* chunks of the last batch that used the surrogate; use[c] = 1 / 0 when not NULL */
+int lvn_meshgen_surrogate_chunks(lvn_meshgen* ctx, int32_t* use, int32_t capacity);
 
 #ifdef __cplusplus
 }

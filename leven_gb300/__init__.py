@@ -25,7 +25,7 @@ LVN_MEMORY_DEVICE = 1
 LVN_DENSITY_REFERENCE, LVN_DENSITY_FBM2D, LVN_DENSITY_CAVES = 0, 1, 2
 LVN_OPT_CROSSING_MODE, LVN_OPT_CACHE, LVN_OPT_PROFILE, LVN_OPT_GRAPHS = 1, 2, 3, 4
 (DEBUG_MATERIALS, DEBUG_EDGE_KEYS, DEBUG_EDGE_INFO, DEBUG_NODE_CODES, DEBUG_NODE_INFO, DEBUG_EDGE_TABLE,
- DEBUG_EDGE_STASH, DEBUG_NODE_TABLE, DEBUG_NODE_STASH, DEBUG_PLAIN_EDGES) = range(10)
+ DEBUG_EDGE_STASH, DEBUG_NODE_TABLE, DEBUG_NODE_STASH, DEBUG_PLAIN_EDGES, DEBUG_SIMP_REPS) = range(11)
 
 
 class LvnError(RuntimeError):
@@ -77,8 +77,12 @@ EXPORTS = [
     "lvn_meshgen_voxels_per_chunk", "lvn_meshgen_apply_csg_operations", "lvn_meshgen_free_chunk_octree",
     "lvn_meshgen_is_chunk_empty", "lvn_meshgen_generate_chunk_mesh", "lvn_meshgen_generate_chunks",
     "lvn_meshgen_set_stream", "lvn_meshgen_get_stream", "lvn_meshgen_set_option", "lvn_meshgen_stage_times",
-    "lvn_meshgen_stage_name", "lvn_meshgen_reset_stage_times", "lvn_meshgen_debug_fetch",
-    "lvn_generate_chunk_mesh_noalloc",
+    "lvn_meshgen_stage_name", "lvn_meshgen_reset_stage_times", "lvn_meshgen_set_simplify",
+    "lvn_meshgen_autotune", "lvn_meshgen_debug_fetch", "lvn_generate_chunk_mesh_noalloc",
+    "lvn_surrogate_create", "lvn_surrogate_destroy", "lvn_surrogate_num_params", "lvn_surrogate_set_params",
+    "lvn_surrogate_get_params", "lvn_surrogate_sample", "lvn_surrogate_train", "lvn_surrogate_grad",
+    "lvn_surrogate_eval", "lvn_surrogate_eval_lattices", "lvn_surrogate_domain", "lvn_surrogate_get_stream",
+    "lvn_meshgen_set_surrogate", "lvn_meshgen_surrogate_chunks",
 ]
 
 _lib = None
@@ -118,6 +122,25 @@ def lib():
     L.lvn_meshgen_stage_name.argtypes = [C.c_int32]
     L.lvn_meshgen_stage_name.restype = C.c_char_p
     L.lvn_meshgen_reset_stage_times.argtypes = [C.c_void_p]
+    L.lvn_meshgen_set_simplify.argtypes = [C.c_void_p, C.c_float]
+    L.lvn_meshgen_autotune.argtypes = [C.c_void_p, C.POINTER(ChunkDesc), C.c_int32, i32p]
+    f32p = C.POINTER(C.c_float)
+    L.lvn_surrogate_create.argtypes = [C.c_float * 3, C.c_float * 3, C.c_uint64]
+    L.lvn_surrogate_create.restype = C.c_void_p
+    L.lvn_surrogate_destroy.argtypes = [C.c_void_p]
+    L.lvn_surrogate_destroy.restype = None
+    L.lvn_surrogate_set_params.argtypes = [C.c_void_p, f32p, C.c_int64]
+    L.lvn_surrogate_get_params.argtypes = [C.c_void_p, f32p, C.c_int64]
+    L.lvn_surrogate_sample.argtypes = [C.c_void_p, C.c_int64, C.c_uint64, C.c_void_p]
+    L.lvn_surrogate_train.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_float, C.c_void_p]
+    L.lvn_surrogate_grad.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, f32p]
+    L.lvn_surrogate_eval.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32]
+    L.lvn_surrogate_get_stream.argtypes = [C.c_void_p]
+    L.lvn_surrogate_eval_lattices.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]
+    L.lvn_surrogate_domain.argtypes = [C.c_void_p, C.c_float * 3, C.c_float * 3]
+    L.lvn_meshgen_set_surrogate.argtypes = [C.c_void_p, C.c_void_p, C.c_float]
+    L.lvn_meshgen_surrogate_chunks.argtypes = [C.c_void_p, i32p, C.c_int32]
+    L.lvn_surrogate_get_stream.restype = C.c_void_p
     L.lvn_meshgen_debug_fetch.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int64]
     L.lvn_meshgen_debug_fetch.restype = C.c_int64
     L.lvn_generate_chunk_mesh_noalloc.argtypes = [i32p, C.c_int32, C.c_int32, C.POINTER(MeshOut), C.c_void_p]
@@ -222,6 +245,36 @@ class MeshGen:
     def set_option(self, option, value):
         return _check(lib().lvn_meshgen_set_option(self._h, option, value), "lvn_meshgen_set_option")
 
+    def set_simplify(self, threshold):
+        """Bottom-up octree simplification with QEF-error bound `threshold`
+        (voxel^2); a negative threshold turns it off."""
+        return _check(lib().lvn_meshgen_set_simplify(self._h, threshold), "lvn_meshgen_set_simplify")
+
+    def autotune(self, chunks):
+        """Tune the persistent-grid shapes for batches like `chunks`; returns
+        {stage name: CTAs per SM} for the stages it chose."""
+        n = len(chunks)
+        descs = (ChunkDesc * max(1, n))()
+        for i, (mn, size) in enumerate(chunks):
+            descs[i] = ChunkDesc((C.c_int32 * 3)(*mn), size)
+        out = (C.c_int32 * 32)()
+        _check(lib().lvn_meshgen_autotune(self._h, descs, n, out), "lvn_meshgen_autotune")
+        names = self.stage_times()
+        return {name: out[i] for i, name in enumerate(names) if out[i] > 0}
+
+    def set_surrogate(self, surrogate, gate=0.5):
+        """Mesh fresh chunks with a learned surrogate where its probe gate
+        passes (None = plain only)."""
+        self._surrogate = surrogate  # kept alive while the context uses it
+        h = surrogate._h if surrogate is not None else None
+        return _check(lib().lvn_meshgen_set_surrogate(self._h, h, gate), "lvn_meshgen_set_surrogate")
+
+    def surrogate_chunks(self, n):
+        use = (C.c_int32 * max(1, n))()
+        k = lib().lvn_meshgen_surrogate_chunks(self._h, use, n)
+        _check(min(k, 0), "lvn_meshgen_surrogate_chunks")
+        return np.array(use[:n], np.int32)
+
     def stream(self):
         return lib().lvn_meshgen_get_stream(self._h)
 
@@ -302,3 +355,64 @@ class MeshGen:
 
     def reset_stage_times(self):
         return lib().lvn_meshgen_reset_stage_times(self._h)
+
+
+class Surrogate:
+    """Learned density surrogate (lvn_surrogate_*): Fourier features -> 4 x
+    [128, SiLU] -> 1, trained and evaluated with the library's tensor-core
+    kernels."""
+
+    def __init__(self, domain_min, domain_max, seed=1):
+        self._h = lib().lvn_surrogate_create((C.c_float * 3)(*domain_min), (C.c_float * 3)(*domain_max), seed)
+        if not self._h:
+            raise LvnError(LVN_ERR_INVALID, "lvn_surrogate_create")
+        self.domain_min, self.domain_max = tuple(domain_min), tuple(domain_max)
+
+    def close(self):
+        if self._h:
+            lib().lvn_surrogate_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    @staticmethod
+    def num_params():
+        return lib().lvn_surrogate_num_params()
+
+    def params(self):
+        out = np.zeros(self.num_params(), np.float32)
+        n = lib().lvn_surrogate_get_params(self._h, out.ctypes.data_as(C.POINTER(C.c_float)), out.size)
+        _check(min(n, 0), "lvn_surrogate_get_params")
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        _check(lib().lvn_surrogate_set_params(self._h, p.ctypes.data_as(C.POINTER(C.c_float)), p.size),
+               "lvn_surrogate_set_params")
+
+    def sample(self, n, seed=1, fetch=False):
+        out = np.zeros((n, 4), np.float32) if fetch else None
+        _check(lib().lvn_surrogate_sample(self._h, n, seed, out.ctypes.data if fetch else None), "lvn_surrogate_sample")
+        return out
+
+    def train(self, steps, batch=65536, lr=1e-3):
+        losses = np.zeros(max(steps, 1), np.float32)
+        _check(lib().lvn_surrogate_train(self._h, steps, batch, lr, losses.ctypes.data), "lvn_surrogate_train")
+        return losses[:steps]
+
+    def grad(self, samples):
+        samples = np.ascontiguousarray(samples, np.float32)
+        g = np.zeros(self.num_params(), np.float32)
+        loss = C.c_float()
+        _check(lib().lvn_surrogate_grad(self._h, samples.ctypes.data, samples.shape[0], g.ctypes.data, C.byref(loss)),
+               "lvn_surrogate_grad")
+        return g, loss.value
+
+    def eval(self, points):
+        pts = np.zeros((len(points), 4), np.float32)
+        pts[:, :3] = np.asarray(points, np.float32)[:, :3]
+        out = np.zeros(len(points), np.float32)
+        _check(lib().lvn_surrogate_eval(self._h, pts.ctypes.data, pts.shape[0], out.ctypes.data, LVN_MEMORY_HOST),
+               "lvn_surrogate_eval")
+        return out

@@ -292,12 +292,23 @@ struct lvn_meshgen {
     int crossing_mode = 0;
     bool cache = true;
     bool profile = false;
+    float simp_threshold = -1.f;  // bottom-up octree simplification; < 0 = off
+    lvn_surrogate* surrogate = nullptr;  // learned density for the chunks that pass its probe gate
+    float surrogate_gate = 0.5f;
+    std::vector<int32_t> last_suse;
 
     // pools
     DevBuf desc, cs, bs, brushes, mats, planes, edge_tiles, vox_tiles;
     DevBuf edge_keys, edge_chunk, edge_info, edge_work, node_codes, node_info, node_chunk;
     DevBuf edge_slots, node_slots, quad_scratch, node_tile_counts, chunk_tile_off;
     DevBuf vertices, triangles, seams;
+    // octree simplification
+    DevBuf leaf_vertices, leaf_qef, simp_grid, simp_nodes, simp_count, simp_rep, simp_entry, simp_newidx, simp_mask,
+        simp_tile_counts;
+    int64_t simp_vcap = 0, simp_grid_chunks = 0, simp_node_cap = 0, simp_tile_cap = 0;
+    // surrogate meshing
+    DevBuf probe_pts, probe_plain, probe_s, gate_ok, sslot, sdens, lattices;
+    HostBuf h_gate, h_sslot, h_lattices;
     HostBuf h_desc, h_brushes, h_cs, h_bs;
     int64_t ecap = 0, vcap = 0, eslot_cap = 0, nslot_cap = 0, ntile_cap = 0;
     int64_t vert_cap = 0, tri_cap = 0, seam_cap = 0;
@@ -318,6 +329,10 @@ struct lvn_meshgen {
     cudaStream_t side = nullptr;
     cudaEvent_t ev_leaf = nullptr, ev_side = nullptr;
 
+    // autotuned persistent-grid shapes (CTAs per SM per stage), keyed by
+    // density mode, crossing mode, simplification on/off and log2(batch size)
+    std::map<std::array<int, 4>, std::array<int, ST_COUNT>> tunes;
+
     // profiling
     cudaEvent_t ev[ST_COUNT + 1] = {};
     double stage_ms[ST_COUNT] = {};
@@ -332,6 +347,20 @@ namespace {
 struct Capacity {
     int64_t ecap, vcap;
 };
+
+// Entries of the simplification's level lists: level k holds at most one
+// entry per voxel and per level-k cell of each chunk.  `off` receives each
+// level's first entry.
+int64_t simp_node_capacity(int vpc, int n, int64_t vcap, int64_t* off) {
+    int64_t total = 0;
+    for (int k = 0; k < 8; k++) {
+        if (off) off[k] = total;
+        if (k == 0 || k > octree_depth(vpc)) continue;
+        const int64_t cells = (int64_t)n * (vpc >> k) * (vpc >> k) * (vpc >> k);
+        total += std::min(vcap, cells);
+    }
+    return total;
+}
 
 // Size every pool for `n` chunks with at least the given edge / node capacity.
 int ensure_pools(lvn_meshgen* m, int n, Capacity want) {
@@ -386,6 +415,31 @@ int ensure_pools(lvn_meshgen* m, int n, Capacity want) {
         m->ntile_cap = ntiles;
     }
     (void)C;
+    if (m->simp_threshold >= 0.f) {
+        if (m->vcap > m->simp_vcap) {
+            LVN_CK(m->leaf_vertices.ensure(sizeof(lvn_mesh_vertex) * m->vcap));
+            LVN_CK(m->leaf_qef.ensure(sizeof(SimpQef) * m->vcap));
+            LVN_CK(m->simp_rep.ensure(sizeof(int) * m->vcap));
+            LVN_CK(m->simp_entry.ensure(sizeof(int) * m->vcap));
+            LVN_CK(m->simp_newidx.ensure(sizeof(int) * m->vcap));
+            LVN_CK(m->simp_mask.ensure(m->vcap));
+            m->simp_vcap = m->vcap;
+        }
+        if (n > m->simp_grid_chunks) {
+            LVN_CK(m->simp_grid.ensure(sizeof(int) * (size_t)n * (size_t)simp_grid_cells(m->vpc)));
+            m->simp_grid_chunks = n;
+        }
+        const int64_t nodes = simp_node_capacity(m->vpc, n, m->vcap, nullptr);
+        if (nodes > m->simp_node_cap) {
+            LVN_CK(m->simp_nodes.ensure(sizeof(SimpNode) * nodes));
+            m->simp_node_cap = nodes;
+        }
+        LVN_CK(m->simp_count.ensure(sizeof(int) * 8));
+        if (m->ntile_cap > m->simp_tile_cap) {
+            LVN_CK(m->simp_tile_counts.ensure(sizeof(int2) * m->ntile_cap));
+            m->simp_tile_cap = m->ntile_cap;
+        }
+    }
     m->chunk_cap = std::max(m->chunk_cap, n);
     return LVN_OK;
 }
@@ -398,9 +452,18 @@ Capacity default_capacity(const lvn_meshgen* m, int n) {
                     (int64_t)n * (int64_t)std::min(C, 24 * 1024) + (int64_t)C};
 }
 
+std::array<int, 4> tune_key(const lvn_meshgen* m, int n) {
+    int bucket = 0;
+    while ((2 << bucket) <= n) bucket++;
+    return {g.density.mode, m->crossing_mode, m->simp_threshold >= 0.f ? 1 : 0, bucket};
+}
+
 BatchPtrs make_ptrs(lvn_meshgen* m, int n) {
     BatchPtrs b;
     std::memset(&b, 0, sizeof(b));
+    auto tuned = m->tunes.find(tune_key(m, n));
+    if (tuned != m->tunes.end())
+        for (int st = 0; st < ST_COUNT; st++) b.grid_per_sm[st] = tuned->second[st];
     b.n = n;
     b.vpc = m->vpc;
     b.crossing_mode = m->crossing_mode;
@@ -444,6 +507,21 @@ BatchPtrs make_ptrs(lvn_meshgen* m, int n) {
     b.triangle_cap = m->tri_cap;
     b.seams = m->seams.as<lvn_seam_node>();
     b.seam_cap = m->seam_cap;
+    if (m->simp_threshold >= 0.f) {
+        b.simp_on = 1;
+        b.simp_threshold = m->simp_threshold;
+        b.leaf_out = m->leaf_vertices.as<lvn_mesh_vertex>();
+        b.leaf_qef = m->leaf_qef.as<SimpQef>();
+        b.simp_grid = m->simp_grid.as<int>();
+        b.simp_nodes = m->simp_nodes.as<SimpNode>();
+        simp_node_capacity(m->vpc, n, m->vcap, b.simp_level_off);
+        b.simp_count = m->simp_count.as<int>();
+        b.simp_rep = m->simp_rep.as<int>();
+        b.simp_entry = m->simp_entry.as<int>();
+        b.simp_newidx = m->simp_newidx.as<int>();
+        b.simp_mask = m->simp_mask.as<uint8_t>();
+        b.simp_tile_counts = m->simp_tile_counts.as<int2>();
+    }
     return b;
 }
 
@@ -488,10 +566,11 @@ struct DirectOut {
     int64_t cap[3];
 };
 
-// ConstructOctreeFromField + GenerateMeshFromOctree + GatherSeamNodesFromOctree.
-// With `direct`, the vertices are exported on a side stream as soon as the
-// leaves are written, overlapping the mesh stages, and the triangles and
-// seams after the last stage.
+// ConstructOctreeFromField + GenerateMeshFromOctree + GatherSeamNodesFromOctree,
+// then the octree simplification when it is on.  With `direct`, the vertices
+// are exported on a side stream as soon as the leaves are written, overlapping
+// the mesh stages (after the simplification when it is on), and the triangles
+// and seams after the last stage.
 int enqueue_octree_stages(lvn_meshgen* m, const BatchPtrs& b, const DirectOut* direct = nullptr) {
     LVN_STAGE(ST_VOX_COUNT, launch_vox_count);
     LVN_STAGE(ST_VOX_PLAN, launch_vox_plan);
@@ -500,7 +579,7 @@ int enqueue_octree_stages(lvn_meshgen* m, const BatchPtrs& b, const DirectOut* d
     LVN_STAGE(ST_HASH_FILL, launch_hash_fill);
     LVN_STAGE(ST_EDGE_INSERT, launch_edge_insert);
     LVN_STAGE(ST_LEAF, launch_leaf);
-    if (direct) {
+    if (direct && !b.simp_on) {
         LVN_CK(cudaEventRecord(m->ev_leaf, m->stream));
         LVN_CK(cudaStreamWaitEvent(m->side, m->ev_leaf, 0));
         LVN_CK(launch_export(b, 0, direct->dst[0], direct->cap[0], m->side));
@@ -510,10 +589,12 @@ int enqueue_octree_stages(lvn_meshgen* m, const BatchPtrs& b, const DirectOut* d
     LVN_STAGE(ST_MESH_COUNT, launch_mesh_count);
     LVN_STAGE(ST_MESH_PLAN, launch_mesh_plan);
     LVN_STAGE(ST_MESH_SCATTER, launch_mesh_scatter);
+    if (b.simp_on) LVN_STAGE(ST_SIMPLIFY, launch_simplify);
     if (direct) {
+        if (b.simp_on) LVN_CK(launch_export(b, 0, direct->dst[0], direct->cap[0], m->stream));
         LVN_CK(launch_export(b, 1, direct->dst[1], direct->cap[1], m->stream));
         LVN_CK(launch_export(b, 2, direct->dst[2], direct->cap[2], m->stream));
-        LVN_CK(cudaStreamWaitEvent(m->stream, m->ev_side, 0));
+        if (!b.simp_on) LVN_CK(cudaStreamWaitEvent(m->stream, m->ev_side, 0));
     }
     return LVN_OK;
 }
@@ -636,6 +717,69 @@ bool redraw_failed(lvn_meshgen* m, std::vector<ChunkDesc>& descs) {
 
 constexpr int kMaxHashRetries = 16;
 
+// Learned-surrogate prologue of a fresh batch: probe every chunk, gate it,
+// and evaluate the surrogate on the field lattices of the chunks that passed.
+// Fills b's surrogate fields; the stages then read sdens for those chunks.
+int surrogate_prologue(lvn_meshgen* m, const std::vector<ChunkDesc>& descs, size_t n_brushes, BatchPtrs& b) {
+    const int n = (int)descs.size();
+    const int FD = m->vpc + 2;
+    const size_t F = (size_t)field_size(m->vpc);
+    LVN_CK(m->probe_pts.ensure(sizeof(float4) * kProbes * n));
+    LVN_CK(m->probe_plain.ensure(sizeof(float) * kProbes * n));
+    LVN_CK(m->probe_s.ensure(sizeof(float) * kProbes * n));
+    LVN_CK(m->gate_ok.ensure(sizeof(int) * n));
+    LVN_CK(m->sslot.ensure(sizeof(int) * n));
+    LVN_CK(m->h_gate.ensure(sizeof(int) * n));
+    LVN_CK(m->h_sslot.ensure(sizeof(int) * n));
+    b.s_on = 1;
+    b.probe_pts = m->probe_pts.as<float4>();
+    b.probe_plain = m->probe_plain.as<float>();
+    b.probe_s = m->probe_s.as<float>();
+    b.gate_ok = m->gate_ok.as<int>();
+    b.gate = m->surrogate_gate;
+    int rc = enqueue_inputs(m, n, n_brushes);
+    if (rc) return rc;
+    LVN_CK(launch_probe(b, m->stream));
+    LVN_CK(cudaStreamSynchronize(m->stream));
+    if ((rc = lvn_surrogate_eval(m->surrogate, m->probe_pts.as<float>(), (int64_t)kProbes * n, m->probe_s.as<float>(),
+                                 LVN_MEMORY_DEVICE)))
+        return rc;
+    LVN_CK(launch_gate(b, m->stream));
+    LVN_CK(cudaMemcpyAsync(m->h_gate.p, m->gate_ok.p, sizeof(int) * n, cudaMemcpyDeviceToHost, m->stream));
+    LVN_CK(cudaStreamSynchronize(m->stream));
+    float lo[3], hi[3];
+    if ((rc = lvn_surrogate_domain(m->surrogate, lo, hi))) return rc;
+    int32_t* slot = m->h_sslot.as<int32_t>();
+    std::vector<float> lat;
+    int k = 0;
+    for (int c = 0; c < n; c++) {
+        const ChunkDesc& d = descs[c];
+        bool inside = m->h_gate.as<int32_t>()[c] != 0;
+        for (int a = 0; a < 3 && inside; a++)
+            inside = (float)d.off[a] >= lo[a] && (float)(d.off[a] + d.scale * (FD - 1)) <= hi[a];
+        slot[c] = inside ? k++ : -1;
+        if (inside) lat.insert(lat.end(), {(float)d.off[0], (float)d.off[1], (float)d.off[2], (float)d.scale});
+    }
+    m->last_suse.assign(n, 0);
+    for (int c = 0; c < n; c++) m->last_suse[c] = slot[c] >= 0;
+    LVN_CK(cudaMemcpyAsync(m->sslot.p, slot, sizeof(int) * n, cudaMemcpyHostToDevice, m->stream));
+    b.sslot = m->sslot.as<int>();
+    if (k > 0) {
+        LVN_CK(m->sdens.ensure(sizeof(float) * F * k));
+        LVN_CK(m->lattices.ensure(sizeof(float) * lat.size()));
+        LVN_CK(m->h_lattices.ensure(sizeof(float) * lat.size()));
+        std::memcpy(m->h_lattices.p, lat.data(), sizeof(float) * lat.size());
+        LVN_CK(cudaMemcpyAsync(m->lattices.p, m->h_lattices.p, sizeof(float) * lat.size(), cudaMemcpyHostToDevice,
+                               m->stream));
+        LVN_CK(cudaStreamSynchronize(m->stream));
+        if ((rc = lvn_surrogate_eval_lattices(m->surrogate, m->lattices.as<float>(), k, FD, m->sdens.as<float>())))
+            return rc;
+        b.sdens = m->sdens.as<float>();
+    }
+    LVN_CK(cudaStreamSynchronize(m->stream));
+    return LVN_OK;
+}
+
 // Run fresh chunks end to end into the internal pools (or the caller's device
 // buffers when `dev_out` is given).  Grows the pools and reruns once when a
 // pool overflowed; retries the hash with new parameters when an insert failed.
@@ -659,6 +803,10 @@ int run_fresh_batch(lvn_meshgen* m, std::vector<ChunkDesc>& descs, const std::ve
             b.seams = dev_out->seams;
             b.seam_cap = dev_out->seam_capacity;
         }
+        if (m->surrogate) {
+            rc = surrogate_prologue(m, descs, brushes.size(), b);
+            if (rc) return rc;
+        }
         auto enqueue_all = [&]() -> int {
             int r = enqueue_inputs(m, n, brushes.size());
             if (!r) r = enqueue_field_stages(m, b, !brushes.empty());
@@ -666,7 +814,7 @@ int run_fresh_batch(lvn_meshgen* m, std::vector<ChunkDesc>& descs, const std::ve
             if (!r) r = enqueue_state_readback(m, n);
             return r;
         };
-        if (m->use_graphs && !m->profile) {
+        if (m->use_graphs && !m->profile && !m->surrogate) {
             // N3: the batch is one graph launch; re-captured only when a
             // buffer, a capacity or the shape of the batch changes
             std::vector<uintptr_t> key = {(uintptr_t)n, (uintptr_t)brushes.size(), (uintptr_t)m->crossing_mode,
@@ -682,7 +830,14 @@ int run_fresh_batch(lvn_meshgen* m, std::vector<ChunkDesc>& descs, const std::ve
                                           (uintptr_t)(direct ? direct->dst[1] : nullptr),
                                           (uintptr_t)(direct ? direct->dst[2] : nullptr),
                                           (uintptr_t)(direct ? direct->cap[0] : 0), (uintptr_t)(direct ? direct->cap[1] : 0),
-                                          (uintptr_t)(direct ? direct->cap[2] : 0), (uintptr_t)g.default_material};
+                                          (uintptr_t)(direct ? direct->cap[2] : 0), (uintptr_t)g.default_material,
+                                          (uintptr_t)b.simp_on, (uintptr_t)m->leaf_vertices.p, (uintptr_t)m->simp_nodes.p,
+                                          (uintptr_t)m->simp_grid.p, (uintptr_t)m->simp_rep.p,
+                                          (uintptr_t)m->simp_tile_counts.p};
+            uint32_t thr_bits;
+            std::memcpy(&thr_bits, &m->simp_threshold, 4);
+            key.push_back(thr_bits);
+            for (int st = 0; st < ST_COUNT; st++) key.push_back((uintptr_t)b.grid_per_sm[st]);
             const uint32_t* dk = reinterpret_cast<const uint32_t*>(&g.density);
             for (size_t i = 0; i < sizeof(g.density) / 4; i++) key.push_back(dk[i]);
             if (!m->graph_exec || key != m->graph_key) {
@@ -736,11 +891,19 @@ int run_fresh_batch(lvn_meshgen* m, std::vector<ChunkDesc>& descs, const std::ve
 
 void fill_results(lvn_meshgen* m, int n, lvn_chunk_result* r) {
     const ChunkState* cs = m->h_cs.as<ChunkState>();
+    const bool simp = m->simp_threshold >= 0.f;
     for (int c = 0; c < n; c++) {
-        r[c].vertex_offset = cs[c].node_off;
-        r[c].num_vertices = cs[c].quads > 0 ? cs[c].nodes : 0;
-        r[c].triangle_offset = 2 * cs[c].quad_off;
-        r[c].num_triangles = 2 * cs[c].quads;
+        if (simp) {
+            r[c].vertex_offset = cs[c].simp_vert_off;
+            r[c].num_vertices = cs[c].simp_tris > 0 ? cs[c].simp_verts : 0;
+            r[c].triangle_offset = cs[c].simp_tri_off;
+            r[c].num_triangles = cs[c].simp_tris;
+        } else {
+            r[c].vertex_offset = cs[c].node_off;
+            r[c].num_vertices = cs[c].quads > 0 ? cs[c].nodes : 0;
+            r[c].triangle_offset = 2 * cs[c].quad_off;
+            r[c].num_triangles = 2 * cs[c].quads;
+        }
         r[c].seam_offset = cs[c].seam_off;
         r[c].num_seams = cs[c].seams;
         r[c].num_edges = cs[c].num_edges;
@@ -980,15 +1143,19 @@ int export_chunk(lvn_meshgen* m, const OctreeEntry& o, lvn_mesh_out* out) {
 // Pull chunk 0's mesh out of the pools into host vectors.
 int pull_chunk(lvn_meshgen* m, OctreeEntry& o) {
     const ChunkState& cs = m->last_cs[0];
-    o.num_vertices = cs.quads > 0 ? cs.nodes : 0;
+    const bool simp = m->simp_threshold >= 0.f;
+    const int ntri = simp ? cs.simp_tris : 2 * cs.quads;
+    o.num_vertices = ntri > 0 ? (simp ? cs.simp_verts : cs.nodes) : 0;
     o.vertices.resize(o.num_vertices);
-    o.triangles.resize(2 * (size_t)cs.quads);
+    o.triangles.resize((size_t)ntri);
     o.seams.resize(cs.seams);
     if (o.num_vertices)
-        LVN_CK(cudaMemcpyAsync(o.vertices.data(), m->vertices.as<lvn_mesh_vertex>() + cs.node_off,
+        LVN_CK(cudaMemcpyAsync(o.vertices.data(),
+                               m->vertices.as<lvn_mesh_vertex>() + (simp ? cs.simp_vert_off : cs.node_off),
                                sizeof(lvn_mesh_vertex) * o.num_vertices, cudaMemcpyDeviceToHost, m->stream));
-    if (cs.quads)
-        LVN_CK(cudaMemcpyAsync(o.triangles.data(), m->triangles.as<lvn_mesh_triangle>() + 2 * (size_t)cs.quad_off,
+    if (ntri)
+        LVN_CK(cudaMemcpyAsync(o.triangles.data(),
+                               m->triangles.as<lvn_mesh_triangle>() + (simp ? (size_t)cs.simp_tri_off : 2 * (size_t)cs.quad_off),
                                sizeof(lvn_mesh_triangle) * o.triangles.size(), cudaMemcpyDeviceToHost, m->stream));
     if (cs.seams)
         LVN_CK(cudaMemcpyAsync(o.seams.data(), m->seams.as<lvn_seam_node>() + cs.seam_off,
@@ -1102,12 +1269,17 @@ void lvn_meshgen_destroy(lvn_meshgen* m) {
                       &m->edge_tiles, &m->vox_tiles,  &m->edge_keys,  &m->edge_chunk,   &m->edge_info, &m->edge_work,
                       &m->node_codes, &m->node_info,  &m->node_chunk, &m->edge_slots,   &m->node_slots,
                       &m->quad_scratch, &m->node_tile_counts, &m->chunk_tile_off, &m->vertices, &m->triangles,
-                      &m->seams};
+                      &m->seams, &m->leaf_vertices, &m->leaf_qef, &m->simp_grid, &m->simp_nodes, &m->simp_count,
+                      &m->simp_rep, &m->simp_entry, &m->simp_newidx, &m->simp_mask, &m->simp_tile_counts,
+                      &m->probe_pts, &m->probe_plain, &m->probe_s, &m->gate_ok, &m->sslot, &m->sdens, &m->lattices};
     for (DevBuf* b : bufs) b->release();
     m->h_desc.release();
     m->h_brushes.release();
     m->h_cs.release();
     m->h_bs.release();
+    m->h_gate.release();
+    m->h_sslot.release();
+    m->h_lattices.release();
     for (auto& kv : m->fields) {
         kv.second.mats.release();
         kv.second.planes.release();
@@ -1162,6 +1334,86 @@ int lvn_meshgen_stage_times(lvn_meshgen* m, float* ms, int32_t* launches, int32_
 
 const char* lvn_meshgen_stage_name(int32_t s) { return stage_name(s); }
 
+// N3 autotuner: times the batch's persistent-grid stages at 2..32 CTAs per SM
+// and keeps each stage's fastest shape for batches of this kind.
+int lvn_meshgen_autotune(lvn_meshgen* m, const lvn_chunk_desc* chunks, int32_t n, int32_t* grid_per_sm) {
+    if (!g.initialised) return LVN_ERR_NOT_INITIALISED;
+    if (!m || n <= 0 || !chunks || n > 65535) return LVN_ERR_INVALID;
+    std::vector<ChunkDesc> descs;
+    std::vector<Brush> brushes;
+    int rc = build_descs(m, chunks, n, descs, brushes, true);
+    if (rc) return rc;
+    const auto key = tune_key(m, n);
+    const bool profile = m->profile;
+    double saved_ms[ST_COUNT];
+    int saved_launches[ST_COUNT];
+    std::memcpy(saved_ms, m->stage_ms, sizeof(saved_ms));
+    std::memcpy(saved_launches, m->stage_launches, sizeof(saved_launches));
+    m->profile = true;
+    static const int kCandidates[] = {2, 4, 8, 16, 32};
+    std::array<double, ST_COUNT> best_ms;
+    std::array<int, ST_COUNT> best{};
+    best_ms.fill(1e30);
+    for (int cand : kCandidates) {
+        std::array<int, ST_COUNT> shape{};
+        for (int st = 0; st < ST_COUNT; st++) shape[st] = stage_has_persistent_grid(st) ? cand : 0;
+        m->tunes[key] = shape;
+        std::array<double, ST_COUNT> ms;
+        ms.fill(1e30);
+        for (int rep = 0; rep < 3 && rc == LVN_OK; rep++) {  // the first run also sizes the pools
+            for (int st = 0; st < ST_COUNT; st++) m->stage_ms[st] = 0.0, m->stage_launches[st] = 0;
+            rc = run_fresh_batch(m, descs, brushes, nullptr);
+            for (int st = 0; st < ST_COUNT; st++)
+                if (m->stage_launches[st]) ms[st] = std::min(ms[st], m->stage_ms[st]);
+        }
+        if (rc) break;
+        for (int st = 0; st < ST_COUNT; st++)
+            if (stage_has_persistent_grid(st) && ms[st] < best_ms[st]) {
+                best_ms[st] = ms[st];
+                best[st] = cand;
+            }
+    }
+    m->profile = profile;
+    std::memcpy(m->stage_ms, saved_ms, sizeof(saved_ms));
+    std::memcpy(m->stage_launches, saved_launches, sizeof(saved_launches));
+    if (rc) {
+        m->tunes.erase(key);
+        return rc;
+    }
+    m->tunes[key] = best;
+    if (grid_per_sm)
+        for (int st = 0; st < ST_COUNT; st++) grid_per_sm[st] = best[st];
+    return LVN_OK;
+}
+
+int lvn_meshgen_set_surrogate(lvn_meshgen* m, lvn_surrogate* s, float gate) {
+    if (!m || !(gate >= 0.f)) return LVN_ERR_INVALID;
+    LVN_CK(cudaStreamSynchronize(m->stream));
+    m->surrogate = s;
+    m->surrogate_gate = gate;
+    m->octrees.clear();
+    m->fields.clear();
+    return LVN_OK;
+}
+
+int lvn_meshgen_surrogate_chunks(lvn_meshgen* m, int32_t* use, int32_t capacity) {
+    if (!m) return LVN_ERR_INVALID;
+    int count = 0;
+    for (size_t c = 0; c < m->last_suse.size(); c++) {
+        if (use && (int32_t)c < capacity) use[c] = m->last_suse[c];
+        count += m->last_suse[c];
+    }
+    return count;
+}
+
+int lvn_meshgen_set_simplify(lvn_meshgen* m, float threshold) {
+    if (!m || threshold != threshold) return LVN_ERR_INVALID;
+    LVN_CK(cudaStreamSynchronize(m->stream));
+    m->simp_threshold = threshold < 0.f ? -1.f : threshold;
+    m->octrees.clear();  // cached meshes were made with the previous setting
+    return LVN_OK;
+}
+
 int lvn_meshgen_reset_stage_times(lvn_meshgen* m) {
     if (!m) return LVN_ERR_INVALID;
     for (int i = 0; i < ST_COUNT; i++) {
@@ -1193,8 +1445,9 @@ int lvn_meshgen_generate_chunks(lvn_meshgen* m, const lvn_chunk_desc* chunks, in
     }
     rc = run_fresh_batch(m, descs, brushes, dev ? out : nullptr, use_direct ? &direct : nullptr);
     const BatchState& bs = *m->h_bs.as<BatchState>();
-    out->total_vertices = bs.total_nodes;
-    out->total_triangles = 2 * (int64_t)bs.total_quads;
+    const bool simp = m->simp_threshold >= 0.f;
+    out->total_vertices = simp ? bs.total_simp_verts : bs.total_nodes;
+    out->total_triangles = simp ? bs.total_simp_tris : 2 * (int64_t)bs.total_quads;
     out->total_seams = bs.total_seams;
     if (rc) return rc;
     if (out->chunks) fill_results(m, n, out->chunks);
@@ -1339,6 +1592,10 @@ int64_t lvn_meshgen_debug_fetch(lvn_meshgen* m, int32_t what, int32_t chunk, voi
             src = m->node_slots.as<unsigned long long>() + cs.node_table_off + cs.node_prime;
             count = cs.node_prime ? CUCKOO_STASH_SIZE : 0; elem = 8; break;
         case LVN_DEBUG_PLAIN_EDGES: return cs.plain_edges;
+        case LVN_DEBUG_SIMP_REPS:
+            if (m->simp_threshold < 0.f) return LVN_ERR_INVALID;
+            src = m->simp_rep.as<int>() + cs.node_off;
+            count = cs.nodes; elem = 4; break;
         default: return LVN_ERR_INVALID;
     }
     if (count * elem > cap) return LVN_ERR_CAPACITY;

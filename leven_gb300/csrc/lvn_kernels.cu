@@ -355,6 +355,100 @@ __device__ __forceinline__ void qef_solve(const Qef& q, float& ox, float& oy, fl
     oz = z + mz;
 }
 
+
+// ---------------------------------------------------------------------------
+// Octree simplification QEFs (not in the reference): a node's QEF in its own
+// frame (origin at its min corner, unit = one voxel) with btb, so that the
+// classic QEF value E(x) = x.ATA x - 2 x.ATb + btb is well conditioned.
+// Children are summed in child order after moving them by d = child origin -
+// node origin: ATb += ATA d, btb += 2 d.ATb + d.ATA d, mass point += w d.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void simp_zero(SimpQef& q) {
+#pragma unroll
+    for (int i = 0; i < 6; i++) q.ata[i] = 0.f;
+    q.btb = q.w = q.pad[0] = q.pad[1] = q.pad[2] = 0.f;
+#pragma unroll
+    for (int i = 0; i < 3; i++) q.atb[i] = q.mp[i] = q.ns[i] = 0.f;
+}
+
+// qef_add_point (qef.cl:170-191) plus btb, count and normal sum
+__device__ __forceinline__ void simp_add_point(SimpQef& q, float px, float py, float pz, float nx, float ny, float nz) {
+    q.ata[0] += nx * nx;
+    q.ata[1] += nx * ny;
+    q.ata[2] += nx * nz;
+    q.ata[3] += ny * ny;
+    q.ata[4] += ny * nz;
+    q.ata[5] += nz * nz;
+    const float bb = dot3(px, py, pz, nx, ny, nz);
+    q.atb[0] += nx * bb;
+    q.atb[1] += ny * bb;
+    q.atb[2] += nz * bb;
+    q.btb = fmaf(bb, bb, q.btb);
+    q.mp[0] += px;
+    q.mp[1] += py;
+    q.mp[2] += pz;
+    q.w += 1.f;
+    q.ns[0] += nx;
+    q.ns[1] += ny;
+    q.ns[2] += nz;
+}
+
+__device__ __forceinline__ void simp_merge(SimpQef& q, const SimpQef& c, float dx, float dy, float dz) {
+    const float* A = c.ata;
+    const float adx = dot3(A[0], A[1], A[2], dx, dy, dz);
+    const float ady = dot3(A[1], A[3], A[4], dx, dy, dz);
+    const float adz = dot3(A[2], A[4], A[5], dx, dy, dz);
+#pragma unroll
+    for (int i = 0; i < 6; i++) q.ata[i] += A[i];
+    q.atb[0] += c.atb[0] + adx;
+    q.atb[1] += c.atb[1] + ady;
+    q.atb[2] += c.atb[2] + adz;
+    q.btb += c.btb + fmaf(2.f, dot3(dx, dy, dz, c.atb[0], c.atb[1], c.atb[2]), dot3(dx, dy, dz, adx, ady, adz));
+    q.mp[0] += fmaf(c.w, dx, c.mp[0]);
+    q.mp[1] += fmaf(c.w, dy, c.mp[1]);
+    q.mp[2] += fmaf(c.w, dz, c.mp[2]);
+    q.w += c.w;
+    q.ns[0] += c.ns[0];
+    q.ns[1] += c.ns[1];
+    q.ns[2] += c.ns[2];
+}
+
+__device__ __forceinline__ float simp_error(const SimpQef& q, float x, float y, float z) {
+    const float* A = q.ata;
+    const float ax = dot3(A[0], A[1], A[2], x, y, z);
+    const float ay = dot3(A[1], A[3], A[4], x, y, z);
+    const float az = dot3(A[2], A[4], A[5], x, y, z);
+    return fmaf(-2.f, dot3(x, y, z, q.atb[0], q.atb[1], q.atb[2]), dot3(x, y, z, ax, ay, az)) + q.btb;
+}
+
+// qef_solve on the node's QEF (its mass point is the running sum, which
+// qef_solve divides by the count); a solution outside the node's cube of side
+// s falls back to the mass point.  Returns the QEF value at the position.
+__device__ __forceinline__ float simp_solve(const SimpQef& q, float s, float& ox, float& oy, float& oz) {
+    Qef r;
+#pragma unroll
+    for (int i = 0; i < 6; i++) r.ata[i] = q.ata[i];
+    r.atb[0] = q.atb[0];
+    r.atb[1] = q.atb[1];
+    r.atb[2] = q.atb[2];
+    r.mp[0] = q.mp[0];
+    r.mp[1] = q.mp[1];
+    r.mp[2] = q.mp[2];
+    r.mp[3] = q.w;
+    float x, y, z;
+    qef_solve(r, x, y, z);
+    if (!(x >= 0.f && x <= s && y >= 0.f && y <= s && z >= 0.f && z <= s)) {
+        x = q.mp[0] / q.w;
+        y = q.mp[1] / q.w;
+        z = q.mp[2] / q.w;
+    }
+    ox = x;
+    oy = y;
+    oz = z;
+    return simp_error(q, x, y, z);
+}
+
 // ---------------------------------------------------------------------------
 // stage 0: reset per-chunk state
 // ---------------------------------------------------------------------------
@@ -437,6 +531,7 @@ __global__ void __launch_bounds__(96) k_field(BatchPtrs b) {
     if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
     __syncthreads();
     const int c = blockIdx.y, z = blockIdx.x;
+    if (b.s_on && b.sslot[c] >= 0) return;  // the surrogate's field (k_field_sdens)
     const int x = threadIdx.x;
     const bool valid = x < G::FD;
     // descriptor fields in registers: the byte stores below may alias them
@@ -452,44 +547,27 @@ __global__ void __launch_bounds__(96) k_field(BatchPtrs b) {
     uint8_t* mats = b.mats + (size_t)c * G::F + x + G::FD * G::FD * z;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     uint32_t pw = 0;  // lane l keeps the ballot of row (y & ~31) + l
-    if (MODE != LVN_DENSITY_CAVES) {
-        // y - amp * h rounds monotonically in y, so the column is solid below
-        // the first y whose density is >= 0 and air from there up
-        int ycross = 0;
-        if (valid && dm != MATERIAL_AIR) {
-            int lo = 0, hi = G::FD;  // first y in [lo, hi) with density >= 0, hi if none
-            while (lo < hi) {
-                const int mid = (lo + hi) >> 1;
-                if (dens_h<MODE>(nz, dp, h, wx, (float)(mid * scale + oy), wz) < 0.f) lo = mid + 1;
-                else hi = mid;
-            }
-            ycross = lo;
+    static_assert(MODE != LVN_DENSITY_CAVES, "a density with a 3D term uses k_field_caves");
+    // y - amp * h rounds monotonically in y, so the column is solid below
+    // the first y whose density is >= 0 and air from there up
+    int ycross = 0;
+    if (valid && dm != MATERIAL_AIR) {
+        int lo = 0, hi = G::FD;  // first y in [lo, hi) with density >= 0, hi if none
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (dens_h<MODE>(nz, dp, h, wx, (float)(mid * scale + oy), wz) < 0.f) lo = mid + 1;
+            else hi = mid;
         }
-        for (int y = 0; y < G::FD; y++) {
-            const bool solid = y < ycross;
-            if (valid && write_mats) mats[G::FD * y] = (uint8_t)(solid ? dm : MATERIAL_AIR);
-            const unsigned sb = __ballot_sync(FULL, solid);
-            pw = (y & 31) == lane ? sb : pw;
-            if ((y & 31) == 31 || y == G::FD - 1) {
-                const int yy = (y & ~31) + lane;
-                if (yy <= y) words[warp][yy] = pw;
-            }
-        }
-    } else {
-        for (int y = 0; y < G::FD; y++) {
-            bool solid = false;
-            if (valid) {
-                const float dv = dens_h<MODE>(nz, dp, h, wx, (float)(y * scale + oy), wz);
-                const int m = dv < 0.f ? dm : MATERIAL_AIR;
-                if (write_mats) mats[G::FD * y] = (uint8_t)m;
-                solid = m != MATERIAL_AIR;
-            }
-            const unsigned sb = __ballot_sync(FULL, solid);
-            pw = (y & 31) == lane ? sb : pw;
-            if ((y & 31) == 31 || y == G::FD - 1) {
-                const int yy = (y & ~31) + lane;
-                if (yy <= y) words[warp][yy] = pw;
-            }
+        ycross = lo;
+    }
+    for (int y = 0; y < G::FD; y++) {
+        const bool solid = y < ycross;
+        if (valid && write_mats) mats[G::FD * y] = (uint8_t)(solid ? dm : MATERIAL_AIR);
+        const unsigned sb = __ballot_sync(FULL, solid);
+        pw = (y & 31) == lane ? sb : pw;
+        if ((y & 31) == 31 || y == G::FD - 1) {
+            const int yy = (y & ~31) + lane;
+            if (yy <= y) words[warp][yy] = pw;
         }
     }
     __syncthreads();
@@ -511,6 +589,117 @@ __global__ void __launch_bounds__(96) k_field(BatchPtrs b) {
 // apply_csg_operation.cl:179-241) inside the chunk's operation bounding box;
 // rows there get their final-air and changed bits rewritten.
 // ---------------------------------------------------------------------------
+
+// Field of a density with a 3D term (the cave fBm): every point is evaluated.
+// One CTA per z slice; the slice's 66 column heights are computed once into
+// shared memory, then the 66 x 66 points are spread over all lanes (97% of
+// lanes busy, against 69% for one thread per column) and their solid bits
+// are gathered into the row words with shared-memory atomics.
+template <int VPC>
+__global__ void __launch_bounds__(128) k_field_caves(BatchPtrs b) {
+    using G = Geo<VPC>;
+    __shared__ float sg[64];
+    __shared__ float hs[G::FD];
+    __shared__ uint32_t words[3][G::FD];
+    if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
+    for (int i = threadIdx.x; i < 3 * G::FD; i += blockDim.x) (&words[0][0])[i] = 0u;
+    const int c = blockIdx.y, z = blockIdx.x;
+    if (b.s_on && b.sslot[c] >= 0) return;  // the surrogate's field (k_field_sdens)
+    const int scale = b.desc[c].scale;
+    const int ox = b.desc[c].off[0], oy = b.desc[c].off[1], oz = b.desc[c].off[2];
+    const DensityParams& dp = b.density;
+    const float wz = (float)(z * scale + oz);
+    __syncthreads();
+    const Noise nz{b.perm, b.perm_k4, sg};
+    const int tx = (int)threadIdx.x;  // signed: chunk offsets may be negative
+    if (tx < G::FD) hs[tx] = height_m<LVN_DENSITY_CAVES>(nz, dp, (float)(tx * scale + ox), wz);
+    __syncthreads();
+    const int dm = b.default_material;
+    const bool write_mats = b.need_mats != 0;
+    uint8_t* mats = b.mats + (size_t)c * G::F + G::FD * G::FD * z;
+    for (int i = threadIdx.x; i < G::FD * G::FD; i += blockDim.x) {
+        const int y = i / G::FD, x = i - G::FD * y;
+        const float dv = dens_h<LVN_DENSITY_CAVES>(nz, dp, hs[x], (float)(x * scale + ox), (float)(y * scale + oy), wz);
+        const int m = dv < 0.f ? dm : MATERIAL_AIR;
+        if (write_mats) mats[i] = (uint8_t)m;
+        if (m != MATERIAL_AIR) atomicOr(&words[x >> 5][y], 1u << (x & 31));
+    }
+    __syncthreads();
+    const uint4 V = low_bits(G::FD);
+    uint4* P = plane_ptr<VPC>(b, c, 0) + G::FD * z;
+    uint4* A = plane_ptr<VPC>(b, c, 1) + G::FD * z;
+    uint4* X = plane_ptr<VPC>(b, c, 2) + G::FD * z;
+    for (int y = threadIdx.x; y < G::FD; y += blockDim.x) {
+        const uint4 p = make_uint4(words[0][y], words[1][y], words[2][y], 0u);
+        P[y] = p;
+        A[y] = and4(not4(p), V);
+        X[y] = make_uint4(0u, 0u, 0u, 0u);
+    }
+}
+
+// Field of a chunk that takes the learned surrogate's densities (density
+// < 0 is solid, as DensityFunc's sign is read by GenerateDefaultField).
+template <int VPC>
+__global__ void __launch_bounds__(128) k_field_sdens(BatchPtrs b) {
+    using G = Geo<VPC>;
+    __shared__ uint32_t words[3][G::FD];
+    const int c = blockIdx.y, z = blockIdx.x;
+    const int slot = b.sslot[c];
+    if (slot < 0) return;
+    for (int i = threadIdx.x; i < 3 * G::FD; i += blockDim.x) (&words[0][0])[i] = 0u;
+    __syncthreads();
+    const float* dens = b.sdens + (size_t)slot * G::F + (size_t)G::FD * G::FD * z;
+    const int dm = b.default_material;
+    const bool write_mats = b.need_mats != 0;
+    uint8_t* mats = b.mats + (size_t)c * G::F + G::FD * G::FD * z;
+    for (int i = threadIdx.x; i < G::FD * G::FD; i += blockDim.x) {
+        const int y = i / G::FD, x = i - G::FD * y;
+        const int m = dens[i] < 0.f ? dm : MATERIAL_AIR;
+        if (write_mats) mats[i] = (uint8_t)m;
+        if (m != MATERIAL_AIR) atomicOr(&words[x >> 5][y], 1u << (x & 31));
+    }
+    __syncthreads();
+    const uint4 V = low_bits(G::FD);
+    uint4* P = plane_ptr<VPC>(b, c, 0) + G::FD * z;
+    uint4* A = plane_ptr<VPC>(b, c, 1) + G::FD * z;
+    uint4* X = plane_ptr<VPC>(b, c, 2) + G::FD * z;
+    for (int y = threadIdx.x; y < G::FD; y += blockDim.x) {
+        const uint4 p = make_uint4(words[0][y], words[1][y], words[2][y], 0u);
+        P[y] = p;
+        A[y] = and4(not4(p), V);
+        X[y] = make_uint4(0u, 0u, 0u, 0u);
+    }
+}
+
+// 8 x 8 x 8 probes per chunk at field points (FD - 1) * (2i + 1) / 16, with
+// the plain density there
+template <int VPC>
+__global__ void __launch_bounds__(kProbes) k_probe(BatchPtrs b) {
+    using G = Geo<VPC>;
+    __shared__ float sg[64];
+    if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
+    __syncthreads();
+    const int c = blockIdx.x, p = threadIdx.x;
+    const ChunkDesc& d = b.desc[c];
+    const int ix = (G::FD - 1) * (2 * (p & 7) + 1) / 16, iy = (G::FD - 1) * (2 * ((p >> 3) & 7) + 1) / 16,
+              iz = (G::FD - 1) * (2 * (p >> 6) + 1) / 16;
+    const float wx = (float)(d.off[0] + d.scale * ix), wy = (float)(d.off[1] + d.scale * iy),
+                wz = (float)(d.off[2] + d.scale * iz);
+    const Noise nz{b.perm, b.perm_k4, sg};
+    b.probe_pts[(size_t)c * kProbes + p] = make_float4(wx, wy, wz, 0.f);
+    b.probe_plain[(size_t)c * kProbes + p] = nz.density(b.density, wx, wy, wz);
+}
+
+__global__ void __launch_bounds__(kProbes) k_gate(BatchPtrs b) {
+    __shared__ int bad;
+    const int c = blockIdx.x, p = threadIdx.x;
+    if (p == 0) bad = 0;
+    __syncthreads();
+    const size_t i = (size_t)c * kProbes + p;
+    if (!(fabsf(b.probe_s[i] - b.probe_plain[i]) <= b.gate)) bad = 1;
+    __syncthreads();
+    if (p == 0) b.gate_ok[c] = bad ? 0 : 1;
+}
 
 template <int VPC>
 __global__ void __launch_bounds__(96) k_csg(BatchPtrs b) {
@@ -957,6 +1146,43 @@ __device__ __forceinline__ float4 hermite_brush(const BatchPtrs& b, const ChunkD
     return make_float4(nx, ny, nzv, t);
 }
 
+// Hermite data of an edge of a surrogate chunk: crossing by linear
+// interpolation of the end points' densities, normal from central
+// differences of the density field (one-sided at the field's faces)
+// interpolated to the crossing.
+template <int VPC>
+__device__ __forceinline__ float4 hermite_sdens(const BatchPtrs& b, int slot, int key) {
+    using G = Geo<VPC>;
+    const int axis = key & 3;
+    const int hidx = key >> 2;
+    const int lx = hidx & G::MASK, ly = (hidx >> G::SHIFT) & G::MASK, lz = (hidx >> (2 * G::SHIFT)) & G::MASK;
+    const float* D = b.sdens + (size_t)slot * G::F;
+    auto at = [&](int x, int y, int z) {
+        x = min(max(x, 0), G::FD - 1);
+        y = min(max(y, 0), G::FD - 1);
+        z = min(max(z, 0), G::FD - 1);
+        return D[x + G::FD * (y + G::FD * z)];
+    };
+    const int ox = axis == 0, oy = axis == 1, oz = axis == 2;
+    const float d0 = at(lx, ly, lz), d1 = at(lx + ox, ly + oy, lz + oz);
+    const float den = d0 - d1;
+    float t = den != 0.f ? d0 / den : 0.5f;
+    t = fminf(fmaxf(t, 0.f), 1.f);
+    float g[2][3];
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+        const int x = lx + e * ox, y = ly + e * oy, z = lz + e * oz;
+        g[e][0] = at(x + 1, y, z) - at(x - 1, y, z);
+        g[e][1] = at(x, y + 1, z) - at(x, y - 1, z);
+        g[e][2] = at(x, y, z + 1) - at(x, y, z - 1);
+    }
+    float nx = fmaf(g[1][0] - g[0][0], t, g[0][0]);
+    float ny = fmaf(g[1][1] - g[0][1], t, g[0][1]);
+    float nzv = fmaf(g[1][2] - g[0][2], t, g[0][2]);
+    normalize3(nx, ny, nzv);
+    return make_float4(nx, ny, nzv, t);
+}
+
 template <int VPC, int MODE>
 __global__ void __launch_bounds__(kThreads) k_hermite(BatchPtrs b) {
     __shared__ float sg[64];
@@ -973,7 +1199,10 @@ __global__ void __launch_bounds__(kThreads) k_hermite(BatchPtrs b) {
         const int c = b.edge_chunk[i];
         const ChunkDesc& d = b.desc[c];
         const int key = b.edge_keys[i];
-        b.edge_info[i] = w >= nplain ? hermite_brush<VPC>(b, d, key) : hermite_density<VPC, MODE>(b, nz, d, key);
+        const int slot = b.s_on ? b.sslot[c] : -1;
+        b.edge_info[i] = w >= nplain ? hermite_brush<VPC>(b, d, key)
+                         : slot >= 0 ? hermite_sdens<VPC>(b, slot, key)
+                                     : hermite_density<VPC, MODE>(b, nz, d, key);
     }
 }
 
@@ -1074,7 +1303,9 @@ __global__ void __launch_bounds__(1024) k_vox_plan(BatchPtrs b) {
         b.bs->total_nodes = (int)total;
         b.bs->total_node_slots = slots;
         int ovf = 0;
-        if (total > b.vcap || total > b.vertex_cap) ovf |= OVF_NODES;
+        // with simplification the leaves go to leaf_out (vcap); the caller's
+        // vertex array is checked against the simplified count
+        if (total > b.vcap || (!b.simp_on && total > b.vertex_cap)) ovf |= OVF_NODES;
         if (slots > b.node_slot_cap) ovf |= OVF_NODE_SLOTS;
         if (tiles > b.node_tile_cap) ovf |= OVF_NODES;
         b.bs->overflow |= ovf;
@@ -1239,6 +1470,9 @@ __global__ void __launch_bounds__(kThreads) k_leaf(BatchPtrs b) {
         q.atb[0] = q.atb[1] = q.atb[2] = 0.f;
         q.mp[0] = q.mp[1] = q.mp[2] = q.mp[3] = 0.f;
         float sx = 0.f, sy = 0.f, sz = 0.f, sw = 0.f;
+        const bool simp = b.simp_on != 0;
+        SimpQef sq;
+        if (simp) simp_zero(sq);
         for (int e = 0; e < 12; e++) {
             if (!((edge_list >> e) & 1)) continue;
             const int e0 = edge_c0(e), e1 = edge_c1(e);
@@ -1274,7 +1508,11 @@ __global__ void __launch_bounds__(kThreads) k_leaf(BatchPtrs b) {
             sy += ny;
             sz += nzv;
             sw += 1.f;
+            if (simp)  // the same crossing in the voxel's own frame
+                simp_add_point(sq, fmaf((float)(o1x - o0x), ed.w, (float)o0x), fmaf((float)(o1y - o0y), ed.w, (float)o0y),
+                               fmaf((float)(o1z - o0z), ed.w, (float)o0z), nx, ny, nzv);
         }
+        if (simp) b.leaf_qef[i] = sq;
         // qef_create_from_points divides the mass point by its count (qef.cl:302)
         const float mw = q.mp[3];
         q.mp[0] = q.mp[0] / mw;
@@ -1296,7 +1534,7 @@ __global__ void __launch_bounds__(kThreads) k_leaf(BatchPtrs b) {
         vtx.colour[1] = d.colour[1];
         vtx.colour[2] = d.colour[2];
         vtx.colour[3] = (float)((ni & 0xffff) >> 8);
-        float4* dst = reinterpret_cast<float4*>(b.vertices + i);
+        float4* dst = reinterpret_cast<float4*>((simp ? b.leaf_out : b.vertices) + i);
         dst[0] = make_float4(vtx.position[0], vtx.position[1], vtx.position[2], vtx.position[3]);
         dst[1] = make_float4(vtx.normal[0], vtx.normal[1], vtx.normal[2], vtx.normal[3]);
         dst[2] = make_float4(vtx.colour[0], vtx.colour[1], vtx.colour[2], vtx.colour[3]);
@@ -1408,7 +1646,7 @@ __global__ void __launch_bounds__(1024) k_mesh_plan(BatchPtrs b) {
         b.bs->total_quads = (int)tq;
         b.bs->total_seams = (int)ts;
         int ovf = 0;
-        if (2 * tq > b.triangle_cap) ovf |= OVF_QUADS;
+        if (!b.simp_on && 2 * tq > b.triangle_cap) ovf |= OVF_QUADS;  // simplified triangles are checked later
         if (ts > b.seam_cap) ovf |= OVF_SEAMS;
         b.bs->overflow |= ovf;
     }
@@ -1449,7 +1687,7 @@ __global__ void __launch_bounds__(kNodeTile) k_mesh_scatter(BatchPtrs b) {
             int qp = st.quad_off + toff.x + (ex & 0xffff);
 #pragma unroll
             for (int a = 0; a < 3; a++) {
-                if (!(q[a].w & 1)) continue;
+                if (!(q[a].w & 1) || b.simp_on) continue;
                 const int idx[4] = {local, q[a].x, q[a].y, q[a].z};
                 const int* w = (q[a].w & 2) ? w1 : w0;
                 lvn_mesh_triangle* tri = b.triangles + 2 * (size_t)qp;
@@ -1463,12 +1701,347 @@ __global__ void __launch_bounds__(kNodeTile) k_mesh_scatter(BatchPtrs b) {
             }
             if (seam) {
                 const int sp = st.seam_off + toff.y + (ex >> 16);
-                const float4* v = reinterpret_cast<const float4*>(b.vertices + i);
+                const float4* v = reinterpret_cast<const float4*>((b.simp_on ? b.leaf_out : b.vertices) + i);
                 int4* dst = reinterpret_cast<int4*>(b.seams + sp);
                 dst[0] = make_int4(pos[0], pos[1], pos[2], b.node_info[i] & 0xffff);
                 const float4 p = v[0], nrm = v[1];
                 reinterpret_cast<float4*>(dst)[1] = p;
                 reinterpret_cast<float4*>(dst)[2] = nrm;
+            }
+        }
+    }
+}
+
+
+// ---------------------------------------------------------------------------
+// Bottom-up octree simplification (not in the reference): classic dual
+// contouring collapse (Ju et al. 2002) of each chunk's leaf octree, level by
+// level.  A node at level k (2^k voxels) has one entry, created by the first
+// of its children to claim its cell in the chunk's level-k grid; it collapses
+// when every child that exists collapsed (leaves count, seam voxels do not),
+// and its QEF error is at most the threshold.  The mesh keeps GenerateMesh's
+// quads (octree.cl:385-442) remapped to each leaf's highest collapsed ancestor
+// (its representative): a quad survives on the first sign change along the
+// minimal edge (the edge of the smallest of its four representatives) when
+// that edge's end points differ in sign, and triangles with a repeated vertex
+// are dropped.  Vertices are the representatives, ordered by their first leaf.
+// ---------------------------------------------------------------------------
+
+template <int VPC>
+__device__ __forceinline__ int simp_grid_off(int k) {  // cells before level k's grid in a chunk
+    int s = 0;
+    for (int j = 1; j < k; j++) s += (VPC >> j) * (VPC >> j) * (VPC >> j);
+    return s;
+}
+
+template <int VPC>
+__device__ __forceinline__ int* simp_cell(const BatchPtrs& b, int c, int k, int x, int y, int z) {
+    const int n = VPC >> k;
+    return b.simp_grid + (size_t)c * simp_grid_off<VPC>(Geo<VPC>::DEPTH + 1) + simp_grid_off<VPC>(k) + x +
+           n * (y + n * z);
+}
+
+// create the level-k entry of cell (x, y, z) of chunk c if it has none
+template <int VPC>
+__device__ __forceinline__ void simp_claim(const BatchPtrs& b, int c, int k, int x, int y, int z) {
+    int* cell = simp_cell<VPC>(b, c, k, x, y, z);
+    if (atomicCAS(cell, -1, -2) != -1) return;
+    const int e = atomicAdd(b.simp_count + k, 1);
+    SimpNode& n = b.simp_nodes[b.simp_level_off[k] + e];
+    n.chunk = c;
+    n.pos = x | (y << 8) | (z << 16);
+    n.collapsed = 0;
+    n.anchor = 0;
+    atomicExch(cell, e);
+}
+
+template <int VPC>
+__global__ void __launch_bounds__(kThreads) k_simp_seed(BatchPtrs b) {
+    if (b.bs->overflow) return;
+    const int total = b.bs->total_nodes;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        int x, y, z;
+        position_for_code<VPC>(b.node_codes[i], x, y, z);
+        simp_claim<VPC>(b, b.node_chunk[i], 1, x >> 1, y >> 1, z >> 1);
+    }
+}
+
+template <int VPC>
+__global__ void __launch_bounds__(kThreads) k_simp_level(BatchPtrs b, int k) {
+    if (b.bs->overflow) return;
+    const int count = b.simp_count[k];
+    SimpNode* nodes = b.simp_nodes + b.simp_level_off[k];
+    const SimpNode* below = b.simp_nodes + b.simp_level_off[k > 1 ? k - 1 : 1];
+    const int h = 1 << (k - 1);
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x) {
+        SimpNode& nd = nodes[e];
+        const int c = nd.chunk;
+        const int px = nd.pos & 255, py = (nd.pos >> 8) & 255, pz = nd.pos >> 16;
+        const ChunkState& st = b.cs[c];
+        HashView hv;
+        if (k == 1) {
+            hv.prime = st.node_prime;
+            hv.magic = st.node_magic;
+            hv.table = b.node_slots + st.node_table_off;
+            hv.stash = hv.table + hv.prime;
+            hv.stash_used = st.node_stash_used;
+#pragma unroll
+            for (int j = 0; j < 10; j++) hv.p[j] = b.desc[c].node_params[j];
+        }
+        bool blocked = false;
+        SimpQef q;
+        simp_zero(q);
+        int mats[8];
+        int anchor = 0x7fffffff;
+        for (int i = 0; i < 8; i++) {
+            const int ox = (i >> 2) & 1, oy = (i >> 1) & 1, oz = i & 1;  // CHILD_MIN_OFFSETS
+            const int cx = 2 * px + ox, cy = 2 * py + oy, cz = 2 * pz + oz;
+            mats[i] = MATERIAL_NONE;
+            if (blocked) continue;
+            if (k == 1) {
+                const uint32_t local = hv.find(code_for_position<VPC>(cx, cy, cz));
+                if (local == ~0u) continue;
+                if (cx == 0 || cx == VPC - 1 || cy == 0 || cy == VPC - 1 || cz == 0 || cz == VPC - 1) {
+                    blocked = true;  // seam voxels stay leaves
+                    continue;
+                }
+                const int vi = st.node_off + (int)local;
+                simp_merge(q, b.leaf_qef[vi], (float)(ox * h), (float)(oy * h), (float)(oz * h));
+                mats[i] = (b.node_info[vi] >> 8) & 0xff;
+                anchor = min(anchor, (int)local);
+            } else {
+                const int ce = *simp_cell<VPC>(b, c, k - 1, cx, cy, cz);
+                if (ce < 0) continue;
+                const SimpNode& ch = below[ce];
+                if (!ch.collapsed) {
+                    blocked = true;
+                    continue;
+                }
+                simp_merge(q, ch.q, (float)(ox * h), (float)(oy * h), (float)(oz * h));
+                mats[i] = ch.material;
+                anchor = min(anchor, ch.anchor);
+            }
+        }
+        int collapsed = 0;
+        if (!blocked) {
+            float x, y, z;
+            const float err = simp_solve(q, (float)(2 * h), x, y, z);
+            if (err <= b.simp_threshold) {
+                collapsed = 1;
+                const ChunkDesc& d = b.desc[c];
+                const float fs = (float)d.scale;
+                nd.wpos[0] = fmaf(fs * ((float)(px << k) + x), (float)LEAF_SIZE_SCALE, (float)d.min[0]);
+                nd.wpos[1] = fmaf(fs * ((float)(py << k) + y), (float)LEAF_SIZE_SCALE, (float)d.min[1]);
+                nd.wpos[2] = fmaf(fs * ((float)(pz << k) + z), (float)LEAF_SIZE_SCALE, (float)d.min[2]);
+                nd.material = dominant_material(mats);
+                nd.anchor = anchor;
+                nd.q = q;
+            }
+        }
+        nd.collapsed = collapsed;
+        if (k < Geo<VPC>::DEPTH) simp_claim<VPC>(b, c, k + 1, px >> 1, py >> 1, pz >> 1);
+    }
+}
+
+// each leaf's representative; anchors counted per node tile
+template <int VPC>
+__global__ void __launch_bounds__(kNodeTile) k_simp_map(BatchPtrs b) {
+    __shared__ int sm[kNodeTile / 32 + 1];
+    if (b.bs->overflow) return;
+    const int ntiles = b.chunk_tile_off[b.n];
+    for (int vt = blockIdx.x; vt < ntiles; vt += gridDim.x) {
+        const int c = chunk_of_tile(b.chunk_tile_off, b.n, vt);
+        const ChunkState& st = b.cs[c];
+        const int local = (vt - b.chunk_tile_off[c]) * kNodeTile + threadIdx.x;
+        int is_anchor = 0;
+        if (local < st.nodes) {
+            const int i = st.node_off + local;
+            int x, y, z;
+            position_for_code<VPC>(b.node_codes[i], x, y, z);
+            int level = 0, anchor = local, entry = -1;
+            for (int k = 1; k <= Geo<VPC>::DEPTH; k++) {
+                const int e = *simp_cell<VPC>(b, c, k, x >> k, y >> k, z >> k);
+                if (e < 0) break;
+                const int64_t ge = b.simp_level_off[k] + e;
+                const SimpNode& nd = b.simp_nodes[ge];
+                if (!nd.collapsed) break;
+                level = k;
+                anchor = nd.anchor;
+                entry = (int)ge;
+            }
+            b.simp_rep[i] = anchor | (level << 20);
+            b.simp_entry[i] = entry;
+            is_anchor = anchor == local ? 1 : 0;
+        }
+        const int total = block_sum<kNodeTile>(is_anchor, sm);
+        if (threadIdx.x == 0) b.simp_tile_counts[vt].x = total;
+    }
+}
+
+// the triangles each leaf quad keeps
+template <int VPC>
+__global__ void __launch_bounds__(kNodeTile) k_simp_tcount(BatchPtrs b) {
+    using G = Geo<VPC>;
+    __shared__ int sm[kNodeTile / 32 + 1];
+    if (b.bs->overflow) return;
+    const int w0[6] = {0, 1, 3, 0, 3, 2};
+    const int w1[6] = {0, 3, 1, 0, 2, 3};
+    const int ntiles = b.chunk_tile_off[b.n];
+    for (int vt = blockIdx.x; vt < ntiles; vt += gridDim.x) {
+        const int c = chunk_of_tile(b.chunk_tile_off, b.n, vt);
+        const ChunkState& st = b.cs[c];
+        const int local = (vt - b.chunk_tile_off[c]) * kNodeTile + threadIdx.x;
+        int tris = 0;
+        if (local < st.nodes) {
+            const int i = st.node_off + local;
+            int pos[3];
+            position_for_code<VPC>(b.node_codes[i], pos[0], pos[1], pos[2]);
+            const uint4* A = plane_ptr<VPC>(b, c, 1);
+            const int rep0 = b.simp_rep[i];
+            int mask = 0;
+            for (int a = 0; a < 3; a++) {
+                const int4 q = b.quad_scratch[3 * (size_t)i + a];
+                if (!(q.w & 1)) continue;
+                const int r[4] = {rep0, b.simp_rep[st.node_off + q.x], b.simp_rep[st.node_off + q.y],
+                                  b.simp_rep[st.node_off + q.z]};
+                const int minlev = min(min(r[0] >> 20, r[1] >> 20), min(r[2] >> 20, r[3] >> 20));
+                if (minlev > 0) {
+                    // the minimal edge along axis a through the quad edge's other coordinates
+                    const int len = 1 << minlev;
+                    int p0[3] = {pos[0], pos[1], pos[2]};
+                    p0[(a + 1) % 3] += 1;
+                    p0[(a + 2) % 3] += 1;
+                    const int s0 = pos[a] & ~(len - 1);
+                    auto solid = [&](int t) {
+                        int qq[3] = {p0[0], p0[1], p0[2]};
+                        qq[a] = t;
+                        return !bit4(A[qq[1] + G::FD * qq[2]], qq[0]);
+                    };
+                    const bool first = solid(s0);
+                    bool keep = first != solid(s0 + len);
+                    for (int t = s0 + 1; keep && t <= pos[a]; t++) keep = solid(t) == first;
+                    if (!keep) continue;
+                }
+                const int* w = (q.w & 2) ? w1 : w0;
+#pragma unroll
+                for (int t = 0; t < 2; t++) {
+                    const int a0 = r[w[3 * t]] & 0xfffff, a1 = r[w[3 * t + 1]] & 0xfffff, a2 = r[w[3 * t + 2]] & 0xfffff;
+                    if (a0 == a1 || a1 == a2 || a0 == a2) continue;
+                    mask |= 1 << (2 * a + t);
+                    tris++;
+                }
+            }
+            b.simp_mask[i] = (uint8_t)mask;
+        }
+        const int total = block_sum<kNodeTile>(tris, sm);
+        if (threadIdx.x == 0) b.simp_tile_counts[vt].y = total;
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_simp_plan(BatchPtrs b) {
+    __shared__ int sm[1024 / 32 + 1];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (b.bs->overflow) return;
+    for (int c = warp; c < b.n; c += 32) {
+        const int t0 = b.chunk_tile_off[c], nt = b.chunk_tile_off[c + 1] - t0;
+        int2* t = b.simp_tile_counts + t0;
+        int cv = 0, ct = 0;
+        for (int base = 0; base < nt; base += 32) {
+            const int i = base + lane;
+            const int2 v = i < nt ? t[i] : make_int2(0, 0);
+            const int iv = warp_inclusive(v.x), it = warp_inclusive(v.y);
+            if (i < nt) t[i] = make_int2(cv + iv - v.x, ct + it - v.y);
+            cv += __shfl_sync(FULL, iv, 31);
+            ct += __shfl_sync(FULL, it, 31);
+        }
+        if (lane == 0) {
+            b.cs[c].simp_verts = cv;
+            b.cs[c].simp_tris = ct;
+        }
+    }
+    __syncthreads();
+    const long long tv = cta_scan(
+        b.n, [&](int c) { return b.cs[c].simp_verts; }, [&](int c, long long ex) { b.cs[c].simp_vert_off = (int)ex; },
+        nullptr, sm);
+    const long long tt = cta_scan(
+        b.n, [&](int c) { return b.cs[c].simp_tris; }, [&](int c, long long ex) { b.cs[c].simp_tri_off = (int)ex; },
+        nullptr, sm);
+    if (threadIdx.x == 0) {
+        b.bs->total_simp_verts = (int)tv;
+        b.bs->total_simp_tris = (int)tt;
+        int ovf = 0;
+        if (tt > b.triangle_cap) ovf |= OVF_QUADS;
+        if (tv > b.vertex_cap) ovf |= OVF_NODES;
+        b.bs->overflow |= ovf;
+    }
+}
+
+// vertices of the representatives, at their anchors' ranks
+template <int VPC>
+__global__ void __launch_bounds__(kNodeTile) k_simp_vscatter(BatchPtrs b) {
+    __shared__ int sm[kNodeTile / 32 + 1];
+    if (b.bs->overflow) return;
+    const int ntiles = b.chunk_tile_off[b.n];
+    for (int vt = blockIdx.x; vt < ntiles; vt += gridDim.x) {
+        const int c = chunk_of_tile(b.chunk_tile_off, b.n, vt);
+        const ChunkState& st = b.cs[c];
+        const int local = (vt - b.chunk_tile_off[c]) * kNodeTile + threadIdx.x;
+        const int i = st.node_off + local;
+        const bool anchor = local < st.nodes && (b.simp_rep[i] & 0xfffff) == local;
+        int total;
+        const int ex = block_exclusive<kNodeTile>(anchor ? 1 : 0, total, sm);
+        if (anchor) {
+            const int ni = b.simp_tile_counts[vt].x + ex;
+            b.simp_newidx[i] = ni;
+            float4* dst = reinterpret_cast<float4*>(b.vertices + st.simp_vert_off + ni);
+            const int entry = b.simp_entry[i];
+            if (entry < 0) {
+                const float4* src = reinterpret_cast<const float4*>(b.leaf_out + i);
+                dst[0] = src[0];
+                dst[1] = src[1];
+                dst[2] = src[2];
+            } else {
+                const SimpNode& nd = b.simp_nodes[entry];
+                const ChunkDesc& d = b.desc[c];
+                dst[0] = make_float4(nd.wpos[0], nd.wpos[1], nd.wpos[2], 1.f);
+                dst[1] = make_float4(nd.q.ns[0] / nd.q.w, nd.q.ns[1] / nd.q.w, nd.q.ns[2] / nd.q.w, 0.f);
+                dst[2] = make_float4(d.colour[0], d.colour[1], d.colour[2], (float)nd.material);
+            }
+        }
+    }
+}
+
+template <int VPC>
+__global__ void __launch_bounds__(kNodeTile) k_simp_tscatter(BatchPtrs b) {
+    __shared__ int sm[kNodeTile / 32 + 1];
+    if (b.bs->overflow) return;
+    const int w0[6] = {0, 1, 3, 0, 3, 2};
+    const int w1[6] = {0, 3, 1, 0, 2, 3};
+    const int ntiles = b.chunk_tile_off[b.n];
+    for (int vt = blockIdx.x; vt < ntiles; vt += gridDim.x) {
+        const int c = chunk_of_tile(b.chunk_tile_off, b.n, vt);
+        const ChunkState& st = b.cs[c];
+        const int local = (vt - b.chunk_tile_off[c]) * kNodeTile + threadIdx.x;
+        const int i = st.node_off + local;
+        const int mask = local < st.nodes ? b.simp_mask[i] : 0;
+        int total;
+        const int ex = block_exclusive<kNodeTile>(__popc(mask), total, sm);
+        if (mask) {
+            int tp = st.simp_tri_off + b.simp_tile_counts[vt].y + ex;
+            const int rep0 = b.simp_rep[i];
+            for (int a = 0; a < 3; a++) {
+                if (!((mask >> (2 * a)) & 3)) continue;
+                const int4 q = b.quad_scratch[3 * (size_t)i + a];
+                const int r[4] = {rep0, b.simp_rep[st.node_off + q.x], b.simp_rep[st.node_off + q.y],
+                                  b.simp_rep[st.node_off + q.z]};
+                const int* w = (q.w & 2) ? w1 : w0;
+                for (int t = 0; t < 2; t++) {
+                    if (!((mask >> (2 * a + t)) & 1)) continue;
+                    lvn_mesh_triangle* tri = b.triangles + tp++;
+#pragma unroll
+                    for (int j = 0; j < 3; j++)
+                        tri->indices[j] = b.simp_newidx[st.node_off + (r[w[3 * t + j]] & 0xfffff)];
+                }
             }
         }
     }
@@ -1488,8 +2061,15 @@ __global__ void __launch_bounds__(256) k_export(BatchPtrs b, int which, void* ds
     if (bs.overflow) return;
     const void* src;
     int64_t count, elem;
-    if (which == 0) { src = b.vertices; count = bs.total_nodes; elem = sizeof(lvn_mesh_vertex); }
-    else if (which == 1) { src = b.triangles; count = 2 * (int64_t)bs.total_quads; elem = sizeof(lvn_mesh_triangle); }
+    if (which == 0) {
+        src = b.vertices;
+        count = b.simp_on ? bs.total_simp_verts : bs.total_nodes;
+        elem = sizeof(lvn_mesh_vertex);
+    } else if (which == 1) {
+        src = b.triangles;
+        count = b.simp_on ? bs.total_simp_tris : 2 * (int64_t)bs.total_quads;
+        elem = sizeof(lvn_mesh_triangle);
+    }
     else { src = b.seams; count = bs.total_seams; elem = sizeof(lvn_seam_node); }
     if (count > capacity) {
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&b.bs->status, 1 << which);
@@ -1522,7 +2102,7 @@ const char* stage_name(int s) {
     static const char* names[ST_COUNT] = {"field",      "csg",        "edge_count", "edge_plan",   "edge_scatter",
                                           "hermite",    "vox_count",  "vox_plan",   "vox_scatter", "primes", "hash_fill",
                                           "edge_insert", "leaf",      "node_insert", "mesh_count", "mesh_plan",
-                                          "mesh_scatter"};
+                                          "mesh_scatter", "simplify"};
     return s >= 0 && s < ST_COUNT ? names[s] : "?";
 }
 
@@ -1535,7 +2115,10 @@ const char* stage_name(int s) {
         default: return cudaErrorInvalidValue;          \
     }
 
-static inline int persistent_grid(const BatchPtrs& b, int per_sm) { return b.num_sms * per_sm; }
+// persistent grid of stage `st`: the autotuner's CTAs per SM, else `per_sm`
+static inline int persistent_grid(const BatchPtrs& b, int st, int per_sm) {
+    return b.num_sms * (b.grid_per_sm[st] > 0 ? b.grid_per_sm[st] : per_sm);
+}
 
 cudaError_t launch_reset(const BatchPtrs& b, cudaStream_t s) {
     k_reset<<<(b.n + 255) / 256, 256, 0, s>>>(b);
@@ -1547,8 +2130,19 @@ cudaError_t launch_field(const BatchPtrs& b, cudaStream_t s) {
     switch (b.density.mode) {
         case LVN_DENSITY_REFERENCE: LVN_VPC_DISPATCH(b.vpc, (k_field<V, LVN_DENSITY_REFERENCE><<<grid, 96, 0, s>>>(b))); break;
         case LVN_DENSITY_FBM2D: LVN_VPC_DISPATCH(b.vpc, (k_field<V, LVN_DENSITY_FBM2D><<<grid, 96, 0, s>>>(b))); break;
-        default: LVN_VPC_DISPATCH(b.vpc, (k_field<V, LVN_DENSITY_CAVES><<<grid, 96, 0, s>>>(b))); break;
+        default: LVN_VPC_DISPATCH(b.vpc, (k_field_caves<V><<<grid, 128, 0, s>>>(b))); break;
     }
+    if (b.s_on) LVN_VPC_DISPATCH(b.vpc, (k_field_sdens<V><<<grid, 128, 0, s>>>(b)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_probe(const BatchPtrs& b, cudaStream_t s) {
+    LVN_VPC_DISPATCH(b.vpc, (k_probe<V><<<b.n, kProbes, 0, s>>>(b)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gate(const BatchPtrs& b, cudaStream_t s) {
+    k_gate<<<b.n, kProbes, 0, s>>>(b);
     return cudaGetLastError();
 }
 
@@ -1581,7 +2175,7 @@ cudaError_t launch_edge_scatter(const BatchPtrs& b, cudaStream_t s) {
 }
 
 cudaError_t launch_hermite(const BatchPtrs& b, cudaStream_t s) {
-    const int g = persistent_grid(b, 8);
+    const int g = persistent_grid(b, ST_HERMITE, 8);
     switch (b.density.mode) {
         case LVN_DENSITY_REFERENCE: LVN_VPC_DISPATCH(b.vpc, (k_hermite<V, LVN_DENSITY_REFERENCE><<<g, kThreads, 0, s>>>(b))); break;
         case LVN_DENSITY_FBM2D: LVN_VPC_DISPATCH(b.vpc, (k_hermite<V, LVN_DENSITY_FBM2D><<<g, kThreads, 0, s>>>(b))); break;
@@ -1613,27 +2207,42 @@ cudaError_t launch_primes(const BatchPtrs& b, cudaStream_t s) {
 }
 
 cudaError_t launch_hash_fill(const BatchPtrs& b, cudaStream_t s) {
-    k_hash_fill<<<persistent_grid(b, 4), 256, 0, s>>>(b);
+    k_hash_fill<<<persistent_grid(b, ST_HASH_FILL, 4), 256, 0, s>>>(b);
     return cudaGetLastError();
 }
 
 cudaError_t launch_edge_insert(const BatchPtrs& b, cudaStream_t s) {
-    k_edge_insert<<<persistent_grid(b, 8), kThreads, 0, s>>>(b);
+    k_edge_insert<<<persistent_grid(b, ST_EDGE_INSERT, 8), kThreads, 0, s>>>(b);
     return cudaGetLastError();
 }
 
 cudaError_t launch_leaf(const BatchPtrs& b, cudaStream_t s) {
-    LVN_VPC_DISPATCH(b.vpc, (k_leaf<V><<<persistent_grid(b, 8), kThreads, 0, s>>>(b)));
+    LVN_VPC_DISPATCH(b.vpc, (k_leaf<V><<<persistent_grid(b, ST_LEAF, 8), kThreads, 0, s>>>(b)));
     return cudaGetLastError();
 }
 
 cudaError_t launch_node_insert(const BatchPtrs& b, cudaStream_t s) {
-    k_node_insert<<<persistent_grid(b, 8), kThreads, 0, s>>>(b);
+    k_node_insert<<<persistent_grid(b, ST_NODE_INSERT, 8), kThreads, 0, s>>>(b);
     return cudaGetLastError();
 }
 
 cudaError_t launch_mesh_count(const BatchPtrs& b, cudaStream_t s) {
-    LVN_VPC_DISPATCH(b.vpc, (k_mesh_count<V><<<persistent_grid(b, 8), kNodeTile, 0, s>>>(b)));
+    LVN_VPC_DISPATCH(b.vpc, (k_mesh_count<V><<<persistent_grid(b, ST_MESH_COUNT, 8), kNodeTile, 0, s>>>(b)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_simplify(const BatchPtrs& b, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(b.simp_grid, 0xff, sizeof(int) * (size_t)b.n * (size_t)simp_grid_cells(b.vpc), s);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(b.simp_count, 0, sizeof(int) * 8, s)) != cudaSuccess) return e;
+    const int g = persistent_grid(b, ST_SIMPLIFY, 8);
+    LVN_VPC_DISPATCH(b.vpc, (k_simp_seed<V><<<g, kThreads, 0, s>>>(b)));
+    for (int k = 1; k <= octree_depth(b.vpc); k++) LVN_VPC_DISPATCH(b.vpc, (k_simp_level<V><<<g, kThreads, 0, s>>>(b, k)));
+    LVN_VPC_DISPATCH(b.vpc, (k_simp_map<V><<<g, kNodeTile, 0, s>>>(b)));
+    LVN_VPC_DISPATCH(b.vpc, (k_simp_tcount<V><<<g, kNodeTile, 0, s>>>(b)));
+    k_simp_plan<<<1, 1024, 0, s>>>(b);
+    LVN_VPC_DISPATCH(b.vpc, (k_simp_vscatter<V><<<g, kNodeTile, 0, s>>>(b)));
+    LVN_VPC_DISPATCH(b.vpc, (k_simp_tscatter<V><<<g, kNodeTile, 0, s>>>(b)));
     return cudaGetLastError();
 }
 
@@ -1643,12 +2252,12 @@ cudaError_t launch_mesh_plan(const BatchPtrs& b, cudaStream_t s) {
 }
 
 cudaError_t launch_export(const BatchPtrs& b, int which, void* dst, int64_t capacity, cudaStream_t s) {
-    k_export<<<persistent_grid(b, 4), 256, 0, s>>>(b, which, dst, capacity);
+    k_export<<<b.num_sms * 4, 256, 0, s>>>(b, which, dst, capacity);
     return cudaGetLastError();
 }
 
 cudaError_t launch_mesh_scatter(const BatchPtrs& b, cudaStream_t s) {
-    LVN_VPC_DISPATCH(b.vpc, (k_mesh_scatter<V><<<persistent_grid(b, 8), kNodeTile, 0, s>>>(b)));
+    LVN_VPC_DISPATCH(b.vpc, (k_mesh_scatter<V><<<persistent_grid(b, ST_MESH_SCATTER, 8), kNodeTile, 0, s>>>(b)));
     return cudaGetLastError();
 }
 

@@ -67,6 +67,37 @@ struct BatchPtrs {
     lvn_seam_node* seams;        // [seam_cap]
     int64_t seam_cap;
 
+    // bottom-up octree simplification (simp_on = 1): the leaves are written to
+    // leaf_out, the simplified mesh to vertices / triangles
+    int simp_on;
+    float simp_threshold;        // collapse when the QEF error (voxel^2) is at most this
+    lvn_mesh_vertex* leaf_out;   // [vcap]
+    SimpQef* leaf_qef;           // [vcap]
+    int* simp_grid;              // [n][simp_grid_cells(vpc)] node entry per level cell, -1 = none
+    SimpNode* simp_nodes;        // level k's entries start at simp_level_off[k]
+    int64_t simp_level_off[8];
+    int* simp_count;             // [8] entries per level
+    int* simp_rep;               // [vcap] representative: anchor | level << 20
+    int* simp_entry;             // [vcap] the representative's node (-1 = the leaf itself)
+    int* simp_newidx;            // [vcap] output vertex of an anchor leaf
+    uint8_t* simp_mask;          // [vcap] kept triangles, bit 2 * axis + t
+    int2* simp_tile_counts;      // [node tile cap] (vertices, triangles) per node tile, then offsets
+
+    // learned-surrogate meshing (s_on = 1): chunks with sslot[c] >= 0 take their
+    // field from sdens[sslot[c]][F] instead of the plain density
+    int s_on;
+    const float* sdens;
+    const int* sslot;            // [n]
+    float4* probe_pts;           // [n][512] probe positions
+    float* probe_plain;          // [n][512] plain density at the probes
+    const float* probe_s;        // [n][512] surrogate density at the probes
+    int* gate_ok;                // [n] 1 when every probe is within `gate`
+    float gate;
+
+    // launch shapes chosen by the autotuner: CTAs per SM of each stage's
+    // persistent grid (0 = the built-in default)
+    int grid_per_sm[24];
+
     // cached-field CSG: the field's current edge list (chunk 0 only)
     const int32_t* prev_keys;
     const float4* prev_info;
@@ -82,6 +113,13 @@ inline int field_size(int vpc) { return (vpc + 2) * (vpc + 2) * (vpc + 2); }
 inline int field_rows(int vpc) { return (vpc + 2) * (vpc + 2); }
 inline int edge_tiles_per_chunk(int vpc) { return (field_rows(vpc) + kRowTile - 1) / kRowTile; }
 inline int vox_tiles_per_chunk(int vpc) { return (vpc * vpc + kRowTile - 1) / kRowTile; }
+inline int octree_depth(int vpc) { return vpc == 8 ? 3 : vpc == 16 ? 4 : vpc == 32 ? 5 : 6; }
+// cells of the level grids 1..depth of one chunk: sum (vpc >> k)^3
+inline int64_t simp_grid_cells(int vpc) {
+    int64_t s = 0;
+    for (int k = 1; k <= octree_depth(vpc); k++) s += (int64_t)(vpc >> k) * (vpc >> k) * (vpc >> k);
+    return s;
+}
 
 // Stage identifiers for profiling (order of execution).
 enum Stage {
@@ -102,8 +140,15 @@ enum Stage {
     ST_MESH_COUNT,
     ST_MESH_PLAN,
     ST_MESH_SCATTER,
+    ST_SIMPLIFY,
     ST_COUNT
 };
+static_assert(ST_COUNT <= 24, "BatchPtrs::grid_per_sm holds one entry per stage");
+// the stages whose kernels run on a persistent grid, tunable by CTAs per SM
+inline bool stage_has_persistent_grid(int st) {
+    return st == ST_HERMITE || st == ST_HASH_FILL || st == ST_EDGE_INSERT || st == ST_LEAF || st == ST_NODE_INSERT ||
+           st == ST_MESH_COUNT || st == ST_MESH_SCATTER || st == ST_SIMPLIFY;
+}
 const char* stage_name(int s);
 
 // Launchers: each enqueues one kernel of the pipeline on `stream`.
@@ -126,6 +171,13 @@ cudaError_t launch_node_insert(const BatchPtrs& b, cudaStream_t stream);
 cudaError_t launch_mesh_count(const BatchPtrs& b, cudaStream_t stream);
 cudaError_t launch_mesh_plan(const BatchPtrs& b, cudaStream_t stream);
 cudaError_t launch_mesh_scatter(const BatchPtrs& b, cudaStream_t stream);
+// surrogate probes: 512 field points per chunk with their plain density, and
+// the gate that compares them with the surrogate's
+constexpr int kProbes = 512;
+cudaError_t launch_probe(const BatchPtrs& b, cudaStream_t stream);
+cudaError_t launch_gate(const BatchPtrs& b, cudaStream_t stream);
+// the whole simplification pass (level grids reset, levels, map, plan, scatter)
+cudaError_t launch_simplify(const BatchPtrs& b, cudaStream_t stream);
 // which: 0 vertices, 1 triangles, 2 seams; dst must be device-addressable
 cudaError_t launch_export(const BatchPtrs& b, int which, void* dst, int64_t capacity, cudaStream_t stream);
 

@@ -1,0 +1,850 @@
+// lvn_surrogate.cu -- learned density surrogate (not in the reference).
+//
+// A multilayer perceptron from a density-space position to the density:
+//   16 frequencies per axis, sin and cos (96 Fourier features)
+//   -> 4 x [Linear 128, SiLU] -> Linear 1
+// 62,081 parameters.  Weights and activations are BF16, every product is
+// accumulated in FP32, the master weights and Adam moments are FP32.
+//
+// Every matrix product (the four hidden layers forward, their input gradients
+// and their weight gradients) runs on the 5th-generation tensor cores: one
+// elected thread issues tcgen05.mma (kind::f16, BF16 in, FP32 accumulator in
+// tensor memory) on 128-row tiles staged in shared memory, the CTA waits on
+// the MMA's mbarrier commit (bounded), and the epilogue reads the accumulator
+// back with tcgen05.ld and fuses bias + SiLU (forward), SiLU' (input
+// gradient) or the split-K reduction (weight gradient).  The 128 -> 1 head,
+// the Fourier features, the loss and Adam run on the CUDA cores.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "../../include/lvn.h"
+#include "lvn_noise.cuh"
+#include "lvn_state.h"
+
+namespace lvn {
+namespace {
+
+constexpr int kHidden = 128;
+constexpr int kFreqs = 16;
+constexpr int kIn = 6 * kFreqs;  // 96
+constexpr int kLayers = 4;       // hidden layers
+constexpr int kTile = 128;       // rows per CTA tile (MMA M)
+constexpr int kKC = 128;         // K per shared-memory stage
+constexpr uint32_t kWaitLimit = 1u << 20;  // mbarrier polls before a CTA gives up
+
+// parameter offsets in the flat FP32 vector: W0 b0 W1 b1 W2 b2 W3 b3 w4 b4
+constexpr int kIn_[kLayers] = {kIn, kHidden, kHidden, kHidden};
+constexpr int w_off(int l) { return l == 0 ? 0 : w_off(l - 1) + kHidden * kIn_[l - 1] + kHidden; }
+constexpr int b_off(int l) { return w_off(l) + kHidden * kIn_[l]; }
+constexpr int kHeadW = w_off(kLayers);
+constexpr int kHeadB = kHeadW + kHidden;
+constexpr int kParams = kHeadB + 1;
+static_assert(kParams == 62081, "4 x 128 SiLU MLP on 96 features");
+// BF16 copies: W_l (out x in) and W_l^T (in x out) for l >= 1
+constexpr int wb_off(int l) { return l == 0 ? 0 : wb_off(l - 1) + kHidden * kIn_[l - 1]; }
+constexpr int kWb = wb_off(kLayers);
+
+// ---------------------------------------------------------------------------
+// tcgen05 / mbarrier primitives (inline PTX, sm_100 family)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.b32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// UMMA shared-memory descriptor, K-major without swizzle: core matrices of
+// 8 rows x 16 bytes; `lbo` = bytes between core matrices along K, `sbo` =
+// bytes between core matrices along M / N.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;  // descriptor version of the tcgen05 family; base offset 0, no swizzle
+    return d;
+}
+// instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major
+__host__ __device__ constexpr uint32_t umma_idesc(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+// 32 consecutive accumulator columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ float silu(float z) { return z / (1.f + __expf(-z)); }
+__device__ __forceinline__ float silu_grad(float z) {
+    const float s = 1.f / (1.f + __expf(-z));
+    return s * (1.f + z * (1.f - s));
+}
+
+// ---------------------------------------------------------------------------
+// GEMM: D[M x N] = A[M x K] B[N x K]^T, A and B BF16 row-major (K contiguous),
+// one 128-row tile of D per CTA, K split over blockIdx.y.
+// ---------------------------------------------------------------------------
+
+enum Epilogue { EPI_FWD = 0, EPI_DX = 1, EPI_DW = 2 };
+
+struct GemmArgs {
+    const __nv_bfloat16* A;
+    const __nv_bfloat16* B;
+    int M, K, lda, ldb;
+    int k_per_split;
+    // EPI_FWD: z = acc + bias -> Z (fp32, optional), X = silu(z) (bf16), Xt (bf16, optional)
+    // EPI_DX : dz = acc * silu'(Zp)  -> X = dz (bf16), Xt (bf16)
+    // EPI_DW : G[row][col] += acc (fp32 atomics)
+    const float* bias;
+    const float* Zp;
+    float* Z;
+    __nv_bfloat16* X;
+    __nv_bfloat16* Xt;
+    float* G;
+    int* status;  // set to 1 when a CTA gave up waiting on its MMAs
+};
+
+constexpr int kGemmSmem = 2 * kTile * kKC * 2;  // A and B stages, 64 KB
+
+template <int EPI, int N>
+__global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tmem_base;
+    uint8_t* sA = smem;
+    uint8_t* sB = smem + kTile * kKC * 2;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.x * kTile;
+    const int kb = blockIdx.y * g.k_per_split;
+    const int ke = min(g.K, kb + g.k_per_split);
+    if (warp == 0) tmem_alloc(&tmem_base, 128);
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+    constexpr uint32_t kIdesc = umma_idesc(kTile, N);
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int k0 = kb; k0 < ke && ok; k0 += kKC) {
+        const int kc = min(kKC, ke - k0);  // a multiple of 16
+        const int cores = kc / 8;          // 16-byte core-matrix columns along K
+        // core matrix (row group i, K column c) at c * lbo + i * 128, rows 16 B apart
+        const uint32_t lboA = (kTile / 8) * 128, lboB = (N / 8) * 128;
+        for (int i = threadIdx.x; i < kTile * cores; i += blockDim.x) {
+            const int r = i % kTile, c = i / kTile;
+            const uint4 v = *reinterpret_cast<const uint4*>(g.A + (size_t)(m0 + r) * g.lda + k0 + 8 * c);
+            *reinterpret_cast<uint4*>(sA + c * lboA + r * 16) = v;
+        }
+        for (int i = threadIdx.x; i < N * cores; i += blockDim.x) {
+            const int r = i % N, c = i / N;
+            const uint4 v = *reinterpret_cast<const uint4*>(g.B + (size_t)r * g.ldb + k0 + 8 * c);
+            *reinterpret_cast<uint4*>(sB + c * lboB + r * 16) = v;
+        }
+        fence_proxy_async();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            tc_fence_after();
+            const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+            for (int s = 0; s < kc / 16; s++)
+                umma_bf16(tmem, umma_desc(a0 + 2 * s * lboA, lboA, 128), umma_desc(b0 + 2 * s * lboB, lboB, 128),
+                          kIdesc, (k0 > kb || s > 0) ? 1u : 0u);
+            umma_commit(&bar);
+        }
+        uint32_t polls = 0;
+        while (!mbar_try_wait(&bar, phase))
+            if (++polls == kWaitLimit) {
+                ok = false;
+                break;
+            }
+        phase ^= 1u;
+        tc_fence_after();
+    }
+    if (!ok) {
+        if (lane == 0) atomicExch(g.status, 1);
+    } else if (kb < ke) {
+        const int row = warp * 32 + lane;  // D row = TMEM lane
+        const int m = m0 + row;
+#pragma unroll 1
+        for (int cc = 0; cc < N / 32; cc++) {
+            float v[32];
+            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cc * 32), v);
+            const int n0 = cc * 32;
+            if (EPI == EPI_DW) {
+#pragma unroll
+                for (int j = 0; j < 32; j++) atomicAdd(g.G + (size_t)row * N + n0 + j, v[j]);
+            } else {
+                if (EPI == EPI_FWD) {
+#pragma unroll
+                    for (int j = 0; j < 32; j++) v[j] += __ldg(g.bias + n0 + j);
+                    if (g.Z) {
+                        float4* z4 = reinterpret_cast<float4*>(g.Z + (size_t)m * N + n0);
+#pragma unroll
+                        for (int j = 0; j < 8; j++) z4[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+                    }
+#pragma unroll
+                    for (int j = 0; j < 32; j++) v[j] = silu(v[j]);
+                } else {
+                    const float4* z4 = reinterpret_cast<const float4*>(g.Zp + (size_t)m * N + n0);
+#pragma unroll
+                    for (int j = 0; j < 8; j++) {
+                        const float4 z = z4[j];
+                        v[4 * j] *= silu_grad(z.x);
+                        v[4 * j + 1] *= silu_grad(z.y);
+                        v[4 * j + 2] *= silu_grad(z.z);
+                        v[4 * j + 3] *= silu_grad(z.w);
+                    }
+                }
+                __nv_bfloat162* x2 = reinterpret_cast<__nv_bfloat162*>(g.X + (size_t)m * N + n0);
+#pragma unroll
+                for (int j = 0; j < 16; j++) x2[j] = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+                if (g.Xt) {
+#pragma unroll
+                    for (int j = 0; j < 32; j++) g.Xt[(size_t)(n0 + j) * g.M + m] = __float2bfloat16_rn(v[j]);
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, 128);
+}
+
+template <int EPI, int N>
+cudaError_t gemm(const GemmArgs& g, int splits, cudaStream_t s) {
+    static bool configured = false;
+    if (!configured) {
+        const cudaError_t e = cudaFuncSetAttribute(k_gemm<EPI, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    dim3 grid(EPI == EPI_DW ? 1 : g.M / kTile, splits);
+    k_gemm<EPI, N><<<grid, 128, kGemmSmem, s>>>(g);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// CUDA-core kernels: samples, features, head + loss, bias gradients, Adam
+// ---------------------------------------------------------------------------
+
+struct Domain {
+    float lo[3], hi[3];
+};
+
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {  // splitmix64 finaliser
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+__device__ __forceinline__ float unit(uint64_t h) { return (float)(h >> 40) * (1.f / 16777216.f); }
+
+// 70% of the samples within 4 voxels of the heightfield surface (y = amp h +
+// U(-4, 4), so |d| <= 4 for the heightfield), 30% uniform in the domain;
+// target = the plain density.
+__global__ void k_samples(float4* out, int n, uint64_t seed, Domain dom, const uint8_t* perm, const uint16_t* perm_k4,
+                          const float* grad, DensityParams dp) {
+    __shared__ float sg[64];
+    if (threadIdx.x < 64) sg[threadIdx.x] = grad[threadIdx.x];
+    __syncthreads();
+    const Noise nz{perm, perm_k4, sg};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint64_t h0 = mix64(seed ^ mix64((uint64_t)i * 4 + 0)), h1 = mix64(seed ^ mix64((uint64_t)i * 4 + 1));
+        const uint64_t h2 = mix64(seed ^ mix64((uint64_t)i * 4 + 2)), h3 = mix64(seed ^ mix64((uint64_t)i * 4 + 3));
+        const float x = dom.lo[0] + unit(h1) * (dom.hi[0] - dom.lo[0]);
+        const float z = dom.lo[2] + unit(h2) * (dom.hi[2] - dom.lo[2]);
+        float y;
+        if (unit(h0) < 0.7f) y = nz.height_amp(dp) * nz.height(dp, x, z) + (unit(h3) * 8.f - 4.f);
+        else y = dom.lo[1] + unit(h3) * (dom.hi[1] - dom.lo[1]);
+        out[i] = make_float4(x, y, z, nz.density(dp, x, y, z));
+    }
+}
+
+struct FeatureFreqs {
+    float f[3][kFreqs];
+};
+
+// Positions of lattice points: point i of a batch is point (first + i) of the
+// concatenated lattices, lattice l = (origin xyz, step) of dim^3 points with x
+// fastest.  Writes float4 positions for k_features.
+__global__ void k_lattice_points(const float4* lattices, int64_t first, int n, int dim, float4* pts) {
+    const int64_t per = (int64_t)dim * dim * dim;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int64_t g = first + i;
+        const int64_t l = g / per;
+        const int r = (int)(g - l * per);
+        const int z = r / (dim * dim), y = (r / dim) % dim, x = r % dim;
+        const float4 o = lattices[l];
+        pts[i] = make_float4(o.x + o.w * (float)x, o.y + o.w * (float)y, o.z + o.w * (float)z, 0.f);
+    }
+}
+
+// Fourier features of a position normalised to [-1, 1] over the domain:
+// [sin(pi f u_x) x16, cos x16, then y, then z]
+__global__ void k_features(const float4* pts, int n, Domain dom, FeatureFreqs ff, __nv_bfloat16* X,
+                           __nv_bfloat16* Xt) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 p = pts[i];
+        const float c[3] = {p.x, p.y, p.z};
+        __nv_bfloat16* row = X + (size_t)i * kIn;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const float u = 2.f * (c[a] - dom.lo[a]) / (dom.hi[a] - dom.lo[a]) - 1.f;
+#pragma unroll 4
+            for (int k = 0; k < kFreqs; k++) {
+                float s, co;
+                sincospif(ff.f[a][k] * u, &s, &co);
+                const __nv_bfloat16 bs = __float2bfloat16_rn(s), bc = __float2bfloat16_rn(co);
+                row[a * 2 * kFreqs + k] = bs;
+                row[a * 2 * kFreqs + kFreqs + k] = bc;
+                if (Xt) {
+                    Xt[(size_t)(a * 2 * kFreqs + k) * n + i] = bs;
+                    Xt[(size_t)(a * 2 * kFreqs + kFreqs + k) * n + i] = bc;
+                }
+            }
+        }
+    }
+}
+
+// Head: y = X4 . w4 + b4 (density / out_scale).  Training: r = y - t / s,
+// loss += r^2 / n, dy = 2 r / n, dZ3 = dy w4 silu'(Z3), gw4 += dy X4, gb4 += dy.
+__global__ void __launch_bounds__(128) k_head(const __nv_bfloat16* X4, const float* Z3, const float4* pts, int n,
+                                              const float* params, float out_scale, float* dens_out,
+                                              __nv_bfloat16* dZ, __nv_bfloat16* dZt, float* grads, float* loss) {
+    __shared__ float w4[kHidden];
+    __shared__ float gw[kHidden];
+    __shared__ float red[4];
+    if (threadIdx.x < kHidden) {
+        w4[threadIdx.x] = params[kHeadW + threadIdx.x];
+        gw[threadIdx.x] = 0.f;
+    }
+    __syncthreads();
+    const float b4 = params[kHeadB];
+    const bool train = loss != nullptr;
+    float l = 0.f, gb = 0.f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const __nv_bfloat162* x2 = reinterpret_cast<const __nv_bfloat162*>(X4 + (size_t)i * kHidden);
+        float y = b4;
+#pragma unroll 8
+        for (int j = 0; j < kHidden / 2; j++) {
+            const float2 x = __bfloat1622float2(x2[j]);
+            y = fmaf(x.x, w4[2 * j], y);
+            y = fmaf(x.y, w4[2 * j + 1], y);
+        }
+        if (!train) {
+            dens_out[i] = y * out_scale;
+            continue;
+        }
+        const float r = y - pts[i].w / out_scale;
+        l += r * r;
+        const float dy = 2.f * r / (float)n;
+        gb += dy;
+        const float* z = Z3 + (size_t)i * kHidden;
+#pragma unroll 4
+        for (int j = 0; j < kHidden; j++) {
+            const float x = __bfloat162float(X4[(size_t)i * kHidden + j]);
+            atomicAdd(&gw[j], dy * x);
+            const __nv_bfloat16 d = __float2bfloat16_rn(dy * w4[j] * silu_grad(z[j]));
+            dZ[(size_t)i * kHidden + j] = d;
+            dZt[(size_t)j * n + i] = d;
+        }
+    }
+    if (!train) return;
+    __syncthreads();
+    if (threadIdx.x < kHidden) atomicAdd(&grads[kHeadW + threadIdx.x], gw[threadIdx.x]);
+    for (int o = 16; o; o >>= 1) {
+        l += __shfl_xor_sync(0xffffffffu, l, o);
+        gb += __shfl_xor_sync(0xffffffffu, gb, o);
+    }
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = l;
+    __syncthreads();
+    if (threadIdx.x == 0) atomicAdd(loss, (red[0] + red[1] + red[2] + red[3]) / (float)n);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&grads[kHeadB], gb);
+}
+
+// bias gradient of layer l: sum over the batch of dZ (rows of dZ^T)
+__global__ void __launch_bounds__(256) k_bias_grad(const __nv_bfloat16* dZt, int n, float* g) {
+    __shared__ float red[8];
+    const __nv_bfloat16* row = dZt + (size_t)blockIdx.x * n;
+    float s = 0.f;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += __bfloat162float(row[i]);
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+        for (int w = 0; w < 8; w++) t += red[w];
+        g[blockIdx.x] += t;
+    }
+}
+
+struct LayerMap {
+    int w[kLayers], b[kLayers], in[kLayers], wb[kLayers];
+};
+
+// Adam (beta 0.9 / 0.999, eps 1e-8) on the FP32 master weights; refreshes the
+// BF16 copies W_l and W_l^T.
+__global__ void k_adam(float* p, const float* g, float* m, float* v, int n, float lr, float c1, float c2,
+                       __nv_bfloat16* wb, __nv_bfloat16* wt, LayerMap lm) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = 0.9f * m[i] + 0.1f * gi;
+        const float vi = 0.999f * v[i] + 0.001f * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        const float pi = p[i] - lr * (mi * c1) / (sqrtf(vi * c2) + 1e-8f);
+        p[i] = pi;
+#pragma unroll
+        for (int l = 0; l < kLayers; l++) {
+            const int rel = i - lm.w[l];
+            if (rel >= 0 && rel < kHidden * lm.in[l]) {
+                const int o = rel / lm.in[l], k = rel - o * lm.in[l];
+                wb[lm.wb[l] + rel] = __float2bfloat16_rn(pi);
+                wt[lm.wb[l] + k * kHidden + o] = __float2bfloat16_rn(pi);
+            }
+        }
+    }
+}
+
+__global__ void k_to_bf16(const float* p, int n, __nv_bfloat16* wb, __nv_bfloat16* wt, LayerMap lm) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int l = 0; l < kLayers; l++) {
+            const int rel = i - lm.w[l];
+            if (rel >= 0 && rel < kHidden * lm.in[l]) {
+                const int o = rel / lm.in[l], k = rel - o * lm.in[l];
+                wb[lm.wb[l] + rel] = __float2bfloat16_rn(p[i]);
+                wt[lm.wb[l] + k * kHidden + o] = __float2bfloat16_rn(p[i]);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+#define SG_CK(x)                                       \
+    do {                                               \
+        const cudaError_t e__ = (x);                   \
+        if (e__ != cudaSuccess) {                      \
+            cudaGetLastError();                        \
+            return e__ == cudaErrorMemoryAllocation ? LVN_ERR_OUT_OF_MEMORY : LVN_ERR_CUDA; \
+        }                                              \
+    } while (0)
+
+struct Buf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t b) {
+        if (b <= bytes) return LVN_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        SG_CK(cudaMalloc(&p, b));
+        bytes = b;
+        return LVN_OK;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <typename T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+LayerMap layer_map() {
+    LayerMap lm;
+    for (int l = 0; l < kLayers; l++) {
+        lm.w[l] = w_off(l);
+        lm.b[l] = b_off(l);
+        lm.in[l] = kIn_[l];
+        lm.wb[l] = wb_off(l);
+    }
+    return lm;
+}
+
+}  // namespace
+}  // namespace lvn
+
+using namespace lvn;
+
+struct lvn_surrogate {
+    Domain dom;
+    FeatureFreqs ff;
+    float out_scale = 8.f;  // the network predicts density / out_scale
+    cudaStream_t stream = nullptr;
+    Buf params, grads, adam_m, adam_v, wb, wt, loss, status;
+    // batch activations
+    int cap = 0;
+    Buf pts, X[kLayers + 1], Xt[kLayers + 1], Z[kLayers], dZ[2], dZt[2], dens;
+    Buf pool;  // training samples
+    int64_t pool_n = 0;
+    int64_t pool_next = 0;
+    int step = 0;
+
+    int ensure_batch(int n) {
+        if (n <= cap) return LVN_OK;
+        int rc;
+        if ((rc = pts.ensure(sizeof(float4) * n))) return rc;
+        for (int l = 0; l <= kLayers; l++) {
+            const int w = l == 0 ? kIn : kHidden;
+            if ((rc = X[l].ensure(2ull * n * w))) return rc;
+            if ((rc = Xt[l].ensure(2ull * n * w))) return rc;
+        }
+        for (int l = 0; l < kLayers; l++)
+            if ((rc = Z[l].ensure(4ull * n * kHidden))) return rc;
+        for (int i = 0; i < 2; i++) {
+            if ((rc = dZ[i].ensure(2ull * n * kHidden))) return rc;
+            if ((rc = dZt[i].ensure(2ull * n * kHidden))) return rc;
+        }
+        if ((rc = dens.ensure(4ull * n))) return rc;
+        cap = n;
+        return LVN_OK;
+    }
+
+    // forward through the hidden layers (transposes only when training)
+    int forward(int n, bool train) {
+        GemmArgs g;
+        std::memset(&g, 0, sizeof(g));
+        g.status = status.as<int>();
+        const int grid = std::min(1184, (n + 255) / 256);
+        k_features<<<grid, 256, 0, stream>>>(pts.as<float4>(), n, dom, ff, X[0].as<__nv_bfloat16>(),
+                                             train ? Xt[0].as<__nv_bfloat16>() : nullptr);
+        SG_CK(cudaGetLastError());
+        for (int l = 0; l < kLayers; l++) {
+            g.A = X[l].as<__nv_bfloat16>();
+            g.B = wb.as<__nv_bfloat16>() + wb_off(l);
+            g.M = n;
+            g.K = kIn_[l];
+            g.lda = g.ldb = kIn_[l];
+            g.k_per_split = kIn_[l];
+            g.bias = params.as<float>() + b_off(l);
+            g.Z = train ? Z[l].as<float>() : nullptr;
+            g.X = X[l + 1].as<__nv_bfloat16>();
+            g.Xt = train ? Xt[l + 1].as<__nv_bfloat16>() : nullptr;
+            SG_CK((gemm<EPI_FWD, kHidden>(g, 1, stream)));
+        }
+        return LVN_OK;
+    }
+
+    // one forward + backward on the n samples in pts; gradients into grads
+    int backward(int n) {
+        SG_CK(cudaMemsetAsync(grads.p, 0, sizeof(float) * kParams, stream));
+        SG_CK(cudaMemsetAsync(loss.p, 0, sizeof(float), stream));
+        int rc = forward(n, true);
+        if (rc) return rc;
+        k_head<<<std::min(1184, (n + 127) / 128), 128, 0, stream>>>(
+            X[kLayers].as<__nv_bfloat16>(), Z[kLayers - 1].as<float>(), pts.as<float4>(), n, params.as<float>(),
+            out_scale, nullptr, dZ[1].as<__nv_bfloat16>(), dZt[1].as<__nv_bfloat16>(), grads.as<float>(),
+            loss.as<float>());
+        SG_CK(cudaGetLastError());
+        GemmArgs g;
+        std::memset(&g, 0, sizeof(g));
+        g.status = status.as<int>();
+        // split-K over the batch for the weight gradients: 128 samples per MMA stage
+        const int per_split = std::max(kKC, ((n / 148) + kKC - 1) / kKC * kKC);
+        const int splits = (n + per_split - 1) / per_split;
+        for (int l = kLayers - 1; l >= 0; l--) {
+            // dZ of the last hidden layer is in buffer 1 (k_head), then the buffers alternate
+            const int buf = ((kLayers - 1 - l) & 1) ? 0 : 1;
+            // dW_l = dZ_l^T X_l
+            g.A = dZt[buf].as<__nv_bfloat16>();
+            g.B = Xt[l].as<__nv_bfloat16>();
+            g.M = kHidden;
+            g.K = n;
+            g.lda = g.ldb = n;
+            g.k_per_split = per_split;
+            g.G = grads.as<float>() + w_off(l);
+            if (l == 0) SG_CK((gemm<EPI_DW, kIn>(g, splits, stream)));
+            else SG_CK((gemm<EPI_DW, kHidden>(g, splits, stream)));
+            k_bias_grad<<<kHidden, 256, 0, stream>>>(dZt[buf].as<__nv_bfloat16>(), n, grads.as<float>() + b_off(l));
+            SG_CK(cudaGetLastError());
+            if (l == 0) break;
+            // dZ_{l-1} = (dZ_l W_l) * silu'(Z_{l-1})
+            GemmArgs d;
+            std::memset(&d, 0, sizeof(d));
+            d.status = status.as<int>();
+            d.A = dZ[buf].as<__nv_bfloat16>();
+            d.B = wt.as<__nv_bfloat16>() + wb_off(l);
+            d.M = n;
+            d.K = kHidden;
+            d.lda = d.ldb = kHidden;
+            d.k_per_split = kHidden;
+            d.Zp = Z[l - 1].as<float>();
+            d.X = dZ[buf ^ 1].as<__nv_bfloat16>();
+            d.Xt = dZt[buf ^ 1].as<__nv_bfloat16>();
+            SG_CK((gemm<EPI_DX, kHidden>(d, 1, stream)));
+        }
+        return LVN_OK;
+    }
+};
+
+namespace {
+
+int check_status(lvn_surrogate* s) {
+    int st = 0;
+    SG_CK(cudaMemcpyAsync(&st, s->status.p, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    SG_CK(cudaStreamSynchronize(s->stream));
+    return st ? LVN_ERR_DEVICE_STATUS : LVN_OK;
+}
+
+int upload_samples(lvn_surrogate* s, const float* host, int n) {
+    int rc = s->ensure_batch(n);
+    if (rc) return rc;
+    SG_CK(cudaMemcpyAsync(s->pts.p, host, sizeof(float4) * n, cudaMemcpyHostToDevice, s->stream));
+    return LVN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+lvn_surrogate* lvn_surrogate_create(const float domain_min[3], const float domain_max[3], uint64_t seed) {
+    if (!domain_min || !domain_max) return nullptr;
+    for (int a = 0; a < 3; a++)
+        if (!(domain_max[a] > domain_min[a])) return nullptr;
+    lvn_surrogate* s = new lvn_surrogate();
+    for (int a = 0; a < 3; a++) {
+        s->dom.lo[a] = domain_min[a];
+        s->dom.hi[a] = domain_max[a];
+        // frequencies from one period over the domain to a 2-voxel period
+        const double top = std::log2(std::max(2.0, (double)(domain_max[a] - domain_min[a]) / 2.0));
+        for (int k = 0; k < kFreqs; k++) s->ff.f[a][k] = (float)std::exp2(top * k / (kFreqs - 1));
+    }
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete s;
+        return nullptr;
+    }
+    bool ok = !s->params.ensure(4ull * kParams) && !s->grads.ensure(4ull * kParams) && !s->adam_m.ensure(4ull * kParams) &&
+              !s->adam_v.ensure(4ull * kParams) && !s->wb.ensure(2ull * kWb) && !s->wt.ensure(2ull * kWb) &&
+              !s->loss.ensure(4) && !s->status.ensure(4);
+    // PyTorch's Linear initialisation: U(-1/sqrt(fan_in), 1/sqrt(fan_in)), from splitmix64(seed)
+    std::vector<float> h(kParams);
+    uint64_t st = seed;
+    auto next = [&st]() {
+        st += 0x9E3779B97F4A7C15ull;
+        uint64_t x = st;
+        x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+        x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+        x ^= x >> 31;
+        return (float)(x >> 40) * (1.f / 16777216.f);
+    };
+    for (int l = 0; l <= kLayers; l++) {
+        const int fan_in = l < kLayers ? kIn_[l] : kHidden;
+        const int wo = l < kLayers ? w_off(l) : kHeadW, bo = l < kLayers ? b_off(l) : kHeadB;
+        const int nw = l < kLayers ? kHidden * fan_in : kHidden, nb = l < kLayers ? kHidden : 1;
+        const float bound = 1.f / std::sqrt((float)fan_in);
+        for (int i = 0; i < nw; i++) h[wo + i] = (2.f * next() - 1.f) * bound;
+        for (int i = 0; i < nb; i++) h[bo + i] = (2.f * next() - 1.f) * bound;
+    }
+    if (ok && lvn_surrogate_set_params(s, h.data(), kParams) != LVN_OK) ok = false;
+    if (!ok) {
+        lvn_surrogate_destroy(s);
+        return nullptr;
+    }
+    return s;
+}
+
+void lvn_surrogate_destroy(lvn_surrogate* s) {
+    if (!s) return;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    Buf* bufs[] = {&s->params, &s->grads, &s->adam_m, &s->adam_v, &s->wb, &s->wt, &s->loss, &s->status,
+                   &s->pts, &s->dZ[0], &s->dZ[1], &s->dZt[0], &s->dZt[1], &s->dens, &s->pool};
+    for (Buf* b : bufs) b->release();
+    for (int l = 0; l <= kLayers; l++) {
+        s->X[l].release();
+        s->Xt[l].release();
+    }
+    for (int l = 0; l < kLayers; l++) s->Z[l].release();
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+int32_t lvn_surrogate_num_params(void) { return kParams; }
+
+int lvn_surrogate_set_params(lvn_surrogate* s, const float* host, int64_t n) {
+    if (!s || !host || n != kParams) return LVN_ERR_INVALID;
+    SG_CK(cudaMemcpyAsync(s->params.p, host, 4ull * kParams, cudaMemcpyHostToDevice, s->stream));
+    SG_CK(cudaMemsetAsync(s->adam_m.p, 0, 4ull * kParams, s->stream));
+    SG_CK(cudaMemsetAsync(s->adam_v.p, 0, 4ull * kParams, s->stream));
+    SG_CK(cudaMemsetAsync(s->status.p, 0, 4, s->stream));
+    k_to_bf16<<<64, 256, 0, s->stream>>>(s->params.as<float>(), kParams, s->wb.as<__nv_bfloat16>(),
+                                         s->wt.as<__nv_bfloat16>(), layer_map());
+    SG_CK(cudaGetLastError());
+    s->step = 0;
+    SG_CK(cudaStreamSynchronize(s->stream));
+    return LVN_OK;
+}
+
+int lvn_surrogate_get_params(lvn_surrogate* s, float* host, int64_t n) {
+    if (!s || !host || n < kParams) return LVN_ERR_INVALID;
+    SG_CK(cudaMemcpyAsync(host, s->params.p, 4ull * kParams, cudaMemcpyDeviceToHost, s->stream));
+    SG_CK(cudaStreamSynchronize(s->stream));
+    return kParams;
+}
+
+int lvn_surrogate_sample(lvn_surrogate* s, int64_t n, uint64_t seed, float* host_out) {
+    if (!s || n <= 0) return LVN_ERR_INVALID;
+    const GlobalView gv = global_view();
+    if (!gv.initialised) return LVN_ERR_NOT_INITIALISED;
+    int rc = s->pool.ensure(sizeof(float4) * (size_t)n);
+    if (rc) return rc;
+    k_samples<<<gv.num_sms * 8, 256, 0, s->stream>>>(s->pool.as<float4>(), (int)n, seed, s->dom, gv.perm, gv.perm_k4,
+                                                     gv.grad, gv.density);
+    SG_CK(cudaGetLastError());
+    s->pool_n = n;
+    s->pool_next = 0;
+    if (host_out) SG_CK(cudaMemcpyAsync(host_out, s->pool.p, sizeof(float4) * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+    SG_CK(cudaStreamSynchronize(s->stream));
+    return LVN_OK;
+}
+
+int lvn_surrogate_grad(lvn_surrogate* s, const float* samples, int32_t n, float* grad_out, float* loss_out) {
+    if (!s || !samples || n <= 0 || n % kTile) return LVN_ERR_INVALID;
+    int rc = upload_samples(s, samples, n);
+    if (rc) return rc;
+    if ((rc = s->backward(n))) return rc;
+    if ((rc = check_status(s))) return rc;
+    if (grad_out) SG_CK(cudaMemcpy(grad_out, s->grads.p, 4ull * kParams, cudaMemcpyDeviceToHost));
+    if (loss_out) SG_CK(cudaMemcpy(loss_out, s->loss.p, 4, cudaMemcpyDeviceToHost));
+    return LVN_OK;
+}
+
+int lvn_surrogate_train(lvn_surrogate* s, int32_t steps, int32_t batch, float lr, float* losses) {
+    if (!s || steps < 0 || batch <= 0 || batch % kTile || !(lr > 0.f)) return LVN_ERR_INVALID;
+    if (s->pool_n < batch) return LVN_ERR_INVALID;  // lvn_surrogate_sample first
+    int rc = s->ensure_batch(batch);
+    if (rc) return rc;
+    const LayerMap lm = layer_map();
+    for (int it = 0; it < steps; it++) {
+        // the next `batch` samples of the pool (wrapping)
+        const int64_t first = s->pool_next;
+        const int64_t take = std::min<int64_t>(batch, s->pool_n - first);
+        SG_CK(cudaMemcpyAsync(s->pts.p, s->pool.as<float4>() + first, sizeof(float4) * take, cudaMemcpyDeviceToDevice,
+                              s->stream));
+        if (take < batch)
+            SG_CK(cudaMemcpyAsync(s->pts.as<float4>() + take, s->pool.p, sizeof(float4) * (batch - take),
+                                  cudaMemcpyDeviceToDevice, s->stream));
+        s->pool_next = (first + batch) % s->pool_n;
+        if ((rc = s->backward(batch))) return rc;
+        s->step++;
+        const float c1 = 1.f / (1.f - std::pow(0.9f, (float)s->step));
+        const float c2 = 1.f / (1.f - std::pow(0.999f, (float)s->step));
+        k_adam<<<64, 256, 0, s->stream>>>(s->params.as<float>(), s->grads.as<float>(), s->adam_m.as<float>(),
+                                          s->adam_v.as<float>(), kParams, lr, c1, c2, s->wb.as<__nv_bfloat16>(),
+                                          s->wt.as<__nv_bfloat16>(), lm);
+        SG_CK(cudaGetLastError());
+        if (losses) SG_CK(cudaMemcpyAsync(losses + it, s->loss.p, 4, cudaMemcpyDeviceToHost, s->stream));
+    }
+    return check_status(s);
+}
+
+int lvn_surrogate_eval(lvn_surrogate* s, const float* points, int64_t n, float* density, int32_t memory) {
+    if (!s || !points || !density || n <= 0) return LVN_ERR_INVALID;
+    const int64_t chunk = 1 << 20;
+    int rc = s->ensure_batch((int)std::min<int64_t>(chunk, (n + kTile - 1) / kTile * kTile));
+    if (rc) return rc;
+    const cudaMemcpyKind in = memory == LVN_MEMORY_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    const cudaMemcpyKind out = memory == LVN_MEMORY_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    for (int64_t first = 0; first < n; first += chunk) {
+        const int m = (int)std::min<int64_t>(chunk, n - first);
+        const int padded = (m + kTile - 1) / kTile * kTile;
+        if (padded > m) SG_CK(cudaMemsetAsync(s->pts.as<float4>() + m, 0, sizeof(float4) * (padded - m), s->stream));
+        SG_CK(cudaMemcpyAsync(s->pts.p, points + 4 * first, sizeof(float4) * m, in, s->stream));
+        if ((rc = s->forward(padded, false))) return rc;
+        k_head<<<std::min(1184, (padded + 127) / 128), 128, 0, s->stream>>>(
+            s->X[kLayers].as<__nv_bfloat16>(), nullptr, nullptr, padded, s->params.as<float>(), s->out_scale,
+            s->dens.as<float>(), nullptr, nullptr, nullptr, nullptr);
+        SG_CK(cudaGetLastError());
+        SG_CK(cudaMemcpyAsync(density + first, s->dens.p, sizeof(float) * m, out, s->stream));
+    }
+    return check_status(s);
+}
+
+int lvn_surrogate_eval_lattices(lvn_surrogate* s, const float* lattices, int32_t count, int32_t dim, float* density) {
+    if (!s || !lattices || !density || count < 0 || dim <= 0) return LVN_ERR_INVALID;
+    const int64_t n = (int64_t)count * dim * dim * dim;
+    if (n == 0) return LVN_OK;
+    const int64_t chunk = 1 << 20;
+    int rc = s->ensure_batch((int)std::min<int64_t>(chunk, (n + kTile - 1) / kTile * kTile));
+    if (rc) return rc;
+    for (int64_t first = 0; first < n; first += chunk) {
+        const int m = (int)std::min<int64_t>(chunk, n - first);
+        const int padded = (m + kTile - 1) / kTile * kTile;
+        if (padded > m) SG_CK(cudaMemsetAsync(s->pts.as<float4>() + m, 0, sizeof(float4) * (padded - m), s->stream));
+        k_lattice_points<<<std::min(1184, (m + 255) / 256), 256, 0, s->stream>>>(
+            reinterpret_cast<const float4*>(lattices), first, m, dim, s->pts.as<float4>());
+        SG_CK(cudaGetLastError());
+        if ((rc = s->forward(padded, false))) return rc;
+        k_head<<<std::min(1184, (padded + 127) / 128), 128, 0, s->stream>>>(
+            s->X[kLayers].as<__nv_bfloat16>(), nullptr, nullptr, padded, s->params.as<float>(), s->out_scale,
+            s->dens.as<float>(), nullptr, nullptr, nullptr, nullptr);
+        SG_CK(cudaGetLastError());
+        SG_CK(cudaMemcpyAsync(density + first, s->dens.p, sizeof(float) * m, cudaMemcpyDeviceToDevice, s->stream));
+    }
+    return check_status(s);
+}
+
+int lvn_surrogate_domain(const lvn_surrogate* s, float domain_min[3], float domain_max[3]) {
+    if (!s || !domain_min || !domain_max) return LVN_ERR_INVALID;
+    for (int a = 0; a < 3; a++) {
+        domain_min[a] = s->dom.lo[a];
+        domain_max[a] = s->dom.hi[a];
+    }
+    return LVN_OK;
+}
+
+void* lvn_surrogate_get_stream(lvn_surrogate* s) { return s ? (void*)s->stream : nullptr; }
+
+}  // extern "C"

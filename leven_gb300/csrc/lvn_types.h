@@ -80,9 +80,13 @@ struct ChunkState {
     int32_t wl_c_off;
     uint32_t edge_magic;     // floor((2^32 - 1) / edge_prime), for the table modulo
     uint32_t node_magic;
+    int32_t simp_verts;      // simplified mesh: vertices, first vertex, triangles, first triangle
+    int32_t simp_vert_off;
+    int32_t simp_tris;
+    int32_t simp_tri_off;
     int32_t pad[2];
 };
-static_assert(sizeof(ChunkState) == 112, "ChunkState layout");
+static_assert(sizeof(ChunkState) == 128, "ChunkState layout");
 
 // Batch-wide totals and status (device).
 struct BatchState {
@@ -97,8 +101,35 @@ struct BatchState {
     int32_t total_xz;        // hermite work-list segment sizes
     int32_t total_y;
     int32_t total_created;
-    int32_t pad[3];
+    int32_t total_simp_verts;  // simplified mesh totals
+    int32_t total_simp_tris;
+    int32_t pad[1];
 };
+
+// Octree simplification: a node's QEF in its own frame (origin at the node's
+// min corner, unit = one voxel).  ATA and ATb as in QEFData (qef.cl:7-14),
+// plus btb = sum (n.p)^2, the point count, the mass-point sum and the normal sum.
+struct SimpQef {
+    float ata[6];
+    float btb, w;
+    float atb[3];
+    float mp[3];
+    float ns[3];
+    float pad[3];
+};
+static_assert(sizeof(SimpQef) == 80, "SimpQef layout");
+
+// One octree node above the leaves (level k >= 1) of the simplification.
+struct SimpNode {
+    int32_t chunk;
+    int32_t pos;        // x | y << 8 | z << 16 in units of the node size
+    int32_t collapsed;  // 1 when the node replaces its subtree
+    int32_t anchor;     // first leaf voxel (chunk-local index) below the node
+    float wpos[3];      // world position of the collapsed node's vertex
+    int32_t material;
+    SimpQef q;
+};
+static_assert(sizeof(SimpNode) == 112, "SimpNode layout");
 
 enum OverflowBits : int32_t {
     OVF_EDGES = 1,

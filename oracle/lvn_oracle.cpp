@@ -28,12 +28,15 @@
 #include <algorithm>
 #include <array>
 #include <atomic>
+#include <climits>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <random>
 #include <thread>
+#include <unordered_map>
 #include <unordered_set>
 #include <vector>
 
@@ -828,6 +831,14 @@ struct Chunk {
     std::vector<float> vertices;     // 12 floats per MeshVertex
     std::vector<int32_t> seams;      // 12 x 4-byte words per SeamNodeInfo
     int mesh_vertex_count = 0;
+    // the chunk's arguments, for the simplification pass
+    int vpc = 0, scale = 0, size = 0;
+    int min[3] = {0, 0, 0};
+    // bottom-up octree simplification (orc_chunk_simplify)
+    std::vector<float> simp_vertices;
+    std::vector<int32_t> simp_triangles;
+    std::vector<int32_t> simp_reps;  // per voxel: anchor | level << 20
+    int simp_vertex_count = 0;
 };
 
 inline int edge_key(const Dims& D, int x, int y, int z, int axis) {
@@ -989,6 +1000,10 @@ int run_chunk(Chunk& ch, const orc_density& dn, const orc_chunk_args& a, const P
     ch = Chunk();
     const int scale = a.size / (D.vpc * LEAF_SIZE_SCALE);
     if (scale <= 0) return -1;
+    ch.vpc = D.vpc;
+    ch.scale = scale;
+    ch.size = a.size;
+    for (int i = 0; i < 3; i++) ch.min[i] = a.min[i];
     const int off[3] = {a.min[0] / LEAF_SIZE_SCALE, a.min[1] / LEAF_SIZE_SCALE, a.min[2] / LEAF_SIZE_SCALE};
 
     // GenerateDefaultField (density_field.cl:11-37)
@@ -1172,6 +1187,320 @@ int run_chunk(Chunk& ch, const orc_density& dn, const orc_chunk_args& a, const P
     return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Bottom-up octree simplification (not in the reference).  Classic dual
+// contouring collapse (Ju et al. 2002, section 4) over the chunk's leaf
+// octree, with the reference's QEF solver (qef_solve, qef.cl:239-256):
+//
+//   * every node keeps its QEF in its own frame: origin at the node's min
+//     corner, unit = one voxel, so that the error is well conditioned at every
+//     LOD.  Next to ATA and ATb (qef.cl:7-14) it carries btb = sum (n.p)^2, the
+//     point count w, the mass-point sum and the normal sum;
+//   * a leaf's QEF holds its edge crossings (the ones CreateLeafNodes uses,
+//     octree.cl:236-312), in edge order, as qef_add_point does (qef.cl:170-191);
+//   * a node at level k (2^k voxels) sums its children's QEFs in child order
+//     (CHILD_MIN_OFFSETS, shared_constants.cl:11-22), each moved from the child's
+//     frame by d = child origin - node origin: ATb += ATA d, btb += 2 d.ATb +
+//     d.ATA d, mass point += w d;
+//   * it is solved with qef_solve (the mass point is the running sum over w,
+//     which qef_solve divides out); if the solution leaves the node's cube the
+//     mass point is used; the error is the QEF's value there,
+//     E(x) = x.ATA x - 2 x.ATb + btb;
+//   * a node collapses when E <= threshold, every child that exists collapsed
+//     (leaves count as collapsed) and no child is a seam voxel (a voxel on the
+//     chunk's faces, FindSeamNodes octree.cl:506-520), so the seams that the
+//     neighbouring chunks stitch against are unchanged.
+//
+// The mesh is classic DC contouring of the collapsed octree expressed over the
+// leaf quads of GenerateMesh (octree.cl:385-442): each leaf voxel stands for
+// its highest collapsed ancestor (its representative); a quad is kept only on
+// the first sign change along its minimal edge (the edge of the smallest of its
+// four representatives) when that edge's end points differ in sign, its two
+// triangles are remapped to the representatives' vertices and triangles with a
+// repeated vertex are dropped.  Vertices are the representatives, ordered by
+// their first voxel in the leaf order.
+// ---------------------------------------------------------------------------
+
+struct SQef {
+    float ata[6];
+    float btb, w;
+    float atb[3];
+    float mp[3];
+    float ns[3];
+    float pad;
+};
+
+void sqef_zero(SQef& q) { std::memset(&q, 0, sizeof(q)); }
+
+// a leaf's QEF in its voxel frame from its crossings (p in [0,1]^3, n)
+void sqef_add_point(SQef& q, float px, float py, float pz, float nx, float ny, float nz) {
+    q.ata[0] += nx * nx;
+    q.ata[1] += nx * ny;
+    q.ata[2] += nx * nz;
+    q.ata[3] += ny * ny;
+    q.ata[4] += ny * nz;
+    q.ata[5] += nz * nz;
+    const float b = dot3(px, py, pz, nx, ny, nz);
+    q.atb[0] += nx * b;
+    q.atb[1] += ny * b;
+    q.atb[2] += nz * b;
+    q.btb = std::fmaf(b, b, q.btb);
+    q.mp[0] += px;
+    q.mp[1] += py;
+    q.mp[2] += pz;
+    q.w += 1.f;
+    q.ns[0] += nx;
+    q.ns[1] += ny;
+    q.ns[2] += nz;
+}
+
+// q += child moved by d (child origin - node origin, voxels)
+void sqef_merge(SQef& q, const SQef& c, float dx, float dy, float dz) {
+    const float* A = c.ata;
+    const float adx = dot3(A[0], A[1], A[2], dx, dy, dz);
+    const float ady = dot3(A[1], A[3], A[4], dx, dy, dz);
+    const float adz = dot3(A[2], A[4], A[5], dx, dy, dz);
+    for (int i = 0; i < 6; i++) q.ata[i] += A[i];
+    q.atb[0] += c.atb[0] + adx;
+    q.atb[1] += c.atb[1] + ady;
+    q.atb[2] += c.atb[2] + adz;
+    q.btb += c.btb + std::fmaf(2.f, dot3(dx, dy, dz, c.atb[0], c.atb[1], c.atb[2]), dot3(dx, dy, dz, adx, ady, adz));
+    q.mp[0] += std::fmaf(c.w, dx, c.mp[0]);
+    q.mp[1] += std::fmaf(c.w, dy, c.mp[1]);
+    q.mp[2] += std::fmaf(c.w, dz, c.mp[2]);
+    q.w += c.w;
+    q.ns[0] += c.ns[0];
+    q.ns[1] += c.ns[1];
+    q.ns[2] += c.ns[2];
+}
+
+float sqef_error(const SQef& q, float x, float y, float z) {
+    const float* A = q.ata;
+    const float ax = dot3(A[0], A[1], A[2], x, y, z);
+    const float ay = dot3(A[1], A[3], A[4], x, y, z);
+    const float az = dot3(A[2], A[4], A[5], x, y, z);
+    return std::fmaf(-2.f, dot3(x, y, z, q.atb[0], q.atb[1], q.atb[2]), dot3(x, y, z, ax, ay, az)) + q.btb;
+}
+
+// solve a node's QEF (node size s voxels): position in the node frame and error
+float sqef_solve(const SQef& q, float s, float out[3]) {
+    QEF r;
+    std::memset(&r, 0, sizeof(r));
+    for (int i = 0; i < 6; i++) r.ata[i] = q.ata[i];
+    r.atb = F4{q.atb[0], q.atb[1], q.atb[2], 0.f};
+    r.masspoint = F4{q.mp[0], q.mp[1], q.mp[2], q.w};
+    F4 x = qef_solve(r);
+    if (!(x.x >= 0.f && x.x <= s && x.y >= 0.f && x.y <= s && x.z >= 0.f && x.z <= s)) {
+        x.x = q.mp[0] / q.w;
+        x.y = q.mp[1] / q.w;
+        x.z = q.mp[2] / q.w;
+    }
+    out[0] = x.x;
+    out[1] = x.y;
+    out[2] = x.z;
+    return sqef_error(q, x.x, x.y, x.z);
+}
+
+struct SNode {
+    int collapsed = 0;
+    int anchor = 0;
+    int material = 0;
+    float pos[3] = {0.f, 0.f, 0.f};  // world
+    SQef q;
+};
+
+int simplify_chunk(Chunk& ch, float threshold) {
+    ch.simp_vertices.clear();
+    ch.simp_triangles.clear();
+    ch.simp_reps.clear();
+    ch.simp_vertex_count = 0;
+    const int V = (int)ch.node_codes.size();
+    if (ch.vpc == 0 || V == 0) return 0;
+    const Dims D(ch.vpc);
+    const int L = D.depth;
+    const float fs = (float)ch.scale;
+
+    // leaf QEFs from the same crossings the leaves were solved with
+    std::unordered_map<int32_t, int> edge_index;
+    for (size_t i = 0; i < ch.edge_keys.size(); i++) edge_index.emplace(ch.edge_keys[i], (int)i);
+    std::vector<SQef> leaf(V);
+    std::vector<std::array<int, 3>> vpos(V);
+    std::unordered_map<int, int> voxel_at;  // packed position -> voxel
+    auto pack = [](int x, int y, int z) { return x | (y << 8) | (z << 16); };
+    for (int v = 0; v < V; v++) {
+        int pos[3];
+        position_for_code(ch.node_codes[v], D.depth, pos);
+        vpos[v] = {pos[0], pos[1], pos[2]};
+        voxel_at[pack(pos[0], pos[1], pos[2])] = v;
+        sqef_zero(leaf[v]);
+        for (int i = 0; i < 12; i++) {
+            if (!((ch.node_edges[v] >> i) & 1)) continue;
+            const int e0 = kEdgeMap[i][0], e1 = kEdgeMap[i][1];
+            const int key = edge_key(D, pos[0] + kChildMinOffsets[e0][0], pos[1] + kChildMinOffsets[e0][1],
+                                     pos[2] + kChildMinOffsets[e0][2], i / 4);
+            auto it = edge_index.find(key);
+            if (it == edge_index.end()) continue;
+            const F4 e = ch.edge_info[it->second];
+            float p[3];
+            for (int a = 0; a < 3; a++) {
+                const float o0 = (float)kChildMinOffsets[e0][a], o1 = (float)kChildMinOffsets[e1][a];
+                p[a] = std::fmaf(o1 - o0, e.w, o0);
+            }
+            sqef_add_point(leaf[v], p[0], p[1], p[2], e.x, e.y, e.z);
+        }
+    }
+    auto is_seam = [&](int v) {
+        for (int a = 0; a < 3; a++)
+            if (vpos[v][a] == 0 || vpos[v][a] == D.vpc - 1) return true;
+        return false;
+    };
+
+    // levels 1..L
+    std::vector<std::map<int, SNode>> lv(L + 1);
+    for (int k = 1; k <= L; k++) {
+        std::map<int, SNode>& cur = lv[k];
+        for (int v = 0; v < V; v++) cur[pack(vpos[v][0] >> k, vpos[v][1] >> k, vpos[v][2] >> k)];
+        const int h = 1 << (k - 1);
+        for (auto& kv : cur) {
+            const int px = kv.first & 255, py = (kv.first >> 8) & 255, pz = kv.first >> 16;
+            SNode& n = kv.second;
+            bool blocked = false;
+            SQef q;
+            sqef_zero(q);
+            int mats[8];
+            int anchor = INT32_MAX;
+            for (int i = 0; i < 8; i++) {
+                const int cx = 2 * px + kChildMinOffsets[i][0], cy = 2 * py + kChildMinOffsets[i][1],
+                          cz = 2 * pz + kChildMinOffsets[i][2];
+                mats[i] = MATERIAL_NONE;
+                const SQef* cq = nullptr;
+                if (k == 1) {
+                    auto it = voxel_at.find(pack(cx, cy, cz));
+                    if (it == voxel_at.end()) continue;
+                    if (is_seam(it->second)) { blocked = true; continue; }
+                    cq = &leaf[it->second];
+                    mats[i] = ch.node_materials[it->second] >> 8;
+                    anchor = std::min(anchor, it->second);
+                } else {
+                    auto it = lv[k - 1].find(pack(cx, cy, cz));
+                    if (it == lv[k - 1].end()) continue;
+                    if (!it->second.collapsed) { blocked = true; continue; }
+                    cq = &it->second.q;
+                    mats[i] = it->second.material;
+                    anchor = std::min(anchor, it->second.anchor);
+                }
+                sqef_merge(q, *cq, (float)(kChildMinOffsets[i][0] * h), (float)(kChildMinOffsets[i][1] * h),
+                           (float)(kChildMinOffsets[i][2] * h));
+            }
+            if (blocked) continue;
+            float x[3];
+            const float err = sqef_solve(q, (float)(2 * h), x);
+            if (!(err <= threshold)) continue;
+            n.collapsed = 1;
+            n.anchor = anchor;
+            n.material = dominant_material(mats);
+            n.q = q;
+            const int org[3] = {px << k, py << k, pz << k};
+            for (int a = 0; a < 3; a++)
+                n.pos[a] = std::fmaf(fs * ((float)org[a] + x[a]), (float)LEAF_SIZE_SCALE, (float)ch.min[a]);
+        }
+    }
+
+    // representatives: the highest collapsed ancestor
+    std::vector<int> rep_level(V, 0), rep_anchor(V);
+    std::vector<const SNode*> rep_node(V, nullptr);
+    ch.simp_reps.resize(V);
+    for (int v = 0; v < V; v++) {
+        rep_anchor[v] = v;
+        for (int k = 1; k <= L; k++) {
+            const SNode& n = lv[k].at(pack(vpos[v][0] >> k, vpos[v][1] >> k, vpos[v][2] >> k));
+            if (!n.collapsed) break;
+            rep_level[v] = k;
+            rep_anchor[v] = n.anchor;
+            rep_node[v] = &n;
+        }
+        ch.simp_reps[v] = rep_anchor[v] | (rep_level[v] << 20);
+    }
+
+    // triangles over the leaf quads (GenerateMesh, octree.cl:385-442)
+    std::vector<int> tri_local;  // anchors, remapped below
+    auto solid = [&](int x, int y, int z) { return ch.materials[D.field_index(x, y, z)] != MATERIAL_AIR; };
+    for (int v = 0; v < V; v++) {
+        const int* pos = vpos[v].data();
+        for (int axis = 0; axis < 3; axis++) {
+            const int aa = pos[(axis + 1) % 3], bb = pos[(axis + 2) % 3];
+            if (aa == D.vpc - 1 || bb == D.vpc - 1) continue;
+            int idx[4];
+            idx[0] = v;
+            bool all = true;
+            for (int n = 1; n < 4; n++) {
+                auto it = voxel_at.find(pack(pos[0] + kEdgeNodeOffsets[axis][n][0], pos[1] + kEdgeNodeOffsets[axis][n][1],
+                                             pos[2] + kEdgeNodeOffsets[axis][n][2]));
+                if (it == voxel_at.end()) { all = false; break; }
+                idx[n] = it->second;
+            }
+            if (!all) continue;
+            const int edge = axis * 4 + 3;
+            const int corners = ch.node_materials[v] & 0xff;
+            const int m1 = (corners >> kEdgeMap[edge][0]) & 1, m2 = (corners >> kEdgeMap[edge][1]) & 1;
+            if (m1 == m2) continue;
+            int minlev = L + 1;
+            for (int n = 0; n < 4; n++) minlev = std::min(minlev, rep_level[idx[n]]);
+            if (minlev > 0) {
+                // the minimal edge: along `axis` through the edge's other two coordinates
+                const int len = 1 << minlev;
+                int p0[3] = {pos[0], pos[1], pos[2]};
+                p0[(axis + 1) % 3] += 1;
+                p0[(axis + 2) % 3] += 1;
+                const int s0 = pos[axis] & ~(len - 1);
+                auto sign_at = [&](int t) {
+                    int q[3] = {p0[0], p0[1], p0[2]};
+                    q[axis] = t;
+                    return solid(q[0], q[1], q[2]);
+                };
+                const bool first = sign_at(s0);
+                bool keep = first != sign_at(s0 + len);
+                for (int t = s0 + 1; keep && t <= pos[axis]; t++) keep = sign_at(t) == first;
+                if (!keep) continue;
+            }
+            static const int kWinding[2][6] = {{0, 1, 3, 0, 3, 2}, {0, 3, 1, 0, 2, 3}};
+            const int flip = m1 != 0 ? 1 : 0;
+            for (int t = 0; t < 2; t++) {
+                const int a0 = rep_anchor[idx[kWinding[flip][3 * t]]];
+                const int a1 = rep_anchor[idx[kWinding[flip][3 * t + 1]]];
+                const int a2 = rep_anchor[idx[kWinding[flip][3 * t + 2]]];
+                if (a0 == a1 || a1 == a2 || a0 == a2) continue;
+                tri_local.push_back(a0);
+                tri_local.push_back(a1);
+                tri_local.push_back(a2);
+            }
+        }
+    }
+
+    // vertices: one per representative, in the order of their anchors
+    std::vector<int> new_index(V, -1);
+    float col[3];
+    colour_for_min_leaf_size(ch.size / 256, col);
+    int nv = 0;
+    for (int v = 0; v < V; v++) {
+        if (rep_anchor[v] != v) continue;
+        new_index[v] = nv++;
+        float o[12];
+        if (rep_level[v] == 0) {
+            std::memcpy(o, &ch.vertices[(size_t)v * 12], sizeof(o));
+        } else {
+            const SNode& n = *rep_node[v];
+            o[0] = n.pos[0]; o[1] = n.pos[1]; o[2] = n.pos[2]; o[3] = 1.f;
+            o[4] = n.q.ns[0] / n.q.w; o[5] = n.q.ns[1] / n.q.w; o[6] = n.q.ns[2] / n.q.w; o[7] = 0.f;
+            o[8] = col[0]; o[9] = col[1]; o[10] = col[2]; o[11] = (float)n.material;
+        }
+        ch.simp_vertices.insert(ch.simp_vertices.end(), o, o + 12);
+    }
+    for (int a : tri_local) ch.simp_triangles.push_back(new_index[a]);
+    ch.simp_vertex_count = ch.simp_triangles.empty() ? 0 : nv;
+    return 0;
+}
+
 template <typename T>
 int copy_out(const std::vector<T>& v, void* out, int64_t cap) {
     const int64_t bytes = (int64_t)(v.size() * sizeof(T));
@@ -1211,6 +1540,12 @@ int orc_chunk_run(void* h, const orc_density* d, const orc_chunk_args* a) {
     return run_chunk(*static_cast<Chunk*>(h), *d, *a, g_lut);
 }
 
+int orc_chunk_simplify(void* h, float threshold) {
+    Chunk& c = *static_cast<Chunk*>(h);
+    if (threshold < 0.f) return -1;
+    return simplify_chunk(c, threshold);
+}
+
 int orc_chunk_count(void* hp, int what) {
     const Chunk& c = *static_cast<Chunk*>(hp);
     switch (what) {
@@ -1223,6 +1558,10 @@ int orc_chunk_count(void* hp, int what) {
         case ORC_PLAIN_EDGE_KEYS: return (int)c.plain_edge_keys.size();
         case ORC_MESH_VERTEX_COUNT: return c.mesh_vertex_count;
         case ORC_CREATED_EDGE_KEYS: return (int)c.created_keys.size();
+        case ORC_SIMP_VERTICES: return (int)c.simp_vertices.size() / 12;
+        case ORC_SIMP_TRIANGLES: return (int)c.simp_triangles.size() / 3;
+        case ORC_SIMP_VERTEX_COUNT: return c.simp_vertex_count;
+        case ORC_SIMP_REPS: return (int)c.simp_reps.size();
         default: return -1;
     }
 }
@@ -1242,6 +1581,9 @@ int orc_chunk_get(void* hp, int what, void* out, int64_t cap) {
         case ORC_PLAIN_EDGE_KEYS: return copy_out(c.plain_edge_keys, out, cap);
         case ORC_QEFS: return copy_out(c.qefs, out, cap);
         case ORC_CREATED_EDGE_KEYS: return copy_out(c.created_keys, out, cap);
+        case ORC_SIMP_VERTICES: return copy_out(c.simp_vertices, out, cap) < 0 ? -2 : (int)c.simp_vertices.size() / 12;
+        case ORC_SIMP_TRIANGLES: return copy_out(c.simp_triangles, out, cap) < 0 ? -2 : (int)c.simp_triangles.size() / 3;
+        case ORC_SIMP_REPS: return copy_out(c.simp_reps, out, cap);
         default: return -1;
     }
 }
@@ -1292,6 +1634,11 @@ int orc_aabb_overlaps(const int32_t amin[3], const int32_t amax[3], const int32_
 }
 
 int64_t orc_mesh_chunks(const orc_density* d, const orc_chunk_args* chunks, int32_t n, int32_t threads) {
+    return orc_mesh_chunks_simplified(d, chunks, n, threads, -1.f);
+}
+
+int64_t orc_mesh_chunks_simplified(const orc_density* d, const orc_chunk_args* chunks, int32_t n, int32_t threads,
+                                   float threshold) {
     if (!g_lut_ready || n <= 0) return -1;
     if (threads < 1) threads = 1;
     std::atomic<int> next{0};
@@ -1301,8 +1648,13 @@ int64_t orc_mesh_chunks(const orc_density* d, const orc_chunk_args* chunks, int3
         for (;;) {
             const int i = next.fetch_add(1);
             if (i >= n) break;
-            if (run_chunk(ch, *d, chunks[i], g_lut) == 0)
+            if (run_chunk(ch, *d, chunks[i], g_lut) != 0) continue;
+            if (threshold >= 0.f) {
+                simplify_chunk(ch, threshold);
+                total += (int64_t)ch.simp_vertex_count + (int64_t)ch.simp_triangles.size() / 3;
+            } else {
                 total += (int64_t)ch.mesh_vertex_count + (int64_t)ch.triangles.size() / 3;
+            }
         }
     };
     std::vector<std::thread> pool;

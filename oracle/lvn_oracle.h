@@ -68,7 +68,11 @@ enum {
     ORC_QEFS = 10,          /* QEFData[V] (64 B)                             */
     ORC_MESH_VERTEX_COUNT = 11, /* reported vertex count (0 when no tris)     */
     ORC_CREATED_EDGE_KEYS = 12, /* int32[]   CSG-created edge keys           */
-    ORC_NUM_WHAT = 13
+    ORC_SIMP_VERTICES = 13, /* MeshVertex[]  simplified mesh (orc_chunk_simplify) */
+    ORC_SIMP_TRIANGLES = 14,/* int32[3 * T'] simplified triangles            */
+    ORC_SIMP_VERTEX_COUNT = 15, /* reported simplified vertex count          */
+    ORC_SIMP_REPS = 16,     /* int32[V] representative anchor | level << 20  */
+    ORC_NUM_WHAT = 17
 };
 
 int   orc_set_seed(int32_t seed);
@@ -83,6 +87,9 @@ void  orc_chunk_free(void* h);
 int   orc_chunk_run(void* h, const orc_density* d, const orc_chunk_args* a);
 int   orc_chunk_count(void* h, int what);
 int   orc_chunk_get(void* h, int what, void* out, int64_t cap_bytes);
+/* bottom-up octree simplification of a chunk that orc_chunk_run meshed
+ * (threshold = QEF error bound in voxel^2; not in the reference) */
+int   orc_chunk_simplify(void* h, float threshold);
 
 /* cuckoo restatement (cuckoo.cl + compute_cuckoo.cpp), sequential insert */
 typedef struct orc_cuckoo orc_cuckoo;
@@ -103,6 +110,9 @@ int  orc_aabb_overlaps(const int32_t amin[3], const int32_t amax[3],
  * host threads; returns total vertices + triangles for sanity */
 int64_t orc_mesh_chunks(const orc_density* d, const orc_chunk_args* chunks, int32_t n,
                         int32_t threads);
+/* the same followed by orc_chunk_simplify(threshold) of each chunk (threshold < 0: none) */
+int64_t orc_mesh_chunks_simplified(const orc_density* d, const orc_chunk_args* chunks, int32_t n,
+                                   int32_t threads, float threshold);
 
 #ifdef __cplusplus
 }

@@ -15,7 +15,7 @@ REF_SO = ROOT / "oracle" / "_ref" / "libref.so"
 
 (ORC_MATERIALS, ORC_EDGE_KEYS, ORC_EDGE_INFO, ORC_NODE_CODES, ORC_NODE_EDGES, ORC_NODE_MATERIALS,
  ORC_VERTICES, ORC_TRIANGLES, ORC_SEAMS, ORC_PLAIN_EDGE_KEYS, ORC_QEFS, ORC_MESH_VERTEX_COUNT,
- ORC_CREATED_EDGE_KEYS) = range(13)
+ ORC_CREATED_EDGE_KEYS, ORC_SIMP_VERTICES, ORC_SIMP_TRIANGLES, ORC_SIMP_VERTEX_COUNT, ORC_SIMP_REPS) = range(17)
 
 
 class CsgOp(C.Structure):
@@ -63,6 +63,7 @@ def lib():
         L.orc_chunk_run.argtypes = [C.c_void_p, C.POINTER(Density), C.POINTER(ChunkArgs)]
         L.orc_chunk_count.argtypes = [C.c_void_p, C.c_int]
         L.orc_chunk_get.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int64]
+        L.orc_chunk_simplify.argtypes = [C.c_void_p, C.c_float]
         L.orc_cuckoo_build.argtypes = [C.c_void_p, C.c_int32, C.c_uint32, C.POINTER(C.c_int32)]
         L.orc_cuckoo_build.restype = C.c_void_p
         L.orc_cuckoo_find.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32)]
@@ -73,6 +74,9 @@ def lib():
         L.orc_aabb_overlaps.argtypes = [C.c_int32 * 3] * 4
         L.orc_mesh_chunks.argtypes = [C.POINTER(Density), C.POINTER(ChunkArgs), C.c_int32, C.c_int32]
         L.orc_mesh_chunks.restype = C.c_int64
+        L.orc_mesh_chunks_simplified.argtypes = [C.POINTER(Density), C.POINTER(ChunkArgs), C.c_int32, C.c_int32,
+                                                 C.c_float]
+        L.orc_mesh_chunks_simplified.restype = C.c_int64
         _lib = L
     return _lib
 
@@ -161,6 +165,25 @@ class OracleChunk:
 
     def mesh_vertex_count(self):
         return self.count(ORC_MESH_VERTEX_COUNT)
+
+    # bottom-up octree simplification
+    def simplify(self, threshold):
+        rc = lib().orc_chunk_simplify(self._h, threshold)
+        if rc != 0:
+            raise RuntimeError(f"orc_chunk_simplify failed: {rc}")
+        return self
+
+    def simp_vertices(self):
+        return self.get(ORC_SIMP_VERTICES, np.float32, 12)
+
+    def simp_triangles(self):
+        return self.get(ORC_SIMP_TRIANGLES, np.int32, 3)
+
+    def simp_reps(self):
+        return self.get(ORC_SIMP_REPS, np.int32)
+
+    def simp_vertex_count(self):
+        return self.count(ORC_SIMP_VERTEX_COUNT)
 
 
 def set_seed(seed):

@@ -115,6 +115,28 @@ def test_single_chunk(lvn_gpu, mode, vpc, crossing):
         g.close()
 
 
+@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("mn,size", [((-512, 0, 768), 256), ((-1024, -256, -2048), 1024)])
+def test_negative_coordinates(lvn_gpu, mode, mn, size):
+    """Chunks whose field starts at negative density-space coordinates (every
+    index computation is signed)."""
+    lvn = lvn_gpu
+    lvn.clear_csg_operations()
+    lvn.set_density(**density_args(mode))
+    g = lvn.MeshGen(64)
+    try:
+        g.set_option(lvn.LVN_OPT_CACHE, 0)
+        mesh = g.generate_chunk_mesh(mn, size)
+        O.set_seed(1)
+        ref = O.OracleChunk(oracle_density(mode), mn, size, vpc=64)
+        scale = size // 256
+        if ref.count(O.ORC_EDGE_KEYS):
+            compare_stages(lvn, g, 0, ref, 64, scale)
+        compare_mesh(mesh.vertices, mesh.triangles, mesh.seams, ref, scale)
+    finally:
+        g.close()
+
+
 def table_entries(table):
     t = table[table != np.uint64(0xFFFFFFFFFFFFFFFF)]
     return set(zip((t & np.uint64(0xFFFFFFFF)).astype(np.int64).tolist(), (t >> np.uint64(32)).astype(np.int64).tolist()))

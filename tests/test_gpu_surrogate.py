@@ -1,0 +1,153 @@
+"""The learned density surrogate's tensor-core kernels against a float64
+reference of the same network (torch on the CPU).
+
+Tolerances: the kernels keep weights and activations in BF16 (8-bit
+mantissa) and accumulate in FP32, so the forward value and the gradient agree
+with float64 to about 1% (relative L2 per parameter block), which these
+tests bound at 5%; the reference uses the BF16-rounded hidden weights the
+kernels use.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from leven_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+LO, HI = (-1024.0, -128.0, -1024.0), (1024.0, 128.0, 1024.0)
+IN = [96, 128, 128, 128]
+
+
+def unpack(p):
+    """Flat parameters -> [(W, b)] x 4 + (w4, b4), float64 tensors."""
+    out, o = [], 0
+    for k in IN:
+        w = torch.tensor(p[o:o + 128 * k], dtype=torch.float64).reshape(128, k)
+        o += 128 * k
+        b = torch.tensor(p[o:o + 128], dtype=torch.float64)
+        o += 128
+        out.append((w, b))
+    w4 = torch.tensor(p[o:o + 128], dtype=torch.float64)
+    b4 = torch.tensor(p[o + 128:o + 129], dtype=torch.float64)
+    return out, w4, b4
+
+
+def bf16(t):
+    return t.to(torch.bfloat16).to(torch.float64)
+
+
+def features(pts):
+    cols = []
+    for a in range(3):
+        ext = HI[a] - LO[a]
+        top = math.log2(max(2.0, ext / 2.0))
+        u = 2.0 * (torch.tensor(pts[:, a], dtype=torch.float64) - LO[a]) / ext - 1.0
+        f = torch.tensor([2.0 ** (top * k / 15) for k in range(16)], dtype=torch.float64)
+        ang = math.pi * u[:, None] * f[None, :]
+        cols += [torch.sin(ang), torch.cos(ang)]
+    return bf16(torch.cat(cols, dim=1))
+
+
+def reference(p, pts, targets=None, scale=8.0):
+    layers, w4, b4 = unpack(p)
+    params = [t.clone().requires_grad_(True) for wb in layers for t in wb] + [w4.clone().requires_grad_(True),
+                                                                           b4.clone().requires_grad_(True)]
+    x = features(pts)
+    for i in range(4):
+        w, b = params[2 * i], params[2 * i + 1]
+        w_eff = w + (bf16(w.detach()) - w.detach())  # the BF16 value, the gradient of w
+        x = torch.nn.functional.silu(x @ w_eff.T + b)
+    y = x @ params[8] + params[9]
+    if targets is None:
+        return (y * scale).detach().numpy()
+    loss = torch.mean((y - torch.tensor(targets, dtype=torch.float64) / scale) ** 2)
+    loss.backward()
+    g = np.concatenate([t.grad.numpy().ravel() for t in params])
+    return g, loss.item()
+
+
+@pytest.fixture
+def surrogate(lvn_gpu):
+    lvn = lvn_gpu
+    lvn.set_density(**W.FBM2D)
+    s = lvn.Surrogate(LO, HI, seed=3)
+    yield s
+    s.close()
+
+
+def blocks():
+    o = 0
+    for k in IN:
+        yield o, o + 128 * k
+        yield o + 128 * k, o + 128 * k + 128
+        o += 128 * k + 128
+    yield o, o + 128
+    yield o + 128, o + 129
+
+
+def test_forward_matches_float64(surrogate):
+    pts = surrogate.sample(1024, seed=5, fetch=True)
+    got = surrogate.eval(pts)
+    want = reference(surrogate.params(), pts)
+    err = np.abs(got - want)
+    assert np.linalg.norm(got - want) <= 0.05 * np.linalg.norm(want) + 1e-3, err.max()
+
+
+def test_gradient_matches_float64(surrogate):
+    pts = surrogate.sample(512, seed=7, fetch=True)
+    g, loss = surrogate.grad(pts)
+    rg, rloss = reference(surrogate.params(), pts, pts[:, 3])
+    assert abs(loss - rloss) <= 0.02 * rloss
+    for a, b in blocks():
+        num = np.linalg.norm(g[a:b] - rg[a:b])
+        assert num <= 0.05 * np.linalg.norm(rg[a:b]) + 1e-7, (a, b, num, np.linalg.norm(rg[a:b]))
+
+
+def test_training_reduces_loss(surrogate):
+    surrogate.sample(1 << 18, seed=11)
+    losses = surrogate.train(200, batch=8192, lr=1e-3)
+    assert np.isfinite(losses).all()
+    assert losses[-20:].mean() < 0.5 * losses[:5].mean(), (losses[:5], losses[-20:])
+    # the trained weights are the ones the kernels evaluate
+    pts = surrogate.sample(512, seed=13, fetch=True)
+    got = surrogate.eval(pts)
+    want = reference(surrogate.params(), pts)
+    assert np.linalg.norm(got - want) <= 0.05 * np.linalg.norm(want) + 1e-3
+
+
+def test_surrogate_meshing_gate(lvn_gpu, surrogate):
+    """Chunks take the surrogate's field only where its probe gate passes and
+    the chunk lies in its domain; a closed gate gives the plain meshes
+    exactly, an open one valid meshes from the surrogate's field."""
+    lvn = lvn_gpu
+    lvn.clear_csg_operations()
+    surrogate.sample(1 << 18, seed=17)
+    surrogate.train(300, batch=8192, lr=1e-3)
+    chunks = [((256 * i, 0, 256 * j), 256) for i in range(-2, 2) for j in range(-2, 2)] + [((8192, 0, 0), 256)]
+    g = lvn.MeshGen(64)
+    try:
+        V0, T0, S0, _ = g.generate_chunks(chunks)
+        g.set_surrogate(surrogate, gate=0.0)
+        V1, T1, S1, _ = g.generate_chunks(chunks)
+        assert g.surrogate_chunks(len(chunks)).sum() == 0
+        assert np.array_equal(V1.view(np.int32), V0.view(np.int32)) and np.array_equal(T1, T0)
+        g.set_surrogate(surrogate, gate=1e9)
+        V2, T2, S2, res = g.generate_chunks(chunks)
+        use = g.surrogate_chunks(len(chunks))
+        assert use[:-1].all() and not use[-1]  # the last chunk is outside the domain
+        assert np.isfinite(V2[:, :8]).all()
+        for r in res:
+            t = T2[r[2]:r[2] + r[3]]
+            if t.size:
+                assert t.min() >= 0 and t.max() < r[1]
+        assert T2.shape[0] > 0.5 * T0.shape[0]
+        # the fallback chunk is the plain one
+        r0 = res[-1]
+        g.set_surrogate(None)
+        V3, T3, S3, res3 = g.generate_chunks(chunks[-1:])
+        assert np.array_equal(T2[r0[2]:r0[2] + r0[3]], T3)
+    finally:
+        g.close()
