@@ -56,6 +56,7 @@ def parse():
                         "mesh the 1024-chunk clipmap set plain and with the surrogate")
     p.add_argument("--train-steps", type=int, default=20000)
     p.add_argument("--gate", type=float, default=0.5, help="surrogate probe gate (density units)")
+    p.add_argument("--mesh-chunks", type=int, default=0, help="surrogate run: mesh only the first N chunks (0 = all)")
     p.add_argument("--simplify", type=float, default=None,
                    help="octree simplification QEF-error threshold (voxel^2); default 0.05 for the clipmap "
                         "workload, off otherwise; < 0 = off")
@@ -546,6 +547,8 @@ def run_surrogate(args):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     chunks = W.clipmap_caves().chunks
+    if args.mesh_chunks:
+        chunks = chunks[:args.mesh_chunks]
     lvn.initialise(1, 0, 2)
     lvn.set_density(**W.FBM2D)
     lvn.clear_csg_operations()

@@ -67,35 +67,29 @@ struct Noise {
         const int kk2 = q >> 12;
         const float2* g2 = reinterpret_cast<const float2*>(g);
 
-        float n0 = 0.f, n1 = 0.f, n2 = 0.f;
-        float t0 = 0.5f - dot2(x0, y0, x0, y0);
-        if (!(t0 < 0.f)) {
-            const float2 gg = g2[2 * k0];
-            t0 = t0 * t0;
-            n0 = (t0 * t0) * dot2(gg.x, gg.y, x0, y0);
-        }
+        // A corner outside the kernel radius (t < 0) contributes 0.  Clamping
+        // t to 0 instead of branching gives 0 * dot = +-0 there, and a signed
+        // zero term leaves every sum below unchanged: the fractals accumulate
+        // with fma(s, amplitude, acc) and the ridged one takes |s| first.
+        const float2 ga = g2[2 * k0], gb = g2[2 * k1], gc = g2[2 * kk2];
+        float t0 = fmaxf(0.5f - dot2(x0, y0, x0, y0), 0.f);
+        t0 = t0 * t0;
+        const float n0 = (t0 * t0) * dot2(ga.x, ga.y, x0, y0);
         const float x1 = (x0 - (xgt ? 1.f : 0.f)) + G2, y1 = (y0 - (xgt ? 0.f : 1.f)) + G2;
-        float t1 = 0.5f - dot2(x1, y1, x1, y1);
-        if (!(t1 < 0.f)) {
-            const float2 gg = g2[2 * k1];
-            t1 = t1 * t1;
-            n1 = (t1 * t1) * dot2(gg.x, gg.y, x1, y1);
-        }
+        float t1 = fmaxf(0.5f - dot2(x1, y1, x1, y1), 0.f);
+        t1 = t1 * t1;
+        const float n1 = (t1 * t1) * dot2(gb.x, gb.y, x1, y1);
         const float x2 = x0 - C2, y2 = y0 - C2;
-        float t2 = 0.5f - dot2(x2, y2, x2, y2);
-        if (!(t2 < 0.f)) {
-            const float2 gg = g2[2 * kk2];
-            t2 = t2 * t2;
-            n2 = (t2 * t2) * dot2(gg.x, gg.y, x2, y2);
-        }
+        float t2 = fmaxf(0.5f - dot2(x2, y2, x2, y2), 0.f);
+        t2 = t2 * t2;
+        const float n2 = (t2 * t2) * dot2(gc.x, gc.y, x2, y2);
         return 70.f * ((n0 + n1) + n2);
     }
 
     __device__ __forceinline__ float corner3(int ix, int iy, int iz, float x, float y, float z) const {
         const int a = perm(texel(iy, ix));
         const int k = perm(texel(iz, alpha_column(a))) & 15;
-        float tt = 0.6f - dot3(x, y, z, x, y, z);
-        if (tt < 0.f) return 0.f;
+        float tt = fmaxf(0.6f - dot3(x, y, z, x, y, z), 0.f);  // clamped as in snoise2
         tt = tt * tt;
         return (tt * tt) * dot3(g[4 * k], g[4 * k + 1], g[4 * k + 2], x, y, z);
     }
