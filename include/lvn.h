@@ -224,7 +224,9 @@ int lvn_meshgen_set_simplify(lvn_meshgen* ctx, float threshold);
  * persistent grid at 2, 4, 8, 16 and 32 CTAs per SM, and keeps the fastest
  * shape of every stage for later batches with the same density mode,
  * crossing mode, simplification setting and power-of-two batch size.  The
- * chosen CTAs per SM, indexed by stage (0 = built-in default), go to
+ * hermite stage, which a batch runs beside the voxel / hash / quad stages, is
+ * then tuned again by the time of the whole batch.  The chosen CTAs per SM,
+ * indexed by stage (0 = built-in default), go to
  * grid_per_sm[0 .. lvn_meshgen_stage_times' count) when it is not NULL. */
 int lvn_meshgen_autotune(lvn_meshgen* ctx, const lvn_chunk_desc* chunks, int32_t num_chunks, int32_t* grid_per_sm);
 

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <array>
 #include <cmath>
 #include <cstdio>
@@ -328,10 +329,16 @@ struct lvn_meshgen {
     // export of pinned host outputs: a side stream and its events
     cudaStream_t side = nullptr;
     cudaEvent_t ev_leaf = nullptr, ev_side = nullptr;
+    // the fresh-batch DAG: hermite on `aux` beside the voxel, hash and quad
+    // stages, with a grid of dag_hermite_per_sm CTAs per SM (0 = its tuned shape)
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_herm = nullptr;
+    int dag_hermite_per_sm = 0;
 
     // autotuned persistent-grid shapes (CTAs per SM per stage), keyed by
     // density mode, crossing mode, simplification on/off and log2(batch size)
     std::map<std::array<int, 4>, std::array<int, ST_COUNT>> tunes;
+    std::map<std::array<int, 4>, int> dag_tunes;  // hermite's CTAs per SM inside the batch DAG
 
     // profiling
     cudaEvent_t ev[ST_COUNT + 1] = {};
@@ -560,18 +567,9 @@ int enqueue_field_stages(lvn_meshgen* m, const BatchPtrs& b, bool any_ops) {
     return LVN_OK;
 }
 
-// Caller arrays the export kernels write directly (pinned host memory).
-struct DirectOut {
-    void* dst[3];
-    int64_t cap[3];
-};
-
 // ConstructOctreeFromField + GenerateMeshFromOctree + GatherSeamNodesFromOctree,
-// then the octree simplification when it is on.  With `direct`, the vertices
-// are exported on a side stream as soon as the leaves are written, overlapping
-// the mesh stages (after the simplification when it is on), and the triangles
-// and seams after the last stage.
-int enqueue_octree_stages(lvn_meshgen* m, const BatchPtrs& b, const DirectOut* direct = nullptr) {
+// then the octree simplification when it is on, one stage at a time.
+int enqueue_octree_stages(lvn_meshgen* m, const BatchPtrs& b) {
     LVN_STAGE(ST_VOX_COUNT, launch_vox_count);
     LVN_STAGE(ST_VOX_PLAN, launch_vox_plan);
     LVN_STAGE(ST_VOX_SCATTER, launch_vox_scatter);
@@ -579,22 +577,100 @@ int enqueue_octree_stages(lvn_meshgen* m, const BatchPtrs& b, const DirectOut* d
     LVN_STAGE(ST_HASH_FILL, launch_hash_fill);
     LVN_STAGE(ST_EDGE_INSERT, launch_edge_insert);
     LVN_STAGE(ST_LEAF, launch_leaf);
-    if (direct && !b.simp_on) {
-        LVN_CK(cudaEventRecord(m->ev_leaf, m->stream));
-        LVN_CK(cudaStreamWaitEvent(m->side, m->ev_leaf, 0));
-        LVN_CK(launch_export(b, 0, direct->dst[0], direct->cap[0], m->side));
-        LVN_CK(cudaEventRecord(m->ev_side, m->side));
-    }
     LVN_STAGE(ST_NODE_INSERT, launch_node_insert);
     LVN_STAGE(ST_MESH_COUNT, launch_mesh_count);
     LVN_STAGE(ST_MESH_PLAN, launch_mesh_plan);
     LVN_STAGE(ST_MESH_SCATTER, launch_mesh_scatter);
     if (b.simp_on) LVN_STAGE(ST_SIMPLIFY, launch_simplify);
+    return LVN_OK;
+}
+
+// Caller arrays the export kernels write directly (pinned host memory).
+struct DirectOut {
+    void* dst[3];
+    int64_t cap[3];
+};
+
+// All three outputs, in order, on one stream.
+int enqueue_exports(lvn_meshgen* m, const BatchPtrs& b, const DirectOut* direct, cudaStream_t s) {
+    for (int which = 0; which < 3; which++) LVN_CK(launch_export(b, which, direct->dst[which], direct->cap[which], s));
+    return LVN_OK;
+}
+
+constexpr int kLeafSlices = 4;  // leaf / vertex-export pipeline depth for pinned host outputs
+
+// The fresh-batch DAG (one graph when captured):
+//   field, CSG, edges                                         (stream)
+//   -> hermite                                                 (aux)
+//   || voxels, primes, hash tables, quads, triangles           (stream)
+//      [pinned outputs: triangles exported on the side stream meanwhile]
+//   -> join -> leaves in slices [each slice's vertices exported on the side
+//      stream while the next is computed], seams, simplification
+// The chain beside hermite reads no hermite data (edge keys, not edge
+// information), so the FP32-bound hermite overlaps the latency-bound hash and
+// quad stages when its grid leaves room (the autotuner sizes it by the time of
+// the whole batch); the exports over C2C (about 190 GB/s) overlap the rest.
+int enqueue_fresh_dag(lvn_meshgen* m, const BatchPtrs& b, bool any_ops, const DirectOut* direct) {
+    cudaStream_t s0 = m->stream;
+    LVN_CK(launch_reset(b, s0));
+    LVN_CK(launch_field(b, s0));
+    if (any_ops) LVN_CK(launch_csg(b, s0));
+    LVN_CK(launch_edge_count(b, s0));
+    LVN_CK(launch_edge_plan(b, s0));
+    LVN_CK(launch_edge_scatter(b, s0));
+    LVN_CK(cudaEventRecord(m->ev_fork, s0));
+    LVN_CK(cudaStreamWaitEvent(m->aux, m->ev_fork, 0));
+    BatchPtrs bh = b;
+    if (m->dag_hermite_per_sm > 0) bh.grid_per_sm[ST_HERMITE] = m->dag_hermite_per_sm;
+    LVN_CK(launch_hermite(bh, m->aux));
+    LVN_CK(cudaEventRecord(m->ev_herm, m->aux));
+    LVN_CK(launch_vox_count(b, s0));
+    LVN_CK(launch_vox_plan(b, s0));
+    LVN_CK(launch_vox_scatter(b, s0));
+    LVN_CK(launch_primes(b, s0));
+    LVN_CK(launch_hash_fill(b, s0));
+    LVN_CK(launch_edge_insert(b, s0));
+    LVN_CK(launch_node_insert(b, s0));
+    LVN_CK(launch_mesh_count(b, s0));
+    LVN_CK(launch_mesh_plan(b, s0));
+    const bool simp = b.simp_on != 0;
+    const bool pipelined = direct && !simp;
+    if (!simp) {
+        BatchPtrs bt = b;
+        bt.scatter_what = 1;  // triangles now, seams once the leaves exist
+        LVN_CK(launch_mesh_scatter(bt, s0));
+        if (pipelined) {
+            LVN_CK(cudaEventRecord(m->ev_leaf, s0));
+            LVN_CK(cudaStreamWaitEvent(m->side, m->ev_leaf, 0));
+            LVN_CK(launch_export(b, 1, direct->dst[1], direct->cap[1], m->side));
+        }
+    }
+    LVN_CK(cudaStreamWaitEvent(s0, m->ev_herm, 0));
+    const int slices = pipelined ? kLeafSlices : 1;
+    for (int sl = 0; sl < slices; sl++) {
+        BatchPtrs bl = b;
+        bl.slice = sl;
+        bl.nslices = slices;
+        LVN_CK(launch_leaf(bl, s0));
+        if (pipelined) {
+            LVN_CK(cudaEventRecord(m->ev_leaf, s0));
+            LVN_CK(cudaStreamWaitEvent(m->side, m->ev_leaf, 0));
+            LVN_CK(launch_export(bl, 0, direct->dst[0], direct->cap[0], m->side));
+        }
+    }
+    BatchPtrs bs = b;
+    bs.scatter_what = simp ? 0 : 2;
+    LVN_CK(launch_mesh_scatter(bs, s0));
+    if (simp) LVN_CK(launch_simplify(b, s0));
     if (direct) {
-        if (b.simp_on) LVN_CK(launch_export(b, 0, direct->dst[0], direct->cap[0], m->stream));
-        LVN_CK(launch_export(b, 1, direct->dst[1], direct->cap[1], m->stream));
-        LVN_CK(launch_export(b, 2, direct->dst[2], direct->cap[2], m->stream));
-        if (!b.simp_on) LVN_CK(cudaStreamWaitEvent(m->stream, m->ev_side, 0));
+        if (simp) {
+            const int rc = enqueue_exports(m, b, direct, s0);
+            if (rc) return rc;
+        } else {
+            LVN_CK(launch_export(b, 2, direct->dst[2], direct->cap[2], s0));
+            LVN_CK(cudaEventRecord(m->ev_side, m->side));
+            LVN_CK(cudaStreamWaitEvent(s0, m->ev_side, 0));
+        }
     }
     return LVN_OK;
 }
@@ -789,6 +865,8 @@ int run_fresh_batch(lvn_meshgen* m, std::vector<ChunkDesc>& descs, const std::ve
     Capacity cap = default_capacity(m, n);
     cap.ecap = std::max(cap.ecap, m->ecap);
     cap.vcap = std::max(cap.vcap, m->vcap);
+    const auto dag = m->dag_tunes.find(tune_key(m, n));
+    m->dag_hermite_per_sm = dag != m->dag_tunes.end() ? dag->second : 0;
     for (int attempt = 0; attempt < kMaxHashRetries + 2; attempt++) {
         int rc = ensure_pools(m, n, cap);
         if (rc) return rc;
@@ -807,10 +885,20 @@ int run_fresh_batch(lvn_meshgen* m, std::vector<ChunkDesc>& descs, const std::ve
             rc = surrogate_prologue(m, descs, brushes.size(), b);
             if (rc) return rc;
         }
+        if (!m->aux) {
+            LVN_CK(cudaStreamCreateWithFlags(&m->aux, cudaStreamNonBlocking));
+            LVN_CK(cudaEventCreateWithFlags(&m->ev_fork, cudaEventDisableTiming));
+            LVN_CK(cudaEventCreateWithFlags(&m->ev_herm, cudaEventDisableTiming));
+        }
         auto enqueue_all = [&]() -> int {
             int r = enqueue_inputs(m, n, brushes.size());
-            if (!r) r = enqueue_field_stages(m, b, !brushes.empty());
-            if (!r) r = enqueue_octree_stages(m, b, direct);
+            if (m->profile) {  // one stage at a time, each timed
+                if (!r) r = enqueue_field_stages(m, b, !brushes.empty());
+                if (!r) r = enqueue_octree_stages(m, b);
+                if (!r && direct) r = enqueue_exports(m, b, direct, m->stream);
+            } else if (!r) {
+                r = enqueue_fresh_dag(m, b, !brushes.empty(), direct);
+            }
             if (!r) r = enqueue_state_readback(m, n);
             return r;
         };
@@ -838,6 +926,7 @@ int run_fresh_batch(lvn_meshgen* m, std::vector<ChunkDesc>& descs, const std::ve
             std::memcpy(&thr_bits, &m->simp_threshold, 4);
             key.push_back(thr_bits);
             for (int st = 0; st < ST_COUNT; st++) key.push_back((uintptr_t)b.grid_per_sm[st]);
+            key.push_back((uintptr_t)m->dag_hermite_per_sm);
             const uint32_t* dk = reinterpret_cast<const uint32_t*>(&g.density);
             for (size_t i = 0; i < sizeof(g.density) / 4; i++) key.push_back(dk[i]);
             if (!m->graph_exec || key != m->graph_key) {
@@ -1289,9 +1378,12 @@ void lvn_meshgen_destroy(lvn_meshgen* m) {
     for (int i = 0; i <= ST_COUNT; i++)
         if (m->ev[i]) cudaEventDestroy(m->ev[i]);
     if (m->graph_exec) cudaGraphExecDestroy(m->graph_exec);
+    if (m->ev_fork) cudaEventDestroy(m->ev_fork);
     if (m->ev_leaf) cudaEventDestroy(m->ev_leaf);
     if (m->ev_side) cudaEventDestroy(m->ev_side);
     if (m->side) cudaStreamDestroy(m->side);
+    if (m->ev_herm) cudaEventDestroy(m->ev_herm);
+    if (m->aux) cudaStreamDestroy(m->aux);
     if (m->own_stream) cudaStreamDestroy(m->stream);
     delete m;
 }
@@ -1381,8 +1473,34 @@ int lvn_meshgen_autotune(lvn_meshgen* m, const lvn_chunk_desc* chunks, int32_t n
         return rc;
     }
     m->tunes[key] = best;
-    if (grid_per_sm)
+    // hermite shares the GPU with the voxel / hash / quad chain in the batch
+    // DAG: its grid is chosen by the time of the whole batch graph
+    double best_total = 1e30;
+    int best_h = 0;
+    for (int cand : kCandidates) {
+        m->dag_tunes[key] = cand;
+        double t = 1e30;
+        for (int rep = 0; rep < 3 && rc == LVN_OK; rep++) {  // the first run captures the graph
+            const auto t0 = std::chrono::steady_clock::now();
+            rc = run_fresh_batch(m, descs, brushes, nullptr);
+            const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            if (rep > 0) t = std::min(t, dt);
+        }
+        if (rc) break;
+        if (t < best_total) {
+            best_total = t;
+            best_h = cand;
+        }
+    }
+    if (rc) {
+        m->dag_tunes.erase(key);
+        return rc;
+    }
+    m->dag_tunes[key] = best_h;
+    if (grid_per_sm) {
         for (int st = 0; st < ST_COUNT; st++) grid_per_sm[st] = best[st];
+        grid_per_sm[ST_HERMITE] = best_h;  // the shape used in batches
+    }
     return LVN_OK;
 }
 

@@ -1446,7 +1446,12 @@ template <int VPC>
 __global__ void __launch_bounds__(kThreads) k_leaf(BatchPtrs b) {
     if (b.bs->overflow) return;
     const int total = b.bs->total_nodes;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    int lo = 0, hi = total;
+    if (b.nslices > 1) {  // this launch's share of the leaves
+        lo = (int)((long long)total * b.slice / b.nslices);
+        hi = (int)((long long)total * (b.slice + 1) / b.nslices);
+    }
+    for (int i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += gridDim.x * blockDim.x) {
         const int c = b.node_chunk[i];
         const ChunkState& st = b.cs[c];
         const ChunkDesc& d = b.desc[c];
@@ -1687,7 +1692,7 @@ __global__ void __launch_bounds__(kNodeTile) k_mesh_scatter(BatchPtrs b) {
             int qp = st.quad_off + toff.x + (ex & 0xffff);
 #pragma unroll
             for (int a = 0; a < 3; a++) {
-                if (!(q[a].w & 1) || b.simp_on) continue;
+                if (!(q[a].w & 1) || b.simp_on || b.scatter_what == 2) continue;
                 const int idx[4] = {local, q[a].x, q[a].y, q[a].z};
                 const int* w = (q[a].w & 2) ? w1 : w0;
                 lvn_mesh_triangle* tri = b.triangles + 2 * (size_t)qp;
@@ -1699,7 +1704,7 @@ __global__ void __launch_bounds__(kNodeTile) k_mesh_scatter(BatchPtrs b) {
                 tri[1].indices[2] = idx[w[5]];
                 qp++;
             }
-            if (seam) {
+            if (seam && b.scatter_what != 1) {
                 const int sp = st.seam_off + toff.y + (ex >> 16);
                 const float4* v = reinterpret_cast<const float4*>((b.simp_on ? b.leaf_out : b.vertices) + i);
                 int4* dst = reinterpret_cast<int4*>(b.seams + sp);
@@ -2051,9 +2056,9 @@ __global__ void __launch_bounds__(kNodeTile) k_simp_tscatter(BatchPtrs b) {
 
 // ---------------------------------------------------------------------------
 // export: copy one output pool (vertices, triangles or seams) to the caller's
-// array, which may be pinned host memory reached over NVLink-C2C.  The element
-// count is read on the device; an array too small is not written and the
-// batch is flagged.
+// array, which may be pinned host memory reached over NVLink-C2C, in 16-byte
+// stores.  The element count is read on the device; an array too small is not
+// written and the batch is flagged.
 // ---------------------------------------------------------------------------
 
 __global__ void __launch_bounds__(256) k_export(BatchPtrs b, int which, void* dst, int64_t capacity) {
@@ -2069,28 +2074,34 @@ __global__ void __launch_bounds__(256) k_export(BatchPtrs b, int which, void* ds
         src = b.triangles;
         count = b.simp_on ? bs.total_simp_tris : 2 * (int64_t)bs.total_quads;
         elem = sizeof(lvn_mesh_triangle);
+    } else {
+        src = b.seams;
+        count = bs.total_seams;
+        elem = sizeof(lvn_seam_node);
     }
-    else { src = b.seams; count = bs.total_seams; elem = sizeof(lvn_seam_node); }
     if (count > capacity) {
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&b.bs->status, 1 << which);
         return;
     }
-    const int64_t nbytes = count * elem;
+    // this launch's share: slice `slice` of `nslices` equal element ranges
+    int64_t e0 = 0, e1 = count;
+    if (b.nslices > 1) {
+        e0 = count * b.slice / b.nslices;
+        e1 = count * (b.slice + 1) / b.nslices;
+    }
+    const int64_t b0 = e0 * elem, b1 = e1 * elem;  // byte range, a multiple of 4
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15) == 0) {
-        const int64_t n16 = nbytes >> 4;
+    const uint32_t* s1 = static_cast<const uint32_t*>(src);
+    uint32_t* d1 = static_cast<uint32_t*>(dst);
+    if (((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src) | (uintptr_t)b0) & 15) == 0) {
         const uint4* s4 = static_cast<const uint4*>(src);
         uint4* d4 = static_cast<uint4*>(dst);
-        for (int64_t i = t0; i < n16; i += stride) d4[i] = s4[i];
-        const int64_t done = n16 << 4;
-        const uint32_t* s1 = static_cast<const uint32_t*>(src);
-        uint32_t* d1 = static_cast<uint32_t*>(dst);
-        for (int64_t i = (done >> 2) + t0; i < (nbytes >> 2); i += stride) d1[i] = s1[i];
+        const int64_t q1 = b1 >> 4;
+        for (int64_t i = (b0 >> 4) + t0; i < q1; i += stride) d4[i] = s4[i];
+        for (int64_t i = ((q1 << 4) >> 2) + t0; i < (b1 >> 2); i += stride) d1[i] = s1[i];
     } else {
-        const uint32_t* s1 = static_cast<const uint32_t*>(src);
-        uint32_t* d1 = static_cast<uint32_t*>(dst);
-        for (int64_t i = t0; i < (nbytes >> 2); i += stride) d1[i] = s1[i];
+        for (int64_t i = (b0 >> 2) + t0; i < (b1 >> 2); i += stride) d1[i] = s1[i];
     }
 }
 
@@ -2252,7 +2263,7 @@ cudaError_t launch_mesh_plan(const BatchPtrs& b, cudaStream_t s) {
 }
 
 cudaError_t launch_export(const BatchPtrs& b, int which, void* dst, int64_t capacity, cudaStream_t s) {
-    k_export<<<b.num_sms * 4, 256, 0, s>>>(b, which, dst, capacity);
+    k_export<<<b.num_sms * 2, 256, 0, s>>>(b, which, dst, capacity);
     return cudaGetLastError();
 }
 

@@ -94,6 +94,12 @@ struct BatchPtrs {
     int* gate_ok;                // [n] 1 when every probe is within `gate`
     float gate;
 
+    // k_mesh_scatter writes triangles (scatter_what 1), seams (2) or both (0);
+    // k_leaf and the vertex export take slice `slice` of `nslices` equal leaf
+    // ranges (nslices <= 1: all of them)
+    int scatter_what;
+    int slice, nslices;
+
     // launch shapes chosen by the autotuner: CTAs per SM of each stage's
     // persistent grid (0 = the built-in default)
     int grid_per_sm[24];
@@ -176,9 +182,10 @@ cudaError_t launch_mesh_scatter(const BatchPtrs& b, cudaStream_t stream);
 constexpr int kProbes = 512;
 cudaError_t launch_probe(const BatchPtrs& b, cudaStream_t stream);
 cudaError_t launch_gate(const BatchPtrs& b, cudaStream_t stream);
+// copy one output pool (which: 0 vertices, 1 triangles, 2 seams) to the
+// caller's array; dst must be device-addressable (device or pinned host memory)
+cudaError_t launch_export(const BatchPtrs& b, int which, void* dst, int64_t capacity, cudaStream_t stream);
 // the whole simplification pass (level grids reset, levels, map, plan, scatter)
 cudaError_t launch_simplify(const BatchPtrs& b, cudaStream_t stream);
-// which: 0 vertices, 1 triangles, 2 seams; dst must be device-addressable
-cudaError_t launch_export(const BatchPtrs& b, int which, void* dst, int64_t capacity, cudaStream_t stream);
 
 }  // namespace lvn

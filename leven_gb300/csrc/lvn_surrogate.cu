@@ -39,14 +39,15 @@ constexpr uint32_t kWaitLimit = 1u << 20;  // mbarrier polls before a CTA gives 
 
 // parameter offsets in the flat FP32 vector: W0 b0 W1 b1 W2 b2 W3 b3 w4 b4
 constexpr int kIn_[kLayers] = {kIn, kHidden, kHidden, kHidden};
-constexpr int w_off(int l) { return l == 0 ? 0 : w_off(l - 1) + kHidden * kIn_[l - 1] + kHidden; }
-constexpr int b_off(int l) { return w_off(l) + kHidden * kIn_[l]; }
+__host__ __device__ constexpr int in_dim(int l) { return l == 0 ? kIn : kHidden; }
+__host__ __device__ constexpr int w_off(int l) { return l == 0 ? 0 : w_off(l - 1) + kHidden * in_dim(l - 1) + kHidden; }
+__host__ __device__ constexpr int b_off(int l) { return w_off(l) + kHidden * in_dim(l); }
 constexpr int kHeadW = w_off(kLayers);
 constexpr int kHeadB = kHeadW + kHidden;
 constexpr int kParams = kHeadB + 1;
 static_assert(kParams == 62081, "4 x 128 SiLU MLP on 96 features");
 // BF16 copies: W_l (out x in) and W_l^T (in x out) for l >= 1
-constexpr int wb_off(int l) { return l == 0 ? 0 : wb_off(l - 1) + kHidden * kIn_[l - 1]; }
+__host__ __device__ constexpr int wb_off(int l) { return l == 0 ? 0 : wb_off(l - 1) + kHidden * in_dim(l - 1); }
 constexpr int kWb = wb_off(kLayers);
 
 // ---------------------------------------------------------------------------
@@ -123,10 +124,22 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
     for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
-__device__ __forceinline__ float silu(float z) { return z / (1.f + __expf(-z)); }
+// 16-byte global -> shared copies that stay in flight together
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+__device__ __forceinline__ float silu(float z) { return __fdividef(z, 1.f + __expf(-z)); }
 __device__ __forceinline__ float silu_grad(float z) {
-    const float s = 1.f / (1.f + __expf(-z));
+    const float s = __fdividef(1.f, 1.f + __expf(-z));
     return s * (1.f + z * (1.f - s));
+}
+// sin(pi r), cos(pi r): r reduced to [-1, 1] exactly (an even number of half
+// turns removed), then the fast intrinsics on a small argument
+__device__ __forceinline__ void sincos_pi(float r, float& s, float& c) {
+    r -= 2.f * rintf(0.5f * r);
+    __sincosf(3.14159265358979f * r, &s, &c);
 }
 
 // ---------------------------------------------------------------------------
@@ -182,14 +195,13 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
         const uint32_t lboA = (kTile / 8) * 128, lboB = (N / 8) * 128;
         for (int i = threadIdx.x; i < kTile * cores; i += blockDim.x) {
             const int r = i % kTile, c = i / kTile;
-            const uint4 v = *reinterpret_cast<const uint4*>(g.A + (size_t)(m0 + r) * g.lda + k0 + 8 * c);
-            *reinterpret_cast<uint4*>(sA + c * lboA + r * 16) = v;
+            cp_async16(sA + c * lboA + r * 16, g.A + (size_t)(m0 + r) * g.lda + k0 + 8 * c);
         }
         for (int i = threadIdx.x; i < N * cores; i += blockDim.x) {
             const int r = i % N, c = i / N;
-            const uint4 v = *reinterpret_cast<const uint4*>(g.B + (size_t)r * g.ldb + k0 + 8 * c);
-            *reinterpret_cast<uint4*>(sB + c * lboB + r * 16) = v;
+            cp_async16(sB + c * lboB + r * 16, g.B + (size_t)r * g.ldb + k0 + 8 * c);
         }
+        cp_async_wait_all();
         fence_proxy_async();
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -201,12 +213,14 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
             umma_commit(&bar);
         }
         uint32_t polls = 0;
+        bool late = false;
         while (!mbar_try_wait(&bar, phase))
             if (++polls == kWaitLimit) {
-                ok = false;
+                late = true;
                 break;
             }
         phase ^= 1u;
+        ok = !__syncthreads_or(late);  // the whole CTA takes the same path
         tc_fence_after();
     }
     if (!ok) {
@@ -313,21 +327,6 @@ struct FeatureFreqs {
     float f[3][kFreqs];
 };
 
-// Positions of lattice points: point i of a batch is point (first + i) of the
-// concatenated lattices, lattice l = (origin xyz, step) of dim^3 points with x
-// fastest.  Writes float4 positions for k_features.
-__global__ void k_lattice_points(const float4* lattices, int64_t first, int n, int dim, float4* pts) {
-    const int64_t per = (int64_t)dim * dim * dim;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int64_t g = first + i;
-        const int64_t l = g / per;
-        const int r = (int)(g - l * per);
-        const int z = r / (dim * dim), y = (r / dim) % dim, x = r % dim;
-        const float4 o = lattices[l];
-        pts[i] = make_float4(o.x + o.w * (float)x, o.y + o.w * (float)y, o.z + o.w * (float)z, 0.f);
-    }
-}
-
 // Fourier features of a position normalised to [-1, 1] over the domain:
 // [sin(pi f u_x) x16, cos x16, then y, then z]
 __global__ void k_features(const float4* pts, int n, Domain dom, FeatureFreqs ff, __nv_bfloat16* X,
@@ -342,7 +341,7 @@ __global__ void k_features(const float4* pts, int n, Domain dom, FeatureFreqs ff
 #pragma unroll 4
             for (int k = 0; k < kFreqs; k++) {
                 float s, co;
-                sincospif(ff.f[a][k] * u, &s, &co);
+                sincos_pi(ff.f[a][k] * u, s, co);
                 const __nv_bfloat16 bs = __float2bfloat16_rn(s), bc = __float2bfloat16_rn(co);
                 row[a * 2 * kFreqs + k] = bs;
                 row[a * 2 * kFreqs + kFreqs + k] = bc;
@@ -470,6 +469,184 @@ __global__ void k_to_bf16(const float* p, int n, __nv_bfloat16* wb, __nv_bfloat1
 }
 
 // ---------------------------------------------------------------------------
+// Fused inference: the whole network on 128-point tiles in one CTA.  The four
+// hidden layers' BF16 weights stay in shared memory for the kernel's life.
+// Two warpgroups each own a tile stream, a 128-column TMEM accumulator and an
+// activation tile: a warpgroup computes its tile's features into the tile,
+// its elected thread issues the layer's MMAs and commits to its mbarrier, and
+// its epilogue turns the accumulator into the next layer's operand (bias,
+// SiLU, BF16) in place, or into the density after the last layer.  While one
+// warpgroup is in an epilogue the tensor core works on the other's layer.
+// ---------------------------------------------------------------------------
+
+constexpr int kWbBytes = 2 * kWb;                 // 120 KB of weights
+constexpr int kActBytes = kTile * kHidden * 2;    // 32 KB per activation tile
+constexpr int kInferSmem = kWbBytes + 2 * kActBytes + (kLayers * kHidden + kHidden + 1) * 4;
+
+struct InferArgs {
+    const float4* pts;       // points (x, y, z, -), or
+    const float4* lattices;  // when not null: lattices (x0, y0, z0, step) of dim^3 points, x fastest
+    int dim;
+    int64_t n;
+    const __nv_bfloat16* wb;
+    const float* params;
+    Domain dom;
+    FeatureFreqs ff;
+    float out_scale;
+    float* out;
+    int* status;
+};
+
+__device__ __forceinline__ void wg_sync(int wg) {  // named barrier of one warpgroup
+    asm volatile("bar.sync %0, 128;" ::"r"(1 + wg) : "memory");
+}
+// named barrier of one warpgroup that also ORs a predicate across it
+__device__ __forceinline__ bool wg_any(int wg, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n.reg .pred p, q;\nsetp.ne.u32 p, %1, 0;\nbar.red.or.pred q, %2, 128, p;\nselp.u32 %0, 1, 0, q;\n}"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(1 + wg)
+        : "memory");
+    return r != 0;
+}
+
+__global__ void __launch_bounds__(256, 1) k_mlp_infer(InferArgs a) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t bars[2];
+    __shared__ uint32_t tmem_base;
+    uint8_t* sW = smem;
+    uint8_t* sAct = smem + kWbBytes;
+    float* sBias = reinterpret_cast<float*>(sAct + 2 * kActBytes);  // [4][128] biases, w4[128], b4
+    const int warp = threadIdx.x >> 5;
+    const int wg = warp >> 2;
+    const int row = threadIdx.x & 127;  // tile row = TMEM lane
+    // weights: layer l is N = 128 rows (out) x K = in_l, K-major core matrices
+    constexpr uint32_t kLbo = (kTile / 8) * 128;  // 2048: 128 rows per K column of core matrices
+    for (int l = 0; l < kLayers; l++) {
+        const int in = in_dim(l), cores = in / 8;
+        uint8_t* dst = sW + 2 * wb_off(l);
+        for (int i = threadIdx.x; i < kHidden * cores; i += blockDim.x) {
+            const int r = i % kHidden, c = i / kHidden;
+            cp_async16(dst + c * kLbo + r * 16, a.wb + wb_off(l) + (size_t)r * in + 8 * c);
+        }
+    }
+    for (int i = threadIdx.x; i < kLayers * kHidden; i += blockDim.x)
+        sBias[i] = a.params[b_off(i / kHidden) + (i % kHidden)];
+    for (int i = threadIdx.x; i <= kHidden; i += blockDim.x) sBias[kLayers * kHidden + i] = a.params[kHeadW + i];
+    if (warp == 0) tmem_alloc(&tmem_base, 256);
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+    }
+    cp_async_wait_all();
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base + (uint32_t)(wg * kHidden);  // this warpgroup's columns
+    const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+    uint8_t* act = sAct + wg * kActBytes;
+    const uint32_t act_addr = smem_u32(act), w_addr = smem_u32(sW);
+    const float* w4 = sBias + kLayers * kHidden;
+    const float b4 = w4[kHidden];
+    constexpr uint32_t kIdesc = umma_idesc(kTile, kHidden);
+    uint32_t phase = 0;
+    bool ok = true;
+    const int64_t ntiles = (a.n + kTile - 1) / kTile;
+    const int64_t per = (int64_t)a.dim * a.dim * a.dim;
+    for (int64_t t = (int64_t)blockIdx.x * 2 + wg; t < ntiles && ok; t += (int64_t)gridDim.x * 2) {
+        const int64_t p = t * kTile + row;
+        float c[3] = {0.f, 0.f, 0.f};
+        if (p < a.n) {
+            if (a.lattices) {
+                const int64_t l = p / per;
+                const int r = (int)(p - l * per);
+                const float4 o = a.lattices[l];
+                c[0] = o.x + o.w * (float)(r % a.dim);
+                c[1] = o.y + o.w * (float)((r / a.dim) % a.dim);
+                c[2] = o.z + o.w * (float)(r / (a.dim * a.dim));
+            } else {
+                const float4 q = a.pts[p];
+                c[0] = q.x;
+                c[1] = q.y;
+                c[2] = q.z;
+            }
+        }
+        // features -> this row of the activation tile (12 core-matrix columns)
+#pragma unroll
+        for (int ax = 0; ax < 3; ax++) {
+            const float u = 2.f * (c[ax] - a.dom.lo[ax]) / (a.dom.hi[ax] - a.dom.lo[ax]) - 1.f;
+            __align__(16) __nv_bfloat16 sv[16], cv[16];
+#pragma unroll
+            for (int k = 0; k < kFreqs; k++) {
+                float s, co;
+                sincos_pi(a.ff.f[ax][k] * u, s, co);
+                sv[k] = __float2bfloat16_rn(s);
+                cv[k] = __float2bfloat16_rn(co);
+            }
+            const int c0 = ax * 4;  // 32 features = 4 core columns per axis
+            *reinterpret_cast<uint4*>(act + (c0 + 0) * kLbo + row * 16) = *reinterpret_cast<uint4*>(sv);
+            *reinterpret_cast<uint4*>(act + (c0 + 1) * kLbo + row * 16) = *reinterpret_cast<uint4*>(sv + 8);
+            *reinterpret_cast<uint4*>(act + (c0 + 2) * kLbo + row * 16) = *reinterpret_cast<uint4*>(cv);
+            *reinterpret_cast<uint4*>(act + (c0 + 3) * kLbo + row * 16) = *reinterpret_cast<uint4*>(cv + 8);
+        }
+        float y = b4;
+        for (int l = 0; l < kLayers && ok; l++) {
+            fence_proxy_async();
+            tc_fence_before();
+            wg_sync(wg);
+            tc_fence_after();
+            if (row == 0) {
+                const uint32_t wl = w_addr + 2 * wb_off(l);
+                for (int s = 0; s < in_dim(l) / 16; s++)
+                    umma_bf16(tmem, umma_desc(act_addr + 2 * s * kLbo, kLbo, 128),
+                              umma_desc(wl + 2 * s * kLbo, kLbo, 128), kIdesc, s > 0 ? 1u : 0u);
+                umma_commit(&bars[wg]);
+            }
+            uint32_t polls = 0;
+            bool late = false;
+            while (!mbar_try_wait(&bars[wg], phase))
+                if (++polls == kWaitLimit) {
+                    late = true;
+                    break;
+                }
+            phase ^= 1u;
+            ok = !wg_any(wg, late);  // the whole warpgroup takes the same path
+            tc_fence_after();
+            if (!ok) break;
+            const float* bias = sBias + l * kHidden;
+#pragma unroll 1
+            for (int cc = 0; cc < kHidden / 32; cc++) {
+                float v[32];
+                tmem_ld32(tmem + lane_base + (uint32_t)(cc * 32), v);
+                if (l < kLayers - 1) {
+                    __align__(16) __nv_bfloat16 h[32];
+#pragma unroll
+                    for (int j = 0; j < 32; j++) h[j] = __float2bfloat16_rn(silu(v[j] + bias[cc * 32 + j]));
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        *reinterpret_cast<uint4*>(act + (cc * 4 + q) * kLbo + row * 16) =
+                            *reinterpret_cast<uint4*>(h + 8 * q);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 32; j++) {
+                        // the head reads the BF16 activation, as in training
+                        const float x = __bfloat162float(__float2bfloat16_rn(silu(v[j] + bias[cc * 32 + j])));
+                        y = fmaf(x, w4[cc * 32 + j], y);
+                    }
+                }
+            }
+        }
+        if (ok && p < a.n) a.out[p] = y * a.out_scale;
+    }
+    if (!ok && (threadIdx.x & 127) == 0) atomicExch(a.status, 1);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem_base, 256);
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 
@@ -529,6 +706,34 @@ struct lvn_surrogate {
     int cap = 0;
     Buf pts, X[kLayers + 1], Xt[kLayers + 1], Z[kLayers], dZ[2], dZt[2], dens;
     Buf pool;  // training samples
+    int num_sms = 0;
+
+    // fused inference of n points (explicit `pts`, or `lattices` of dim^3) into out (device)
+    int infer(const float4* pts_d, const float4* lattices_d, int dim, int64_t n, float* out_d) {
+        static bool configured = false;
+        if (!configured) {
+            SG_CK(cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, kInferSmem));
+            configured = true;
+        }
+        InferArgs a;
+        std::memset(&a, 0, sizeof(a));
+        a.pts = pts_d;
+        a.lattices = lattices_d;
+        a.dim = dim;
+        a.n = n;
+        a.wb = wb.as<__nv_bfloat16>();
+        a.params = params.as<float>();
+        a.dom = dom;
+        a.ff = ff;
+        a.out_scale = out_scale;
+        a.out = out_d;
+        a.status = status.as<int>();
+        const int64_t tiles = (n + kTile - 1) / kTile;
+        const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(num_sms, (tiles + 1) / 2));
+        k_mlp_infer<<<grid, 256, kInferSmem, stream>>>(a);
+        SG_CK(cudaGetLastError());
+        return LVN_OK;
+    }
     int64_t pool_n = 0;
     int64_t pool_next = 0;
     int step = 0;
@@ -666,6 +871,9 @@ lvn_surrogate* lvn_surrogate_create(const float domain_min[3], const float domai
         delete s;
         return nullptr;
     }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, dev);
     bool ok = !s->params.ensure(4ull * kParams) && !s->grads.ensure(4ull * kParams) && !s->adam_m.ensure(4ull * kParams) &&
               !s->adam_v.ensure(4ull * kParams) && !s->wb.ensure(2ull * kWb) && !s->wt.ensure(2ull * kWb) &&
               !s->loss.ensure(4) && !s->status.ensure(4);
@@ -792,22 +1000,19 @@ int lvn_surrogate_train(lvn_surrogate* s, int32_t steps, int32_t batch, float lr
 
 int lvn_surrogate_eval(lvn_surrogate* s, const float* points, int64_t n, float* density, int32_t memory) {
     if (!s || !points || !density || n <= 0) return LVN_ERR_INVALID;
+    int rc;
+    if (memory == LVN_MEMORY_DEVICE) {
+        if ((rc = s->infer(reinterpret_cast<const float4*>(points), nullptr, 0, n, density))) return rc;
+        return check_status(s);
+    }
+    // host arrays: staged through the batch buffers, 2^20 points at a time
     const int64_t chunk = 1 << 20;
-    int rc = s->ensure_batch((int)std::min<int64_t>(chunk, (n + kTile - 1) / kTile * kTile));
-    if (rc) return rc;
-    const cudaMemcpyKind in = memory == LVN_MEMORY_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-    const cudaMemcpyKind out = memory == LVN_MEMORY_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if ((rc = s->ensure_batch((int)std::min<int64_t>(chunk, (n + kTile - 1) / kTile * kTile)))) return rc;
     for (int64_t first = 0; first < n; first += chunk) {
         const int m = (int)std::min<int64_t>(chunk, n - first);
-        const int padded = (m + kTile - 1) / kTile * kTile;
-        if (padded > m) SG_CK(cudaMemsetAsync(s->pts.as<float4>() + m, 0, sizeof(float4) * (padded - m), s->stream));
-        SG_CK(cudaMemcpyAsync(s->pts.p, points + 4 * first, sizeof(float4) * m, in, s->stream));
-        if ((rc = s->forward(padded, false))) return rc;
-        k_head<<<std::min(1184, (padded + 127) / 128), 128, 0, s->stream>>>(
-            s->X[kLayers].as<__nv_bfloat16>(), nullptr, nullptr, padded, s->params.as<float>(), s->out_scale,
-            s->dens.as<float>(), nullptr, nullptr, nullptr, nullptr);
-        SG_CK(cudaGetLastError());
-        SG_CK(cudaMemcpyAsync(density + first, s->dens.p, sizeof(float) * m, out, s->stream));
+        SG_CK(cudaMemcpyAsync(s->pts.p, points + 4 * first, sizeof(float4) * m, cudaMemcpyHostToDevice, s->stream));
+        if ((rc = s->infer(s->pts.as<float4>(), nullptr, 0, m, s->dens.as<float>()))) return rc;
+        SG_CK(cudaMemcpyAsync(density + first, s->dens.p, sizeof(float) * m, cudaMemcpyDeviceToHost, s->stream));
     }
     return check_status(s);
 }
@@ -816,23 +1021,8 @@ int lvn_surrogate_eval_lattices(lvn_surrogate* s, const float* lattices, int32_t
     if (!s || !lattices || !density || count < 0 || dim <= 0) return LVN_ERR_INVALID;
     const int64_t n = (int64_t)count * dim * dim * dim;
     if (n == 0) return LVN_OK;
-    const int64_t chunk = 1 << 20;
-    int rc = s->ensure_batch((int)std::min<int64_t>(chunk, (n + kTile - 1) / kTile * kTile));
+    const int rc = s->infer(nullptr, reinterpret_cast<const float4*>(lattices), dim, n, density);
     if (rc) return rc;
-    for (int64_t first = 0; first < n; first += chunk) {
-        const int m = (int)std::min<int64_t>(chunk, n - first);
-        const int padded = (m + kTile - 1) / kTile * kTile;
-        if (padded > m) SG_CK(cudaMemsetAsync(s->pts.as<float4>() + m, 0, sizeof(float4) * (padded - m), s->stream));
-        k_lattice_points<<<std::min(1184, (m + 255) / 256), 256, 0, s->stream>>>(
-            reinterpret_cast<const float4*>(lattices), first, m, dim, s->pts.as<float4>());
-        SG_CK(cudaGetLastError());
-        if ((rc = s->forward(padded, false))) return rc;
-        k_head<<<std::min(1184, (padded + 127) / 128), 128, 0, s->stream>>>(
-            s->X[kLayers].as<__nv_bfloat16>(), nullptr, nullptr, padded, s->params.as<float>(), s->out_scale,
-            s->dens.as<float>(), nullptr, nullptr, nullptr, nullptr);
-        SG_CK(cudaGetLastError());
-        SG_CK(cudaMemcpyAsync(density + first, s->dens.p, sizeof(float) * m, cudaMemcpyDeviceToDevice, s->stream));
-    }
     return check_status(s);
 }
 

@@ -151,3 +151,26 @@ def test_surrogate_meshing_gate(lvn_gpu, surrogate):
         assert np.array_equal(T2[r0[2]:r0[2] + r0[3]], T3)
     finally:
         g.close()
+
+
+def test_lattice_and_point_evaluation_agree(lvn_gpu, surrogate):
+    """The fused inference kernel gives the same densities for a lattice as
+    for the same positions passed explicitly."""
+    import ctypes as C
+
+    lvn = lvn_gpu
+    lat = np.array([[-100.0, -20.0, 37.0, 2.0], [500.0, 3.0, -900.0, 0.5]], np.float32)
+    dim = 9
+    d_lat = torch.tensor(lat, device="cuda")
+    d_out = torch.zeros(2 * dim ** 3, dtype=torch.float32, device="cuda")
+    rc = lvn.lib().lvn_surrogate_eval_lattices(surrogate._h, d_lat.data_ptr(), 2, dim, d_out.data_ptr())
+    assert rc == 0
+    torch.cuda.synchronize()
+    pts = []
+    for o in lat:
+        for k in range(dim):
+            for j in range(dim):
+                for i in range(dim):
+                    pts.append((o[0] + o[3] * i, o[1] + o[3] * j, o[2] + o[3] * k))
+    got = surrogate.eval(np.array(pts, np.float32))
+    assert np.array_equal(d_out.cpu().numpy().view(np.int32), got.view(np.int32))
