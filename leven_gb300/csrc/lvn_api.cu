@@ -1557,7 +1557,10 @@ int lvn_meshgen_generate_chunks(lvn_meshgen* m, const lvn_chunk_desc* chunks, in
     DirectOut direct;
     const bool use_direct = !dev && direct_addresses(out, &direct);
     if (use_direct && !m->side) {
-        LVN_CK(cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking));
+        // exports take free SM slots ahead of the compute kernels they overlap
+        int lo = 0, hi = 0;
+        LVN_CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        LVN_CK(cudaStreamCreateWithPriority(&m->side, cudaStreamNonBlocking, hi));
         LVN_CK(cudaEventCreateWithFlags(&m->ev_leaf, cudaEventDisableTiming));
         LVN_CK(cudaEventCreateWithFlags(&m->ev_side, cudaEventDisableTiming));
     }

@@ -526,7 +526,7 @@ __device__ __forceinline__ float dens_h(const Noise& nz, const DensityParams& dp
 template <int VPC, int MODE>
 __global__ void __launch_bounds__(96) k_field(BatchPtrs b) {
     using G = Geo<VPC>;
-    __shared__ float sg[64];
+    __shared__ __align__(16) float sg[64];
     __shared__ uint32_t words[3][G::FD];  // solid-bit word of each warp, per row y
     if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
     __syncthreads();
@@ -598,7 +598,7 @@ __global__ void __launch_bounds__(96) k_field(BatchPtrs b) {
 template <int VPC>
 __global__ void __launch_bounds__(128) k_field_caves(BatchPtrs b) {
     using G = Geo<VPC>;
-    __shared__ float sg[64];
+    __shared__ __align__(16) float sg[64];
     __shared__ float hs[G::FD];
     __shared__ uint32_t words[3][G::FD];
     if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
@@ -676,7 +676,7 @@ __global__ void __launch_bounds__(128) k_field_sdens(BatchPtrs b) {
 template <int VPC>
 __global__ void __launch_bounds__(kProbes) k_probe(BatchPtrs b) {
     using G = Geo<VPC>;
-    __shared__ float sg[64];
+    __shared__ __align__(16) float sg[64];
     if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
     __syncthreads();
     const int c = blockIdx.x, p = threadIdx.x;
@@ -1185,7 +1185,7 @@ __device__ __forceinline__ float4 hermite_sdens(const BatchPtrs& b, int slot, in
 
 template <int VPC, int MODE>
 __global__ void __launch_bounds__(kThreads) k_hermite(BatchPtrs b) {
-    __shared__ float sg[64];
+    __shared__ __align__(16) float sg[64];
     if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
     __syncthreads();
     if (b.bs->overflow) return;
@@ -2263,7 +2263,7 @@ cudaError_t launch_mesh_plan(const BatchPtrs& b, cudaStream_t s) {
 }
 
 cudaError_t launch_export(const BatchPtrs& b, int which, void* dst, int64_t capacity, cudaStream_t s) {
-    k_export<<<b.num_sms * 2, 256, 0, s>>>(b, which, dst, capacity);
+    k_export<<<b.num_sms, 256, 0, s>>>(b, which, dst, capacity);  // one CTA per SM saturates C2C
     return cudaGetLastError();
 }
 

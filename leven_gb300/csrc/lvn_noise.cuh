@@ -91,7 +91,8 @@ struct Noise {
         const int k = perm(texel(iz, alpha_column(a))) & 15;
         float tt = fmaxf(0.6f - dot3(x, y, z, x, y, z), 0.f);  // clamped as in snoise2
         tt = tt * tt;
-        return (tt * tt) * dot3(g[4 * k], g[4 * k + 1], g[4 * k + 2], x, y, z);
+        const float4 gk = reinterpret_cast<const float4*>(g)[k];  // one 16-byte shared load
+        return (tt * tt) * dot3(gk.x, gk.y, gk.z, x, y, z);
     }
 
     // snoise3 (simplex.cl:218-289) with simplex() ranking (simplex.cl:133-156)

@@ -307,7 +307,7 @@ __device__ __forceinline__ float unit(uint64_t h) { return (float)(h >> 40) * (1
 // target = the plain density.
 __global__ void k_samples(float4* out, int n, uint64_t seed, Domain dom, const uint8_t* perm, const uint16_t* perm_k4,
                           const float* grad, DensityParams dp) {
-    __shared__ float sg[64];
+    __shared__ __align__(16) float sg[64];
     if (threadIdx.x < 64) sg[threadIdx.x] = grad[threadIdx.x];
     __syncthreads();
     const Noise nz{perm, perm_k4, sg};
