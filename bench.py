@@ -571,7 +571,13 @@ def run_surrogate(args):
     mg.set_option(lvn.LVN_OPT_CACHE, 0)
     stream = torch.cuda.ExternalStream(mg.stream(), device=dev)
     Vp, Tp, Sp, resp = mg.generate_chunks(chunks)
-    cap_v, cap_t, cap_s = int(resp[:, 7].sum()) + 1024, 2 * Tp.shape[0] + 4096, Sp.shape[0] + 1024
+    mg.set_surrogate(sur, args.gate)  # the surrogate's meshes size the outputs too
+    Vs, Ts, Ss, ress = mg.generate_chunks(chunks)
+    use = mg.surrogate_chunks(n)
+    mg.set_surrogate(None)
+    cap_v = max(int(resp[:, 7].sum()), int(ress[:, 7].sum())) + 1024
+    cap_t = max(Tp.shape[0], Ts.shape[0]) + 4096
+    cap_s = max(Sp.shape[0], Ss.shape[0]) + 1024
     d_vert = torch.empty(cap_v * 12, dtype=torch.float32, device=dev)
     d_tri = torch.empty(cap_t * 3, dtype=torch.int32, device=dev)
     d_seam = torch.empty(cap_s * 12, dtype=torch.int32, device=dev)
@@ -599,8 +605,6 @@ def run_surrogate(args):
         ms_plain = timed(args.steps, args.warmup)
         mg.set_surrogate(sur, args.gate)
         ms_sur = timed(args.steps, args.warmup)
-    use = mg.surrogate_chunks(n)
-    Vs, Ts, Ss, ress = mg.generate_chunks(chunks)
     hd = []
     for c in np.flatnonzero(use):
         rp, rs = resp[c], ress[c]
@@ -608,9 +612,14 @@ def run_surrogate(args):
         h = hausdorff_voxels(Vp[rp[0]:rp[0] + rp[1], :3], Vs[rs[0]:rs[0] + rs[1], :3], voxel)
         if h is not None:
             hd.append(h)
-    # density error of the surrogate against the plain FP32 density on fresh samples
+    # density error of the surrogate against the plain FP32 density and against
+    # the FP64 density, on fresh samples
     pts = sur.sample(1 << 16, seed=99, fetch=True)
-    err = np.abs(sur.eval(pts) - pts[:, 3])
+    d_sur = sur.eval(pts)
+    d64 = lvn.density_f64(pts)
+    err = np.abs(d_sur - pts[:, 3])
+    err64 = np.abs(d_sur - d64)
+    err32_64 = np.abs(pts[:, 3] - d64)
     line = {
         "metric": "64^3 chunks meshed/sec on 1 GB300, plain vs learned density", "impl": "lvn-surrogate",
         "value": round(n / (ms_sur / 1e3), 2), "plain": round(n / (ms_plain / 1e3), 2), "unit": "chunks/s",
@@ -626,6 +635,9 @@ def run_surrogate(args):
                       "loss_first": float(losses[0]) if len(losses) else None,
                       "loss_last100": float(np.mean(losses[-100:])) if len(losses) else None,
                       "density_abs_err_mean": float(err.mean()), "density_abs_err_p99": float(np.quantile(err, 0.99)),
+                      "density_abs_err_vs_fp64_mean": float(err64.mean()),
+                      "density_abs_err_vs_fp64_p99": float(np.quantile(err64, 0.99)),
+                      "plain_fp32_abs_err_vs_fp64_max": float(err32_64.max()),
                       "hausdorff_voxels_mean": round(float(np.mean(hd)), 4) if hd else None,
                       "hausdorff_voxels_max": round(float(np.max(hd)), 4) if hd else None,
                       "chunks_within_0.05_mean_0.5_max": int(sum(h <= 0.5 for h in hd))},

@@ -308,6 +308,12 @@ int     lvn_surrogate_eval_lattices(lvn_surrogate* s, const float* lattices, int
 int     lvn_surrogate_domain(const lvn_surrogate* s, float domain_min[3], float domain_max[3]);
 void*   lvn_surrogate_get_stream(lvn_surrogate* s);
 
+/* the density set by lvn_set_density (2D fBm, or 2D fBm + caves) at n points
+ * (x, y, z, unused; host) in double precision with the exact simplex
+ * constants, into density[n] (host): the FP64 reference the FP32 density and
+ * the surrogate are measured against */
+int     lvn_density_f64(const float* points, int64_t n, double* density);
+
 /* Mesh with the surrogate: every fresh chunk of this context is probed at
  * 8 x 8 x 8 of its field points; when the surrogate lies inside the domain
  * for the whole chunk and within `gate` (density units) of the plain density

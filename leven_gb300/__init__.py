@@ -82,7 +82,7 @@ EXPORTS = [
     "lvn_surrogate_create", "lvn_surrogate_destroy", "lvn_surrogate_num_params", "lvn_surrogate_set_params",
     "lvn_surrogate_get_params", "lvn_surrogate_sample", "lvn_surrogate_train", "lvn_surrogate_grad",
     "lvn_surrogate_eval", "lvn_surrogate_eval_lattices", "lvn_surrogate_domain", "lvn_surrogate_get_stream",
-    "lvn_meshgen_set_surrogate", "lvn_meshgen_surrogate_chunks",
+    "lvn_meshgen_set_surrogate", "lvn_meshgen_surrogate_chunks", "lvn_density_f64",
 ]
 
 _lib = None
@@ -140,6 +140,7 @@ def lib():
     L.lvn_surrogate_domain.argtypes = [C.c_void_p, C.c_float * 3, C.c_float * 3]
     L.lvn_meshgen_set_surrogate.argtypes = [C.c_void_p, C.c_void_p, C.c_float]
     L.lvn_meshgen_surrogate_chunks.argtypes = [C.c_void_p, i32p, C.c_int32]
+    L.lvn_density_f64.argtypes = [C.c_void_p, C.c_int64, C.c_void_p]
     L.lvn_surrogate_get_stream.restype = C.c_void_p
     L.lvn_meshgen_debug_fetch.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int64]
     L.lvn_meshgen_debug_fetch.restype = C.c_int64
@@ -416,3 +417,12 @@ class Surrogate:
         _check(lib().lvn_surrogate_eval(self._h, pts.ctypes.data, pts.shape[0], out.ctypes.data, LVN_MEMORY_HOST),
                "lvn_surrogate_eval")
         return out
+
+
+def density_f64(points):
+    """The current density at points (N x 3+) in double precision (GPU)."""
+    pts = np.zeros((len(points), 4), np.float32)
+    pts[:, :3] = np.asarray(points, np.float32)[:, :3]
+    out = np.zeros(len(points), np.float64)
+    _check(lib().lvn_density_f64(pts.ctypes.data, pts.shape[0], out.ctypes.data), "lvn_density_f64")
+    return out

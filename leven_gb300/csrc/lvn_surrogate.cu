@@ -130,9 +130,17 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-__device__ __forceinline__ float silu(float z) { return __fdividef(z, 1.f + __expf(-z)); }
+// SiLU through sigmoid(z) = (1 + tanh(z / 2)) / 2: one special-function
+// instruction (tanh.approx, relative error about 2^-11, below BF16's 2^-8)
+__device__ __forceinline__ float tanh_approx(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float sigmoid(float z) { return fmaf(0.5f, tanh_approx(0.5f * z), 0.5f); }
+__device__ __forceinline__ float silu(float z) { return z * sigmoid(z); }
 __device__ __forceinline__ float silu_grad(float z) {
-    const float s = __fdividef(1.f, 1.f + __expf(-z));
+    const float s = sigmoid(z);
     return s * (1.f + z * (1.f - s));
 }
 // sin(pi r), cos(pi r): r reduced to [-1, 1] exactly (an even number of half
@@ -471,7 +479,7 @@ __global__ void k_to_bf16(const float* p, int n, __nv_bfloat16* wb, __nv_bfloat1
 // ---------------------------------------------------------------------------
 // Fused inference: the whole network on 128-point tiles in one CTA.  The four
 // hidden layers' BF16 weights stay in shared memory for the kernel's life.
-// Two warpgroups each own a tile stream, a 128-column TMEM accumulator and an
+// Three warpgroups each own a tile stream, a 128-column TMEM accumulator and an
 // activation tile: a warpgroup computes its tile's features into the tile,
 // its elected thread issues the layer's MMAs and commits to its mbarrier, and
 // its epilogue turns the accumulator into the next layer's operand (bias,
@@ -481,7 +489,9 @@ __global__ void k_to_bf16(const float* p, int n, __nv_bfloat16* wb, __nv_bfloat1
 
 constexpr int kWbBytes = 2 * kWb;                 // 120 KB of weights
 constexpr int kActBytes = kTile * kHidden * 2;    // 32 KB per activation tile
-constexpr int kInferSmem = kWbBytes + 2 * kActBytes + (kLayers * kHidden + kHidden + 1) * 4;
+constexpr int kInferWG = 3;                       // warpgroups (tile streams) per CTA
+constexpr int kInferSmem = kWbBytes + kInferWG * kActBytes + (kLayers * kHidden + kHidden + 1) * 4;
+static_assert(kInferSmem <= 227 * 1024, "one CTA per SM");
 
 struct InferArgs {
     const float4* pts;       // points (x, y, z, -), or
@@ -511,13 +521,13 @@ __device__ __forceinline__ bool wg_any(int wg, bool v) {
     return r != 0;
 }
 
-__global__ void __launch_bounds__(256, 1) k_mlp_infer(InferArgs a) {
+__global__ void __launch_bounds__(128 * kInferWG, 1) k_mlp_infer(InferArgs a) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ uint64_t bars[2];
+    __shared__ uint64_t bars[kInferWG];
     __shared__ uint32_t tmem_base;
     uint8_t* sW = smem;
     uint8_t* sAct = smem + kWbBytes;
-    float* sBias = reinterpret_cast<float*>(sAct + 2 * kActBytes);  // [4][128] biases, w4[128], b4
+    float* sBias = reinterpret_cast<float*>(sAct + kInferWG * kActBytes);  // [4][128] biases, w4[128], b4
     const int warp = threadIdx.x >> 5;
     const int wg = warp >> 2;
     const int row = threadIdx.x & 127;  // tile row = TMEM lane
@@ -534,11 +544,8 @@ __global__ void __launch_bounds__(256, 1) k_mlp_infer(InferArgs a) {
     for (int i = threadIdx.x; i < kLayers * kHidden; i += blockDim.x)
         sBias[i] = a.params[b_off(i / kHidden) + (i % kHidden)];
     for (int i = threadIdx.x; i <= kHidden; i += blockDim.x) sBias[kLayers * kHidden + i] = a.params[kHeadW + i];
-    if (warp == 0) tmem_alloc(&tmem_base, 256);
-    if (threadIdx.x == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
-    }
+    if (warp == 0) tmem_alloc(&tmem_base, 512);  // a power of two >= 128 per warpgroup
+    if (threadIdx.x < kInferWG) mbar_init(&bars[threadIdx.x], 1);
     cp_async_wait_all();
     fence_proxy_async();
     tc_fence_before();
@@ -555,7 +562,7 @@ __global__ void __launch_bounds__(256, 1) k_mlp_infer(InferArgs a) {
     bool ok = true;
     const int64_t ntiles = (a.n + kTile - 1) / kTile;
     const int64_t per = (int64_t)a.dim * a.dim * a.dim;
-    for (int64_t t = (int64_t)blockIdx.x * 2 + wg; t < ntiles && ok; t += (int64_t)gridDim.x * 2) {
+    for (int64_t t = (int64_t)blockIdx.x * kInferWG + wg; t < ntiles && ok; t += (int64_t)gridDim.x * kInferWG) {
         const int64_t p = t * kTile + row;
         float c[3] = {0.f, 0.f, 0.f};
         if (p < a.n) {
@@ -643,7 +650,89 @@ __global__ void __launch_bounds__(256, 1) k_mlp_infer(InferArgs a) {
     if (!ok && (threadIdx.x & 127) == 0) atomicExch(a.status, 1);
     tc_fence_before();
     __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem_base, 256);
+    if (warp == 0) tmem_dealloc(tmem_base, 512);
+}
+
+// ---------------------------------------------------------------------------
+// FP64 density: the 2D fBm heightfield (+ 3D fBm caves) in double precision,
+// with the exact simplex constants, over the same permutation image and
+// gradient table, as the reference the surrogate's and the FP32 density's
+// errors are measured against.
+// ---------------------------------------------------------------------------
+
+__device__ double snoise2_f64(const uint8_t* perm, const float* grad, double px, double py) {
+    const double F2 = 0.36602540378443864676, G2 = 0.21132486540518711775;
+    const double s = (px + py) * F2;
+    const double fi = floor(px + s), fj = floor(py + s);
+    const double t = (fi + fj) * G2;
+    const double x0 = px - (fi - t), y0 = py - (fj - t);
+    const int i = (int)fi, j = (int)fj;
+    const int i1 = x0 > y0 ? 1 : 0, j1 = 1 - i1;
+    const double xs[3] = {x0, x0 - i1 + G2, x0 - 1.0 + 2.0 * G2};
+    const double ys[3] = {y0, y0 - j1 + G2, y0 - 1.0 + 2.0 * G2};
+    const int oi[3] = {0, i1, 1}, oj[3] = {0, j1, 1};
+    double n = 0.0;
+    for (int c = 0; c < 3; c++) {
+        double tt = 0.5 - xs[c] * xs[c] - ys[c] * ys[c];
+        if (tt <= 0.0) continue;
+        const int k = perm[texel(j + oj[c], i + oi[c])] & 15;
+        tt *= tt;
+        n += tt * tt * ((double)grad[4 * k] * xs[c] + (double)grad[4 * k + 1] * ys[c]);
+    }
+    return 70.0 * n;
+}
+
+__device__ double snoise3_f64(const uint8_t* perm, const float* grad, double px, double py, double pz) {
+    const double F3 = 1.0 / 3.0, G3 = 1.0 / 6.0;
+    const double s = (px + py + pz) * F3;
+    const double fi = floor(px + s), fj = floor(py + s), fk = floor(pz + s);
+    const double t = (fi + fj + fk) * G3;
+    const double x0 = px - (fi - t), y0 = py - (fj - t), z0 = pz - (fk - t);
+    const int i = (int)fi, j = (int)fj, k = (int)fk;
+    // the reference's ranking (simplex.cl:133-156)
+    const int sxy = x0 >= y0, sxz = x0 >= z0, syz = y0 >= z0;
+    const int rx = sxy + sxz, ry = (1 - sxy) + syz, rz = (1 - sxz) + (1 - syz);
+    const int o2[3] = {rx >= 1, ry >= 1, rz >= 1}, o1[3] = {rx >= 2, ry >= 2, rz >= 2};
+    const int oi[4] = {0, o1[0], o2[0], 1}, oj[4] = {0, o1[1], o2[1], 1}, ok[4] = {0, o1[2], o2[2], 1};
+    double n = 0.0;
+    for (int c = 0; c < 4; c++) {
+        const double x = x0 - oi[c] + c * G3, y = y0 - oj[c] + c * G3, z = z0 - ok[c] + c * G3;
+        double tt = 0.6 - x * x - y * y - z * z;
+        if (tt <= 0.0) continue;
+        const int a = perm[texel(j + oj[c], i + oi[c])];
+        const int g = perm[texel(k + ok[c], alpha_column(a))] & 15;
+        tt *= tt;
+        n += tt * tt * ((double)grad[4 * g] * x + (double)grad[4 * g + 1] * y + (double)grad[4 * g + 2] * z);
+    }
+    return 32.0 * n;
+}
+
+__global__ void k_density_f64(const float4* pts, int64_t n, const uint8_t* perm, const float* grad, DensityParams d,
+                              double* out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 p = pts[i];
+        double fx = p.x * (double)d.freq2, fz = p.z * (double)d.freq2, amp = 1.0, h = 0.0;
+        for (int o = 0; o < d.octaves2; o++) {
+            h += snoise2_f64(perm, grad, fx, fz) * amp;
+            fx *= d.lacunarity2;
+            fz *= d.lacunarity2;
+            amp *= d.gain2;
+        }
+        double v = (double)p.y - (double)d.amp2 * h;
+        if (d.mode == LVN_DENSITY_CAVES) {
+            double gx = p.x * (double)d.freq3, gy = p.y * (double)d.freq3, gz = p.z * (double)d.freq3, a3 = 1.0,
+                   c = 0.0;
+            for (int o = 0; o < d.octaves3; o++) {
+                c += snoise3_f64(perm, grad, gx, gy, gz) * a3;
+                gx *= d.lacunarity3;
+                gy *= d.lacunarity3;
+                gz *= d.lacunarity3;
+                a3 *= d.gain3;
+            }
+            v += (double)d.amp3 * c;
+        }
+        out[i] = v;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -729,8 +818,8 @@ struct lvn_surrogate {
         a.out = out_d;
         a.status = status.as<int>();
         const int64_t tiles = (n + kTile - 1) / kTile;
-        const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(num_sms, (tiles + 1) / 2));
-        k_mlp_infer<<<grid, 256, kInferSmem, stream>>>(a);
+        const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(num_sms, (tiles + kInferWG - 1) / kInferWG));
+        k_mlp_infer<<<grid, 128 * kInferWG, kInferSmem, stream>>>(a);
         SG_CK(cudaGetLastError());
         return LVN_OK;
     }
@@ -1036,5 +1125,25 @@ int lvn_surrogate_domain(const lvn_surrogate* s, float domain_min[3], float doma
 }
 
 void* lvn_surrogate_get_stream(lvn_surrogate* s) { return s ? (void*)s->stream : nullptr; }
+
+int lvn_density_f64(const float* points, int64_t n, double* density) {
+    if (!points || !density || n <= 0) return LVN_ERR_INVALID;
+    const GlobalView gv = global_view();
+    if (!gv.initialised) return LVN_ERR_NOT_INITIALISED;
+    if (gv.density.mode != LVN_DENSITY_FBM2D && gv.density.mode != LVN_DENSITY_CAVES) return LVN_ERR_INVALID;
+    Buf p, o;
+    int rc;
+    if ((rc = p.ensure(sizeof(float4) * (size_t)n)) || (rc = o.ensure(sizeof(double) * (size_t)n))) {
+        p.release();
+        return rc;
+    }
+    cudaMemcpy(p.p, points, sizeof(float4) * (size_t)n, cudaMemcpyHostToDevice);
+    k_density_f64<<<gv.num_sms * 4, 256>>>(p.as<float4>(), n, gv.perm, gv.grad, gv.density, o.as<double>());
+    const cudaError_t e = cudaGetLastError();
+    const cudaError_t c = cudaMemcpy(density, o.p, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost);
+    p.release();
+    o.release();
+    return e == cudaSuccess && c == cudaSuccess ? LVN_OK : LVN_ERR_CUDA;
+}
 
 }  // extern "C"

@@ -174,3 +174,23 @@ def test_lattice_and_point_evaluation_agree(lvn_gpu, surrogate):
                     pts.append((o[0] + o[3] * i, o[1] + o[3] * j, o[2] + o[3] * k))
     got = surrogate.eval(np.array(pts, np.float32))
     assert np.array_equal(d_out.cpu().numpy().view(np.int32), got.view(np.int32))
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_density_f64_reference(lvn_gpu, mode):
+    """The FP64 density agrees with the FP32 restatement of the same density
+    (the oracle's) to float rounding: |d32 - d64| <= 1e-4 (1 + |d|)."""
+    import ctypes
+
+    import oracle_lib as O
+
+    lvn = lvn_gpu
+    dens = W.FBM2D if mode == 1 else W.CAVES
+    lvn.set_density(**dens)
+    rng = np.random.default_rng(3)
+    pts = np.stack([rng.uniform(-2000, 2000, 4096), rng.uniform(-100, 100, 4096), rng.uniform(-2000, 2000, 4096)], 1)
+    d64 = lvn.density_f64(pts)
+    O.set_seed(1)
+    od = O.density(mode=mode)
+    d32 = np.array([O.lib().orc_density_at(ctypes.byref(od), *map(float, p)) for p in pts[:256]])
+    assert np.abs(d32 - d64[:256]).max() <= 1e-4 * (1 + np.abs(d64[:256]).max())
