@@ -299,7 +299,7 @@ struct lvn_meshgen {
     std::vector<int32_t> last_suse;
 
     // pools
-    DevBuf desc, cs, bs, brushes, mats, planes, edge_tiles, vox_tiles;
+    DevBuf desc, cs, bs, brushes, mats, planes, edge_tiles, vox_tiles, hmap;
     DevBuf edge_keys, edge_chunk, edge_info, edge_work, node_codes, node_info, node_chunk;
     DevBuf edge_slots, node_slots, quad_scratch, node_tile_counts, chunk_tile_off;
     DevBuf vertices, triangles, seams;
@@ -331,8 +331,8 @@ struct lvn_meshgen {
     cudaEvent_t ev_leaf = nullptr, ev_side = nullptr;
     // the fresh-batch DAG: hermite on `aux` beside the voxel, hash and quad
     // stages, with a grid of dag_hermite_per_sm CTAs per SM (0 = its tuned shape)
-    cudaStream_t aux = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_herm = nullptr;
+    cudaStream_t aux = nullptr, aux2 = nullptr;  // hermite; the quad chain
+    cudaEvent_t ev_fork = nullptr, ev_herm = nullptr, ev_hash = nullptr, ev_mesh = nullptr;
     int dag_hermite_per_sm = 0;
 
     // autotuned persistent-grid shapes (CTAs per SM per stage), keyed by
@@ -380,6 +380,7 @@ int ensure_pools(lvn_meshgen* m, int n, Capacity want) {
     LVN_CK(m->bs.ensure(sizeof(BatchState)));
     LVN_CK(m->mats.ensure((size_t)F * n));
     LVN_CK(m->planes.ensure(sizeof(uint4) * 3 * (size_t)field_rows(m->vpc) * n));
+    LVN_CK(m->hmap.ensure(sizeof(float) * (size_t)field_rows(m->vpc) * n));
     LVN_CK(m->edge_tiles.ensure(sizeof(int4) * (size_t)edge_tiles_per_chunk(m->vpc) * n));
     LVN_CK(m->vox_tiles.ensure(sizeof(int) * (size_t)vox_tiles_per_chunk(m->vpc) * n));
     LVN_CK(m->chunk_tile_off.ensure(sizeof(int) * (size_t)(n + 1)));
@@ -489,6 +490,7 @@ BatchPtrs make_ptrs(lvn_meshgen* m, int n) {
     b.grad = g.grad.as<float>();
     b.mats = m->mats.as<uint8_t>();
     b.planes = m->planes.as<uint4>();
+    b.hmap = m->hmap.as<float>();
     b.edge_tiles = m->edge_tiles.as<int4>();
     b.vox_tiles = m->vox_tiles.as<int>();
     b.edge_keys = m->edge_keys.as<int32_t>();
@@ -600,16 +602,21 @@ int enqueue_exports(lvn_meshgen* m, const BatchPtrs& b, const DirectOut* direct,
 constexpr int kLeafSlices = 4;  // leaf / vertex-export pipeline depth for pinned host outputs
 
 // The fresh-batch DAG (one graph when captured):
-//   field, CSG, edges                                         (stream)
-//   -> hermite                                                 (aux)
-//   || voxels, primes, hash tables, quads, triangles           (stream)
-//      [pinned outputs: triangles exported on the side stream meanwhile]
-//   -> join -> leaves in slices [each slice's vertices exported on the side
-//      stream while the next is computed], seams, simplification
-// The chain beside hermite reads no hermite data (edge keys, not edge
-// information), so the FP32-bound hermite overlaps the latency-bound hash and
-// quad stages when its grid leaves room (the autotuner sizes it by the time of
-// the whole batch); the exports over C2C (about 190 GB/s) overlap the rest.
+//   field, CSG, edges                                           (stream)
+//   -> hermite                                                   (aux)
+//   || voxels, primes, hash-table fill                           (stream)
+//      -> leaf-hash insert, quads, triangles                     (aux2)
+//         [pinned outputs: triangles exported on aux2]
+//      || edge-hash insert, join hermite, leaves in slices       (stream)
+//         [pinned outputs: each slice's vertices exported on the side
+//          stream while the next is computed]
+//   -> join -> seams, simplification, exports' join              (stream)
+// No branch reads what another writes before their join: the chain beside
+// hermite reads edge keys, not edge information; the quad chain reads leaf
+// codes and corners, not leaf vertices.  The FP32-bound hermite overlaps the
+// latency-bound hash stages (its grid is sized by the autotuner for this), the
+// leaves overlap the quad stages, and the exports over C2C (about 190 GB/s)
+// start as soon as their data exists.
 int enqueue_fresh_dag(lvn_meshgen* m, const BatchPtrs& b, bool any_ops, const DirectOut* direct) {
     cudaStream_t s0 = m->stream;
     LVN_CK(launch_reset(b, s0));
@@ -629,22 +636,23 @@ int enqueue_fresh_dag(lvn_meshgen* m, const BatchPtrs& b, bool any_ops, const Di
     LVN_CK(launch_vox_scatter(b, s0));
     LVN_CK(launch_primes(b, s0));
     LVN_CK(launch_hash_fill(b, s0));
-    LVN_CK(launch_edge_insert(b, s0));
-    LVN_CK(launch_node_insert(b, s0));
-    LVN_CK(launch_mesh_count(b, s0));
-    LVN_CK(launch_mesh_plan(b, s0));
     const bool simp = b.simp_on != 0;
     const bool pipelined = direct && !simp;
+    // the quad chain
+    LVN_CK(cudaEventRecord(m->ev_hash, s0));
+    LVN_CK(cudaStreamWaitEvent(m->aux2, m->ev_hash, 0));
+    LVN_CK(launch_node_insert(b, m->aux2));
+    LVN_CK(launch_mesh_count(b, m->aux2));
+    LVN_CK(launch_mesh_plan(b, m->aux2));
     if (!simp) {
         BatchPtrs bt = b;
         bt.scatter_what = 1;  // triangles now, seams once the leaves exist
-        LVN_CK(launch_mesh_scatter(bt, s0));
-        if (pipelined) {
-            LVN_CK(cudaEventRecord(m->ev_leaf, s0));
-            LVN_CK(cudaStreamWaitEvent(m->side, m->ev_leaf, 0));
-            LVN_CK(launch_export(b, 1, direct->dst[1], direct->cap[1], m->side));
-        }
+        LVN_CK(launch_mesh_scatter(bt, m->aux2));
+        if (pipelined) LVN_CK(launch_export(b, 1, direct->dst[1], direct->cap[1], m->aux2));
     }
+    LVN_CK(cudaEventRecord(m->ev_mesh, m->aux2));
+    // the leaves
+    LVN_CK(launch_edge_insert(b, s0));
     LVN_CK(cudaStreamWaitEvent(s0, m->ev_herm, 0));
     const int slices = pipelined ? kLeafSlices : 1;
     for (int sl = 0; sl < slices; sl++) {
@@ -658,6 +666,7 @@ int enqueue_fresh_dag(lvn_meshgen* m, const BatchPtrs& b, bool any_ops, const Di
             LVN_CK(launch_export(bl, 0, direct->dst[0], direct->cap[0], m->side));
         }
     }
+    LVN_CK(cudaStreamWaitEvent(s0, m->ev_mesh, 0));
     BatchPtrs bs = b;
     bs.scatter_what = simp ? 0 : 2;
     LVN_CK(launch_mesh_scatter(bs, s0));
@@ -887,8 +896,11 @@ int run_fresh_batch(lvn_meshgen* m, std::vector<ChunkDesc>& descs, const std::ve
         }
         if (!m->aux) {
             LVN_CK(cudaStreamCreateWithFlags(&m->aux, cudaStreamNonBlocking));
+            LVN_CK(cudaStreamCreateWithFlags(&m->aux2, cudaStreamNonBlocking));
             LVN_CK(cudaEventCreateWithFlags(&m->ev_fork, cudaEventDisableTiming));
             LVN_CK(cudaEventCreateWithFlags(&m->ev_herm, cudaEventDisableTiming));
+            LVN_CK(cudaEventCreateWithFlags(&m->ev_hash, cudaEventDisableTiming));
+            LVN_CK(cudaEventCreateWithFlags(&m->ev_mesh, cudaEventDisableTiming));
         }
         auto enqueue_all = [&]() -> int {
             int r = enqueue_inputs(m, n, brushes.size());
@@ -1089,6 +1101,7 @@ int apply_csg_to_field(lvn_meshgen* m, const int32_t min[3], int32_t size, Field
     b.plain_class = 0;
     b.need_mats = 1;
     b.derive_mats = 0;
+    b.hmap = nullptr;  // no field kernel runs here: nothing to share
     b.prev_keys = f.keys.as<int32_t>();
     b.prev_info = f.info.as<float4>();
     b.prev_count = f.num_edges;
@@ -1354,7 +1367,7 @@ lvn_meshgen* lvn_meshgen_create(int32_t voxels_per_chunk) {
 void lvn_meshgen_destroy(lvn_meshgen* m) {
     if (!m) return;
     cudaStreamSynchronize(m->stream);
-    DevBuf* bufs[] = {&m->desc,       &m->cs,         &m->bs,         &m->brushes,      &m->mats,  &m->planes,
+    DevBuf* bufs[] = {&m->desc,       &m->cs,         &m->bs,         &m->brushes,      &m->mats,  &m->planes, &m->hmap,
                       &m->edge_tiles, &m->vox_tiles,  &m->edge_keys,  &m->edge_chunk,   &m->edge_info, &m->edge_work,
                       &m->node_codes, &m->node_info,  &m->node_chunk, &m->edge_slots,   &m->node_slots,
                       &m->quad_scratch, &m->node_tile_counts, &m->chunk_tile_off, &m->vertices, &m->triangles,
@@ -1379,6 +1392,9 @@ void lvn_meshgen_destroy(lvn_meshgen* m) {
         if (m->ev[i]) cudaEventDestroy(m->ev[i]);
     if (m->graph_exec) cudaGraphExecDestroy(m->graph_exec);
     if (m->ev_fork) cudaEventDestroy(m->ev_fork);
+    if (m->ev_hash) cudaEventDestroy(m->ev_hash);
+    if (m->ev_mesh) cudaEventDestroy(m->ev_mesh);
+    if (m->aux2) cudaStreamDestroy(m->aux2);
     if (m->ev_leaf) cudaEventDestroy(m->ev_leaf);
     if (m->ev_side) cudaEventDestroy(m->ev_side);
     if (m->side) cudaStreamDestroy(m->side);

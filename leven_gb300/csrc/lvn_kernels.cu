@@ -542,6 +542,7 @@ __global__ void __launch_bounds__(96) k_field(BatchPtrs b) {
     const float wx = (float)(x * scale + ox);
     const float wz = (float)(z * scale + oz);
     const float h = valid ? height_m<MODE>(nz, dp, wx, wz) : 0.f;
+    if (valid && b.hmap) b.hmap[(size_t)c * G::FD * G::FD + x + G::FD * z] = h;
     const int dm = b.default_material;
     const bool write_mats = b.need_mats != 0;
     uint8_t* mats = b.mats + (size_t)c * G::F + x + G::FD * G::FD * z;
@@ -612,7 +613,11 @@ __global__ void __launch_bounds__(128) k_field_caves(BatchPtrs b) {
     __syncthreads();
     const Noise nz{b.perm, b.perm_k4, sg};
     const int tx = (int)threadIdx.x;  // signed: chunk offsets may be negative
-    if (tx < G::FD) hs[tx] = height_m<LVN_DENSITY_CAVES>(nz, dp, (float)(tx * scale + ox), wz);
+    if (tx < G::FD) {
+        const float h = height_m<LVN_DENSITY_CAVES>(nz, dp, (float)(tx * scale + ox), wz);
+        hs[tx] = h;
+        if (b.hmap) b.hmap[(size_t)c * G::FD * G::FD + tx + G::FD * z] = h;
+    }
     __syncthreads();
     const int dm = b.default_material;
     const bool write_mats = b.need_mats != 0;
@@ -1027,8 +1032,12 @@ __global__ void __launch_bounds__(kThreads) k_edge_scatter(BatchPtrs b) {
 // fixed, so its height term is evaluated once; the other edges evaluate it
 // per sample.  Each density evaluation has one call site in a loop, which
 // keeps the kernel small enough for the instruction cache.
+// `hm` is the chunk's height map (the field kernel's height term per column),
+// or null: the height at an edge's end points is then read, not recomputed,
+// with the same arguments and so the same value.
 template <int VPC, int MODE>
-__device__ __forceinline__ float4 hermite_density(const BatchPtrs& b, const Noise& nz, const ChunkDesc& d, int key) {
+__device__ __forceinline__ float4 hermite_density(const BatchPtrs& b, const Noise& nz, const ChunkDesc& d, int key,
+                                                  const float* hm) {
     using G = Geo<VPC>;
     const int axis = key & 3;
     const int hidx = key >> 2;
@@ -1047,12 +1056,18 @@ __device__ __forceinline__ float4 hermite_density(const BatchPtrs& b, const Nois
         // 17-sample search for min |d| (density_field.cl:122-136); first minimum wins
         float minv = FLT_MAX;
         float cur = 0.f;
-        const float hy = yedge ? height_m<MODE>(nz, dp, p0x, p0z) : 0.f;
+        // the end points are field columns: (lx, lz) and (lx, lz) + the x or z step
+        const int c0 = lx + G::FD * lz, c1 = c0 + (axis == 0 ? 1 : axis == 2 ? G::FD : 0);
+        float hy = 0.f;
+        if (yedge) hy = hm ? hm[c0] : height_m<MODE>(nz, dp, p0x, p0z);
         for (int i = 0; i <= 16; i++) {
             const float px = fmaf(p1x - p0x, cur, p0x);
             const float py = fmaf(p1y - p0y, cur, p0y);
             const float pz = fmaf(p1z - p0z, cur, p0z);
-            const float h = yedge ? hy : height_m<MODE>(nz, dp, px, pz);
+            // t = 0 and t = 1 (cur sums 16 exact 1/16 steps) land on the end points
+            const float h = yedge ? hy
+                            : (hm && (i == 0 || i == 16)) ? hm[i == 0 ? c0 : c1]
+                                                          : height_m<MODE>(nz, dp, px, pz);
             const float dv = fabsf(dens_h<MODE>(nz, dp, h, px, py, pz));
             if (dv < minv) { t = cur; minv = dv; hbest = h; }
             cur += 0.0625f;
@@ -1200,9 +1215,10 @@ __global__ void __launch_bounds__(kThreads) k_hermite(BatchPtrs b) {
         const ChunkDesc& d = b.desc[c];
         const int key = b.edge_keys[i];
         const int slot = b.s_on ? b.sslot[c] : -1;
+        const float* hm = b.hmap ? b.hmap + (size_t)c * Geo<VPC>::FD * Geo<VPC>::FD : nullptr;
         b.edge_info[i] = w >= nplain ? hermite_brush<VPC>(b, d, key)
                          : slot >= 0 ? hermite_sdens<VPC>(b, slot, key)
-                                     : hermite_density<VPC, MODE>(b, nz, d, key);
+                                     : hermite_density<VPC, MODE>(b, nz, d, key, hm);
     }
 }
 

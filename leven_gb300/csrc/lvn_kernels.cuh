@@ -94,6 +94,10 @@ struct BatchPtrs {
     int* gate_ok;                // [n] 1 when every probe is within `gate`
     float gate;
 
+    // the height term of a heightfield density per field column (x + FD z) of
+    // each chunk, written by the field kernels; null: hermite evaluates it
+    float* hmap;                 // [n][FD * FD]
+
     // k_mesh_scatter writes triangles (scatter_what 1), seams (2) or both (0);
     // k_leaf and the vertex export take slice `slice` of `nslices` equal leaf
     // ranges (nslices <= 1: all of them)
