@@ -466,10 +466,13 @@ def run_lvn(args):
         torch.distributed.destroy_process_group()
 
 
+PROFILE_TAG = {"tiled": "tiled_csg_128", "clipmap": "clipmap_caves_1024", "one": "one_chunk"}
+
+
 def committed_traffic(kernel):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary
-    (profiles/<kernel>_tiled_csg_128.md, line `dram_bytes_per_launch`)."""
-    path = ROOT / "profiles" / f"{kernel}_tiled_csg_128.md"
+    """DRAM bytes per launch of `kernel` on this workload from the committed ncu
+    summary (profiles/<kernel>_<workload>.md, line `dram_bytes_per_launch`)."""
+    path = ROOT / "profiles" / f"{kernel}_{PROFILE_TAG.get(WORKLOAD, WORKLOAD)}.md"
     try:
         for line in path.read_text().splitlines():
             if "dram_bytes_per_launch" in line:

@@ -97,7 +97,7 @@ struct Global {
     int num_sms = 0;
     int32_t default_material = 0;
     int32_t seed = 0;
-    DevBuf perm, perm_k4, grad;
+    DevBuf perm, perm_k4, perm_ak, grad;
     DensityParams density{LVN_DENSITY_REFERENCE, 8, 1.f / 256.f, 2.f, 0.5f, 48.f, 6, 1.f / 64.f, 2.f, 0.5f, 12.f};
     std::vector<StoredOp> ops;
     std::mt19937 hash_gen;  // default-seeded, drawn in call order (compute_cuckoo.cpp:46-47)
@@ -169,6 +169,13 @@ int upload_perm(int seed) {
         }
     LVN_CK(g.perm.ensure(65536));
     LVN_CK(g.perm_k4.ensure(sizeof(uint16_t) * 65536));
+    // per texel, for snoise3's two chained lookups: the first lookup's column
+    // (alpha, with 255 read as column 0) in the low byte, the second lookup's
+    // gradient index (alpha & 15) in bits 8-11
+    std::vector<uint16_t> ak(65536);
+    for (int t = 0; t < 65536; t++) ak[t] = (uint16_t)((v[t] == 255 ? 0 : v[t]) | ((v[t] & 15) << 8));
+    LVN_CK(g.perm_ak.ensure(sizeof(uint16_t) * 65536));
+    LVN_CK(cudaMemcpy(g.perm_ak.p, ak.data(), sizeof(uint16_t) * 65536, cudaMemcpyHostToDevice));
     LVN_CK(g.grad.ensure(sizeof(grad)));
     LVN_CK(cudaMemcpy(g.perm.p, v.data(), 65536, cudaMemcpyHostToDevice));
     LVN_CK(cudaMemcpy(g.perm_k4.p, k4.data(), sizeof(uint16_t) * 65536, cudaMemcpyHostToDevice));
@@ -487,6 +494,7 @@ BatchPtrs make_ptrs(lvn_meshgen* m, int n) {
     b.brushes = m->brushes.as<Brush>();
     b.perm = g.perm.as<uint8_t>();
     b.perm_k4 = g.perm_k4.as<uint16_t>();
+    b.perm_ak = g.perm_ak.as<uint16_t>();
     b.grad = g.grad.as<float>();
     b.mats = m->mats.as<uint8_t>();
     b.planes = m->planes.as<uint4>();
@@ -1292,6 +1300,7 @@ int lvn_initialise(int32_t noise_seed, uint32_t default_material, int32_t num_cs
 int lvn_shutdown(void) {
     g.perm.release();
     g.perm_k4.release();
+    g.perm_ak.release();
     g.grad.release();
     g.ops.clear();
     g.initialised = false;
@@ -1757,6 +1766,7 @@ GlobalView global_view() {
     v.default_material = g.default_material;
     v.perm = g.perm.as<uint8_t>();
     v.perm_k4 = g.perm_k4.as<uint16_t>();
+    v.perm_ak = g.perm_ak.as<uint16_t>();
     v.grad = g.grad.as<float>();
     v.density = g.density;
     return v;

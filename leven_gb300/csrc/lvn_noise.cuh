@@ -39,12 +39,11 @@ __device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, fl
 }
 
 struct Noise {
-    const uint8_t* __restrict__ v;    // alpha channel (shuffled permutation value) per texel
+    const uint16_t* __restrict__ ak;  // per texel: its alpha as the 3D second lookup's column (255 read as
+                                      // column 0) in bits 0-7, alpha & 15 in bits 8-11
     const uint16_t* __restrict__ k4;  // per texel (row j, col i): the 2D gradient indices (alpha & 15) of
                                       // texels (j, i), (j, i+1), (j+1, i), (j+1, i+1), 4 bits each
     const float* __restrict__ g;      // 16 x 4 gradient table, staged in shared memory
-
-    __device__ __forceinline__ int perm(int idx) const { return __ldg(v + idx); }
 
     // snoise2 (simplex.cl:158-216).  The three corners' texels are (iy, ix),
     // (iy, ix+1) or (iy+1, ix) by the x0 > y0 test, and (iy+1, ix+1): one
@@ -86,9 +85,11 @@ struct Noise {
         return 70.f * ((n0 + n1) + n2);
     }
 
+    // one corner of snoise3: the texel (iy, ix)'s alpha picks the column of
+    // the texel in row iz whose alpha & 15 is the gradient index
     __device__ __forceinline__ float corner3(int ix, int iy, int iz, float x, float y, float z) const {
-        const int a = perm(texel(iy, ix));
-        const int k = perm(texel(iz, alpha_column(a))) & 15;
+        const int a = __ldg(ak + texel(iy, ix)) & 255;  // alpha_column(alpha)
+        const int k = __ldg(ak + texel(iz, a)) >> 8;     // alpha & 15
         float tt = fmaxf(0.6f - dot3(x, y, z, x, y, z), 0.f);  // clamped as in snoise2
         tt = tt * tt;
         const float4 gk = reinterpret_cast<const float4*>(g)[k];  // one 16-byte shared load
@@ -110,14 +111,12 @@ struct Noise {
         const float y0 = py - (piy - t);
         const float z0 = pz - (piz - t);
         const int ix = (int)pix, iy = (int)piy, iz = (int)piz;
-        const int isx_y = x0 >= y0 ? 1 : 0;
-        const int isx_z = x0 >= z0 ? 1 : 0;
-        const int isy_z = y0 >= z0 ? 1 : 0;
-        const int off_x = isx_y + isx_z;
-        const int off_y = (1 - isx_y) + isy_z;
-        const int off_z = (1 - isx_z) + (1 - isy_z);
-        const int o2x = min(max(off_x, 0), 1), o2y = min(max(off_y, 0), 1), o2z = min(max(off_z, 0), 1);
-        const int o1x = min(max(off_x - 1, 0), 1), o1y = min(max(off_y - 1, 0), 1), o1z = min(max(off_z - 1, 0), 1);
+        // simplex() ranks each axis by its two comparisons (rank 0..2): the
+        // second corner steps the axes of rank 2, the third those of rank >= 1,
+        // i.e. clamp(rank - 1, 0, 1) = both comparisons, clamp(rank, 0, 1) = either
+        const bool xy = x0 >= y0, xz = x0 >= z0, yz = y0 >= z0;
+        const int o1x = xy && xz, o1y = !xy && yz, o1z = !xz && !yz;
+        const int o2x = xy || xz, o2y = !xy || yz, o2z = !xz || !yz;
         const float n0 = corner3(ix, iy, iz, x0, y0, z0);
         const float n1 = corner3(ix + o1x, iy + o1y, iz + o1z, (x0 - (float)o1x) + G3, (y0 - (float)o1y) + G3,
                                  (z0 - (float)o1z) + G3);
