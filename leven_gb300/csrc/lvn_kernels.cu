@@ -1494,14 +1494,23 @@ __global__ void __launch_bounds__(kThreads) k_leaf(BatchPtrs b) {
         const bool simp = b.simp_on != 0;
         SimpQef sq;
         if (simp) simp_zero(sq);
+        // every edge lookup first, so that their table probes are in flight
+        // together, then the crossings in edge order
+        uint32_t dis[12];
+#pragma unroll
         for (int e = 0; e < 12; e++) {
-            if (!((edge_list >> e) & 1)) continue;
+            const int e0 = edge_c0(e);
+            dis[e] = ((edge_list >> e) & 1)
+                         ? hv.find((uint32_t)edge_key<VPC>(x + (e0 >> 2), y + ((e0 >> 1) & 1), z + (e0 & 1), e / 4))
+                         : ~0u;
+        }
+#pragma unroll
+        for (int e = 0; e < 12; e++) {
+            const uint32_t di = dis[e];
+            if (di == ~0u) continue;
             const int e0 = edge_c0(e), e1 = edge_c1(e);
             const int o0x = e0 >> 2, o0y = (e0 >> 1) & 1, o0z = e0 & 1;
             const int o1x = e1 >> 2, o1y = (e1 >> 1) & 1, o1z = e1 & 1;
-            const int axis = e / 4;
-            const uint32_t di = hv.find((uint32_t)edge_key<VPC>(x + o0x, y + o0y, z + o0z, axis));
-            if (di == ~0u) continue;
             const float4 ed = info[di];
             const float p0x = (float)x + (float)o0x, p0y = (float)y + (float)o0y, p0z = (float)z + (float)o0z;
             const float p1x = (float)x + (float)o1x, p1y = (float)y + (float)o1y, p1z = (float)z + (float)o1z;
