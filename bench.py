@@ -20,7 +20,11 @@ a bounded sample of the same workload.
 `--workload clipmap`: 1024 chunks over clipmap LODs 0-4 around a moving
 seeded camera, 2D fBm heightfield + 3D fBm caves, followed by the octree
 simplification at QEF error 0.05 (CPU baseline: the same, simplification
-included).  `--surrogate`: trains the learned density surrogate on the GPU
+included).  `--workload select`: the clipmap's active-node selection
+(SelectActiveClipmapNodes) for 4096 cameras on 64 seeded paths through the
+2^15-unit world, one launch per step (its own JSON line, impl "lvn-select";
+the reference arm times the oracle's recursion on all host threads).
+`--surrogate`: trains the learned density surrogate on the GPU
 and meshes the clipmap chunk set with the 2D fBm density plain and through
 the surrogate (its own JSON line, impl "lvn-surrogate").
 """
@@ -60,9 +64,9 @@ def parse():
     p.add_argument("--simplify", type=float, default=None,
                    help="octree simplification QEF-error threshold (voxel^2); default 0.05 for the clipmap "
                         "workload, off otherwise; < 0 = off")
-    p.add_argument("--workload", default="tiled", choices=["tiled", "clipmap", "one"],
+    p.add_argument("--workload", default="tiled", choices=["tiled", "clipmap", "one", "select"],
                    help="tiled: 128 LOD0 chunks + 32 CSG ops (default); clipmap: 1024 chunks over LOD 0-4 with "
-                        "3D caves; one: a single LOD0 chunk")
+                        "3D caves; one: a single LOD0 chunk; select: clipmap node selection for 4096 cameras")
     return p.parse_args()
 
 
@@ -229,6 +233,8 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
+    if WORKLOAD == "select":
+        return run_select_reference(args)
     wl = workload()
     threads = host_threads()
     cb = CpuBaseline(wl, threads, simplify_threshold(args))
@@ -466,7 +472,8 @@ def run_lvn(args):
         torch.distributed.destroy_process_group()
 
 
-PROFILE_TAG = {"tiled": "tiled_csg_128", "clipmap": "clipmap_caves_1024", "one": "one_chunk"}
+PROFILE_TAG = {"tiled": "tiled_csg_128", "clipmap": "clipmap_caves_1024", "one": "one_chunk",
+               "select": "select_4096"}
 
 
 def committed_traffic(kernel):
@@ -650,6 +657,155 @@ def run_surrogate(args):
     sur.close()
 
 
+SELECT_METRIC = "clipmap camera selections/sec on 1 GB300 (SelectActiveClipmapNodes, 2^15 root)"
+
+
+class SelectBaseline:
+    """The oracle's SelectActiveClipmapNodes recursion over the cameras on
+    `threads` host threads (one orc_clipmap_select_many call per pass)."""
+
+    def __init__(self, cams, threads):
+        sys.path.insert(0, str(ROOT / "tests"))
+        import oracle_lib as O
+        from leven_gb300 import workloads as W
+
+        O.build()
+        self.O, self.cams, self.threads, self.W = O, cams, threads, W
+
+    def run(self):
+        t0 = time.perf_counter()
+        self.O.clipmap_select_many(self.cams, self.W.CLIPMAP_ROOT_MIN, self.W.CLIPMAP_ROOT_SIZE, self.threads)
+        return time.perf_counter() - t0
+
+    def rate(self, target_s):
+        done, total = 0, 0.0
+        while total < target_s:
+            total += self.run()
+            done += len(self.cams)
+        return done / total, total, done
+
+
+def run_select_reference(args):
+    from leven_gb300 import workloads as W
+
+    cams = W.clipmap_cameras()
+    threads = host_threads()
+    cb = SelectBaseline(cams, threads)
+    for _ in range(args.warmup):
+        cb.run()
+    vals = [len(cams) / cb.run() for _ in range(args.steps)]
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": SELECT_METRIC, "value": round(value, 1), "unit": "cameras/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * len(cams) / value, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"clipmap-select-{len(cams)}cameras", "root_size": W.CLIPMAP_ROOT_SIZE},
+        "cpu_baseline": {"value": round(value, 1), "unit": "cameras/s", "cores": threads, "kind": "port",
+                         "sample": f"all {len(cams)} cameras per step"},
+        "e2e": {"value": round(value, 1), "unit": "cameras/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_select(args):
+    """The clipmap's active-node selection for the 4096-camera workload: the
+    device form (cameras resident, lists left in HBM) per step, and end to end
+    through the host-buffer C-ABI call."""
+    import numpy as np
+    import torch
+
+    import leven_gb300 as lvn
+    from leven_gb300 import workloads as W
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    cams = W.clipmap_cameras()
+    n = len(cams)
+    rmin, rsize = W.CLIPMAP_ROOT_MIN, W.CLIPMAP_ROOT_SIZE
+    stride = 1024
+    d_cams = torch.from_numpy(cams).to(dev)
+    d_out = torch.empty((n * stride, 4), dtype=torch.int32, device=dev)
+    d_counts = torch.empty(n, dtype=torch.int32, device=dev)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.int32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    for _ in range(max(args.warmup, 3)):
+        lvn.clipmap_select_device(d_cams, rmin, rsize, d_out, stride, d_counts, stream=stream)
+    torch.cuda.synchronize()
+    counts = d_counts.cpu().numpy()
+    assert (counts >= 0).all() and (counts <= stride).all(), "selection lists exceed the device stride"
+    total_nodes = int(counts.sum())
+
+    h_cams = torch.from_numpy(cams).pin_memory()
+    h_out = torch.empty((total_nodes + 1024, 4), dtype=torch.int32).pin_memory()
+    h_counts = np.zeros(n, np.int32)
+    L = lvn.lib()
+
+    def host_call():
+        rc = L.lvn_clipmap_select(h_cams.data_ptr(), n, lvn._ivec3(rmin), rsize, h_out.data_ptr(), h_out.shape[0],
+                                  h_counts.ctypes.data)
+        assert rc == 0, rc
+
+    for _ in range(max(args.warmup, 3)):
+        host_call()
+    assert int(h_counts.sum()) == total_nodes
+
+    with ClockSampler(local) as clocks:
+        ts = []
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            lvn.clipmap_select_device(d_cams, rmin, rsize, d_out, stride, d_counts, stream=stream)
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        te = []
+        for _ in range(args.steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            host_call()
+            te.append(time.perf_counter() - t0)
+    ms = sum(ts) / len(ts)
+    ms_e2e = 1e3 * sum(te) / len(te)
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    # algorithmic bytes of one launch: the cameras in, the lists and counts out
+    algo = 12 * n + 16 * total_nodes + 4 * n
+    ach = algo / (ms / 1e3) / 1e9
+    line = {
+        "metric": SELECT_METRIC, "impl": "lvn-select", "value": round(n / (ms / 1e3), 1), "unit": "cameras/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"clipmap-select-{n}cameras", "root_size": rsize, "nodes_listed": total_nodes,
+                   "stride": stride, "l2": "flushed between steps (256 MiB write)"},
+        "e2e": {"value": round(n / (ms_e2e / 1e3), 1), "unit": "cameras/s", "h2d_bytes_per_step": 12 * n,
+                "d2h_bytes_per_step": 16 * total_nodes + 4 * n, "ms_per_step": round(ms_e2e, 4)},
+        "gpu_launches": 1,
+        "roofline": {"bound": "hbm", "achieved": round(ach, 1), "peak": hbm_peak, "unit": "GB/s",
+                     "frac": round(ach / hbm_peak, 4), "traffic": committed_traffic("clipmap_walk"),
+                     "kernel": "k_clipmap_walk", "ms_per_launch": round(ms, 4),
+                     "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                     "algorithmic_bytes_per_launch": algo},
+        "clocks": clocks.summary(),
+    }
+    if not args.no_cpu_baseline:
+        threads = host_threads()
+        v, dt, m = SelectBaseline(cams, threads).rate(3.0)
+        line["cpu_baseline"] = {"value": round(v, 1), "unit": "cameras/s", "cores": threads, "kind": "port",
+                                "sample": f"{m // n} passes over the {n} cameras, {dt:.1f} s"}
+    print(json.dumps(line), flush=True)
+
+
 if __name__ == "__main__":
     a = parse()
     WORKLOAD = a.workload
@@ -657,5 +813,7 @@ if __name__ == "__main__":
         run_reference(a)
     elif a.surrogate:
         run_surrogate(a)
+    elif a.workload == "select":
+        run_select(a)
     else:
         run_lvn(a)

@@ -325,6 +325,41 @@ int lvn_meshgen_set_surrogate(lvn_meshgen* ctx, lvn_surrogate* s, float gate);
 /* chunks of the last batch that used the surrogate; use[c] = 1 / 0 when not NULL */
 int lvn_meshgen_surrogate_chunks(lvn_meshgen* ctx, int32_t* use, int32_t capacity);
 
+/* ---- clipmap chunk lists (class Clipmap, clipmap.h / clipmap.cpp) ----------
+ * Over a complete clipmap octree: root_min, root_size (a power of two, at
+ * least 256 = CLIPMAP_LEAF_SIZE and at most 16 LOD_MAX_NODE_SIZE nodes per
+ * axis) with every node subdivided down to CLIPMAP_LEAF_SIZE, as
+ * Clipmap::constructTree / ConstructChildren (clipmap.cpp:715-735, 797-818)
+ * build it.  Nodes are written as chunk descriptors (min, size), ready for
+ * lvn_meshgen_generate_chunks.  One query lists at most LVN_CLIPMAP_MAX_NODES
+ * nodes and opens at most LVN_CLIPMAP_MAX_OPEN nodes per level; beyond that the
+ * call returns LVN_ERR_DEVICE_STATUS.  The calls share scratch on the first
+ * device they run on and serialise each other. */
+#define LVN_CLIPMAP_MAX_NODES 8192
+#define LVN_CLIPMAP_MAX_OPEN  4096
+
+/* SelectActiveClipmapNodes (clipmap.cpp:1084-1128, DistanceToNode 1056-1064)
+ * for num_cameras cameras (x, y, z each) in one launch: camera q's nodes in
+ * the reference's recursion order (pre-order over CHILD_MIN_OFFSETS), the
+ * cameras' lists back to back in out; counts[q] = camera q's node count.
+ * When the lists do not fit `capacity`, LVN_ERR_CAPACITY (counts set). */
+int lvn_clipmap_select(const float* cameras, int32_t num_cameras, const int32_t root_min[3], int32_t root_size,
+                       lvn_chunk_desc* out, int32_t capacity, int32_t* counts);
+/* The same on device buffers, enqueued on cuda_stream (NULL: the legacy
+ * default stream) with no host synchronisation: d_cameras[3 num_cameras],
+ * camera q's list at d_out[q stride ..] (its first `stride` nodes), its count
+ * in d_counts[q] (-1: an internal limit was exceeded).  Calls on different
+ * streams share the scratch: order them. */
+int lvn_clipmap_select_device(const float* d_cameras, int32_t num_cameras, const int32_t root_min[3],
+                              int32_t root_size, lvn_chunk_desc* d_out, int32_t stride, int32_t* d_counts,
+                              void* cuda_stream);
+/* The nodes a batch of CSG operations touches (processCSGOperationsImpl,
+ * clipmap.cpp:1661-1669): every node no larger than LOD_MAX_NODE_SIZE whose
+ * box overlaps an operation's CalcCSGOperationBounds (FindNodesInsideAABB,
+ * clipmap.cpp:1571-1597), each once, in the recursion's post-order. */
+int lvn_clipmap_touched(const lvn_csg_op* ops, int32_t num_ops, const int32_t root_min[3], int32_t root_size,
+                        lvn_chunk_desc* out, int32_t capacity, int32_t* count);
+
 #ifdef __cplusplus
 }
 #endif

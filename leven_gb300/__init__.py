@@ -19,7 +19,14 @@ _PKG = pathlib.Path(__file__).resolve().parent
 LIB_PATH = _PKG / "liblvn.so"
 
 LVN_OK = 0
+LVN_ERR_NO_DEVICE = -1
+LVN_ERR_OUT_OF_MEMORY = -5
+LVN_ERR_INVALID = -30
 LVN_ERR_CAPACITY = -100
+LVN_ERR_NOT_INITIALISED = -101
+LVN_ERR_HASH = -102
+LVN_ERR_DEVICE_STATUS = -103
+LVN_ERR_CUDA = -99999
 LVN_MEMORY_HOST = 0
 LVN_MEMORY_DEVICE = 1
 LVN_DENSITY_REFERENCE, LVN_DENSITY_FBM2D, LVN_DENSITY_CAVES = 0, 1, 2
@@ -83,6 +90,7 @@ EXPORTS = [
     "lvn_surrogate_get_params", "lvn_surrogate_sample", "lvn_surrogate_train", "lvn_surrogate_grad",
     "lvn_surrogate_eval", "lvn_surrogate_eval_lattices", "lvn_surrogate_domain", "lvn_surrogate_get_stream",
     "lvn_meshgen_set_surrogate", "lvn_meshgen_surrogate_chunks", "lvn_density_f64",
+    "lvn_clipmap_select", "lvn_clipmap_select_device", "lvn_clipmap_touched",
 ]
 
 _lib = None
@@ -141,6 +149,10 @@ def lib():
     L.lvn_meshgen_set_surrogate.argtypes = [C.c_void_p, C.c_void_p, C.c_float]
     L.lvn_meshgen_surrogate_chunks.argtypes = [C.c_void_p, i32p, C.c_int32]
     L.lvn_density_f64.argtypes = [C.c_void_p, C.c_int64, C.c_void_p]
+    L.lvn_clipmap_select.argtypes = [C.c_void_p, C.c_int32, i32p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]
+    L.lvn_clipmap_select_device.argtypes = [C.c_void_p, C.c_int32, i32p, C.c_int32, C.c_void_p, C.c_int32,
+                                            C.c_void_p, C.c_void_p]
+    L.lvn_clipmap_touched.argtypes = [C.POINTER(CsgOp), C.c_int32, i32p, C.c_int32, C.c_void_p, C.c_int32, i32p]
     L.lvn_surrogate_get_stream.restype = C.c_void_p
     L.lvn_meshgen_debug_fetch.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int64]
     L.lvn_meshgen_debug_fetch.restype = C.c_int64
@@ -197,6 +209,59 @@ def csg_operation_bounds(op):
     lo, hi = (C.c_int32 * 3)(), (C.c_int32 * 3)()
     _check(lib().lvn_csg_operation_bounds(C.byref(op), lo, hi), "lvn_csg_operation_bounds")
     return list(lo), list(hi)
+
+
+LVN_CLIPMAP_MAX_NODES = 8192
+
+
+def clipmap_select(cameras, root_min, root_size):
+    """SelectActiveClipmapNodes (clipmap.cpp:1084-1128) for every camera of
+    `cameras` (n x 3) over the complete octree (root_min, root_size), in one
+    launch.  Returns one (count, 4) int32 array (min x, y, z, size) per camera,
+    in the reference's recursion order."""
+    cams = np.ascontiguousarray(np.asarray(cameras, dtype=np.float32).reshape(-1, 3))
+    n = cams.shape[0]
+    counts = np.zeros(max(n, 1), np.int32)
+    cap = max(1024, 640 * n)
+    for _ in range(2):
+        out = np.zeros((cap, 4), np.int32)
+        rc = lib().lvn_clipmap_select(cams.ctypes.data, n, _ivec3(root_min), int(root_size), out.ctypes.data, cap,
+                                      counts.ctypes.data)
+        if rc != LVN_ERR_CAPACITY:
+            break
+        cap = int(counts[:n].sum())
+    _check(rc, "lvn_clipmap_select")
+    offs = np.concatenate([[0], np.cumsum(counts[:n])])
+    return [out[offs[i]:offs[i + 1]] for i in range(n)]
+
+
+def clipmap_select_device(d_cameras, root_min, root_size, d_out, stride, d_counts, stream=None):
+    """The device form: torch tensors d_cameras (n, 3) f32, d_out (n * stride, 4)
+    i32, d_counts (n,) i32, all on the GPU; enqueued on `stream` (a
+    torch.cuda.Stream, default the current stream), no host synchronisation."""
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    n = d_cameras.shape[0]
+    return _check(lib().lvn_clipmap_select_device(d_cameras.data_ptr(), n, _ivec3(root_min), int(root_size),
+                                                  d_out.data_ptr(), int(stride), d_counts.data_ptr(),
+                                                  C.c_void_p(s.cuda_stream)), "lvn_clipmap_select_device")
+
+
+def clipmap_touched(ops, root_min, root_size):
+    """The clipmap nodes a batch of CSG operations touches (processCSGOperationsImpl,
+    clipmap.cpp:1661-1669), each once, in the recursion's post-order: (count, 4) int32."""
+    arr = (CsgOp * max(len(ops), 1))(*ops)
+    cap = 4096
+    count = C.c_int32(0)
+    for _ in range(2):
+        out = np.zeros((cap, 4), np.int32)
+        rc = lib().lvn_clipmap_touched(arr, len(ops), _ivec3(root_min), int(root_size), out.ctypes.data, cap,
+                                       C.byref(count))
+        if rc != LVN_ERR_CAPACITY:
+            break
+        cap = count.value
+    _check(rc, "lvn_clipmap_touched")
+    return out[:count.value]
 
 
 def store_csg_operation(op, aabb=None):

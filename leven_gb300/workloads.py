@@ -178,6 +178,27 @@ def select_clipmap_nodes(root_min, root_size, cam):
     return out
 
 
+CLIPMAP_ROOT_MIN = (-(1 << 14), -(1 << 14), -(1 << 14))
+CLIPMAP_ROOT_SIZE = 1 << 15
+
+
+def clipmap_cameras(n_paths=64, per_path=64, seed=1):
+    """Camera positions for the clipmap selection workload: n_paths seeded
+    straight paths of per_path positions each through the 2^15-unit world
+    centred on the origin, as the engine re-selects while the camera travels
+    (start x, z U[-2048, 2048], y U[-64, 64]; 256 * U[-1, 1] per step in x and
+    z); float32, (n_paths * per_path, 3)."""
+    import numpy as np
+
+    rng = MT19937(seed)
+    out = []
+    for _ in range(n_paths):
+        cam0 = (rng.uniform(-2048.0, 2048.0), rng.uniform(-64.0, 64.0), rng.uniform(-2048.0, 2048.0))
+        step = (rng.uniform(-1.0, 1.0) * 256.0, 0.0, rng.uniform(-1.0, 1.0) * 256.0)
+        out += [[cam0[i] + k * step[i] for i in range(3)] for k in range(per_path)]
+    return np.array(out, np.float32)
+
+
 def clipmap_caves(n_chunks=1024, max_lod=4, seed=1):
     """configs[2]: n_chunks chunks over clipmap LODs 0..max_lod, density = 2D
     fBm heightfield + 3D fBm caves (6 octaves, 1/64, amplitude 12).  One

@@ -1633,6 +1633,149 @@ int orc_aabb_overlaps(const int32_t amin[3], const int32_t amax[3], const int32_
              amin[1] > bmax[1] || amin[2] > bmax[2]);
 }
 
+// ---- clipmap chunk lists ------------------------------------------------------
+
+}  // extern "C"
+
+namespace clipmap {
+constexpr int kLeaf = 256;                  // CLIPMAP_LEAF_SIZE (volume_constants.h:15)
+constexpr int kLodMax = kLeaf * (1 << 5);   // LOD_MAX_NODE_SIZE (clipmap.cpp:31)
+const float kActive[6] = {0.f, kLeaf * 1.5f, kLeaf * 3.5f, kLeaf * 5.5f, kLeaf * 7.5f, kLeaf * 13.5f};  // clipmap.cpp:33-41
+
+struct Out {
+    int32_t* out4;
+    int32_t cap;
+    int32_t n = 0;
+    void push(const int32_t mn[3], int32_t size) {
+        if (n < cap) {
+            out4[4 * n] = mn[0];
+            out4[4 * n + 1] = mn[1];
+            out4[4 * n + 2] = mn[2];
+            out4[4 * n + 3] = size;
+        }
+        n++;
+    }
+};
+
+// DistanceToNode (clipmap.cpp:1056-1064), float arithmetic
+float distance_to_node(const int32_t mn[3], int32_t size, const float cam[3]) {
+    float d[3];
+    for (int a = 0; a < 3; a++) {
+        const float lo = (float)mn[a], hi = (float)(mn[a] + size);
+        d[a] = std::max(std::max(lo - cam[a], 0.f), cam[a] - hi);
+    }
+    return std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+}
+
+void child_min(const int32_t mn[3], int32_t half, int i, int32_t c[3]) {
+    // CHILD_MIN_OFFSETS order: x << 2 | y << 1 | z
+    c[0] = mn[0] + ((i >> 2) & 1) * half;
+    c[1] = mn[1] + ((i >> 1) & 1) * half;
+    c[2] = mn[2] + (i & 1) * half;
+}
+
+// SelectActiveClipmapNodes (clipmap.cpp:1084-1128)
+void select(const int32_t mn[3], int32_t size, bool parent_active, const float cam[3], Out& o) {
+    bool active = false;
+    if (!parent_active && size <= kLodMax) {
+        int lod = 0;
+        while ((kLeaf << lod) < size) lod++;  // log2(size / CLIPMAP_LEAF_SIZE)
+        if (distance_to_node(mn, size, cam) >= kActive[lod]) {
+            o.push(mn, size);
+            active = true;
+        }
+    }
+    if (size == kLeaf || parent_active || active) return;  // nothing below is selected
+    const int32_t half = size / 2;
+    for (int i = 0; i < 8; i++) {
+        int32_t c[3];
+        child_min(mn, half, i, c);
+        select(c, half, false, cam, o);
+    }
+}
+
+bool overlaps(const int32_t mn[3], int32_t size, const int32_t bmin[3], const int32_t bmax[3]) {
+    const int32_t nmax[3] = {mn[0] + size, mn[1] + size, mn[2] + size};
+    return orc_aabb_overlaps(bmin, bmax, mn, nmax) != 0;
+}
+
+// FindNodesInsideAABB (clipmap.cpp:1571-1597) generalised to a set of boxes:
+// a node is visited when it overlaps any of them.  With one box this is the
+// reference's recursion; with several, a node overlapping box j has every
+// ancestor overlapping box j, so the union of the per-box walks is exactly
+// the nodes this walk lists.
+void inside(const int32_t mn[3], int32_t size, const std::vector<int32_t>& boxes, Out& o) {
+    bool any = false;
+    for (size_t b = 0; b < boxes.size(); b += 6)
+        if (overlaps(mn, size, &boxes[b], &boxes[b + 3])) {
+            any = true;
+            break;
+        }
+    if (!any) return;
+    if (size > kLeaf) {
+        const int32_t half = size / 2;
+        for (int i = 0; i < 8; i++) {
+            int32_t c[3];
+            child_min(mn, half, i, c);
+            inside(c, half, boxes, o);
+        }
+    }
+    if (size <= kLodMax) o.push(mn, size);
+}
+
+bool valid_root(int32_t root_size) { return root_size >= kLeaf && (root_size & (root_size - 1)) == 0; }
+}  // namespace clipmap
+
+extern "C" {
+
+int orc_clipmap_select(const float cam[3], const int32_t root_min[3], int32_t root_size, int32_t* out4, int32_t cap) {
+    if (!clipmap::valid_root(root_size)) return -1;
+    clipmap::Out o{out4, cap};
+    clipmap::select(root_min, root_size, false, cam, o);
+    return o.n;
+}
+
+int orc_clipmap_nodes_in_aabb(const int32_t bmin[3], const int32_t bmax[3], const int32_t root_min[3],
+                              int32_t root_size, int32_t* out4, int32_t cap) {
+    if (!clipmap::valid_root(root_size)) return -1;
+    std::vector<int32_t> boxes = {bmin[0], bmin[1], bmin[2], bmax[0], bmax[1], bmax[2]};
+    clipmap::Out o{out4, cap};
+    clipmap::inside(root_min, root_size, boxes, o);
+    return o.n;
+}
+
+int orc_clipmap_touched(const orc_csg_op* ops, int32_t n, const int32_t root_min[3], int32_t root_size,
+                        int32_t* out4, int32_t cap) {
+    if (!clipmap::valid_root(root_size)) return -1;
+    std::vector<int32_t> boxes(6 * (size_t)std::max(n, 0));
+    for (int i = 0; i < n; i++) orc_csg_op_bounds(&ops[i], &boxes[6 * i], &boxes[6 * i + 3]);
+    clipmap::Out o{out4, cap};
+    if (n > 0) clipmap::inside(root_min, root_size, boxes, o);
+    return o.n;
+}
+
+int64_t orc_clipmap_select_many(const float* cams, int32_t n, const int32_t root_min[3], int32_t root_size,
+                                int32_t threads) {
+    if (!clipmap::valid_root(root_size) || n < 0) return -1;
+    if (threads < 1) threads = 1;
+    std::atomic<int> next{0};
+    std::atomic<int64_t> total{0};
+    auto worker = [&]() {
+        std::vector<int32_t> buf(4 * 8192);
+        for (;;) {
+            const int i = next.fetch_add(1);
+            if (i >= n) break;
+            clipmap::Out o{buf.data(), 8192};
+            clipmap::select(root_min, root_size, false, cams + 3 * (size_t)i, o);
+            total += o.n;
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; t++) pool.emplace_back(worker);
+    for (auto& t : pool) t.join();
+    return total.load();
+}
+
 int64_t orc_mesh_chunks(const orc_density* d, const orc_chunk_args* chunks, int32_t n, int32_t threads) {
     return orc_mesh_chunks_simplified(d, chunks, n, threads, -1.f);
 }

@@ -106,6 +106,27 @@ void orc_csg_op_bounds(const orc_csg_op* op, int32_t out_min[3], int32_t out_max
 int  orc_aabb_overlaps(const int32_t amin[3], const int32_t amax[3],
                        const int32_t bmin[3], const int32_t bmax[3]);
 
+/* Clipmap chunk lists over a complete octree (root_min, root_size; every node
+ * subdivided down to 256-unit leaves, ConstructChildren clipmap.cpp:715-735).
+ * Nodes are written as (min x, y, z, size) int32 quadruples, at most cap of
+ * them; the return value is the full count.
+ * orc_clipmap_select: SelectActiveClipmapNodes (clipmap.cpp:1084-1128) for one
+ * camera, in its recursion's pre-order.
+ * orc_clipmap_nodes_in_aabb: FindNodesInsideAABB (clipmap.cpp:1571-1597) for
+ * one box, in its recursion's post-order.
+ * orc_clipmap_touched: the touch set of processCSGOperationsImpl
+ * (clipmap.cpp:1661-1669), the union over the operations' bounds, each node
+ * once, in the octree's post-order. */
+int orc_clipmap_select(const float cam[3], const int32_t root_min[3], int32_t root_size, int32_t* out4, int32_t cap);
+int orc_clipmap_nodes_in_aabb(const int32_t bmin[3], const int32_t bmax[3], const int32_t root_min[3],
+                              int32_t root_size, int32_t* out4, int32_t cap);
+int orc_clipmap_touched(const orc_csg_op* ops, int32_t n, const int32_t root_min[3], int32_t root_size,
+                        int32_t* out4, int32_t cap);
+/* CPU baseline: orc_clipmap_select for n cameras on `threads` host threads;
+ * returns the total node count */
+int64_t orc_clipmap_select_many(const float* cams, int32_t n, const int32_t root_min[3], int32_t root_size,
+                                int32_t threads);
+
 /* CPU baseline: mesh n chunks (each a fresh field with its ops) on `threads`
  * host threads; returns total vertices + triangles for sanity */
 int64_t orc_mesh_chunks(const orc_density* d, const orc_chunk_args* chunks, int32_t n,

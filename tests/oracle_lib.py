@@ -77,6 +77,13 @@ def lib():
         L.orc_mesh_chunks_simplified.argtypes = [C.POINTER(Density), C.POINTER(ChunkArgs), C.c_int32, C.c_int32,
                                                  C.c_float]
         L.orc_mesh_chunks_simplified.restype = C.c_int64
+        L.orc_clipmap_select.argtypes = [C.c_float * 3, C.c_int32 * 3, C.c_int32, C.c_void_p, C.c_int32]
+        L.orc_clipmap_nodes_in_aabb.argtypes = [C.c_int32 * 3, C.c_int32 * 3, C.c_int32 * 3, C.c_int32, C.c_void_p,
+                                                C.c_int32]
+        L.orc_clipmap_touched.argtypes = [C.POINTER(CsgOp), C.c_int32, C.c_int32 * 3, C.c_int32, C.c_void_p,
+                                          C.c_int32]
+        L.orc_clipmap_select_many.argtypes = [C.c_void_p, C.c_int32, C.c_int32 * 3, C.c_int32, C.c_int32]
+        L.orc_clipmap_select_many.restype = C.c_int64
         _lib = L
     return _lib
 
@@ -213,3 +220,40 @@ def op_bounds(op_tuple):
     hi = (C.c_int32 * 3)()
     lib().orc_csg_op_bounds(ops, lo, hi)
     return list(lo), list(hi)
+
+
+def _i3(v):
+    return (C.c_int32 * 3)(*[int(x) for x in v])
+
+
+def _nodes(fn, *args):
+    cap = 4096
+    while True:
+        out = np.zeros((cap, 4), np.int32)
+        n = fn(*args, out.ctypes.data, cap)
+        if n < 0:
+            raise ValueError("invalid clipmap root")
+        if n <= cap:
+            return out[:n]
+        cap = n
+
+
+def clipmap_select(cam, root_min, root_size):
+    """SelectActiveClipmapNodes for one camera: (count, 4) int32 in pre-order."""
+    return _nodes(lib().orc_clipmap_select, (C.c_float * 3)(*[float(x) for x in cam]), _i3(root_min), int(root_size))
+
+
+def clipmap_nodes_in_aabb(bmin, bmax, root_min, root_size):
+    """FindNodesInsideAABB for one box: (count, 4) int32 in post-order."""
+    return _nodes(lib().orc_clipmap_nodes_in_aabb, _i3(bmin), _i3(bmax), _i3(root_min), int(root_size))
+
+
+def clipmap_touched(op_tuples, root_min, root_size):
+    """The CSG touch set of the operations: (count, 4) int32 in post-order."""
+    ops = make_ops(op_tuples)
+    return _nodes(lib().orc_clipmap_touched, ops, len(op_tuples), _i3(root_min), int(root_size))
+
+
+def clipmap_select_many(cams, root_min, root_size, threads):
+    c = np.ascontiguousarray(np.asarray(cams, np.float32).reshape(-1, 3))
+    return lib().orc_clipmap_select_many(c.ctypes.data, c.shape[0], _i3(root_min), int(root_size), int(threads))
