@@ -360,6 +360,32 @@ int lvn_clipmap_select_device(const float* d_cameras, int32_t num_cameras, const
 int lvn_clipmap_touched(const lvn_csg_op* ops, int32_t num_ops, const int32_t root_min[3], int32_t root_size,
                         lvn_chunk_desc* out, int32_t capacity, int32_t* count);
 
+/* ---- seam meshes (GenerateClipmapSeamMesh, clipmap.cpp:573-610) -----------
+ * The clipmap's active nodes are `chunks` (disjoint, inside the complete
+ * octree root_min / root_size, as above); chunk c's seam nodes, as
+ * lvn_meshgen_generate_chunks returns them (SeamNodeInfo), are
+ * seams[seam_offsets[c] .. seam_offsets[c + 1]) (seam_offsets[0] = 0; seams in
+ * host or device memory per seams_memory).  For each host (an index into
+ * chunks) the seam nodes of the host and of the active nodes next to it are
+ * gathered (FindNode / FindActiveNodes / SelectSeamNodes / FilterSeamNode,
+ * clipmap.cpp:508-570, 982-1013, 1449-1479), built into an octree
+ * (Octree_ConstructUpwards, octree.cpp:90-148) and contoured
+ * (Octree_GenerateMesh, octree.cpp:197-551): every leaf becomes a vertex
+ * (position, normal, rgb = colour, a = material) in the octree's depth-first
+ * order and the quads of edges straddling chunks become triangles of
+ * host-local indices, in the recursion's order.  out->chunks[h] gives host h's
+ * offsets and counts (num_nodes = its seam leaves); a host without triangles
+ * has no mesh (no vertices).  Limits per host: LVN_SEAM_MAX_LEAVES leaves and
+ * LVN_SEAM_MAX_QUADS quads (else LVN_ERR_DEVICE_STATUS) and 2 x host size at
+ * most 4096 x the smallest leaf gathered (else LVN_ERR_INVALID).  Calls
+ * share scratch on the first device they run on and serialise each other. */
+#define LVN_SEAM_MAX_LEAVES 8192
+#define LVN_SEAM_MAX_QUADS  8192
+int lvn_seam_generate(const lvn_chunk_desc* chunks, const int32_t* seam_offsets, int32_t num_chunks,
+                      const lvn_seam_node* seams, int32_t seams_memory, int32_t voxels_per_chunk,
+                      const int32_t root_min[3], int32_t root_size, const int32_t* hosts, int32_t num_hosts,
+                      const float colour[3], lvn_batch_out* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -90,7 +90,7 @@ EXPORTS = [
     "lvn_surrogate_get_params", "lvn_surrogate_sample", "lvn_surrogate_train", "lvn_surrogate_grad",
     "lvn_surrogate_eval", "lvn_surrogate_eval_lattices", "lvn_surrogate_domain", "lvn_surrogate_get_stream",
     "lvn_meshgen_set_surrogate", "lvn_meshgen_surrogate_chunks", "lvn_density_f64",
-    "lvn_clipmap_select", "lvn_clipmap_select_device", "lvn_clipmap_touched",
+    "lvn_clipmap_select", "lvn_clipmap_select_device", "lvn_clipmap_touched", "lvn_seam_generate",
 ]
 
 _lib = None
@@ -153,6 +153,8 @@ def lib():
     L.lvn_clipmap_select_device.argtypes = [C.c_void_p, C.c_int32, i32p, C.c_int32, C.c_void_p, C.c_int32,
                                             C.c_void_p, C.c_void_p]
     L.lvn_clipmap_touched.argtypes = [C.POINTER(CsgOp), C.c_int32, i32p, C.c_int32, C.c_void_p, C.c_int32, i32p]
+    L.lvn_seam_generate.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32, i32p,
+                                    C.c_int32, C.c_void_p, C.c_int32, C.c_float * 3, C.POINTER(BatchOut)]
     L.lvn_surrogate_get_stream.restype = C.c_void_p
     L.lvn_meshgen_debug_fetch.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int64]
     L.lvn_meshgen_debug_fetch.restype = C.c_int64
@@ -245,6 +247,42 @@ def clipmap_select_device(d_cameras, root_min, root_size, d_out, stride, d_count
     return _check(lib().lvn_clipmap_select_device(d_cameras.data_ptr(), n, _ivec3(root_min), int(root_size),
                                                   d_out.data_ptr(), int(stride), d_counts.data_ptr(),
                                                   C.c_void_p(s.cuda_stream)), "lvn_clipmap_select_device")
+
+
+def seam_generate(chunks, seam_offsets, seams, voxels_per_chunk, root_min, root_size, hosts,
+                  colour=(1.0, 1.0, 1.0)):
+    """GenerateClipmapSeamMesh (clipmap.cpp:573-610) for every host in `hosts`
+    (indices into `chunks`, the clipmap's active nodes as (min_xyz, size)).
+    `seams`: (S, 12) int32 SeamNodeInfo rows (host) or a torch int32 CUDA
+    tensor of the same shape; chunk c's rows are seams[seam_offsets[c] ..
+    seam_offsets[c + 1]).  Returns (vertices (V, 12) f32, triangles (T, 3)
+    i32, results (H, 8) i32 as lvn_chunk_result)."""
+    n = len(chunks)
+    descs = (ChunkDesc * max(1, n))()
+    for i, (mn, size) in enumerate(chunks):
+        descs[i] = ChunkDesc((C.c_int32 * 3)(*[int(v) for v in mn]), int(size))
+    offs = np.ascontiguousarray(np.asarray(seam_offsets, np.int32))
+    hs = np.ascontiguousarray(np.asarray(hosts, np.int32))
+    if isinstance(seams, np.ndarray):
+        sp = np.ascontiguousarray(seams.astype(np.int32, copy=False))
+        ptr, mem = sp.ctypes.data, LVN_MEMORY_HOST
+    else:
+        ptr, mem = seams.data_ptr(), LVN_MEMORY_DEVICE
+    results = (ChunkResult * max(1, len(hs)))()
+    cap_v, cap_t = 1 << 16, 1 << 17
+    while True:
+        v = np.zeros((cap_v, 12), np.float32)
+        t = np.zeros((cap_t, 3), np.int32)
+        bo = BatchOut(LVN_MEMORY_HOST, v.ctypes.data, cap_v, 0, t.ctypes.data, cap_t, 0, None, 0, 0,
+                      C.cast(results, C.POINTER(ChunkResult)))
+        rc = lib().lvn_seam_generate(descs, offs.ctypes.data, n, ptr, mem, int(voxels_per_chunk), _ivec3(root_min),
+                                     int(root_size), hs.ctypes.data, len(hs), (C.c_float * 3)(*colour), C.byref(bo))
+        if rc == LVN_ERR_CAPACITY:
+            cap_v, cap_t = max(cap_v, int(bo.total_vertices)), max(cap_t, int(bo.total_triangles))
+            continue
+        _check(rc, "lvn_seam_generate")
+        res = np.ctypeslib.as_array(C.cast(results, C.POINTER(C.c_int32)), shape=(max(1, len(hs)), 8))[:len(hs)]
+        return v[:bo.total_vertices].copy(), t[:bo.total_triangles].copy(), res.copy()
 
 
 def clipmap_touched(ops, root_min, root_size):

@@ -1,0 +1,795 @@
+// lvn_seam.cu -- the clipmap's seam meshes on the GPU: GenerateClipmapSeamMesh
+// (leven/src/clipmap.cpp:573-610) for a batch of host chunks.  The reference
+// gathers the seam nodes of a host and of the active nodes next to it
+// (SelectSeamNodes / FilterSeamNode, clipmap.cpp:508-570), builds a pointer
+// octree from them (Octree_ConstructUpwards, octree.cpp:90-148), numbers its
+// leaves depth first (GenerateVertexIndices, octree.cpp:197-232) and contours
+// it recursively (ContourCellProc / ContourFaceProc / ContourEdgeProc /
+// ContourProcessEdge, octree.cpp:236-474) on the CPU.
+//
+// Here the neighbour search, which walks the clipmap's node tree, stays on the
+// host; everything that touches seam nodes runs on the device, one CTA per
+// host, without building the tree:
+//   * the depth-first leaf order is the Morton order of the leaves' minimum
+//     corners (children are visited x << 2 | y << 1 | z), so the leaves are
+//     sorted by Morton key in shared memory and numbered by rank;
+//   * the recursion emits one quad per final edge segment: an edge of the
+//     smallest of the four leaves around it, all four present, not all four
+//     in one CLIPMAP_LEAF_SIZE block (the straddle test of ContourEdgeProc /
+//     ContourFaceProc prunes exactly those), with a sign change on that
+//     leaf's edge.  Each leaf tests its 12 edges; the other three leaves come
+//     from binary searches of the sorted keys;
+//   * the recursion's order is restored by a key spelling the path the
+//     recursion takes to the segment (cell: child 0-7, face 8-19, edge 20-25
+//     in 5 bits; face: sub-face 0-3, edge 4-7 in 3 bits; edge: half in 1 bit),
+//     by which the quads are sorted.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
+
+#include "../../include/lvn.h"
+#include "lvn_types.h"
+
+namespace lvn {
+namespace {
+
+constexpr int kMaxLeaves = LVN_SEAM_MAX_LEAVES;  // per host
+constexpr int kMaxQuads = LVN_SEAM_MAX_QUADS;    // per host
+constexpr int kSlotBits = 14;                    // leaf sort entry: (morton << 4 | size log2) << 14 | slot
+constexpr int kRankBits = 13;                    // quad payload: 4 ranks of 13 bits, flip at bit 52
+static_assert(kMaxLeaves <= (1 << kRankBits) && kMaxLeaves <= (1 << kSlotBits), "rank bits");
+constexpr int kMaxLevels = 12;  // log2(2 host size / smallest leaf): path keys of 5 bits per level fit 64 bits
+constexpr int kBuildThreads = 512;
+constexpr size_t kBuildSmem = (size_t)kMaxLeaves * (8 + 4) + (size_t)kMaxQuads * 16;
+
+// the dual-contouring tables of contour_constants.h, as the reference's
+// recursion uses them (its output order depends on them)
+__constant__ int8_t cEdgeVMap[12][2] = {{0, 4}, {1, 5}, {2, 6}, {3, 7}, {0, 2}, {1, 3},
+                                        {4, 6}, {5, 7}, {0, 1}, {2, 3}, {4, 5}, {6, 7}};
+__constant__ int8_t cCellProcFaceMask[12][3] = {{0, 4, 0}, {1, 5, 0}, {2, 6, 0}, {3, 7, 0}, {0, 2, 1}, {4, 6, 1},
+                                                {1, 3, 1}, {5, 7, 1}, {0, 1, 2}, {2, 3, 2}, {4, 5, 2}, {6, 7, 2}};
+__constant__ int8_t cCellProcEdgeMask[6][5] = {{0, 1, 2, 3, 0}, {4, 5, 6, 7, 0}, {0, 4, 1, 5, 1},
+                                               {2, 6, 3, 7, 1}, {0, 2, 4, 6, 2}, {1, 3, 5, 7, 2}};
+__constant__ int8_t cFaceProcFaceMask[3][4][3] = {{{4, 0, 0}, {5, 1, 0}, {6, 2, 0}, {7, 3, 0}},
+                                                  {{2, 0, 1}, {6, 4, 1}, {3, 1, 1}, {7, 5, 1}},
+                                                  {{1, 0, 2}, {3, 2, 2}, {5, 4, 2}, {7, 6, 2}}};
+__constant__ int8_t cFaceProcEdgeMask[3][4][6] = {
+    {{1, 4, 0, 5, 1, 1}, {1, 6, 2, 7, 3, 1}, {0, 4, 6, 0, 2, 2}, {0, 5, 7, 1, 3, 2}},
+    {{0, 2, 3, 0, 1, 0}, {0, 6, 7, 4, 5, 0}, {1, 2, 0, 6, 4, 2}, {1, 3, 1, 7, 5, 2}},
+    {{1, 1, 0, 3, 2, 0}, {1, 5, 4, 7, 6, 0}, {0, 1, 5, 0, 4, 1}, {0, 3, 7, 2, 6, 1}}};
+__constant__ int8_t cProcessEdgeMask[3][4] = {{3, 2, 1, 0}, {7, 5, 6, 4}, {11, 10, 9, 8}};
+
+__device__ __forceinline__ int cbit(int child, int axis) { return (child >> (2 - axis)) & 1; }
+
+struct SeamHost {
+    int32_t min[3];
+    int32_t size;
+    int32_t unit;        // smallest leaf size among the gathered chunks
+    int32_t lev;         // log2(2 size / unit)
+    int32_t pair_begin;  // gathered (chunk, neighbour mask) pairs
+    int32_t pair_end;
+    int64_t leaf_off;    // sorted seam indices, filled by the build
+    int64_t quad_off;    // quads (12 per leaf at most), filled by the build
+};
+
+struct SeamArgs {
+    const SeamHost* hosts;
+    const int2* pairs;            // (chunk, mask of neighbour indices 0-7)
+    const int4* chunks;           // (min xyz, size)
+    const int32_t* seam_offsets;  // [num_chunks + 1]
+    const lvn_seam_node* seams;
+    int vpc;
+    int32_t* counts;    // leaves per host (count kernel)
+    int32_t* qcounts;   // quads per host, -1: over a limit (build kernel)
+    uint32_t* leaves;   // sorted seam indices
+    uint64_t* quads;    // sorted quad payloads
+    // emit
+    const int64_t* vout_off;
+    const int64_t* tout_off;
+    lvn_mesh_vertex* vout;
+    lvn_mesh_triangle* tout;
+    float colour[3];
+};
+
+// FilterSeamNode (clipmap.cpp:508-538)
+__device__ __forceinline__ bool filter_seam_node(int child, const int32_t b[3], const int32_t mn[3],
+                                                 const int32_t mx[3]) {
+    switch (child) {
+        case 0: return mx[0] == b[0] || mx[1] == b[1] || mx[2] == b[2];
+        case 1: return mn[2] == b[2];
+        case 2: return mn[1] == b[1];
+        case 3: return mn[1] == b[1] || mn[2] == b[2];
+        case 4: return mn[0] == b[0];
+        case 5: return mn[0] == b[0] || mn[2] == b[2];
+        case 6: return mn[0] == b[0] || mn[1] == b[1];
+        default: return mn[0] == b[0] && mn[1] == b[1] && mn[2] == b[2];
+    }
+}
+
+// SelectSeamNodes (clipmap.cpp:542-570): is seam node k of `chunk` one of the
+// host's, for any of the neighbour indices in `mask`?  A chunk reached through
+// several neighbour indices is tested once with all of them (the reference
+// may list such a node twice; the octree it builds holds it once).
+__device__ __forceinline__ bool seam_selected(const SeamHost& h, int4 chunk, int mask, const lvn_seam_node& s,
+                                              int vpc, int32_t mn[3]) {
+    const int node_size = chunk.w / vpc;
+    const int extent = (chunk.w / (vpc * 4)) * 4;  // size * LEAF_SIZE_SCALE (clipmap.cpp:553-560)
+    mn[0] = s.localspace_min[0] * node_size + chunk.x;
+    mn[1] = s.localspace_min[1] * node_size + chunk.y;
+    mn[2] = s.localspace_min[2] * node_size + chunk.z;
+    for (int a = 0; a < 3; a++)
+        if (mn[a] < h.min[a] || mn[a] >= h.min[a] + 2 * h.size) return false;  // AABB::pointIsInside
+    const int32_t b[3] = {h.min[0] + h.size, h.min[1] + h.size, h.min[2] + h.size};
+    const int32_t mx[3] = {mn[0] + extent, mn[1] + extent, mn[2] + extent};
+    for (int i = 0; i < 8; i++)
+        if (((mask >> i) & 1) && filter_seam_node(i, b, mn, mx)) return true;
+    return false;
+}
+
+__device__ __forceinline__ uint64_t spread3(uint32_t v, int lev) {
+    uint64_t r = 0;
+    for (int bit = lev - 1; bit >= 0; bit--) r = (r << 3) | ((v >> bit) & 1);
+    return r;
+}
+
+__device__ __forceinline__ uint64_t morton(const int32_t rel[3], int unit_log, int lev) {
+    return (spread3((uint32_t)(rel[0] >> unit_log), lev) << 2) | (spread3((uint32_t)(rel[1] >> unit_log), lev) << 1) |
+           spread3((uint32_t)(rel[2] >> unit_log), lev);
+}
+
+__device__ __forceinline__ void unmorton(uint64_t code, int lev, int unit_log, int32_t rel[3]) {
+    int32_t p[3] = {0, 0, 0};
+    for (int bit = lev - 1; bit >= 0; bit--) {
+        const int t = (int)((code >> (3 * bit)) & 7);
+        p[0] = (p[0] << 1) | ((t >> 2) & 1);
+        p[1] = (p[1] << 1) | ((t >> 1) & 1);
+        p[2] = (p[2] << 1) | (t & 1);
+    }
+    for (int a = 0; a < 3; a++) rel[a] = p[a] << unit_log;
+}
+
+__global__ void __launch_bounds__(256) k_seam_count(SeamArgs A) {
+    const SeamHost h = A.hosts[blockIdx.x];
+    int n = 0;
+    for (int p = h.pair_begin; p < h.pair_end; p++) {
+        const int2 pr = A.pairs[p];
+        const int4 ch = A.chunks[pr.x];
+        const int s0 = A.seam_offsets[pr.x], s1 = A.seam_offsets[pr.x + 1];
+        for (int k = s0 + threadIdx.x; k < s1; k += blockDim.x) {
+            int32_t mn[3];
+            n += seam_selected(h, ch, pr.y, A.seams[k], A.vpc, mn);
+        }
+    }
+    __shared__ int s_n;
+    if (threadIdx.x == 0) s_n = 0;
+    __syncthreads();
+    for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&s_n, n);
+    __syncthreads();
+    if (threadIdx.x == 0) A.counts[blockIdx.x] = s_n;
+}
+
+// bitonic sort of n entries (keys, with an optional payload moved alongside)
+template <bool Pair>
+__device__ void block_sort(uint64_t* key, uint64_t* val, int n) {
+    int p2 = 1;
+    while (p2 < n) p2 <<= 1;
+    for (int i = n + threadIdx.x; i < p2; i += blockDim.x) {
+        key[i] = ~0ull;
+        if (Pair) val[i] = 0;
+    }
+    __syncthreads();
+    for (int k = 2; k <= p2; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < p2; i += blockDim.x) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const uint64_t a = key[i], b = key[l];
+                    if (((i & k) == 0) == (a > b)) {
+                        key[i] = b;
+                        key[l] = a;
+                        if (Pair) {
+                            const uint64_t t = val[i];
+                            val[i] = val[l];
+                            val[l] = t;
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+struct LeafView {
+    const uint64_t* ent;  // sorted entries
+    int n;
+    int lev, unit_log;
+    int32_t hmin[3];
+    int32_t root;  // 2 host size
+};
+
+__device__ __forceinline__ uint64_t ent_code(uint64_t e) { return e >> (kSlotBits + 4); }
+__device__ __forceinline__ int ent_size_log(uint64_t e) { return (int)((e >> kSlotBits) & 15); }
+
+// The leaf covering the region (min rel, size 1 << size_log units): its rank,
+// -1 when nothing is there (a null child in the reference's tree), -2 when the
+// region is subdivided (smaller leaves inside).
+__device__ int find_leaf(const LeafView& v, const int32_t rel[3], int size_log) {
+    for (int a = 0; a < 3; a++)
+        if (rel[a] < 0 || rel[a] >= v.root) return -1;
+    const uint64_t k = morton(rel, v.unit_log, v.lev);
+    const uint64_t vol = 1ull << (3 * size_log);
+    int lo = 0, hi = v.n;  // first entry with code >= k
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (ent_code(v.ent[mid]) < k)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    if (lo < v.n && ent_code(v.ent[lo]) < k + vol) {
+        if (ent_code(v.ent[lo]) == k && ent_size_log(v.ent[lo]) >= size_log) return lo;
+        return -2;
+    }
+    if (lo > 0) {  // a larger leaf before it in Morton order may contain the region
+        const uint64_t e = v.ent[lo - 1];
+        const int sl = ent_size_log(e);
+        if (sl > size_log && (k >> (3 * sl)) == (ent_code(e) >> (3 * sl))) return lo - 1;
+    }
+    return -1;
+}
+
+// The path of the reference's recursion (ContourCellProc from the seam
+// octree's root) to the final segment along `dir` at line coordinates line[]
+// (host-relative), starting at t0 along dir, `len` long.
+__device__ uint64_t path_key(int32_t root, int dir, const int32_t line[3], int32_t t0, int32_t len) {
+    uint64_t key = 0;
+    int nbits = 0;
+    auto put = [&](int digit, int width) {
+        nbits += width;
+        key |= (uint64_t)digit << (64 - nbits);
+    };
+    const int a1 = dir == 0 ? 1 : 0, a2 = dir == 2 ? 1 : 2;
+    int32_t m[3] = {0, 0, 0};
+    int32_t S = root;
+    int32_t e0 = 0, es = 0;  // edge state: start along dir, length
+    for (;;) {  // cell
+        const int32_t h = S >> 1;
+        const int32_t mid[3] = {m[0] + h, m[1] + h, m[2] + h};
+        const bool on1 = line[a1] == mid[a1], on2 = line[a2] == mid[a2];
+        const int hd = t0 >= mid[dir];
+        if (!on1 && !on2) {
+            int c = hd << (2 - dir);
+            c |= (line[a1] > mid[a1]) << (2 - a1);
+            c |= (line[a2] > mid[a2]) << (2 - a2);
+            put(c, 5);
+            for (int a = 0; a < 3; a++) m[a] += cbit(c, a) * h;
+            S = h;
+            continue;
+        }
+        if (on1 && on2) {
+            int e = 0;
+            for (int i = 0; i < 6; i++)
+                if (cCellProcEdgeMask[i][4] == dir && cbit(cCellProcEdgeMask[i][0], dir) == hd) e = i;
+            put(20 + e, 5);
+            e0 = m[dir] + hd * h;
+            es = h;
+            break;
+        }
+        const int a = on1 ? a1 : a2, b = on1 ? a2 : a1;
+        const int bs = line[b] > mid[b];
+        const int c0 = (bs << (2 - b)) | (hd << (2 - dir)), c1 = c0 | (1 << (2 - a));
+        int f = 0;
+        for (int i = 0; i < 12; i++)
+            if (cCellProcFaceMask[i][0] == c0 && cCellProcFaceMask[i][1] == c1) f = i;
+        put(8 + f, 5);
+        int32_t fb = m[b] + bs * h, fd = m[dir] + hd * h, fs = h;
+        for (;;) {  // face, plane perpendicular to a
+            const int32_t hh = fs >> 1;
+            const int fhd = t0 >= fd + hh;
+            if (line[b] != fb + hh) {
+                const int fbs = line[b] > fb + hh;
+                int i4 = 0;
+                for (int i = 0; i < 4; i++) {
+                    const int c = cFaceProcFaceMask[a][i][1];
+                    if (cbit(c, b) == fbs && cbit(c, dir) == fhd) i4 = i;
+                }
+                put(i4, 3);
+                fb += fbs * hh;
+                fd += fhd * hh;
+                fs = hh;
+                continue;
+            }
+            int i4 = 0;
+            for (int i = 0; i < 4; i++)
+                if (cFaceProcEdgeMask[a][i][5] == dir && cbit(cFaceProcEdgeMask[a][i][1], dir) == fhd) i4 = i;
+            put(4 + i4, 3);
+            e0 = fd + fhd * hh;
+            es = hh;
+            break;
+        }
+        break;
+    }
+    while (es > len) {  // edge: halves along dir
+        const int32_t eh = es >> 1;
+        const int hf = t0 >= e0 + eh;
+        put(hf, 1);
+        e0 += hf * eh;
+        es = eh;
+    }
+    return key;
+}
+
+__global__ void __launch_bounds__(kBuildThreads) k_seam_build(SeamArgs A) {
+    extern __shared__ uint64_t smem[];
+    uint64_t* ent = smem;                                    // [kMaxLeaves]
+    uint32_t* gidx = (uint32_t*)(smem + kMaxLeaves);         // [kMaxLeaves] seam index per slot
+    uint64_t* qkey = smem + kMaxLeaves + kMaxLeaves / 2;     // [kMaxQuads]
+    uint64_t* qval = qkey + kMaxQuads;                       // [kMaxQuads]
+    __shared__ int s_n, s_q, s_over;
+    const SeamHost h = A.hosts[blockIdx.x];
+    int unit_log = 0;
+    while ((1 << unit_log) < h.unit) unit_log++;
+    if (threadIdx.x == 0) {
+        s_n = s_q = 0;
+        s_over = 0;
+    }
+    __syncthreads();
+    // the host's leaves
+    for (int p = h.pair_begin; p < h.pair_end; p++) {
+        const int2 pr = A.pairs[p];
+        const int4 ch = A.chunks[pr.x];
+        int size_log = 0;
+        while ((h.unit << size_log) < ch.w / A.vpc) size_log++;
+        const int s0 = A.seam_offsets[pr.x], s1 = A.seam_offsets[pr.x + 1];
+        for (int k = s0 + threadIdx.x; k < s1; k += blockDim.x) {
+            int32_t mn[3];
+            if (!seam_selected(h, ch, pr.y, A.seams[k], A.vpc, mn)) continue;
+            const int slot = atomicAdd(&s_n, 1);
+            if (slot >= kMaxLeaves) {
+                s_over = 1;
+                continue;
+            }
+            const int32_t rel[3] = {mn[0] - h.min[0], mn[1] - h.min[1], mn[2] - h.min[2]};
+            ent[slot] = ((morton(rel, unit_log, h.lev) << 4 | (uint64_t)size_log) << kSlotBits) | (uint64_t)slot;
+            gidx[slot] = (uint32_t)k;
+        }
+    }
+    __syncthreads();
+    if (s_over) {
+        if (threadIdx.x == 0) A.qcounts[blockIdx.x] = -1;
+        return;
+    }
+    const int n = s_n;
+    block_sort<false>(ent, nullptr, n);
+    for (int r = threadIdx.x; r < n; r += blockDim.x)
+        A.leaves[h.leaf_off + r] = gidx[ent[r] & ((1u << kSlotBits) - 1)];
+    // quads: each leaf's 12 edges
+    LeafView v;
+    v.ent = ent;
+    v.n = n;
+    v.lev = h.lev;
+    v.unit_log = unit_log;
+    v.root = 2 * h.size;
+    for (int a = 0; a < 3; a++) v.hmin[a] = h.min[a];
+    for (int item = threadIdx.x; item < n * 12; item += blockDim.x) {
+        const int r = item / 12, e = item - 12 * (item / 12);
+        const uint64_t me = ent[r];
+        const int corners = A.seams[gidx[me & ((1u << kSlotBits) - 1)]].localspace_min[3] & 0xff;
+        const int c0 = cEdgeVMap[e][0], c1 = cEdgeVMap[e][1];
+        const int m0 = (corners >> c0) & 1, m1 = (corners >> c1) & 1;
+        if (m0 == m1) continue;  // no sign change on the edge of the smallest leaf: no quad
+        const int dir = e >> 2;
+        int j = 0;
+        for (int q = 0; q < 4; q++)
+            if (cProcessEdgeMask[dir][q] == e) j = q;
+        const int sl = ent_size_log(me);
+        const int32_t s = h.unit << sl;
+        int32_t lmin[3];
+        unmorton(ent_code(me), h.lev, unit_log, lmin);
+        int32_t line[3];
+        for (int a = 0; a < 3; a++) line[a] = lmin[a] + cbit(c0, a) * s;
+        const int slot_entry = dir * 2;  // cellProcEdgeMask entry whose children give the slots' sides
+        int rank[4];
+        bool ok = true;
+        for (int q = 0; q < 4 && ok; q++) {
+            if (q == j) {
+                rank[q] = r;
+                continue;
+            }
+            const int child = cCellProcEdgeMask[slot_entry][q];
+            int32_t rel[3];
+            for (int a = 0; a < 3; a++) rel[a] = a == dir ? lmin[a] : line[a] - s + cbit(child, a) * s;
+            rank[q] = find_leaf(v, rel, sl);
+            ok = rank[q] >= 0;
+        }
+        if (!ok) continue;
+        int min_index = 0, min_log = 64;  // ContourProcessEdge: the first of the smallest leaves
+        for (int q = 0; q < 4; q++) {
+            const int lq = ent_size_log(ent[rank[q]]);
+            if (lq < min_log) {
+                min_log = lq;
+                min_index = q;
+            }
+        }
+        if (min_index != j) continue;  // that leaf's edge is this segment: it emits the quad
+        // the straddle test: not all four leaves in one CLIPMAP_LEAF_SIZE block
+        bool one_block = true;
+        int32_t b0[3];
+        for (int q = 0; q < 4; q++) {
+            int32_t rel[3];
+            unmorton(ent_code(ent[rank[q]]), h.lev, unit_log, rel);
+            for (int a = 0; a < 3; a++) {
+                const int32_t blk = (int32_t)((uint32_t)(rel[a] + h.min[a]) & ~(uint32_t)(CLIPMAP_LEAF_SIZE - 1));
+                if (q == 0)
+                    b0[a] = blk;
+                else
+                    one_block &= blk == b0[a];
+            }
+        }
+        if (one_block) continue;
+        const uint64_t key = path_key(2 * h.size, dir, line, lmin[dir], s);
+        const int qi = atomicAdd(&s_q, 1);
+        if (qi >= kMaxQuads) {
+            s_over = 1;
+            continue;
+        }
+        qkey[qi] = key;
+        qval[qi] = (uint64_t)rank[0] | ((uint64_t)rank[1] << kRankBits) | ((uint64_t)rank[2] << (2 * kRankBits)) |
+                   ((uint64_t)rank[3] << (3 * kRankBits)) | ((uint64_t)(m1 != 1) << (4 * kRankBits));
+    }
+    __syncthreads();
+    if (s_over) {
+        if (threadIdx.x == 0) A.qcounts[blockIdx.x] = -1;
+        return;
+    }
+    const int nq = s_q;
+    block_sort<true>(qkey, qval, nq);
+    for (int i = threadIdx.x; i < nq; i += blockDim.x) A.quads[h.quad_off + i] = qval[i];
+    if (threadIdx.x == 0) A.qcounts[blockIdx.x] = nq;
+}
+
+// vertices (hosts with triangles only) and triangles, back to back by host
+__global__ void __launch_bounds__(256) k_seam_emit(SeamArgs A) {
+    const SeamHost h = A.hosts[blockIdx.x];
+    const int nq = A.qcounts[blockIdx.x];
+    if (nq <= 0) return;
+    const int n = A.counts[blockIdx.x];
+    const int64_t vo = A.vout_off[blockIdx.x], to = A.tout_off[blockIdx.x];
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+        const lvn_seam_node s = A.seams[A.leaves[h.leaf_off + r]];
+        lvn_mesh_vertex v;
+        for (int a = 0; a < 3; a++) {
+            v.position[a] = s.position[a];
+            v.normal[a] = s.normal[a];
+            v.colour[a] = A.colour[a];
+        }
+        v.position[3] = 0.f;
+        v.normal[3] = 0.f;
+        v.colour[3] = (float)(s.localspace_min[3] >> 8);
+        A.vout[vo + r] = v;
+    }
+    const uint64_t mask = (1ull << kRankBits) - 1;
+    for (int i = threadIdx.x; i < nq; i += blockDim.x) {
+        const uint64_t q = A.quads[h.quad_off + i];
+        const int i0 = (int)(q & mask), i1 = (int)((q >> kRankBits) & mask), i2 = (int)((q >> (2 * kRankBits)) & mask),
+                  i3 = (int)((q >> (3 * kRankBits)) & mask);
+        const bool flip = (q >> (4 * kRankBits)) & 1;
+        lvn_mesh_triangle t0, t1;
+        if (!flip) {
+            t0 = {{i0, i1, i3}};
+            t1 = {{i0, i3, i2}};
+        } else {
+            t0 = {{i0, i3, i1}};
+            t1 = {{i0, i2, i3}};
+        }
+        A.tout[to + 2 * i] = t0;
+        A.tout[to + 2 * i + 1] = t1;
+    }
+}
+
+// ---- host side -----------------------------------------------------------
+
+template <class T, bool Host = false>
+struct Grow {
+    T* p = nullptr;
+    size_t cap = 0;
+    cudaError_t fit(size_t need) {
+        if (need <= cap) return cudaSuccess;
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) return e;
+        need = std::max(need, 2 * cap);
+        if (p) Host ? cudaFreeHost(p) : cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        e = Host ? cudaMallocHost(&p, sizeof(T) * need) : cudaMalloc(&p, sizeof(T) * need);
+        if (e == cudaSuccess) cap = need;
+        return e;
+    }
+};
+
+struct SeamWork {
+    std::mutex mu;
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    Grow<SeamHost> hosts;
+    Grow<int2> pairs;
+    Grow<int4> chunks;
+    Grow<int32_t> seam_offsets, counts, qcounts;
+    Grow<lvn_seam_node> seams;
+    Grow<uint32_t> leaves;
+    Grow<uint64_t> quads;
+    Grow<int64_t> offs;  // vertex offsets, triangle offsets
+    Grow<lvn_mesh_vertex> vstage;
+    Grow<lvn_mesh_triangle> tstage;
+    Grow<int32_t, true> hcounts;  // pinned: counts, qcounts
+};
+SeamWork& seam_work() {
+    static SeamWork w;
+    return w;
+}
+
+int cuda_rc(cudaError_t e) {
+    if (e == cudaSuccess) return LVN_OK;
+    cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? LVN_ERR_OUT_OF_MEMORY : LVN_ERR_CUDA;
+}
+
+#define SM_TRY(x)                        \
+    do {                                 \
+        const int rc__ = cuda_rc(x);     \
+        if (rc__ != LVN_OK) return rc__; \
+    } while (0)
+
+struct Key4Hash {
+    size_t operator()(const std::array<int32_t, 4>& k) const {
+        uint64_t h = 1469598103934665603ull;
+        for (int32_t v : k) h = (h ^ (uint32_t)v) * 1099511628211ull;
+        return (size_t)h;
+    }
+};
+
+// The clipmap's active nodes (the chunks) and the nodes above them, keyed by
+// (min, size); FindNode / FindActiveNodes (clipmap.cpp:982-1013, 1449-1479)
+// over the complete octree rooted at (root_min, root_size).
+struct ActiveSet {
+    int32_t root_min[3];
+    int32_t root_size;
+    std::unordered_map<std::array<int32_t, 4>, int, Key4Hash> active;
+    std::unordered_set<std::array<int32_t, 4>, Key4Hash> above;  // nodes with an active node below them
+
+    bool in_root(const int32_t mn[3], int32_t size) const {
+        for (int a = 0; a < 3; a++) {
+            const int64_t rel = (int64_t)mn[a] - root_min[a];
+            if (rel < 0 || rel + size > root_size || rel % size) return false;
+        }
+        return true;
+    }
+    // the active nodes FindActiveNodes lists for the node (mn, size)
+    void find_active(const int32_t mn[3], int32_t size, std::vector<int>& out) const {
+        // an active node containing mn (the node itself or above it)
+        for (int32_t s = size; s <= root_size; s *= 2) {
+            int32_t a[3];
+            for (int k = 0; k < 3; k++) a[k] = root_min[k] + (int32_t)(((int64_t)mn[k] - root_min[k]) / s * s);
+            auto it = active.find({a[0], a[1], a[2], s});
+            if (it != active.end()) {
+                out.push_back(it->second);
+                return;
+            }
+        }
+        descend(mn, size, out);
+    }
+    void descend(const int32_t mn[3], int32_t size, std::vector<int>& out) const {
+        if (size <= CLIPMAP_LEAF_SIZE || !above.count({mn[0], mn[1], mn[2], size})) return;
+        const int32_t h = size / 2;
+        for (int i = 0; i < 8; i++) {
+            const int32_t c[3] = {mn[0] + ((i >> 2) & 1) * h, mn[1] + ((i >> 1) & 1) * h, mn[2] + (i & 1) * h};
+            auto it = active.find({c[0], c[1], c[2], h});
+            if (it != active.end())
+                out.push_back(it->second);
+            else
+                descend(c, h, out);
+        }
+    }
+};
+
+}  // namespace
+}  // namespace lvn
+
+using namespace lvn;
+
+extern "C" {
+
+int lvn_seam_generate(const lvn_chunk_desc* chunks, const int32_t* seam_offsets, int32_t num_chunks,
+                      const lvn_seam_node* seams, int32_t seams_memory, int32_t voxels_per_chunk,
+                      const int32_t root_min[3], int32_t root_size, const int32_t* hosts, int32_t num_hosts,
+                      const float colour[3], lvn_batch_out* out) {
+    if (!out || !root_min || !colour || num_chunks < 0 || num_hosts < 0 || (num_chunks > 0 && (!chunks || !seam_offsets)) ||
+        (num_hosts > 0 && !hosts) || voxels_per_chunk < 8 || voxels_per_chunk > 64 ||
+        (voxels_per_chunk & (voxels_per_chunk - 1)) || (seams_memory != LVN_MEMORY_HOST && seams_memory != LVN_MEMORY_DEVICE) ||
+        (out->memory != LVN_MEMORY_HOST && out->memory != LVN_MEMORY_DEVICE) || (num_hosts > 0 && !out->chunks))
+        return LVN_ERR_INVALID;
+    if (root_size < CLIPMAP_LEAF_SIZE || (root_size & (root_size - 1))) return LVN_ERR_INVALID;
+    const int vpc = voxels_per_chunk;
+    ActiveSet act;
+    for (int a = 0; a < 3; a++) act.root_min[a] = root_min[a];
+    act.root_size = root_size;
+    for (int c = 0; c < num_chunks; c++) {
+        const lvn_chunk_desc& d = chunks[c];
+        if (d.size < CLIPMAP_LEAF_SIZE || (d.size & (d.size - 1)) || !act.in_root(d.min, d.size) ||
+            seam_offsets[c + 1] < seam_offsets[c])
+            return LVN_ERR_INVALID;
+        act.active[{d.min[0], d.min[1], d.min[2], d.size}] = c;
+        for (int32_t s = d.size * 2; s <= root_size; s *= 2) {
+            int32_t a[3];
+            for (int k = 0; k < 3; k++) a[k] = root_min[k] + (int32_t)(((int64_t)d.min[k] - root_min[k]) / s * s);
+            if (!act.above.insert({a[0], a[1], a[2], s}).second) break;
+        }
+    }
+    const int64_t num_seams = num_chunks ? seam_offsets[num_chunks] : 0;
+    if (seam_offsets && num_chunks && seam_offsets[0] != 0) return LVN_ERR_INVALID;
+    // the gathered (chunk, neighbour mask) pairs of every host
+    std::vector<SeamHost> hv(num_hosts);
+    std::vector<int2> pairs;
+    for (int hi = 0; hi < num_hosts; hi++) {
+        if (hosts[hi] < 0 || hosts[hi] >= num_chunks) return LVN_ERR_INVALID;
+        const lvn_chunk_desc& d = chunks[hosts[hi]];
+        SeamHost& h = hv[hi];
+        for (int a = 0; a < 3; a++) h.min[a] = d.min[a];
+        h.size = d.size;
+        h.pair_begin = (int32_t)pairs.size();
+        std::vector<std::pair<int, int>> found;  // (chunk, neighbour index)
+        for (int i = 0; i < 8; i++) {
+            const int32_t nmin[3] = {d.min[0] + ((i >> 2) & 1) * d.size, d.min[1] + ((i >> 1) & 1) * d.size,
+                                     d.min[2] + (i & 1) * d.size};
+            if (!act.in_root(nmin, d.size)) continue;  // Clipmap::findNode finds no node there
+            std::vector<int> cs;
+            act.find_active(nmin, d.size, cs);
+            for (int c : cs) found.push_back({c, i});
+        }
+        std::sort(found.begin(), found.end());
+        int unit = d.size / vpc;
+        for (size_t k = 0; k < found.size();) {
+            int mask = 0;
+            const int c = found[k].first;
+            for (; k < found.size() && found[k].first == c; k++) mask |= 1 << found[k].second;
+            pairs.push_back(make_int2(c, mask));
+            unit = std::min(unit, chunks[c].size / vpc);
+        }
+        h.pair_end = (int32_t)pairs.size();
+        h.unit = unit;
+        h.lev = 0;
+        while ((unit << h.lev) < 2 * d.size) h.lev++;
+        if (h.lev > kMaxLevels) return LVN_ERR_INVALID;
+    }
+    SeamWork& w = seam_work();
+    std::lock_guard<std::mutex> lock(w.mu);
+    int dev = 0;
+    SM_TRY(cudaGetDevice(&dev));
+    if (w.device != dev) {
+        if (w.device >= 0) return LVN_ERR_INVALID;  // the scratch lives on the first device used
+        SM_TRY(cudaStreamCreateWithFlags(&w.stream, cudaStreamNonBlocking));
+        SM_TRY(cudaFuncSetAttribute(k_seam_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBuildSmem));
+        w.device = dev;
+    }
+    if (num_hosts == 0) {
+        out->total_vertices = out->total_triangles = out->total_seams = 0;
+        return LVN_OK;
+    }
+    const size_t nh = (size_t)num_hosts;
+    SM_TRY(w.hosts.fit(nh));
+    SM_TRY(w.pairs.fit(std::max<size_t>(pairs.size(), 1)));
+    SM_TRY(w.chunks.fit(std::max(num_chunks, 1)));
+    SM_TRY(w.seam_offsets.fit((size_t)num_chunks + 1));
+    SM_TRY(w.counts.fit(nh));
+    SM_TRY(w.qcounts.fit(nh));
+    SM_TRY(w.offs.fit(2 * nh));
+    SM_TRY(w.hcounts.fit(2 * nh));
+    std::vector<int4> c4(std::max(num_chunks, 1));
+    for (int c = 0; c < num_chunks; c++)
+        c4[c] = make_int4(chunks[c].min[0], chunks[c].min[1], chunks[c].min[2], chunks[c].size);
+    cudaStream_t st = w.stream;
+    SM_TRY(cudaMemcpyAsync(w.pairs.p, pairs.data(), sizeof(int2) * pairs.size(), cudaMemcpyHostToDevice, st));
+    SM_TRY(cudaMemcpyAsync(w.chunks.p, c4.data(), sizeof(int4) * num_chunks, cudaMemcpyHostToDevice, st));
+    SM_TRY(cudaMemcpyAsync(w.seam_offsets.p, seam_offsets, sizeof(int32_t) * (num_chunks + 1), cudaMemcpyHostToDevice,
+                           st));
+    const lvn_seam_node* dseams = seams;
+    if (seams_memory == LVN_MEMORY_HOST && num_seams > 0) {
+        SM_TRY(w.seams.fit((size_t)num_seams));
+        SM_TRY(cudaMemcpyAsync(w.seams.p, seams, sizeof(lvn_seam_node) * num_seams, cudaMemcpyHostToDevice, st));
+        dseams = w.seams.p;
+    }
+    SeamArgs A;
+    std::memset(&A, 0, sizeof(A));
+    A.hosts = w.hosts.p;
+    A.pairs = w.pairs.p;
+    A.chunks = w.chunks.p;
+    A.seam_offsets = w.seam_offsets.p;
+    A.seams = dseams;
+    A.vpc = vpc;
+    A.counts = w.counts.p;
+    A.qcounts = w.qcounts.p;
+    for (int a = 0; a < 3; a++) A.colour[a] = colour[a];
+    // 1: leaves per host
+    SM_TRY(cudaMemcpyAsync(w.hosts.p, hv.data(), sizeof(SeamHost) * nh, cudaMemcpyHostToDevice, st));
+    k_seam_count<<<num_hosts, 256, 0, st>>>(A);
+    SM_TRY(cudaGetLastError());
+    SM_TRY(cudaMemcpyAsync(w.hcounts.p, w.counts.p, sizeof(int32_t) * nh, cudaMemcpyDeviceToHost, st));
+    SM_TRY(cudaStreamSynchronize(st));
+    int64_t leaf_total = 0, quad_total = 0;
+    bool limit = false;
+    for (size_t i = 0; i < nh; i++) {
+        const int n = w.hcounts.p[i];
+        limit |= n > kMaxLeaves;
+        hv[i].leaf_off = leaf_total;
+        hv[i].quad_off = quad_total;
+        leaf_total += n;
+        quad_total += std::min<int64_t>(12 * (int64_t)n, kMaxQuads);
+    }
+    if (limit) return LVN_ERR_DEVICE_STATUS;
+    // 2: sorted leaves and quads per host
+    SM_TRY(w.leaves.fit(std::max<int64_t>(leaf_total, 1)));
+    SM_TRY(w.quads.fit(std::max<int64_t>(quad_total, 1)));
+    A.leaves = w.leaves.p;
+    A.quads = w.quads.p;
+    SM_TRY(cudaMemcpyAsync(w.hosts.p, hv.data(), sizeof(SeamHost) * nh, cudaMemcpyHostToDevice, st));
+    k_seam_build<<<num_hosts, kBuildThreads, kBuildSmem, st>>>(A);
+    SM_TRY(cudaGetLastError());
+    SM_TRY(cudaMemcpyAsync(w.hcounts.p + nh, w.qcounts.p, sizeof(int32_t) * nh, cudaMemcpyDeviceToHost, st));
+    SM_TRY(cudaStreamSynchronize(st));
+    // 3: output layout: hosts with triangles, back to back
+    std::vector<int64_t> offs(2 * nh);
+    int64_t tv = 0, tt = 0;
+    for (size_t i = 0; i < nh; i++) {
+        const int nq = w.hcounts.p[nh + i];
+        if (nq < 0) return LVN_ERR_DEVICE_STATUS;
+        const int nv = nq > 0 ? w.hcounts.p[i] : 0;
+        lvn_chunk_result& r = out->chunks[i];
+        std::memset(&r, 0, sizeof(r));
+        r.vertex_offset = (int32_t)tv;
+        r.num_vertices = nv;
+        r.triangle_offset = (int32_t)tt;
+        r.num_triangles = 2 * nq;
+        r.num_nodes = w.hcounts.p[i];
+        offs[i] = tv;
+        offs[nh + i] = tt;
+        tv += nv;
+        tt += 2 * nq;
+    }
+    out->total_vertices = tv;
+    out->total_triangles = tt;
+    out->total_seams = 0;
+    if (tv > out->vertex_capacity || tt > out->triangle_capacity) return LVN_ERR_CAPACITY;
+    if (tt == 0) return LVN_OK;
+    if ((tv && !out->vertices) || (tt && !out->triangles)) return LVN_ERR_INVALID;
+    SM_TRY(cudaMemcpyAsync(w.offs.p, offs.data(), sizeof(int64_t) * 2 * nh, cudaMemcpyHostToDevice, st));
+    A.vout_off = w.offs.p;
+    A.tout_off = w.offs.p + nh;
+    if (out->memory == LVN_MEMORY_DEVICE) {
+        A.vout = out->vertices;
+        A.tout = out->triangles;
+    } else {
+        SM_TRY(w.vstage.fit((size_t)tv));
+        SM_TRY(w.tstage.fit((size_t)tt));
+        A.vout = w.vstage.p;
+        A.tout = w.tstage.p;
+    }
+    k_seam_emit<<<num_hosts, 256, 0, st>>>(A);
+    SM_TRY(cudaGetLastError());
+    if (out->memory == LVN_MEMORY_HOST) {
+        SM_TRY(cudaMemcpyAsync(out->vertices, w.vstage.p, sizeof(lvn_mesh_vertex) * tv, cudaMemcpyDeviceToHost, st));
+        SM_TRY(cudaMemcpyAsync(out->triangles, w.tstage.p, sizeof(lvn_mesh_triangle) * tt, cudaMemcpyDeviceToHost, st));
+    }
+    SM_TRY(cudaStreamSynchronize(st));
+    return LVN_OK;
+}
+
+}  // extern "C"

@@ -1726,6 +1726,347 @@ void inside(const int32_t mn[3], int32_t size, const std::vector<int32_t>& boxes
 bool valid_root(int32_t root_size) { return root_size >= kLeaf && (root_size & (root_size - 1)) == 0; }
 }  // namespace clipmap
 
+// ---- seam octree and contouring -------------------------------------------------
+//
+// GenerateClipmapSeamMesh (clipmap.cpp:573-610) restated as the reference runs
+// it: the active nodes around a host (FindNode / FindActiveNodes, clipmap.cpp:
+// 982-1013, 1449-1479) give their seam nodes (GenerateMeshDataForNode,
+// clipmap.cpp:398-418) to SelectSeamNodes / FilterSeamNode (clipmap.cpp:
+// 508-570); Octree_ConstructUpwards (octree.cpp:31-148) builds a pointer
+// octree from them and Octree_GenerateMesh (octree.cpp:197-551) numbers its
+// leaves and contours it.
+
+namespace seam {
+
+constexpr int kLeafChunk = 256;  // CLIPMAP_LEAF_SIZE (volume_constants.h:15)
+
+// the dual-contouring tables of contour_constants.h (the standard tables of
+// the method; the recursion's order depends on them)
+const int kEdgeVMap[12][2] = {{0, 4}, {1, 5}, {2, 6}, {3, 7}, {0, 2}, {1, 3},
+                              {4, 6}, {5, 7}, {0, 1}, {2, 3}, {4, 5}, {6, 7}};
+const int kCellProcFaceMask[12][3] = {{0, 4, 0}, {1, 5, 0}, {2, 6, 0}, {3, 7, 0}, {0, 2, 1}, {4, 6, 1},
+                                      {1, 3, 1}, {5, 7, 1}, {0, 1, 2}, {2, 3, 2}, {4, 5, 2}, {6, 7, 2}};
+const int kCellProcEdgeMask[6][5] = {{0, 1, 2, 3, 0}, {4, 5, 6, 7, 0}, {0, 4, 1, 5, 1},
+                                     {2, 6, 3, 7, 1}, {0, 2, 4, 6, 2}, {1, 3, 5, 7, 2}};
+const int kFaceProcFaceMask[3][4][3] = {{{4, 0, 0}, {5, 1, 0}, {6, 2, 0}, {7, 3, 0}},
+                                        {{2, 0, 1}, {6, 4, 1}, {3, 1, 1}, {7, 5, 1}},
+                                        {{1, 0, 2}, {3, 2, 2}, {5, 4, 2}, {7, 6, 2}}};
+const int kFaceProcEdgeMask[3][4][6] = {{{1, 4, 0, 5, 1, 1}, {1, 6, 2, 7, 3, 1}, {0, 4, 6, 0, 2, 2}, {0, 5, 7, 1, 3, 2}},
+                                        {{0, 2, 3, 0, 1, 0}, {0, 6, 7, 4, 5, 0}, {1, 2, 0, 6, 4, 2}, {1, 3, 1, 7, 5, 2}},
+                                        {{1, 1, 0, 3, 2, 0}, {1, 5, 4, 7, 6, 0}, {0, 1, 5, 0, 4, 1}, {0, 3, 7, 2, 6, 1}}};
+const int kEdgeProcEdgeMask[3][2][5] = {{{3, 2, 1, 0, 0}, {7, 6, 5, 4, 0}},
+                                        {{5, 1, 4, 0, 1}, {7, 3, 6, 2, 1}},
+                                        {{6, 4, 2, 0, 2}, {7, 5, 3, 1, 2}}};
+const int kProcessEdgeMask[3][4] = {{3, 2, 1, 0}, {7, 5, 6, 4}, {11, 10, 9, 8}};
+
+inline void child_offset(int i, int o[3]) {  // CHILD_MIN_OFFSETS (x << 2 | y << 1 | z)
+    o[0] = (i >> 2) & 1;
+    o[1] = (i >> 1) & 1;
+    o[2] = i & 1;
+}
+
+struct Node {
+    bool leaf = false;
+    int32_t min[3] = {0, 0, 0};
+    int32_t size = 0;
+    Node* child[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    float position[3] = {0, 0, 0}, normal[3] = {0, 0, 0};
+    int32_t material_info = 0;
+    int32_t index = -1;
+};
+
+struct Mesh {
+    std::vector<float> vertices;    // 12 floats each (MeshVertex)
+    std::vector<int32_t> triangles;  // 3 each
+};
+
+bool same3(const int32_t a[3], const int32_t b[3]) { return a[0] == b[0] && a[1] == b[1] && a[2] == b[2]; }
+
+// ConstructParents (octree.cpp:31-86); `pool` owns the new nodes
+std::vector<Node*> construct_parents(std::vector<Node*>& nodes, int parent_size, const int32_t root_min[3],
+                                     std::vector<std::unique_ptr<Node>>& pool) {
+    std::unordered_map<uint64_t, Node*> parents;
+    std::vector<Node*> order;
+    for (Node* n : nodes) {
+        int32_t ppos[3];
+        for (int a = 0; a < 3; a++) ppos[a] = n->min[a] - ((n->min[a] - root_min[a]) % parent_size);
+        const uint64_t key = (uint64_t)(uint32_t)(ppos[0] - root_min[0]) |
+                             ((uint64_t)(uint32_t)(ppos[1] - root_min[1]) << 20) |
+                             ((uint64_t)(uint32_t)(ppos[2] - root_min[2]) << 40);  // HashOctreeMin (octree.cpp:24-27)
+        Node* p;
+        auto it = parents.find(key);
+        if (it == parents.end()) {
+            pool.emplace_back(new Node());
+            p = pool.back().get();
+            for (int a = 0; a < 3; a++) p->min[a] = ppos[a];
+            p->size = parent_size;
+            parents.emplace(key, p);
+            order.push_back(p);
+        } else {
+            p = it->second;
+        }
+        for (int i = 0; i < 8; i++) {
+            int o[3];
+            child_offset(i, o);
+            const int32_t cpos[3] = {ppos[0] + (parent_size / 2) * o[0], ppos[1] + (parent_size / 2) * o[1],
+                                     ppos[2] + (parent_size / 2) * o[2]};
+            if (same3(cpos, n->min)) {
+                p->child[i] = n;
+                break;
+            }
+        }
+    }
+    return order;
+}
+
+// Octree_ConstructUpwards (octree.cpp:90-148)
+Node* construct_upwards(std::vector<Node*> nodes, const int32_t root_min[3], int root_size,
+                        std::vector<std::unique_ptr<Node>>& pool) {
+    if (nodes.empty()) return nullptr;
+    std::stable_sort(nodes.begin(), nodes.end(), [](const Node* a, const Node* b) { return a->size < b->size; });
+    while (nodes.front()->size != nodes.back()->size) {
+        auto it = nodes.begin();
+        const int size = (*it)->size;
+        do {
+            ++it;
+        } while ((*it)->size == size);
+        std::vector<Node*> run(nodes.begin(), it);
+        std::vector<Node*> next = construct_parents(run, size * 2, root_min, pool);
+        next.insert(next.end(), it, nodes.end());
+        nodes.swap(next);
+    }
+    for (int parent = nodes.front()->size * 2; parent <= root_size; parent *= 2)
+        nodes = construct_parents(nodes, parent, root_min, pool);
+    return nodes.size() == 1 ? nodes.front() : nullptr;
+}
+
+// GenerateVertexIndices (octree.cpp:197-232)
+void vertex_indices(Node* n, const float colour[3], Mesh& m) {
+    if (!n) return;
+    bool has_children = false;
+    for (int i = 0; i < 8; i++) has_children |= n->child[i] != nullptr;
+    if (has_children) {
+        for (int i = 0; i < 8; i++) vertex_indices(n->child[i], colour, m);
+        return;
+    }
+    n->index = (int32_t)(m.vertices.size() / 12);
+    const float v[12] = {n->position[0], n->position[1], n->position[2], 0.f,
+                         n->normal[0],   n->normal[1],   n->normal[2],   0.f,
+                         colour[0],      colour[1],      colour[2],      (float)(n->material_info >> 8)};
+    m.vertices.insert(m.vertices.end(), v, v + 12);
+}
+
+void chunk_min(const int32_t p[3], int32_t out[3]) {  // ChunkMinForPosition (volume.cpp:30-34)
+    const unsigned mask = ~(unsigned)(kLeafChunk - 1);
+    for (int a = 0; a < 3; a++) out[a] = (int32_t)((unsigned)p[a] & mask);
+}
+
+// ContourProcessEdge (octree.cpp:236-282)
+void process_edge(Node* node[4], int dir, Mesh& m) {
+    int min_size = INT_MAX, min_index = 0, indices[4] = {-1, -1, -1, -1};
+    bool flip = false, sign_change[4] = {false, false, false, false};
+    for (int i = 0; i < 4; i++) {
+        if (node[i]->leaf) {
+            const int edge = kProcessEdgeMask[dir][i];
+            const int c0 = kEdgeVMap[edge][0], c1 = kEdgeVMap[edge][1];
+            const int corners = node[i]->material_info & 0xff;
+            const int m0 = (corners >> c0) & 1, m1 = (corners >> c1) & 1;
+            if (node[i]->size < min_size) {
+                min_size = node[i]->size;
+                min_index = i;
+                flip = m1 != 1;
+            }
+            indices[i] = node[i]->index;
+            sign_change[i] = (m0 && !m1) || (!m0 && m1);
+        }
+    }
+    if (!sign_change[min_index]) return;
+    const int t[2][3] = {{indices[0], indices[1], indices[3]}, {indices[0], indices[3], indices[2]}};
+    const int tf[2][3] = {{indices[0], indices[3], indices[1]}, {indices[0], indices[2], indices[3]}};
+    for (int k = 0; k < 2; k++) m.triangles.insert(m.triangles.end(), flip ? tf[k] : t[k], (flip ? tf[k] : t[k]) + 3);
+}
+
+// ContourEdgeProc (octree.cpp:286-347)
+void edge_proc(Node* node[4], int dir, Mesh& m) {
+    if (!node[0] || !node[1] || !node[2] || !node[3]) return;
+    int32_t c0[3];
+    chunk_min(node[0]->min, c0);
+    bool one_chunk = true;
+    for (int i = 1; i < 4; i++) {
+        int32_t ci[3];
+        chunk_min(node[i]->min, ci);
+        one_chunk &= same3(ci, c0);
+    }
+    if (one_chunk) return;  // only edges straddling chunks are contoured
+    const bool branch[4] = {!node[0]->leaf, !node[1]->leaf, !node[2]->leaf, !node[3]->leaf};
+    if (!branch[0] && !branch[1] && !branch[2] && !branch[3]) {
+        process_edge(node, dir, m);
+        return;
+    }
+    for (int i = 0; i < 2; i++) {
+        Node* e[4];
+        for (int j = 0; j < 4; j++) e[j] = branch[j] ? node[j]->child[kEdgeProcEdgeMask[dir][i][j]] : node[j];
+        edge_proc(e, kEdgeProcEdgeMask[dir][i][4], m);
+    }
+}
+
+// ContourFaceProc (octree.cpp:351-432)
+void face_proc(Node* node[2], int dir, Mesh& m) {
+    if (!node[0] || !node[1]) return;
+    int32_t a[3], b[3];
+    chunk_min(node[0]->min, a);
+    chunk_min(node[1]->min, b);
+    if (same3(a, b)) return;
+    const bool branch[2] = {!node[0]->leaf, !node[1]->leaf};
+    if (!branch[0] && !branch[1]) return;
+    for (int i = 0; i < 4; i++) {
+        Node* f[2];
+        for (int j = 0; j < 2; j++) f[j] = branch[j] ? node[j]->child[kFaceProcFaceMask[dir][i][j]] : node[j];
+        face_proc(f, kFaceProcFaceMask[dir][i][2], m);
+    }
+    const int orders[2][4] = {{0, 0, 1, 1}, {0, 1, 0, 1}};
+    for (int i = 0; i < 4; i++) {
+        const int* order = orders[kFaceProcEdgeMask[dir][i][0]];
+        Node* e[4];
+        for (int j = 0; j < 4; j++)
+            e[j] = branch[order[j]] ? node[order[j]]->child[kFaceProcEdgeMask[dir][i][1 + j]] : node[order[j]];
+        edge_proc(e, kFaceProcEdgeMask[dir][i][5], m);
+    }
+}
+
+// ContourCellProc (octree.cpp:436-474)
+void cell_proc(Node* n, Mesh& m) {
+    if (!n || n->leaf) return;
+    for (int i = 0; i < 8; i++) cell_proc(n->child[i], m);
+    for (int i = 0; i < 12; i++) {
+        Node* f[2] = {n->child[kCellProcFaceMask[i][0]], n->child[kCellProcFaceMask[i][1]]};
+        face_proc(f, kCellProcFaceMask[i][2], m);
+    }
+    for (int i = 0; i < 6; i++) {
+        Node* e[4];
+        for (int j = 0; j < 4; j++) e[j] = n->child[kCellProcEdgeMask[i][j]];
+        edge_proc(e, kCellProcEdgeMask[i][4], m);
+    }
+}
+
+// FilterSeamNode (clipmap.cpp:508-538)
+bool filter_seam_node(int child, const int32_t bounds[3], const int32_t mn[3], const int32_t mx[3]) {
+    switch (child) {
+        case 0: return mx[0] == bounds[0] || mx[1] == bounds[1] || mx[2] == bounds[2];
+        case 1: return mn[2] == bounds[2];
+        case 2: return mn[1] == bounds[1];
+        case 3: return mn[1] == bounds[1] || mn[2] == bounds[2];
+        case 4: return mn[0] == bounds[0];
+        case 5: return mn[0] == bounds[0] || mn[2] == bounds[2];
+        case 6: return mn[0] == bounds[0] || mn[1] == bounds[1];
+        case 7: return same3(mn, bounds);
+    }
+    return false;
+}
+
+bool inside(const int32_t mn[3], int32_t size, const int32_t p[3]) {  // AABB::pointIsInside (aabb.h:37-43)
+    for (int a = 0; a < 3; a++)
+        if (!(p[a] >= mn[a] && p[a] < mn[a] + size)) return false;
+    return true;
+}
+
+struct Clipmap {
+    int32_t root_min[3];
+    int32_t root_size;
+    std::map<std::array<int32_t, 4>, int> active;  // (min, size) -> chunk index
+
+    // FindNode (clipmap.cpp:982-1006) over the complete octree
+    bool find_node(const int32_t mn[3], int32_t size, const int32_t nmin[3], int32_t nsize) const {
+        if (nsize == size && same3(nmin, mn)) return true;
+        if (!inside(nmin, nsize, mn) || nsize <= kLeafChunk) return false;
+        for (int i = 0; i < 8; i++) {
+            int o[3];
+            child_offset(i, o);
+            const int32_t c[3] = {nmin[0] + o[0] * nsize / 2, nmin[1] + o[1] * nsize / 2, nmin[2] + o[2] * nsize / 2};
+            if (find_node(mn, size, c, nsize / 2)) return true;
+        }
+        return false;
+    }
+    // FindActiveNodes (clipmap.cpp:1449-1472)
+    void find_active(const int32_t nmin[3], int32_t nsize, const int32_t rmin[3], int32_t rsize,
+                     std::vector<int>& out) const {
+        if (inside(nmin, nsize, rmin) || inside(rmin, rsize, nmin)) {
+            auto it = active.find({nmin[0], nmin[1], nmin[2], nsize});
+            if (it != active.end()) {
+                out.push_back(it->second);
+            } else if (nsize > kLeafChunk) {
+                for (int i = 0; i < 8; i++) {
+                    int o[3];
+                    child_offset(i, o);
+                    const int32_t c[3] = {nmin[0] + o[0] * nsize / 2, nmin[1] + o[1] * nsize / 2,
+                                          nmin[2] + o[2] * nsize / 2};
+                    find_active(c, nsize / 2, rmin, rsize, out);
+                }
+            }
+        }
+    }
+};
+
+struct Input {
+    const int32_t* chunks4;
+    const int32_t* seam_offsets;
+    const int32_t* seams;  // SeamNodeInfo, 12 words each
+    int vpc;
+    float colour[3];
+};
+
+// GenerateClipmapSeamMesh (clipmap.cpp:573-610) for the host chunk `h`
+Mesh seam_mesh(const Clipmap& cm, const Input& in, int h) {
+    const int32_t* host = in.chunks4 + 4 * h;
+    const int32_t hsize = host[3];
+    std::vector<std::unique_ptr<Node>> pool;
+    std::vector<Node*> nodes;
+    for (int i = 0; i < 8; i++) {
+        int o[3];
+        child_offset(i, o);
+        const int32_t nmin[3] = {host[0] + o[0] * hsize, host[1] + o[1] * hsize, host[2] + o[2] * hsize};
+        if (!cm.find_node(nmin, hsize, cm.root_min, cm.root_size)) continue;
+        std::vector<int> act;
+        cm.find_active(cm.root_min, cm.root_size, nmin, hsize, act);
+        for (int c : act) {
+            // SelectSeamNodes (clipmap.cpp:542-570) over the seam nodes GenerateMeshDataForNode made
+            const int32_t* ch = in.chunks4 + 4 * c;
+            const int32_t bounds[3] = {host[0] + hsize, host[1] + hsize, host[2] + hsize};
+            const int size = ch[3] / (in.vpc * LEAF_SIZE_SCALE);
+            const int node_size = ch[3] / in.vpc;
+            for (int k = in.seam_offsets[c]; k < in.seam_offsets[c + 1]; k++) {
+                const int32_t* s = in.seams + 12 * (size_t)k;
+                const int32_t mn[3] = {s[0] * node_size + ch[0], s[1] * node_size + ch[1], s[2] * node_size + ch[2]};
+                const int32_t mx[3] = {mn[0] + size * LEAF_SIZE_SCALE, mn[1] + size * LEAF_SIZE_SCALE,
+                                       mn[2] + size * LEAF_SIZE_SCALE};
+                if (!filter_seam_node(i, bounds, mn, mx) || !inside(host, 2 * hsize, mn)) continue;
+                pool.emplace_back(new Node());
+                Node* n = pool.back().get();
+                n->leaf = true;
+                for (int a = 0; a < 3; a++) n->min[a] = mn[a];
+                n->size = node_size;
+                float f[8];
+                std::memcpy(f, s + 4, sizeof(f));
+                for (int a = 0; a < 3; a++) {
+                    n->position[a] = f[a];
+                    n->normal[a] = f[4 + a];
+                }
+                n->material_info = s[3];
+                nodes.push_back(n);
+            }
+        }
+    }
+    Mesh m;
+    Node* root = construct_upwards(nodes, host, 2 * hsize, pool);
+    if (!root) return m;
+    vertex_indices(root, in.colour, m);
+    cell_proc(root, m);
+    if (m.triangles.empty()) m.vertices.clear();  // Octree_GenerateMesh returns no mesh (octree.cpp:536-540)
+    return m;
+}
+
+}  // namespace seam
+
 extern "C" {
 
 int orc_clipmap_select(const float cam[3], const int32_t root_min[3], int32_t root_size, int32_t* out4, int32_t cap) {
@@ -1752,6 +2093,48 @@ int orc_clipmap_touched(const orc_csg_op* ops, int32_t n, const int32_t root_min
     clipmap::Out o{out4, cap};
     if (n > 0) clipmap::inside(root_min, root_size, boxes, o);
     return o.n;
+}
+
+int orc_seam_generate(const int32_t* chunks4, const int32_t* seam_offsets, int32_t num_chunks, const int32_t* seams,
+                      int32_t vpc, const int32_t root_min[3], int32_t root_size, const int32_t* hosts,
+                      int32_t num_hosts, const float colour[3], float* vertices, int64_t vertex_cap,
+                      int32_t* triangles, int64_t triangle_cap, int32_t* host_counts, int32_t threads) {
+    if (num_chunks < 0 || num_hosts < 0 || vpc <= 0) return -1;
+    seam::Clipmap cm;
+    for (int a = 0; a < 3; a++) cm.root_min[a] = root_min[a];
+    cm.root_size = root_size;
+    for (int c = 0; c < num_chunks; c++)
+        cm.active[{chunks4[4 * c], chunks4[4 * c + 1], chunks4[4 * c + 2], chunks4[4 * c + 3]}] = c;
+    seam::Input in{chunks4, seam_offsets, seams, vpc, {colour[0], colour[1], colour[2]}};
+    std::vector<seam::Mesh> meshes(num_hosts);
+    if (threads < 1) threads = 1;
+    std::atomic<int> next{0};
+    auto worker = [&]() {
+        for (;;) {
+            const int i = next.fetch_add(1);
+            if (i >= num_hosts) break;
+            meshes[i] = seam::seam_mesh(cm, in, hosts[i]);
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; t++) pool.emplace_back(worker);
+    for (auto& t : pool) t.join();
+    int64_t nv = 0, nt = 0;
+    for (int i = 0; i < num_hosts; i++) {
+        host_counts[2 * i] = (int32_t)(meshes[i].vertices.size() / 12);
+        host_counts[2 * i + 1] = (int32_t)(meshes[i].triangles.size() / 3);
+        nv += host_counts[2 * i];
+        nt += host_counts[2 * i + 1];
+    }
+    if (nv > vertex_cap || nt > triangle_cap) return -2;
+    int64_t ov = 0, ot = 0;
+    for (int i = 0; i < num_hosts; i++) {
+        if (vertices) std::memcpy(vertices + 12 * ov, meshes[i].vertices.data(), meshes[i].vertices.size() * 4);
+        if (triangles) std::memcpy(triangles + 3 * ot, meshes[i].triangles.data(), meshes[i].triangles.size() * 4);
+        ov += host_counts[2 * i];
+        ot += host_counts[2 * i + 1];
+    }
+    return 0;
 }
 
 int64_t orc_clipmap_select_many(const float* cams, int32_t n, const int32_t root_min[3], int32_t root_size,

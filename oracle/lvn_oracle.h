@@ -127,6 +127,18 @@ int orc_clipmap_touched(const orc_csg_op* ops, int32_t n, const int32_t root_min
 int64_t orc_clipmap_select_many(const float* cams, int32_t n, const int32_t root_min[3], int32_t root_size,
                                 int32_t threads);
 
+/* GenerateClipmapSeamMesh (clipmap.cpp:573-610) for each host: the active
+ * clipmap nodes are chunks4 (min xyz, size), chunk c's seam nodes (SeamNodeInfo,
+ * 12 words) seams[seam_offsets[c] .. seam_offsets[c + 1]); hosts index chunks.
+ * Writes the hosts' meshes back to back (MeshVertex, 12 floats; triangles, 3
+ * int32 host-local indices) and per host (vertices, triangles) into
+ * host_counts; a host without triangles has no mesh (0, 0).  Returns 0, -2
+ * when the capacities are too small (host_counts set), -1 on bad arguments. */
+int orc_seam_generate(const int32_t* chunks4, const int32_t* seam_offsets, int32_t num_chunks, const int32_t* seams,
+                      int32_t vpc, const int32_t root_min[3], int32_t root_size, const int32_t* hosts,
+                      int32_t num_hosts, const float colour[3], float* vertices, int64_t vertex_cap,
+                      int32_t* triangles, int64_t triangle_cap, int32_t* host_counts, int32_t threads);
+
 /* CPU baseline: mesh n chunks (each a fresh field with its ops) on `threads`
  * host threads; returns total vertices + triangles for sanity */
 int64_t orc_mesh_chunks(const orc_density* d, const orc_chunk_args* chunks, int32_t n,

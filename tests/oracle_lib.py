@@ -84,6 +84,9 @@ def lib():
                                           C.c_int32]
         L.orc_clipmap_select_many.argtypes = [C.c_void_p, C.c_int32, C.c_int32 * 3, C.c_int32, C.c_int32]
         L.orc_clipmap_select_many.restype = C.c_int64
+        L.orc_seam_generate.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32 * 3,
+                                        C.c_int32, C.c_void_p, C.c_int32, C.c_float * 3, C.c_void_p, C.c_int64,
+                                        C.c_void_p, C.c_int64, C.c_void_p, C.c_int32]
         _lib = L
     return _lib
 
@@ -257,3 +260,26 @@ def clipmap_touched(op_tuples, root_min, root_size):
 def clipmap_select_many(cams, root_min, root_size, threads):
     c = np.ascontiguousarray(np.asarray(cams, np.float32).reshape(-1, 3))
     return lib().orc_clipmap_select_many(c.ctypes.data, c.shape[0], _i3(root_min), int(root_size), int(threads))
+
+
+def seam_generate(chunks, seam_offsets, seams, vpc, root_min, root_size, hosts, colour=(1.0, 1.0, 1.0), threads=1):
+    """GenerateClipmapSeamMesh restated: (vertices (V, 12) f32, triangles (T, 3)
+    i32, counts (H, 2) = (vertices, triangles) per host), hosts back to back."""
+    c4 = np.ascontiguousarray(np.array([[*mn, s] for mn, s in chunks], np.int32).reshape(-1, 4))
+    offs = np.ascontiguousarray(np.asarray(seam_offsets, np.int32))
+    sm = np.ascontiguousarray(np.asarray(seams, np.int32).reshape(-1, 12))
+    hs = np.ascontiguousarray(np.asarray(hosts, np.int32))
+    counts = np.zeros((max(1, len(hs)), 2), np.int32)
+    cap_v, cap_t = 1 << 14, 1 << 15
+    while True:
+        v = np.zeros((cap_v, 12), np.float32)
+        t = np.zeros((cap_t, 3), np.int32)
+        rc = lib().orc_seam_generate(c4.ctypes.data, offs.ctypes.data, len(c4), sm.ctypes.data, int(vpc), _i3(root_min),
+                                     int(root_size), hs.ctypes.data, len(hs), (C.c_float * 3)(*colour), v.ctypes.data,
+                                     cap_v, t.ctypes.data, cap_t, counts.ctypes.data, int(threads))
+        if rc == -2:
+            cap_v, cap_t = int(counts[:, 0].sum()), int(counts[:, 1].sum())
+            continue
+        assert rc == 0, rc
+        nv, nt = int(counts[:len(hs), 0].sum()), int(counts[:len(hs), 1].sum())
+        return v[:nv], t[:nt], counts[:len(hs)]
