@@ -24,6 +24,11 @@ included).  `--workload select`: the clipmap's active-node selection
 (SelectActiveClipmapNodes) for 4096 cameras on 64 seeded paths through the
 2^15-unit world, one launch per step (its own JSON line, impl "lvn-select";
 the reference arm times the oracle's recursion on all host threads).
+`--workload seams`: the seam meshes (GenerateClipmapSeamMesh) of all 428
+active clipmap nodes one camera selects (LOD 0-5, caves density), from their
+seam nodes as the batch meshing left them in device memory (its own JSON line, impl "lvn-seams"; the
+reference arm times the oracle's octree construction and contouring on all
+host threads).
 `--surrogate`: trains the learned density surrogate on the GPU
 and meshes the clipmap chunk set with the 2D fBm density plain and through
 the surrogate (its own JSON line, impl "lvn-surrogate").
@@ -64,9 +69,10 @@ def parse():
     p.add_argument("--simplify", type=float, default=None,
                    help="octree simplification QEF-error threshold (voxel^2); default 0.05 for the clipmap "
                         "workload, off otherwise; < 0 = off")
-    p.add_argument("--workload", default="tiled", choices=["tiled", "clipmap", "one", "select"],
+    p.add_argument("--workload", default="tiled", choices=["tiled", "clipmap", "one", "select", "seams"],
                    help="tiled: 128 LOD0 chunks + 32 CSG ops (default); clipmap: 1024 chunks over LOD 0-4 with "
-                        "3D caves; one: a single LOD0 chunk; select: clipmap node selection for 4096 cameras")
+                        "3D caves; one: a single LOD0 chunk; select: clipmap node selection for 4096 cameras; "
+                        "seams: the seam meshes of the 1024 clipmap chunks")
     return p.parse_args()
 
 
@@ -235,6 +241,8 @@ def run_reference(args):
         return
     if WORKLOAD == "select":
         return run_select_reference(args)
+    if WORKLOAD == "seams":
+        return run_seams_reference(args)
     wl = workload()
     threads = host_threads()
     cb = CpuBaseline(wl, threads, simplify_threshold(args))
@@ -473,7 +481,7 @@ def run_lvn(args):
 
 
 PROFILE_TAG = {"tiled": "tiled_csg_128", "clipmap": "clipmap_caves_1024", "one": "one_chunk",
-               "select": "select_4096"}
+               "select": "select_4096", "seams": "seams_clipmap_frame_428"}
 
 
 def committed_traffic(kernel):
@@ -806,6 +814,179 @@ def run_select(args):
     print(json.dumps(line), flush=True)
 
 
+SEAMS_METRIC = "clipmap seam meshes/sec on 1 GB300 (GenerateClipmapSeamMesh, 64^3 chunks, LOD 0-5)"
+SEAM_COLOUR = (0.25, 0.5, 0.75)
+
+
+def seams_inputs():
+    """One camera's active clipmap nodes (a disjoint tiling of the world, as
+    the engine's clipmap holds them) meshed once on the GPU: (workload, seam
+    offsets, seam rows (S, 12) int32)."""
+    import numpy as np
+    import torch
+
+    import leven_gb300 as lvn
+    from leven_gb300 import workloads as W
+
+    wl = W.clipmap_frame()
+    lvn.initialise(wl.noise_seed, 0, 2)
+    lvn.set_density(**wl.density)
+    lvn.clear_csg_operations()
+    g = lvn.MeshGen(64)
+    try:
+        _, _, s, res = g.generate_chunks(wl.chunks)
+    finally:
+        g.close()
+    rows = np.concatenate([s[o:o + n] for o, n in zip(res[:, 4], res[:, 5])]).astype(np.int32)
+    offs = np.concatenate([[0], np.cumsum(res[:, 5])]).astype(np.int32)
+    return wl, offs, rows
+
+
+def run_seams_reference(args):
+    import torch  # noqa: F401  (the GPU meshes the inputs once, outside the timed region)
+
+    from leven_gb300 import workloads as W
+
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_lib as O
+
+    O.build()
+    wl, offs, rows = seams_inputs()
+    hosts = list(range(len(wl.chunks)))
+    threads = host_threads()
+
+    def one():
+        t0 = time.perf_counter()
+        O.seam_generate(wl.chunks, offs, rows, 64, W.CLIPMAP_ROOT_MIN, W.CLIPMAP_ROOT_SIZE, hosts, SEAM_COLOUR,
+                        threads=threads)
+        return time.perf_counter() - t0
+
+    for _ in range(args.warmup):
+        one()
+    vals = [len(hosts) / one() for _ in range(args.steps)]
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": SEAMS_METRIC, "value": round(value, 1), "unit": "seam meshes/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * len(hosts) / value, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": f"seams-{wl.name}", "seam_nodes": int(offs[-1])},
+        "cpu_baseline": {"value": round(value, 1), "unit": "seam meshes/s", "cores": threads, "kind": "port",
+                         "sample": f"all {len(hosts)} hosts per step"},
+        "e2e": {"value": round(value, 1), "unit": "seam meshes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_seams(args):
+    """Seam meshes of every chunk of the caves clipmap set: seam nodes and
+    outputs in device memory (value), and from / to pinned host arrays (e2e)."""
+    import numpy as np
+    import torch
+
+    import leven_gb300 as lvn
+    from leven_gb300 import workloads as W
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    wl, offs, rows = seams_inputs()
+    n = len(wl.chunks)
+    hosts = np.arange(n, dtype=np.int32)
+    descs = (lvn.ChunkDesc * n)()
+    for i, (mn, size) in enumerate(wl.chunks):
+        descs[i] = lvn.ChunkDesc((C.c_int32 * 3)(*mn), size)
+    results = (lvn.ChunkResult * n)()
+    d_rows = torch.from_numpy(rows).to(dev)
+    h_rows = torch.from_numpy(rows).pin_memory()
+    v, t, res = lvn.seam_generate(wl.chunks, offs, rows, 64, W.CLIPMAP_ROOT_MIN, W.CLIPMAP_ROOT_SIZE, hosts,
+                                  SEAM_COLOUR)
+    nv, nt = len(v), len(t)
+    d_v = torch.empty((nv + 1, 12), dtype=torch.float32, device=dev)
+    d_t = torch.empty((nt + 1, 3), dtype=torch.int32, device=dev)
+    h_v = torch.empty((nv + 1, 12), dtype=torch.float32).pin_memory()
+    h_t = torch.empty((nt + 1, 3), dtype=torch.int32).pin_memory()
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.int32, device=dev)
+    L = lvn.lib()
+    rmin = lvn._ivec3(W.CLIPMAP_ROOT_MIN)
+    colour = (C.c_float * 3)(*SEAM_COLOUR)
+
+    def call(device):
+        if device:
+            bo = lvn.BatchOut(lvn.LVN_MEMORY_DEVICE, d_v.data_ptr(), nv + 1, 0, d_t.data_ptr(), nt + 1, 0, None, 0, 0,
+                              C.cast(results, C.POINTER(lvn.ChunkResult)))
+            src, mem = d_rows.data_ptr(), lvn.LVN_MEMORY_DEVICE
+        else:
+            bo = lvn.BatchOut(lvn.LVN_MEMORY_HOST, h_v.data_ptr(), nv + 1, 0, h_t.data_ptr(), nt + 1, 0, None, 0, 0,
+                              C.cast(results, C.POINTER(lvn.ChunkResult)))
+            src, mem = h_rows.data_ptr(), lvn.LVN_MEMORY_HOST
+        rc = L.lvn_seam_generate(descs, offs.ctypes.data, n, src, mem, 64, rmin, W.CLIPMAP_ROOT_SIZE,
+                                 hosts.ctypes.data, n, colour, C.byref(bo))
+        assert rc == 0 and bo.total_vertices == nv and bo.total_triangles == nt, rc
+
+    def timed(device):
+        for _ in range(max(args.warmup, 3)):
+            call(device)
+        ts = []
+        for _ in range(args.steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            call(device)  # returns once its last copy has landed
+            ts.append(time.perf_counter() - t0)
+        return 1e3 * sum(ts) / len(ts)
+
+    with ClockSampler(local) as clocks:
+        ms = timed(True)
+        ms_e2e = timed(False)
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    leaves = int(res[:, 7].sum())
+    # algorithmic bytes: every seam node of every chunk gathered (48 B) and the
+    # meshes written (48 B a vertex, 12 B a triangle)
+    algo = 48 * leaves + 48 * nv + 12 * nt
+    ach = algo / (ms / 1e3) / 1e9
+    line = {
+        "metric": SEAMS_METRIC, "impl": "lvn-seams", "value": round(n / (ms / 1e3), 1), "unit": "seam meshes/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": f"seams-{wl.name}", "seam_nodes": int(offs[-1]), "leaves": leaves,
+                   "vertices": nv, "triangles": nt, "l2": "flushed between steps (256 MiB write)",
+                   "timing": "host clock around the synchronous C-ABI call (its own stream, three waits)"},
+        "e2e": {"value": round(n / (ms_e2e / 1e3), 1), "unit": "seam meshes/s", "h2d_bytes_per_step": int(48 * offs[-1]),
+                "d2h_bytes_per_step": int(48 * nv + 12 * nt), "ms_per_step": round(ms_e2e, 4)},
+        "gpu_launches": 3,
+        "roofline": {"bound": "hbm", "achieved": round(ach, 1), "peak": hbm_peak, "unit": "GB/s",
+                     "frac": round(ach / hbm_peak, 4), "traffic": committed_traffic("seam_build"),
+                     "kernel": "k_seam_build (+ count, emit)", "ms_per_launch": round(ms, 4),
+                     "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                     "algorithmic_bytes_per_launch": algo},
+        "clocks": clocks.summary(),
+    }
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, str(ROOT / "tests"))
+        import oracle_lib as O
+
+        O.build()
+        threads = host_threads()
+        done, total = 0, 0.0
+        while total < 3.0:
+            t0 = time.perf_counter()
+            O.seam_generate(wl.chunks, offs, rows, 64, W.CLIPMAP_ROOT_MIN, W.CLIPMAP_ROOT_SIZE, list(hosts),
+                            SEAM_COLOUR, threads=threads)
+            total += time.perf_counter() - t0
+            done += n
+        line["cpu_baseline"] = {"value": round(done / total, 1), "unit": "seam meshes/s", "cores": threads,
+                                "kind": "port", "sample": f"{done // n} passes over the {n} hosts, {total:.1f} s"}
+    print(json.dumps(line), flush=True)
+
+
 if __name__ == "__main__":
     a = parse()
     WORKLOAD = a.workload
@@ -815,5 +996,7 @@ if __name__ == "__main__":
         run_surrogate(a)
     elif a.workload == "select":
         run_select(a)
+    elif a.workload == "seams":
+        run_seams(a)
     else:
         run_lvn(a)

@@ -362,7 +362,8 @@ int lvn_clipmap_touched(const lvn_csg_op* ops, int32_t num_ops, const int32_t ro
 
 /* ---- seam meshes (GenerateClipmapSeamMesh, clipmap.cpp:573-610) -----------
  * The clipmap's active nodes are `chunks` (disjoint, inside the complete
- * octree root_min / root_size, as above); chunk c's seam nodes, as
+ * octree root_min / root_size, as above; overlapping or repeated chunks are
+ * LVN_ERR_INVALID); chunk c's seam nodes, as
  * lvn_meshgen_generate_chunks returns them (SeamNodeInfo), are
  * seams[seam_offsets[c] .. seam_offsets[c + 1]) (seam_offsets[0] = 0; seams in
  * host or device memory per seams_memory).  For each host (an index into
@@ -375,12 +376,11 @@ int lvn_clipmap_touched(const lvn_csg_op* ops, int32_t num_ops, const int32_t ro
  * order and the quads of edges straddling chunks become triangles of
  * host-local indices, in the recursion's order.  out->chunks[h] gives host h's
  * offsets and counts (num_nodes = its seam leaves); a host without triangles
- * has no mesh (no vertices).  Limits per host: LVN_SEAM_MAX_LEAVES leaves and
- * LVN_SEAM_MAX_QUADS quads (else LVN_ERR_DEVICE_STATUS) and 2 x host size at
- * most 4096 x the smallest leaf gathered (else LVN_ERR_INVALID).  Calls
- * share scratch on the first device they run on and serialise each other. */
-#define LVN_SEAM_MAX_LEAVES 8192
-#define LVN_SEAM_MAX_QUADS  8192
+ * has no mesh (no vertices).  Limits per host: LVN_SEAM_MAX_LEAVES leaves
+ * (else LVN_ERR_DEVICE_STATUS) and 2 x host size at most 4096 x the smallest
+ * leaf gathered (else LVN_ERR_INVALID).  Calls share scratch on the first
+ * device they run on and serialise each other. */
+#define LVN_SEAM_MAX_LEAVES 32768
 int lvn_seam_generate(const lvn_chunk_desc* chunks, const int32_t* seam_offsets, int32_t num_chunks,
                       const lvn_seam_node* seams, int32_t seams_memory, int32_t voxels_per_chunk,
                       const int32_t root_min[3], int32_t root_size, const int32_t* hosts, int32_t num_hosts,

@@ -12,13 +12,15 @@
 // host, without building the tree:
 //   * the depth-first leaf order is the Morton order of the leaves' minimum
 //     corners (children are visited x << 2 | y << 1 | z), so the leaves are
-//     sorted by Morton key in shared memory and numbered by rank;
+//     sorted by Morton key (in shared memory when they fit, else in global
+//     memory, which the L2 holds) and numbered by rank;
 //   * the recursion emits one quad per final edge segment: an edge of the
 //     smallest of the four leaves around it, all four present, not all four
 //     in one CLIPMAP_LEAF_SIZE block (the straddle test of ContourEdgeProc /
 //     ContourFaceProc prunes exactly those), with a sign change on that
 //     leaf's edge.  Each leaf tests its 12 edges; the other three leaves come
-//     from binary searches of the sorted keys;
+//     from binary searches of the sorted keys.  This runs over blocks of 256
+//     leaves, so a large host spreads over many CTAs;
 //   * the recursion's order is restored by a key spelling the path the
 //     recursion takes to the segment (cell: child 0-7, face 8-19, edge 20-25
 //     in 5 bits; face: sub-face 0-3, edge 4-7 in 3 bits; edge: half in 1 bit),
@@ -41,13 +43,23 @@ namespace lvn {
 namespace {
 
 constexpr int kMaxLeaves = LVN_SEAM_MAX_LEAVES;  // per host
-constexpr int kMaxQuads = LVN_SEAM_MAX_QUADS;    // per host
-constexpr int kSlotBits = 14;                    // leaf sort entry: (morton << 4 | size log2) << 14 | slot
-constexpr int kRankBits = 13;                    // quad payload: 4 ranks of 13 bits, flip at bit 52
+constexpr int kSlotBits = 15;                    // leaf sort entry: (morton << 4 | size log2) << 15 | slot
+constexpr int kRankBits = 15;                    // quad payload: 4 ranks of 15 bits, flip at bit 60
 static_assert(kMaxLeaves <= (1 << kRankBits) && kMaxLeaves <= (1 << kSlotBits), "rank bits");
-constexpr int kMaxLevels = 12;  // log2(2 host size / smallest leaf): path keys of 5 bits per level fit 64 bits
-constexpr int kBuildThreads = 512;
-constexpr size_t kBuildSmem = (size_t)kMaxLeaves * (8 + 4) + (size_t)kMaxQuads * 16;
+constexpr int kMaxLevels = 12;    // log2(2 host size / smallest leaf): path keys of 5 bits per level fit 64 bits
+constexpr int kSortLeaves = 28672;  // hosts with more leaves sort them in global memory
+constexpr int kSmemLeaves = 8192;   // hosts with more leaves search them in global memory
+constexpr int kSmemQuads = 14336;   // hosts with more quads sort them in global memory
+constexpr int kQuadBlock = 256;     // leaves per CTA of the quad enumeration (hosts up to kSmemLeaves)
+constexpr int kBigQuadBlock = 512;  // leaves per CTA of the quad enumeration (larger hosts)
+constexpr size_t kLeafSmem = (size_t)kSortLeaves * 8;
+constexpr size_t kQuadSmem = (size_t)kSmemLeaves * 8;
+constexpr size_t kBigQuadSmem = (size_t)kSortLeaves * 8;
+constexpr size_t kSortSmem = (size_t)kSmemQuads * 16;
+constexpr int kSmallLeaves = 2048;  // leaf sorts up to this size run several CTAs per SM
+constexpr int kSmallQuads = 2048;   // as do quad sorts up to this size
+constexpr size_t kSmallLeafSmem = (size_t)kSmallLeaves * 8;
+constexpr size_t kSmallSortSmem = (size_t)kSmallQuads * 16;
 
 // the dual-contouring tables of contour_constants.h, as the reference's
 // recursion uses them (its output order depends on them)
@@ -68,6 +80,7 @@ __constant__ int8_t cProcessEdgeMask[3][4] = {{3, 2, 1, 0}, {7, 5, 6, 4}, {11, 1
 
 __device__ __forceinline__ int cbit(int child, int axis) { return (child >> (2 - axis)) & 1; }
 
+
 struct SeamHost {
     int32_t min[3];
     int32_t size;
@@ -75,21 +88,27 @@ struct SeamHost {
     int32_t lev;         // log2(2 size / unit)
     int32_t pair_begin;  // gathered (chunk, neighbour mask) pairs
     int32_t pair_end;
-    int64_t leaf_off;    // sorted seam indices, filled by the build
-    int64_t quad_off;    // quads (12 per leaf at most), filled by the build
+    int64_t sel_off;     // the host's selected seam nodes (room for every node of its pairs)
+    int64_t leaf_off;    // the host's leaves in the leaf arrays
+    int64_t quad_off;    // the host's quads (12 per leaf at most) in the quad arrays
 };
 
 struct SeamArgs {
     const SeamHost* hosts;
-    const int2* pairs;            // (chunk, mask of neighbour indices 0-7)
+    const int4* pairs;            // (chunk, mask of neighbour indices 0-7, host, -)
     const int4* chunks;           // (min xyz, size)
     const int32_t* seam_offsets;  // [num_chunks + 1]
     const lvn_seam_node* seams;
     int vpc;
-    int32_t* counts;    // leaves per host (count kernel)
-    int32_t* qcounts;   // quads per host, -1: over a limit (build kernel)
-    uint32_t* leaves;   // sorted seam indices
-    uint64_t* quads;    // sorted quad payloads
+    int32_t* counts;    // leaves per host
+    int32_t* qcounts;   // quads per host
+    uint64_t* sel;      // selected leaves' sort entries, per host at sel_off, unsorted
+    uint32_t* slots;    // their seam indices, by the slot in the entry
+    uint64_t* ent;      // sorted leaf entries
+    uint32_t* leaves;   // seam index per rank
+    uint64_t* qkey;     // quad path keys
+    uint64_t* qval;     // quad payloads (sorted by key after the sort kernel)
+    const int2* items;  // quad enumeration: (host, first leaf)
     // emit
     const int64_t* vout_off;
     const int64_t* tout_off;
@@ -133,66 +152,88 @@ __device__ __forceinline__ bool seam_selected(const SeamHost& h, int4 chunk, int
     return false;
 }
 
-__device__ __forceinline__ uint64_t spread3(uint32_t v, int lev) {
-    uint64_t r = 0;
-    for (int bit = lev - 1; bit >= 0; bit--) r = (r << 3) | ((v >> bit) & 1);
-    return r;
+// bit interleaving by shifts and masks (bit i of v to bit 3i), and back
+__device__ __forceinline__ uint64_t part1by2(uint64_t v) {
+    v &= 0x1fffffull;
+    v = (v | v << 32) & 0x1f00000000ffffull;
+    v = (v | v << 16) & 0x1f0000ff0000ffull;
+    v = (v | v << 8) & 0x100f00f00f00f00full;
+    v = (v | v << 4) & 0x10c30c30c30c30c3ull;
+    v = (v | v << 2) & 0x1249249249249249ull;
+    return v;
 }
 
+__device__ __forceinline__ uint32_t compact1by2(uint64_t v) {
+    v &= 0x1249249249249249ull;
+    v = (v ^ (v >> 2)) & 0x10c30c30c30c30c3ull;
+    v = (v ^ (v >> 4)) & 0x100f00f00f00f00full;
+    v = (v ^ (v >> 8)) & 0x1f0000ff0000ffull;
+    v = (v ^ (v >> 16)) & 0x1f00000000ffffull;
+    v = (v ^ (v >> 32)) & 0x1fffffull;
+    return (uint32_t)v;
+}
+
+// Morton code of a host-relative position in units of 1 << unit_log: x in
+// the highest bit of each triple, as the octree's children are numbered
 __device__ __forceinline__ uint64_t morton(const int32_t rel[3], int unit_log, int lev) {
-    return (spread3((uint32_t)(rel[0] >> unit_log), lev) << 2) | (spread3((uint32_t)(rel[1] >> unit_log), lev) << 1) |
-           spread3((uint32_t)(rel[2] >> unit_log), lev);
+    (void)lev;
+    return (part1by2((uint32_t)rel[0] >> unit_log) << 2) | (part1by2((uint32_t)rel[1] >> unit_log) << 1) |
+           part1by2((uint32_t)rel[2] >> unit_log);
 }
 
 __device__ __forceinline__ void unmorton(uint64_t code, int lev, int unit_log, int32_t rel[3]) {
-    int32_t p[3] = {0, 0, 0};
-    for (int bit = lev - 1; bit >= 0; bit--) {
-        const int t = (int)((code >> (3 * bit)) & 7);
-        p[0] = (p[0] << 1) | ((t >> 2) & 1);
-        p[1] = (p[1] << 1) | ((t >> 1) & 1);
-        p[2] = (p[2] << 1) | (t & 1);
-    }
-    for (int a = 0; a < 3; a++) rel[a] = p[a] << unit_log;
+    (void)lev;
+    rel[0] = (int32_t)(compact1by2(code >> 2) << unit_log);
+    rel[1] = (int32_t)(compact1by2(code >> 1) << unit_log);
+    rel[2] = (int32_t)(compact1by2(code) << unit_log);
 }
 
-__global__ void __launch_bounds__(256) k_seam_count(SeamArgs A) {
-    const SeamHost h = A.hosts[blockIdx.x];
-    int n = 0;
-    for (int p = h.pair_begin; p < h.pair_end; p++) {
-        const int2 pr = A.pairs[p];
-        const int4 ch = A.chunks[pr.x];
-        const int s0 = A.seam_offsets[pr.x], s1 = A.seam_offsets[pr.x + 1];
-        for (int k = s0 + threadIdx.x; k < s1; k += blockDim.x) {
-            int32_t mn[3];
-            n += seam_selected(h, ch, pr.y, A.seams[k], A.vpc, mn);
-        }
+// SelectSeamNodes for every (host, gathered chunk) pair: the selected seam
+// nodes' sort entries ((morton << 4 | size log2) << 15 | slot, host-relative
+// Morton code in units of the host's smallest leaf) and seam indices, in the
+// host's region, in no particular order; counts[host] = how many.
+__global__ void __launch_bounds__(128) k_seam_select(SeamArgs A) {
+    const int4 pr = A.pairs[blockIdx.x];
+    const SeamHost h = A.hosts[pr.z];
+    const int4 ch = A.chunks[pr.x];
+    int unit_log = 0;
+    while ((1 << unit_log) < h.unit) unit_log++;
+    int size_log = 0;
+    while ((h.unit << size_log) < ch.w / A.vpc) size_log++;
+    const int s0 = A.seam_offsets[pr.x], s1 = A.seam_offsets[pr.x + 1];
+    const int lane = threadIdx.x & 31;
+    for (int base = s0; base < s1; base += blockDim.x) {
+        const int k = base + threadIdx.x;
+        int32_t mn[3];
+        const bool take = k < s1 && seam_selected(h, ch, pr.y, A.seams[k], A.vpc, mn);
+        const unsigned ballot = __ballot_sync(0xffffffffu, take);
+        if (!ballot) continue;
+        int first = 0;
+        if (lane == 0) first = atomicAdd(&A.counts[pr.z], __popc(ballot));
+        first = __shfl_sync(0xffffffffu, first, 0);
+        if (!take) continue;
+        const int slot = first + __popc(ballot & ((1u << lane) - 1));
+        if (slot >= kMaxLeaves) continue;  // the host reports the count; nothing past its region is written
+        const int32_t rel[3] = {mn[0] - h.min[0], mn[1] - h.min[1], mn[2] - h.min[2]};
+        A.sel[h.sel_off + slot] =
+            ((morton(rel, unit_log, h.lev) << 4 | (uint64_t)size_log) << kSlotBits) | (uint64_t)slot;
+        A.slots[h.sel_off + slot] = (uint32_t)k;
     }
-    __shared__ int s_n;
-    if (threadIdx.x == 0) s_n = 0;
-    __syncthreads();
-    for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(&s_n, n);
-    __syncthreads();
-    if (threadIdx.x == 0) A.counts[blockIdx.x] = s_n;
 }
 
-// bitonic sort of n entries (keys, with an optional payload moved alongside)
+// Ascending sort of n entries in place (a bitonic network whose first step of
+// each merge compares mirrored positions, so every comparator is ascending and
+// entries past n never move: any n, no padding), keys with an optional payload.
 template <bool Pair>
 __device__ void block_sort(uint64_t* key, uint64_t* val, int n) {
-    int p2 = 1;
-    while (p2 < n) p2 <<= 1;
-    for (int i = n + threadIdx.x; i < p2; i += blockDim.x) {
-        key[i] = ~0ull;
-        if (Pair) val[i] = 0;
-    }
-    __syncthreads();
-    for (int k = 2; k <= p2; k <<= 1) {
+    for (int k = 2; k < 2 * n; k <<= 1) {
         for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = threadIdx.x; i < p2; i += blockDim.x) {
-                const int l = i ^ j;
-                if (l > i) {
+            const int mask = j == (k >> 1) ? k - 1 : j;
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                const int l = i ^ mask;
+                if (l > i && l < n) {
                     const uint64_t a = key[i], b = key[l];
-                    if (((i & k) == 0) == (a > b)) {
+                    if (a > b) {
                         key[i] = b;
                         key[l] = a;
                         if (Pair) {
@@ -212,7 +253,6 @@ struct LeafView {
     const uint64_t* ent;  // sorted entries
     int n;
     int lev, unit_log;
-    int32_t hmin[3];
     int32_t root;  // 2 host size
 };
 
@@ -245,6 +285,12 @@ __device__ int find_leaf(const LeafView& v, const int32_t rel[3], int size_log) 
         if (sl > size_log && (k >> (3 * sl)) == (ent_code(e) >> (3 * sl))) return lo - 1;
     }
     return -1;
+}
+
+__device__ __forceinline__ int log2_units(int32_t size, int32_t unit) {
+    int l = 0;
+    while ((unit << l) < size) l++;
+    return l;
 }
 
 // The path of the reference's recursion (ContourCellProc from the seam
@@ -328,62 +374,53 @@ __device__ uint64_t path_key(int32_t root, int dir, const int32_t line[3], int32
     return key;
 }
 
-__global__ void __launch_bounds__(kBuildThreads) k_seam_build(SeamArgs A) {
+// The leaves of host list[blockIdx.x], sorted: entries to A.ent, seam
+// indices by rank to A.leaves; in shared memory when they fit `cap`.
+__global__ void __launch_bounds__(1024) k_seam_leaves(SeamArgs A, const int32_t* list, int cap) {
     extern __shared__ uint64_t smem[];
-    uint64_t* ent = smem;                                    // [kMaxLeaves]
-    uint32_t* gidx = (uint32_t*)(smem + kMaxLeaves);         // [kMaxLeaves] seam index per slot
-    uint64_t* qkey = smem + kMaxLeaves + kMaxLeaves / 2;     // [kMaxQuads]
-    uint64_t* qval = qkey + kMaxQuads;                       // [kMaxQuads]
-    __shared__ int s_n, s_q, s_over;
-    const SeamHost h = A.hosts[blockIdx.x];
-    int unit_log = 0;
-    while ((1 << unit_log) < h.unit) unit_log++;
-    if (threadIdx.x == 0) {
-        s_n = s_q = 0;
-        s_over = 0;
+    const int hi = list[blockIdx.x];
+    const SeamHost h = A.hosts[hi];
+    const int n = A.counts[hi];
+    uint64_t* ent = A.sel + h.sel_off;
+    if (n <= cap) {
+        for (int i = threadIdx.x; i < n; i += blockDim.x) smem[i] = ent[i];
+        __syncthreads();
+        ent = smem;
     }
-    __syncthreads();
-    // the host's leaves
-    for (int p = h.pair_begin; p < h.pair_end; p++) {
-        const int2 pr = A.pairs[p];
-        const int4 ch = A.chunks[pr.x];
-        int size_log = 0;
-        while ((h.unit << size_log) < ch.w / A.vpc) size_log++;
-        const int s0 = A.seam_offsets[pr.x], s1 = A.seam_offsets[pr.x + 1];
-        for (int k = s0 + threadIdx.x; k < s1; k += blockDim.x) {
-            int32_t mn[3];
-            if (!seam_selected(h, ch, pr.y, A.seams[k], A.vpc, mn)) continue;
-            const int slot = atomicAdd(&s_n, 1);
-            if (slot >= kMaxLeaves) {
-                s_over = 1;
-                continue;
-            }
-            const int32_t rel[3] = {mn[0] - h.min[0], mn[1] - h.min[1], mn[2] - h.min[2]};
-            ent[slot] = ((morton(rel, unit_log, h.lev) << 4 | (uint64_t)size_log) << kSlotBits) | (uint64_t)slot;
-            gidx[slot] = (uint32_t)k;
-        }
-    }
-    __syncthreads();
-    if (s_over) {
-        if (threadIdx.x == 0) A.qcounts[blockIdx.x] = -1;
-        return;
-    }
-    const int n = s_n;
     block_sort<false>(ent, nullptr, n);
-    for (int r = threadIdx.x; r < n; r += blockDim.x)
-        A.leaves[h.leaf_off + r] = gidx[ent[r] & ((1u << kSlotBits) - 1)];
-    // quads: each leaf's 12 edges
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+        const uint64_t e = ent[r];
+        A.ent[h.leaf_off + r] = e;
+        A.leaves[h.leaf_off + r] = A.slots[h.sel_off + (e & ((1u << kSlotBits) - 1))];
+    }
+}
+
+// The quads of the leaves [first, first + block) of one host, unsorted,
+// with their recursion path keys.  The host's sorted entries are copied to
+// shared memory when they fit `cap`, else searched in global memory.
+__global__ void __launch_bounds__(1024) k_seam_quads(SeamArgs A, int block, int cap) {
+    extern __shared__ uint64_t smem[];
+    const int2 it = A.items[blockIdx.x];
+    const SeamHost h = A.hosts[it.x];
+    const int n = A.counts[it.x];
+    const uint64_t* ent = A.ent + h.leaf_off;
+    if (n <= cap) {  // binary searches in shared memory
+        for (int i = threadIdx.x; i < n; i += blockDim.x) smem[i] = ent[i];
+        __syncthreads();
+        ent = smem;
+    }
+    const int unit_log = log2_units(h.unit, 1);
     LeafView v;
     v.ent = ent;
     v.n = n;
     v.lev = h.lev;
     v.unit_log = unit_log;
     v.root = 2 * h.size;
-    for (int a = 0; a < 3; a++) v.hmin[a] = h.min[a];
-    for (int item = threadIdx.x; item < n * 12; item += blockDim.x) {
-        const int r = item / 12, e = item - 12 * (item / 12);
+    const int r_end = min(n, it.y + block);
+    for (int item = it.y * 12 + threadIdx.x; item < r_end * 12; item += blockDim.x) {
+        const int r = item / 12, e = item - 12 * r;
         const uint64_t me = ent[r];
-        const int corners = A.seams[gidx[me & ((1u << kSlotBits) - 1)]].localspace_min[3] & 0xff;
+        const int corners = A.seams[A.leaves[h.leaf_off + r]].localspace_min[3] & 0xff;
         const int c0 = cEdgeVMap[e][0], c1 = cEdgeVMap[e][1];
         const int m0 = (corners >> c0) & 1, m1 = (corners >> c1) & 1;
         if (m0 == m1) continue;  // no sign change on the edge of the smallest leaf: no quad
@@ -397,7 +434,8 @@ __global__ void __launch_bounds__(kBuildThreads) k_seam_build(SeamArgs A) {
         unmorton(ent_code(me), h.lev, unit_log, lmin);
         int32_t line[3];
         for (int a = 0; a < 3; a++) line[a] = lmin[a] + cbit(c0, a) * s;
-        const int slot_entry = dir * 2;  // cellProcEdgeMask entry whose children give the slots' sides
+        // the four leaves around the edge, in the order ContourEdgeProc passes
+        // them (the children of cellProcEdgeMask's first entry along dir)
         int rank[4];
         bool ok = true;
         for (int q = 0; q < 4 && ok; q++) {
@@ -405,7 +443,7 @@ __global__ void __launch_bounds__(kBuildThreads) k_seam_build(SeamArgs A) {
                 rank[q] = r;
                 continue;
             }
-            const int child = cCellProcEdgeMask[slot_entry][q];
+            const int child = cCellProcEdgeMask[2 * dir][q];
             int32_t rel[3];
             for (int a = 0; a < 3; a++) rel[a] = a == dir ? lmin[a] : line[a] - s + cbit(child, a) * s;
             rank[q] = find_leaf(v, rel, sl);
@@ -436,25 +474,38 @@ __global__ void __launch_bounds__(kBuildThreads) k_seam_build(SeamArgs A) {
             }
         }
         if (one_block) continue;
-        const uint64_t key = path_key(2 * h.size, dir, line, lmin[dir], s);
-        const int qi = atomicAdd(&s_q, 1);
-        if (qi >= kMaxQuads) {
-            s_over = 1;
-            continue;
+        const int qi = atomicAdd(&A.qcounts[it.x], 1);  // < 12 n: every leaf edge emits at most once
+        A.qkey[h.quad_off + qi] = path_key(2 * h.size, dir, line, lmin[dir], s);
+        A.qval[h.quad_off + qi] = (uint64_t)rank[0] | ((uint64_t)rank[1] << kRankBits) |
+                                  ((uint64_t)rank[2] << (2 * kRankBits)) | ((uint64_t)rank[3] << (3 * kRankBits)) |
+                                  ((uint64_t)(m1 != 1) << (4 * kRankBits));
+    }
+}
+
+// The quads of host list[blockIdx.x] in the recursion's order: payloads
+// sorted in place, in shared memory when they fit `cap`.  With `only_above`,
+// hosts with at most that many quads are left to the other size class.
+__global__ void __launch_bounds__(1024) k_seam_qsort(SeamArgs A, const int32_t* list, int cap, int only_above) {
+    extern __shared__ uint64_t smem[];
+    const int hi = list[blockIdx.x];
+    const SeamHost h = A.hosts[hi];
+    const int nq = A.qcounts[hi];
+    if (nq <= only_above || (only_above < 0 && nq > kSmallQuads)) return;
+    uint64_t* key = A.qkey + h.quad_off;
+    uint64_t* val = A.qval + h.quad_off;
+    if (nq <= cap) {
+        uint64_t* sk = smem;
+        uint64_t* sv = smem + cap;
+        for (int i = threadIdx.x; i < nq; i += blockDim.x) {
+            sk[i] = key[i];
+            sv[i] = val[i];
         }
-        qkey[qi] = key;
-        qval[qi] = (uint64_t)rank[0] | ((uint64_t)rank[1] << kRankBits) | ((uint64_t)rank[2] << (2 * kRankBits)) |
-                   ((uint64_t)rank[3] << (3 * kRankBits)) | ((uint64_t)(m1 != 1) << (4 * kRankBits));
+        __syncthreads();
+        block_sort<true>(sk, sv, nq);
+        for (int i = threadIdx.x; i < nq; i += blockDim.x) val[i] = sv[i];
+    } else {
+        block_sort<true>(key, val, nq);
     }
-    __syncthreads();
-    if (s_over) {
-        if (threadIdx.x == 0) A.qcounts[blockIdx.x] = -1;
-        return;
-    }
-    const int nq = s_q;
-    block_sort<true>(qkey, qval, nq);
-    for (int i = threadIdx.x; i < nq; i += blockDim.x) A.quads[h.quad_off + i] = qval[i];
-    if (threadIdx.x == 0) A.qcounts[blockIdx.x] = nq;
 }
 
 // vertices (hosts with triangles only) and triangles, back to back by host
@@ -479,7 +530,7 @@ __global__ void __launch_bounds__(256) k_seam_emit(SeamArgs A) {
     }
     const uint64_t mask = (1ull << kRankBits) - 1;
     for (int i = threadIdx.x; i < nq; i += blockDim.x) {
-        const uint64_t q = A.quads[h.quad_off + i];
+        const uint64_t q = A.qval[h.quad_off + i];
         const int i0 = (int)(q & mask), i1 = (int)((q >> kRankBits) & mask), i2 = (int)((q >> (2 * kRankBits)) & mask),
                   i3 = (int)((q >> (3 * kRankBits)) & mask);
         const bool flip = (q >> (4 * kRankBits)) & 1;
@@ -519,14 +570,17 @@ struct Grow {
 struct SeamWork {
     std::mutex mu;
     int device = -1;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr, side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_fork2 = nullptr, ev_join2 = nullptr;
     Grow<SeamHost> hosts;
-    Grow<int2> pairs;
+    Grow<int4> pairs;
     Grow<int4> chunks;
     Grow<int32_t> seam_offsets, counts, qcounts;
     Grow<lvn_seam_node> seams;
-    Grow<uint32_t> leaves;
-    Grow<uint64_t> quads;
+    Grow<uint64_t> sel, ent, qkey, qval;
+    Grow<uint32_t> slots, leaves;
+    Grow<int2> items;
+    Grow<int32_t> lists;
     Grow<int64_t> offs;  // vertex offsets, triangle offsets
     Grow<lvn_mesh_vertex> vstage;
     Grow<lvn_mesh_triangle> tstage;
@@ -627,18 +681,29 @@ int lvn_seam_generate(const lvn_chunk_desc* chunks, const int32_t* seam_offsets,
         if (d.size < CLIPMAP_LEAF_SIZE || (d.size & (d.size - 1)) || !act.in_root(d.min, d.size) ||
             seam_offsets[c + 1] < seam_offsets[c])
             return LVN_ERR_INVALID;
-        act.active[{d.min[0], d.min[1], d.min[2], d.size}] = c;
+        if (!act.active.emplace(std::array<int32_t, 4>{d.min[0], d.min[1], d.min[2], d.size}, c).second)
+            return LVN_ERR_INVALID;  // listed twice
         for (int32_t s = d.size * 2; s <= root_size; s *= 2) {
             int32_t a[3];
             for (int k = 0; k < 3; k++) a[k] = root_min[k] + (int32_t)(((int64_t)d.min[k] - root_min[k]) / s * s);
             if (!act.above.insert({a[0], a[1], a[2], s}).second) break;
         }
     }
+    // the clipmap's active nodes never overlap: a chunk with a chunk above it is an error
+    for (const auto& kv : act.active) {
+        if (act.above.count(kv.first)) return LVN_ERR_INVALID;
+        const std::array<int32_t, 4>& k = kv.first;
+        for (int32_t s = k[3] * 2; s <= root_size; s *= 2) {
+            int32_t a[3];
+            for (int q = 0; q < 3; q++) a[q] = root_min[q] + (int32_t)(((int64_t)k[q] - root_min[q]) / s * s);
+            if (act.active.count({a[0], a[1], a[2], s})) return LVN_ERR_INVALID;
+        }
+    }
     const int64_t num_seams = num_chunks ? seam_offsets[num_chunks] : 0;
     if (seam_offsets && num_chunks && seam_offsets[0] != 0) return LVN_ERR_INVALID;
     // the gathered (chunk, neighbour mask) pairs of every host
     std::vector<SeamHost> hv(num_hosts);
-    std::vector<int2> pairs;
+    std::vector<int4> pairs;
     for (int hi = 0; hi < num_hosts; hi++) {
         if (hosts[hi] < 0 || hosts[hi] >= num_chunks) return LVN_ERR_INVALID;
         const lvn_chunk_desc& d = chunks[hosts[hi]];
@@ -661,7 +726,7 @@ int lvn_seam_generate(const lvn_chunk_desc* chunks, const int32_t* seam_offsets,
             int mask = 0;
             const int c = found[k].first;
             for (; k < found.size() && found[k].first == c; k++) mask |= 1 << found[k].second;
-            pairs.push_back(make_int2(c, mask));
+            pairs.push_back(make_int4(c, mask, hi, 0));
             unit = std::min(unit, chunks[c].size / vpc);
         }
         h.pair_end = (int32_t)pairs.size();
@@ -677,7 +742,14 @@ int lvn_seam_generate(const lvn_chunk_desc* chunks, const int32_t* seam_offsets,
     if (w.device != dev) {
         if (w.device >= 0) return LVN_ERR_INVALID;  // the scratch lives on the first device used
         SM_TRY(cudaStreamCreateWithFlags(&w.stream, cudaStreamNonBlocking));
-        SM_TRY(cudaFuncSetAttribute(k_seam_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBuildSmem));
+        SM_TRY(cudaStreamCreateWithFlags(&w.side, cudaStreamNonBlocking));
+        SM_TRY(cudaEventCreateWithFlags(&w.ev_fork, cudaEventDisableTiming));
+        SM_TRY(cudaEventCreateWithFlags(&w.ev_join, cudaEventDisableTiming));
+        SM_TRY(cudaEventCreateWithFlags(&w.ev_fork2, cudaEventDisableTiming));
+        SM_TRY(cudaEventCreateWithFlags(&w.ev_join2, cudaEventDisableTiming));
+        SM_TRY(cudaFuncSetAttribute(k_seam_leaves, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLeafSmem));
+        SM_TRY(cudaFuncSetAttribute(k_seam_quads, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBigQuadSmem));
+        SM_TRY(cudaFuncSetAttribute(k_seam_qsort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSortSmem));
         w.device = dev;
     }
     if (num_hosts == 0) {
@@ -687,6 +759,14 @@ int lvn_seam_generate(const lvn_chunk_desc* chunks, const int32_t* seam_offsets,
     const size_t nh = (size_t)num_hosts;
     SM_TRY(w.hosts.fit(nh));
     SM_TRY(w.pairs.fit(std::max<size_t>(pairs.size(), 1)));
+    int64_t sel_total = 0;
+    for (size_t i = 0; i < nh; i++) {
+        hv[i].sel_off = sel_total;
+        for (int p = hv[i].pair_begin; p < hv[i].pair_end; p++)
+            sel_total += seam_offsets[pairs[p].x + 1] - seam_offsets[pairs[p].x];
+    }
+    SM_TRY(w.sel.fit(std::max<int64_t>(sel_total, 1)));
+    SM_TRY(w.slots.fit(std::max<int64_t>(sel_total, 1)));
     SM_TRY(w.chunks.fit(std::max(num_chunks, 1)));
     SM_TRY(w.seam_offsets.fit((size_t)num_chunks + 1));
     SM_TRY(w.counts.fit(nh));
@@ -697,7 +777,7 @@ int lvn_seam_generate(const lvn_chunk_desc* chunks, const int32_t* seam_offsets,
     for (int c = 0; c < num_chunks; c++)
         c4[c] = make_int4(chunks[c].min[0], chunks[c].min[1], chunks[c].min[2], chunks[c].size);
     cudaStream_t st = w.stream;
-    SM_TRY(cudaMemcpyAsync(w.pairs.p, pairs.data(), sizeof(int2) * pairs.size(), cudaMemcpyHostToDevice, st));
+    SM_TRY(cudaMemcpyAsync(w.pairs.p, pairs.data(), sizeof(int4) * pairs.size(), cudaMemcpyHostToDevice, st));
     SM_TRY(cudaMemcpyAsync(w.chunks.p, c4.data(), sizeof(int4) * num_chunks, cudaMemcpyHostToDevice, st));
     SM_TRY(cudaMemcpyAsync(w.seam_offsets.p, seam_offsets, sizeof(int32_t) * (num_chunks + 1), cudaMemcpyHostToDevice,
                            st));
@@ -718,31 +798,91 @@ int lvn_seam_generate(const lvn_chunk_desc* chunks, const int32_t* seam_offsets,
     A.counts = w.counts.p;
     A.qcounts = w.qcounts.p;
     for (int a = 0; a < 3; a++) A.colour[a] = colour[a];
-    // 1: leaves per host
+    A.sel = w.sel.p;
+    A.slots = w.slots.p;
+    // 1: the selected seam nodes of every host
     SM_TRY(cudaMemcpyAsync(w.hosts.p, hv.data(), sizeof(SeamHost) * nh, cudaMemcpyHostToDevice, st));
-    k_seam_count<<<num_hosts, 256, 0, st>>>(A);
-    SM_TRY(cudaGetLastError());
+    SM_TRY(cudaMemsetAsync(w.counts.p, 0, sizeof(int32_t) * nh, st));
+    if (!pairs.empty()) {
+        k_seam_select<<<(int)pairs.size(), 128, 0, st>>>(A);
+        SM_TRY(cudaGetLastError());
+    }
     SM_TRY(cudaMemcpyAsync(w.hcounts.p, w.counts.p, sizeof(int32_t) * nh, cudaMemcpyDeviceToHost, st));
     SM_TRY(cudaStreamSynchronize(st));
     int64_t leaf_total = 0, quad_total = 0;
     bool limit = false;
+    std::vector<int2> items, big_items;  // (host, first leaf) of the quad enumeration's CTAs
+    std::vector<int32_t> small_hosts, big_hosts;  // size classes of the sorts
     for (size_t i = 0; i < nh; i++) {
         const int n = w.hcounts.p[i];
         limit |= n > kMaxLeaves;
         hv[i].leaf_off = leaf_total;
         hv[i].quad_off = quad_total;
         leaf_total += n;
-        quad_total += std::min<int64_t>(12 * (int64_t)n, kMaxQuads);
+        quad_total += 12 * (int64_t)n;
+        (n <= kSmallLeaves ? small_hosts : big_hosts).push_back((int32_t)i);
+        if (n <= kSmemLeaves)
+            for (int r = 0; r < n; r += kQuadBlock) items.push_back(make_int2((int)i, r));
+        else
+            for (int r = 0; r < n; r += kBigQuadBlock) big_items.push_back(make_int2((int)i, r));
     }
     if (limit) return LVN_ERR_DEVICE_STATUS;
-    // 2: sorted leaves and quads per host
+    // 2: sorted leaves, quads, quads in order
+    SM_TRY(w.ent.fit(std::max<int64_t>(leaf_total, 1)));
     SM_TRY(w.leaves.fit(std::max<int64_t>(leaf_total, 1)));
-    SM_TRY(w.quads.fit(std::max<int64_t>(quad_total, 1)));
+    SM_TRY(w.qkey.fit(std::max<int64_t>(quad_total, 1)));
+    SM_TRY(w.qval.fit(std::max<int64_t>(quad_total, 1)));
+    SM_TRY(w.items.fit(std::max<size_t>(items.size() + big_items.size(), 1)));
+    SM_TRY(w.lists.fit(nh));
+    std::vector<int32_t> lists(small_hosts);
+    lists.insert(lists.end(), big_hosts.begin(), big_hosts.end());
+    SM_TRY(cudaMemcpyAsync(w.lists.p, lists.data(), sizeof(int32_t) * nh, cudaMemcpyHostToDevice, st));
+    const int32_t* d_small = w.lists.p;
+    const int32_t* d_big = w.lists.p + small_hosts.size();
+    items.insert(items.end(), big_items.begin(), big_items.end());
+    const int n_small = (int)(items.size() - big_items.size());
+    A.ent = w.ent.p;
     A.leaves = w.leaves.p;
-    A.quads = w.quads.p;
+    A.qkey = w.qkey.p;
+    A.qval = w.qval.p;
+    A.items = w.items.p;
     SM_TRY(cudaMemcpyAsync(w.hosts.p, hv.data(), sizeof(SeamHost) * nh, cudaMemcpyHostToDevice, st));
-    k_seam_build<<<num_hosts, kBuildThreads, kBuildSmem, st>>>(A);
+    SM_TRY(cudaMemcpyAsync(w.items.p, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice, st));
+    SM_TRY(cudaMemsetAsync(w.qcounts.p, 0, sizeof(int32_t) * nh, st));
+    // the large hosts' sorts and enumeration beside the small hosts', on the second stream
+    SM_TRY(cudaEventRecord(w.ev_fork, st));
+    SM_TRY(cudaStreamWaitEvent(w.side, w.ev_fork, 0));
+    if (!big_hosts.empty()) {
+        k_seam_leaves<<<(int)big_hosts.size(), 1024, kLeafSmem, w.side>>>(A, d_big, kSortLeaves);
+        SM_TRY(cudaGetLastError());
+    }
+    if (!small_hosts.empty()) {
+        k_seam_leaves<<<(int)small_hosts.size(), 256, kSmallLeafSmem, st>>>(A, d_small, kSmallLeaves);
+        SM_TRY(cudaGetLastError());
+    }
+    SM_TRY(cudaEventRecord(w.ev_fork2, st));
+    SM_TRY(cudaStreamWaitEvent(w.side, w.ev_fork2, 0));  // the enumeration reads every host's sorted leaves
+    if (!big_items.empty()) {
+        SeamArgs B = A;
+        B.items = w.items.p + n_small;
+        k_seam_quads<<<(int)big_items.size(), 1024, kBigQuadSmem, w.side>>>(B, kBigQuadBlock, kSortLeaves);
+        SM_TRY(cudaGetLastError());
+        SM_TRY(cudaEventRecord(w.ev_join, w.side));
+    }
+    if (n_small) {
+        k_seam_quads<<<n_small, 256, kQuadSmem, st>>>(A, kQuadBlock, kSmemLeaves);
+        SM_TRY(cudaGetLastError());
+    }
+    if (!big_items.empty()) SM_TRY(cudaStreamWaitEvent(st, w.ev_join, 0));
+    SM_TRY(cudaEventRecord(w.ev_join, st));
+    SM_TRY(cudaStreamWaitEvent(w.side, w.ev_join, 0));
+    // quad sorts: up to kSmallQuads quads in the small class, the rest (any host) on the side stream
+    k_seam_qsort<<<num_hosts, 256, kSmallSortSmem, st>>>(A, w.lists.p, kSmallQuads, -1);
     SM_TRY(cudaGetLastError());
+    k_seam_qsort<<<num_hosts, 1024, kSortSmem, w.side>>>(A, w.lists.p, kSmemQuads, kSmallQuads);
+    SM_TRY(cudaGetLastError());
+    SM_TRY(cudaEventRecord(w.ev_join2, w.side));
+    SM_TRY(cudaStreamWaitEvent(st, w.ev_join2, 0));
     SM_TRY(cudaMemcpyAsync(w.hcounts.p + nh, w.qcounts.p, sizeof(int32_t) * nh, cudaMemcpyDeviceToHost, st));
     SM_TRY(cudaStreamSynchronize(st));
     // 3: output layout: hosts with triangles, back to back
@@ -750,7 +890,6 @@ int lvn_seam_generate(const lvn_chunk_desc* chunks, const int32_t* seam_offsets,
     int64_t tv = 0, tt = 0;
     for (size_t i = 0; i < nh; i++) {
         const int nq = w.hcounts.p[nh + i];
-        if (nq < 0) return LVN_ERR_DEVICE_STATUS;
         const int nv = nq > 0 ? w.hcounts.p[i] : 0;
         lvn_chunk_result& r = out->chunks[i];
         std::memset(&r, 0, sizeof(r));

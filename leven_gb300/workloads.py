@@ -199,8 +199,18 @@ def clipmap_cameras(n_paths=64, per_path=64, seed=1):
     return np.array(out, np.float32)
 
 
+def clipmap_frame(seed=1):
+    """The clipmap's active nodes for one camera: SelectActiveClipmapNodes over
+    the 2^15-unit world at the starting camera of the caves path (428 nodes,
+    LOD 0-5, a disjoint tiling of the world), caves density."""
+    rng = MT19937(seed)
+    cam = (rng.uniform(-2048.0, 2048.0), rng.uniform(-64.0, 64.0), rng.uniform(-2048.0, 2048.0))
+    nodes = select_clipmap_nodes(CLIPMAP_ROOT_MIN, CLIPMAP_ROOT_SIZE, cam)
+    return Workload(f"clipmap-frame-{len(nodes)}chunks-lod0-5", [(tuple(mn), size) for mn, size in nodes], [], CAVES)
+
+
 def clipmap_caves(n_chunks=1024, max_lod=4, seed=1):
-    """configs[2]: n_chunks chunks over clipmap LODs 0..max_lod, density = 2D
+    """n_chunks chunks over clipmap LODs 0..max_lod, density = 2D
     fBm heightfield + 3D fBm caves (6 octaves, 1/64, amplitude 12).  One
     camera selects about 370 nodes of LOD <= 4 (SelectActiveClipmapNodes over
     a 2^15-unit world centred on the origin), so the chunks are the union of

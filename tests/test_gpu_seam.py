@@ -75,3 +75,8 @@ def test_seams_errors(lvn_gpu):
         lvn.seam_generate(chunks, offs, seams, 16, (-1024, -1024, -1024), 2048, [3])  # host out of range
     with pytest.raises(lvn.LvnError):
         lvn.seam_generate([((0, 0, 0), 384)], offs, seams, 16, (-1024, -1024, -1024), 2048, [0])  # not a node size
+    two = np.array([0, 0, 0], np.int32)
+    with pytest.raises(lvn.LvnError):  # overlapping active nodes
+        lvn.seam_generate([((0, 0, 0), 256), ((0, 0, 0), 512)], two, seams, 16, (-1024, -1024, -1024), 2048, [0])
+    with pytest.raises(lvn.LvnError):  # a chunk listed twice
+        lvn.seam_generate([((0, 0, 0), 256), ((0, 0, 0), 256)], two, seams, 16, (-1024, -1024, -1024), 2048, [0])
