@@ -481,7 +481,7 @@ def run_lvn(args):
 
 
 PROFILE_TAG = {"tiled": "tiled_csg_128", "clipmap": "clipmap_caves_1024", "one": "one_chunk",
-               "select": "select_4096", "seams": "seams_clipmap_frame_428"}
+               "select": "select_4096", "seams": "clipmap_frame_428"}
 
 
 def committed_traffic(kernel):
@@ -961,10 +961,10 @@ def run_seams(args):
                    "timing": "host clock around the synchronous C-ABI call (its own stream, three waits)"},
         "e2e": {"value": round(n / (ms_e2e / 1e3), 1), "unit": "seam meshes/s", "h2d_bytes_per_step": int(48 * offs[-1]),
                 "d2h_bytes_per_step": int(48 * nv + 12 * nt), "ms_per_step": round(ms_e2e, 4)},
-        "gpu_launches": 3,
+        "gpu_launches": 8,
         "roofline": {"bound": "hbm", "achieved": round(ach, 1), "peak": hbm_peak, "unit": "GB/s",
-                     "frac": round(ach / hbm_peak, 4), "traffic": committed_traffic("seam_build"),
-                     "kernel": "k_seam_build (+ count, emit)", "ms_per_launch": round(ms, 4),
+                     "frac": round(ach / hbm_peak, 4), "traffic": None,
+                     "kernel": "k_seam_select/leaves/quads/qsort/emit (one call)", "ms_per_launch": round(ms, 4),
                      "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
                      "algorithmic_bytes_per_launch": algo},
         "clocks": clocks.summary(),

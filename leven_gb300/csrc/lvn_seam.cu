@@ -508,14 +508,16 @@ __global__ void __launch_bounds__(1024) k_seam_qsort(SeamArgs A, const int32_t* 
     }
 }
 
-// vertices (hosts with triangles only) and triangles, back to back by host
+// vertices (hosts with triangles only) and triangles, back to back by host;
+// blockIdx.y splits a host's ranges over gridDim.y CTAs
 __global__ void __launch_bounds__(256) k_seam_emit(SeamArgs A) {
     const SeamHost h = A.hosts[blockIdx.x];
     const int nq = A.qcounts[blockIdx.x];
     if (nq <= 0) return;
     const int n = A.counts[blockIdx.x];
     const int64_t vo = A.vout_off[blockIdx.x], to = A.tout_off[blockIdx.x];
-    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    const int t0 = blockIdx.y * blockDim.x + threadIdx.x, step = gridDim.y * blockDim.x;
+    for (int r = t0; r < n; r += step) {
         const lvn_seam_node s = A.seams[A.leaves[h.leaf_off + r]];
         lvn_mesh_vertex v;
         for (int a = 0; a < 3; a++) {
@@ -529,7 +531,7 @@ __global__ void __launch_bounds__(256) k_seam_emit(SeamArgs A) {
         A.vout[vo + r] = v;
     }
     const uint64_t mask = (1ull << kRankBits) - 1;
-    for (int i = threadIdx.x; i < nq; i += blockDim.x) {
+    for (int i = t0; i < nq; i += step) {
         const uint64_t q = A.qval[h.quad_off + i];
         const int i0 = (int)(q & mask), i1 = (int)((q >> kRankBits) & mask), i2 = (int)((q >> (2 * kRankBits)) & mask),
                   i3 = (int)((q >> (3 * kRankBits)) & mask);
@@ -921,7 +923,7 @@ int lvn_seam_generate(const lvn_chunk_desc* chunks, const int32_t* seam_offsets,
         A.vout = w.vstage.p;
         A.tout = w.tstage.p;
     }
-    k_seam_emit<<<num_hosts, 256, 0, st>>>(A);
+    k_seam_emit<<<dim3(num_hosts, 16), 256, 0, st>>>(A);
     SM_TRY(cudaGetLastError());
     if (out->memory == LVN_MEMORY_HOST) {
         SM_TRY(cudaMemcpyAsync(out->vertices, w.vstage.p, sizeof(lvn_mesh_vertex) * tv, cudaMemcpyDeviceToHost, st));
