@@ -386,6 +386,35 @@ int lvn_seam_generate(const lvn_chunk_desc* chunks, const int32_t* seam_offsets,
                       const int32_t root_min[3], int32_t root_size, const int32_t* hosts, int32_t num_hosts,
                       const float colour[3], lvn_batch_out* out);
 
+/* ---- edge-collapse mesh simplification (ngMeshSimplifier) -----------------
+ * MeshSimplificationOptions (ng_mesh_simplify.h:8-31); the clipmap scales
+ * max_error and max_edge_size by the node's leaf size (clipmap.cpp:456-462). */
+typedef struct lvn_simplify_options {
+    float   edge_fraction;      /* candidate edges drawn per iteration        */
+    int32_t max_iterations;
+    float   target_percentage;  /* stop at this fraction of the triangles     */
+    float   max_error;          /* 1 / QEF error, plus the degree penalty     */
+    float   max_edge_size;
+    float   min_angle_cosine;
+} lvn_simplify_options;
+/* the header's defaults: 0.125, 10, 0.05, 5, 2.5, 0.8 */
+void lvn_simplify_options_default(lvn_simplify_options* options);
+/* ngMeshSimplifier (ng_mesh_simplify.cpp:441-540) for num_meshes meshes in
+ * one launch.  Mesh m is vertices[meshes[m].vertex_offset ..
+ * + num_vertices) with triangles[triangle_offset .. + num_triangles)
+ * (indices local to the mesh), worldSpaceOffset offsets[4m .. 4m + 3] and
+ * options[m]; inputs and outputs in host or device memory per `memory`.  The
+ * simplified mesh is written at the same offsets of out_vertices /
+ * out_triangles (which may be the inputs) and meshes[m]'s counts are updated.
+ * Meshes under 100 triangles or vertices are copied unchanged, as in the
+ * reference.  The QEF's approximate _mm_rsqrt_ps (qef_simd.h:209) is an exact
+ * 1 / sqrt here; the random candidate edges follow std::mt19937(42) with
+ * libstdc++'s uniform_int_distribution. */
+int lvn_mesh_simplify(const lvn_mesh_vertex* vertices, const lvn_mesh_triangle* triangles, int32_t memory,
+                      lvn_chunk_result* meshes, int32_t num_meshes, const float* offsets,
+                      const lvn_simplify_options* options, lvn_mesh_vertex* out_vertices,
+                      lvn_mesh_triangle* out_triangles);
+
 #ifdef __cplusplus
 }
 #endif

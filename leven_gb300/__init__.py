@@ -70,6 +70,11 @@ class ChunkResult(C.Structure):
                 ("num_edges", C.c_int32), ("num_nodes", C.c_int32)]
 
 
+class SimplifyOptions(C.Structure):
+    _fields_ = [("edge_fraction", C.c_float), ("max_iterations", C.c_int32), ("target_percentage", C.c_float),
+                ("max_error", C.c_float), ("max_edge_size", C.c_float), ("min_angle_cosine", C.c_float)]
+
+
 class BatchOut(C.Structure):
     _fields_ = [("memory", C.c_int32), ("vertices", C.c_void_p), ("vertex_capacity", C.c_int64),
                 ("total_vertices", C.c_int64), ("triangles", C.c_void_p), ("triangle_capacity", C.c_int64),
@@ -91,6 +96,7 @@ EXPORTS = [
     "lvn_surrogate_eval", "lvn_surrogate_eval_lattices", "lvn_surrogate_domain", "lvn_surrogate_get_stream",
     "lvn_meshgen_set_surrogate", "lvn_meshgen_surrogate_chunks", "lvn_density_f64",
     "lvn_clipmap_select", "lvn_clipmap_select_device", "lvn_clipmap_touched", "lvn_seam_generate",
+    "lvn_simplify_options_default", "lvn_mesh_simplify",
 ]
 
 _lib = None
@@ -153,6 +159,10 @@ def lib():
     L.lvn_clipmap_select_device.argtypes = [C.c_void_p, C.c_int32, i32p, C.c_int32, C.c_void_p, C.c_int32,
                                             C.c_void_p, C.c_void_p]
     L.lvn_clipmap_touched.argtypes = [C.POINTER(CsgOp), C.c_int32, i32p, C.c_int32, C.c_void_p, C.c_int32, i32p]
+    L.lvn_simplify_options_default.argtypes = [C.POINTER(SimplifyOptions)]
+    L.lvn_simplify_options_default.restype = None
+    L.lvn_mesh_simplify.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(ChunkResult), C.c_int32, C.c_void_p,
+                                    C.POINTER(SimplifyOptions), C.c_void_p, C.c_void_p]
     L.lvn_seam_generate.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32, i32p,
                                     C.c_int32, C.c_void_p, C.c_int32, C.c_float * 3, C.POINTER(BatchOut)]
     L.lvn_surrogate_get_stream.restype = C.c_void_p
@@ -283,6 +293,50 @@ def seam_generate(chunks, seam_offsets, seams, voxels_per_chunk, root_min, root_
         _check(rc, "lvn_seam_generate")
         res = np.ctypeslib.as_array(C.cast(results, C.POINTER(C.c_int32)), shape=(max(1, len(hs)), 8))[:len(hs)]
         return v[:bo.total_vertices].copy(), t[:bo.total_triangles].copy(), res.copy()
+
+
+def engine_simplify_options(size, max_error=5.0, max_edge_len=2.5, min_cos=0.7):
+    """The options ConstructClipmapNodeData passes for a node of `size`
+    (clipmap.cpp:456-462, with the engine's Options defaults, options.h:14-16)."""
+    o = SimplifyOptions()
+    lib().lvn_simplify_options_default(C.byref(o))
+    leaf = 4.0 * (size / 256)
+    o.max_error, o.max_edge_size, o.min_angle_cosine = max_error * leaf, max_edge_len * leaf, min_cos
+    return o
+
+
+def node_offset(mn, size):
+    """worldSpaceOffset of a clipmap node: vec4(vec3(min) + vec3(size / 2.f), 0) (clipmap.cpp:455)."""
+    return [float(np.float32(mn[a]) + np.float32(size / 2.0)) for a in range(3)] + [0.0]
+
+
+def mesh_simplify(vertices, triangles, ranges, offsets, options):
+    """ngMeshSimplifier (ng_mesh_simplify.cpp:441-540) for every mesh of a
+    batch in one launch.  vertices (V, 12) f32 and triangles (T, 3) i32 as
+    host arrays, or CUDA tensors (simplified in place); ranges (M, 4) =
+    (vertex offset, vertices, triangle offset, triangles); offsets (M, 4);
+    options: one SimplifyOptions per mesh.  Returns (vertices, triangles,
+    ranges) with the simplified meshes at the same offsets."""
+    r = np.ascontiguousarray(np.asarray(ranges, np.int32).reshape(-1, 4))
+    m = len(r)
+    res = (ChunkResult * max(1, m))()
+    for i in range(m):
+        res[i].vertex_offset, res[i].num_vertices, res[i].triangle_offset, res[i].num_triangles = (int(x) for x in r[i])
+    offs = np.ascontiguousarray(np.asarray(offsets, np.float32).reshape(-1, 4))
+    opts = (SimplifyOptions * max(1, m))(*options)
+    if isinstance(vertices, np.ndarray):
+        v = np.ascontiguousarray(vertices, np.float32)
+        t = np.ascontiguousarray(triangles, np.int32)
+        ov, ot = v.copy(), t.copy()
+        _check(lib().lvn_mesh_simplify(v.ctypes.data, t.ctypes.data, LVN_MEMORY_HOST, res, m, offs.ctypes.data, opts,
+                                       ov.ctypes.data, ot.ctypes.data), "lvn_mesh_simplify")
+    else:
+        ov, ot = vertices, triangles
+        _check(lib().lvn_mesh_simplify(vertices.data_ptr(), triangles.data_ptr(), LVN_MEMORY_DEVICE, res, m,
+                                       offs.ctypes.data, opts, vertices.data_ptr(), triangles.data_ptr()),
+               "lvn_mesh_simplify")
+    out = np.ctypeslib.as_array(C.cast(res, C.POINTER(C.c_int32)), shape=(max(1, m), 8))[:m, :4].copy()
+    return ov, ot, out
 
 
 def clipmap_touched(ops, root_min, root_size):

@@ -2067,6 +2067,298 @@ Mesh seam_mesh(const Clipmap& cm, const Input& in, int h) {
 
 }  // namespace seam
 
+// ---- edge-collapse mesh simplification ------------------------------------------
+//
+// ngMeshSimplifier (ng_mesh_simplify.cpp:441-540) with its QEF
+// (qef_simd.h:93-530) restated in scalar float arithmetic, lane by lane as the
+// SSE code computes it.  One deliberate difference: givens_coeffs_sym's
+// c = _mm_rsqrt_ps(1 + tan^2) (qef_simd.h:209), an approximation whose result
+// differs between x86 implementations, is 1 / sqrt(1 + tan^2) correctly
+// rounded here.  The random edge subsets come from std::mt19937 and
+// std::uniform_int_distribution as the reference calls them (libstdc++'s
+// distribution; an MSVC build of the reference draws differently).
+
+namespace collapse {
+
+struct Opt {
+    float edge_fraction;
+    int32_t max_iterations;
+    float target_percentage;
+    float max_error;
+    float max_edge_size;
+    float min_angle_cosine;
+};
+struct MV {  // MeshVertex
+    float p[4], n[4], c[4];
+};
+
+float dot4(const float a[4], const float b[4]) {  // vec4_dot (qef_simd.h:101-109)
+    float m[4];
+    for (int i = 0; i < 4; i++) m[i] = a[i] * b[i];
+    return (m[0] + m[1]) + (m[3] + m[2]);
+}
+void mul_m4(const float a[4], const float B[4][4], float r[4]) {  // vec4_mul_m4x4 (qef_simd.h:114-121)
+    for (int j = 0; j < 4; j++) {
+        float t = a[0] * B[0][j];
+        t = t + a[1] * B[1][j];
+        t = t + a[2] * B[2][j];
+        t = t + a[3] * B[3][j];
+        r[j] = t;
+    }
+}
+
+void givens(const float vt[4][4], float c[3], float s[3]) {  // givens_coeffs_sym (qef_simd.h:163-224)
+    const float pp[3] = {vt[0][0], vt[0][0], vt[1][1]};
+    const float pq[3] = {vt[0][1], vt[0][2], vt[1][2]};
+    const float qq[3] = {vt[1][1], vt[2][2], vt[2][2]};
+    for (int k = 0; k < 3; k++) {
+        const float tau = (qq[k] - pp[k]) / (pq[k] * 2.f);
+        const float stt = std::sqrt(tau * tau + 1.f);
+        const float tan = 1.f / (tau >= 0.f ? tau + stt : tau - stt);
+        const float ck = 1.f / std::sqrt(1.f + tan * tan);
+        const float sk = tan * ck;
+        c[k] = pq[k] == 0.f ? 1.f : ck;
+        s[k] = pq[k] == 0.f ? 0.f : sk;
+    }
+}
+
+void rotateq_xy(float vt[4][4], const float c[3], const float s[3]) {  // qef_simd.h:228-277, as written
+    const float u[3] = {vt[0][0], vt[0][0], vt[1][1]};
+    const float v[3] = {vt[1][1], vt[2][2], vt[2][2]};
+    const float a[3] = {vt[0][1], vt[0][2], vt[1][2]};
+    float x[3], y[3];
+    for (int k = 0; k < 3; k++) {
+        const float cc = c[k] * c[k], ss = s[k] * s[k];
+        const float mx = ((2.f * c[k]) * s[k]) * a[k];
+        const float x0 = cc * u[k];
+        x[k] = (x0 - mx) + ss * v[k];
+        y[k] = (x0 + mx) + (cc + v[k]);
+    }
+    vt[0][0] = x[0];
+    vt[0][0] = x[1];
+    vt[1][1] = x[2];
+    vt[0][1] = y[0];
+    vt[0][2] = y[1];
+    vt[1][2] = y[2];
+}
+
+void svd_rotate(float vt[4][4], float V[4][4], float c, float s, int a, int b) {  // qef_simd.h:281-322
+    if (vt[a][b] == 0.f) return;
+    const float u[4] = {V[0][a], V[1][a], V[2][a], vt[0][3 - b]};
+    const float v[4] = {V[0][b], V[1][b], V[2][b], vt[1 - a][2]};
+    float x[4], y[4];
+    for (int k = 0; k < 4; k++) {
+        x[k] = c * u[k] - s * v[k];
+        y[k] = s * u[k] + c * v[k];
+    }
+    for (int i = 0; i < 3; i++) V[i][a] = x[i];
+    vt[0][3 - b] = x[3];
+    for (int i = 0; i < 3; i++) V[i][b] = y[i];
+    vt[1 - a][2] = y[3];
+    vt[a][b] = 0.f;
+}
+
+// qef_solve_from_points over two (position, normal) pairs (qef_simd.h:403-480)
+float qef2(const MV& v0, const MV& v1, float out[4]) {
+    float ATA[4][4] = {}, ATb[4] = {}, acc[4] = {};
+    const MV* vs[2] = {&v0, &v1};
+    for (const MV* v : vs) {
+        const float* n = v->n;
+        for (int r = 0; r < 3; r++)
+            for (int j = 0; j < 4; j++) ATA[r][j] = ATA[r][j] + n[r] * n[j];
+        const float d = dot4(v->p, n);
+        for (int j = 0; j < 3; j++) ATb[j] = ATb[j] + d * n[j];
+        ATb[3] = ATb[3] + 0.f * n[3];
+        for (int j = 0; j < 4; j++) acc[j] = acc[j] + v->p[j];
+    }
+    float mass[4];
+    for (int j = 0; j < 4; j++) mass[j] = acc[j] / acc[3];
+    float p[4];
+    mul_m4(mass, ATA, p);
+    for (int j = 0; j < 4; j++) p[j] = ATb[j] - p[j];
+    // svd_solve_ATA_ATb (qef_simd.h:384-399)
+    float V[4][4] = {{1.f, 0.f, 0.f, 0.f}, {0.f, 1.f, 0.f, 0.f}, {0.f, 0.f, 1.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+    float vt[4][4];
+    std::memcpy(vt, ATA, sizeof(vt));
+    for (int sweep = 0; sweep < 5; sweep++) {
+        float c[3], s[3];
+        givens(vt, c, s);
+        rotateq_xy(vt, c, s);
+        svd_rotate(vt, V, c[0], s[0], 0, 1);
+        svd_rotate(vt, V, c[1], s[1], 0, 2);
+        svd_rotate(vt, V, c[2], s[2], 1, 2);
+    }
+    const float sigma[4] = {vt[0][0], vt[1][1], vt[2][2], 0.f};
+    float inv[4];
+    for (int j = 0; j < 4; j++) {  // svd_invdet (qef_simd.h:354-365)
+        const float ox = 1.f / sigma[j];
+        const float ax = std::fabs(sigma[j]), aox = std::fabs(ox);
+        const float mn = ax < aox ? ax : aox;
+        inv[j] = mn >= 0.1f ? ox : 0.f;
+    }
+    float O[4][4];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 4; j++) O[i][j] = V[i][j] * inv[j];
+    for (int j = 0; j < 4; j++) O[3][j] = 0.f;
+    for (int i = 0; i < 4; i++) {
+        float row[4];
+        mul_m4(O[i], V, row);
+        std::memcpy(O[i], row, sizeof(row));
+    }
+    float x[4];
+    mul_m4(p, O, x);
+    float t[4];
+    mul_m4(x, ATA, t);
+    for (int j = 0; j < 4; j++) t[j] = ATb[j] - t[j];
+    const float error = dot4(t, t);
+    for (int j = 0; j < 4; j++) out[j] = x[j] + mass[j];
+    return error;
+}
+
+struct Edge {
+    uint32_t mn, mx;
+    uint64_t idx() const { return (uint64_t)mn | ((uint64_t)mx << 32); }  // the union's idx_ (little endian)
+};
+
+// ngMeshSimplifier (ng_mesh_simplify.cpp:441-540); returns the simplified mesh
+void simplify(std::vector<MV>& verts, std::vector<std::array<int32_t, 3>>& tris, const float offset[4],
+              const Opt& o) {
+    if (tris.size() < 100 || verts.size() < 100) return;
+    std::vector<MV> vs = verts;
+    for (MV& v : vs)
+        for (int j = 0; j < 4; j++) v.p[j] = v.p[j] - offset[j];
+    std::vector<std::array<int32_t, 3>> ts = tris;
+    // BuildCandidateEdges (ng_mesh_simplify.cpp:122-177)
+    std::vector<Edge> edges;
+    for (const auto& t : ts) {
+        edges.push_back({(uint32_t)std::min(t[0], t[1]), (uint32_t)std::max(t[0], t[1])});
+        edges.push_back({(uint32_t)std::min(t[1], t[2]), (uint32_t)std::max(t[1], t[2])});
+        edges.push_back({(uint32_t)std::min(t[0], t[2]), (uint32_t)std::max(t[0], t[2])});
+    }
+    std::sort(edges.begin(), edges.end(), [](const Edge& a, const Edge& b) { return a.idx() < b.idx(); });
+    std::vector<Edge> filtered;
+    std::vector<char> boundary(vs.size(), 0);
+    Edge prev = edges[0];
+    int count = 1;
+    for (size_t i = 1; i < edges.size(); i++) {  // the last run is never examined, as in the reference
+        const Edge cur = edges[i];
+        if (cur.idx() != prev.idx()) {
+            if (count == 1)
+                boundary[prev.mn] = boundary[prev.mx] = 1;
+            else
+                filtered.push_back(prev);
+            count = 1;
+        } else {
+            count++;
+        }
+        prev = cur;
+    }
+    edges.clear();
+    for (const Edge& e : filtered)
+        if (!boundary[e.mn] && !boundary[e.mx]) edges.push_back(e);
+    std::vector<int> degree(vs.size(), 0);
+    for (const auto& t : ts)
+        for (int k = 0; k < 3; k++) degree[t[k]]++;
+    const int target = (int)((float)ts.size() * o.target_percentage);
+    std::vector<float> cpos(4 * edges.size()), cnrm(4 * edges.size());
+    int iterations = 0;
+    while ((int)ts.size() > target && iterations++ < o.max_iterations) {
+        std::vector<int> edge_id(vs.size(), -1), coll_target(vs.size(), -1);
+        std::vector<int> valid;
+        // FindValidCollapses (ng_mesh_simplify.cpp:181-278)
+        std::mt19937 prng;
+        prng.seed(42);
+        const int num_random = (int)((float)edges.size() * o.edge_fraction);
+        std::uniform_int_distribution<int> dist(0, (int)(edges.size() - 1));
+        std::vector<int> random(num_random);
+        for (int i = 0; i < num_random; i++) random[i] = dist(prng);
+        std::sort(random.begin(), random.end());
+        std::vector<float> min_cost(vs.size(), FLT_MAX);
+        int valid_count = 0;
+        for (int i : random) {
+            const Edge& e = edges[i];
+            const MV& a = vs[e.mn];
+            const MV& b = vs[e.mx];
+            if (dot4(a.n, b.n) < o.min_angle_cosine) continue;
+            float d[4];
+            for (int j = 0; j < 4; j++) d[j] = b.p[j] - a.p[j];
+            if (dot4(d, d) > o.max_edge_size * o.max_edge_size) continue;
+            if ((double)std::fabs(a.c[3] - b.c[3]) > 1e-3) continue;
+            const int deg = degree[e.mn] + degree[e.mx];
+            if (deg > 16) continue;  // COLLAPSE_MAX_DEGREE
+            float pos[4];
+            float error = qef2(a, b, pos);
+            if (error > 0.f) error = 1.f / error;
+            const int penalty = std::max(0, deg - 10);
+            error += (float)penalty * (o.max_error * 0.1f);
+            if (error > o.max_error) continue;
+            valid.push_back(i);
+            for (int j = 0; j < 4; j++) cnrm[4 * i + j] = (a.n[j] - b.n[j]) * 0.5f;
+            cpos[4 * i] = pos[0];
+            cpos[4 * i + 1] = pos[1];
+            cpos[4 * i + 2] = pos[2];
+            cpos[4 * i + 3] = 1.f;
+            if (error < min_cost[e.mn]) {
+                min_cost[e.mn] = error;
+                edge_id[e.mn] = i;
+            }
+            if (error < min_cost[e.mx]) {
+                min_cost[e.mx] = error;
+                edge_id[e.mx] = i;
+            }
+            valid_count++;
+        }
+        if (valid_count == 0) break;
+        // CollapseEdges (ng_mesh_simplify.cpp:282-306)
+        for (int i : valid) {
+            const Edge& e = edges[i];
+            if (edge_id[e.mn] == i && edge_id[e.mx] == i) {
+                coll_target[e.mx] = (int)e.mn;
+                std::memcpy(vs[e.mn].p, &cpos[4 * i], 16);
+                std::memcpy(vs[e.mn].n, &cnrm[4 * i], 16);
+            }
+        }
+        // RemoveTriangles (ng_mesh_simplify.cpp:310-352)
+        std::fill(degree.begin(), degree.end(), 0);
+        std::vector<std::array<int32_t, 3>> kept;
+        for (auto t : ts) {
+            for (int k = 0; k < 3; k++)
+                if (coll_target[t[k]] != -1) t[k] = coll_target[t[k]];
+            if (t[0] == t[1] || t[0] == t[2] || t[1] == t[2]) continue;
+            for (int k = 0; k < 3; k++) degree[t[k]]++;
+            kept.push_back(t);
+        }
+        ts.swap(kept);
+        // RemoveEdges (ng_mesh_simplify.cpp:356-380)
+        std::vector<Edge> ek;
+        for (Edge e : edges) {
+            if (coll_target[e.mn] != -1) e.mn = (uint32_t)coll_target[e.mn];
+            if (coll_target[e.mx] != -1) e.mx = (uint32_t)coll_target[e.mx];
+            if (e.mn != e.mx) ek.push_back(e);
+        }
+        edges.swap(ek);
+    }
+    // CompactVertices (ng_mesh_simplify.cpp:384-421) and the offset added back
+    std::vector<char> used(vs.size(), 0);
+    for (const auto& t : ts)
+        for (int k = 0; k < 3; k++) used[t[k]] = 1;
+    std::vector<int> remap(vs.size(), -1);
+    std::vector<MV> out;
+    for (size_t i = 0; i < vs.size(); i++)
+        if (used[i]) {
+            remap[i] = (int)out.size();
+            out.push_back(vs[i]);
+        }
+    for (auto& t : ts)
+        for (int k = 0; k < 3; k++) t[k] = remap[t[k]];
+    for (MV& v : out)
+        for (int j = 0; j < 4; j++) v.p[j] = v.p[j] + offset[j];
+    verts.swap(out);
+    tris.swap(ts);
+}
+
+}  // namespace collapse
+
 extern "C" {
 
 int orc_clipmap_select(const float cam[3], const int32_t root_min[3], int32_t root_size, int32_t* out4, int32_t cap) {
@@ -2135,6 +2427,57 @@ int orc_seam_generate(const int32_t* chunks4, const int32_t* seam_offsets, int32
         ot += host_counts[2 * i + 1];
     }
     return 0;
+}
+
+int orc_mesh_collapse(const float* vertices, int32_t nv, const int32_t* triangles, int32_t nt, const float offset[4],
+                      const float options[6], float* out_vertices, int32_t* out_nv, int32_t* out_triangles,
+                      int32_t* out_nt) {
+    collapse::Opt o{options[0], (int32_t)options[1], options[2], options[3], options[4], options[5]};
+    std::vector<collapse::MV> vs(nv);
+    std::memcpy(vs.data(), vertices, sizeof(collapse::MV) * nv);
+    std::vector<std::array<int32_t, 3>> ts(nt);
+    std::memcpy(ts.data(), triangles, 12 * (size_t)nt);
+    collapse::simplify(vs, ts, offset, o);
+    std::memcpy(out_vertices, vs.data(), sizeof(collapse::MV) * vs.size());
+    std::memcpy(out_triangles, ts.data(), 12 * ts.size());
+    *out_nv = (int32_t)vs.size();
+    *out_nt = (int32_t)ts.size();
+    return 0;
+}
+
+int orc_uniform_draws(int32_t hi, int32_t n, int32_t* out) {
+    // the draws FindValidCollapses makes (ng_mesh_simplify.cpp:194-205)
+    std::mt19937 prng;
+    prng.seed(42);
+    std::uniform_int_distribution<int> dist(0, hi);
+    for (int i = 0; i < n; i++) out[i] = dist(prng);
+    return 0;
+}
+
+int64_t orc_mesh_collapse_many(const float* vertices, const int32_t* triangles, const int32_t* ranges, int32_t n,
+                               const float* offsets, const float* options, int32_t threads) {
+    if (threads < 1) threads = 1;
+    std::atomic<int> next{0};
+    std::atomic<int64_t> total{0};
+    auto worker = [&]() {
+        std::vector<float> ov;
+        std::vector<int32_t> ot;
+        for (;;) {
+            const int i = next.fetch_add(1);
+            if (i >= n) break;
+            const int32_t* r = ranges + 4 * i;  // vertex offset, vertices, triangle offset, triangles
+            ov.resize(12 * (size_t)std::max(r[1], 1));
+            ot.resize(3 * (size_t)std::max(r[3], 1));
+            int32_t nv = 0, nt = 0;
+            orc_mesh_collapse(vertices + 12 * (size_t)r[0], r[1], triangles + 3 * (size_t)r[2], r[3], offsets + 4 * i,
+                              options + 6 * i, ov.data(), &nv, ot.data(), &nt);
+            total += nt;
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; t++) pool.emplace_back(worker);
+    for (auto& t : pool) t.join();
+    return total.load();
 }
 
 int64_t orc_clipmap_select_many(const float* cams, int32_t n, const int32_t root_min[3], int32_t root_size,

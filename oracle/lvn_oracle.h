@@ -139,6 +139,23 @@ int orc_seam_generate(const int32_t* chunks4, const int32_t* seam_offsets, int32
                       int32_t num_hosts, const float colour[3], float* vertices, int64_t vertex_cap,
                       int32_t* triangles, int64_t triangle_cap, int32_t* host_counts, int32_t threads);
 
+/* ngMeshSimplifier (ng_mesh_simplify.cpp:441-540) on one mesh: vertices
+ * (MeshVertex, 12 floats) and triangles (3 int32), worldSpaceOffset (4 floats),
+ * options = MeshSimplificationOptions {edgeFraction, maxIterations,
+ * targetPercentage, maxError, maxEdgeSize, minAngleCosine} as 6 floats.  The
+ * outputs hold at most nv vertices and nt triangles. */
+int orc_mesh_collapse(const float* vertices, int32_t nv, const int32_t* triangles, int32_t nt, const float offset[4],
+                      const float options[6], float* out_vertices, int32_t* out_nv, int32_t* out_triangles,
+                      int32_t* out_nt);
+/* n draws of std::uniform_int_distribution<int>(0, hi) from std::mt19937
+ * seeded 42, as FindValidCollapses makes them */
+int orc_uniform_draws(int32_t hi, int32_t n, int32_t* out);
+/* CPU baseline: orc_mesh_collapse over n meshes on `threads` host threads;
+ * ranges = 4 per mesh (vertex offset, vertices, triangle offset, triangles),
+ * offsets 4 and options 6 floats per mesh; returns the total triangles left */
+int64_t orc_mesh_collapse_many(const float* vertices, const int32_t* triangles, const int32_t* ranges, int32_t n,
+                               const float* offsets, const float* options, int32_t threads);
+
 /* CPU baseline: mesh n chunks (each a fresh field with its ops) on `threads`
  * host threads; returns total vertices + triangles for sanity */
 int64_t orc_mesh_chunks(const orc_density* d, const orc_chunk_args* chunks, int32_t n,

@@ -84,6 +84,12 @@ def lib():
                                           C.c_int32]
         L.orc_clipmap_select_many.argtypes = [C.c_void_p, C.c_int32, C.c_int32 * 3, C.c_int32, C.c_int32]
         L.orc_clipmap_select_many.restype = C.c_int64
+        L.orc_mesh_collapse.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.POINTER(C.c_int32), C.c_void_p, C.POINTER(C.c_int32)]
+        L.orc_mesh_collapse_many.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
+                                             C.c_int32]
+        L.orc_mesh_collapse_many.restype = C.c_int64
+        L.orc_uniform_draws.argtypes = [C.c_int32, C.c_int32, C.c_void_p]
         L.orc_seam_generate.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32 * 3,
                                         C.c_int32, C.c_void_p, C.c_int32, C.c_float * 3, C.c_void_p, C.c_int64,
                                         C.c_void_p, C.c_int64, C.c_void_p, C.c_int32]
@@ -283,3 +289,37 @@ def seam_generate(chunks, seam_offsets, seams, vpc, root_min, root_size, hosts, 
         assert rc == 0, rc
         nv, nt = int(counts[:len(hs), 0].sum()), int(counts[:len(hs), 1].sum())
         return v[:nv], t[:nt], counts[:len(hs)]
+
+
+def simplify_options(size, max_error=5.0, max_edge_len=2.5, min_cos=0.7):
+    """The options ConstructClipmapNodeData passes for a node of `size`
+    (clipmap.cpp:456-462, Options defaults options.h:14-16) as the 6 floats
+    orc_mesh_collapse takes."""
+    leaf = 4.0 * (size / 256)
+    return np.array([0.125, 10, 0.05, max_error * leaf, max_edge_len * leaf, min_cos], np.float32)
+
+
+def node_offset(mn, size):
+    """worldSpaceOffset = vec4(vec3(min) + vec3(size / 2.f), 0) (clipmap.cpp:455)."""
+    return np.array([np.float32(mn[0]) + np.float32(size / 2.0), np.float32(mn[1]) + np.float32(size / 2.0),
+                     np.float32(mn[2]) + np.float32(size / 2.0), 0.0], np.float32)
+
+
+def mesh_collapse(vertices, triangles, offset, options):
+    """ngMeshSimplifier restated, one mesh: (vertices (V', 12), triangles (T', 3))."""
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 12)
+    t = np.ascontiguousarray(triangles, np.int32).reshape(-1, 3)
+    ov = np.zeros((max(1, len(v)), 12), np.float32)
+    ot = np.zeros((max(1, len(t)), 3), np.int32)
+    a, b = C.c_int32(), C.c_int32()
+    off = np.ascontiguousarray(offset, np.float32)
+    opt = np.ascontiguousarray(options, np.float32)
+    lib().orc_mesh_collapse(v.ctypes.data, len(v), t.ctypes.data, len(t), off.ctypes.data, opt.ctypes.data,
+                            ov.ctypes.data, C.byref(a), ot.ctypes.data, C.byref(b))
+    return ov[:a.value], ot[:b.value]
+
+
+def uniform_draws(hi, n):
+    out = np.zeros(max(1, n), np.int32)
+    lib().orc_uniform_draws(int(hi), int(n), out.ctypes.data)
+    return out[:n]
