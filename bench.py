@@ -29,6 +29,10 @@ active clipmap nodes one camera selects (LOD 0-5, caves density), from their
 seam nodes as the batch meshing left them in device memory (its own JSON line, impl "lvn-seams"; the
 reference arm times the oracle's octree construction and contouring on all
 host threads).
+`--workload collapse`: the engine's edge-collapse simplification
+(ngMeshSimplifier) of the same 428 meshes, each with its node's options as
+ConstructClipmapNodeData sets them (its own JSON line, impl "lvn-collapse";
+the reference arm times the oracle's simplifier on all host threads).
 `--surrogate`: trains the learned density surrogate on the GPU
 and meshes the clipmap chunk set with the 2D fBm density plain and through
 the surrogate (its own JSON line, impl "lvn-surrogate").
@@ -69,10 +73,11 @@ def parse():
     p.add_argument("--simplify", type=float, default=None,
                    help="octree simplification QEF-error threshold (voxel^2); default 0.05 for the clipmap "
                         "workload, off otherwise; < 0 = off")
-    p.add_argument("--workload", default="tiled", choices=["tiled", "clipmap", "one", "select", "seams"],
+    p.add_argument("--workload", default="tiled", choices=["tiled", "clipmap", "one", "select", "seams", "collapse"],
                    help="tiled: 128 LOD0 chunks + 32 CSG ops (default); clipmap: 1024 chunks over LOD 0-4 with "
                         "3D caves; one: a single LOD0 chunk; select: clipmap node selection for 4096 cameras; "
-                        "seams: the seam meshes of the 1024 clipmap chunks")
+                        "seams: the seam meshes of one camera's clipmap; collapse: the engine's edge-collapse "
+                        "simplification of that clipmap's meshes")
     return p.parse_args()
 
 
@@ -243,6 +248,8 @@ def run_reference(args):
         return run_select_reference(args)
     if WORKLOAD == "seams":
         return run_seams_reference(args)
+    if WORKLOAD == "collapse":
+        return run_collapse_reference(args)
     wl = workload()
     threads = host_threads()
     cb = CpuBaseline(wl, threads, simplify_threshold(args))
@@ -987,6 +994,176 @@ def run_seams(args):
     print(json.dumps(line), flush=True)
 
 
+COLLAPSE_METRIC = "clipmap meshes simplified/sec on 1 GB300 (ngMeshSimplifier, 64^3 chunks, LOD 0-5)"
+
+
+def collapse_inputs():
+    """One camera's clipmap meshed once on the GPU: (workload, vertices,
+    triangles, ranges (M, 4), offsets (M, 4)) for the meshes with triangles."""
+    import numpy as np
+
+    import leven_gb300 as lvn
+    from leven_gb300 import workloads as W
+
+    wl = W.clipmap_frame()
+    lvn.initialise(wl.noise_seed, 0, 2)
+    lvn.set_density(**wl.density)
+    lvn.clear_csg_operations()
+    g = lvn.MeshGen(64)
+    try:
+        v, t, _, res = g.generate_chunks(wl.chunks)
+    finally:
+        g.close()
+    keep = [i for i in range(len(wl.chunks)) if res[i, 3] > 0]
+    ranges = res[keep, :4].astype(np.int32)
+    offsets = np.array([lvn.node_offset(*wl.chunks[i]) for i in keep], np.float32)
+    sizes = [wl.chunks[i][1] for i in keep]
+    return wl, v, t, ranges, offsets, sizes
+
+
+def collapse_cpu(v, t, ranges, offsets, sizes, threads):
+    sys.path.insert(0, str(ROOT / "tests"))
+    import numpy as np
+    import oracle_lib as O
+
+    O.build()
+    opts = np.ascontiguousarray(np.stack([O.simplify_options(s) for s in sizes]).astype(np.float32))
+    vv = np.ascontiguousarray(v, np.float32)
+    tt = np.ascontiguousarray(t, np.int32)
+    rr = np.ascontiguousarray(ranges, np.int32)
+    oo = np.ascontiguousarray(offsets, np.float32)
+
+    def one():
+        t0 = time.perf_counter()
+        O.lib().orc_mesh_collapse_many(vv.ctypes.data, tt.ctypes.data, rr.ctypes.data, len(rr), oo.ctypes.data,
+                                       opts.ctypes.data, threads)
+        return time.perf_counter() - t0
+
+    return one
+
+
+def run_collapse_reference(args):
+    wl, v, t, ranges, offsets, sizes = collapse_inputs()
+    threads = host_threads()
+    one = collapse_cpu(v, t, ranges, offsets, sizes, threads)
+    for _ in range(args.warmup):
+        one()
+    vals = [len(ranges) / one() for _ in range(args.steps)]
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": COLLAPSE_METRIC, "value": round(value, 1), "unit": "meshes/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * len(ranges) / value, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"collapse-{wl.name}", "meshes": len(ranges), "triangles_in": int(ranges[:, 3].sum())},
+        "cpu_baseline": {"value": round(value, 1), "unit": "meshes/s", "cores": threads, "kind": "port",
+                         "sample": f"all {len(ranges)} meshes per step"},
+        "e2e": {"value": round(value, 1), "unit": "meshes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_collapse(args):
+    """The edge-collapse simplification of one camera's clipmap meshes:
+    meshes in device memory (value) and from / to pinned host arrays (e2e)."""
+    import numpy as np
+    import torch
+
+    import leven_gb300 as lvn
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    wl, v, t, ranges, offsets, sizes = collapse_inputs()
+    m = len(ranges)
+    opts = (lvn.SimplifyOptions * m)(*[lvn.engine_simplify_options(s) for s in sizes])
+    offs = np.ascontiguousarray(offsets, np.float32)
+    res = (lvn.ChunkResult * m)()
+
+    def reset():
+        for i in range(m):
+            res[i].vertex_offset, res[i].num_vertices, res[i].triangle_offset, res[i].num_triangles = (
+                int(x) for x in ranges[i])
+
+    d_v = torch.from_numpy(v).to(dev)
+    d_t = torch.from_numpy(t).to(dev)
+    d_ov = torch.empty_like(d_v)
+    d_ot = torch.empty_like(d_t)
+    h_v = torch.from_numpy(v).pin_memory()
+    h_t = torch.from_numpy(t).pin_memory()
+    h_ov = torch.empty_like(h_v).pin_memory()
+    h_ot = torch.empty_like(h_t).pin_memory()
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.int32, device=dev)
+    L = lvn.lib()
+
+    def call(device):
+        reset()
+        if device:
+            rc = L.lvn_mesh_simplify(d_v.data_ptr(), d_t.data_ptr(), lvn.LVN_MEMORY_DEVICE, res, m, offs.ctypes.data,
+                                     opts, d_ov.data_ptr(), d_ot.data_ptr())
+        else:
+            rc = L.lvn_mesh_simplify(h_v.data_ptr(), h_t.data_ptr(), lvn.LVN_MEMORY_HOST, res, m, offs.ctypes.data,
+                                     opts, h_ov.data_ptr(), h_ot.data_ptr())
+        assert rc == 0, rc
+
+    def timed(device):
+        for _ in range(max(args.warmup, 3)):
+            call(device)
+        ts = []
+        for _ in range(args.steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            call(device)  # returns once the meshes (and their counts) are out
+            ts.append(time.perf_counter() - t0)
+        return 1e3 * sum(ts) / len(ts)
+
+    with ClockSampler(local) as clocks:
+        ms = timed(True)
+        ms_e2e = timed(False)
+    tris_out = sum(res[i].num_triangles for i in range(m))
+    verts_out = sum(res[i].num_vertices for i in range(m))
+    tris_in, verts_in = int(ranges[:, 3].sum()), int(ranges[:, 1].sum())
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    algo = 48 * verts_in + 12 * tris_in + 48 * verts_out + 12 * tris_out
+    ach = algo / (ms / 1e3) / 1e9
+    line = {
+        "metric": COLLAPSE_METRIC, "impl": "lvn-collapse", "value": round(m / (ms / 1e3), 1), "unit": "meshes/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"collapse-{wl.name}", "meshes": m, "triangles_in": tris_in, "triangles_out": tris_out,
+                   "vertices_in": verts_in, "vertices_out": verts_out, "l2": "flushed between steps (256 MiB write)",
+                   "options": "ConstructClipmapNodeData: max error 5, edge 2.5 (x leaf size), cos 0.7",
+                   "timing": "host clock around the synchronous C-ABI call"},
+        "e2e": {"value": round(m / (ms_e2e / 1e3), 1), "unit": "meshes/s",
+                "h2d_bytes_per_step": 48 * verts_in + 12 * tris_in,
+                "d2h_bytes_per_step": 48 * verts_out + 12 * tris_out, "ms_per_step": round(ms_e2e, 4)},
+        "gpu_launches": 1,
+        "roofline": {"bound": "hbm", "achieved": round(ach, 1), "peak": hbm_peak, "unit": "GB/s",
+                     "frac": round(ach / hbm_peak, 4), "traffic": None, "kernel": "k_mesh_collapse",
+                     "ms_per_launch": round(ms, 4), "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                     "algorithmic_bytes_per_launch": algo},
+        "clocks": clocks.summary(),
+    }
+    if not args.no_cpu_baseline:
+        threads = host_threads()
+        one = collapse_cpu(v, t, ranges, offsets, sizes, threads)
+        done, total = 0, 0.0
+        while total < 3.0:
+            total += one()
+            done += m
+        line["cpu_baseline"] = {"value": round(done / total, 1), "unit": "meshes/s", "cores": threads, "kind": "port",
+                                "sample": f"{done // m} passes over the {m} meshes, {total:.1f} s"}
+    print(json.dumps(line), flush=True)
+
+
 if __name__ == "__main__":
     a = parse()
     WORKLOAD = a.workload
@@ -998,5 +1175,7 @@ if __name__ == "__main__":
         run_select(a)
     elif a.workload == "seams":
         run_seams(a)
+    elif a.workload == "collapse":
+        run_collapse(a)
     else:
         run_lvn(a)
