@@ -9,8 +9,10 @@
 // collapse error (1 / QEF error of its two end points, qef_simd.h) is small
 // enough claims both end points, and an edge that holds both claims collapses.
 // Here each phase is a parallel pass over the CTA:
-//   * the candidate edges are sorted in shared memory (global memory beyond
-//     224 KB) and reduced to the interior edges by run-length tests;
+//   * the candidate edges are put in the reference's sort order (the union's
+//     idx_ = min | max << 32) by a counting sort on max and an insertion sort
+//     of each vertex's few entries by min, then reduced to the interior edges
+//     by run-length tests;
 //   * the draws are the reference's std::mt19937(42) stream (reseeded each
 //     iteration) passed through libstdc++'s uniform_int_distribution (Lemire's
 //     method: a raw value is rejected when the low half of raw * range falls
@@ -37,8 +39,8 @@
 namespace lvn {
 namespace {
 
-constexpr int kThreads = 1024;
-constexpr int kSortCap = 28672;  // u64 entries sorted in shared memory (224 KB)
+constexpr int kThreads = 512;    // two CTAs (meshes) per SM
+constexpr int kSortCap = 12288;  // u64 draws sorted in shared memory (96 KB); more sort in global memory
 constexpr size_t kSmem = (size_t)kSortCap * 8;
 constexpr int kMaxDegree = 16;  // COLLAPSE_MAX_DEGREE (ng_mesh_simplify.cpp:17)
 
@@ -216,10 +218,26 @@ __device__ void block_sort(uint64_t* key, int n) {
     }
 }
 
+// Exclusive scan of the per-warp counts in s_warp (warp 0, by shuffles); the
+// total to *s_total.  Call between barriers.
+__device__ __forceinline__ void scan_warp_counts(int* s_warp, int* s_total) {
+    const int lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    if (threadIdx.x < 32) {
+        const int c = lane < nwarps ? s_warp[lane] : 0;
+        int inc = c;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        if (lane < nwarps) s_warp[lane] = inc - c;
+        if (lane == 31) *s_total = inc;
+    }
+}
+
 // Order-preserving compaction of [0, n): keep(i) -> emit(i, rank); returns the count.
 template <class Keep, class Emit>
 __device__ int block_compact(int n, Keep keep, Emit emit, int* s_warp, int* s_total) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     int base = 0;
     for (int start = 0; start < n; start += blockDim.x) {
         const int i = start + threadIdx.x;
@@ -227,15 +245,7 @@ __device__ int block_compact(int n, Keep keep, Emit emit, int* s_warp, int* s_to
         const unsigned ballot = __ballot_sync(0xffffffffu, k);
         if (lane == 0) s_warp[warp] = __popc(ballot);
         __syncthreads();
-        if (threadIdx.x == 0) {
-            int run = 0;
-            for (int w = 0; w < nwarps; w++) {
-                const int c = s_warp[w];
-                s_warp[w] = run;
-                run += c;
-            }
-            *s_total = run;
-        }
+        scan_warp_counts(s_warp, s_total);
         __syncthreads();
         if (k) emit(i, base + s_warp[warp] + __popc(ballot & ((1u << lane) - 1)));
         base += *s_total;
@@ -251,7 +261,7 @@ __device__ __forceinline__ uint32_t orderable(float e) {
 
 // ---- the simplifier ---------------------------------------------------------
 
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kThreads, 2)
     k_mesh_collapse(const MeshJob* __restrict__ jobs, const lvn_mesh_vertex* in_v, const lvn_mesh_triangle* in_t,
                     lvn_mesh_vertex* out_v, lvn_mesh_triangle* out_t, int32_t* counts, Scratch S,
                     const uint32_t* __restrict__ raw, int raw_len) {
@@ -294,9 +304,13 @@ __global__ void __launch_bounds__(kThreads, 1)
         flag[i] = 0;
     }
     __syncthreads();
-    // BuildCandidateEdges (ng_mesh_simplify.cpp:122-177)
+    // BuildCandidateEdges (ng_mesh_simplify.cpp:122-177).  The edges are sorted
+    // by the union's idx_ = min | max << 32: a counting sort on max (bucket
+    // sizes from target[], then a scan), then each bucket's few entries by min.
     const int ne0 = 3 * J.nt;
-    uint64_t* ekeys = ne0 <= kSortCap ? smem : edg[1];
+    uint64_t* ekeys = edg[1];
+    for (int i = tid; i < nv; i += nth) target[i] = 0;
+    __syncthreads();
     for (int t = tid; t < J.nt; t += nth) {
         const lvn_mesh_triangle tr = in_t[J.t_off + t];
         const int a = tr.indices[0], b = tr.indices[1], c = tr.indices[2];
@@ -304,12 +318,56 @@ __global__ void __launch_bounds__(kThreads, 1)
         atomicAdd(&degree[a], 1);
         atomicAdd(&degree[b], 1);
         atomicAdd(&degree[c], 1);
-        const uint32_t e0[3] = {(uint32_t)min(a, b), (uint32_t)min(b, c), (uint32_t)min(a, c)};
-        const uint32_t e1[3] = {(uint32_t)max(a, b), (uint32_t)max(b, c), (uint32_t)max(a, c)};
-        for (int k = 0; k < 3; k++) ekeys[3 * t + k] = (uint64_t)e0[k] | ((uint64_t)e1[k] << 32);
+        atomicAdd(&target[max(a, b)], 1);
+        atomicAdd(&target[max(b, c)], 1);
+        atomicAdd(&target[max(a, c)], 1);
     }
     __syncthreads();
-    block_sort(ekeys, ne0);
+    {  // exclusive scan of the bucket sizes: bucket starts to claim[], cursors to target[]
+        int base = 0;
+        for (int start = 0; start < nv; start += nth) {
+            const int i = start + tid;
+            const int c = i < nv ? target[i] : 0;
+            int inc = c;
+            const int lane = tid & 31, warp = tid >> 5;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += t;
+            }
+            if (lane == 31) s_warp[warp] = inc;
+            __syncthreads();
+            scan_warp_counts(s_warp, &s_total);
+            __syncthreads();
+            if (i < nv) {
+                claim[i] = (uint64_t)(base + s_warp[warp] + inc - c);  // bucket start
+                target[i] = base + s_warp[warp] + inc - c;              // cursor
+            }
+            base += s_total;
+            __syncthreads();
+        }
+    }
+    for (int t = tid; t < J.nt; t += nth) {
+        const int3 x = tri[0][t];
+        const int pa[3][2] = {{x.x, x.y}, {x.y, x.z}, {x.x, x.z}};
+        for (int k = 0; k < 3; k++) {
+            const uint32_t lo = (uint32_t)min(pa[k][0], pa[k][1]), hi = (uint32_t)max(pa[k][0], pa[k][1]);
+            ekeys[atomicAdd(&target[hi], 1)] = (uint64_t)lo | ((uint64_t)hi << 32);
+        }
+    }
+    __syncthreads();
+    for (int v = tid; v < nv; v += nth) {  // insertion sort of bucket v by min
+        const int b0 = (int)claim[v], b1 = target[v];
+        for (int i = b0 + 1; i < b1; i++) {
+            const uint64_t k = ekeys[i];
+            int j = i - 1;
+            while (j >= b0 && ekeys[j] > k) {
+                ekeys[j + 1] = ekeys[j];
+                j--;
+            }
+            ekeys[j + 1] = k;
+        }
+    }
+    __syncthreads();
     const uint64_t last = ekeys[ne0 - 1];  // the final run is never examined (ng_mesh_simplify.cpp:143-164)
     for (int i = tid; i < ne0; i += nth) {
         const uint64_t k = ekeys[i];
@@ -362,15 +420,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             const unsigned ballot = __ballot_sync(0xffffffffu, acc);
             if (lane == 0) s_warp[warp] = __popc(ballot);
             __syncthreads();
-            if (tid == 0) {
-                int run = 0;
-                for (int w = 0; w < (nth >> 5); w++) {
-                    const int c = s_warp[w];
-                    s_warp[w] = run;
-                    run += c;
-                }
-                s_total = run;
-            }
+            scan_warp_counts(s_warp, &s_total);
             __syncthreads();
             const int r = got + s_warp[warp] + __popc(ballot & ((1u << lane) - 1));
             if (acc && r < num_random) draws[r] = prod >> 32;
