@@ -58,10 +58,11 @@ struct MeshJob {
 
 struct Scratch {
     MV* verts;            // working vertices
-    int3* tris[2];        // ping-pong triangles
-    uint64_t* edges[2];   // ping-pong edges (min | max << 32)
-    float4* cpos;         // collapse position per edge
-    float4* cnrm;         // collapse normal per edge
+    int3* tris;           // triangles (compacted in place)
+    uint64_t* edges;      // edges, min | max << 32 (compacted in place)
+    uint8_t* eflag;       // candidate edge kept (setup)
+    float4* cpos;         // collapse position per draw
+    float4* cnrm;         // collapse normal per draw
     int32_t* degree;      // triangles per vertex
     uint64_t* claim;      // (orderable error << 32 | edge) per vertex
     int32_t* target;      // collapse target per vertex
@@ -88,7 +89,7 @@ __device__ __forceinline__ void mul_m4(const float a[4], const float B[4][4], fl
     }
 }
 
-__device__ float qef2(const MV& v0, const MV& v1, float out[4]) {
+__device__ __noinline__ float qef2(const MV& v0, const MV& v1, float out[4]) {
     float ATA[4][4], ATb[4], acc[4];
     for (int r = 0; r < 4; r++) {
         ATb[r] = 0.f;
@@ -259,6 +260,39 @@ __device__ __forceinline__ uint32_t orderable(float e) {
     return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
 }
 
+// Order-preserving compaction with four consecutive items per thread and the
+// kept value computed once: test(i, &v) -> keep, emit(rank, v).  Returns the count.
+template <class T, class Test, class Emit>
+__device__ int block_compact4(int n, Test test, Emit emit, int* s_warp, int* s_total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int base = 0;
+    for (int start = 0; start < n; start += 4 * blockDim.x) {
+        const int i0 = start + 4 * threadIdx.x;
+        T v[4];
+        bool k[4];
+        int c = 0;
+        for (int q = 0; q < 4; q++) {
+            k[q] = i0 + q < n && test(i0 + q, &v[q]);
+            c += k[q];
+        }
+        int inc = c;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        if (lane == 31) s_warp[warp] = inc;
+        __syncthreads();
+        scan_warp_counts(s_warp, s_total);
+        __syncthreads();
+        int r = base + s_warp[warp] + inc - c;
+        for (int q = 0; q < 4; q++)
+            if (k[q]) emit(r++, v[q]);
+        base += *s_total;
+        __syncthreads();
+    }
+    return base;
+}
+
 // ---- the simplifier ---------------------------------------------------------
 
 __global__ void __launch_bounds__(kThreads, 2)
@@ -280,10 +314,11 @@ __global__ void __launch_bounds__(kThreads, 2)
         return;
     }
     MV* vs = S.verts + J.s_v;
-    int3* tri[2] = {S.tris[0] + J.s_t, S.tris[1] + J.s_t};
-    uint64_t* edg[2] = {S.edges[0] + J.s_e, S.edges[1] + J.s_e};
-    float4* cpos = S.cpos + J.s_e;
-    float4* cnrm = S.cnrm + J.s_e;
+    int3* T = S.tris + J.s_t;
+    uint64_t* E = S.edges + J.s_e;
+    uint8_t* eflag = S.eflag + J.s_e;
+    float4* cpos = S.cpos + J.s_r;
+    float4* cnrm = S.cnrm + J.s_r;
     int32_t* degree = S.degree + J.s_v;
     uint64_t* claim = S.claim + J.s_v;
     int32_t* target = S.target + J.s_v;
@@ -308,13 +343,13 @@ __global__ void __launch_bounds__(kThreads, 2)
     // by the union's idx_ = min | max << 32: a counting sort on max (bucket
     // sizes from target[], then a scan), then each bucket's few entries by min.
     const int ne0 = 3 * J.nt;
-    uint64_t* ekeys = edg[1];
+    uint64_t* ekeys = E;
     for (int i = tid; i < nv; i += nth) target[i] = 0;
     __syncthreads();
     for (int t = tid; t < J.nt; t += nth) {
         const lvn_mesh_triangle tr = in_t[J.t_off + t];
         const int a = tr.indices[0], b = tr.indices[1], c = tr.indices[2];
-        tri[0][t] = make_int3(a, b, c);
+        T[t] = make_int3(a, b, c);
         atomicAdd(&degree[a], 1);
         atomicAdd(&degree[b], 1);
         atomicAdd(&degree[c], 1);
@@ -347,7 +382,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         }
     }
     for (int t = tid; t < J.nt; t += nth) {
-        const int3 x = tri[0][t];
+        const int3 x = T[t];
         const int pa[3][2] = {{x.x, x.y}, {x.y, x.z}, {x.x, x.z}};
         for (int k = 0; k < 3; k++) {
             const uint32_t lo = (uint32_t)min(pa[k][0], pa[k][1]), hi = (uint32_t)max(pa[k][0], pa[k][1]);
@@ -378,21 +413,23 @@ __global__ void __launch_bounds__(kThreads, 2)
         }
     }
     __syncthreads();
-    int ne = block_compact(
-        ne0,
-        [&](int i) {
-            const uint64_t k = ekeys[i];
-            return k != last && (i == 0 || ekeys[i - 1] != k) && ekeys[i + 1] == k && !flag[(uint32_t)k] &&
+    for (int i = tid; i < ne0; i += nth) {  // an interior run's first entry, away from the boundary
+        const uint64_t k = ekeys[i];
+        eflag[i] = k != last && (i == 0 || ekeys[i - 1] != k) && ekeys[i + 1] == k && !flag[(uint32_t)k] &&
                    !flag[(uint32_t)(k >> 32)];
+    }
+    __syncthreads();
+    int ne = block_compact4<uint64_t>(
+        ne0,
+        [&](int i, uint64_t* out) {
+            *out = ekeys[i];
+            return eflag[i] != 0;
         },
-        [&](int i, int r) { edg[0][r] = ekeys[i]; }, s_warp, &s_total);
-    int cur = 0;
+        [&](int r, uint64_t e) { E[r] = e; }, s_warp, &s_total);
     int nt = J.nt;
     const int target_tris = (int)((float)J.nt * o.target_percentage);
     int iterations = 0;
     while (nt > target_tris && iterations++ < o.max_iterations) {
-        uint64_t* E = edg[cur];
-        int3* T = tri[cur];
         for (int i = tid; i < nv; i += nth) {
             claim[i] = ~0ull;
             target[i] = -1;
@@ -456,9 +493,9 @@ __global__ void __launch_bounds__(kThreads, 2)
             if (error > o.max_error) continue;
             valid[j] = 1;
             my_valid++;
-            cnrm[i] = make_float4((a.n[0] - b.n[0]) * 0.5f, (a.n[1] - b.n[1]) * 0.5f, (a.n[2] - b.n[2]) * 0.5f,
+            cnrm[j] = make_float4((a.n[0] - b.n[0]) * 0.5f, (a.n[1] - b.n[1]) * 0.5f, (a.n[2] - b.n[2]) * 0.5f,
                                   (a.n[3] - b.n[3]) * 0.5f);
-            cpos[i] = make_float4(pos[0], pos[1], pos[2], 1.f);
+            cpos[j] = make_float4(pos[0], pos[1], pos[2], 1.f);
             if (error < FLT_MAX) {
                 const uint64_t key = ((uint64_t)orderable(error) << 32) | (uint32_t)i;
                 atomicMin((unsigned long long*)&claim[emn], (unsigned long long)key);
@@ -478,7 +515,7 @@ __global__ void __launch_bounds__(kThreads, 2)
             if ((uint32_t)claim[emn] == (uint32_t)i && (uint32_t)claim[emx] == (uint32_t)i &&
                 claim[emn] != ~0ull && claim[emx] != ~0ull) {
                 target[emx] = (int)emn;
-                const float4 cp = cpos[i], cn = cnrm[i];
+                const float4 cp = cpos[j], cn = cnrm[j];
                 vs[emn].p[0] = cp.x;
                 vs[emn].p[1] = cp.y;
                 vs[emn].p[2] = cp.z;
@@ -492,47 +529,44 @@ __global__ void __launch_bounds__(kThreads, 2)
         for (int i = tid; i < nv; i += nth) degree[i] = 0;
         __syncthreads();
         // RemoveTriangles (ng_mesh_simplify.cpp:310-352)
-        int3* T2 = tri[cur ^ 1];
-        nt = block_compact(
+        nt = block_compact4<int3>(
             nt,
-            [&](int t) {
+            [&](int t, int3* out) {
                 int3 x = T[t];
-                if (target[x.x] != -1) x.x = target[x.x];
-                if (target[x.y] != -1) x.y = target[x.y];
-                if (target[x.z] != -1) x.z = target[x.z];
+                int m = target[x.x];
+                if (m != -1) x.x = m;
+                m = target[x.y];
+                if (m != -1) x.y = m;
+                m = target[x.z];
+                if (m != -1) x.z = m;
+                *out = x;
                 return !(x.x == x.y || x.x == x.z || x.y == x.z);
             },
-            [&](int t, int r) {
-                int3 x = T[t];
-                if (target[x.x] != -1) x.x = target[x.x];
-                if (target[x.y] != -1) x.y = target[x.y];
-                if (target[x.z] != -1) x.z = target[x.z];
-                T2[r] = x;
+            [&](int r, const int3& x) {
+                T[r] = x;  // in place: r <= t, and a chunk's reads precede its writes
                 atomicAdd(&degree[x.x], 1);
                 atomicAdd(&degree[x.y], 1);
                 atomicAdd(&degree[x.z], 1);
             },
             s_warp, &s_total);
         // RemoveEdges (ng_mesh_simplify.cpp:356-380)
-        uint64_t* E2 = edg[cur ^ 1];
         auto remap = [&](uint64_t e) {
             uint32_t emn = (uint32_t)e, emx = (uint32_t)(e >> 32);
             if (target[emn] != -1) emn = (uint32_t)target[emn];
             if (target[emx] != -1) emx = (uint32_t)target[emx];
             return (uint64_t)emn | ((uint64_t)emx << 32);
         };
-        ne = block_compact(
+        ne = block_compact4<uint64_t>(
             ne,
-            [&](int i) {
+            [&](int i, uint64_t* out) {
                 const uint64_t e = remap(E[i]);
+                *out = e;
                 return (uint32_t)e != (uint32_t)(e >> 32);
             },
-            [&](int i, int r) { E2[r] = remap(E[i]); }, s_warp, &s_total);
-        cur ^= 1;
+            [&](int r, uint64_t e) { E[r] = e; }, s_warp, &s_total);
         __syncthreads();
     }
     // CompactVertices (ng_mesh_simplify.cpp:384-421) and the offset added back
-    int3* T = tri[cur];
     for (int i = tid; i < nv; i += nth) flag[i] = 0;
     __syncthreads();
     for (int t = tid; t < nt; t += nth) {
@@ -597,8 +631,9 @@ struct CollapseWork {
     cudaStream_t stream = nullptr;
     Grow<MeshJob> jobs;
     Grow<MV> verts;
-    Grow<int3> tris0, tris1;
-    Grow<uint64_t> edges0, edges1, claim, draws;
+    Grow<int3> tris;
+    Grow<uint64_t> edges, claim, draws;
+    Grow<uint8_t> eflag;
     Grow<float4> cpos, cnrm;
     Grow<int32_t> degree, target, flag, counts;
     Grow<uint8_t> valid;
@@ -709,12 +744,11 @@ int lvn_mesh_simplify(const lvn_mesh_vertex* vertices, const lvn_mesh_triangle* 
     CL_TRY(w.claim.fit(std::max<int64_t>(sv, 1)));
     CL_TRY(w.target.fit(std::max<int64_t>(sv, 1)));
     CL_TRY(w.flag.fit(std::max<int64_t>(sv, 1)));
-    CL_TRY(w.tris0.fit(std::max<int64_t>(st, 1)));
-    CL_TRY(w.tris1.fit(std::max<int64_t>(st, 1)));
-    CL_TRY(w.edges0.fit(std::max<int64_t>(se, 1)));
-    CL_TRY(w.edges1.fit(std::max<int64_t>(se, 1)));
-    CL_TRY(w.cpos.fit(std::max<int64_t>(se, 1)));
-    CL_TRY(w.cnrm.fit(std::max<int64_t>(se, 1)));
+    CL_TRY(w.tris.fit(std::max<int64_t>(st, 1)));
+    CL_TRY(w.edges.fit(std::max<int64_t>(se, 1)));
+    CL_TRY(w.eflag.fit(std::max<int64_t>(se, 1)));
+    CL_TRY(w.cpos.fit(std::max<int64_t>(sr, 1)));
+    CL_TRY(w.cnrm.fit(std::max<int64_t>(sr, 1)));
     CL_TRY(w.draws.fit(std::max<int64_t>(sr, 1)));
     CL_TRY(w.valid.fit(std::max<int64_t>(sr, 1)));
     CL_TRY(w.counts.fit(2 * (size_t)num_meshes));
@@ -737,10 +771,9 @@ int lvn_mesh_simplify(const lvn_mesh_vertex* vertices, const lvn_mesh_triangle* 
     }
     Scratch S;
     S.verts = w.verts.p;
-    S.tris[0] = w.tris0.p;
-    S.tris[1] = w.tris1.p;
-    S.edges[0] = w.edges0.p;
-    S.edges[1] = w.edges1.p;
+    S.tris = w.tris.p;
+    S.edges = w.edges.p;
+    S.eflag = w.eflag.p;
     S.cpos = w.cpos.p;
     S.cnrm = w.cnrm.p;
     S.degree = w.degree.p;
