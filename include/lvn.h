@@ -415,6 +415,43 @@ int lvn_mesh_simplify(const lvn_mesh_vertex* vertices, const lvn_mesh_triangle* 
                       const lvn_simplify_options* options, lvn_mesh_vertex* out_vertices,
                       lvn_mesh_triangle* out_triangles);
 
+/* ---- device-resident render meshes (headless GL upload) --------------------
+ * The engine uploads a MeshBuffer into GL buffers from a fixed pool of render
+ * meshes (Render_AllocRenderMesh / RenderMesh::uploadData,
+ * render_mesh.cpp:9-30, 94-138).  GL is not part of this library: a pool here
+ * is one vertex arena and one triangle arena in device memory, allocated at
+ * creation, that meshes take ranges of (first fit, freed ranges coalesce).
+ * A renderer reads a mesh through its handle. */
+typedef struct lvn_render_pool lvn_render_pool;
+typedef struct lvn_render_mesh_view {
+    const lvn_mesh_vertex*   vertices;   /* device */
+    int32_t                  num_vertices;
+    const lvn_mesh_triangle* triangles;  /* device, mesh-local indices */
+    int32_t                  num_triangles;
+    float                    position[3];
+} lvn_render_mesh_view;
+/* NULL on failure (bad sizes, out of device memory) */
+lvn_render_pool* lvn_render_pool_create(int64_t vertex_capacity, int64_t triangle_capacity, int32_t max_meshes);
+void lvn_render_pool_destroy(lvn_render_pool* pool);
+/* Render_AllocRenderMesh(tag, buffer, position): a mesh without triangles
+ * gets no render mesh (*handle = -1, LVN_OK); LVN_ERR_CAPACITY when the
+ * arenas or handles are exhausted. */
+int lvn_render_mesh_upload(lvn_render_pool* pool, const lvn_mesh_vertex* vertices, int32_t num_vertices,
+                           const lvn_mesh_triangle* triangles, int32_t num_triangles, int32_t memory,
+                           const float position[3], int32_t* handle);
+/* every chunk of a batch left in device memory (batch->memory =
+ * LVN_MEMORY_DEVICE) in one gather launch: handles[c] (-1 for chunks
+ * without triangles); positions[3c..] as the engine passes them (may be
+ * NULL).  All or nothing: on LVN_ERR_CAPACITY no mesh is taken. */
+int lvn_render_meshes_from_batch(lvn_render_pool* pool, const lvn_batch_out* batch, int32_t num_chunks,
+                                 const float* positions, int32_t* handles);
+int lvn_render_mesh_get(lvn_render_pool* pool, int32_t handle, lvn_render_mesh_view* out);
+/* a mesh's data to host arrays of at least its counts (tests, file dumps) */
+int lvn_render_mesh_download(lvn_render_pool* pool, int32_t handle, lvn_mesh_vertex* vertices,
+                             lvn_mesh_triangle* triangles);
+int lvn_render_mesh_free(lvn_render_pool* pool, int32_t handle);
+int lvn_render_pool_usage(lvn_render_pool* pool, int64_t* vertices_used, int64_t* triangles_used, int32_t* meshes);
+
 #ifdef __cplusplus
 }
 #endif

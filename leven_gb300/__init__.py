@@ -75,6 +75,11 @@ class SimplifyOptions(C.Structure):
                 ("max_error", C.c_float), ("max_edge_size", C.c_float), ("min_angle_cosine", C.c_float)]
 
 
+class RenderMeshView(C.Structure):
+    _fields_ = [("vertices", C.c_void_p), ("num_vertices", C.c_int32), ("triangles", C.c_void_p),
+                ("num_triangles", C.c_int32), ("position", C.c_float * 3)]
+
+
 class BatchOut(C.Structure):
     _fields_ = [("memory", C.c_int32), ("vertices", C.c_void_p), ("vertex_capacity", C.c_int64),
                 ("total_vertices", C.c_int64), ("triangles", C.c_void_p), ("triangle_capacity", C.c_int64),
@@ -96,7 +101,10 @@ EXPORTS = [
     "lvn_surrogate_eval", "lvn_surrogate_eval_lattices", "lvn_surrogate_domain", "lvn_surrogate_get_stream",
     "lvn_meshgen_set_surrogate", "lvn_meshgen_surrogate_chunks", "lvn_density_f64",
     "lvn_clipmap_select", "lvn_clipmap_select_device", "lvn_clipmap_touched", "lvn_seam_generate",
-    "lvn_simplify_options_default", "lvn_mesh_simplify",
+    "lvn_simplify_options_default", "lvn_mesh_simplify", "lvn_render_pool_create", "lvn_render_pool_destroy",
+    "lvn_render_mesh_upload", "lvn_render_meshes_from_batch", "lvn_render_mesh_get", "lvn_render_mesh_download",
+    "lvn_render_mesh_free",
+    "lvn_render_pool_usage",
 ]
 
 _lib = None
@@ -163,6 +171,17 @@ def lib():
     L.lvn_simplify_options_default.restype = None
     L.lvn_mesh_simplify.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(ChunkResult), C.c_int32, C.c_void_p,
                                     C.POINTER(SimplifyOptions), C.c_void_p, C.c_void_p]
+    L.lvn_render_pool_create.argtypes = [C.c_int64, C.c_int64, C.c_int32]
+    L.lvn_render_pool_create.restype = C.c_void_p
+    L.lvn_render_pool_destroy.argtypes = [C.c_void_p]
+    L.lvn_render_pool_destroy.restype = None
+    L.lvn_render_mesh_upload.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32,
+                                         C.c_void_p, i32p]
+    L.lvn_render_meshes_from_batch.argtypes = [C.c_void_p, C.POINTER(BatchOut), C.c_int32, C.c_void_p, C.c_void_p]
+    L.lvn_render_mesh_get.argtypes = [C.c_void_p, C.c_int32, C.POINTER(RenderMeshView)]
+    L.lvn_render_mesh_download.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]
+    L.lvn_render_mesh_free.argtypes = [C.c_void_p, C.c_int32]
+    L.lvn_render_pool_usage.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), i32p]
     L.lvn_seam_generate.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32, i32p,
                                     C.c_int32, C.c_void_p, C.c_int32, C.c_float * 3, C.POINTER(BatchOut)]
     L.lvn_surrogate_get_stream.restype = C.c_void_p
@@ -337,6 +356,61 @@ def mesh_simplify(vertices, triangles, ranges, offsets, options):
                "lvn_mesh_simplify")
     out = np.ctypeslib.as_array(C.cast(res, C.POINTER(C.c_int32)), shape=(max(1, m), 8))[:m, :4].copy()
     return ov, ot, out
+
+
+class RenderPool:
+    """Device-resident render meshes (the headless stand-in for the engine's
+    GL upload, render_mesh.cpp:94-138): one vertex and one triangle arena."""
+
+    def __init__(self, vertex_capacity, triangle_capacity, max_meshes=8192):
+        self._h = lib().lvn_render_pool_create(int(vertex_capacity), int(triangle_capacity), int(max_meshes))
+        if not self._h:
+            raise LvnError(LVN_ERR_OUT_OF_MEMORY, "lvn_render_pool_create")
+
+    def close(self):
+        if self._h:
+            lib().lvn_render_pool_destroy(self._h)
+            self._h = None
+
+    def upload(self, vertices, triangles, position=(0.0, 0.0, 0.0)):
+        """Host arrays (V, 12) f32 / (T, 3) i32 -> handle (-1: no triangles)."""
+        v = np.ascontiguousarray(vertices, np.float32)
+        t = np.ascontiguousarray(triangles, np.int32)
+        h = C.c_int32(-1)
+        pos = np.asarray(position, np.float32)
+        _check(lib().lvn_render_mesh_upload(self._h, v.ctypes.data, len(v), t.ctypes.data, len(t), LVN_MEMORY_HOST,
+                                            pos.ctypes.data, C.byref(h)), "lvn_render_mesh_upload")
+        return h.value
+
+    def from_batch(self, batch_out, n, positions=None):
+        handles = np.full(max(1, n), -1, np.int32)
+        pos = None if positions is None else np.ascontiguousarray(positions, np.float32)
+        _check(lib().lvn_render_meshes_from_batch(self._h, C.byref(batch_out), n,
+                                                  None if pos is None else pos.ctypes.data, handles.ctypes.data),
+               "lvn_render_meshes_from_batch")
+        return handles[:n]
+
+    def view(self, handle):
+        v = RenderMeshView()
+        _check(lib().lvn_render_mesh_get(self._h, int(handle), C.byref(v)), "lvn_render_mesh_get")
+        return v
+
+    def download(self, handle):
+        """The mesh's (vertices (V, 12), triangles (T, 3)) as host arrays."""
+        v = self.view(handle)
+        vs = np.zeros((max(1, v.num_vertices), 12), np.float32)
+        ts = np.zeros((max(1, v.num_triangles), 3), np.int32)
+        _check(lib().lvn_render_mesh_download(self._h, int(handle), vs.ctypes.data, ts.ctypes.data),
+               "lvn_render_mesh_download")
+        return vs[:v.num_vertices], ts[:v.num_triangles]
+
+    def free(self, handle):
+        return _check(lib().lvn_render_mesh_free(self._h, int(handle)), "lvn_render_mesh_free")
+
+    def usage(self):
+        a, b, c = C.c_int64(), C.c_int64(), C.c_int32()
+        _check(lib().lvn_render_pool_usage(self._h, C.byref(a), C.byref(b), C.byref(c)), "lvn_render_pool_usage")
+        return a.value, b.value, c.value
 
 
 def clipmap_touched(ops, root_min, root_size):

@@ -12,7 +12,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "liblvn.so"
 SOURCES = ["lvn_kernels.cu", "lvn_api.cu", "lvn_noalloc.cu", "lvn_surrogate.cu", "lvn_clipmap.cu",
-           "lvn_seam.cu", "lvn_collapse.cu"]
+           "lvn_seam.cu", "lvn_collapse.cu", "lvn_render.cu"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 # -fmad=false: no implicit multiply-add contraction, so that density signs are
 # the exact IEEE sequence the kernels spell out (explicit fmaf where fused).
