@@ -103,4 +103,37 @@ private:
     lvn_meshgen* ctx_;
 };
 
+// ngMeshSimplifier (ng_mesh_simplify.cpp:441-540) for one mesh buffer in host
+// memory, in place; `options` as MeshSimplificationOptions.  Batches of meshes
+// go to lvn_mesh_simplify directly.
+inline void ngMeshSimplifier(LvnMeshBuffer* mesh, const std::array<float, 4>& worldSpaceOffset,
+                             const lvn_simplify_options& options) {
+    if (!mesh || mesh->numTriangles == 0) return;
+    lvn_chunk_result r = {0, mesh->numVertices, 0, mesh->numTriangles, 0, 0, 0, 0};
+    if (lvn_mesh_simplify(mesh->vertices.data(), mesh->triangles.data(), LVN_MEMORY_HOST, &r, 1,
+                          worldSpaceOffset.data(), &options, mesh->vertices.data(), mesh->triangles.data()) != LVN_OK)
+        return;
+    mesh->numVertices = r.num_vertices;
+    mesh->numTriangles = r.num_triangles;
+    mesh->vertices.resize(r.num_vertices);
+    mesh->triangles.resize(r.num_triangles);
+}
+
+// SelectActiveClipmapNodes (clipmap.cpp:1084-1128) for one camera over the
+// complete clipmap octree (rootMin, rootSize): the nodes' (min, size).
+inline int SelectActiveClipmapNodes(const std::array<float, 3>& cameraPosition, const std::array<int, 3>& rootMin,
+                                    int rootSize, std::vector<lvn_chunk_desc>& selectedNodes) {
+    int32_t count = 0;
+    selectedNodes.resize(1024);
+    int rc = lvn_clipmap_select(cameraPosition.data(), 1, rootMin.data(), rootSize, selectedNodes.data(),
+                                (int32_t)selectedNodes.size(), &count);
+    if (rc == LVN_ERR_CAPACITY) {
+        selectedNodes.resize(count);
+        rc = lvn_clipmap_select(cameraPosition.data(), 1, rootMin.data(), rootSize, selectedNodes.data(), count,
+                                &count);
+    }
+    selectedNodes.resize(rc == LVN_OK ? count : 0);
+    return rc;
+}
+
 #endif  // LVN_COMPUTE_HPP

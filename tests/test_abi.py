@@ -79,3 +79,60 @@ def test_workload_generator():
         assert 0 <= o.origin[0] < 512 and -64 <= o.origin[1] < 64 and 0 <= o.origin[2] < 512
         assert all(2 <= d <= 12 for d in o.dimensions)
     assert W.op_bounds(W.Op(1, 1, 201, (10.5, 20.5, -3.5), (3.0, 3.0, 3.0))) == ([26, 66, -30], [54, 94, -2])
+
+
+def test_headers_compile_and_link(tmp_path):
+    """include/lvn.h as C and include/lvn_compute.hpp as C++ compile against
+    liblvn.so; calls that need no device run."""
+    import pathlib
+    import shutil
+    import subprocess
+
+    import leven_gb300 as lvn
+
+    root = pathlib.Path(__file__).resolve().parents[1]
+    lib = lvn.LIB_PATH
+    lvn.lib()
+    if not shutil.which("gcc") or not shutil.which("g++"):
+        pytest.skip("no host compiler")
+    c_src = tmp_path / "abi.c"
+    c_src.write_text(r'''
+#include "lvn.h"
+#include <stdio.h>
+#include <string.h>
+int main(void) {
+    lvn_simplify_options o;
+    lvn_simplify_options_default(&o);
+    if (o.max_iterations != 10 || o.edge_fraction != 0.125f) return 1;
+    if (strcmp(lvn_error_string(LVN_ERR_DEVICE_STATUS), "LVN_ERR_DEVICE_STATUS")) return 2;
+    if (sizeof(lvn_mesh_vertex) != 48 || sizeof(lvn_seam_node) != 48 || sizeof(lvn_csg_op) != 48 ||
+        sizeof(lvn_mesh_triangle) != 12 || sizeof(lvn_chunk_desc) != 16 || sizeof(lvn_chunk_result) != 32)
+        return 3;
+    int32_t n = 0;
+    if (lvn_clipmap_select(0, -1, 0, 0, 0, 0, &n) != LVN_ERR_INVALID) return 4;
+    if (lvn_render_pool_create(0, 0, 0) != 0) return 5;
+    puts("c ok");
+    return 0;
+}
+''')
+    cpp_src = tmp_path / "facade.cpp"
+    cpp_src.write_text(r'''
+#include "lvn_compute.hpp"
+#include <cstdio>
+int main() {
+    lvn_simplify_options o;
+    lvn_simplify_options_default(&o);
+    LvnMeshBuffer mesh;
+    ngMeshSimplifier(&mesh, {0.f, 0.f, 0.f, 0.f}, o);  // no triangles: nothing to do
+    std::vector<lvn_chunk_desc> nodes;
+    if (SelectActiveClipmapNodes({0.f, 0.f, 0.f}, {0, 0, 0}, 100, nodes) != LVN_ERR_INVALID) return 1;
+    std::puts(GetCLErrorString(LVN_ERR_CAPACITY));
+    return 0;
+}
+''')
+    for cc, src, std in (("gcc", c_src, "-std=c11"), ("g++", cpp_src, "-std=c++17")):
+        exe = tmp_path / (src.stem + ".bin")
+        subprocess.run([cc, std, "-I", str(root / "include"), str(src), str(lib), f"-Wl,-rpath,{lib.parent}", "-o",
+                        str(exe)], check=True)
+        out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+        assert out.returncode == 0, (src.name, out.returncode, out.stderr)
