@@ -32,8 +32,6 @@
 #include <cstdint>
 #include <cstring>
 #include <mutex>
-#include <unordered_map>
-#include <unordered_set>
 #include <vector>
 
 #include "../../include/lvn.h"
@@ -57,6 +55,8 @@ constexpr size_t kQuadSmem = (size_t)kSmemLeaves * 8;
 constexpr size_t kBigQuadSmem = (size_t)kSortLeaves * 8;
 constexpr size_t kSortSmem = (size_t)kSmemQuads * 16;
 constexpr int kSmallLeaves = 2048;  // leaf sorts up to this size run several CTAs per SM
+constexpr int kBucketBits = 6;      // leaves of larger hosts are sorted in 64 Morton-prefix buckets
+constexpr int kBuckets = 1 << kBucketBits;
 constexpr int kSmallQuads = 2048;   // as do quad sorts up to this size
 constexpr size_t kSmallLeafSmem = (size_t)kSmallLeaves * 8;
 constexpr size_t kSmallSortSmem = (size_t)kSmallQuads * 16;
@@ -102,8 +102,12 @@ struct SeamArgs {
     int vpc;
     int32_t* counts;    // leaves per host
     int32_t* qcounts;   // quads per host
-    uint64_t* sel;      // selected leaves' sort entries, per host at sel_off, unsorted
+    uint64_t* sel;      // selected leaves' sort entries, per host at sel_off, by bucket
     uint32_t* slots;    // their seam indices, by the slot in the entry
+    int32_t* bcount;    // leaves per (host, Morton-prefix bucket)
+    const int32_t* bstart;  // the bucket's first slot in the host's region
+    int32_t* cursor;    // next slot in the bucket
+    const int4* lsort;  // leaf sorts: (host, first slot, count, -)
     uint64_t* ent;      // sorted leaf entries
     uint32_t* leaves;   // seam index per rank
     uint64_t* qkey;     // quad path keys
@@ -188,10 +192,13 @@ __device__ __forceinline__ void unmorton(uint64_t code, int lev, int unit_log, i
     rel[2] = (int32_t)(compact1by2(code) << unit_log);
 }
 
-// SelectSeamNodes for every (host, gathered chunk) pair: the selected seam
-// nodes' sort entries ((morton << 4 | size log2) << 15 | slot, host-relative
-// Morton code in units of the host's smallest leaf) and seam indices, in the
-// host's region, in no particular order; counts[host] = how many.
+// SelectSeamNodes for every (host, gathered chunk) pair.  The counting pass
+// (Place = false) counts the selected seam nodes per host and per bucket of
+// the top kBucketBits bits of their host-relative Morton code (units of the
+// host's smallest leaf); the placing pass writes each one's sort entry
+// ((morton << 4 | size log2) << 15 | slot) and seam index at a slot of its
+// bucket, so that each host's region holds its buckets in Morton order.
+template <bool Place>
 __global__ void __launch_bounds__(128) k_seam_select(SeamArgs A) {
     const int4 pr = A.pairs[blockIdx.x];
     const SeamHost h = A.hosts[pr.z];
@@ -202,21 +209,26 @@ __global__ void __launch_bounds__(128) k_seam_select(SeamArgs A) {
     while ((h.unit << size_log) < ch.w / A.vpc) size_log++;
     const int s0 = A.seam_offsets[pr.x], s1 = A.seam_offsets[pr.x + 1];
     const int lane = threadIdx.x & 31;
+    const int shift = 3 * h.lev - kBucketBits;  // lev >= 4: 2 host size / smallest leaf >= 16
     for (int base = s0; base < s1; base += blockDim.x) {
         const int k = base + threadIdx.x;
         int32_t mn[3];
         const bool take = k < s1 && seam_selected(h, ch, pr.y, A.seams[k], A.vpc, mn);
-        const unsigned ballot = __ballot_sync(0xffffffffu, take);
-        if (!ballot) continue;
-        int first = 0;
-        if (lane == 0) first = atomicAdd(&A.counts[pr.z], __popc(ballot));
-        first = __shfl_sync(0xffffffffu, first, 0);
+        if (!Place) {
+            const unsigned ballot = __ballot_sync(0xffffffffu, take);
+            if (lane == 0 && ballot) atomicAdd(&A.counts[pr.z], __popc(ballot));
+        }
         if (!take) continue;
-        const int slot = first + __popc(ballot & ((1u << lane) - 1));
-        if (slot >= kMaxLeaves) continue;  // the host reports the count; nothing past its region is written
         const int32_t rel[3] = {mn[0] - h.min[0], mn[1] - h.min[1], mn[2] - h.min[2]};
-        A.sel[h.sel_off + slot] =
-            ((morton(rel, unit_log, h.lev) << 4 | (uint64_t)size_log) << kSlotBits) | (uint64_t)slot;
+        const uint64_t code = morton(rel, unit_log, h.lev);
+        const int b = pr.z * kBuckets + (int)(code >> shift);
+        if (!Place) {
+            atomicAdd(&A.bcount[b], 1);
+            continue;
+        }
+        const int slot = A.bstart[b] + atomicAdd(&A.cursor[b], 1);
+        if (slot >= kMaxLeaves) continue;  // the host reported the count; nothing past its region is written
+        A.sel[h.sel_off + slot] = ((code << 4 | (uint64_t)size_log) << kSlotBits) | (uint64_t)slot;
         A.slots[h.sel_off + slot] = (uint32_t)k;
     }
 }
@@ -374,14 +386,17 @@ __device__ uint64_t path_key(int32_t root, int dir, const int32_t line[3], int32
     return key;
 }
 
-// The leaves of host list[blockIdx.x], sorted: entries to A.ent, seam
-// indices by rank to A.leaves; in shared memory when they fit `cap`.
-__global__ void __launch_bounds__(1024) k_seam_leaves(SeamArgs A, const int32_t* list, int cap) {
+// Leaf sort lsort[blockIdx.x] = (host, first, count): the host's slots
+// [first, first + count) sorted (in shared memory when they fit `cap`) to
+// A.ent and A.leaves at the same positions of the host's leaf range.  A
+// small host is one sort; a larger one a sort per Morton-prefix bucket, which
+// together order the whole host.
+__global__ void __launch_bounds__(1024) k_seam_leaves(SeamArgs A, int cap) {
     extern __shared__ uint64_t smem[];
-    const int hi = list[blockIdx.x];
-    const SeamHost h = A.hosts[hi];
-    const int n = A.counts[hi];
-    uint64_t* ent = A.sel + h.sel_off;
+    const int4 it = A.lsort[blockIdx.x];
+    const SeamHost h = A.hosts[it.x];
+    const int n = it.z;
+    uint64_t* ent = A.sel + h.sel_off + it.y;
     if (n <= cap) {
         for (int i = threadIdx.x; i < n; i += blockDim.x) smem[i] = ent[i];
         __syncthreads();
@@ -390,8 +405,8 @@ __global__ void __launch_bounds__(1024) k_seam_leaves(SeamArgs A, const int32_t*
     block_sort<false>(ent, nullptr, n);
     for (int r = threadIdx.x; r < n; r += blockDim.x) {
         const uint64_t e = ent[r];
-        A.ent[h.leaf_off + r] = e;
-        A.leaves[h.leaf_off + r] = A.slots[h.sel_off + (e & ((1u << kSlotBits) - 1))];
+        A.ent[h.leaf_off + it.y + r] = e;
+        A.leaves[h.leaf_off + it.y + r] = A.slots[h.sel_off + (e & ((1u << kSlotBits) - 1))];
     }
 }
 
@@ -582,7 +597,9 @@ struct SeamWork {
     Grow<uint64_t> sel, ent, qkey, qval;
     Grow<uint32_t> slots, leaves;
     Grow<int2> items;
-    Grow<int32_t> lists;
+    Grow<int32_t> lists, bcount, bstart, cursor;
+    Grow<int4> lsort;
+    Grow<int32_t, true> hbuckets;  // pinned
     Grow<int64_t> offs;  // vertex offsets, triangle offsets
     Grow<lvn_mesh_vertex> vstage;
     Grow<lvn_mesh_triangle> tstage;
@@ -605,23 +622,60 @@ int cuda_rc(cudaError_t e) {
         if (rc__ != LVN_OK) return rc__; \
     } while (0)
 
-struct Key4Hash {
-    size_t operator()(const std::array<int32_t, 4>& k) const {
-        uint64_t h = 1469598103934665603ull;
-        for (int32_t v : k) h = (h ^ (uint32_t)v) * 1099511628211ull;
-        return (size_t)h;
+// Open-addressing hash table of 64-bit keys (linear probing, never full).
+class FlatTable {
+   public:
+    void reserve(size_t n) {
+        size_t cap = 16;
+        while (cap < 4 * n) cap <<= 1;
+        keys_.assign(cap, kEmpty);
+        vals_.assign(cap, -1);
+        mask_ = cap - 1;
     }
+    // inserts (key, val) unless key is present; returns false when it was
+    bool insert(uint64_t key, int32_t val) {
+        for (size_t i = slot(key);; i = (i + 1) & mask_) {
+            if (keys_[i] == key) return false;
+            if (keys_[i] == kEmpty) {
+                keys_[i] = key;
+                vals_[i] = val;
+                return true;
+            }
+        }
+    }
+    int32_t find(uint64_t key) const {  // -1 when absent
+        for (size_t i = slot(key);; i = (i + 1) & mask_) {
+            if (keys_[i] == key) return vals_[i];
+            if (keys_[i] == kEmpty) return -1;
+        }
+    }
+
+   private:
+    static constexpr uint64_t kEmpty = ~0ull;
+    size_t slot(uint64_t key) const { return (size_t)((key * 0x9e3779b97f4a7c15ull) >> 20) & mask_; }
+    std::vector<uint64_t> keys_;
+    std::vector<int32_t> vals_;
+    size_t mask_ = 0;
 };
 
-// The clipmap's active nodes (the chunks) and the nodes above them, keyed by
-// (min, size); FindNode / FindActiveNodes (clipmap.cpp:982-1013, 1449-1479)
-// over the complete octree rooted at (root_min, root_size).
+// The clipmap's active nodes (the chunks) and the nodes above them;
+// FindNode / FindActiveNodes (clipmap.cpp:982-1013, 1449-1479) over the
+// complete octree rooted at (root_min, root_size).  A node is keyed by its
+// root-relative position in CLIPMAP_LEAF_SIZE units (19 bits per axis: roots
+// up to 2^27) and log2(size / CLIPMAP_LEAF_SIZE).
 struct ActiveSet {
     int32_t root_min[3];
     int32_t root_size;
-    std::unordered_map<std::array<int32_t, 4>, int, Key4Hash> active;
-    std::unordered_set<std::array<int32_t, 4>, Key4Hash> above;  // nodes with an active node below them
+    FlatTable active;  // -> chunk index
+    FlatTable above;   // nodes with an active node below them (value unused)
 
+    uint64_t key(const int32_t mn[3], int32_t size) const {
+        int lg = 0;
+        while ((CLIPMAP_LEAF_SIZE << lg) < size) lg++;
+        uint64_t k = 0;
+        for (int a = 0; a < 3; a++) k = (k << 19) | (uint64_t)(((int64_t)mn[a] - root_min[a]) / CLIPMAP_LEAF_SIZE);
+        return (k << 5) | (uint64_t)lg;
+    }
     bool in_root(const int32_t mn[3], int32_t size) const {
         for (int a = 0; a < 3; a++) {
             const int64_t rel = (int64_t)mn[a] - root_min[a];
@@ -635,22 +689,22 @@ struct ActiveSet {
         for (int32_t s = size; s <= root_size; s *= 2) {
             int32_t a[3];
             for (int k = 0; k < 3; k++) a[k] = root_min[k] + (int32_t)(((int64_t)mn[k] - root_min[k]) / s * s);
-            auto it = active.find({a[0], a[1], a[2], s});
-            if (it != active.end()) {
-                out.push_back(it->second);
+            const int32_t c = active.find(key(a, s));
+            if (c >= 0) {
+                out.push_back(c);
                 return;
             }
         }
         descend(mn, size, out);
     }
     void descend(const int32_t mn[3], int32_t size, std::vector<int>& out) const {
-        if (size <= CLIPMAP_LEAF_SIZE || !above.count({mn[0], mn[1], mn[2], size})) return;
+        if (size <= CLIPMAP_LEAF_SIZE || above.find(key(mn, size)) < 0) return;
         const int32_t h = size / 2;
         for (int i = 0; i < 8; i++) {
             const int32_t c[3] = {mn[0] + ((i >> 2) & 1) * h, mn[1] + ((i >> 1) & 1) * h, mn[2] + (i & 1) * h};
-            auto it = active.find({c[0], c[1], c[2], h});
-            if (it != active.end())
-                out.push_back(it->second);
+            const int32_t ci = active.find(key(c, h));
+            if (ci >= 0)
+                out.push_back(ci);
             else
                 descend(c, h, out);
         }
@@ -675,30 +729,27 @@ int lvn_seam_generate(const lvn_chunk_desc* chunks, const int32_t* seam_offsets,
         return LVN_ERR_INVALID;
     if (root_size < CLIPMAP_LEAF_SIZE || (root_size & (root_size - 1))) return LVN_ERR_INVALID;
     const int vpc = voxels_per_chunk;
+    if (root_size > (1 << 27)) return LVN_ERR_INVALID;
     ActiveSet act;
     for (int a = 0; a < 3; a++) act.root_min[a] = root_min[a];
     act.root_size = root_size;
+    act.active.reserve((size_t)num_chunks);
+    act.above.reserve((size_t)num_chunks * 4 + 16);
     for (int c = 0; c < num_chunks; c++) {
         const lvn_chunk_desc& d = chunks[c];
         if (d.size < CLIPMAP_LEAF_SIZE || (d.size & (d.size - 1)) || !act.in_root(d.min, d.size) ||
             seam_offsets[c + 1] < seam_offsets[c])
             return LVN_ERR_INVALID;
-        if (!act.active.emplace(std::array<int32_t, 4>{d.min[0], d.min[1], d.min[2], d.size}, c).second)
-            return LVN_ERR_INVALID;  // listed twice
+        if (!act.active.insert(act.key(d.min, d.size), c)) return LVN_ERR_INVALID;  // listed twice
+    }
+    for (int c = 0; c < num_chunks; c++) {
+        const lvn_chunk_desc& d = chunks[c];
         for (int32_t s = d.size * 2; s <= root_size; s *= 2) {
             int32_t a[3];
             for (int k = 0; k < 3; k++) a[k] = root_min[k] + (int32_t)(((int64_t)d.min[k] - root_min[k]) / s * s);
-            if (!act.above.insert({a[0], a[1], a[2], s}).second) break;
-        }
-    }
-    // the clipmap's active nodes never overlap: a chunk with a chunk above it is an error
-    for (const auto& kv : act.active) {
-        if (act.above.count(kv.first)) return LVN_ERR_INVALID;
-        const std::array<int32_t, 4>& k = kv.first;
-        for (int32_t s = k[3] * 2; s <= root_size; s *= 2) {
-            int32_t a[3];
-            for (int q = 0; q < 3; q++) a[q] = root_min[q] + (int32_t)(((int64_t)k[q] - root_min[q]) / s * s);
-            if (act.active.count({a[0], a[1], a[2], s})) return LVN_ERR_INVALID;
+            // the clipmap's active nodes never overlap: an active node above an active node is an error
+            if (act.active.find(act.key(a, s)) >= 0) return LVN_ERR_INVALID;
+            if (!act.above.insert(act.key(a, s), 0)) break;
         }
     }
     const int64_t num_seams = num_chunks ? seam_offsets[num_chunks] : 0;
@@ -802,19 +853,54 @@ int lvn_seam_generate(const lvn_chunk_desc* chunks, const int32_t* seam_offsets,
     for (int a = 0; a < 3; a++) A.colour[a] = colour[a];
     A.sel = w.sel.p;
     A.slots = w.slots.p;
-    // 1: the selected seam nodes of every host
+    const size_t nb = nh * kBuckets;
+    SM_TRY(w.bcount.fit(nb));
+    SM_TRY(w.bstart.fit(nb));
+    SM_TRY(w.cursor.fit(nb));
+    SM_TRY(w.hbuckets.fit(nb));
+    A.bcount = w.bcount.p;
+    A.bstart = w.bstart.p;
+    A.cursor = w.cursor.p;
+    // 1: the selected seam nodes of every host, counted by bucket
     SM_TRY(cudaMemcpyAsync(w.hosts.p, hv.data(), sizeof(SeamHost) * nh, cudaMemcpyHostToDevice, st));
     SM_TRY(cudaMemsetAsync(w.counts.p, 0, sizeof(int32_t) * nh, st));
+    SM_TRY(cudaMemsetAsync(w.bcount.p, 0, sizeof(int32_t) * nb, st));
+    SM_TRY(cudaMemsetAsync(w.cursor.p, 0, sizeof(int32_t) * nb, st));
     if (!pairs.empty()) {
-        k_seam_select<<<(int)pairs.size(), 128, 0, st>>>(A);
+        k_seam_select<false><<<(int)pairs.size(), 128, 0, st>>>(A);
         SM_TRY(cudaGetLastError());
     }
     SM_TRY(cudaMemcpyAsync(w.hcounts.p, w.counts.p, sizeof(int32_t) * nh, cudaMemcpyDeviceToHost, st));
+    SM_TRY(cudaMemcpyAsync(w.hbuckets.p, w.bcount.p, sizeof(int32_t) * nb, cudaMemcpyDeviceToHost, st));
     SM_TRY(cudaStreamSynchronize(st));
+    // bucket starts, and the leaf sorts: one per small host, one per non-empty bucket of a larger one
+    std::vector<int32_t> bstart(nb);
+    std::vector<int4> small_sorts, big_sorts;
+    for (size_t i = 0; i < nh; i++) {
+        int run = 0;
+        for (int b = 0; b < kBuckets; b++) {
+            bstart[i * kBuckets + b] = run;
+            run += w.hbuckets.p[i * kBuckets + b];
+        }
+        const int n = w.hcounts.p[i];
+        if (n == 0) continue;
+        if (n <= kSmallLeaves) {
+            small_sorts.push_back(make_int4((int)i, 0, n, 0));
+            continue;
+        }
+        for (int b = 0; b < kBuckets; b++) {
+            const int c = w.hbuckets.p[i * kBuckets + b];
+            if (c) (c <= kSmallLeaves ? small_sorts : big_sorts).push_back(make_int4((int)i, bstart[i * kBuckets + b], c, 0));
+        }
+    }
+    SM_TRY(cudaMemcpyAsync(w.bstart.p, bstart.data(), sizeof(int32_t) * nb, cudaMemcpyHostToDevice, st));
+    if (!pairs.empty()) {
+        k_seam_select<true><<<(int)pairs.size(), 128, 0, st>>>(A);
+        SM_TRY(cudaGetLastError());
+    }
     int64_t leaf_total = 0, quad_total = 0;
     bool limit = false;
     std::vector<int2> items, big_items;  // (host, first leaf) of the quad enumeration's CTAs
-    std::vector<int32_t> small_hosts, big_hosts;  // size classes of the sorts
     for (size_t i = 0; i < nh; i++) {
         const int n = w.hcounts.p[i];
         limit |= n > kMaxLeaves;
@@ -822,7 +908,6 @@ int lvn_seam_generate(const lvn_chunk_desc* chunks, const int32_t* seam_offsets,
         hv[i].quad_off = quad_total;
         leaf_total += n;
         quad_total += 12 * (int64_t)n;
-        (n <= kSmallLeaves ? small_hosts : big_hosts).push_back((int32_t)i);
         if (n <= kSmemLeaves)
             for (int r = 0; r < n; r += kQuadBlock) items.push_back(make_int2((int)i, r));
         else
@@ -836,11 +921,14 @@ int lvn_seam_generate(const lvn_chunk_desc* chunks, const int32_t* seam_offsets,
     SM_TRY(w.qval.fit(std::max<int64_t>(quad_total, 1)));
     SM_TRY(w.items.fit(std::max<size_t>(items.size() + big_items.size(), 1)));
     SM_TRY(w.lists.fit(nh));
-    std::vector<int32_t> lists(small_hosts);
-    lists.insert(lists.end(), big_hosts.begin(), big_hosts.end());
+    std::vector<int32_t> lists(nh);
+    for (size_t i = 0; i < nh; i++) lists[i] = (int32_t)i;
     SM_TRY(cudaMemcpyAsync(w.lists.p, lists.data(), sizeof(int32_t) * nh, cudaMemcpyHostToDevice, st));
-    const int32_t* d_small = w.lists.p;
-    const int32_t* d_big = w.lists.p + small_hosts.size();
+    const size_t n_sorts = small_sorts.size() + big_sorts.size();
+    SM_TRY(w.lsort.fit(std::max<size_t>(n_sorts, 1)));
+    std::vector<int4> sorts(small_sorts);
+    sorts.insert(sorts.end(), big_sorts.begin(), big_sorts.end());
+    SM_TRY(cudaMemcpyAsync(w.lsort.p, sorts.data(), sizeof(int4) * n_sorts, cudaMemcpyHostToDevice, st));
     items.insert(items.end(), big_items.begin(), big_items.end());
     const int n_small = (int)(items.size() - big_items.size());
     A.ent = w.ent.p;
@@ -854,12 +942,15 @@ int lvn_seam_generate(const lvn_chunk_desc* chunks, const int32_t* seam_offsets,
     // the large hosts' sorts and enumeration beside the small hosts', on the second stream
     SM_TRY(cudaEventRecord(w.ev_fork, st));
     SM_TRY(cudaStreamWaitEvent(w.side, w.ev_fork, 0));
-    if (!big_hosts.empty()) {
-        k_seam_leaves<<<(int)big_hosts.size(), 1024, kLeafSmem, w.side>>>(A, d_big, kSortLeaves);
+    if (!big_sorts.empty()) {
+        SeamArgs B = A;
+        B.lsort = w.lsort.p + small_sorts.size();
+        k_seam_leaves<<<(int)big_sorts.size(), 1024, kLeafSmem, w.side>>>(B, kSortLeaves);
         SM_TRY(cudaGetLastError());
     }
-    if (!small_hosts.empty()) {
-        k_seam_leaves<<<(int)small_hosts.size(), 256, kSmallLeafSmem, st>>>(A, d_small, kSmallLeaves);
+    if (!small_sorts.empty()) {
+        A.lsort = w.lsort.p;
+        k_seam_leaves<<<(int)small_sorts.size(), 256, kSmallLeafSmem, st>>>(A, kSmallLeaves);
         SM_TRY(cudaGetLastError());
     }
     SM_TRY(cudaEventRecord(w.ev_fork2, st));
