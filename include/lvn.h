@@ -405,7 +405,8 @@ void lvn_simplify_options_default(lvn_simplify_options* options);
  * (indices local to the mesh), worldSpaceOffset offsets[4m .. 4m + 3] and
  * options[m]; inputs and outputs in host or device memory per `memory`.  The
  * simplified mesh is written at the same offsets of out_vertices /
- * out_triangles (which may be the inputs) and meshes[m]'s counts are updated.
+ * out_triangles (which may be the inputs) and meshes[m]'s counts are updated;
+ * the rest of each mesh's input range holds unspecified values afterwards.
  * Meshes under 100 triangles or vertices are copied unchanged, as in the
  * reference.  The QEF's approximate _mm_rsqrt_ps (qef_simd.h:209) is an exact
  * 1 / sqrt here; the random candidate edges follow std::mt19937(42) with

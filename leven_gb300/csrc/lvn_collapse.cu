@@ -40,6 +40,8 @@ namespace lvn {
 namespace {
 
 constexpr int kThreads = 512;    // two CTAs (meshes) per SM
+constexpr int kBigThreads = 1024;  // meshes above kBigTriangles: one CTA per SM, on a second stream
+constexpr int kBigTriangles = 12000;
 constexpr int kSortCap = 12288;  // u64 draws sorted in shared memory (96 KB); more sort in global memory
 constexpr size_t kSmem = (size_t)kSortCap * 8;
 constexpr int kMaxDegree = 16;  // COLLAPSE_MAX_DEGREE (ng_mesh_simplify.cpp:17)
@@ -295,21 +297,23 @@ __device__ int block_compact4(int n, Test test, Emit emit, int* s_warp, int* s_t
 
 // ---- the simplifier ---------------------------------------------------------
 
-__global__ void __launch_bounds__(kThreads, 2)
-    k_mesh_collapse(const MeshJob* __restrict__ jobs, const lvn_mesh_vertex* in_v, const lvn_mesh_triangle* in_t,
-                    lvn_mesh_vertex* out_v, lvn_mesh_triangle* out_t, int32_t* counts, Scratch S,
-                    const uint32_t* __restrict__ raw, int raw_len) {
+template <int Threads>
+__global__ void __launch_bounds__(Threads, 1024 / Threads)
+    k_mesh_collapse(const MeshJob* __restrict__ jobs, const int32_t* __restrict__ order, const lvn_mesh_vertex* in_v,
+                    const lvn_mesh_triangle* in_t, lvn_mesh_vertex* out_v, lvn_mesh_triangle* out_t, int32_t* counts,
+                    Scratch S, const uint32_t* __restrict__ raw, int raw_len) {
     extern __shared__ uint64_t smem[];
     __shared__ int s_warp[32], s_total, s_count, s_flag;
-    const MeshJob J = jobs[blockIdx.x];
+    const int jid = order[blockIdx.x];
+    const MeshJob J = jobs[jid];
     const int tid = threadIdx.x, nth = blockDim.x;
     const lvn_simplify_options& o = J.opt;
     if (J.nt < 100 || J.nv < 100) {  // left as generated (ng_mesh_simplify.cpp:445-448)
         for (int i = tid; i < J.nv; i += nth) out_v[J.v_off + i] = in_v[J.v_off + i];
         for (int i = tid; i < J.nt; i += nth) out_t[J.t_off + i] = in_t[J.t_off + i];
         if (tid == 0) {
-            counts[2 * blockIdx.x] = J.nv;
-            counts[2 * blockIdx.x + 1] = J.nt;
+            counts[2 * jid] = J.nv;
+            counts[2 * jid + 1] = J.nt;
         }
         return;
     }
@@ -600,8 +604,8 @@ __global__ void __launch_bounds__(kThreads, 2)
         out_t[J.t_off + t] = w;
     }
     if (tid == 0) {
-        counts[2 * blockIdx.x] = s_flag ? -1 : nv_out;
-        counts[2 * blockIdx.x + 1] = nt;
+        counts[2 * jid] = s_flag ? -1 : nv_out;
+        counts[2 * jid + 1] = nt;
     }
 }
 
@@ -628,8 +632,10 @@ struct Grow {
 struct CollapseWork {
     std::mutex mu;
     int device = -1;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr, side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     Grow<MeshJob> jobs;
+    Grow<int32_t> order;
     Grow<MV> verts;
     Grow<int3> tris;
     Grow<uint64_t> edges, claim, draws;
@@ -722,7 +728,13 @@ int lvn_mesh_simplify(const lvn_mesh_vertex* vertices, const lvn_mesh_triangle* 
     if (w.device != dev) {
         if (w.device >= 0) return LVN_ERR_INVALID;  // the scratch lives on the first device used
         CL_TRY(cudaStreamCreateWithFlags(&w.stream, cudaStreamNonBlocking));
-        CL_TRY(cudaFuncSetAttribute(k_mesh_collapse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem));
+        CL_TRY(cudaStreamCreateWithFlags(&w.side, cudaStreamNonBlocking));
+        CL_TRY(cudaEventCreateWithFlags(&w.fork, cudaEventDisableTiming));
+        CL_TRY(cudaEventCreateWithFlags(&w.join, cudaEventDisableTiming));
+        CL_TRY(cudaFuncSetAttribute(k_mesh_collapse<kThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kSmem));
+        CL_TRY(cudaFuncSetAttribute(k_mesh_collapse<kBigThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kSmem));
         w.device = dev;
     }
     cudaStream_t s = w.stream;
@@ -782,8 +794,27 @@ int lvn_mesh_simplify(const lvn_mesh_vertex* vertices, const lvn_mesh_triangle* 
     S.flag = w.flag.p;
     S.draws = w.draws.p;
     S.valid = w.valid.p;
-    k_mesh_collapse<<<num_meshes, kThreads, kSmem, s>>>(w.jobs.p, dv, dt, ov, ot, w.counts.p, S, w.raw.p,
-                                                        (int)w.raw_len);
+    // large meshes with twice the threads on a second stream, beside the rest
+    std::vector<int32_t> order;
+    for (int m = 0; m < num_meshes; m++)
+        if (jobs[m].nt > kBigTriangles) order.push_back(m);
+    const int n_big = (int)order.size();
+    for (int m = 0; m < num_meshes; m++)
+        if (jobs[m].nt <= kBigTriangles) order.push_back(m);
+    CL_TRY(w.order.fit(num_meshes));
+    CL_TRY(cudaMemcpyAsync(w.order.p, order.data(), sizeof(int32_t) * num_meshes, cudaMemcpyHostToDevice, s));
+    if (n_big) {
+        CL_TRY(cudaEventRecord(w.fork, s));
+        CL_TRY(cudaStreamWaitEvent(w.side, w.fork, 0));
+        k_mesh_collapse<kBigThreads><<<n_big, kBigThreads, kSmem, w.side>>>(
+            w.jobs.p, w.order.p, dv, dt, ov, ot, w.counts.p, S, w.raw.p, (int)w.raw_len);
+        CL_TRY(cudaGetLastError());
+        CL_TRY(cudaEventRecord(w.join, w.side));
+    }
+    if (num_meshes > n_big)
+        k_mesh_collapse<kThreads><<<num_meshes - n_big, kThreads, kSmem, s>>>(
+            w.jobs.p, w.order.p + n_big, dv, dt, ov, ot, w.counts.p, S, w.raw.p, (int)w.raw_len);
+    if (n_big) CL_TRY(cudaStreamWaitEvent(s, w.join, 0));
     CL_TRY(cudaGetLastError());
     w.hcounts.resize(2 * (size_t)num_meshes);
     CL_TRY(cudaMemcpyAsync(w.hcounts.data(), w.counts.p, sizeof(int32_t) * 2 * num_meshes, cudaMemcpyDeviceToHost, s));
@@ -794,15 +825,28 @@ int lvn_mesh_simplify(const lvn_mesh_vertex* vertices, const lvn_mesh_triangle* 
         meshes[m].num_triangles = w.hcounts[2 * m + 1];
     }
     if (memory == LVN_MEMORY_HOST) {
-        for (int m = 0; m < num_meshes; m++) {
-            const MeshJob& J = jobs[m];
-            if (meshes[m].num_vertices)
-                CL_TRY(cudaMemcpyAsync(out_vertices + J.v_off, ov + J.v_off,
-                                       sizeof(lvn_mesh_vertex) * meshes[m].num_vertices, cudaMemcpyDeviceToHost, s));
-            if (meshes[m].num_triangles)
-                CL_TRY(cudaMemcpyAsync(out_triangles + J.t_off, ot + J.t_off,
-                                       sizeof(lvn_mesh_triangle) * meshes[m].num_triangles, cudaMemcpyDeviceToHost, s));
-        }
+        // the meshes' input ranges, merged where they touch: one copy per run
+        auto copy_runs = [&](bool verts) -> int {
+            std::vector<std::pair<int64_t, int64_t>> r;
+            for (const MeshJob& J : jobs)
+                if (verts ? J.nv : J.nt) r.push_back(verts ? std::make_pair((int64_t)J.v_off, (int64_t)J.v_off + J.nv)
+                                                           : std::make_pair((int64_t)J.t_off, (int64_t)J.t_off + J.nt));
+            std::sort(r.begin(), r.end());
+            for (size_t i = 0; i < r.size();) {
+                int64_t a = r[i].first, b = r[i].second;
+                for (i++; i < r.size() && r[i].first <= b; i++) b = std::max(b, r[i].second);
+                const cudaError_t e =
+                    verts ? cudaMemcpyAsync(out_vertices + a, ov + a, sizeof(lvn_mesh_vertex) * (b - a),
+                                            cudaMemcpyDeviceToHost, s)
+                          : cudaMemcpyAsync(out_triangles + a, ot + a, sizeof(lvn_mesh_triangle) * (b - a),
+                                            cudaMemcpyDeviceToHost, s);
+                if (e != cudaSuccess) return cuda_rc(e);
+            }
+            return LVN_OK;
+        };
+        int rc = copy_runs(true);
+        if (rc == LVN_OK) rc = copy_runs(false);
+        if (rc) return rc;
         CL_TRY(cudaStreamSynchronize(s));
     }
     return LVN_OK;
