@@ -805,10 +805,11 @@ def run_select(args):
                    "stride": stride, "l2": "flushed between steps (256 MiB write)"},
         "e2e": {"value": round(n / (ms_e2e / 1e3), 1), "unit": "cameras/s", "h2d_bytes_per_step": 12 * n,
                 "d2h_bytes_per_step": 16 * total_nodes + 4 * n, "ms_per_step": round(ms_e2e, 4)},
-        "gpu_launches": 1,
+        "gpu_launches": 2,
         "roofline": {"bound": "hbm", "achieved": round(ach, 1), "peak": hbm_peak, "unit": "GB/s",
-                     "frac": round(ach / hbm_peak, 4), "traffic": committed_traffic("clipmap_walk"),
-                     "kernel": "k_clipmap_walk", "ms_per_launch": round(ms, 4),
+                     "frac": round(ach / hbm_peak, 4), "traffic": None,
+                     "kernel": "k_clipmap_select_warp (+ k_clipmap_walk for cameras past its limits)",
+                     "ms_per_launch": round(ms, 4),
                      "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
                      "algorithmic_bytes_per_launch": algo},
         "clocks": clocks.summary(),

@@ -45,6 +45,10 @@ constexpr int kWalkThreads = 256;
 constexpr int kSlotNodes = 2 * kMaxOpen + kMaxNodes;  // scratch per CTA: two open lists + the listed nodes
 constexpr int kHostStride = 1024;                     // first-pass list length per camera, host-buffer form
 constexpr int kMaxBoxes = 4096;                       // operations per touch-set call
+constexpr int kWarpList = 1024;  // selection by one warp per camera: listed nodes
+constexpr int kWarpOpen = 512;   // and open nodes per level; beyond either the CTA walk redoes the camera
+constexpr int kWarpsPerCta = 8;
+constexpr int kRedo = -2;        // count of a camera the warp walk left to the CTA walk
 
 struct Node {
     int32_t min[3];
@@ -112,7 +116,7 @@ __device__ __forceinline__ unsigned long long order_key(const Node& n, const Tre
 __global__ void __launch_bounds__(kWalkThreads) k_clipmap_walk(Tree t, const float* __restrict__ cams, int num_queries,
                                                                const int32_t* __restrict__ boxes, int num_boxes,
                                                                Node* __restrict__ scratch, lvn_chunk_desc* out,
-                                                               int stride, int32_t* counts) {
+                                                               int stride, int32_t* counts, int redo_only) {
     extern __shared__ unsigned long long sk[];  // [kMaxNodes] sort entries
     __shared__ int s_open[2], s_listed, s_over;
     const bool post = cams == nullptr;
@@ -120,6 +124,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_clipmap_walk(Tree t, const flo
     Node* const listed = open + 2 * kMaxOpen;
     const int tid = threadIdx.x, nth = blockDim.x;
     for (int q = blockIdx.x; q < num_queries; q += gridDim.x) {
+        if (redo_only && counts[q] != kRedo) continue;  // the warp walk answered this camera
         float cam[3] = {0.f, 0.f, 0.f};
         if (!post)
             for (int a = 0; a < 3; a++) cam[a] = cams[3 * q + a];
@@ -220,6 +225,117 @@ __global__ void __launch_bounds__(kWalkThreads) k_clipmap_walk(Tree t, const flo
     }
 }
 
+// Selection with one warp per camera (warp-synchronous: ballots, shuffles and
+// __syncwarp, no CTA barriers).  Open nodes are packed leaf-grid positions
+// (10 bits an axis) and LOD; a listed node is kept only as its sort key, which
+// identifies it (first leaf and LOD).  A camera that lists more than
+// kWarpList nodes or opens more than kWarpOpen in a level gets kRedo.
+__device__ __forceinline__ uint64_t pack_open(const int32_t p[3], int lod) {
+    return ((uint64_t)p[0] << 23) | ((uint64_t)p[1] << 13) | ((uint64_t)p[2] << 3) | (uint64_t)lod;
+}
+
+__global__ void __launch_bounds__(kWarpsPerCta * 32) k_clipmap_select_warp(Tree t, const float* __restrict__ cams,
+                                                                          int num_queries, uint64_t* scratch,
+                                                                          lvn_chunk_desc* out, int stride,
+                                                                          int32_t* counts) {
+    extern __shared__ unsigned long long wkeys[];  // [kWarpsPerCta][kWarpList]
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const unsigned below = (1u << lane) - 1;
+    unsigned long long* keys = wkeys + wib * kWarpList;
+    const int wslot = blockIdx.x * kWarpsPerCta + wib;
+    uint64_t* open = scratch + (size_t)wslot * 2 * kWarpOpen;  // list c at open + c * kWarpOpen
+    const int leaf = CLIPMAP_LEAF_SIZE;
+    for (int q = wslot; q < num_queries; q += gridDim.x * kWarpsPerCta) {
+        const float cam[3] = {cams[3 * q], cams[3 * q + 1], cams[3 * q + 2]};
+        const int per = t.per, ntop = per * per * per, top_units = t.top_size / leaf;
+        for (int i = lane; i < ntop; i += 32) {  // the host keeps ntop <= kWarpOpen for this walk
+            const int32_t p[3] = {(i / (per * per)) * top_units, ((i / per) % per) * top_units, (i % per) * top_units};
+            open[i] = pack_open(p, t.top_lod);
+        }
+        __syncwarp();
+        int cur = 0, n = ntop, listed = 0;
+        bool over = false;
+        for (int lod = t.top_lod; lod >= 0; lod--) {
+            int next = 0;
+            for (int base = 0; base < n; base += 32) {
+                const int i = base + lane;
+                Node nd;
+                bool list = false, expand = false;
+                if (i < n) {
+                    const uint64_t o = open[cur * kWarpOpen + i];
+                    const int32_t p[3] = {(int32_t)((o >> 23) & 1023), (int32_t)((o >> 13) & 1023),
+                                          (int32_t)((o >> 3) & 1023)};
+                    for (int a = 0; a < 3; a++) nd.min[a] = t.root_min[a] + p[a] * leaf;
+                    nd.size = leaf << lod;
+                    list = distance_to_node(nd, cam) >= kLodActiveDistances[lod];
+                    expand = !list && lod > 0;
+                }
+                const unsigned bl = __ballot_sync(0xffffffffu, list);
+                if (list) {
+                    const int pos = listed + __popc(bl & below);
+                    if (pos < kWarpList) keys[pos] = order_key(nd, t, lod, false);
+                }
+                listed += __popc(bl);
+                const unsigned be = __ballot_sync(0xffffffffu, expand);
+                if (expand) {
+                    const int pos = next + 8 * __popc(be & below);
+                    const int32_t h = (nd.size >> 1) / leaf;
+                    int32_t p[3];
+                    for (int a = 0; a < 3; a++) p[a] = (nd.min[a] - t.root_min[a]) / leaf;
+                    for (int c = 0; c < 8; c++) {
+                        const int32_t cp[3] = {p[0] + ((c >> 2) & 1) * h, p[1] + ((c >> 1) & 1) * h, p[2] + (c & 1) * h};
+                        if (pos + c < kWarpOpen) open[(cur ^ 1) * kWarpOpen + pos + c] = pack_open(cp, lod - 1);
+                    }
+                }
+                next += 8 * __popc(be);
+            }
+            __syncwarp();
+            over |= next > kWarpOpen;
+            n = min(next, kWarpOpen);
+            cur ^= 1;
+        }
+        over |= listed > kWarpList;
+        if (!over) {
+            // bitonic network over any n (mirrored first step), warp-synchronous
+            for (int k = 2; k < 2 * listed; k <<= 1) {
+                for (int j = k >> 1; j > 0; j >>= 1) {
+                    const int mask = j == (k >> 1) ? k - 1 : j;
+                    for (int i = lane; i < listed; i += 32) {
+                        const int l = i ^ mask;
+                        if (l > i && l < listed) {
+                            const unsigned long long a = keys[i], b = keys[l];
+                            if (a > b) {
+                                keys[i] = b;
+                                keys[l] = a;
+                            }
+                        }
+                    }
+                    __syncwarp();
+                }
+            }
+            const int nout = min(listed, stride);
+            for (int i = lane; i < nout; i += 32) {
+                const unsigned long long key = keys[i];
+                const int lod = (int)(key & 7);
+                const unsigned long long code = key >> 3;
+                int32_t p[3] = {0, 0, 0};
+                for (int bit = t.depth - 1; bit >= 0; bit--) {
+                    const int tr = (int)((code >> (3 * bit)) & 7);
+                    p[0] = (p[0] << 1) | ((tr >> 2) & 1);
+                    p[1] = (p[1] << 1) | ((tr >> 1) & 1);
+                    p[2] = (p[2] << 1) | (tr & 1);
+                }
+                lvn_chunk_desc d;
+                for (int a = 0; a < 3; a++) d.min[a] = t.root_min[a] + p[a] * leaf;
+                d.size = leaf << lod;
+                out[(size_t)q * stride + i] = d;
+            }
+        }
+        if (lane == 0) counts[q] = over ? kRedo : listed;
+        __syncwarp();
+    }
+}
+
 // Packs the host form's lists back to back: list q (counts[q] nodes) goes to
 // packed[place[2q]] from the first pass (stride kHostStride) or, when
 // place[2q + 1] >= 0, from that row of the second pass (stride kMaxNodes).
@@ -266,6 +382,7 @@ struct Work {
     Grow<lvn_chunk_desc> wide, wide_big, packed;   // pass outputs (stride kHostStride / kMaxNodes), packed lists
     Grow<int32_t, true> hcounts, hplace;           // pinned
     int32_t* dboxes = nullptr;                     // kMaxBoxes x 6
+    Grow<uint64_t> wscratch;                       // the warp walk's open lists
 };
 Work& work() {
     static Work w;
@@ -314,6 +431,8 @@ int ensure_work(Work& w, int num_queries) {
         CM_TRY(cudaDeviceGetAttribute(&w.num_sms, cudaDevAttrMultiProcessorCount, dev));
         CM_TRY(cudaFuncSetAttribute(k_clipmap_walk, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)(sizeof(unsigned long long) * kMaxNodes)));
+        CM_TRY(cudaFuncSetAttribute(k_clipmap_select_warp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(sizeof(unsigned long long) * kWarpList * kWarpsPerCta)));
         CM_TRY(cudaStreamCreateWithFlags(&w.stream, cudaStreamNonBlocking));
         CM_TRY(cudaMalloc(&w.dboxes, sizeof(int32_t) * 6 * kMaxBoxes));
         w.device = dev;
@@ -333,10 +452,27 @@ int ensure_work(Work& w, int num_queries) {
 }
 
 void launch_walk(const Work& w, const Tree& t, const float* dcams, int num_queries, const int32_t* dboxes,
-                 int num_boxes, lvn_chunk_desc* out, int stride, int32_t* counts, cudaStream_t s) {
+                 int num_boxes, lvn_chunk_desc* out, int stride, int32_t* counts, cudaStream_t s, int redo_only = 0) {
     const int ctas = std::min(walk_ctas(w, num_queries), w.scratch_ctas);
     k_clipmap_walk<<<ctas, kWalkThreads, sizeof(unsigned long long) * kMaxNodes, s>>>(
-        t, dcams, num_queries, dboxes, num_boxes, w.scratch, out, stride, counts);
+        t, dcams, num_queries, dboxes, num_boxes, w.scratch, out, stride, counts, redo_only);
+}
+
+// Selection for cameras: the warp walk where the top level fits it, then the
+// CTA walk for the cameras it left (on the same stream).
+int launch_select(Work& w, const Tree& t, const float* dcams, int num_queries, lvn_chunk_desc* out, int stride,
+                  int32_t* counts, cudaStream_t s) {
+    if (t.per * t.per * t.per > kWarpOpen) {
+        launch_walk(w, t, dcams, num_queries, nullptr, 0, out, stride, counts, s);
+        return cuda_rc(cudaGetLastError());
+    }
+    const int ctas = std::max(1, std::min((num_queries + kWarpsPerCta - 1) / kWarpsPerCta, 3 * w.num_sms));
+    CM_TRY(w.wscratch.fit((size_t)ctas * kWarpsPerCta * 2 * kWarpOpen));
+    k_clipmap_select_warp<<<ctas, kWarpsPerCta * 32, sizeof(unsigned long long) * kWarpList * kWarpsPerCta, s>>>(
+        t, dcams, num_queries, w.wscratch.p, out, stride, counts);
+    CM_TRY(cudaGetLastError());
+    launch_walk(w, t, dcams, num_queries, nullptr, 0, out, stride, counts, s, 1);
+    return cuda_rc(cudaGetLastError());
 }
 
 }  // namespace
@@ -367,8 +503,8 @@ int lvn_clipmap_select(const float* cameras, int32_t num_cameras, const int32_t 
     CM_TRY(w.hplace.fit(2 * n));
     // first pass: every camera, lists cut at kHostStride nodes
     CM_TRY(cudaMemcpyAsync(w.dcams.p, cameras, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, w.stream));
-    launch_walk(w, t, w.dcams.p, num_cameras, nullptr, 0, w.wide.p, kHostStride, w.dcounts.p, w.stream);
-    CM_TRY(cudaGetLastError());
+    rc = launch_select(w, t, w.dcams.p, num_cameras, w.wide.p, kHostStride, w.dcounts.p, w.stream);
+    if (rc) return rc;
     CM_TRY(cudaMemcpyAsync(w.hcounts.p, w.dcounts.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, w.stream));
     CM_TRY(cudaStreamSynchronize(w.stream));
     int64_t total = 0;
@@ -425,8 +561,7 @@ int lvn_clipmap_select_device(const float* d_cameras, int32_t num_cameras, const
     std::lock_guard<std::mutex> lock(w.mu);
     rc = ensure_work(w, num_cameras);
     if (rc) return rc;
-    launch_walk(w, t, d_cameras, num_cameras, nullptr, 0, d_out, stride, d_counts, (cudaStream_t)cuda_stream);
-    return cuda_rc(cudaGetLastError());
+    return launch_select(w, t, d_cameras, num_cameras, d_out, stride, d_counts, (cudaStream_t)cuda_stream);
 }
 
 int lvn_clipmap_touched(const lvn_csg_op* ops, int32_t num_ops, const int32_t root_min[3], int32_t root_size,
