@@ -1495,18 +1495,27 @@ __global__ void __launch_bounds__(kThreads) k_leaf(BatchPtrs b) {
         SimpQef sq;
         if (simp) simp_zero(sq);
         // every edge lookup first, so that their table probes are in flight
-        // together, then the crossings in edge order
+        // together, then the crossings in edge order.  Iteration k handles the
+        // leaf's k-th active edge (ascending), so a warp runs as many
+        // iterations as its busiest leaf has edges, not one per edge index.
+        const int cnt = __popc(edge_list & 0xfff);
         uint32_t dis[12];
+        int rest = edge_list & 0xfff;
 #pragma unroll
-        for (int e = 0; e < 12; e++) {
+        for (int k = 0; k < 12; k++) {
+            if (k >= cnt) break;
+            const int e = __ffs(rest) - 1;
+            rest &= rest - 1;
             const int e0 = edge_c0(e);
-            dis[e] = ((edge_list >> e) & 1)
-                         ? hv.find((uint32_t)edge_key<VPC>(x + (e0 >> 2), y + ((e0 >> 1) & 1), z + (e0 & 1), e / 4))
-                         : ~0u;
+            dis[k] = hv.find((uint32_t)edge_key<VPC>(x + (e0 >> 2), y + ((e0 >> 1) & 1), z + (e0 & 1), e / 4));
         }
+        rest = edge_list & 0xfff;
 #pragma unroll
-        for (int e = 0; e < 12; e++) {
-            const uint32_t di = dis[e];
+        for (int k = 0; k < 12; k++) {
+            if (k >= cnt) break;
+            const int e = __ffs(rest) - 1;
+            rest &= rest - 1;
+            const uint32_t di = dis[k];
             if (di == ~0u) continue;
             const int e0 = edge_c0(e), e1 = edge_c1(e);
             const int o0x = e0 >> 2, o0y = (e0 >> 1) & 1, o0z = e0 & 1;
