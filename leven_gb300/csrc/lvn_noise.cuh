@@ -38,6 +38,34 @@ __device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, fl
     return fmaf(az, bz, fmaf(ay, by, ax * bx));
 }
 
+// Two-lane single precision arithmetic (the f32x2 forms of add, sub, mul and
+// fma, sm_100 and later): each lane is the IEEE round-to-nearest result of the
+// scalar operation on that lane, so two independent evaluations step through
+// one instruction together and give the scalar code's bits.
+// One exception: the code generator fuses a two-lane product that feeds a
+// two-lane add or sub into one two-lane fma, even with -fmad=false and an
+// explicit .rn (measured on GB300: every such mismatch equals the fused
+// result).  So a product whose only use is an add or sub is taken in scalar
+// (mul2s below): scalar products with a rounding mode are never fused.
+__device__ __forceinline__ float2 v2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+    float2 d;
+    asm("{.reg .b64 ra, rb, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\t"
+        "mov.b64 rb, {%4, %5};\n\t"
+        "sub.rn.f32x2 rd, ra, rb;\n\t"
+        "mov.b64 {%0, %1}, rd;}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+__device__ __forceinline__ float2 mul2s(float2 a, float2 b) { return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)); }
+__device__ __forceinline__ float2 floor2(float2 a) { return make_float2(floorf(a.x), floorf(a.y)); }
+__device__ __forceinline__ float2 max02(float2 a) { return make_float2(fmaxf(a.x, 0.f), fmaxf(a.y, 0.f)); }
+
 struct Noise {
     const uint16_t* __restrict__ ak;  // per texel: its alpha as the 3D second lookup's column (255 read as
                                       // column 0) in bits 0-7, alpha & 15 in bits 8-11
@@ -85,6 +113,39 @@ struct Noise {
         return 70.f * ((n0 + n1) + n2);
     }
 
+    // snoise2 at two points, one per lane, in the operation order of snoise2
+    __device__ __forceinline__ float2 snoise2x2(float2 px, float2 py) const {
+        const float F2 = 0.366025403784f;
+        const float G2 = 0.211324865405f;
+        const float C2 = 1.f - 2.f * G2;
+        const float2 s = mul2s(add2(px, py), v2(F2));
+        const float2 pix = floor2(add2(px, s));
+        const float2 piy = floor2(add2(py, s));
+        const float2 t = mul2s(add2(pix, piy), v2(G2));
+        const float2 x0 = sub2(px, sub2(pix, t));
+        const float2 y0 = sub2(py, sub2(piy, t));
+        const bool xg0 = x0.x > y0.x, xg1 = x0.y > y0.y;
+        const unsigned qa = __ldg(k4 + ((((int)piy.x & 255) << 8) | ((int)pix.x & 255)));
+        const unsigned qb = __ldg(k4 + ((((int)piy.y & 255) << 8) | ((int)pix.y & 255)));
+        const float2* g2 = reinterpret_cast<const float2*>(g);
+        const float2 ga0 = g2[2 * (qa & 15)], gb0 = g2[2 * ((qa >> (xg0 ? 4 : 8)) & 15)], gc0 = g2[2 * (qa >> 12)];
+        const float2 ga1 = g2[2 * (qb & 15)], gb1 = g2[2 * ((qb >> (xg1 ? 4 : 8)) & 15)], gc1 = g2[2 * (qb >> 12)];
+
+        float2 t0 = max02(sub2(v2(0.5f), fma2(y0, y0, mul2(x0, x0))));
+        t0 = mul2(t0, t0);
+        const float2 n0 = mul2s(mul2(t0, t0), make_float2(dot2(ga0.x, ga0.y, x0.x, y0.x), dot2(ga1.x, ga1.y, x0.y, y0.y)));
+        const float2 x1 = add2(sub2(x0, make_float2(xg0 ? 1.f : 0.f, xg1 ? 1.f : 0.f)), v2(G2));
+        const float2 y1 = add2(sub2(y0, make_float2(xg0 ? 0.f : 1.f, xg1 ? 0.f : 1.f)), v2(G2));
+        float2 t1 = max02(sub2(v2(0.5f), fma2(y1, y1, mul2(x1, x1))));
+        t1 = mul2(t1, t1);
+        const float2 n1 = mul2s(mul2(t1, t1), make_float2(dot2(gb0.x, gb0.y, x1.x, y1.x), dot2(gb1.x, gb1.y, x1.y, y1.y)));
+        const float2 x2 = sub2(x0, v2(C2)), y2 = sub2(y0, v2(C2));
+        float2 t2 = max02(sub2(v2(0.5f), fma2(y2, y2, mul2(x2, x2))));
+        t2 = mul2(t2, t2);
+        const float2 n2 = mul2s(mul2(t2, t2), make_float2(dot2(gc0.x, gc0.y, x2.x, y2.x), dot2(gc1.x, gc1.y, x2.y, y2.y)));
+        return mul2(v2(70.f), add2(add2(n0, n1), n2));
+    }
+
     // one corner of snoise3: the texel (iy, ix)'s alpha picks the column of
     // the texel in row iz whose alpha & 15 is the gradient index
     __device__ __forceinline__ float corner3(int ix, int iy, int iz, float x, float y, float z) const {
@@ -126,8 +187,60 @@ struct Noise {
         return 32.f * (((n0 + n1) + n2) + n3);
     }
 
-    // BasicFractal (noise.cl:8-36), NOISE_SCALE == 1; the octave loop is
-    // fully unrolled for the common 8-octave case
+    // the gradient of one snoise3 corner: two chained lookups
+    __device__ __forceinline__ float4 grad3(int ix, int iy, int iz) const {
+        const int a = __ldg(ak + texel(iy, ix)) & 255;
+        const int k = __ldg(ak + texel(iz, a)) >> 8;
+        return reinterpret_cast<const float4*>(g)[k];
+    }
+    // one snoise3 corner at two points, one per lane (corner3's operations)
+    __device__ __forceinline__ float2 corner3x2(float4 ga, float4 gb, float2 x, float2 y, float2 z) const {
+        float2 tt = max02(sub2(v2(0.6f), fma2(z, z, fma2(y, y, mul2(x, x)))));
+        tt = mul2(tt, tt);
+        return mul2s(mul2(tt, tt), make_float2(dot3(ga.x, ga.y, ga.z, x.x, y.x, z.x), dot3(gb.x, gb.y, gb.z, x.y, y.y, z.y)));
+    }
+
+    // snoise3 at two points, one per lane, in the operation order of snoise3
+    __device__ __forceinline__ float2 snoise3x2(float2 px, float2 py, float2 pz) const {
+        const float F3 = 0.333333333333f;
+        const float G3 = 0.166666666667f;
+        const float C2 = 2.f * G3;
+        const float C3 = 1.f - 3.f * G3;
+        const float2 s = mul2s(add2(add2(px, py), pz), v2(F3));
+        const float2 pix = floor2(add2(px, s));
+        const float2 piy = floor2(add2(py, s));
+        const float2 piz = floor2(add2(pz, s));
+        const float2 t = mul2s(add2(add2(pix, piy), piz), v2(G3));
+        const float2 x0 = sub2(px, sub2(pix, t));
+        const float2 y0 = sub2(py, sub2(piy, t));
+        const float2 z0 = sub2(pz, sub2(piz, t));
+        const int ixa = (int)pix.x, iya = (int)piy.x, iza = (int)piz.x;
+        const int ixb = (int)pix.y, iyb = (int)piy.y, izb = (int)piz.y;
+        const bool xya = x0.x >= y0.x, xza = x0.x >= z0.x, yza = y0.x >= z0.x;
+        const bool xyb = x0.y >= y0.y, xzb = x0.y >= z0.y, yzb = y0.y >= z0.y;
+        const int o1xa = xya && xza, o1ya = !xya && yza, o1za = !xza && !yza;
+        const int o2xa = xya || xza, o2ya = !xya || yza, o2za = !xza || !yza;
+        const int o1xb = xyb && xzb, o1yb = !xyb && yzb, o1zb = !xzb && !yzb;
+        const int o2xb = xyb || xzb, o2yb = !xyb || yzb, o2zb = !xzb || !yzb;
+        const float2 n0 = corner3x2(grad3(ixa, iya, iza), grad3(ixb, iyb, izb), x0, y0, z0);
+        const float2 n1 = corner3x2(grad3(ixa + o1xa, iya + o1ya, iza + o1za), grad3(ixb + o1xb, iyb + o1yb, izb + o1zb),
+                                    add2(sub2(x0, make_float2((float)o1xa, (float)o1xb)), v2(G3)),
+                                    add2(sub2(y0, make_float2((float)o1ya, (float)o1yb)), v2(G3)),
+                                    add2(sub2(z0, make_float2((float)o1za, (float)o1zb)), v2(G3)));
+        const float2 n2 = corner3x2(grad3(ixa + o2xa, iya + o2ya, iza + o2za), grad3(ixb + o2xb, iyb + o2yb, izb + o2zb),
+                                    add2(sub2(x0, make_float2((float)o2xa, (float)o2xb)), v2(C2)),
+                                    add2(sub2(y0, make_float2((float)o2ya, (float)o2yb)), v2(C2)),
+                                    add2(sub2(z0, make_float2((float)o2za, (float)o2zb)), v2(C2)));
+        const float2 n3 = corner3x2(grad3(ixa + 1, iya + 1, iza + 1), grad3(ixb + 1, iyb + 1, izb + 1), sub2(x0, v2(C3)),
+                                    sub2(y0, v2(C3)), sub2(z0, v2(C3)));
+        return mul2(v2(32.f), add2(add2(add2(n0, n1), n2), n3));
+    }
+
+    // BasicFractal (noise.cl:8-36), NOISE_SCALE == 1, two octaves a step:
+    // octaves i and i + 1 are the two lanes of one paired evaluation.  The
+    // coordinates, amplitudes and the accumulation keep the scalar order,
+    // octave by octave.  The loop is fully unrolled for the common 8-octave
+    // case.
     template <int OCT>
     __device__ __forceinline__ float fbm2_fixed(float frequency, float lacunarity, float persistence, float x,
                                                 float y) const {
@@ -136,12 +249,17 @@ struct Noise {
         px = px * frequency;
         py = py * frequency;
 #pragma unroll
-        for (int i = 0; i < OCT; i++) {
-            noise = fmaf(snoise2(px, py), amplitude, noise);
-            px = px * lacunarity;
-            py = py * lacunarity;
+        for (int i = 0; i + 1 < OCT; i += 2) {
+            const float qx = px * lacunarity, qy = py * lacunarity;
+            const float2 n = snoise2x2(make_float2(px, qx), make_float2(py, qy));
+            noise = fmaf(n.x, amplitude, noise);
             amplitude = amplitude * persistence;
+            noise = fmaf(n.y, amplitude, noise);
+            amplitude = amplitude * persistence;
+            px = qx * lacunarity;
+            py = qy * lacunarity;
         }
+        if (OCT & 1) noise = fmaf(snoise2(px, py), amplitude, noise);
         return noise;
     }
     __device__ __forceinline__ float fbm2(int octaves, float frequency, float lacunarity, float persistence, float x,
@@ -151,27 +269,39 @@ struct Noise {
         float noise = 0.f, amplitude = 1.f;
         px = px * frequency;
         py = py * frequency;
-        for (int i = 0; i < octaves; i++) {
-            noise = fmaf(snoise2(px, py), amplitude, noise);
-            px = px * lacunarity;
-            py = py * lacunarity;
+        int i = 0;
+        for (; i + 1 < octaves; i += 2) {
+            const float qx = px * lacunarity, qy = py * lacunarity;
+            const float2 n = snoise2x2(make_float2(px, qx), make_float2(py, qy));
+            noise = fmaf(n.x, amplitude, noise);
             amplitude = amplitude * persistence;
+            noise = fmaf(n.y, amplitude, noise);
+            amplitude = amplitude * persistence;
+            px = qx * lacunarity;
+            py = qy * lacunarity;
         }
+        if (i < octaves) noise = fmaf(snoise2(px, py), amplitude, noise);
         return noise;
     }
 
-    // 3D analogue of BasicFractal (the cave term)
+    // 3D analogue of BasicFractal (the cave term), two octaves a step as fbm2
     __device__ __forceinline__ float fbm3(int octaves, float frequency, float lacunarity, float persistence, float x,
                                           float y, float z) const {
         float px = x * frequency, py = y * frequency, pz = z * frequency;
         float noise = 0.f, amplitude = 1.f;
-        for (int i = 0; i < octaves; i++) {
-            noise = fmaf(snoise3(px, py, pz), amplitude, noise);
-            px = px * lacunarity;
-            py = py * lacunarity;
-            pz = pz * lacunarity;
+        int i = 0;
+        for (; i + 1 < octaves; i += 2) {
+            const float qx = px * lacunarity, qy = py * lacunarity, qz = pz * lacunarity;
+            const float2 n = snoise3x2(make_float2(px, qx), make_float2(py, qy), make_float2(pz, qz));
+            noise = fmaf(n.x, amplitude, noise);
             amplitude = amplitude * persistence;
+            noise = fmaf(n.y, amplitude, noise);
+            amplitude = amplitude * persistence;
+            px = qx * lacunarity;
+            py = qy * lacunarity;
+            pz = qz * lacunarity;
         }
+        if (i < octaves) noise = fmaf(snoise3(px, py, pz), amplitude, noise);
         return noise;
     }
 
