@@ -591,18 +591,23 @@ __global__ void __launch_bounds__(96) k_field(BatchPtrs b) {
 // rows there get their final-air and changed bits rewritten.
 // ---------------------------------------------------------------------------
 
-// Field of a density with a 3D term (the cave fBm): every point is evaluated.
-// One CTA per z slice; the slice's 66 column heights are computed once into
-// shared memory, then the 66 x 66 points are spread over all lanes (97% of
-// lanes busy, against 69% for one thread per column) and their solid bits
-// are gathered into the row words with shared-memory atomics.
+// Field of a density with a 3D term (the cave fBm).  One CTA per z slice;
+// the slice's 66 column heights are computed once into shared memory.  The
+// density is fma(amp3, fbm3, base) with base = y - amp2 h, and |amp3 fbm3| is
+// at most b.cave_band, so where |base| exceeds it the sign of the density,
+// which is all the field keeps, is the sign of base.  The other points go to a
+// shared list that all lanes then evaluate in full; their solid bits are
+// gathered into the row words with shared-memory atomics.
 template <int VPC>
 __global__ void __launch_bounds__(128) k_field_caves(BatchPtrs b) {
     using G = Geo<VPC>;
     __shared__ __align__(16) float sg[64];
     __shared__ float hs[G::FD];
     __shared__ uint32_t words[3][G::FD];
+    __shared__ uint16_t list[G::FD * G::FD];
+    __shared__ int nlist;
     if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
+    if (threadIdx.x == 0) nlist = 0;
     for (int i = threadIdx.x; i < 3 * G::FD; i += blockDim.x) (&words[0][0])[i] = 0u;
     const int c = blockIdx.y, z = blockIdx.x;
     if (b.s_on && b.sslot[c] >= 0) return;  // the surrogate's field (k_field_sdens)
@@ -622,7 +627,30 @@ __global__ void __launch_bounds__(128) k_field_caves(BatchPtrs b) {
     const int dm = b.default_material;
     const bool write_mats = b.need_mats != 0;
     uint8_t* mats = b.mats + (size_t)c * G::F + G::FD * G::FD * z;
-    for (int i = threadIdx.x; i < G::FD * G::FD; i += blockDim.x) {
+    const float amp2 = dp.amp2, band = b.cave_band;
+    const int lane = threadIdx.x & 31;
+    // the whole CTA runs every round, so that each ballot has all 32 lanes
+    for (int i0 = 0; i0 < G::FD * G::FD; i0 += blockDim.x) {
+        const int i = i0 + threadIdx.x;
+        const bool valid = i < G::FD * G::FD;
+        const int y = i / G::FD, x = i - G::FD * y;
+        const float base = valid ? fmaf(-amp2, hs[x], (float)(y * scale + oy)) : 0.f;
+        const bool decided = valid && fabsf(base) > band;  // false for a NaN band or base
+        const unsigned need = __ballot_sync(0xffffffffu, valid && !decided);
+        int slot = 0;
+        if (lane == 0 && need) slot = atomicAdd(&nlist, __popc(need));
+        slot = __shfl_sync(0xffffffffu, slot, 0);
+        if (valid && !decided) list[slot + __popc(need & ((1u << lane) - 1u))] = (uint16_t)i;
+        if (decided) {
+            const int m = base < 0.f ? dm : MATERIAL_AIR;
+            if (write_mats) mats[i] = (uint8_t)m;
+            if (m != MATERIAL_AIR) atomicOr(&words[x >> 5][y], 1u << (x & 31));
+        }
+    }
+    __syncthreads();
+    const int nl = nlist;
+    for (int k = threadIdx.x; k < nl; k += blockDim.x) {
+        const int i = list[k];
         const int y = i / G::FD, x = i - G::FD * y;
         const float dv = dens_h<LVN_DENSITY_CAVES>(nz, dp, hs[x], (float)(x * scale + ox), (float)(y * scale + oy), wz);
         const int m = dv < 0.f ? dm : MATERIAL_AIR;

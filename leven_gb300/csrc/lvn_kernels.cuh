@@ -22,6 +22,7 @@ struct BatchPtrs {
     int need_mats;               // 1: the field kernel writes every byte material (cached fields)
     int num_sms;
     DensityParams density;
+    float cave_band;             // |y - amp2 h| above this: the cave term cannot change the density's sign
     int32_t default_material;
 
     const ChunkDesc* desc;       // [n]

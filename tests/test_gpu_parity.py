@@ -245,6 +245,31 @@ def test_lod_chunk(lvn_gpu, mg):
     compare_mesh(m.vertices, m.triangles, m.seams, ref, 4)
 
 
+def test_cave_field_band(lvn_gpu, mg):
+    """The caves density over chunks from deep underground to open air, LOD0
+    and LOD2.  The field kernel takes a point's material from y - amp2 h
+    alone where the cave term cannot change its sign, and evaluates the cave
+    fBm only inside that band.  Every chunk matches the oracle, and the batch
+    holds chunks wholly below and wholly above the band."""
+    lvn = lvn_gpu
+    lvn.set_density(**W.CAVES)
+    chunks = [((256 * (k % 3), y, 256 * k), 256) for k, y in enumerate((-768, -512, -256, 0, 256, 512))]
+    chunks += [((1024 * k, y, 0), 1024) for k, y in enumerate((-2048, -1024, 0))]
+    V, T, S, res = mg.generate_chunks(chunks)
+    O.set_seed(1)
+    solid = air = 0
+    for c, (mn, size) in enumerate(chunks):
+        ref = O.OracleChunk(oracle_density(2), mn, size, vpc=64)
+        scale = size // 256
+        compare_stages(lvn, mg, c, ref, 64, scale)
+        r = res[c]
+        compare_mesh(V[r[0]:r[0] + r[1]], T[r[2]:r[2] + r[3]], S[r[4]:r[4] + r[5]], ref, scale)
+        mats = ref.materials()
+        solid += bool((mats != AIR).all())
+        air += bool((mats == AIR).all())
+    assert solid >= 1 and air >= 1, (solid, air)
+
+
 def test_empty_chunks(lvn_gpu, mg):
     lvn = lvn_gpu
     lvn.set_density(**W.FBM2D)
