@@ -169,13 +169,16 @@ int upload_perm(int seed) {
         }
     LVN_CK(g.perm.ensure(65536));
     LVN_CK(g.perm_k4.ensure(sizeof(uint16_t) * 65536));
-    // per texel, for snoise3's two chained lookups: the first lookup's column
-    // (alpha, with 255 read as column 0) in the low byte, the second lookup's
-    // gradient index (alpha & 15) in bits 8-11
-    std::vector<uint16_t> ak(65536);
-    for (int t = 0; t < 65536; t++) ak[t] = (uint16_t)((v[t] == 255 ? 0 : v[t]) | ((v[t] & 15) << 8));
-    LVN_CK(g.perm_ak.ensure(sizeof(uint16_t) * 65536));
-    LVN_CK(cudaMemcpy(g.perm_ak.p, ak.data(), sizeof(uint16_t) * 65536, cudaMemcpyHostToDevice));
+    // snoise3's lookup tables (kT3Row x kT3Row texels each, see lvn_types.h)
+    std::vector<uint8_t> t3(kT3Bytes, 0);
+    for (int r = 0; r < kT3Row; r++)
+        for (int c = 0; c < kT3Row; c++) {
+            const uint8_t a = v[(r & 255) * 256 + (c & 255)];
+            t3[r * kT3Row + c] = a == 255 ? 0 : a;
+            t3[kT3Second + r * kT3Row + c] = (uint8_t)((a & 15) * 16);
+        }
+    LVN_CK(g.perm_ak.ensure(kT3Bytes));
+    LVN_CK(cudaMemcpy(g.perm_ak.p, t3.data(), kT3Bytes, cudaMemcpyHostToDevice));
     LVN_CK(g.grad.ensure(sizeof(grad)));
     LVN_CK(cudaMemcpy(g.perm.p, v.data(), 65536, cudaMemcpyHostToDevice));
     LVN_CK(cudaMemcpy(g.perm_k4.p, k4.data(), sizeof(uint16_t) * 65536, cudaMemcpyHostToDevice));
@@ -519,7 +522,7 @@ BatchPtrs make_ptrs(lvn_meshgen* m, int n) {
     b.brushes = m->brushes.as<Brush>();
     b.perm = g.perm.as<uint8_t>();
     b.perm_k4 = g.perm_k4.as<uint16_t>();
-    b.perm_ak = g.perm_ak.as<uint16_t>();
+    b.perm_ak = g.perm_ak.as<uint8_t>();
     b.grad = g.grad.as<float>();
     b.mats = m->mats.as<uint8_t>();
     b.planes = m->planes.as<uint4>();
@@ -1791,7 +1794,7 @@ GlobalView global_view() {
     v.default_material = g.default_material;
     v.perm = g.perm.as<uint8_t>();
     v.perm_k4 = g.perm_k4.as<uint16_t>();
-    v.perm_ak = g.perm_ak.as<uint16_t>();
+    v.perm_ak = g.perm_ak.as<uint8_t>();
     v.grad = g.grad.as<float>();
     v.density = g.density;
     return v;

@@ -67,8 +67,7 @@ __device__ __forceinline__ float2 floor2(float2 a) { return make_float2(floorf(a
 __device__ __forceinline__ float2 max02(float2 a) { return make_float2(fmaxf(a.x, 0.f), fmaxf(a.y, 0.f)); }
 
 struct Noise {
-    const uint16_t* __restrict__ ak;  // per texel: its alpha as the 3D second lookup's column (255 read as
-                                      // column 0) in bits 0-7, alpha & 15 in bits 8-11
+    const uint8_t* __restrict__ t3;   // snoise3's two lookup tables (kT3Row x kT3Row texels each)
     const uint16_t* __restrict__ k4;  // per texel (row j, col i): the 2D gradient indices (alpha & 15) of
                                       // texels (j, i), (j, i+1), (j+1, i), (j+1, i+1), 4 bits each
     const float* __restrict__ g;      // 16 x 4 gradient table, staged in shared memory
@@ -146,14 +145,21 @@ struct Noise {
         return mul2(v2(70.f), add2(add2(n0, n1), n2));
     }
 
-    // one corner of snoise3: the texel (iy, ix)'s alpha picks the column of
-    // the texel in row iz whose alpha & 15 is the gradient index
-    __device__ __forceinline__ float corner3(int ix, int iy, int iz, float x, float y, float z) const {
-        const int a = __ldg(ak + texel(iy, ix)) & 255;  // alpha_column(alpha)
-        const int k = __ldg(ak + texel(iz, a)) >> 8;     // alpha & 15
+    // the gradient of one snoise3 corner: the texel (iy, ix)'s alpha picks the
+    // column of the texel in row iz whose alpha & 15 is the gradient index.
+    // b1 = the first table's index of (iy, ix), b2 = the second table's row
+    // offset of iz (rows and columns in [0, 256], so a corner adds its 0/1
+    // steps without a wrap).
+    __device__ __forceinline__ float4 grad3(int b1, int b2) const {
+        const int a = __ldg(t3 + b1);
+        const int kb = __ldg(t3 + kT3Second + b2 + a);
+        return *reinterpret_cast<const float4*>(reinterpret_cast<const char*>(g) + kb);  // one 16-byte shared load
+    }
+
+    // one corner of snoise3 with its gradient
+    __device__ __forceinline__ float corner3(float4 gk, float x, float y, float z) const {
         float tt = fmaxf(0.6f - dot3(x, y, z, x, y, z), 0.f);  // clamped as in snoise2
         tt = tt * tt;
-        const float4 gk = reinterpret_cast<const float4*>(g)[k];  // one 16-byte shared load
         return (tt * tt) * dot3(gk.x, gk.y, gk.z, x, y, z);
     }
 
@@ -171,28 +177,22 @@ struct Noise {
         const float x0 = px - (pix - t);
         const float y0 = py - (piy - t);
         const float z0 = pz - (piz - t);
-        const int ix = (int)pix, iy = (int)piy, iz = (int)piz;
+        const int b1 = ((int)piy & 255) * kT3Row + ((int)pix & 255), b2 = ((int)piz & 255) * kT3Row;
         // simplex() ranks each axis by its two comparisons (rank 0..2): the
         // second corner steps the axes of rank 2, the third those of rank >= 1,
         // i.e. clamp(rank - 1, 0, 1) = both comparisons, clamp(rank, 0, 1) = either
         const bool xy = x0 >= y0, xz = x0 >= z0, yz = y0 >= z0;
-        const int o1x = xy && xz, o1y = !xy && yz, o1z = !xz && !yz;
-        const int o2x = xy || xz, o2y = !xy || yz, o2z = !xz || !yz;
-        const float n0 = corner3(ix, iy, iz, x0, y0, z0);
-        const float n1 = corner3(ix + o1x, iy + o1y, iz + o1z, (x0 - (float)o1x) + G3, (y0 - (float)o1y) + G3,
-                                 (z0 - (float)o1z) + G3);
-        const float n2 = corner3(ix + o2x, iy + o2y, iz + o2z, (x0 - (float)o2x) + C2, (y0 - (float)o2y) + C2,
-                                 (z0 - (float)o2z) + C2);
-        const float n3 = corner3(ix + 1, iy + 1, iz + 1, x0 - C3, y0 - C3, z0 - C3);
+        const bool o1x = xy && xz, o1y = !xy && yz, o1z = !xz && !yz;
+        const bool o2x = xy || xz, o2y = !xy || yz, o2z = !xz || !yz;
+        const float n0 = corner3(grad3(b1, b2), x0, y0, z0);
+        const float n1 = corner3(grad3(b1 + (o1y ? kT3Row : 0) + o1x, b2 + (o1z ? kT3Row : 0)),
+                                 (x0 - (o1x ? 1.f : 0.f)) + G3, (y0 - (o1y ? 1.f : 0.f)) + G3, (z0 - (o1z ? 1.f : 0.f)) + G3);
+        const float n2 = corner3(grad3(b1 + (o2y ? kT3Row : 0) + o2x, b2 + (o2z ? kT3Row : 0)),
+                                 (x0 - (o2x ? 1.f : 0.f)) + C2, (y0 - (o2y ? 1.f : 0.f)) + C2, (z0 - (o2z ? 1.f : 0.f)) + C2);
+        const float n3 = corner3(grad3(b1 + kT3Row + 1, b2 + kT3Row), x0 - C3, y0 - C3, z0 - C3);
         return 32.f * (((n0 + n1) + n2) + n3);
     }
 
-    // the gradient of one snoise3 corner: two chained lookups
-    __device__ __forceinline__ float4 grad3(int ix, int iy, int iz) const {
-        const int a = __ldg(ak + texel(iy, ix)) & 255;
-        const int k = __ldg(ak + texel(iz, a)) >> 8;
-        return reinterpret_cast<const float4*>(g)[k];
-    }
     // one snoise3 corner at two points, one per lane (corner3's operations)
     __device__ __forceinline__ float2 corner3x2(float4 ga, float4 gb, float2 x, float2 y, float2 z) const {
         float2 tt = max02(sub2(v2(0.6f), fma2(z, z, fma2(y, y, mul2(x, x)))));
@@ -214,25 +214,28 @@ struct Noise {
         const float2 x0 = sub2(px, sub2(pix, t));
         const float2 y0 = sub2(py, sub2(piy, t));
         const float2 z0 = sub2(pz, sub2(piz, t));
-        const int ixa = (int)pix.x, iya = (int)piy.x, iza = (int)piz.x;
-        const int ixb = (int)pix.y, iyb = (int)piy.y, izb = (int)piz.y;
+        const int b1a = ((int)piy.x & 255) * kT3Row + ((int)pix.x & 255), b2a = ((int)piz.x & 255) * kT3Row;
+        const int b1b = ((int)piy.y & 255) * kT3Row + ((int)pix.y & 255), b2b = ((int)piz.y & 255) * kT3Row;
         const bool xya = x0.x >= y0.x, xza = x0.x >= z0.x, yza = y0.x >= z0.x;
         const bool xyb = x0.y >= y0.y, xzb = x0.y >= z0.y, yzb = y0.y >= z0.y;
-        const int o1xa = xya && xza, o1ya = !xya && yza, o1za = !xza && !yza;
-        const int o2xa = xya || xza, o2ya = !xya || yza, o2za = !xza || !yza;
-        const int o1xb = xyb && xzb, o1yb = !xyb && yzb, o1zb = !xzb && !yzb;
-        const int o2xb = xyb || xzb, o2yb = !xyb || yzb, o2zb = !xzb || !yzb;
-        const float2 n0 = corner3x2(grad3(ixa, iya, iza), grad3(ixb, iyb, izb), x0, y0, z0);
-        const float2 n1 = corner3x2(grad3(ixa + o1xa, iya + o1ya, iza + o1za), grad3(ixb + o1xb, iyb + o1yb, izb + o1zb),
-                                    add2(sub2(x0, make_float2((float)o1xa, (float)o1xb)), v2(G3)),
-                                    add2(sub2(y0, make_float2((float)o1ya, (float)o1yb)), v2(G3)),
-                                    add2(sub2(z0, make_float2((float)o1za, (float)o1zb)), v2(G3)));
-        const float2 n2 = corner3x2(grad3(ixa + o2xa, iya + o2ya, iza + o2za), grad3(ixb + o2xb, iyb + o2yb, izb + o2zb),
-                                    add2(sub2(x0, make_float2((float)o2xa, (float)o2xb)), v2(C2)),
-                                    add2(sub2(y0, make_float2((float)o2ya, (float)o2yb)), v2(C2)),
-                                    add2(sub2(z0, make_float2((float)o2za, (float)o2zb)), v2(C2)));
-        const float2 n3 = corner3x2(grad3(ixa + 1, iya + 1, iza + 1), grad3(ixb + 1, iyb + 1, izb + 1), sub2(x0, v2(C3)),
-                                    sub2(y0, v2(C3)), sub2(z0, v2(C3)));
+        const bool o1xa = xya && xza, o1ya = !xya && yza, o1za = !xza && !yza;
+        const bool o2xa = xya || xza, o2ya = !xya || yza, o2za = !xza || !yza;
+        const bool o1xb = xyb && xzb, o1yb = !xyb && yzb, o1zb = !xzb && !yzb;
+        const bool o2xb = xyb || xzb, o2yb = !xyb || yzb, o2zb = !xzb || !yzb;
+        auto f = [](bool o) { return o ? 1.f : 0.f; };
+        const float2 n0 = corner3x2(grad3(b1a, b2a), grad3(b1b, b2b), x0, y0, z0);
+        const float2 n1 = corner3x2(grad3(b1a + (o1ya ? kT3Row : 0) + o1xa, b2a + (o1za ? kT3Row : 0)),
+                                    grad3(b1b + (o1yb ? kT3Row : 0) + o1xb, b2b + (o1zb ? kT3Row : 0)),
+                                    add2(sub2(x0, make_float2(f(o1xa), f(o1xb))), v2(G3)),
+                                    add2(sub2(y0, make_float2(f(o1ya), f(o1yb))), v2(G3)),
+                                    add2(sub2(z0, make_float2(f(o1za), f(o1zb))), v2(G3)));
+        const float2 n2 = corner3x2(grad3(b1a + (o2ya ? kT3Row : 0) + o2xa, b2a + (o2za ? kT3Row : 0)),
+                                    grad3(b1b + (o2yb ? kT3Row : 0) + o2xb, b2b + (o2zb ? kT3Row : 0)),
+                                    add2(sub2(x0, make_float2(f(o2xa), f(o2xb))), v2(C2)),
+                                    add2(sub2(y0, make_float2(f(o2ya), f(o2yb))), v2(C2)),
+                                    add2(sub2(z0, make_float2(f(o2za), f(o2zb))), v2(C2)));
+        const float2 n3 = corner3x2(grad3(b1a + kT3Row + 1, b2a + kT3Row), grad3(b1b + kT3Row + 1, b2b + kT3Row),
+                                    sub2(x0, v2(C3)), sub2(y0, v2(C3)), sub2(z0, v2(C3)));
         return mul2(v2(32.f), add2(add2(add2(n0, n1), n2), n3));
     }
 

@@ -313,7 +313,7 @@ __device__ __forceinline__ float unit(uint64_t h) { return (float)(h >> 40) * (1
 // 70% of the samples within 4 voxels of the heightfield surface (y = amp h +
 // U(-4, 4), so |d| <= 4 for the heightfield), 30% uniform in the domain;
 // target = the plain density.
-__global__ void k_samples(float4* out, int n, uint64_t seed, Domain dom, const uint16_t* perm_ak, const uint16_t* perm_k4,
+__global__ void k_samples(float4* out, int n, uint64_t seed, Domain dom, const uint8_t* perm_ak, const uint16_t* perm_k4,
                           const float* grad, DensityParams dp) {
     __shared__ __align__(16) float sg[64];
     if (threadIdx.x < 64) sg[threadIdx.x] = grad[threadIdx.x];
