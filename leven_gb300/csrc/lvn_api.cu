@@ -97,7 +97,7 @@ struct Global {
     int num_sms = 0;
     int32_t default_material = 0;
     int32_t seed = 0;
-    DevBuf perm, perm_k4, perm_ak, grad;
+    DevBuf perm, perm_t3, grad;
     DensityParams density{LVN_DENSITY_REFERENCE, 8, 1.f / 256.f, 2.f, 0.5f, 48.f, 6, 1.f / 64.f, 2.f, 0.5f, 12.f};
     std::vector<StoredOp> ops;
     std::mt19937 hash_gen;  // default-seeded, drawn in call order (compute_cuckoo.cpp:46-47)
@@ -159,17 +159,8 @@ int upload_perm(int seed) {
         }
         grad[4 * k + 3] = 0.f;
     }
-    // packed gradient indices of texel (j, i) and its wrapped +x, +y, +xy neighbours
-    std::vector<uint16_t> k4(65536);
-    for (int j = 0; j < 256; j++)
-        for (int i = 0; i < 256; i++) {
-            const int i1 = (i + 1) & 255, j1 = (j + 1) & 255;
-            k4[j * 256 + i] = (uint16_t)((v[j * 256 + i] & 15) | ((v[j * 256 + i1] & 15) << 4) |
-                                         ((v[j1 * 256 + i] & 15) << 8) | ((v[j1 * 256 + i1] & 15) << 12));
-        }
     LVN_CK(g.perm.ensure(65536));
-    LVN_CK(g.perm_k4.ensure(sizeof(uint16_t) * 65536));
-    // snoise3's lookup tables (kT3Row x kT3Row texels each, see lvn_types.h)
+    // the simplex lookup tables (kT3Row x kT3Row texels each, see lvn_types.h)
     std::vector<uint8_t> t3(kT3Bytes, 0);
     for (int r = 0; r < kT3Row; r++)
         for (int c = 0; c < kT3Row; c++) {
@@ -177,11 +168,10 @@ int upload_perm(int seed) {
             t3[r * kT3Row + c] = a == 255 ? 0 : a;
             t3[kT3Second + r * kT3Row + c] = (uint8_t)((a & 15) * 16);
         }
-    LVN_CK(g.perm_ak.ensure(kT3Bytes));
-    LVN_CK(cudaMemcpy(g.perm_ak.p, t3.data(), kT3Bytes, cudaMemcpyHostToDevice));
+    LVN_CK(g.perm_t3.ensure(kT3Bytes));
+    LVN_CK(cudaMemcpy(g.perm_t3.p, t3.data(), kT3Bytes, cudaMemcpyHostToDevice));
     LVN_CK(g.grad.ensure(sizeof(grad)));
     LVN_CK(cudaMemcpy(g.perm.p, v.data(), 65536, cudaMemcpyHostToDevice));
-    LVN_CK(cudaMemcpy(g.perm_k4.p, k4.data(), sizeof(uint16_t) * 65536, cudaMemcpyHostToDevice));
     LVN_CK(cudaMemcpy(g.grad.p, grad, sizeof(grad), cudaMemcpyHostToDevice));
     g.seed = seed;
     return LVN_OK;
@@ -521,8 +511,7 @@ BatchPtrs make_ptrs(lvn_meshgen* m, int n) {
     b.bs = m->bs.as<BatchState>();
     b.brushes = m->brushes.as<Brush>();
     b.perm = g.perm.as<uint8_t>();
-    b.perm_k4 = g.perm_k4.as<uint16_t>();
-    b.perm_ak = g.perm_ak.as<uint8_t>();
+    b.perm_t3 = g.perm_t3.as<uint8_t>();
     b.grad = g.grad.as<float>();
     b.mats = m->mats.as<uint8_t>();
     b.planes = m->planes.as<uint4>();
@@ -1327,8 +1316,7 @@ int lvn_initialise(int32_t noise_seed, uint32_t default_material, int32_t num_cs
 
 int lvn_shutdown(void) {
     g.perm.release();
-    g.perm_k4.release();
-    g.perm_ak.release();
+    g.perm_t3.release();
     g.grad.release();
     g.ops.clear();
     g.initialised = false;
@@ -1793,8 +1781,7 @@ GlobalView global_view() {
     v.num_sms = g.num_sms;
     v.default_material = g.default_material;
     v.perm = g.perm.as<uint8_t>();
-    v.perm_k4 = g.perm_k4.as<uint16_t>();
-    v.perm_ak = g.perm_ak.as<uint8_t>();
+    v.perm_t3 = g.perm_t3.as<uint8_t>();
     v.grad = g.grad.as<float>();
     v.density = g.density;
     return v;

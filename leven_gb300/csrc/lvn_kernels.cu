@@ -537,7 +537,7 @@ __global__ void __launch_bounds__(96) k_field(BatchPtrs b) {
     // descriptor fields in registers: the byte stores below may alias them
     const int scale = b.desc[c].scale;
     const int ox = b.desc[c].off[0], oy = b.desc[c].off[1], oz = b.desc[c].off[2];
-    const Noise nz{b.perm_ak, b.perm_k4, sg};
+    const Noise nz{b.perm_t3, sg};
     const DensityParams& dp = b.density;
     const float wx = (float)(x * scale + ox);
     const float wz = (float)(z * scale + oz);
@@ -616,7 +616,7 @@ __global__ void __launch_bounds__(128) k_field_caves(BatchPtrs b) {
     const DensityParams& dp = b.density;
     const float wz = (float)(z * scale + oz);
     __syncthreads();
-    const Noise nz{b.perm_ak, b.perm_k4, sg};
+    const Noise nz{b.perm_t3, sg};
     const int tx = (int)threadIdx.x;  // signed: chunk offsets may be negative
     if (tx < G::FD) {
         const float h = height_m<LVN_DENSITY_CAVES>(nz, dp, (float)(tx * scale + ox), wz);
@@ -718,7 +718,7 @@ __global__ void __launch_bounds__(kProbes) k_probe(BatchPtrs b) {
               iz = (G::FD - 1) * (2 * (p >> 6) + 1) / 16;
     const float wx = (float)(d.off[0] + d.scale * ix), wy = (float)(d.off[1] + d.scale * iy),
                 wz = (float)(d.off[2] + d.scale * iz);
-    const Noise nz{b.perm_ak, b.perm_k4, sg};
+    const Noise nz{b.perm_t3, sg};
     b.probe_pts[(size_t)c * kProbes + p] = make_float4(wx, wy, wz, 0.f);
     b.probe_plain[(size_t)c * kProbes + p] = nz.density(b.density, wx, wy, wz);
 }
@@ -1232,7 +1232,7 @@ __global__ void __launch_bounds__(kThreads) k_hermite(BatchPtrs b) {
     if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
     __syncthreads();
     if (b.bs->overflow) return;
-    const Noise nz{b.perm_ak, b.perm_k4, sg};
+    const Noise nz{b.perm_t3, sg};
     // work list segments: plain x/z edges, plain y edges, CSG-created edges, so
     // that a warp's 32 edges take the same path
     const int nplain = b.bs->total_xz + b.bs->total_y;

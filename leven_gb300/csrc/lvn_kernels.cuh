@@ -31,9 +31,7 @@ struct BatchPtrs {
     const Brush* brushes;        // per-chunk op lists, flattened
 
     const uint8_t* perm;         // 65536 B permutation image (alpha channel)
-    const uint16_t* perm_k4;     // 65536 x 16 bit: the 2D gradient indices of a texel and its +x, +y, +xy
-                                 // neighbours (wrapping), 4 bits each
-    const uint8_t* perm_ak;      // snoise3's two lookup tables, kT3Row x kT3Row texels each (lvn_types.h)
+    const uint8_t* perm_t3;      // the two simplex lookup tables, kT3Row x kT3Row texels each (lvn_types.h)
     const float* grad;           // 16 x 4 gradient table
 
     uint8_t* mats;               // [n][F] field materials, index x + FD*y + FD*FD*z

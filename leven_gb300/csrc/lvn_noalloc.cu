@@ -151,8 +151,7 @@ extern "C" int lvn_generate_chunk_mesh_noalloc(const int32_t min[3], int32_t siz
     b.density = gv.density;
     b.default_material = gv.default_material;
     b.perm = gv.perm;
-    b.perm_k4 = gv.perm_k4;
-    b.perm_ak = gv.perm_ak;
+    b.perm_t3 = gv.perm_t3;
     b.grad = gv.grad;
     b.desc = reinterpret_cast<ChunkDesc*>(base + OFF_DESC);
     b.cs = reinterpret_cast<ChunkState*>(base + OFF_CS);

@@ -22,14 +22,6 @@
 
 namespace lvn {
 
-// Permutation image in the layout the kernels read: v[row*256 + col] is the
-// alpha channel (shuffled permutation value), grad[k] the RGB channel of a
-// texel whose alpha has low nibble k, as read_imagef returns it.
-struct PermTable {
-    const uint8_t* v;   // 65536 bytes, device
-    const float* grad;  // 16 x 4 floats, device (xyz used)
-};
-
 __device__ __forceinline__ int texel(int row, int col) { return ((row & 255) << 8) | (col & 255); }
 __device__ __forceinline__ int alpha_column(int a) { return a == 255 ? 0 : a; }
 
@@ -67,14 +59,19 @@ __device__ __forceinline__ float2 floor2(float2 a) { return make_float2(floorf(a
 __device__ __forceinline__ float2 max02(float2 a) { return make_float2(fmaxf(a.x, 0.f), fmaxf(a.y, 0.f)); }
 
 struct Noise {
-    const uint8_t* __restrict__ t3;   // snoise3's two lookup tables (kT3Row x kT3Row texels each)
-    const uint16_t* __restrict__ k4;  // per texel (row j, col i): the 2D gradient indices (alpha & 15) of
-                                      // texels (j, i), (j, i+1), (j+1, i), (j+1, i+1), 4 bits each
+    const uint8_t* __restrict__ t3;   // the two simplex lookup tables (kT3Row x kT3Row texels each)
     const float* __restrict__ g;      // 16 x 4 gradient table, staged in shared memory
 
+    // the 2D gradient of texel b of the padded tables (row * kT3Row + column):
+    // the second table holds (alpha & 15) * 16, the byte offset of its float4
+    __device__ __forceinline__ float2 grad2(int b) const {
+        const int kb = __ldg(t3 + kT3Second + b);
+        return *reinterpret_cast<const float2*>(reinterpret_cast<const char*>(g) + kb);
+    }
+
     // snoise2 (simplex.cl:158-216).  The three corners' texels are (iy, ix),
-    // (iy, ix+1) or (iy+1, ix) by the x0 > y0 test, and (iy+1, ix+1): one
-    // 16-bit load holds all their gradient indices.
+    // (iy, ix+1) or (iy+1, ix) by the x0 > y0 test, and (iy+1, ix+1), read
+    // from the padded table without a wrap.
     __device__ __forceinline__ float snoise2(float px, float py) const {
         const float F2 = 0.366025403784f;
         const float G2 = 0.211324865405f;
@@ -85,19 +82,14 @@ struct Noise {
         const float t = (pix + piy) * G2;
         const float x0 = px - (pix - t);
         const float y0 = py - (piy - t);
-        const int ix = (int)pix, iy = (int)piy;
         const bool xgt = x0 > y0;
-        const unsigned q = __ldg(k4 + (((iy & 255) << 8) | (ix & 255)));
-        const int k0 = q & 15;
-        const int k1 = (q >> (xgt ? 4 : 8)) & 15;
-        const int kk2 = q >> 12;
-        const float2* g2 = reinterpret_cast<const float2*>(g);
+        const int b = ((int)piy & 255) * kT3Row + ((int)pix & 255);
 
         // A corner outside the kernel radius (t < 0) contributes 0.  Clamping
         // t to 0 instead of branching gives 0 * dot = +-0 there, and a signed
         // zero term leaves every sum below unchanged: the fractals accumulate
         // with fma(s, amplitude, acc) and the ridged one takes |s| first.
-        const float2 ga = g2[2 * k0], gb = g2[2 * k1], gc = g2[2 * kk2];
+        const float2 ga = grad2(b), gb = grad2(b + (xgt ? 1 : kT3Row)), gc = grad2(b + kT3Row + 1);
         float t0 = fmaxf(0.5f - dot2(x0, y0, x0, y0), 0.f);
         t0 = t0 * t0;
         const float n0 = (t0 * t0) * dot2(ga.x, ga.y, x0, y0);
@@ -124,11 +116,10 @@ struct Noise {
         const float2 x0 = sub2(px, sub2(pix, t));
         const float2 y0 = sub2(py, sub2(piy, t));
         const bool xg0 = x0.x > y0.x, xg1 = x0.y > y0.y;
-        const unsigned qa = __ldg(k4 + ((((int)piy.x & 255) << 8) | ((int)pix.x & 255)));
-        const unsigned qb = __ldg(k4 + ((((int)piy.y & 255) << 8) | ((int)pix.y & 255)));
-        const float2* g2 = reinterpret_cast<const float2*>(g);
-        const float2 ga0 = g2[2 * (qa & 15)], gb0 = g2[2 * ((qa >> (xg0 ? 4 : 8)) & 15)], gc0 = g2[2 * (qa >> 12)];
-        const float2 ga1 = g2[2 * (qb & 15)], gb1 = g2[2 * ((qb >> (xg1 ? 4 : 8)) & 15)], gc1 = g2[2 * (qb >> 12)];
+        const int ba = ((int)piy.x & 255) * kT3Row + ((int)pix.x & 255);
+        const int bb = ((int)piy.y & 255) * kT3Row + ((int)pix.y & 255);
+        const float2 ga0 = grad2(ba), gb0 = grad2(ba + (xg0 ? 1 : kT3Row)), gc0 = grad2(ba + kT3Row + 1);
+        const float2 ga1 = grad2(bb), gb1 = grad2(bb + (xg1 ? 1 : kT3Row)), gc1 = grad2(bb + kT3Row + 1);
 
         float2 t0 = max02(sub2(v2(0.5f), fma2(y0, y0, mul2(x0, x0))));
         t0 = mul2(t0, t0);

@@ -12,8 +12,7 @@ struct GlobalView {
     int num_sms;
     int32_t default_material;
     const uint8_t* perm;   // device permutation image (65536 B)
-    const uint16_t* perm_k4;  // device packed 2D gradient indices per texel (65536 x 16 bit)
-    const uint8_t* perm_ak;   // device: snoise3's two lookup tables (kT3Row x kT3Row texels each)
+    const uint8_t* perm_t3;   // device: the two simplex lookup tables (kT3Row x kT3Row texels each)
     const float* grad;     // device gradient table (16 x 4)
     DensityParams density;
 };

@@ -313,12 +313,12 @@ __device__ __forceinline__ float unit(uint64_t h) { return (float)(h >> 40) * (1
 // 70% of the samples within 4 voxels of the heightfield surface (y = amp h +
 // U(-4, 4), so |d| <= 4 for the heightfield), 30% uniform in the domain;
 // target = the plain density.
-__global__ void k_samples(float4* out, int n, uint64_t seed, Domain dom, const uint8_t* perm_ak, const uint16_t* perm_k4,
+__global__ void k_samples(float4* out, int n, uint64_t seed, Domain dom, const uint8_t* perm_t3,
                           const float* grad, DensityParams dp) {
     __shared__ __align__(16) float sg[64];
     if (threadIdx.x < 64) sg[threadIdx.x] = grad[threadIdx.x];
     __syncthreads();
-    const Noise nz{perm_ak, perm_k4, sg};
+    const Noise nz{perm_t3, sg};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint64_t h0 = mix64(seed ^ mix64((uint64_t)i * 4 + 0)), h1 = mix64(seed ^ mix64((uint64_t)i * 4 + 1));
         const uint64_t h2 = mix64(seed ^ mix64((uint64_t)i * 4 + 2)), h3 = mix64(seed ^ mix64((uint64_t)i * 4 + 3));
@@ -1037,7 +1037,7 @@ int lvn_surrogate_sample(lvn_surrogate* s, int64_t n, uint64_t seed, float* host
     if (!gv.initialised) return LVN_ERR_NOT_INITIALISED;
     int rc = s->pool.ensure(sizeof(float4) * (size_t)n);
     if (rc) return rc;
-    k_samples<<<gv.num_sms * 8, 256, 0, s->stream>>>(s->pool.as<float4>(), (int)n, seed, s->dom, gv.perm_ak, gv.perm_k4,
+    k_samples<<<gv.num_sms * 8, 256, 0, s->stream>>>(s->pool.as<float4>(), (int)n, seed, s->dom, gv.perm_t3,
                                                      gv.grad, gv.density);
     SG_CK(cudaGetLastError());
     s->pool_n = n;

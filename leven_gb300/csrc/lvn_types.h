@@ -23,12 +23,13 @@ constexpr uint32_t CUCKOO_MIN_TABLE_SIZE = 2048u;  // compute_cuckoo.cpp:15
 
 typedef lvn_density_params DensityParams;
 
-// snoise3's two chained permutation lookups as two byte tables of 257 x 257
+// The simplex noise permutation lookups as two byte tables of 257 x 257
 // texels: row r, column c holds texel (r & 255, c & 255), so a corner's +x, +y
-// or +z neighbour needs no wrap.  The first table holds the first lookup's
-// result (the alpha read as a column, 255 as 0); the second, from byte
-// kT3Second, the second lookup's gradient as a byte offset ((alpha & 15) * 16)
-// into the 16 x float4 gradient table.
+// or +z neighbour needs no wrap.  The first table holds snoise3's first
+// lookup's result (the alpha read as a column, 255 as 0).  The second, from
+// byte kT3Second, holds a texel's gradient as a byte offset ((alpha & 15) * 16)
+// into the 16 x float4 gradient table: snoise3's second lookup and snoise2's
+// three corners read it.
 constexpr int kT3Row = 257;
 constexpr int kT3Second = 66064;  // 257 * 257 rounded up to 16 bytes
 constexpr int kT3Bytes = 2 * kT3Second;
