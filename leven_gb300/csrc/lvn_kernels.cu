@@ -547,7 +547,6 @@ __global__ void __launch_bounds__(96) k_field(BatchPtrs b) {
     const bool write_mats = b.need_mats != 0;
     uint8_t* mats = b.mats + (size_t)c * G::F + x + G::FD * G::FD * z;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    uint32_t pw = 0;  // lane l keeps the ballot of row (y & ~31) + l
     static_assert(MODE != LVN_DENSITY_CAVES, "a density with a 3D term uses k_field_caves");
     // y - amp * h rounds monotonically in y, so the column is solid below
     // the first y whose density is >= 0 and air from there up
@@ -561,15 +560,27 @@ __global__ void __launch_bounds__(96) k_field(BatchPtrs b) {
         }
         ycross = lo;
     }
-    for (int y = 0; y < G::FD; y++) {
-        const bool solid = y < ycross;
-        if (valid && write_mats) mats[G::FD * y] = (uint8_t)(solid ? dm : MATERIAL_AIR);
-        const unsigned sb = __ballot_sync(FULL, solid);
-        pw = (y & 31) == lane ? sb : pw;
-        if ((y & 31) == 31 || y == G::FD - 1) {
-            const int yy = (y & ~31) + lane;
-            if (yy <= y) words[warp][yy] = pw;
+    if (valid && write_mats)
+        for (int y = 0; y < G::FD; y++) mats[G::FD * y] = (uint8_t)(y < ycross ? dm : MATERIAL_AIR);
+    // the warp's row words: every valid column is solid below the warp's
+    // lowest crossing and air from its highest up, so only the rows between
+    // need a ballot.  Lane l keeps rows l, l + 32 and l + 64.
+    const unsigned vmask = __ballot_sync(FULL, valid);
+    const int ymin = __reduce_min_sync(FULL, valid ? ycross : G::FD);
+    const int ymax = __reduce_max_sync(FULL, valid ? ycross : 0);
+    uint32_t w0 = 0, w1 = 0, w2 = 0;
+    for (int y = ymin; y < ymax; y++) {
+        const unsigned sb = __ballot_sync(FULL, y < ycross);
+        if ((y & 31) == lane) {
+            w0 = y < 32 ? sb : w0;
+            w1 = y >= 32 && y < 64 ? sb : w1;
+            w2 = y >= 64 ? sb : w2;
         }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const int y = lane + 32 * k;
+        if (y < G::FD) words[warp][y] = y < ymin ? vmask : y >= ymax ? 0u : k == 0 ? w0 : k == 1 ? w1 : w2;
     }
     __syncthreads();
     // one thread per row writes the three 16-byte plane rows
@@ -734,8 +745,12 @@ __global__ void __launch_bounds__(kProbes) k_gate(BatchPtrs b) {
     if (p == 0) b.gate_ok[c] = bad ? 0 : 1;
 }
 
+// One CTA per (z slice, chunk): 96 threads along x (three warps, one per
+// plane word) times kCsgRows rows of y taken together.
+constexpr int kCsgRows = 8;
+
 template <int VPC>
-__global__ void __launch_bounds__(96) k_csg(BatchPtrs b) {
+__global__ void __launch_bounds__(96 * kCsgRows) k_csg(BatchPtrs b) {
     using G = Geo<VPC>;
     const int c = blockIdx.y, z = blockIdx.x;
     const ChunkDesc d = b.desc[c];  // a copy: the byte stores below may alias the descriptor
@@ -750,7 +765,7 @@ __global__ void __launch_bounds__(96) k_csg(BatchPtrs b) {
     uint32_t* X = reinterpret_cast<uint32_t*>(plane_ptr<VPC>(b, c, 2) + G::FD * z);
     const float wx = (float)(d.off[0] + d.scale * x);
     const float wz = (float)(d.off[2] + d.scale * z);
-    for (int y = d.csg_lo[1]; y <= d.csg_hi[1]; y++) {
+    for (int y = d.csg_lo[1] + (int)threadIdx.y; y <= d.csg_hi[1]; y += kCsgRows) {  // uniform per warp
         bool air = false, changed = false;
         if (x < G::FD) {
             // a fresh field's materials are the default or AIR, given by its
@@ -2221,7 +2236,7 @@ cudaError_t launch_gate(const BatchPtrs& b, cudaStream_t s) {
 
 cudaError_t launch_csg(const BatchPtrs& b, cudaStream_t s) {
     dim3 grid(b.vpc + 2, b.n);
-    LVN_VPC_DISPATCH(b.vpc, (k_csg<V><<<grid, 96, 0, s>>>(b)));
+    LVN_VPC_DISPATCH(b.vpc, (k_csg<V><<<grid, dim3(96, kCsgRows), 0, s>>>(b)));
     return cudaGetLastError();
 }
 
