@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "lvn_kernels.cuh"
+#include "lvn_state.h"
 
 using namespace lvn;
 
@@ -466,30 +467,6 @@ std::array<int, 4> tune_key(const lvn_meshgen* m, int n) {
     return {g.density.mode, m->crossing_mode, m->simp_threshold >= 0.f ? 1 : 0, bucket};
 }
 
-// A bound on |amp3 * fbm3| as the kernels compute it, for the cave density
-// (0 for the heightfield densities, which have no 3D term).
-// |snoise3| <= 1.2972: each of a point's four simplex corners adds at most
-// (0.6 - r^2)^4 r |g| to the sum before the factor 32, with |g| <= 1.42532 for
-// the gradient table; the corners are among the lattice points within
-// sqrt(0.6) of the point, and the largest sum of (0.6 - r^2)^4 r over those
-// lattice points, over a 200^3 grid of one skewed cell, is 0.025074, plus
-// 0.003367 for the grid spacing (6 lattice points in range, each changing by at
-// most 0.6^4 per unit of distance).  32 * 1.42532 * 0.028441 = 1.2972.  fbm3
-// sums the octaves scaled by amplitudes 1, gain3, gain3^2, ...; the 0.1% on
-// top covers single-precision rounding of those sums and products.
-float cave_band(const DensityParams& d) {
-    if (d.mode != LVN_DENSITY_CAVES) return 0.f;
-    double sum = 0.0;
-    float a = 1.f;
-    for (int i = 0; i < d.octaves3; i++) {
-        sum += std::fabs((double)a);
-        a = a * d.gain3;
-    }
-    const double band = std::fabs((double)d.amp3) * 1.2972 * sum * 1.001;
-    if (!(band < 1e30)) return INFINITY;  // non-finite parameters: every point is evaluated
-    return std::nextafter((float)band, INFINITY);
-}
-
 BatchPtrs make_ptrs(lvn_meshgen* m, int n) {
     BatchPtrs b;
     std::memset(&b, 0, sizeof(b));
@@ -504,8 +481,8 @@ BatchPtrs make_ptrs(lvn_meshgen* m, int n) {
     b.need_mats = 0;
     b.num_sms = g.num_sms;
     b.density = g.density;
-    b.cave_band = cave_band(g.density);
     b.default_material = g.default_material;
+    density_fields(g.density, g.default_material, &b.cave_band, b.dom_by_solid);
     b.desc = m->desc.as<ChunkDesc>();
     b.cs = m->cs.as<ChunkState>();
     b.bs = m->bs.as<BatchState>();
@@ -1774,6 +1751,39 @@ int64_t lvn_meshgen_debug_fetch(lvn_meshgen* m, int32_t what, int32_t chunk, voi
 #include "lvn_state.h"
 
 namespace lvn {
+
+// A bound on |amp3 * fbm3| as the kernels compute it, for the cave density
+// (0 for the heightfield densities, which have no 3D term).
+// |snoise3| <= 1.2972: each of a point's four simplex corners adds at most
+// (0.6 - r^2)^4 r |g| to the sum before the factor 32, with |g| <= 1.42532 for
+// the gradient table; the corners are among the lattice points within
+// sqrt(0.6) of the point, and the largest sum of (0.6 - r^2)^4 r over those
+// lattice points, over a 200^3 grid of one skewed cell, is 0.025074, plus
+// 0.003367 for the grid spacing (6 lattice points in range, each changing by at
+// most 0.6^4 per unit of distance).  32 * 1.42532 * 0.028441 = 1.2972.  fbm3
+// sums the octaves scaled by amplitudes 1, gain3, gain3^2, ...; the 0.1% on
+// top covers single-precision rounding of those sums and products.
+static float cave_band(const DensityParams& d) {
+    if (d.mode != LVN_DENSITY_CAVES) return 0.f;
+    double sum = 0.0;
+    float a = 1.f;
+    for (int i = 0; i < d.octaves3; i++) {
+        sum += std::fabs((double)a);
+        a = a * d.gain3;
+    }
+    const double band = std::fabs((double)d.amp3) * 1.2972 * sum * 1.001;
+    if (!(band < 1e30)) return INFINITY;  // non-finite parameters: every point is evaluated
+    return std::nextafter((float)band, INFINITY);
+}
+
+void density_fields(const DensityParams& d, int32_t default_material, float* band, int32_t dom_by_solid[9]) {
+    *band = cave_band(d);
+    for (int n = 0; n <= 8; n++) {
+        int mats[8];
+        for (int i = 0; i < 8; i++) mats[i] = i < n ? default_material : MATERIAL_AIR;
+        dom_by_solid[n] = dominant_material(mats);
+    }
+}
 
 GlobalView global_view() {
     GlobalView v;

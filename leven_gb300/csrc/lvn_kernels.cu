@@ -1270,32 +1270,6 @@ __global__ void __launch_bounds__(kThreads) k_hermite(BatchPtrs b) {
 // one thread per voxel row (y, z) over the final-air plane.
 // ---------------------------------------------------------------------------
 
-// FindDominantMaterial (octree.cl:96-138)
-__device__ __forceinline__ int dominant_material(int (&m)[8]) {
-#pragma unroll
-    for (int i = 1; i < 8; i++) {
-        const int tmp = m[i];
-        int j = i;
-        for (; j >= 1 && tmp < m[j - 1]; j--) m[j] = m[j - 1];
-        m[j] = tmp;
-    }
-    int current = m[0], count = 1, max_count = 0, max_material = 0;
-#pragma unroll
-    for (int i = 1; i < 8; i++) {
-        const int v = m[i];
-        if (v == MATERIAL_AIR || v == MATERIAL_NONE) continue;
-        if (current != v) {
-            if (count > max_count) { max_count = count; max_material = current; }
-            current = v;
-            count = 1;
-        } else {
-            count++;
-        }
-    }
-    if (count > max_count) max_material = current;
-    return max_material;
-}
-
 struct VoxRow {
     uint4 s[4];    // solid rows (y,z), (y,z+1), (y+1,z), (y+1,z+1): corner bits i & 3
     uint4 active;
@@ -1425,16 +1399,10 @@ __global__ void __launch_bounds__(kThreads) k_vox_scatter(BatchPtrs b) {
         const int y = row % VPC, z = row / VPC;
         const int r = y + G::FD * z;
         int corners = 0;
-        int m[8];
 #pragma unroll
         for (int i = 0; i < 8; i++) {
             const int dx = i >> 2, dy = (i >> 1) & 1, dz = i & 1;
-            const bool air = bit4(A[r + dy + G::FD * dz], x + dx);
-            corners |= (air ? 0 : 1) << i;
-            // a fresh field holds byte materials only inside its CSG box
-            const int cx = x + dx, cy = y + dy, cz = z + dz;
-            const bool in_box = has_ops && cx >= bx0 && cx <= bx1 && cy >= by0 && cy <= by1 && cz >= bz0 && cz <= bz1;
-            m[i] = (fresh && !in_box) ? (air ? MATERIAL_AIR : dm) : mats[cx + G::FD * cy + G::FD * G::FD * cz];
+            corners |= (bit4(A[r + dy + G::FD * dz], x + dx) ? 0 : 1) << i;
         }
         int edges = 0;
 #pragma unroll
@@ -1442,7 +1410,27 @@ __global__ void __launch_bounds__(kThreads) k_vox_scatter(BatchPtrs b) {
             const int s0 = (corners >> edge_c0(i)) & 1, s1 = (corners >> edge_c1(i)) & 1;
             edges |= (s0 != s1 ? 1 : 0) << i;
         }
-        const int dom = dominant_material(m);
+        // a fresh field holds byte materials only inside its CSG box; a voxel
+        // with every corner outside it has the default material at its solid
+        // corners and AIR at the others, whose dominant material depends on
+        // the solid count alone
+        const bool outside = !has_ops || x + 1 < bx0 || x > bx1 || y + 1 < by0 || y > by1 || z + 1 < bz0 || z > bz1;
+        int dom;
+        if (fresh && outside) {
+            dom = b.dom_by_solid[__popc(corners)];
+        } else {
+            int m[8];
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const int dx = i >> 2, dy = (i >> 1) & 1, dz = i & 1;
+                const int cx = x + dx, cy = y + dy, cz = z + dz;
+                const bool in_box =
+                    has_ops && cx >= bx0 && cx <= bx1 && cy >= by0 && cy <= by1 && cz >= bz0 && cz <= bz1;
+                m[i] = (fresh && !in_box) ? (((corners >> i) & 1) ? dm : MATERIAL_AIR)
+                                          : mats[cx + G::FD * cy + G::FD * G::FD * cz];
+            }
+            dom = dominant_material(m);
+        }
         const int pos = base + j;
         b.node_codes[pos] = code_for_position<VPC>(x, y, z);
         b.node_info[pos] = (edges << 16) | (dom << 8) | corners;

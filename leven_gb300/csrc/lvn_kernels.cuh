@@ -24,6 +24,7 @@ struct BatchPtrs {
     DensityParams density;
     float cave_band;             // |y - amp2 h| above this: the cave term cannot change the density's sign
     int32_t default_material;
+    int32_t dom_by_solid[9];     // dominant material of 8 corners, n of them the default material, the rest AIR
 
     const ChunkDesc* desc;       // [n]
     ChunkState* cs;              // [n]

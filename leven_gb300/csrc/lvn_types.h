@@ -9,6 +9,43 @@ namespace lvn {
 
 constexpr int MATERIAL_NONE = 200;  // leven/src/volume_materials.h:7
 constexpr int MATERIAL_AIR = 201;   // leven/src/volume_materials.h:8
+
+#ifdef __CUDACC__
+#define LVN_HD __host__ __device__
+#else
+#define LVN_HD
+#endif
+
+// FindDominantMaterial (octree.cl:96-138): the most frequent material of a
+// voxel's 8 corners after sorting them, AIR and NONE not counted as a run's
+// continuation, the first of equal counts kept.
+LVN_HD inline int dominant_material(int (&m)[8]) {
+#pragma unroll
+    for (int i = 1; i < 8; i++) {
+        const int tmp = m[i];
+        int j = i;
+        for (; j >= 1 && tmp < m[j - 1]; j--) m[j] = m[j - 1];
+        m[j] = tmp;
+    }
+    int current = m[0], count = 1, max_count = 0, max_material = 0;
+#pragma unroll
+    for (int i = 1; i < 8; i++) {
+        const int v = m[i];
+        if (v == MATERIAL_AIR || v == MATERIAL_NONE) continue;
+        if (current != v) {
+            if (count > max_count) {
+                max_count = count;
+                max_material = current;
+            }
+            current = v;
+            count = 1;
+        } else {
+            count++;
+        }
+    }
+    if (count > max_count) max_material = current;
+    return max_material;
+}
 constexpr int LEAF_SIZE_SCALE = 4;  // leven/src/volume_constants.h:7-8
 constexpr int CLIPMAP_LEAF_SIZE = 256;  // volume_constants.h:15
 

@@ -64,6 +64,28 @@ def test_noalloc_matches_generate_chunk_mesh(lvn_gpu):
         lvn.clear_csg_operations()
 
 
+def test_noalloc_caves_density(lvn_gpu):
+    """The caves density (a 3D term): the field kernel's cave band and the
+    batch fields derived from the density are set on this path too."""
+    lvn = lvn_gpu
+    lvn.set_density(**W.CAVES)
+    lvn.clear_csg_operations()
+    mg = lvn.MeshGen(64)
+    try:
+        mg.set_option(lvn.LVN_OPT_CACHE, 0)
+        for mn, size in (((0, 0, 0), 256), ((1024, -1024, 0), 1024)):
+            ref = mg.generate_chunk_mesh(mn, size)
+            v, t, s = noalloc_mesh(lvn, mn, size, 64)
+            assert ref.vertices.shape[0] > 0
+            assert v.shape == ref.vertices.shape and t.shape == ref.triangles.shape and s.shape == ref.seams.shape
+            assert np.array_equal(v.view(np.int32), ref.vertices.view(np.int32))
+            assert np.array_equal(t, ref.triangles)
+            assert np.array_equal(s, ref.seams)
+    finally:
+        mg.close()
+        lvn.set_density(**W.FBM2D)
+
+
 def test_noalloc_rejects_out_of_range(lvn_gpu):
     lvn = lvn_gpu
     out = lvn_mod.MeshOut()
