@@ -1035,35 +1035,46 @@ __global__ void __launch_bounds__(kThreads) k_edge_scatter(BatchPtrs b) {
     int wy = bs.total_xz + st.wl_y_off + toff.y + ey;
     int wc = bs.total_xz + bs.total_y + st.wl_c_off + toff.z + exc;
     const int y = row % G::FD, z = row / G::FD;
-    // emit in (x, axis) order: the reference's (hermite index, axis) order
-    uint4 any = or4(or4(e.kept[0], e.kept[1]), e.kept[2]);
-    while (popc4(any)) {
-        const int x = any.x ? __ffs(any.x) - 1 : any.y ? 31 + __ffs(any.y) : any.z ? 63 + __ffs(any.z) : 95 + __ffs(any.w);
+    // emit in (x, axis) order, the reference's (hermite index, axis) order:
+    // word by word (x = 32 w + bit), lowest set bit first
+    static_assert(G::FD <= 96, "a field row spans at most three 32-bit words");
+    auto word = [](const uint4& u, int w) { return w == 0 ? u.x : w == 1 ? u.y : u.z; };
 #pragma unroll
-        for (int a = 0; a < 3; a++) {
-            if (bit4(e.kept[a], x)) {
-                b.edge_keys[pp] = edge_key<VPC>(x, y, z, a);
+    for (int w = 0; w < 3; w++) {
+        const uint32_t k0 = word(e.kept[0], w), k1 = word(e.kept[1], w), k2 = word(e.kept[2], w);
+        for (uint32_t any = k0 | k1 | k2; any; any &= any - 1) {
+            const int bit = __ffs(any) - 1, x = 32 * w + bit;
+            if ((k0 >> bit) & 1) {
+                b.edge_keys[pp] = edge_key<VPC>(x, y, z, 0);
                 b.edge_chunk[pp] = c;
-                if (a == 1) b.edge_work[wy++] = pp;
-                else b.edge_work[wxz++] = pp;
-                pp++;
+                b.edge_work[wxz++] = pp++;
+            }
+            if ((k1 >> bit) & 1) {
+                b.edge_keys[pp] = edge_key<VPC>(x, y, z, 1);
+                b.edge_chunk[pp] = c;
+                b.edge_work[wy++] = pp++;
+            }
+            if ((k2 >> bit) & 1) {
+                b.edge_keys[pp] = edge_key<VPC>(x, y, z, 2);
+                b.edge_chunk[pp] = c;
+                b.edge_work[wxz++] = pp++;
             }
         }
-        any = and4(any, not4(low_bits(x + 1)));
     }
-    any = or4(or4(e.created[0], e.created[1]), e.created[2]);
-    while (popc4(any)) {
-        const int x = any.x ? __ffs(any.x) - 1 : any.y ? 31 + __ffs(any.y) : any.z ? 63 + __ffs(any.z) : 95 + __ffs(any.w);
 #pragma unroll
-        for (int a = 0; a < 3; a++) {
-            if (bit4(e.created[a], x)) {
-                b.edge_keys[pc] = edge_key<VPC>(x, y, z, a);
-                b.edge_chunk[pc] = c;
-                b.edge_work[wc++] = pc;
-                pc++;
+    for (int w = 0; w < 3; w++) {
+        const uint32_t c0 = word(e.created[0], w), c1 = word(e.created[1], w), c2 = word(e.created[2], w);
+        for (uint32_t any = c0 | c1 | c2; any; any &= any - 1) {
+            const int bit = __ffs(any) - 1, x = 32 * w + bit;
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                if (((a == 0 ? c0 : a == 1 ? c1 : c2) >> bit) & 1) {
+                    b.edge_keys[pc] = edge_key<VPC>(x, y, z, a);
+                    b.edge_chunk[pc] = c;
+                    b.edge_work[wc++] = pc++;
+                }
             }
         }
-        any = and4(any, not4(low_bits(x + 1)));
     }
 }
 
@@ -1654,7 +1665,12 @@ __global__ void __launch_bounds__(kNodeTile) k_mesh_count(BatchPtrs b) {
             for (int axis = 0; axis < 3; axis++) {
                 int4 q = make_int4(-1, -1, -1, 0);
                 const int aa = pos[(axis + 1) % 3], bb = pos[(axis + 2) % 3];
-                if (aa != VPC - 1 && bb != VPC - 1) {
+                // ProcessEdge (octree.cl:335-372): a quad needs the edge's sign
+                // change and all three neighbours; the sign is tested first, so
+                // that the neighbour lookups run only for the edges it passes
+                const int edge = axis * 4 + 3;
+                const int m1 = (corners >> edge_c0(edge)) & 1, m2 = (corners >> edge_c1(edge)) & 1;
+                if (aa != VPC - 1 && bb != VPC - 1 && m1 != m2) {
                     // EDGE_NODE_OFFSETS (octree.cl:376-381)
                     int nb[3];
 #pragma unroll
@@ -1666,13 +1682,8 @@ __global__ void __launch_bounds__(kNodeTile) k_mesh_count(BatchPtrs b) {
                         nb[k - 1] = (int)hv.find(code_for_position<VPC>(pos[0] + ox, pos[1] + oy, pos[2] + oz));
                     }
                     if (nb[0] != -1 && nb[1] != -1 && nb[2] != -1) {
-                        // ProcessEdge (octree.cl:335-372)
-                        const int edge = axis * 4 + 3;
-                        const int m1 = (corners >> edge_c0(edge)) & 1, m2 = (corners >> edge_c1(edge)) & 1;
-                        if (m1 != m2) {
-                            q = make_int4(nb[0], nb[1], nb[2], 1 | (m1 != 0 ? 2 : 0));
-                            quads++;
-                        }
+                        q = make_int4(nb[0], nb[1], nb[2], 1 | (m1 != 0 ? 2 : 0));
+                        quads++;
                     }
                 }
                 b.quad_scratch[3 * (size_t)i + axis] = q;
