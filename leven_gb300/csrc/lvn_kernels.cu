@@ -1747,16 +1747,21 @@ __global__ void __launch_bounds__(kNodeTile) k_mesh_scatter(BatchPtrs b) {
         const int local = (vt - b.chunk_tile_off[c]) * kNodeTile + threadIdx.x;
         const bool valid = local < st.nodes;
         const int i = st.node_off + local;
-        int4 q[3];
+        // the scan packs quads (low 16 bits) and seams (high 16 bits), whose
+        // prefixes are independent, so a pass reads only what it writes:
+        // scatter_what 1 = triangles, 2 = seams, 0 = both
+        int4 q[3] = {make_int4(0, 0, 0, 0), make_int4(0, 0, 0, 0), make_int4(0, 0, 0, 0)};
         int quads = 0;
         bool seam = false;
         int pos[3] = {0, 0, 0};
-        if (valid) {
+        if (valid && b.scatter_what != 2) {
 #pragma unroll
             for (int a = 0; a < 3; a++) {
                 q[a] = b.quad_scratch[3 * (size_t)i + a];
                 quads += q[a].w & 1;
             }
+        }
+        if (valid && b.scatter_what != 1) {
             position_for_code<VPC>(b.node_codes[i], pos[0], pos[1], pos[2]);
             seam = pos[0] == 0 || pos[0] == VPC - 1 || pos[1] == 0 || pos[1] == VPC - 1 || pos[2] == 0 ||
                    pos[2] == VPC - 1;
