@@ -1501,7 +1501,7 @@ __global__ void __launch_bounds__(kThreads) k_node_insert(BatchPtrs b) {
 
 // CreateLeafNodes + SolveQEFs + GenerateMeshVertexBuffer (octree.cl:236-331, 475-487)
 template <int VPC>
-__global__ void __launch_bounds__(kThreads) k_leaf(BatchPtrs b) {
+__global__ void __launch_bounds__(kThreads, 4) k_leaf(BatchPtrs b) {
     if (b.bs->overflow) return;
     const int total = b.bs->total_nodes;
     int lo = 0, hi = total;
