@@ -609,9 +609,11 @@ constexpr int kLeafSlices = 4;  // leaf / vertex-export pipeline depth for pinne
 //   || voxels, primes, hash-table fill                           (stream)
 //      -> leaf-hash insert, quads, triangles                     (aux2)
 //         [pinned outputs: triangles exported on aux2]
-//      || edge-hash insert, join hermite, leaves in slices       (stream)
-//         [pinned outputs: each slice's vertices exported on the side
-//          stream while the next is computed]
+//      || edge-hash insert, join hermite, leaves                 (stream)
+//         [pinned outputs: the leaves write their vertices to the host
+//          array as they are made; an unaligned array instead gets the
+//          leaves in slices, each exported on the side stream while the
+//          next is computed]
 //   -> join -> seams, simplification, exports' join              (stream)
 // No branch reads what another writes before their join: the chain beside
 // hermite reads edge keys, not edge information; the quad chain reads leaf
@@ -656,13 +658,21 @@ int enqueue_fresh_dag(lvn_meshgen* m, const BatchPtrs& b, bool any_ops, const Di
     // the leaves
     LVN_CK(launch_edge_insert(b, s0));
     LVN_CK(cudaStreamWaitEvent(s0, m->ev_herm, 0));
-    const int slices = pipelined ? kLeafSlices : 1;
+    // pinned host vertices: k_leaf writes them itself when the array is
+    // 16-byte aligned; otherwise the leaves run in slices, each exported on
+    // the side stream while the next is computed
+    const bool fused = pipelined && (reinterpret_cast<uintptr_t>(direct->dst[0]) & 15) == 0;
+    const int slices = pipelined && !fused ? kLeafSlices : 1;
     for (int sl = 0; sl < slices; sl++) {
         BatchPtrs bl = b;
         bl.slice = sl;
         bl.nslices = slices;
+        if (fused) {
+            bl.host_vertices = static_cast<float4*>(direct->dst[0]);
+            bl.host_vertex_cap = direct->cap[0];
+        }
         LVN_CK(launch_leaf(bl, s0));
-        if (pipelined) {
+        if (pipelined && !fused) {
             LVN_CK(cudaEventRecord(m->ev_leaf, s0));
             LVN_CK(cudaStreamWaitEvent(m->side, m->ev_leaf, 0));
             LVN_CK(launch_export(bl, 0, direct->dst[0], direct->cap[0], m->side));
@@ -679,8 +689,10 @@ int enqueue_fresh_dag(lvn_meshgen* m, const BatchPtrs& b, bool any_ops, const Di
             if (rc) return rc;
         } else {
             LVN_CK(launch_export(b, 2, direct->dst[2], direct->cap[2], s0));
-            LVN_CK(cudaEventRecord(m->ev_side, m->side));
-            LVN_CK(cudaStreamWaitEvent(s0, m->ev_side, 0));
+            if (!fused) {  // the side stream joined the DAG only for the sliced exports
+                LVN_CK(cudaEventRecord(m->ev_side, m->side));
+                LVN_CK(cudaStreamWaitEvent(s0, m->ev_side, 0));
+            }
         }
     }
     return LVN_OK;

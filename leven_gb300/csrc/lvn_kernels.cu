@@ -1500,7 +1500,7 @@ __global__ void __launch_bounds__(kThreads) k_node_insert(BatchPtrs b) {
 }
 
 // CreateLeafNodes + SolveQEFs + GenerateMeshVertexBuffer (octree.cl:236-331, 475-487)
-template <int VPC>
+template <int VPC, bool HOST>
 __global__ void __launch_bounds__(kThreads, 4) k_leaf(BatchPtrs b) {
     if (b.bs->overflow) return;
     const int total = b.bs->total_nodes;
@@ -1509,7 +1509,23 @@ __global__ void __launch_bounds__(kThreads, 4) k_leaf(BatchPtrs b) {
         lo = (int)((long long)total * b.slice / b.nslices);
         hi = (int)((long long)total * (b.slice + 1) / b.nslices);
     }
-    for (int i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += gridDim.x * blockDim.x) {
+    // HOST: the vertices also go to the caller's pinned host array
+    // (b.host_vertices) as they are made.  Each warp stages its 32 vertices in
+    // shared memory (dynamic, so launches without it keep the whole L1) and
+    // writes them as one contiguous run of 16-byte stores, so the C2C traffic
+    // starts with the leaves instead of after them; for that the warp walks
+    // its 32 consecutive leaves together, lanes past the end idle.  An array
+    // too small is not written and the batch is flagged, as k_export does.
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    float4* const host = b.host_vertices;
+    const bool to_host = HOST && (int64_t)total <= b.host_vertex_cap;
+    if (HOST && !to_host && blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&b.bs->status, 1);
+    extern __shared__ float4 stage_mem[];
+    float4* const stage = stage_mem + 96 * wid;
+    for (int i0 = lo + blockIdx.x * blockDim.x + (HOST ? (threadIdx.x & ~31) : threadIdx.x); i0 < hi;
+         i0 += gridDim.x * blockDim.x) {
+      const int i = HOST ? i0 + lane : i0;
+      if (!HOST || i < hi) {
         const int c = b.node_chunk[i];
         const ChunkState& st = b.cs[c];
         const ChunkDesc& d = b.desc[c];
@@ -1616,9 +1632,25 @@ __global__ void __launch_bounds__(kThreads, 4) k_leaf(BatchPtrs b) {
         vtx.colour[2] = d.colour[2];
         vtx.colour[3] = (float)((ni & 0xffff) >> 8);
         float4* dst = reinterpret_cast<float4*>((simp ? b.leaf_out : b.vertices) + i);
-        dst[0] = make_float4(vtx.position[0], vtx.position[1], vtx.position[2], vtx.position[3]);
-        dst[1] = make_float4(vtx.normal[0], vtx.normal[1], vtx.normal[2], vtx.normal[3]);
-        dst[2] = make_float4(vtx.colour[0], vtx.colour[1], vtx.colour[2], vtx.colour[3]);
+        const float4 f0 = make_float4(vtx.position[0], vtx.position[1], vtx.position[2], vtx.position[3]);
+        const float4 f1 = make_float4(vtx.normal[0], vtx.normal[1], vtx.normal[2], vtx.normal[3]);
+        const float4 f2 = make_float4(vtx.colour[0], vtx.colour[1], vtx.colour[2], vtx.colour[3]);
+        dst[0] = f0;
+        dst[1] = f1;
+        dst[2] = f2;
+        if (HOST && to_host) {
+            stage[3 * lane] = f0;
+            stage[3 * lane + 1] = f1;
+            stage[3 * lane + 2] = f2;
+        }
+      }
+      if (HOST && to_host) {
+        __syncwarp();
+        const int n = min(32, hi - i0);
+        float4* out = host + 3 * (size_t)i0;
+        for (int k = lane; k < 3 * n; k += 32) out[k] = stage[k];
+        __syncwarp();
+      }
     }
 }
 
@@ -2309,7 +2341,12 @@ cudaError_t launch_edge_insert(const BatchPtrs& b, cudaStream_t s) {
 }
 
 cudaError_t launch_leaf(const BatchPtrs& b, cudaStream_t s) {
-    LVN_VPC_DISPATCH(b.vpc, (k_leaf<V><<<persistent_grid(b, ST_LEAF, 8), kThreads, 0, s>>>(b)));
+    if (b.host_vertices) {
+        LVN_VPC_DISPATCH(b.vpc, (k_leaf<V, true><<<persistent_grid(b, ST_LEAF, 8), kThreads,
+                                                   sizeof(float4) * 96 * (kThreads / 32), s>>>(b)));
+    } else {
+        LVN_VPC_DISPATCH(b.vpc, (k_leaf<V, false><<<persistent_grid(b, ST_LEAF, 8), kThreads, 0, s>>>(b)));
+    }
     return cudaGetLastError();
 }
 

@@ -422,6 +422,17 @@ def test_pinned_host_outputs(lvn_gpu, mg):
                          C.cast(results, C.POINTER(lvn.ChunkResult)))
     assert mg.generate_chunks_raw(descs, n, small) == lvn.LVN_ERR_CAPACITY
     assert small.total_triangles == T.shape[0]
+    # a vertex array too small: the leaves, which write it themselves, flag it
+    small_v = lvn.BatchOut(lvn.LVN_MEMORY_HOST, hv.data_ptr(), V.shape[0] - 1, 0, ht.data_ptr(), cap_t, 0,
+                           hs.data_ptr(), cap_s, 0, C.cast(results, C.POINTER(lvn.ChunkResult)))
+    assert mg.generate_chunks_raw(descs, n, small_v) == lvn.LVN_ERR_CAPACITY
+    # a vertex array that is not 16-byte aligned takes the sliced export path
+    hv.zero_()
+    odd = lvn.BatchOut(lvn.LVN_MEMORY_HOST, hv.data_ptr() + 4, cap_v - 1, 0, ht.data_ptr(), cap_t, 0,
+                       hs.data_ptr(), cap_s, 0, C.cast(results, C.POINTER(lvn.ChunkResult)))
+    assert mg.generate_chunks_raw(descs, n, odd) == 0
+    got = hv.numpy()[1:1 + 12 * V.shape[0]].reshape(-1, 12)
+    assert np.array_equal(got.view(np.int32), V.view(np.int32))
     lvn.clear_csg_operations()
 
 
