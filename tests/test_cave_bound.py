@@ -10,6 +10,8 @@ among the lattice points within sqrt(0.6) of the point (farther ones give 0),
 so 32 |g|max times the largest lattice sum of (0.6 - r^2)^4 r over a cell
 bounds |snoise3|.  The lattice sum is maximised over a grid and widened by its
 Lipschitz constant times the grid's half-diagonal."""
+import ctypes as C
+
 import numpy as np
 
 import oracle_lib as O
@@ -68,3 +70,38 @@ def test_oracle_snoise3_within_bound():
     L = O.lib()
     vals = np.array([L.orc_snoise3(float(x), float(y), float(z)) for x, y, z in pts])
     assert np.abs(vals).max() <= BOUND
+
+
+def cave_band(amp3, octaves3, gain3):
+    """The band the library computes (cave_band in lvn_api.cu): |amp3| times
+    the snoise3 bound times the sum of the octave amplitudes, plus 0.1 %."""
+    amp, total = np.float32(1.0), 0.0
+    for _ in range(octaves3):
+        total += abs(float(amp))
+        amp = np.float32(amp * np.float32(gain3))
+    return abs(amp3) * BOUND * total * 1.001
+
+
+def test_cave_term_within_band():
+    """The oracle's cave term (its density minus the same density without the
+    3D term) stays inside the band at random points of the density space."""
+    from leven_gb300 import workloads as W
+
+    O.set_seed(1)
+    d = W.CAVES
+    caves = O.density(mode=2, octaves2=d["octaves2"], freq2=d["freq2"], lac2=d["lacunarity2"], gain2=d["gain2"],
+                      amp2=d["amp2"], octaves3=d["octaves3"], freq3=d["freq3"], lac3=d["lacunarity3"],
+                      gain3=d["gain3"], amp3=d["amp3"])
+    flat = O.density(mode=2, octaves2=d["octaves2"], freq2=d["freq2"], lac2=d["lacunarity2"], gain2=d["gain2"],
+                     amp2=d["amp2"], octaves3=d["octaves3"], freq3=d["freq3"], lac3=d["lacunarity3"],
+                     gain3=d["gain3"], amp3=0.0)
+    band = cave_band(d["amp3"], d["octaves3"], d["gain3"])
+    L = O.lib()
+    rng = np.random.default_rng(11)
+    pts = rng.uniform(-4096.0, 4096.0, (20000, 3)).astype(np.float32)
+    worst = 0.0
+    for x, y, z in pts:
+        a = L.orc_density_at(C.byref(caves), float(x), float(y), float(z))
+        b = L.orc_density_at(C.byref(flat), float(x), float(y), float(z))
+        worst = max(worst, abs(a - b))
+    assert 0.0 < worst <= band, (worst, band)
