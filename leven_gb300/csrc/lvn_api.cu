@@ -681,6 +681,12 @@ int enqueue_fresh_dag(lvn_meshgen* m, const BatchPtrs& b, bool any_ops, const Di
     LVN_CK(cudaStreamWaitEvent(s0, m->ev_mesh, 0));
     BatchPtrs bs = b;
     bs.scatter_what = simp ? 0 : 2;
+    // pinned host seams, 16-byte aligned: the seam pass writes them itself
+    const bool fused_seams = pipelined && (reinterpret_cast<uintptr_t>(direct->dst[2]) & 15) == 0;
+    if (fused_seams) {
+        bs.host_seams = static_cast<int4*>(direct->dst[2]);
+        bs.host_seam_cap = direct->cap[2];
+    }
     LVN_CK(launch_mesh_scatter(bs, s0));
     if (simp) LVN_CK(launch_simplify(b, s0));
     if (direct) {
@@ -688,7 +694,7 @@ int enqueue_fresh_dag(lvn_meshgen* m, const BatchPtrs& b, bool any_ops, const Di
             const int rc = enqueue_exports(m, b, direct, s0);
             if (rc) return rc;
         } else {
-            LVN_CK(launch_export(b, 2, direct->dst[2], direct->cap[2], s0));
+            if (!fused_seams) LVN_CK(launch_export(b, 2, direct->dst[2], direct->cap[2], s0));
             if (!fused) {  // the side stream joined the DAG only for the sliced exports
                 LVN_CK(cudaEventRecord(m->ev_side, m->side));
                 LVN_CK(cudaStreamWaitEvent(s0, m->ev_side, 0));

@@ -1765,11 +1765,20 @@ __global__ void __launch_bounds__(1024) k_mesh_plan(BatchPtrs b) {
     }
 }
 
-template <int VPC>
+template <int VPC, bool HOST>
 __global__ void __launch_bounds__(kNodeTile) k_mesh_scatter(BatchPtrs b) {
     __shared__ int sm[kNodeTile / 32 + 1];
     if (b.bs->overflow) return;
     const int ntiles = b.chunk_tile_off[b.n];
+    // HOST (the seam pass): the seams also go to the caller's pinned host
+    // array (b.host_seams).  A tile's seams are contiguous, so the CTA stages
+    // them in shared memory (dynamic, this variant only) and writes them as
+    // one run of 16-byte stores.  An array too small is not written and the
+    // batch is flagged, as k_export does.
+    int4* const host = b.host_seams;
+    const bool to_host = HOST && (int64_t)b.bs->total_seams <= b.host_seam_cap;
+    if (HOST && !to_host && blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&b.bs->status, 4);
+    extern __shared__ int4 seam_stage[];
     // winding orders by sign-change direction (octree.cl:357-362)
     const int w0[6] = {0, 1, 3, 0, 3, 2};
     const int w1[6] = {0, 3, 1, 0, 2, 3};
@@ -1821,11 +1830,28 @@ __global__ void __launch_bounds__(kNodeTile) k_mesh_scatter(BatchPtrs b) {
                 const int sp = st.seam_off + toff.y + (ex >> 16);
                 const float4* v = reinterpret_cast<const float4*>((b.simp_on ? b.leaf_out : b.vertices) + i);
                 int4* dst = reinterpret_cast<int4*>(b.seams + sp);
-                dst[0] = make_int4(pos[0], pos[1], pos[2], b.node_info[i] & 0xffff);
+                const int4 s0 = make_int4(pos[0], pos[1], pos[2], b.node_info[i] & 0xffff);
                 const float4 p = v[0], nrm = v[1];
+                dst[0] = s0;
                 reinterpret_cast<float4*>(dst)[1] = p;
                 reinterpret_cast<float4*>(dst)[2] = nrm;
+                if (HOST && to_host) {
+                    const int r = ex >> 16;
+                    seam_stage[3 * r] = s0;
+                    reinterpret_cast<float4*>(seam_stage)[3 * r + 1] = p;
+                    reinterpret_cast<float4*>(seam_stage)[3 * r + 2] = nrm;
+                }
             }
+        }
+        if (HOST && to_host) {
+            __syncthreads();
+            const int ns = total >> 16;  // the tile's seams
+            if (ns) {
+                const ChunkState& tst = b.cs[c];
+                int4* out = host + 3 * (size_t)(tst.seam_off + b.node_tile_counts[vt].y);
+                for (int k = threadIdx.x; k < 3 * ns; k += blockDim.x) out[k] = seam_stage[k];
+            }
+            __syncthreads();  // the next tile reuses the staging rows
         }
     }
 }
@@ -2386,7 +2412,13 @@ cudaError_t launch_export(const BatchPtrs& b, int which, void* dst, int64_t capa
 }
 
 cudaError_t launch_mesh_scatter(const BatchPtrs& b, cudaStream_t s) {
-    LVN_VPC_DISPATCH(b.vpc, (k_mesh_scatter<V><<<persistent_grid(b, ST_MESH_SCATTER, 8), kNodeTile, 0, s>>>(b)));
+    if (b.host_seams) {
+        LVN_VPC_DISPATCH(b.vpc, (k_mesh_scatter<V, true><<<persistent_grid(b, ST_MESH_SCATTER, 8), kNodeTile,
+                                                          sizeof(int4) * 3 * kNodeTile, s>>>(b)));
+    } else {
+        LVN_VPC_DISPATCH(b.vpc, (k_mesh_scatter<V, false><<<persistent_grid(b, ST_MESH_SCATTER, 8), kNodeTile, 0,
+                                                           s>>>(b)));
+    }
     return cudaGetLastError();
 }
 

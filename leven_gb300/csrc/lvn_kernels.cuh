@@ -25,6 +25,8 @@ struct BatchPtrs {
     float cave_band;             // |y - amp2 h| above this: the cave term cannot change the density's sign
     float4* host_vertices;       // non-null: k_leaf also writes each vertex to this pinned host array
     int64_t host_vertex_cap;     //   (16-byte aligned), of this many vertices
+    int4* host_seams;            // non-null: the seam pass of k_mesh_scatter also writes this pinned array
+    int64_t host_seam_cap;       //   (16-byte aligned), of this many seam nodes
     int32_t default_material;
     int32_t dom_by_solid[9];     // dominant material of 8 corners, n of them the default material, the rest AIR
 

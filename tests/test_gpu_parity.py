@@ -433,6 +433,15 @@ def test_pinned_host_outputs(lvn_gpu, mg):
     assert mg.generate_chunks_raw(descs, n, odd) == 0
     got = hv.numpy()[1:1 + 12 * V.shape[0]].reshape(-1, 12)
     assert np.array_equal(got.view(np.int32), V.view(np.int32))
+    # the same for the seams, which the seam pass writes itself when aligned
+    small_s = lvn.BatchOut(lvn.LVN_MEMORY_HOST, hv.data_ptr(), cap_v, 0, ht.data_ptr(), cap_t, 0, hs.data_ptr(),
+                           S.shape[0] - 1, 0, C.cast(results, C.POINTER(lvn.ChunkResult)))
+    assert mg.generate_chunks_raw(descs, n, small_s) == lvn.LVN_ERR_CAPACITY
+    hs.zero_()
+    odd_s = lvn.BatchOut(lvn.LVN_MEMORY_HOST, hv.data_ptr(), cap_v, 0, ht.data_ptr(), cap_t, 0, hs.data_ptr() + 4,
+                         cap_s - 1, 0, C.cast(results, C.POINTER(lvn.ChunkResult)))
+    assert mg.generate_chunks_raw(descs, n, odd_s) == 0
+    assert np.array_equal(hs.numpy()[1:1 + 12 * S.shape[0]].reshape(-1, 12), S)
     lvn.clear_csg_operations()
 
 
