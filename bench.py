@@ -1,26 +1,38 @@
 """Benchmark of the chunk-meshing path on GB300.
 
-Workload: 128 LOD0 64^3 chunks tiling a 512 x 128 x 512-voxel region of the
-2D fBm terrain (8 octaves, 1/256, lacunarity 2, gain 0.5, amplitude 48, noise
-seed 1) with 32 seeded CSG operations (half sphere-subtract, half box-union,
-radii / half extents U[2, 12] voxels) stored and replayed per chunk.  A step
-meshes every chunk from a fresh field (caches bypassed): field, CSG, edges,
-hermite data, leaves + QEF, cuckoo tables, mesh, seams.
+Default workload (the large clipmap sweep): 4096 chunks of 64^3 voxels over
+clipmap LODs 0-5 (voxel sizes 1-32), the union of SelectActiveClipmapNodes
+along a seeded camera path, nearest first; density = 2D fBm heightfield (8
+octaves, 1/256, lacunarity 2, gain 0.5, amplitude 48) + 3D fBm caves (6
+octaves, 1/64, amplitude 12), noise seed 1; 64 seeded CSG operations (half
+sphere-subtract, half box-union, radii / half extents U[2, 12] voxels) stored
+and replayed per chunk through the plain path.  A step meshes every chunk
+from a fresh field (caches bypassed): field, CSG, edges, hermite data,
+leaves + QEF, cuckoo tables, mesh, seams.
 
-  value  chunks/s with outputs left in device memory (per-step CUDA events
-         on the library's stream; L2 flushed between steps, outside the
-         timed events)
+  value  plain-path chunks/s with outputs left in device memory (per-step
+         CUDA events on the library's stream; L2 flushed between steps,
+         outside the timed events)
   e2e    chunks/s through the same C-ABI call with host output arrays
          (pinned), device-to-host copies inside the timed region
+  surrogate
+         the learned density: sampled and trained on the GPU (2^24 fresh
+         plain samples, 20k Adam steps at batch 65,536), then the same 4096
+         chunks meshed with it under its per-chunk probe gate; surrogate
+         chunks/s, fallback rate, mesh Hausdorff distance to the plain
+         meshes, density error against FP32 and FP64, training time and
+         tensor throughput
 
 `--impl reference` times the CPU restatement of the reference algorithm
 (oracle/, the reference's OpenCL cannot run here) on all host threads over
 a bounded sample of the same workload.
 
-`--workload clipmap`: 1024 chunks over clipmap LODs 0-4 around a moving
-seeded camera, 2D fBm heightfield + 3D fBm caves, followed by the octree
-simplification at QEF error 0.05 (CPU baseline: the same, simplification
-included).  `--workload select`: the clipmap's active-node selection
+Other workloads (`--workload`): `tiled`, 128 LOD0 chunks tiling a
+512 x 128 x 512-voxel region of the 2D fBm terrain with 32 seeded CSG
+operations; `clipmap`, 1024 chunks over clipmap LODs 0-4 around a moving
+seeded camera, caves density, followed by the octree simplification at QEF
+error 0.05 (CPU baseline: the same, simplification included); `one`, a single
+LOD0 chunk.  `--workload select`: the clipmap's active-node selection
 (SelectActiveClipmapNodes) for 4096 cameras on 64 seeded paths through the
 2^15-unit world, one launch per step (its own JSON line, impl "lvn-select";
 the reference arm times the oracle's recursion on all host threads).
@@ -33,9 +45,8 @@ host threads).
 (ngMeshSimplifier) of the same 428 meshes, each with its node's options as
 ConstructClipmapNodeData sets them (its own JSON line, impl "lvn-collapse";
 the reference arm times the oracle's simplifier on all host threads).
-`--surrogate`: trains the learned density surrogate on the GPU
-and meshes the clipmap chunk set with the 2D fBm density plain and through
-the surrogate (its own JSON line, impl "lvn-surrogate").
+`--surrogate`: the surrogate leg alone, on the 1024-chunk clipmap set with
+the 2D fBm density (its own JSON line, impl "lvn-surrogate").
 """
 import argparse
 import ctypes as C
@@ -52,7 +63,7 @@ ROOT = pathlib.Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 L2_BYTES = 129 * 1024 * 1024
-METRIC = "64^3 chunks meshed/sec on 1 GB300 (plain path)"
+METRIC = "64\u00b3 chunks meshed/sec on 1 GB300, plain vs learned-density at \u22640.05-voxel Hausdorff"
 
 
 def parse():
@@ -68,16 +79,19 @@ def parse():
                    help="learned-density run: train the surrogate (2^24 samples of the 2D fBm density, Adam), then "
                         "mesh the 1024-chunk clipmap set plain and with the surrogate")
     p.add_argument("--train-steps", type=int, default=20000)
-    p.add_argument("--gate", type=float, default=0.5, help="surrogate probe gate (density units)")
+    p.add_argument("--gate", type=float, default=0.5, help="surrogate probe gate (voxels of each chunk)")
     p.add_argument("--mesh-chunks", type=int, default=0, help="surrogate run: mesh only the first N chunks (0 = all)")
     p.add_argument("--simplify", type=float, default=None,
                    help="octree simplification QEF-error threshold (voxel^2); default 0.05 for the clipmap "
                         "workload, off otherwise; < 0 = off")
-    p.add_argument("--workload", default="tiled", choices=["tiled", "clipmap", "one", "select", "seams", "collapse"],
-                   help="tiled: 128 LOD0 chunks + 32 CSG ops (default); clipmap: 1024 chunks over LOD 0-4 with "
+    p.add_argument("--workload", default="sweep",
+                   choices=["sweep", "tiled", "clipmap", "one", "select", "seams", "collapse"],
+                   help="sweep: 4096 chunks over LOD 0-5, caves + 64 CSG ops, plain and surrogate (default); "
+                        "tiled: 128 LOD0 chunks + 32 CSG ops; clipmap: 1024 chunks over LOD 0-4 with "
                         "3D caves; one: a single LOD0 chunk; select: clipmap node selection for 4096 cameras; "
                         "seams: the seam meshes of one camera's clipmap; collapse: the engine's edge-collapse "
                         "simplification of that clipmap's meshes")
+    p.add_argument("--no-surrogate", action="store_true", help="sweep: skip the learned-density leg")
     return p.parse_args()
 
 
@@ -142,7 +156,7 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-WORKLOAD = "tiled"
+WORKLOAD = "sweep"
 
 
 def simplify_threshold(args):
@@ -158,6 +172,8 @@ def simp_name(thr):
 def workload():
     from leven_gb300 import workloads as W
 
+    if WORKLOAD == "sweep":
+        return W.clipmap_sweep()
     if WORKLOAD == "clipmap":
         return W.clipmap_caves()
     if WORKLOAD == "one":
@@ -419,7 +435,8 @@ def run_lvn(args):
     dom_ms = stages[dominant][0] / stages[dominant][1]
     stage_ms = {k: round(v[0] / v[1], 4) for k, v in stages.items() if v[1]}
     E = int(res_np[:, 6].sum())
-    traffic = committed_traffic(dominant)
+    traffic = None  # no profiler inside the timed run; a committed ncu figure is quoted separately
+    traffic_note = committed_traffic(dominant)
     df = density_flops(wl)
     if dominant in ("hermite", "field") and df is not None and (dominant == "hermite" or wl.density["mode"] == 2):
         # FP32 issue-rate roofline: SMs x 128 lanes x 2 flop x clock
@@ -436,13 +453,15 @@ def run_lvn(args):
         ach = flops / (dom_ms / 1e3) / 1e12
         roof = {"bound": "fp32", "achieved": round(ach, 3), "peak": round(fp32_peak, 2),
                 "unit": "TFLOP/s", "frac": round(ach / fp32_peak, 4), "traffic": traffic,
+                "traffic_from_profile": traffic_note,
                 "kernel": dominant, "ms_per_launch": round(dom_ms, 4), "peak_source": f"SMs x 128 x 2 x {clk} MHz",
                 "flop_per_launch": int(flops)}
     else:
         b = stage_work(dominant, res_np, n)
         ach = b / (dom_ms / 1e3) / 1e9 if b else None
         roof = {"bound": "hbm", "achieved": round(ach, 1) if ach else None, "peak": hbm_peak, "unit": "GB/s",
-                "frac": round(ach / hbm_peak, 4) if ach else None, "traffic": traffic, "kernel": dominant,
+                "frac": round(ach / hbm_peak, 4) if ach else None, "traffic": traffic,
+                "traffic_from_profile": traffic_note, "kernel": dominant,
                 "ms_per_launch": round(dom_ms, 4), "peak_source": peak_src}
 
     bo = bo_host
@@ -467,14 +486,39 @@ def run_lvn(args):
         "stage_ms": stage_ms,
         "clocks": clocks.summary(),
     }
+    # achieved HBM bandwidth of each memory-bound stage: its algorithmic bytes
+    # (stage_work) over its profiled time, against the measured copy peak
+    stage_gbs = {}
+    for k, ms_k in stage_ms.items():
+        b = stage_work(k, res_np, n)
+        if b and ms_k > 0:
+            gbs = b / (ms_k / 1e3) / 1e9
+            stage_gbs[k] = {"gbs": round(gbs, 1), "frac": round(gbs / hbm_peak, 4), "bytes": int(b)}
+    line["stage_gbs"] = stage_gbs
+    line["stage_gbs_peak"] = {"hbm_gbs": hbm_peak, "source": peak_src}
+    # density samples a step determines: every field point of every chunk, and
+    # the 23 evaluations (17 search + 6 normal) of each plain edge's hermite data
+    nxz, ny = edge_axis_counts(mg, lvn, n) if n <= 8192 else (0, 0)
+    samples = n * (wl.voxels_per_chunk + 2) ** 3 + 23 * (nxz + ny)
+    line["density_samples_per_s"] = round(samples / (ms / 1e3), 1)
+    line["density_samples_per_step"] = int(samples)
+    # the FP32 leaf solve against an FP64 solve of the same crossings, over
+    # every leaf of the last (device-output) step: a GPU measurement pass
+    step(True)
+    qmax, qmean, qleaves = mg.qef_fp64_error()
+    line["qef_fp64"] = {"max_voxels": qmax, "mean_voxels": qmean, "leaves": qleaves,
+                        "what": "|x_fp32 - x_fp64| of each leaf vertex, in its chunk's voxels"}
+    if rank == 0 and WORKLOAD == "sweep" and not args.no_surrogate:
+        line["surrogate"] = surrogate_leg(args, wl, mg, descs, results, value, stream, flush, local)
     if rank == 0 and not args.no_cpu_baseline:
         threads = host_threads()
         cb = CpuBaseline(wl, threads, simp)
-        if args.cpu_sample:
-            dt = cb.run(args.cpu_sample)
-            m = min(args.cpu_sample, n)
+        if args.cpu_sample or n > 1024:
+            # a bounded sample: about 12 s of CPU work spread over the workload
+            m = min(args.cpu_sample or cb.step_chunks(12.0), n)
+            dt = cb.run(m)
             v = m / dt
-            what = f"{m} chunks spread over the {n}-chunk workload, {dt:.1f} s"
+            what = f"{m} chunks spread evenly over the {n}-chunk workload, {dt:.1f} s"
         else:
             v, dt, m = cb.rate(10.0)
             what = f"{m // n} passes over the {n}-chunk workload ({m} chunks), {dt:.1f} s"
@@ -555,6 +599,111 @@ def hausdorff_voxels(va, vb, voxel):
     d1 = cKDTree(vb).query(va)[0].max()
     d2 = cKDTree(va).query(vb)[0].max()
     return float(max(d1, d2)) / voxel
+
+
+def surrogate_leg(args, wl, mg, descs, results, plain_value, stream, flush, gpu_index):
+    """The learned density on the sweep: sample 2^24 fresh plain samples of
+    the workload's density over the chunk set's x / z extent (y in [-128,
+    128], extrapolated beyond), train 20k Adam steps at batch 65,536 on the
+    tensor cores, then mesh the same chunks with the surrogate under its
+    per-chunk probe gate (in voxels of each chunk); plain and surrogate meshes
+    of every surrogate chunk are compared by symmetric Hausdorff distance."""
+    import numpy as np
+    import torch
+
+    import leven_gb300 as lvn
+
+    n = len(wl.chunks)
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        pass
+    lo = [min(mn[i] for mn, _ in wl.chunks) / 4.0 for i in range(3)]
+    hi = [max(mn[i] + s for mn, s in wl.chunks) / 4.0 for i in range(3)]
+    lo[1], hi[1] = -128.0, 128.0
+    sur = lvn.Surrogate(tuple(lo), tuple(hi), seed=1)
+    t0 = time.perf_counter()
+    sur.sample(1 << 24, seed=1)
+    t_sample = time.perf_counter() - t0
+    steps = args.train_steps
+    t0 = time.perf_counter()
+    losses = sur.train(steps, batch=65536, lr=1e-3)
+    t_train = time.perf_counter() - t0
+    train_flop = 3 * 2 * (96 * 128 + 3 * 128 * 128 + 128) * 65536 * steps
+    train_tflops = train_flop / t_train / 1e12
+    sustained = peaks.get("bf16_tflops_sustained")
+
+    # plain meshes of this batch (host copies), then the surrogate's
+    Vp, Tp, Sp, resp = mg.generate_chunks(wl.chunks)
+    mg.set_surrogate(sur, args.gate)
+    try:
+        Vs, Ts, Ss, ress = mg.generate_chunks(wl.chunks)
+        use = mg.surrogate_chunks(n)
+        cap_v = max(int(resp[:, 7].sum()), int(ress[:, 7].sum())) + 1024
+        cap_t = max(Tp.shape[0], Ts.shape[0]) + 4096
+        cap_s = max(Sp.shape[0], Ss.shape[0]) + 1024
+        d_vert = torch.empty(cap_v * 12, dtype=torch.float32, device="cuda")
+        d_tri = torch.empty(cap_t * 3, dtype=torch.int32, device="cuda")
+        d_seam = torch.empty(cap_s * 12, dtype=torch.int32, device="cuda")
+        bo = lvn.BatchOut(lvn.LVN_MEMORY_DEVICE, d_vert.data_ptr(), cap_v, 0, d_tri.data_ptr(), cap_t, 0,
+                          d_seam.data_ptr(), cap_s, 0, C.cast(results, C.POINTER(lvn.ChunkResult)))
+        for _ in range(max(3, args.warmup // 2)):
+            assert mg.generate_chunks_raw(descs, n, bo) == 0
+        torch.cuda.synchronize()
+        ts = []
+        with ClockSampler(gpu_index) as clocks:
+            for _ in range(max(3, args.steps // 2)):
+                with torch.cuda.stream(stream):
+                    flush.fill_(1)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                assert mg.generate_chunks_raw(descs, n, bo) == 0
+                e1.record(stream)
+                e1.synchronize()
+                ts.append(e0.elapsed_time(e1))
+        ms_sur = sum(ts) / len(ts)
+    finally:
+        mg.set_surrogate(None)
+    hd = []
+    for c in np.flatnonzero(use):
+        rp, rs = resp[c], ress[c]
+        voxel = 4.0 * wl.chunks[c][1] / 256  # world units per voxel of this chunk
+        h = hausdorff_voxels(Vp[rp[0]:rp[0] + rp[1], :3], Vs[rs[0]:rs[0] + rs[1], :3], voxel)
+        if h is not None:
+            hd.append(h)
+    # density error against the plain FP32 density and the FP64 density, on
+    # fresh samples
+    pts = sur.sample(1 << 16, seed=99, fetch=True)
+    d_sur = sur.eval(pts)
+    d64 = lvn.density_f64(pts)
+    err = np.abs(d_sur - pts[:, 3])
+    err64 = np.abs(d_sur - d64)
+    lods = np.array([(s // 256).bit_length() - 1 for _, s in wl.chunks])
+    on = use.astype(bool)
+    samples_sur = int(on.sum()) * (wl.voxels_per_chunk + 2) ** 3 + 512 * n
+    sur.close()
+    hd_a = np.array(hd) if hd else np.zeros(0)
+    return {
+        "value": round(n / (ms_sur / 1e3), 2), "unit": "chunks/s", "ms_per_step": round(ms_sur, 3),
+        "vs_plain": round(n / (ms_sur / 1e3) / plain_value, 4),
+        "gate_voxels": args.gate, "chunks_on_surrogate": int(on.sum()), "fallback_rate": round(1 - on.sum() / n, 4),
+        "on_surrogate_by_lod": {str(k): int((on & (lods == k)).sum()) for k in sorted(set(lods.tolist()))},
+        "hausdorff_voxels_mean": round(float(hd_a.mean()), 4) if hd else None,
+        "hausdorff_voxels_max": round(float(hd_a.max()), 4) if hd else None,
+        "chunks_within_bar": int(((hd_a <= 0.5)).sum()) if hd else 0,
+        "density_samples_per_s": round(samples_sur / (ms_sur / 1e3), 1),
+        "density_abs_err_mean": float(err.mean()), "density_abs_err_p99": float(np.quantile(err, 0.99)),
+        "density_abs_err_vs_fp64_mean": float(err64.mean()),
+        "density_abs_err_vs_fp64_p99": float(np.quantile(err64, 0.99)),
+        "plain_fp32_abs_err_vs_fp64_max": float(np.abs(pts[:, 3] - d64).max()),
+        "train": {"samples": 1 << 24, "steps": steps, "batch": 65536, "lr": 1e-3, "sample_s": round(t_sample, 2),
+                  "train_s": round(t_train, 2), "network_tflops": round(train_tflops, 2),
+                  "tensor_frac_of_sustained_bf16": round(train_tflops / sustained, 4) if sustained else None,
+                  "loss_first": float(losses[0]) if len(losses) else None,
+                  "loss_last100": float(np.mean(losses[-100:])) if len(losses) else None},
+        "domain": [lo, hi], "clocks": clocks.summary(),
+    }
 
 
 def run_surrogate(args):

@@ -247,19 +247,59 @@ int lvn_meshgen_autotune(lvn_meshgen* ctx, const lvn_chunk_desc* chunks, int32_t
                                      first leaf below it | octree level << 20   */
 int64_t lvn_meshgen_debug_fetch(lvn_meshgen* ctx, int32_t what, int32_t chunk, void* host, int64_t cap_bytes);
 
+/* New: the error of the FP32 leaf solve (qef_solve, qef.cl:239-256) against
+ * an FP64 solve of the same crossings and normals, over every leaf of the
+ * context's last fresh batch (not simplified leaves' parents): out[0] max and
+ * out[1] mean distance in voxels of the leaf's chunk, out[2] leaves.  A
+ * measurement pass on the GPU; LVN_ERR_INVALID before any fresh batch. */
+int lvn_meshgen_qef_fp64_error(lvn_meshgen* ctx, double out[3]);
+
+/* Test hook (new).  The device cuckoo table the meshing stages build, over an
+ * arbitrary list of n distinct keys with value = key index: Cuckoo_InsertKeys
+ * (cuckoo.cl:26-71) under Cuckoo_InsertKeys' host retry loop
+ * (compute_cuckoo.cpp:76-139, here bounded to 16 parameter draws), then
+ * Cuckoo_Find (cuckoo.cl:73-104) of every key into values[n] (~0 = not found).
+ * prime 0 sizes the table as Cuckoo_InitialiseTable does
+ * (compute_cuckoo.cpp:49-73: FindNextPrime(max(2048, 2n))); another value
+ * forces that table size, so that a small one sends keys to the 101-entry
+ * stash.  flags LVN_CUCKOO_REFERENCE_FIND looks keys up as the reference's
+ * Cuckoo_Find is written, whose stash probe reads data[h] instead of
+ * stash[h] (cuckoo.cl:93-101), so stashed keys are not found.  table_out
+ * (optional, prime + 101 entries) receives the table then the stash.  info:
+ * prime, stash used, parameter draws, insert failed.  Returns LVN_ERR_HASH
+ * when every draw failed. */
+#define LVN_CUCKOO_REFERENCE_FIND 1
+int lvn_debug_cuckoo(const uint32_t* keys, int32_t n, uint32_t prime, int32_t flags, uint32_t* values,
+                     uint64_t* table_out, int64_t table_capacity, int32_t info[4]);
+
+/* Test hook (new): host-side fault injection, for the failure paths of the
+ * meshing calls.  LVN_FAULT_DEVICE_ALLOC makes the next `count` device
+ * allocations fail as cudaMalloc's out-of-memory does (the call returns
+ * LVN_ERR_OUT_OF_MEMORY); LVN_FAULT_HASH_FAMILY makes the next `count` cuckoo
+ * parameter draws a degenerate family under which no table holds three keys
+ * (the call returns LVN_ERR_HASH after its bounded retries, where the
+ * reference's loop at compute_cuckoo.cpp:86-132 retries without bound);
+ * LVN_FAULT_NONE clears both.  No GPU fault is involved. */
+#define LVN_FAULT_NONE         0
+#define LVN_FAULT_DEVICE_ALLOC 1
+#define LVN_FAULT_HASH_FAMILY  2
+int lvn_debug_inject_fault(int32_t what, int32_t count);
+
 /* No counterpart in the reference.  Meshes one chunk exactly as
  * lvn_meshgen_generate_chunk_mesh does with caching off, but allocates no
  * memory: for engine threads that cannot call cudaMalloc / cudaFree (a
  * frame-locked render or streaming thread, where cudaFree would synchronise
- * the device; engines that reserve all GPU memory at start-up; recording
- * into a CUDA graph).  The caller passes the chunk and its output arrays
- * (host or device per out->memory); the stored CSG operations and the noise
- * seed come from the global state as usual.  All intermediate buffers live
- * in one static device array of LVN_NOALLOC_SCRATCH_BYTES that every GPU
- * loading the library keeps until exit.  The first call on a device looks up
- * that array's address (cudaGetSymbolAddress), so make it before any stream
- * capture.  Chunks beyond the LVN_NOALLOC_MAX_* limits are rejected with
- * LVN_ERR_CAPACITY.  Calls share the array: two calls in flight on the GPU at
+ * the device; engines that reserve all GPU memory at start-up).  The caller
+ * passes the chunk and its output arrays (host or device per out->memory);
+ * the stored CSG operations and the noise seed come from the global state as
+ * usual.  All intermediate buffers live in one static device array of
+ * LVN_NOALLOC_SCRATCH_BYTES that every GPU loading the library keeps until
+ * exit; the first call looks up that array's device address
+ * (cudaGetSymbolAddress).  The call runs on the device lvn_init ran on and
+ * returns LVN_ERR_INVALID when another device is current.  It reads its
+ * counters back and synchronises cuda_stream before returning.  Chunks beyond
+ * the LVN_NOALLOC_MAX_* limits are rejected with LVN_ERR_CAPACITY.  Calls
+ * share the array, from every host thread: two calls in flight on the GPU at
  * the same time (different streams or threads) race; serialise them.
  * cuda_stream may be NULL (the legacy default stream). */
 #define LVN_NOALLOC_SCRATCH_BYTES        (12 * 1024 * 1024)
@@ -288,8 +328,10 @@ int32_t lvn_surrogate_num_params(void);
 int     lvn_surrogate_set_params(lvn_surrogate* s, const float* params, int64_t n);
 int     lvn_surrogate_get_params(lvn_surrogate* s, float* params, int64_t capacity);
 /* generate the training pool: n samples (x, y, z, plain density) of the
- * density set by lvn_set_density, 70% within 4 voxels of the heightfield
- * surface and 30% uniform in the domain; copied to host_out when not NULL */
+ * density set by lvn_set_density, 70% within 4 voxels of the zero set (the
+ * heightfield surface, or with caves up to eight tries within the cave band
+ * of it for |density| <= 4) and 30% uniform in the domain; copied to
+ * host_out when not NULL */
 int     lvn_surrogate_sample(lvn_surrogate* s, int64_t n, uint64_t seed, float* host_out);
 /* `steps` Adam steps on consecutive batches of the pool; losses[steps] (MSE
  * of density / 8) when not NULL.  batch is a multiple of 128. */
@@ -298,7 +340,8 @@ int     lvn_surrogate_train(lvn_surrogate* s, int32_t steps, int32_t batch, floa
  * 128: the gradient of the loss into grad[lvn_surrogate_num_params()] */
 int     lvn_surrogate_grad(lvn_surrogate* s, const float* samples, int32_t n, float* grad, float* loss);
 /* densities of n points (x, y, z, unused) in `memory` (LVN_MEMORY_HOST or
- * LVN_MEMORY_DEVICE) */
+ * LVN_MEMORY_DEVICE).  Above and below the domain's y range the density is
+ * extrapolated with unit slope from the range's edge. */
 int     lvn_surrogate_eval(lvn_surrogate* s, const float* points, int64_t n, float* density, int32_t memory);
 /* densities of `count` lattices of dim^3 points in device memory: lattice l
  * is lattices[4l .. 4l+3] = (x0, y0, z0, step), points x0 + step (i, j, k)
@@ -315,9 +358,10 @@ void*   lvn_surrogate_get_stream(lvn_surrogate* s);
 int     lvn_density_f64(const float* points, int64_t n, double* density);
 
 /* Mesh with the surrogate: every fresh chunk of this context is probed at
- * 8 x 8 x 8 of its field points; when the surrogate lies inside the domain
- * for the whole chunk and within `gate` (density units) of the plain density
- * at every probe, the chunk's field is the surrogate's (signs from its
+ * 8 x 8 x 8 of its field points; when the chunk's field lies inside the
+ * domain in x and z and the surrogate is within `gate` voxels of the chunk
+ * (gate x the chunk's voxel size in density units) of the plain density at
+ * every probe, the chunk's field is the surrogate's (signs from its
  * densities, crossings by linear interpolation, normals from central
  * differences of its field), else the plain path (fallback).  NULL turns it
  * off.  The surrogate must outlive its use by this context. */

@@ -104,7 +104,7 @@ EXPORTS = [
     "lvn_simplify_options_default", "lvn_mesh_simplify", "lvn_render_pool_create", "lvn_render_pool_destroy",
     "lvn_render_mesh_upload", "lvn_render_meshes_from_batch", "lvn_render_mesh_get", "lvn_render_mesh_download",
     "lvn_render_mesh_free",
-    "lvn_render_pool_usage",
+    "lvn_render_pool_usage", "lvn_meshgen_qef_fp64_error", "lvn_debug_cuckoo", "lvn_debug_inject_fault",
 ]
 
 _lib = None
@@ -188,6 +188,10 @@ def lib():
     L.lvn_meshgen_debug_fetch.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int64]
     L.lvn_meshgen_debug_fetch.restype = C.c_int64
     L.lvn_generate_chunk_mesh_noalloc.argtypes = [i32p, C.c_int32, C.c_int32, C.POINTER(MeshOut), C.c_void_p]
+    L.lvn_debug_cuckoo.argtypes = [C.c_void_p, C.c_int32, C.c_uint32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int64,
+                                   i32p]
+    L.lvn_debug_inject_fault.argtypes = [C.c_int32, C.c_int32]
+    L.lvn_meshgen_qef_fp64_error.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
     _lib = L
     return L
 
@@ -570,6 +574,13 @@ class MeshGen:
         """Direct C-ABI call with caller-prepared ctypes structures."""
         return lib().lvn_meshgen_generate_chunks(self._h, descs, n, C.byref(batch_out))
 
+    def qef_fp64_error(self):
+        """(max, mean, leaves): the FP32 leaf solve's distance in voxels from an
+        FP64 solve of the same crossings, over the last fresh batch's leaves."""
+        out = (C.c_double * 3)()
+        _check(lib().lvn_meshgen_qef_fp64_error(self._h, out), "lvn_meshgen_qef_fp64_error")
+        return float(out[0]), float(out[1]), int(out[2])
+
     def debug_fetch(self, what, chunk, dtype, width=1, max_elems=1 << 22):
         buf = np.zeros(max_elems * width, dtype=dtype)
         n = lib().lvn_meshgen_debug_fetch(self._h, what, chunk, buf.ctypes.data, buf.nbytes)
@@ -648,6 +659,44 @@ class Surrogate:
         _check(lib().lvn_surrogate_eval(self._h, pts.ctypes.data, pts.shape[0], out.ctypes.data, LVN_MEMORY_HOST),
                "lvn_surrogate_eval")
         return out
+
+
+LVN_CUCKOO_REFERENCE_FIND = 1
+LVN_FAULT_NONE, LVN_FAULT_DEVICE_ALLOC, LVN_FAULT_HASH_FAMILY = 0, 1, 2
+
+
+def debug_cuckoo(keys, prime=0, reference_find=False, with_table=False):
+    """The device cuckoo table of the meshing stages over `keys` (distinct
+    uint32, value = index): returns (values found per key, ~0 = missing,
+    info = (prime, stash used, parameter draws, insert failed), table + stash
+    or None)."""
+    k = np.ascontiguousarray(keys, np.uint32)
+    vals = np.zeros(max(k.size, 1), np.uint32)
+    info = (C.c_int32 * 4)()
+    p = prime or 0
+    slots = 0
+    if with_table:
+        if not p:
+            p = next_prime(max(2048, 2 * k.size))
+        slots = p + 101
+    table = np.zeros(max(slots, 1), np.uint64)
+    rc = lib().lvn_debug_cuckoo(k.ctypes.data, k.size, p, LVN_CUCKOO_REFERENCE_FIND if reference_find else 0,
+                                vals.ctypes.data, table.ctypes.data if with_table else None, slots, info)
+    _check(rc, "lvn_debug_cuckoo")
+    return vals[:k.size], tuple(info), (table if with_table else None)
+
+
+def next_prime(n):
+    """FindNextPrime (primes.cpp:32-58): the smallest prime >= n."""
+    x = max(n, 2)
+    while any(x % d == 0 for d in range(2, int(x ** 0.5) + 1)):
+        x += 1
+    return x
+
+
+def inject_fault(what, count=1):
+    """Host-side fault injection for the failure paths (test hook)."""
+    _check(lib().lvn_debug_inject_fault(what, count), "lvn_debug_inject_fault")
 
 
 def density_f64(points):

@@ -39,6 +39,12 @@ namespace {
 // buffers
 // ---------------------------------------------------------------------------
 
+// Host-side fault injection (lvn_debug_inject_fault): how many of the next
+// device allocations fail, and how many of the next hash-parameter draws
+// return a degenerate family.  Test hooks; both stay 0 in normal use.
+int g_fault_device_alloc = 0;
+int g_fault_hash_family = 0;
+
 struct DevBuf {
     void* p = nullptr;
     size_t bytes = 0;
@@ -47,6 +53,10 @@ struct DevBuf {
         if (p) cudaFree(p);
         p = nullptr;
         bytes = 0;
+        if (g_fault_device_alloc > 0) {  // an injected allocation failure
+            g_fault_device_alloc--;
+            return cudaErrorMemoryAllocation;
+        }
         const size_t alloc = std::max<size_t>(need, 256);
         cudaError_t e = cudaMalloc(&p, alloc);
         if (e == cudaSuccess) bytes = alloc;
@@ -263,6 +273,33 @@ void lod_colour(int s, float c[3]) {
 void draw_params(uint32_t* p) {
     std::uniform_int_distribution<uint32_t> dist(1u << 15, 1u << 30);
     for (int i = 0; i < CUCKOO_HASH_FN_COUNT * 2; i++) p[i] = dist(g.hash_gen);
+    if (g_fault_hash_family > 0) {
+        // injected: a = 0 and one b for every function, so all keys share one
+        // slot and one stash entry and a third key cannot be inserted
+        g_fault_hash_family--;
+        for (int i = 0; i < CUCKOO_HASH_FN_COUNT * 2; i++) p[i] = (i & 1) ? 1u << 15 : 0u;
+    }
+}
+
+// FindNextPrime (primes.cpp:32-58) on the host
+int host_next_prime(int n) {
+    auto is_prime = [](int x) {
+        int o = 4, i = 5;
+        for (;;) {
+            const int q = x / i;
+            if (q < i) return true;
+            if (x == q * i) return false;
+            o ^= 6;
+            i += o;
+        }
+    };
+    if (n <= 5) return n <= 2 ? 2 : n == 3 ? 3 : 5;
+    const int k = n / 6;
+    int i = n - 6 * k;
+    const int o = i < 2 ? 1 : 5;
+    int x = 6 * k + o;
+    for (i = (3 + o) / 2; !is_prime(x); x += i) i ^= 6;
+    return x;
 }
 
 }  // namespace
@@ -859,8 +896,10 @@ int surrogate_prologue(lvn_meshgen* m, const std::vector<ChunkDesc>& descs, size
     int k = 0;
     for (int c = 0; c < n; c++) {
         const ChunkDesc& d = descs[c];
+        // x and z must lie in the domain; above and below its y range the
+        // surrogate extrapolates (k_mlp_infer)
         bool inside = m->h_gate.as<int32_t>()[c] != 0;
-        for (int a = 0; a < 3 && inside; a++)
+        for (int a = 0; a < 3 && inside; a += 2)
             inside = (float)d.off[a] >= lo[a] && (float)(d.off[a] + d.scale * (FD - 1)) <= hi[a];
         slot[c] = inside ? k++ : -1;
         if (inside) lat.insert(lat.end(), {(float)d.off[0], (float)d.off[1], (float)d.off[2], (float)d.scale});
@@ -1195,28 +1234,8 @@ int mesh_from_field(lvn_meshgen* m, const int32_t min[3], int32_t size, FieldEnt
         cs.num_edges = f.num_edges;
         cs.edge_prime = 0;
         if (f.num_edges > 0) {
-            // FindNextPrime (primes.cpp:32-58) on the host for the cached path
-            auto is_prime = [](int x) {
-                int o = 4, i = 5;
-                for (;;) {
-                    const int q = x / i;
-                    if (q < i) return true;
-                    if (x == q * i) return false;
-                    o ^= 6;
-                    i += o;
-                }
-            };
-            const int nn = std::max((int)CUCKOO_MIN_TABLE_SIZE, f.num_edges * 2);
-            int x;
-            if (nn <= 5) x = nn <= 2 ? 2 : nn == 3 ? 3 : 5;
-            else {
-                const int k = nn / 6;
-                int i = nn - 6 * k;
-                const int o = i < 2 ? 1 : 5;
-                x = 6 * k + o;
-                for (i = (3 + o) / 2; !is_prime(x); x += i) i ^= 6;
-            }
-            cs.edge_prime = (uint32_t)x;
+            // FindNextPrime on the host for the cached path
+            cs.edge_prime = (uint32_t)host_next_prime(std::max((int)CUCKOO_MIN_TABLE_SIZE, f.num_edges * 2));
         }
         BatchState bs;
         std::memset(&bs, 0, sizeof(bs));
@@ -1601,11 +1620,14 @@ int lvn_meshgen_generate_chunks(lvn_meshgen* m, const lvn_chunk_desc* chunks, in
         LVN_CK(cudaEventCreateWithFlags(&m->ev_side, cudaEventDisableTiming));
     }
     rc = run_fresh_batch(m, descs, brushes, dev ? out : nullptr, use_direct ? &direct : nullptr);
-    const BatchState& bs = *m->h_bs.as<BatchState>();
-    const bool simp = m->simp_threshold >= 0.f;
-    out->total_vertices = simp ? bs.total_simp_verts : bs.total_nodes;
-    out->total_triangles = simp ? bs.total_simp_tris : 2 * (int64_t)bs.total_quads;
-    out->total_seams = bs.total_seams;
+    out->total_vertices = out->total_triangles = out->total_seams = 0;
+    if (m->h_bs.p) {  // absent when the first pool allocation failed
+        const BatchState& bs = *m->h_bs.as<BatchState>();
+        const bool simp = m->simp_threshold >= 0.f;
+        out->total_vertices = simp ? bs.total_simp_verts : bs.total_nodes;
+        out->total_triangles = simp ? bs.total_simp_tris : 2 * (int64_t)bs.total_quads;
+        out->total_seams = bs.total_seams;
+    }
     if (rc) return rc;
     if (out->chunks) fill_results(m, n, out->chunks);
     if (!dev && !use_direct) {
@@ -1760,6 +1782,80 @@ int64_t lvn_meshgen_debug_fetch(lvn_meshgen* m, int32_t what, int32_t chunk, voi
     return count;
 }
 
+int lvn_meshgen_qef_fp64_error(lvn_meshgen* m, double out[3]) {
+    if (!m || !out) return LVN_ERR_INVALID;
+    if (!m->last_fresh || m->last_n <= 0) return LVN_ERR_INVALID;
+    BatchPtrs b = make_ptrs(m, m->last_n);
+    DevBuf stats;
+    LVN_CK(stats.ensure(sizeof(unsigned long long) * 3));
+    LVN_CK(cudaMemsetAsync(stats.p, 0, sizeof(unsigned long long) * 3, m->stream));
+    LVN_CK(launch_leaf_qef_check(b, stats.as<unsigned long long>(), m->stream));
+    unsigned long long h[3];
+    const cudaError_t e = cudaMemcpyAsync(h, stats.p, sizeof(h), cudaMemcpyDeviceToHost, m->stream);
+    const cudaError_t e2 = e == cudaSuccess ? cudaStreamSynchronize(m->stream) : e;
+    stats.release();
+    LVN_CK(e2);
+    double mx, sum;
+    std::memcpy(&mx, &h[0], 8);
+    std::memcpy(&sum, &h[1], 8);
+    out[0] = mx;
+    out[1] = h[2] ? sum / (double)h[2] : 0.0;
+    out[2] = (double)h[2];
+    return LVN_OK;
+}
+
+int lvn_debug_inject_fault(int32_t what, int32_t count) {
+    if (count < 0) return LVN_ERR_INVALID;
+    switch (what) {
+        case LVN_FAULT_NONE: g_fault_device_alloc = 0; g_fault_hash_family = 0; return LVN_OK;
+        case LVN_FAULT_DEVICE_ALLOC: g_fault_device_alloc = count; return LVN_OK;
+        case LVN_FAULT_HASH_FAMILY: g_fault_hash_family = count; return LVN_OK;
+        default: return LVN_ERR_INVALID;
+    }
+}
+
+int lvn_debug_cuckoo(const uint32_t* keys, int32_t n, uint32_t prime, int32_t flags, uint32_t* values,
+                     uint64_t* table_out, int64_t table_capacity, int32_t info[4]) {
+    if (!g.initialised) return LVN_ERR_NOT_INITIALISED;
+    if (!keys || !values || !info || n <= 0 || (flags & ~LVN_CUCKOO_REFERENCE_FIND)) return LVN_ERR_INVALID;
+    if (prime == 0) prime = (uint32_t)host_next_prime(std::max((int)CUCKOO_MIN_TABLE_SIZE, 2 * n));
+    if (prime < 2 || prime > (1u << 30)) return LVN_ERR_INVALID;
+    const int64_t slots = (int64_t)prime + CUCKOO_STASH_SIZE;
+    if (table_out && table_capacity < slots) return LVN_ERR_CAPACITY;
+    DevBuf d_keys, d_table, d_status, d_values;
+    LVN_CK(d_keys.ensure(sizeof(uint32_t) * n));
+    LVN_CK(d_table.ensure(sizeof(unsigned long long) * slots));
+    LVN_CK(d_status.ensure(sizeof(int) * 2));
+    LVN_CK(d_values.ensure(sizeof(uint32_t) * n));
+    struct Release {
+        DevBuf* b[4];
+        ~Release() { for (DevBuf* x : b) x->release(); }
+    } release{{&d_keys, &d_table, &d_status, &d_values}};
+    LVN_CK(cudaMemcpy(d_keys.p, keys, sizeof(uint32_t) * n, cudaMemcpyHostToDevice));
+    cudaStream_t stream = nullptr;  // the legacy default stream: a test hook
+    int status[2] = {0, 0};
+    int attempt = 0;
+    CuckooParams cp;
+    for (; attempt < kMaxHashRetries; attempt++) {
+        draw_params(cp.p);  // Cuckoo_InitialiseTable's parameters (compute_cuckoo.cpp:62-67)
+        LVN_CK(cudaMemsetAsync(d_status.p, 0, sizeof(int) * 2, stream));
+        LVN_CK(launch_debug_cuckoo(d_keys.as<uint32_t>(), n, d_table.as<unsigned long long>(), prime, cp,
+                                   d_status.as<int>(), (flags & LVN_CUCKOO_REFERENCE_FIND) ? 1 : 0,
+                                   d_values.as<uint32_t>(), stream));
+        LVN_CK(cudaMemcpyAsync(status, d_status.p, sizeof(status), cudaMemcpyDeviceToHost, stream));
+        LVN_CK(cudaStreamSynchronize(stream));
+        if (!status[1]) break;
+    }
+    info[0] = (int32_t)prime;
+    info[1] = status[0];
+    info[2] = std::min(attempt + 1, kMaxHashRetries);
+    info[3] = status[1];
+    if (status[1]) return LVN_ERR_HASH;
+    LVN_CK(cudaMemcpy(values, d_values.p, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+    if (table_out) LVN_CK(cudaMemcpy(table_out, d_table.p, sizeof(uint64_t) * slots, cudaMemcpyDeviceToHost));
+    return LVN_OK;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
@@ -1806,6 +1902,7 @@ void density_fields(const DensityParams& d, int32_t default_material, float* ban
 GlobalView global_view() {
     GlobalView v;
     v.initialised = g.initialised;
+    v.device = g.device;
     v.num_sms = g.num_sms;
     v.default_material = g.default_material;
     v.perm = g.perm.as<uint8_t>();

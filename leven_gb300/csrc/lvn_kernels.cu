@@ -269,9 +269,9 @@ __device__ __forceinline__ float dot4(float ax, float ay, float az, float aw, fl
 __device__ __forceinline__ void givens_coeffs_sym(float a_pp, float a_pq, float a_qq, float& c, float& s) {
     if (a_pq == 0.f) { c = 1.f; s = 0.f; return; }
     const float tau = (a_qq - a_pp) / (2.f * a_pq);
-    const float stt = sqrtf(fmaf(tau, tau, 1.f));
+    const float stt = sqrtf(1.f + tau * tau);
     const float tn = 1.f / ((tau >= 0.f) ? (tau + stt) : (tau - stt));
-    c = 1.f / sqrtf(fmaf(tn, tn, 1.f));
+    c = 1.f / sqrtf(1.f + tn * tn);
     s = tn * c;
 }
 
@@ -740,7 +740,8 @@ __global__ void __launch_bounds__(kProbes) k_gate(BatchPtrs b) {
     if (p == 0) bad = 0;
     __syncthreads();
     const size_t i = (size_t)c * kProbes + p;
-    if (!(fabsf(b.probe_s[i] - b.probe_plain[i]) <= b.gate)) bad = 1;
+    // the gate is in voxels of the chunk: scale density units per voxel
+    if (!(fabsf(b.probe_s[i] - b.probe_plain[i]) <= b.gate * (float)b.desc[c].scale)) bad = 1;
     __syncthreads();
     if (p == 0) b.gate_ok[c] = bad ? 0 : 1;
 }
@@ -1497,6 +1498,204 @@ __global__ void __launch_bounds__(kThreads) k_node_insert(BatchPtrs b) {
         if (r == 1) st->node_stash_used = 1;
         if (r < 0) st->node_insert_failed = 1;
     }
+}
+
+// Test hook over an arbitrary key list: the same cuckoo_insert and
+// HashView::find the meshing stages run (one table, value = key index).
+__global__ void k_debug_cuckoo_fill(unsigned long long* table, int64_t slots) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < slots; i += (int64_t)gridDim.x * blockDim.x)
+        table[i] = CUCKOO_EMPTY;
+}
+
+__global__ void k_debug_cuckoo_insert(const uint32_t* keys, int n, unsigned long long* table, uint32_t prime,
+                                      uint32_t magic, CuckooParams cp, int* status) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int r = cuckoo_insert(table, table + prime, prime, magic, cp.p, keys[i], (uint32_t)i);
+        if (r == 1) atomicOr(&status[0], 1);
+        if (r < 0) atomicOr(&status[1], 1);
+    }
+}
+
+__global__ void k_debug_cuckoo_find(const uint32_t* keys, int n, const unsigned long long* table, uint32_t prime,
+                                    uint32_t magic, CuckooParams cp, const int* status, int reference_find,
+                                    uint32_t* values) {
+    HashView hv;
+    hv.table = table;
+    hv.stash = table + prime;
+    hv.prime = prime;
+    hv.magic = magic;
+    hv.stash_used = status[0];
+#pragma unroll
+    for (int k = 0; k < 10; k++) hv.p[k] = cp.p[k];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t key = keys[i];
+        if (!reference_find) {
+            values[i] = hv.find(key);
+            continue;
+        }
+        // Cuckoo_Find as written: the stash probe reads data[h] (cuckoo.cl:93-101)
+        uint32_t v = ~0u;
+        for (int f = 0; f < CUCKOO_STASH_HASH_INDEX && v == ~0u; f++) {
+            const unsigned long long e = table[cuckoo_hash(key, cp.p[2 * f], cp.p[2 * f + 1], prime, magic)];
+            if ((uint32_t)e == key) v = (uint32_t)(e >> 32);
+        }
+        if (v == ~0u && hv.stash_used) {
+            const unsigned long long e = table[stash_hash(key, cp.p[8], cp.p[9])];
+            if ((uint32_t)e == key) v = (uint32_t)(e >> 32);
+        }
+        values[i] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The FP32 leaf solve against an FP64 solve of the same crossings: the
+// leaves' inputs gathered as k_leaf gathers them, qef_add_point
+// (qef.cl:170-191) accumulated in double, and qef_solve (qef.cl:239-256) with
+// its ten Jacobi sweeps, 0.1 truncation and mass-point bias in double.  The
+// FP32 solve is the same qef_solve k_leaf runs on the same inputs.  Reports
+// the distance in voxels of the leaf's chunk: max (as the bits of a
+// non-negative double), sum and count.  A measurement pass, not a stage.
+// ---------------------------------------------------------------------------
+
+__device__ void qef_solve_f64(const double ata[6], const double atb[3], const double mpsum[4], double out[3]) {
+    const double w = fmax(mpsum[3], 1.0);
+    const double mp[3] = {mpsum[0] / w, mpsum[1] / w, mpsum[2] / w};
+    const double amp[3] = {atb[0] - (ata[0] * mp[0] + ata[1] * mp[1] + ata[2] * mp[2]),
+                           atb[1] - (ata[1] * mp[0] + ata[3] * mp[1] + ata[4] * mp[2]),
+                           atb[2] - (ata[2] * mp[0] + ata[4] * mp[1] + ata[5] * mp[2])};
+    double V[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    double vt[3][3] = {{ata[0], ata[1], ata[2]}, {0, ata[3], ata[4]}, {0, 0, ata[5]}};
+    const int pa[3] = {0, 0, 1}, pb[3] = {1, 2, 2};
+    for (int it = 0; it < 10; it++)
+        for (int r = 0; r < 3; r++) {
+            const int a = pa[r], bq = pb[r];
+            if (vt[a][bq] == 0.0) continue;
+            const double tau = (vt[bq][bq] - vt[a][a]) / (2.0 * vt[a][bq]);
+            const double stt = sqrt(1.0 + tau * tau);
+            const double tn = 1.0 / (tau >= 0.0 ? tau + stt : tau - stt);
+            const double c = 1.0 / sqrt(1.0 + tn * tn), sn = tn * c;
+            const double cc = c * c, ss = sn * sn, mx = 2.0 * c * sn * vt[a][bq];
+            const double u = vt[a][a], v = vt[bq][bq];
+            vt[a][a] = cc * u - mx + ss * v;
+            vt[bq][bq] = ss * u + mx + cc * v;
+            const double x = vt[0][3 - bq], y = vt[1 - a][2];
+            vt[0][3 - bq] = c * x - sn * y;
+            vt[1 - a][2] = sn * x + c * y;
+            vt[a][bq] = 0.0;
+            for (int k = 0; k < 3; k++) {
+                const double pv = V[k][a], qv = V[k][bq];
+                V[k][a] = c * pv - sn * qv;
+                V[k][bq] = sn * pv + c * qv;
+            }
+        }
+    double d[3];
+    for (int k = 0; k < 3; k++) {
+        const double x = vt[k][k];
+        d[k] = (fabs(x) < 0.1 || fabs(1.0 / x) < 0.1) ? 0.0 : 1.0 / x;
+    }
+    for (int r = 0; r < 3; r++) {
+        double x = 0.0;
+        for (int c = 0; c < 3; c++) x += (V[r][0] * d[0] * V[c][0] + V[r][1] * d[1] * V[c][1] + V[r][2] * d[2] * V[c][2]) * amp[c];
+        out[r] = x + mp[r];
+    }
+}
+
+template <int VPC>
+__global__ void __launch_bounds__(256) k_leaf_qef_check(BatchPtrs b, unsigned long long* stats) {
+    if (b.bs->overflow) return;
+    const int total = b.bs->total_nodes;
+    double local_max = 0.0, local_sum = 0.0;
+    unsigned long long local_n = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int c = b.node_chunk[i];
+        const ChunkState& st = b.cs[c];
+        const ChunkDesc& d = b.desc[c];
+        HashView hv;
+        hv.prime = st.edge_prime;
+        hv.magic = st.edge_magic;
+        hv.table = b.edge_slots + st.edge_table_off;
+        hv.stash = hv.table + hv.prime;
+        hv.stash_used = st.edge_stash_used;
+        for (int k = 0; k < 10; k++) hv.p[k] = d.edge_params[k];
+        const float4* info = b.edge_info + st.edge_off;
+        int x, y, z;
+        position_for_code<VPC>(b.node_codes[i], x, y, z);
+        const int edge_list = b.node_info[i] >> 16;
+        const float fs = (float)d.scale;
+        Qef q;
+        for (int k = 0; k < 6; k++) q.ata[k] = 0.f;
+        q.atb[0] = q.atb[1] = q.atb[2] = 0.f;
+        q.mp[0] = q.mp[1] = q.mp[2] = q.mp[3] = 0.f;
+        double ata[6] = {0, 0, 0, 0, 0, 0}, atb[3] = {0, 0, 0}, mp[4] = {0, 0, 0, 0};
+        for (int e = 0; e < 12; e++) {
+            if (!((edge_list >> e) & 1)) continue;
+            const int e0 = edge_c0(e), e1 = edge_c1(e);
+            const int o0x = e0 >> 2, o0y = (e0 >> 1) & 1, o0z = e0 & 1;
+            const int o1x = e1 >> 2, o1y = (e1 >> 1) & 1, o1z = e1 & 1;
+            const uint32_t di = hv.find((uint32_t)edge_key<VPC>(x + o0x, y + o0y, z + o0z, e / 4));
+            if (di == ~0u) continue;
+            const float4 ed = info[di];
+            const float p0x = (float)x + (float)o0x, p0y = (float)y + (float)o0y, p0z = (float)z + (float)o0z;
+            const float p1x = (float)x + (float)o1x, p1y = (float)y + (float)o1y, p1z = (float)z + (float)o1z;
+            const float px = fs * fmaf(p1x - p0x, ed.w, p0x);
+            const float py = fs * fmaf(p1y - p0y, ed.w, p0y);
+            const float pz = fs * fmaf(p1z - p0z, ed.w, p0z);
+            const float pw = fs * fmaf(0.f - 0.f, ed.w, 0.f);
+            const float nx = ed.x, ny = ed.y, nzv = ed.z;
+            q.ata[0] += nx * nx;
+            q.ata[1] += nx * ny;
+            q.ata[2] += nx * nzv;
+            q.ata[3] += ny * ny;
+            q.ata[4] += ny * nzv;
+            q.ata[5] += nzv * nzv;
+            const float bb = dot4(px, py, pz, pw, nx, ny, nzv, 0.f);
+            q.atb[0] += nx * bb;
+            q.atb[1] += ny * bb;
+            q.atb[2] += nzv * bb;
+            q.mp[0] += px;
+            q.mp[1] += py;
+            q.mp[2] += pz;
+            q.mp[3] += 1.f;
+            // the same crossing and normal in double
+            const double t = ed.w, sd = d.scale;
+            const double P[3] = {sd * (p0x + (p1x - p0x) * t), sd * (p0y + (p1y - p0y) * t), sd * (p0z + (p1z - p0z) * t)};
+            const double N[3] = {nx, ny, nzv};
+            ata[0] += N[0] * N[0];
+            ata[1] += N[0] * N[1];
+            ata[2] += N[0] * N[2];
+            ata[3] += N[1] * N[1];
+            ata[4] += N[1] * N[2];
+            ata[5] += N[2] * N[2];
+            const double bd = P[0] * N[0] + P[1] * N[1] + P[2] * N[2];
+            for (int k = 0; k < 3; k++) atb[k] += N[k] * bd;
+            for (int k = 0; k < 3; k++) mp[k] += P[k];
+            mp[3] += 1.0;
+        }
+        const float mw = q.mp[3];
+        q.mp[0] = q.mp[0] / mw;
+        q.mp[1] = q.mp[1] / mw;
+        q.mp[2] = q.mp[2] / mw;
+        q.mp[3] = q.mp[3] / mw;
+        float ox, oy, oz;
+        qef_solve(q, ox, oy, oz);
+        const float wx = fmaf(ox, (float)LEAF_SIZE_SCALE, (float)d.min[0]);
+        const float wy = fmaf(oy, (float)LEAF_SIZE_SCALE, (float)d.min[1]);
+        const float wz = fmaf(oz, (float)LEAF_SIZE_SCALE, (float)d.min[2]);
+        double o64[3];
+        qef_solve_f64(ata, atb, mp, o64);
+        const double dx = wx - (o64[0] * LEAF_SIZE_SCALE + d.min[0]);
+        const double dy = wy - (o64[1] * LEAF_SIZE_SCALE + d.min[1]);
+        const double dz = wz - (o64[2] * LEAF_SIZE_SCALE + d.min[2]);
+        const double err = sqrt(dx * dx + dy * dy + dz * dz) / (LEAF_SIZE_SCALE * (double)d.scale);
+        if (err == err) {
+            local_max = fmax(local_max, err);
+            local_sum += err;
+            local_n++;
+        }
+    }
+    atomicMax(&stats[0], (unsigned long long)__double_as_longlong(local_max));
+    atomicAdd(reinterpret_cast<double*>(&stats[1]), local_sum);
+    atomicAdd(&stats[2], local_n);
 }
 
 // CreateLeafNodes + SolveQEFs + GenerateMeshVertexBuffer (octree.cl:236-331, 475-487)
@@ -2419,6 +2618,24 @@ cudaError_t launch_mesh_scatter(const BatchPtrs& b, cudaStream_t s) {
         LVN_VPC_DISPATCH(b.vpc, (k_mesh_scatter<V, false><<<persistent_grid(b, ST_MESH_SCATTER, 8), kNodeTile, 0,
                                                            s>>>(b)));
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_debug_cuckoo(const uint32_t* keys, int n, unsigned long long* table, uint32_t prime,
+                                CuckooParams params, int* status, int reference_find, uint32_t* values,
+                                cudaStream_t s) {
+    if (n <= 0 || prime < 2) return cudaErrorInvalidValue;
+    const uint32_t magic = 0xffffffffu / prime;
+    const int64_t slots = (int64_t)prime + CUCKOO_STASH_SIZE;
+    k_debug_cuckoo_fill<<<(int)std::min<int64_t>((slots + 255) / 256, 1024), 256, 0, s>>>(table, slots);
+    const int grid = std::min((n + 255) / 256, 1024);
+    k_debug_cuckoo_insert<<<grid, 256, 0, s>>>(keys, n, table, prime, magic, params, status);
+    k_debug_cuckoo_find<<<grid, 256, 0, s>>>(keys, n, table, prime, magic, params, status, reference_find, values);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_leaf_qef_check(const BatchPtrs& b, unsigned long long* stats, cudaStream_t s) {
+    LVN_VPC_DISPATCH(b.vpc, (k_leaf_qef_check<V><<<b.num_sms * 4, 256, 0, s>>>(b, stats)));
     return cudaGetLastError();
 }
 

@@ -197,4 +197,21 @@ cudaError_t launch_export(const BatchPtrs& b, int which, void* dst, int64_t capa
 // the whole simplification pass (level grids reset, levels, map, plan, scatter)
 cudaError_t launch_simplify(const BatchPtrs& b, cudaStream_t stream);
 
+// Measurement pass over the last batch's leaves: the FP32 solve k_leaf runs
+// against an FP64 solve of the same crossings.  stats (zeroed by the caller):
+// [0] max distance in voxels (double bits), [1] sum (double), [2] leaves.
+cudaError_t launch_leaf_qef_check(const BatchPtrs& b, unsigned long long* stats, cudaStream_t stream);
+
+// Test hook: the meshing stages' cuckoo insert and find over an arbitrary key
+// list.  table holds prime + CUCKOO_STASH_SIZE slots; status[0] = a key went
+// to the stash, status[1] = an insert failed.  reference_find probes the main
+// table at the stash index instead of the stash, as Cuckoo_Find does
+// (cuckoo.cl:93-101).
+struct CuckooParams {
+    uint32_t p[CUCKOO_HASH_FN_COUNT * 2];
+};
+cudaError_t launch_debug_cuckoo(const uint32_t* keys, int n, unsigned long long* table, uint32_t prime,
+                                CuckooParams params, int* status, int reference_find, uint32_t* values,
+                                cudaStream_t stream);
+
 }  // namespace lvn

@@ -4,19 +4,21 @@
 // Who needs it: an engine thread that cannot call cudaMalloc / cudaFree.
 // cudaFree synchronises the whole device and cudaMalloc can stall on the
 // driver's allocator, which a frame-locked render or streaming thread cannot
-// afford; engines that budget GPU memory up front forbid allocation after
-// start-up; and work recorded into a CUDA graph cannot allocate with the
-// plain allocator.  Such callers pass their own input and output memory and
-// get the same mesh as lvn_meshgen_generate_chunk_mesh with caching off.
+// afford; and engines that budget GPU memory up front forbid allocation after
+// start-up.  Such callers pass their own input and output memory and get the
+// same mesh as lvn_meshgen_generate_chunk_mesh with caching off.  The call
+// reads its counters back and synchronises its stream before it returns.
 //
 // Every buffer the pipeline needs between its kernels (field corners, edge
 // list, cuckoo tables, leaf and quad lists, output staging) lives in one
 // file-scope device array of LVN_NOALLOC_SCRATCH_BYTES, held by every GPU
 // that loads the library until the process exits.  Its fixed capacities
 // (LVN_NOALLOC_MAX_*) bound the chunks it accepts; larger ones are rejected
-// with LVN_ERR_CAPACITY.  All calls share the array and each call rewrites
-// what it reads, so calls must not overlap on the GPU: two calls in flight at
-// once (different streams or host threads) race on it.
+// with LVN_ERR_CAPACITY.  All calls, from every host thread, share the array
+// and each call rewrites what it reads, so calls must not overlap on the GPU:
+// two calls in flight at once (different streams or host threads) race on it.
+// The call runs on the device lvn_init ran on (the permutation tables live
+// there); with another device current it returns LVN_ERR_INVALID.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -74,23 +76,30 @@ static_assert(OFF_END <= (size_t)LVN_NOALLOC_SCRATCH_BYTES, "scratch layout exce
 // device address comes from cudaGetSymbolAddress, once per device.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[LVN_NOALLOC_SCRATCH_BYTES];
 
-constexpr int kMaxDevices = 64;
-unsigned char* g_scratch_ptr[kMaxDevices] = {};
+// The scratch array's device address, looked up on the first call (with the
+// init device current) and kept for the device it was looked up on.
+int g_scratch_dev = -1;
+unsigned char* g_scratch_ptr = nullptr;
 
-int scratch_for_current_device(unsigned char** out) {
+int scratch_for_init_device(int init_device, unsigned char** out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return LVN_ERR_NO_DEVICE;
-    if (dev < 0 || dev >= kMaxDevices) return LVN_ERR_NO_DEVICE;
-    if (!g_scratch_ptr[dev]) {
+    if (dev != init_device) {
+        std::fprintf(stderr, "liblvn: noalloc: device %d is current, but lvn_init ran on device %d\n", dev,
+                     init_device);
+        return LVN_ERR_INVALID;
+    }
+    if (g_scratch_dev != dev || !g_scratch_ptr) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) {
             std::fprintf(stderr, "liblvn: cudaGetSymbolAddress(noalloc scratch) failed: %s\n", cudaGetErrorString(e));
             return LVN_ERR_CUDA;
         }
-        g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
+        g_scratch_ptr = static_cast<unsigned char*>(p);
+        g_scratch_dev = dev;
     }
-    *out = g_scratch_ptr[dev];
+    *out = g_scratch_ptr;
     return LVN_OK;
 }
 
@@ -117,7 +126,7 @@ extern "C" int lvn_generate_chunk_mesh_noalloc(const int32_t min[3], int32_t siz
     cudaStream_t stream = static_cast<cudaStream_t>(cuda_stream);
 
     unsigned char* base = nullptr;
-    int rc = scratch_for_current_device(&base);
+    int rc = scratch_for_init_device(gv.device, &base);
     if (rc) return rc;
 
     // chunk descriptor and its stored operations, on the stack

@@ -9,6 +9,7 @@ namespace lvn {
 
 struct GlobalView {
     bool initialised;
+    int device;            // the CUDA device lvn_init ran on; every table below lives there
     int num_sms;
     int32_t default_material;
     const uint8_t* perm;   // device permutation image (65536 B)

@@ -313,8 +313,13 @@ __device__ __forceinline__ float unit(uint64_t h) { return (float)(h >> 40) * (1
 // 70% of the samples within 4 voxels of the heightfield surface (y = amp h +
 // U(-4, 4), so |d| <= 4 for the heightfield), 30% uniform in the domain;
 // target = the plain density.
+// 70% within 4 voxels of the zero set, 30% uniform in the domain.  Without a
+// 3D term the zero set is the height surface, y = amp h(x, z) + U(-4, 4).
+// With one (caves), the zero set lies within `band` of that surface: up to
+// eight heights y = amp h + U(-band - 4, band + 4) are tried and the first
+// with |density| <= 4 is kept (else the last).
 __global__ void k_samples(float4* out, int n, uint64_t seed, Domain dom, const uint8_t* perm_t3,
-                          const float* grad, DensityParams dp) {
+                          const float* grad, DensityParams dp, float band) {
     __shared__ __align__(16) float sg[64];
     if (threadIdx.x < 64) sg[threadIdx.x] = grad[threadIdx.x];
     __syncthreads();
@@ -324,10 +329,26 @@ __global__ void k_samples(float4* out, int n, uint64_t seed, Domain dom, const u
         const uint64_t h2 = mix64(seed ^ mix64((uint64_t)i * 4 + 2)), h3 = mix64(seed ^ mix64((uint64_t)i * 4 + 3));
         const float x = dom.lo[0] + unit(h1) * (dom.hi[0] - dom.lo[0]);
         const float z = dom.lo[2] + unit(h2) * (dom.hi[2] - dom.lo[2]);
-        float y;
-        if (unit(h0) < 0.7f) y = nz.height_amp(dp) * nz.height(dp, x, z) + (unit(h3) * 8.f - 4.f);
-        else y = dom.lo[1] + unit(h3) * (dom.hi[1] - dom.lo[1]);
-        out[i] = make_float4(x, y, z, nz.density(dp, x, y, z));
+        float y, d;
+        if (unit(h0) < 0.7f) {
+            const float surf = nz.height_amp(dp) * nz.height(dp, x, z);
+            if (band > 0.f) {
+                uint64_t h = h3;
+                for (int k = 0; k < 8; k++) {
+                    y = surf + (unit(h) * 2.f - 1.f) * (band + 4.f);
+                    d = nz.density(dp, x, y, z);
+                    if (fabsf(d) <= 4.f) break;
+                    h = mix64(h ^ 0x9E3779B97F4A7C15ull);
+                }
+            } else {
+                y = surf + (unit(h3) * 8.f - 4.f);
+                d = nz.density(dp, x, y, z);
+            }
+        } else {
+            y = dom.lo[1] + unit(h3) * (dom.hi[1] - dom.lo[1]);
+            d = nz.density(dp, x, y, z);
+        }
+        out[i] = make_float4(x, y, z, d);
     }
 }
 
@@ -580,6 +601,13 @@ __global__ void __launch_bounds__(128 * kInferWG, 1) k_mlp_infer(InferArgs a) {
                 c[2] = q.z;
             }
         }
+        // Above and below the domain's y range the density is extrapolated
+        // with unit slope from the range's edge (d = y - h(x, z) + caves has
+        // slope 1 away from the surface band), so tall coarse chunks whose
+        // surface lies inside the range keep the right sign everywhere.
+        const float yc = fminf(fmaxf(c[1], a.dom.lo[1]), a.dom.hi[1]);
+        const float y_out = c[1] - yc;
+        c[1] = yc;
         // features -> this row of the activation tile (12 core-matrix columns)
 #pragma unroll
         for (int ax = 0; ax < 3; ax++) {
@@ -645,7 +673,7 @@ __global__ void __launch_bounds__(128 * kInferWG, 1) k_mlp_infer(InferArgs a) {
                 }
             }
         }
-        if (ok && p < a.n) a.out[p] = y * a.out_scale;
+        if (ok && p < a.n) a.out[p] = fmaf(y, a.out_scale, y_out);
     }
     if (!ok && (threadIdx.x & 127) == 0) atomicExch(a.status, 1);
     tc_fence_before();
@@ -1037,8 +1065,11 @@ int lvn_surrogate_sample(lvn_surrogate* s, int64_t n, uint64_t seed, float* host
     if (!gv.initialised) return LVN_ERR_NOT_INITIALISED;
     int rc = s->pool.ensure(sizeof(float4) * (size_t)n);
     if (rc) return rc;
+    float band = 0.f;
+    int32_t dom_by_solid[9];
+    density_fields(gv.density, gv.default_material, &band, dom_by_solid);
     k_samples<<<gv.num_sms * 8, 256, 0, s->stream>>>(s->pool.as<float4>(), (int)n, seed, s->dom, gv.perm_t3,
-                                                     gv.grad, gv.density);
+                                                     gv.grad, gv.density, band);
     SG_CK(cudaGetLastError());
     s->pool_n = n;
     s->pool_next = 0;

@@ -233,3 +233,39 @@ def clipmap_caves(n_chunks=1024, max_lod=4, seed=1):
     nodes = sorted(chosen, key=lambda nd: (distance_to_node(nd[0], nd[1], cam0), nd[1], nd[0]))[:n_chunks]
     return Workload(f"clipmap-caves-{len(nodes)}chunks-lod0-{max_lod}", [(tuple(mn), size) for mn, size in nodes], [],
                     CAVES)
+
+
+def clipmap_sweep(n_chunks=4096, max_lod=5, n_ops=64, seed=1):
+    """The large clipmap sweep: n_chunks chunks over clipmap LODs 0..max_lod
+    (voxel sizes 1-32), caves density (2D fBm heightfield + 3D fBm caves, as
+    clipmap_caves), with n_ops seeded CSG operations stored and replayed per
+    chunk through the plain path.
+
+    Chunks: the union of SelectActiveClipmapNodes (2^15-unit world centred on
+    the origin) over a camera moving along a seeded straight path in steps of
+    256 * U[-1, 1] world units in x and z, until at least n_chunks nodes are
+    active, then the n_chunks nearest the starting camera.  Operations: as
+    csg_ops (half sphere-subtract, half box-union, radii / half extents U[2, 12]
+    voxels), centres uniform over the camera path's x / z box (density units,
+    widened by 64 voxels) and y in [-48, 48], the terrain's height band."""
+    rng = MT19937(seed)
+    cam0 = (rng.uniform(-2048.0, 2048.0), rng.uniform(-64.0, 64.0), rng.uniform(-2048.0, 2048.0))
+    step = (rng.uniform(-1.0, 1.0) * 256.0, 0.0, rng.uniform(-1.0, 1.0) * 256.0)
+    root_size = 1 << 15
+    root_min = (-root_size // 2, -root_size // 2, -root_size // 2)
+    chosen = {}
+    cams = []
+    for k in range(1024):
+        cam = tuple(cam0[i] + k * step[i] for i in range(3))
+        cams.append(cam)
+        for mn, size in select_clipmap_nodes(root_min, root_size, cam):
+            if size <= CLIPMAP_LEAF_SIZE << max_lod:
+                chosen[(mn, size)] = True
+        if len(chosen) >= n_chunks:
+            break
+    nodes = sorted(chosen, key=lambda nd: (distance_to_node(nd[0], nd[1], cam0), nd[1], nd[0]))[:n_chunks]
+    lo = [min(c[i] for c in cams) / 4.0 - 64.0 for i in (0, 2)]
+    hi = [max(c[i] for c in cams) / 4.0 + 64.0 for i in (0, 2)]
+    ops = csg_ops(n_ops, seed + 1000, (lo[0], -48.0, lo[1]), (hi[0], 48.0, hi[1]))
+    return Workload(f"clipmap-sweep-{len(nodes)}chunks-lod0-{max_lod}-caves-{n_ops}ops",
+                    [(tuple(mn), size) for mn, size in nodes], ops, CAVES)

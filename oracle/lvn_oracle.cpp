@@ -653,9 +653,9 @@ typedef float Mat3[3][3];
 void givens_coeffs_sym(float a_pp, float a_pq, float a_qq, float* c, float* s) {
     if (a_pq == 0.f) { *c = 1.f; *s = 0.f; return; }
     const float tau = (a_qq - a_pp) / (2.f * a_pq);
-    const float stt = std::sqrt(std::fmaf(tau, tau, 1.f));
+    const float stt = std::sqrt(1.f + tau * tau);
     const float tn = 1.f / ((tau >= 0.f) ? (tau + stt) : (tau - stt));
-    *c = 1.f / std::sqrt(std::fmaf(tn, tn, 1.f));
+    *c = 1.f / std::sqrt(1.f + tn * tn);
     *s = tn * (*c);
 }
 
@@ -747,6 +747,83 @@ F4 qef_solve(QEF q) {
     return x;
 }
 
+// FP64 restatement of the same leaf solve, for stating the FP32 solve's
+// error: qef_add_point (qef.cl:170-191) accumulated in double from the same
+// crossing points and normals, then qef_solve (qef.cl:239-256) with its
+// Jacobi sweeps (qef.cl:23-105), the pseudo-inverse truncation at 0.1
+// (svd_invdet, qef.cl:107-111) and the mass-point bias, all in double.  Ten
+// sweeps as qef.cl:16; in double they converge a 3x3 symmetric matrix fully.
+struct QEF64 {
+    double ata[6] = {0, 0, 0, 0, 0, 0};
+    double atb[3] = {0, 0, 0};
+    double mp[4] = {0, 0, 0, 0};
+};
+
+void qef64_add_point(QEF64& q, const double n[3], const double p[3]) {
+    q.ata[0] += n[0] * n[0];
+    q.ata[1] += n[0] * n[1];
+    q.ata[2] += n[0] * n[2];
+    q.ata[3] += n[1] * n[1];
+    q.ata[4] += n[1] * n[2];
+    q.ata[5] += n[2] * n[2];
+    const double b = p[0] * n[0] + p[1] * n[1] + p[2] * n[2];
+    for (int i = 0; i < 3; i++) q.atb[i] += n[i] * b;
+    for (int i = 0; i < 3; i++) q.mp[i] += p[i];
+    q.mp[3] += 1.0;
+}
+
+void svd64_rotate(double vtav[3][3], double v[3][3], int a, int b) {
+    if (vtav[a][b] == 0.0) return;
+    // givens_coeffs_sym (qef.cl:31-42)
+    const double tau = (vtav[b][b] - vtav[a][a]) / (2.0 * vtav[a][b]);
+    const double stt = std::sqrt(1.0 + tau * tau);
+    const double tn = 1.0 / (tau >= 0.0 ? tau + stt : tau - stt);
+    const double c = 1.0 / std::sqrt(1.0 + tn * tn), s = tn * c;
+    // svd_rotateq_xy / svd_rotate_xy (qef.cl:44-56), on the same entries as svd_rotate
+    const double cc = c * c, ss = s * s, mx = 2.0 * c * s * vtav[a][b];
+    const double u = vtav[a][a], w = vtav[b][b];
+    vtav[a][a] = cc * u - mx + ss * w;
+    vtav[b][b] = ss * u + mx + cc * w;
+    const double x = vtav[0][3 - b], y = vtav[1 - a][2];
+    vtav[0][3 - b] = c * x - s * y;
+    vtav[1 - a][2] = s * x + c * y;
+    vtav[a][b] = 0.0;
+    for (int r = 0; r < 3; r++) {
+        const double p = v[r][a], q = v[r][b];
+        v[r][a] = c * p - s * q;
+        v[r][b] = s * p + c * q;
+    }
+}
+
+inline double svd64_invdet(double x, double tol) {
+    return (std::fabs(x) < tol || std::fabs(1.0 / x) < tol) ? 0.0 : 1.0 / x;
+}
+
+void qef64_solve(QEF64 q, double out[3]) {
+    const double w = std::max(q.mp[3], 1.0);
+    const double mp[3] = {q.mp[0] / w, q.mp[1] / w, q.mp[2] / w};
+    const double* A = q.ata;
+    const double amp[3] = {q.atb[0] - (A[0] * mp[0] + A[1] * mp[1] + A[2] * mp[2]),
+                           q.atb[1] - (A[1] * mp[0] + A[3] * mp[1] + A[4] * mp[2]),
+                           q.atb[2] - (A[2] * mp[0] + A[4] * mp[1] + A[5] * mp[2])};
+    double V[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    double vtav[3][3] = {{A[0], A[1], A[2]}, {0, A[3], A[4]}, {0, 0, A[5]}};
+    for (int i = 0; i < 10; i++) {
+        svd64_rotate(vtav, V, 0, 1);
+        svd64_rotate(vtav, V, 0, 2);
+        svd64_rotate(vtav, V, 1, 2);
+    }
+    const double d[3] = {svd64_invdet(vtav[0][0], 0.1), svd64_invdet(vtav[1][1], 0.1), svd64_invdet(vtav[2][2], 0.1)};
+    for (int r = 0; r < 3; r++) {
+        double x = 0.0;
+        for (int c = 0; c < 3; c++) {
+            const double o = V[r][0] * d[0] * V[c][0] + V[r][1] * d[1] * V[c][1] + V[r][2] * d[2] * V[c][2];
+            x += o * amp[c];
+        }
+        out[r] = x + mp[r];
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Octree codes: octree.cl:3-72
 // ---------------------------------------------------------------------------
@@ -827,6 +904,7 @@ struct Chunk {
     std::vector<int32_t> node_materials;
     std::vector<QEF> qefs;
     std::vector<F4> positions, normals;
+    std::vector<double> positions64;  // 4 doubles per leaf: the FP64 solve, world units
     std::vector<int32_t> triangles;  // 3 ints per triangle
     std::vector<float> vertices;     // 12 floats per MeshVertex
     std::vector<int32_t> seams;      // 12 x 4-byte words per SeamNodeInfo
@@ -1070,11 +1148,13 @@ int run_chunk(Chunk& ch, const orc_density& dn, const orc_chunk_args& a, const P
     ch.qefs.resize(V);
     ch.normals.resize(V);
     ch.positions.resize(V);
+    ch.positions64.assign(4 * (size_t)V, 0.0);
     for (int v = 0; v < V; v++) {
         int pos[3];
         position_for_code(ch.node_codes[v], D.depth, pos);
         const int edge_list = ch.node_edges[v];
         F4 ep[12], en[12];
+        QEF64 q64;
         int count = 0;
         for (int i = 0; i < 12; i++) {
             if (!((edge_list >> i) & 1)) continue;
@@ -1093,6 +1173,13 @@ int run_chunk(Chunk& ch, const orc_density& dn, const orc_chunk_args& a, const P
             ep[count] = F4{fs * std::fmaf(p1.x - p0.x, e.w, p0.x), fs * std::fmaf(p1.y - p0.y, e.w, p0.y),
                            fs * std::fmaf(p1.z - p0.z, e.w, p0.z), fs * std::fmaf(p1.w - p0.w, e.w, p0.w)};
             en[count] = F4{e.x, e.y, e.z, 0.f};
+            {
+                const double t = e.w, sd = scale;
+                const double pd[3] = {sd * (p0.x + (p1.x - p0.x) * t), sd * (p0.y + (p1.y - p0.y) * t),
+                                      sd * (p0.z + (p1.z - p0.z) * t)};
+                const double nd[3] = {e.x, e.y, e.z};
+                qef64_add_point(q64, nd, pd);
+            }
             count++;
         }
         // qef_create_from_points (qef.cl:283-303)
@@ -1123,6 +1210,10 @@ int run_chunk(Chunk& ch, const orc_density& dn, const orc_chunk_args& a, const P
         x.z = std::fmaf(x.z, (float)LEAF_SIZE_SCALE, (float)a.min[2]);
         x.w = 1.f;
         ch.positions[v] = x;
+        double x64[3];
+        qef64_solve(q64, x64);
+        for (int i = 0; i < 3; i++) ch.positions64[4 * (size_t)v + i] = x64[i] * LEAF_SIZE_SCALE + a.min[i];
+        ch.positions64[4 * (size_t)v + 3] = count;
     }
 
     // node hash (compute_octree.cpp:143-144) + GenerateMesh (octree.cl:385-442)
@@ -1525,10 +1616,38 @@ int orc_set_seed(int32_t seed) {
 
 void orc_perm_lut(uint8_t* out) { std::memcpy(out, g_lut.v, sizeof(g_lut.v)); }
 
+void orc_perm_image_rgba(uint8_t* out) {
+    // the pixels CreateNoisePermutationLookupImage uploads (compute_density_field.cpp:104-114)
+    for (int t = 0; t < 65536; t++) {
+        const int v = g_lut.v[t];
+        for (int c = 0; c < 3; c++) out[4 * t + c] = (uint8_t)(kGrad3[v & 0x0f][c] * 64 + 64);
+        out[4 * t + 3] = (uint8_t)v;
+    }
+}
+
 float orc_density_at(const orc_density* d, float x, float y, float z) { return density(*d, x, y, z, g_lut); }
 float orc_snoise2(float x, float y) { return snoise2(x, y, g_lut); }
 float orc_snoise3(float x, float y, float z) { return snoise3(x, y, z, g_lut); }
 int orc_find_next_prime(int32_t n) { return find_next_prime(n); }
+
+float orc_qef_solve_points(const float* positions, const float* normals, int32_t count, float* out) {
+    // qef_create_from_points (qef.cl:283-303), then qef_solve (qef.cl:239-256)
+    QEF q;
+    std::memset(&q, 0, sizeof(q));
+    for (int i = 0; i < count && i < 12; i++)
+        qef_add_point(q, F4{normals[4 * i], normals[4 * i + 1], normals[4 * i + 2], normals[4 * i + 3]},
+                      F4{positions[4 * i], positions[4 * i + 1], positions[4 * i + 2], positions[4 * i + 3]});
+    q.masspoint.x /= q.masspoint.w;
+    q.masspoint.y /= q.masspoint.w;
+    q.masspoint.z /= q.masspoint.w;
+    q.masspoint.w /= q.masspoint.w;
+    const F4 x = qef_solve(q);
+    out[0] = x.x;
+    out[1] = x.y;
+    out[2] = x.z;
+    out[3] = x.w;
+    return 0.f;
+}
 
 void* orc_chunk_new(void) { return new Chunk(); }
 void orc_chunk_free(void* h) { delete static_cast<Chunk*>(h); }
@@ -1562,6 +1681,7 @@ int orc_chunk_count(void* hp, int what) {
         case ORC_SIMP_TRIANGLES: return (int)c.simp_triangles.size() / 3;
         case ORC_SIMP_VERTEX_COUNT: return c.simp_vertex_count;
         case ORC_SIMP_REPS: return (int)c.simp_reps.size();
+        case ORC_POSITIONS_F64: return (int)c.positions64.size() / 4;
         default: return -1;
     }
 }
@@ -1584,6 +1704,7 @@ int orc_chunk_get(void* hp, int what, void* out, int64_t cap) {
         case ORC_SIMP_VERTICES: return copy_out(c.simp_vertices, out, cap) < 0 ? -2 : (int)c.simp_vertices.size() / 12;
         case ORC_SIMP_TRIANGLES: return copy_out(c.simp_triangles, out, cap) < 0 ? -2 : (int)c.simp_triangles.size() / 3;
         case ORC_SIMP_REPS: return copy_out(c.simp_reps, out, cap);
+        case ORC_POSITIONS_F64: return copy_out(c.positions64, out, cap) < 0 ? -2 : (int)c.positions64.size() / 4;
         default: return -1;
     }
 }

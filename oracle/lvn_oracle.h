@@ -72,15 +72,22 @@ enum {
     ORC_SIMP_TRIANGLES = 14,/* int32[3 * T'] simplified triangles            */
     ORC_SIMP_VERTEX_COUNT = 15, /* reported simplified vertex count          */
     ORC_SIMP_REPS = 16,     /* int32[V] representative anchor | level << 20  */
-    ORC_NUM_WHAT = 17
+    ORC_POSITIONS_F64 = 17, /* double[4 * V] leaf vertex solved in FP64 (world units, count) */
+    ORC_NUM_WHAT = 18
 };
 
 int   orc_set_seed(int32_t seed);
 void  orc_perm_lut(uint8_t* out65536);
+/* the RGBA8 permutation image (256 x 256 x 4 bytes, row-major): RGB the
+ * gradient bytes, A the permutation value */
+void  orc_perm_image_rgba(uint8_t* out);
 float orc_density_at(const orc_density* d, float x, float y, float z);
 float orc_snoise2(float x, float y);
 float orc_snoise3(float x, float y, float z);
 int   orc_find_next_prime(int32_t n);
+/* qef_create_from_points + qef_solve (qef.cl:239-303) over `count` (<= 12)
+ * points and normals (4 floats each); out[4] = the solved position */
+float orc_qef_solve_points(const float* positions, const float* normals, int32_t count, float* out);
 
 void* orc_chunk_new(void);
 void  orc_chunk_free(void* h);

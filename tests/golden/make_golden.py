@@ -3,9 +3,10 @@
 Reads the twelve octree-key fixtures that the reference's cuckoo tests use
 (leven/src/testdata/octree_keys_*.cpp, consumed by test_cuckoo.cpp:120-179)
 and writes them, unchanged, to tests/golden/octree_keys.npz as uint32 arrays
-without the ~0 terminator.  Run it where the reference tree is mounted:
+without the ~0 terminator.  Run it where the reference tree is mounted, with
+the reference checkout's root as the argument:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference checkout>
 """
 import pathlib
 import re
@@ -30,4 +31,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <reference checkout root>")
+    main(sys.argv[1])

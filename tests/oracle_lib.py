@@ -15,7 +15,8 @@ REF_SO = ROOT / "oracle" / "_ref" / "libref.so"
 
 (ORC_MATERIALS, ORC_EDGE_KEYS, ORC_EDGE_INFO, ORC_NODE_CODES, ORC_NODE_EDGES, ORC_NODE_MATERIALS,
  ORC_VERTICES, ORC_TRIANGLES, ORC_SEAMS, ORC_PLAIN_EDGE_KEYS, ORC_QEFS, ORC_MESH_VERTEX_COUNT,
- ORC_CREATED_EDGE_KEYS, ORC_SIMP_VERTICES, ORC_SIMP_TRIANGLES, ORC_SIMP_VERTEX_COUNT, ORC_SIMP_REPS) = range(17)
+ ORC_CREATED_EDGE_KEYS, ORC_SIMP_VERTICES, ORC_SIMP_TRIANGLES, ORC_SIMP_VERTEX_COUNT, ORC_SIMP_REPS,
+ ORC_POSITIONS_F64) = range(18)
 
 
 class CsgOp(C.Structure):
@@ -90,6 +91,10 @@ def lib():
                                              C.c_int32]
         L.orc_mesh_collapse_many.restype = C.c_int64
         L.orc_uniform_draws.argtypes = [C.c_int32, C.c_int32, C.c_void_p]
+        L.orc_perm_image_rgba.argtypes = [C.c_void_p]
+        L.orc_perm_image_rgba.restype = None
+        L.orc_qef_solve_points.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]
+        L.orc_qef_solve_points.restype = C.c_float
         L.orc_seam_generate.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32 * 3,
                                         C.c_int32, C.c_void_p, C.c_int32, C.c_float * 3, C.c_void_p, C.c_int64,
                                         C.c_void_p, C.c_int64, C.c_void_p, C.c_int32]
@@ -119,6 +124,7 @@ class OracleChunk:
         self._ops = make_ops(list(ops))
         a = ChunkArgs((C.c_int32 * 3)(*min_xyz), size, vpc, default_material, crossing_mode, len(ops),
                       C.cast(self._ops, C.POINTER(CsgOp)), hash_seed)
+        self.scale = size // (vpc * 4)
         rc = L.orc_chunk_run(self._h, C.byref(dens), C.byref(a))
         if rc != 0:
             raise RuntimeError(f"orc_chunk_run failed: {rc}")
@@ -182,6 +188,20 @@ class OracleChunk:
     def mesh_vertex_count(self):
         return self.count(ORC_MESH_VERTEX_COUNT)
 
+    def positions_f64(self):
+        """(V, 4) float64: each leaf's vertex solved in FP64 from the same
+        crossings and normals (world units), and its crossing count."""
+        return self.get(ORC_POSITIONS_F64, np.float64, 4)
+
+    def qef_fp64_error_voxels(self, vertices=None):
+        """|x_fp32 - x_fp64| per leaf in this chunk's voxels (Euclidean), for
+        the FP32 vertices given (default: the oracle's own, which the GPU's
+        equal bit for bit) against the FP64 solve."""
+        v = self.vertices() if vertices is None else vertices
+        p64 = self.positions_f64()
+        voxel = 4.0 * self.scale
+        return np.sqrt(((v[:, :3].astype(np.float64) - p64[:, :3]) ** 2).sum(1)) / voxel
+
     # bottom-up octree simplification
     def simplify(self, threshold):
         rc = lib().orc_chunk_simplify(self._h, threshold)
@@ -210,6 +230,25 @@ def perm_lut():
     out = np.zeros(65536, dtype=np.uint8)
     lib().orc_perm_lut(out.ctypes.data)
     return out
+
+
+def perm_image_rgba():
+    """The RGBA8 permutation image (256 x 256 x 4 bytes) of the current seed."""
+    out = np.zeros(256 * 256 * 4, dtype=np.uint8)
+    lib().orc_perm_image_rgba(out.ctypes.data)
+    return out
+
+
+_ref = None
+
+
+def ref_lib():
+    """oracle/_ref/libref.so (the reference's own code), or None when it was
+    not built (no reference tree)."""
+    global _ref
+    if _ref is None and REF_SO.exists():
+        _ref = C.CDLL(str(REF_SO))
+    return _ref
 
 
 def find_next_prime(n):

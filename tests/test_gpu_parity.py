@@ -418,14 +418,21 @@ def test_pinned_host_outputs(lvn_gpu, mg):
     assert np.array_equal(hv.numpy().reshape(-1, 12)[:V.shape[0]].view(np.int32), V.view(np.int32))
     assert np.array_equal(ht.numpy().reshape(-1, 3)[:T.shape[0]], T)
     assert np.array_equal(hs.numpy().reshape(-1, 12)[:S.shape[0]], S)
+    # an array too small is flagged and left unwritten past its capacity
+    # (sentinels fill the host arrays beyond the capacity each call is given)
+    sentinel = -0x5A5A5A5B
+    ht.fill_(sentinel)
     small = lvn.BatchOut(lvn.LVN_MEMORY_HOST, hv.data_ptr(), cap_v, 0, ht.data_ptr(), 10, 0, hs.data_ptr(), cap_s, 0,
                          C.cast(results, C.POINTER(lvn.ChunkResult)))
     assert mg.generate_chunks_raw(descs, n, small) == lvn.LVN_ERR_CAPACITY
     assert small.total_triangles == T.shape[0]
+    assert (ht.numpy()[3 * 10:] == sentinel).all(), "triangles written past the capacity"
     # a vertex array too small: the leaves, which write it themselves, flag it
+    hv.view(torch.int32).fill_(sentinel)
     small_v = lvn.BatchOut(lvn.LVN_MEMORY_HOST, hv.data_ptr(), V.shape[0] - 1, 0, ht.data_ptr(), cap_t, 0,
                            hs.data_ptr(), cap_s, 0, C.cast(results, C.POINTER(lvn.ChunkResult)))
     assert mg.generate_chunks_raw(descs, n, small_v) == lvn.LVN_ERR_CAPACITY
+    assert (hv.view(torch.int32).numpy()[12 * (V.shape[0] - 1):] == sentinel).all(), "vertices written past the capacity"
     # a vertex array that is not 16-byte aligned takes the sliced export path
     hv.zero_()
     odd = lvn.BatchOut(lvn.LVN_MEMORY_HOST, hv.data_ptr() + 4, cap_v - 1, 0, ht.data_ptr(), cap_t, 0,
@@ -434,9 +441,11 @@ def test_pinned_host_outputs(lvn_gpu, mg):
     got = hv.numpy()[1:1 + 12 * V.shape[0]].reshape(-1, 12)
     assert np.array_equal(got.view(np.int32), V.view(np.int32))
     # the same for the seams, which the seam pass writes itself when aligned
+    hs.fill_(sentinel)
     small_s = lvn.BatchOut(lvn.LVN_MEMORY_HOST, hv.data_ptr(), cap_v, 0, ht.data_ptr(), cap_t, 0, hs.data_ptr(),
                            S.shape[0] - 1, 0, C.cast(results, C.POINTER(lvn.ChunkResult)))
     assert mg.generate_chunks_raw(descs, n, small_s) == lvn.LVN_ERR_CAPACITY
+    assert (hs.numpy()[12 * (S.shape[0] - 1):] == sentinel).all(), "seams written past the capacity"
     hs.zero_()
     odd_s = lvn.BatchOut(lvn.LVN_MEMORY_HOST, hv.data_ptr(), cap_v, 0, ht.data_ptr(), cap_t, 0, hs.data_ptr() + 4,
                          cap_s - 1, 0, C.cast(results, C.POINTER(lvn.ChunkResult)))

@@ -194,3 +194,15 @@ def test_density_f64_reference(lvn_gpu, mode):
     od = O.density(mode=mode)
     d32 = np.array([O.lib().orc_density_at(ctypes.byref(od), *map(float, p)) for p in pts[:256]])
     assert np.abs(d32 - d64[:256]).max() <= 1e-4 * (1 + np.abs(d64[:256]).max())
+
+
+def test_extrapolation_beyond_the_y_range(surrogate):
+    """Above and below the domain's y range the density continues from the
+    range's edge with unit slope, so tall coarse chunks keep the sign of
+    y - h(x, z) far from the surface."""
+    x, z = 123.0, -456.0
+    inside = np.array([[x, HI[1], z], [x, LO[1], z]], np.float32)
+    outside = np.array([[x, HI[1] + 10.0, z], [x, LO[1] - 7.0, z]], np.float32)
+    d_in = surrogate.eval(inside)
+    d_out = surrogate.eval(outside)
+    assert np.allclose(d_out, d_in + np.array([10.0, -7.0]), rtol=1e-5, atol=1e-4), (d_in, d_out)

@@ -1,0 +1,120 @@
+"""The oracle pinned against the reference's own OpenCL code.
+
+oracle/Makefile compiles the reference's leven/cl/simplex.cl, noise.cl (with
+hg_sdf.glsl) and qef.cl as C++ on the host through oracle/ref_shim/cl_shim.h,
+straight from the reference tree (its vector literals rewritten into
+constructor calls in a git-ignored build copy), into oracle/_ref/libref.so.
+These tests run that code and the oracle's restatement on the same inputs and
+require identical bits: simplex noise in 2D and 3D, the reference's terrain
+density (DensityFunc with Terrain, RidgedMultiFractal and BasicFractal), the
+benchmark's fBm heightfield built from the reference's BasicFractal, and the
+QEF solve (qef_create_from_points + qef_solve).
+
+The reference built these with -cl-fast-relaxed-math, so its own bits are
+one of several admissible results.  The harness compiles simplex.cl and
+qef.cl without fusing multiply-adds outside dot(), and noise.cl with fusion
+(a multiply whose one use is an add), which is the restatement's convention;
+the match is therefore exact, and any misread of the algorithm (a constant,
+a corner, a lookup, the sampler's wrap, a sweep) would show as a mismatch.
+
+The permutation image itself (CreateNoisePermutationLookupImage) lives in host
+code that needs an OpenCL runtime to compile; the harness is given the
+oracle's image.  Without the reference tree the harness is absent and these
+tests skip.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+
+
+@pytest.fixture(scope="module")
+def ref():
+    lib = O.ref_lib()
+    if lib is None or not hasattr(lib, "ref_snoise2"):
+        pytest.skip("reference harness not built (no reference tree here)")
+    for f in ("ref_snoise2", "ref_snoise3", "ref_basic_fractal", "ref_ridged_multi_fractal", "ref_terrain",
+              "ref_density_func", "ref_fbm_height_density", "ref_qef_solve_points"):
+        getattr(lib, f).restype = C.c_float
+    lib.ref_set_perm_image.argtypes = [C.c_void_p]
+    lib.ref_snoise2.argtypes = [C.c_float] * 2
+    lib.ref_snoise3.argtypes = [C.c_float] * 3
+    lib.ref_terrain.argtypes = [C.c_float] * 2
+    lib.ref_density_func.argtypes = [C.c_float] * 3
+    lib.ref_ridged_multi_fractal.argtypes = [C.c_int] + [C.c_float] * 5
+    lib.ref_basic_fractal.argtypes = [C.c_int] + [C.c_float] * 5
+    lib.ref_fbm_height_density.argtypes = [C.c_int] + [C.c_float] * 7
+    lib.ref_qef_solve_points.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+    O.set_seed(1)
+    image = O.perm_image_rgba()  # held while the harness copies it
+    lib.ref_set_perm_image(image.ctypes.data)
+    return lib
+
+
+def points(n, lo, hi, seed):
+    rng = np.random.default_rng(seed)
+    return rng.uniform(lo, hi, (n, 3)).astype(np.float32)
+
+
+def test_snoise2_bits(ref):
+    L = O.lib()
+    pts = points(20000, -3000.0, 3000.0, 1)
+    pts[:2000] *= np.float32(1.0 / 256.0)  # the fBm's base-octave scale
+    for p in pts:
+        x, y = float(p[0]), float(p[1])
+        a, b = np.float32(ref.ref_snoise2(x, y)), np.float32(L.orc_snoise2(x, y))
+        assert a.view(np.int32) == b.view(np.int32), (x, y, a, b)
+
+
+def test_snoise3_bits(ref):
+    L = O.lib()
+    pts = points(20000, -3000.0, 3000.0, 2)
+    pts[:2000] *= np.float32(1.0 / 64.0)
+    for p in pts:
+        a, b = np.float32(ref.ref_snoise3(*map(float, p))), np.float32(L.orc_snoise3(*map(float, p)))
+        assert a.view(np.int32) == b.view(np.int32), (p, a, b)
+
+
+def test_reference_terrain_density_bits(ref):
+    """DensityFunc (noise.cl:225-268): y - 900 Terrain(x, z), with the
+    reference's RidgedMultiFractal and BasicFractal."""
+    L = O.lib()
+    dens = O.density(mode=0)
+    for p in points(5000, -20000.0, 20000.0, 3):
+        a = np.float32(ref.ref_density_func(*map(float, p)))
+        b = np.float32(L.orc_density_at(C.byref(dens), *map(float, p)))
+        assert a.view(np.int32) == b.view(np.int32), (p, a, b)
+
+
+def test_fbm_heightfield_density_bits(ref):
+    """The benchmark's heightfield: y - 48 BasicFractal(8, 1/256, 2, 0.5, xz)
+    from the reference's BasicFractal, against the oracle's density mode 1."""
+    L = O.lib()
+    dens = O.density(mode=1)
+    for p in points(5000, -4096.0, 4096.0, 4):
+        a = np.float32(ref.ref_fbm_height_density(8, 1.0 / 256.0, 2.0, 0.5, 48.0, *map(float, p)))
+        b = np.float32(L.orc_density_at(C.byref(dens), *map(float, p)))
+        assert a.view(np.int32) == b.view(np.int32), (p, a, b)
+
+
+def test_qef_solve_bits(ref):
+    """qef_create_from_points + qef_solve (qef.cl:239-303) on 1-12 random
+    crossings with unit normals, as a leaf gathers them."""
+    L = O.lib()
+    L.orc_qef_solve_points.restype = C.c_float
+    L.orc_qef_solve_points.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+    rng = np.random.default_rng(5)
+    for _ in range(20000):
+        n = int(rng.integers(1, 13))
+        pos = np.zeros((12, 4), np.float32)
+        nor = np.zeros((12, 4), np.float32)
+        pos[:n, :3] = rng.uniform(0.0, 1.0, (n, 3)) * rng.choice([1.0, 4.0, 32.0])
+        v = rng.normal(size=(n, 3))
+        nor[:n, :3] = v / np.linalg.norm(v, axis=1, keepdims=True)
+        a = np.zeros(4, np.float32)
+        b = np.zeros(4, np.float32)
+        ref.ref_qef_solve_points(pos.ctypes.data, nor.ctypes.data, n, a.ctypes.data)
+        L.orc_qef_solve_points(pos.ctypes.data, nor.ctypes.data, n, b.ctypes.data)
+        assert np.array_equal(a[:3].view(np.int32), b[:3].view(np.int32)), (n, a, b)
