@@ -505,8 +505,9 @@ def run_lvn(args):
     # the FP32 leaf solve against an FP64 solve of the same crossings, over
     # every leaf of the last (device-output) step: a GPU measurement pass
     step(True)
-    qmax, qmean, qleaves = mg.qef_fp64_error()
+    qmax, qmean, qleaves, qfar = mg.qef_fp64_error()
     line["qef_fp64"] = {"max_voxels": qmax, "mean_voxels": qmean, "leaves": qleaves,
+                        "leaves_beyond_1e-3_voxel": qfar,
                         "what": "|x_fp32 - x_fp64| of each leaf vertex, in its chunk's voxels"}
     if rank == 0 and WORKLOAD == "sweep" and not args.no_surrogate:
         line["surrogate"] = surrogate_leg(args, wl, mg, descs, results, value, stream, flush, local)

@@ -250,9 +250,10 @@ int64_t lvn_meshgen_debug_fetch(lvn_meshgen* ctx, int32_t what, int32_t chunk, v
 /* New: the error of the FP32 leaf solve (qef_solve, qef.cl:239-256) against
  * an FP64 solve of the same crossings and normals, over every leaf of the
  * context's last fresh batch (not simplified leaves' parents): out[0] max and
- * out[1] mean distance in voxels of the leaf's chunk, out[2] leaves.  A
- * measurement pass on the GPU; LVN_ERR_INVALID before any fresh batch. */
-int lvn_meshgen_qef_fp64_error(lvn_meshgen* ctx, double out[3]);
+ * out[1] mean distance in voxels of the leaf's chunk, out[2] leaves, out[3]
+ * leaves farther than 1e-3 voxel.  A measurement pass on the GPU;
+ * LVN_ERR_INVALID before any fresh batch. */
+int lvn_meshgen_qef_fp64_error(lvn_meshgen* ctx, double out[4]);
 
 /* Test hook (new).  The device cuckoo table the meshing stages build, over an
  * arbitrary list of n distinct keys with value = key index: Cuckoo_InsertKeys

@@ -575,11 +575,12 @@ class MeshGen:
         return lib().lvn_meshgen_generate_chunks(self._h, descs, n, C.byref(batch_out))
 
     def qef_fp64_error(self):
-        """(max, mean, leaves): the FP32 leaf solve's distance in voxels from an
-        FP64 solve of the same crossings, over the last fresh batch's leaves."""
-        out = (C.c_double * 3)()
+        """(max, mean, leaves, leaves beyond 1e-3): the FP32 leaf solve's
+        distance in voxels from an FP64 solve of the same crossings, over the
+        last fresh batch's leaves."""
+        out = (C.c_double * 4)()
         _check(lib().lvn_meshgen_qef_fp64_error(self._h, out), "lvn_meshgen_qef_fp64_error")
-        return float(out[0]), float(out[1]), int(out[2])
+        return float(out[0]), float(out[1]), int(out[2]), int(out[3])
 
     def debug_fetch(self, what, chunk, dtype, width=1, max_elems=1 << 22):
         buf = np.zeros(max_elems * width, dtype=dtype)

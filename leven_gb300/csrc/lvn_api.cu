@@ -1782,15 +1782,15 @@ int64_t lvn_meshgen_debug_fetch(lvn_meshgen* m, int32_t what, int32_t chunk, voi
     return count;
 }
 
-int lvn_meshgen_qef_fp64_error(lvn_meshgen* m, double out[3]) {
+int lvn_meshgen_qef_fp64_error(lvn_meshgen* m, double out[4]) {
     if (!m || !out) return LVN_ERR_INVALID;
     if (!m->last_fresh || m->last_n <= 0) return LVN_ERR_INVALID;
     BatchPtrs b = make_ptrs(m, m->last_n);
     DevBuf stats;
-    LVN_CK(stats.ensure(sizeof(unsigned long long) * 3));
-    LVN_CK(cudaMemsetAsync(stats.p, 0, sizeof(unsigned long long) * 3, m->stream));
+    LVN_CK(stats.ensure(sizeof(unsigned long long) * 4));
+    LVN_CK(cudaMemsetAsync(stats.p, 0, sizeof(unsigned long long) * 4, m->stream));
     LVN_CK(launch_leaf_qef_check(b, stats.as<unsigned long long>(), m->stream));
-    unsigned long long h[3];
+    unsigned long long h[4];
     const cudaError_t e = cudaMemcpyAsync(h, stats.p, sizeof(h), cudaMemcpyDeviceToHost, m->stream);
     const cudaError_t e2 = e == cudaSuccess ? cudaStreamSynchronize(m->stream) : e;
     stats.release();
@@ -1801,6 +1801,7 @@ int lvn_meshgen_qef_fp64_error(lvn_meshgen* m, double out[3]) {
     out[0] = mx;
     out[1] = h[2] ? sum / (double)h[2] : 0.0;
     out[2] = (double)h[2];
+    out[3] = (double)h[3];
     return LVN_OK;
 }
 

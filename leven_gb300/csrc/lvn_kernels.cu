@@ -1554,7 +1554,8 @@ __global__ void k_debug_cuckoo_find(const uint32_t* keys, int n, const unsigned 
 // its ten Jacobi sweeps, 0.1 truncation and mass-point bias in double.  The
 // FP32 solve is the same qef_solve k_leaf runs on the same inputs.  Reports
 // the distance in voxels of the leaf's chunk: max (as the bits of a
-// non-negative double), sum and count.  A measurement pass, not a stage.
+// non-negative double), sum, count, and the count above 1e-3 voxel.  A
+// measurement pass, not a stage.
 // ---------------------------------------------------------------------------
 
 __device__ void qef_solve_f64(const double ata[6], const double atb[3], const double mpsum[4], double out[3]) {
@@ -1605,7 +1606,7 @@ __global__ void __launch_bounds__(256) k_leaf_qef_check(BatchPtrs b, unsigned lo
     if (b.bs->overflow) return;
     const int total = b.bs->total_nodes;
     double local_max = 0.0, local_sum = 0.0;
-    unsigned long long local_n = 0;
+    unsigned long long local_n = 0, local_far = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
         const int c = b.node_chunk[i];
         const ChunkState& st = b.cs[c];
@@ -1691,11 +1692,13 @@ __global__ void __launch_bounds__(256) k_leaf_qef_check(BatchPtrs b, unsigned lo
             local_max = fmax(local_max, err);
             local_sum += err;
             local_n++;
+            local_far += err > 1e-3;
         }
     }
     atomicMax(&stats[0], (unsigned long long)__double_as_longlong(local_max));
     atomicAdd(reinterpret_cast<double*>(&stats[1]), local_sum);
     atomicAdd(&stats[2], local_n);
+    atomicAdd(&stats[3], local_far);
 }
 
 // CreateLeafNodes + SolveQEFs + GenerateMeshVertexBuffer (octree.cl:236-331, 475-487)

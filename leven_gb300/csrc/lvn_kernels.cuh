@@ -199,7 +199,8 @@ cudaError_t launch_simplify(const BatchPtrs& b, cudaStream_t stream);
 
 // Measurement pass over the last batch's leaves: the FP32 solve k_leaf runs
 // against an FP64 solve of the same crossings.  stats (zeroed by the caller):
-// [0] max distance in voxels (double bits), [1] sum (double), [2] leaves.
+// [0] max distance in voxels (double bits), [1] sum (double), [2] leaves,
+// [3] leaves farther than 1e-3 voxel.
 cudaError_t launch_leaf_qef_check(const BatchPtrs& b, unsigned long long* stats, cudaStream_t stream);
 
 // Test hook: the meshing stages' cuckoo insert and find over an arbitrary key

@@ -3,8 +3,8 @@
 //
 // TEST INFRASTRUCTURE ONLY.  oracle/ref_shim/cl_to_cpp.py rewrites OpenCL C's
 // vector literals `(floatN)(a, b, ...)` into C++ constructor calls; with that,
-// the reference's noise and QEF functions compile unchanged against this
-// header.  The built-ins follow the same floating-point conventions as the
+// the reference's noise, QEF, cuckoo, field and octree code compiles unchanged
+// against this header.  The built-ins follow the same floating-point conventions as the
 // oracle restatement (oracle/lvn_oracle.cpp): dot() is an fma chain
 // fma(a.z, b.z, fma(a.y, b.y, a.x * b.x)), mix(a, b, t) = fma(b - a, t, a),
 // rsqrt(x) = 1 / sqrt(x), normalize(v) = v / sqrt(dot(v, v)) (zero stays
@@ -254,6 +254,42 @@ inline float4 read_imagef(image2d_t img, sampler_t, const float2& coord) {
     return float4(t[0] / 255.f, t[1] / 255.f, t[2] / 255.f, t[3] / 255.f);
 }
 
+// ---- integer vectors and the kernel built-ins the reference's kernels use ---
+struct int4 {
+    int x, y, z, w;
+    int4() : x(0), y(0), z(0), w(0) {}
+    int4(int a, int b, int c, int d) : x(a), y(b), z(c), w(d) {}
+};
+inline int4 operator+(int4 a, const int4& b) { return int4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+inline int4 operator*(int s, const int4& a) { return int4(s * a.x, s * a.y, s * a.z, s * a.w); }
+inline int4& operator+=(int4& a, const int4& b) { a = a + b; return a; }
+inline int4& operator/=(int4& a, int s) {
+    a.x /= s;
+    a.y /= s;
+    a.z /= s;
+    a.w /= s;
+    return a;
+}
+inline float4 convert_float4(const int4& a) { return float4((float)a.x, (float)a.y, (float)a.z, (float)a.w); }
+// uint and ulong (unsigned int, 64-bit unsigned long) come from glibc's <sys/types.h>
+#include <sys/types.h>
+inline int clz(uint n) { return n ? __builtin_clz(n) : 32; }
+
+// A kernel runs as a loop over its global ids on one host thread; the
+// reference's 64-bit atomics are then plain read-modify-writes.
+extern thread_local int clshim_gid[3];
+inline int get_global_id(int d) { return clshim_gid[d]; }
+inline ulong atom_xchg(ulong* p, ulong v) {
+    const ulong o = *p;
+    *p = v;
+    return o;
+}
+inline ulong atom_cmpxchg(ulong* p, ulong cmp, ulong v) {
+    const ulong o = *p;
+    if (o == cmp) *p = v;
+    return o;
+}
+
 // ---- OpenCL C qualifiers ----------------------------------------------------
 #define read_only
 #define write_only
@@ -261,3 +297,5 @@ inline float4 read_imagef(image2d_t img, sampler_t, const float2& coord) {
 #define __constant static const
 #define __global
 #define __private
+#define global
+#define kernel

@@ -36,7 +36,7 @@ def ref():
     if lib is None or not hasattr(lib, "ref_snoise2"):
         pytest.skip("reference harness not built (no reference tree here)")
     for f in ("ref_snoise2", "ref_snoise3", "ref_basic_fractal", "ref_ridged_multi_fractal", "ref_terrain",
-              "ref_density_func", "ref_fbm_height_density", "ref_qef_solve_points"):
+              "ref_density_func", "ref_harness_density", "ref_qef_solve_points"):
         getattr(lib, f).restype = C.c_float
     lib.ref_set_perm_image.argtypes = [C.c_void_p]
     lib.ref_snoise2.argtypes = [C.c_float] * 2
@@ -45,7 +45,7 @@ def ref():
     lib.ref_density_func.argtypes = [C.c_float] * 3
     lib.ref_ridged_multi_fractal.argtypes = [C.c_int] + [C.c_float] * 5
     lib.ref_basic_fractal.argtypes = [C.c_int] + [C.c_float] * 5
-    lib.ref_fbm_height_density.argtypes = [C.c_int] + [C.c_float] * 7
+    lib.ref_harness_density.argtypes = [C.c_int] + [C.c_float] * 3
     lib.ref_qef_solve_points.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
     O.set_seed(1)
     image = O.perm_image_rgba()  # held while the harness copies it
@@ -88,13 +88,17 @@ def test_reference_terrain_density_bits(ref):
         assert a.view(np.int32) == b.view(np.int32), (p, a, b)
 
 
-def test_fbm_heightfield_density_bits(ref):
-    """The benchmark's heightfield: y - 48 BasicFractal(8, 1/256, 2, 0.5, xz)
-    from the reference's BasicFractal, against the oracle's density mode 1."""
+@pytest.mark.parametrize("mode", [1, 2])
+def test_benchmark_density_bits(ref, mode):
+    """The benchmark's heightfield, y - 48 BasicFractal(8, 1/256, 2, 0.5, xz)
+    from the reference's BasicFractal (mode 1), plus 12 times a 6-octave 3D
+    fBm at 1/64 over the reference's snoise3 (mode 2), against the oracle's
+    density modes."""
     L = O.lib()
-    dens = O.density(mode=1)
+    dens = O.density(mode=mode)
     for p in points(5000, -4096.0, 4096.0, 4):
-        a = np.float32(ref.ref_fbm_height_density(8, 1.0 / 256.0, 2.0, 0.5, 48.0, *map(float, p)))
+        p[1] *= np.float32(1.0 / 32.0)
+        a = np.float32(ref.ref_harness_density(mode, *map(float, p)))
         b = np.float32(L.orc_density_at(C.byref(dens), *map(float, p)))
         assert a.view(np.int32) == b.view(np.int32), (p, a, b)
 
@@ -118,3 +122,52 @@ def test_qef_solve_bits(ref):
         ref.ref_qef_solve_points(pos.ctypes.data, nor.ctypes.data, n, a.ctypes.data)
         L.orc_qef_solve_points(pos.ctypes.data, nor.ctypes.data, n, b.ctypes.data)
         assert np.array_equal(a[:3].view(np.int32), b[:3].view(np.int32)), (n, a, b)
+
+
+def ref_chunk(ref, mode, mn, size, colour):
+    ref.ref_mesh_chunk.argtypes = [C.c_int32 * 3, C.c_int32, C.c_int32, C.c_uint32, C.c_float * 3] + \
+        [C.c_void_p] * 3 + [C.c_int64] + [C.c_void_p] * 3 + [C.c_int64, C.c_int32 * 6]
+    F = 66 ** 3
+    ecap, ncap = 3 * 65 ** 3, 64 ** 3
+    mats = np.zeros(F, np.int32)
+    keys = np.zeros(ecap, np.int32)
+    info = np.zeros((ecap, 4), np.float32)
+    verts = np.zeros((ncap, 12), np.float32)
+    tris = np.zeros(18 * ncap, np.int32)
+    seams = np.zeros((ncap, 12), np.int32)
+    counts = (C.c_int32 * 6)()
+    rc = ref.ref_mesh_chunk((C.c_int32 * 3)(*mn), size, mode, 5489, (C.c_float * 3)(*colour), mats.ctypes.data,
+                            keys.ctypes.data, info.ctypes.data, ecap, verts.ctypes.data, tris.ctypes.data,
+                            seams.ctypes.data, ncap, counts)
+    assert rc == 0
+    E, V, T, S, stash, past = counts
+    return dict(materials=mats, keys=keys[:E], info=info[:E], vertices=verts[:V], triangles=tris[:T].reshape(-1, 3),
+                seams=seams[:S], stash=stash, past=past)
+
+
+@pytest.mark.parametrize("mode,mn,size", [(1, (0, 128, 0), 256), (1, (-512, 0, 768), 256), (2, (0, 0, 0), 256),
+                                          (2, (1024, -1024, 0), 1024), (0, (0, 2304, 0), 256),
+                                          (1, (-2048, -2048, 4096), 4096)])
+def test_whole_chunk_through_the_reference_kernels(ref, mode, mn, size):
+    """A chunk meshed by the reference's own kernels (GenerateDefaultField,
+    FindFieldEdges, FindEdgeIntersectionInfo, FindActiveVoxels,
+    Cuckoo_InsertKeys, CreateLeafNodes, SolveQEFs, GenerateMesh,
+    GenerateMeshVertexBuffer, FindSeamNodes, ExtractSeamNodeInfo; the scans and
+    compactions sequential) equals the oracle's chunk bit for bit: materials,
+    edge keys and order, hermite data, vertices, triangles, seams.  Mode 0 is
+    the reference's DensityFunc; modes 1 and 2 are the benchmark's densities in
+    its place."""
+    O.set_seed(1)
+    image = O.perm_image_rgba()
+    ref.ref_set_perm_image(image.ctypes.data)
+    och = O.OracleChunk(O.density(mode=mode), mn, size, vpc=64)
+    colour = och.vertices()[0, 8:11] if och.count(O.ORC_NODE_CODES) else np.zeros(3, np.float32)
+    got = ref_chunk(ref, mode, mn, size, [float(c) for c in colour])
+    assert np.array_equal(got["materials"], och.materials()), "field materials"
+    assert np.array_equal(got["keys"], och.edge_keys()), "edge keys / compaction order"
+    assert np.array_equal(got["info"].view(np.int32), och.edge_info().view(np.int32)), "hermite data"
+    assert got["stash"] == 0 and got["past"] == 0  # the reference's stash lookup misses stashed keys
+    assert got["keys"].size > 0 and got["vertices"].shape[0] > 0
+    assert np.array_equal(got["vertices"].view(np.int32), och.vertices().view(np.int32)), "vertices"
+    assert np.array_equal(got["triangles"], och.triangles()), "triangle indices"
+    assert np.array_equal(got["seams"], och.seams()), "seam nodes"
