@@ -383,60 +383,106 @@ __global__ void k_features(const float4* pts, int n, Domain dom, FeatureFreqs ff
     }
 }
 
-// Head: y = X4 . w4 + b4 (density / out_scale).  Training: r = y - t / s,
-// loss += r^2 / n, dy = 2 r / n, dZ3 = dy w4 silu'(Z3), gw4 += dy X4, gb4 += dy.
-__global__ void __launch_bounds__(128) k_head(const __nv_bfloat16* X4, const float* Z3, const float4* pts, int n,
-                                              const float* params, float out_scale, float* dens_out,
-                                              __nv_bfloat16* dZ, __nv_bfloat16* dZt, float* grads, float* loss) {
-    __shared__ float w4[kHidden];
-    __shared__ float gw[kHidden];
-    __shared__ float red[4];
-    if (threadIdx.x < kHidden) {
-        w4[threadIdx.x] = params[kHeadW + threadIdx.x];
-        gw[threadIdx.x] = 0.f;
-    }
-    __syncthreads();
+// Head and loss (training): y = X4 . w4 + b4 (density / out_scale),
+// r = y - t / s, loss += r^2 / n, dy = 2 r / n, dZ3 = dy w4 silu'(Z3),
+// gw4 += dy X4, gb4 += dy.  A CTA takes 64-row tiles; a warp takes a row at a
+// time, each lane 4 of its 128 columns, so every global access is a
+// contiguous row segment: X4 and dZ3 as 8-byte, Z3 as 16-byte lane loads and
+// stores.  y is a warp-shuffle sum.  Each lane keeps its 4 columns' gw4
+// partial sums in registers (no shared atomics); the CTA adds them up once at
+// the end.  dZ3^T (the weight gradient's operand) is staged through shared
+// memory and written 64 rows at a time, 128 bytes per column.
+constexpr int kHeadRows = 64;    // rows per tile
+constexpr int kHeadWarps = 8;    // 256 threads
+
+__global__ void __launch_bounds__(32 * kHeadWarps) k_head(const __nv_bfloat16* X4, const float* Z3, const float4* pts,
+                                                          int n, const float* params, float out_scale,
+                                                          __nv_bfloat16* dZ, __nv_bfloat16* dZt, float* grads,
+                                                          float* loss) {
+    __shared__ __align__(16) __nv_bfloat16 sT[kHidden][kHeadRows + 8];  // dZ3 transposed, padded rows
+    __shared__ float gsum[kHeadWarps][kHidden];
+    __shared__ float red[2][kHeadWarps];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int c0 = 4 * lane;  // this lane's columns c0 .. c0 + 3
+    const float4 w = *reinterpret_cast<const float4*>(params + kHeadW + c0);
     const float b4 = params[kHeadB];
-    const bool train = loss != nullptr;
-    float l = 0.f, gb = 0.f;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const __nv_bfloat162* x2 = reinterpret_cast<const __nv_bfloat162*>(X4 + (size_t)i * kHidden);
-        float y = b4;
-#pragma unroll 8
-        for (int j = 0; j < kHidden / 2; j++) {
-            const float2 x = __bfloat1622float2(x2[j]);
-            y = fmaf(x.x, w4[2 * j], y);
-            y = fmaf(x.y, w4[2 * j + 1], y);
+    float gw0 = 0.f, gw1 = 0.f, gw2 = 0.f, gw3 = 0.f, l = 0.f, gb = 0.f;
+    const int tiles = n / kHeadRows;
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
+        const int r0 = t * kHeadRows;
+        for (int rr = warp; rr < kHeadRows; rr += kHeadWarps) {
+            const int i = r0 + rr;
+            const uint2 xr = *reinterpret_cast<const uint2*>(X4 + (size_t)i * kHidden + c0);
+            const float2 xa = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&xr.x));
+            const float2 xb = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&xr.y));
+            float y = fmaf(xa.x, w.x, fmaf(xa.y, w.y, fmaf(xb.x, w.z, xb.y * w.w)));
+#pragma unroll
+            for (int o = 16; o; o >>= 1) y += __shfl_xor_sync(0xffffffffu, y, o);
+            y += b4;
+            const float r = y - pts[i].w / out_scale;
+            const float dy = 2.f * r / (float)n;
+            if (lane == 0) {
+                l += r * r;
+                gb += dy;
+            }
+            gw0 = fmaf(dy, xa.x, gw0);
+            gw1 = fmaf(dy, xa.y, gw1);
+            gw2 = fmaf(dy, xb.x, gw2);
+            gw3 = fmaf(dy, xb.y, gw3);
+            const float4 z = *reinterpret_cast<const float4*>(Z3 + (size_t)i * kHidden + c0);
+            const __nv_bfloat16 d0 = __float2bfloat16_rn(dy * w.x * silu_grad(z.x));
+            const __nv_bfloat16 d1 = __float2bfloat16_rn(dy * w.y * silu_grad(z.y));
+            const __nv_bfloat16 d2 = __float2bfloat16_rn(dy * w.z * silu_grad(z.z));
+            const __nv_bfloat16 d3 = __float2bfloat16_rn(dy * w.w * silu_grad(z.w));
+            __nv_bfloat162 p01, p23;
+            p01.x = d0;
+            p01.y = d1;
+            p23.x = d2;
+            p23.y = d3;
+            uint2 out;
+            out.x = *reinterpret_cast<uint32_t*>(&p01);
+            out.y = *reinterpret_cast<uint32_t*>(&p23);
+            *reinterpret_cast<uint2*>(dZ + (size_t)i * kHidden + c0) = out;
+            sT[c0][rr] = d0;
+            sT[c0 + 1][rr] = d1;
+            sT[c0 + 2][rr] = d2;
+            sT[c0 + 3][rr] = d3;
         }
-        if (!train) {
-            dens_out[i] = y * out_scale;
-            continue;
+        __syncthreads();
+        // dZ3^T: column j's 64 rows (128 bytes) by two threads, 4 x 16 bytes each
+        {
+            const int j = threadIdx.x >> 1, half = threadIdx.x & 1;
+            const uint4* src = reinterpret_cast<const uint4*>(&sT[j][32 * half]);
+            uint4* dst = reinterpret_cast<uint4*>(dZt + (size_t)j * n + r0 + 32 * half);
+#pragma unroll
+            for (int q = 0; q < 4; q++) dst[q] = src[q];
         }
-        const float r = y - pts[i].w / out_scale;
-        l += r * r;
-        const float dy = 2.f * r / (float)n;
-        gb += dy;
-        const float* z = Z3 + (size_t)i * kHidden;
-#pragma unroll 4
-        for (int j = 0; j < kHidden; j++) {
-            const float x = __bfloat162float(X4[(size_t)i * kHidden + j]);
-            atomicAdd(&gw[j], dy * x);
-            const __nv_bfloat16 d = __float2bfloat16_rn(dy * w4[j] * silu_grad(z[j]));
-            dZ[(size_t)i * kHidden + j] = d;
-            dZt[(size_t)j * n + i] = d;
-        }
+        __syncthreads();
     }
-    if (!train) return;
-    __syncthreads();
-    if (threadIdx.x < kHidden) atomicAdd(&grads[kHeadW + threadIdx.x], gw[threadIdx.x]);
-    for (int o = 16; o; o >>= 1) {
-        l += __shfl_xor_sync(0xffffffffu, l, o);
-        gb += __shfl_xor_sync(0xffffffffu, gb, o);
+    gsum[warp][c0] = gw0;
+    gsum[warp][c0 + 1] = gw1;
+    gsum[warp][c0 + 2] = gw2;
+    gsum[warp][c0 + 3] = gw3;
+    if (lane == 0) {
+        red[0][warp] = l;
+        red[1][warp] = gb;
     }
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = l;
     __syncthreads();
-    if (threadIdx.x == 0) atomicAdd(loss, (red[0] + red[1] + red[2] + red[3]) / (float)n);
-    if ((threadIdx.x & 31) == 0) atomicAdd(&grads[kHeadB], gb);
+    if (threadIdx.x < kHidden) {
+        float s = 0.f;
+#pragma unroll
+        for (int k = 0; k < kHeadWarps; k++) s += gsum[k][threadIdx.x];
+        atomicAdd(&grads[kHeadW + threadIdx.x], s);
+    }
+    if (threadIdx.x == 0) {
+        float sl = 0.f, sg = 0.f;
+        for (int k = 0; k < kHeadWarps; k++) {
+            sl += red[0][k];
+            sg += red[1][k];
+        }
+        atomicAdd(loss, sl / (float)n);
+        atomicAdd(&grads[kHeadB], sg);
+    }
 }
 
 // bias gradient of layer l: sum over the batch of dZ (rows of dZ^T)
@@ -819,6 +865,7 @@ struct lvn_surrogate {
     float out_scale = 8.f;  // the network predicts density / out_scale
     cudaStream_t stream = nullptr;
     Buf params, grads, adam_m, adam_v, wb, wt, loss, status;
+    Buf loss_hist;  // one loss per training step, read back once per lvn_surrogate_train
     // batch activations
     int cap = 0;
     Buf pts, X[kLayers + 1], Xt[kLayers + 1], Z[kLayers], dZ[2], dZt[2], dens;
@@ -900,16 +947,16 @@ struct lvn_surrogate {
         return LVN_OK;
     }
 
-    // one forward + backward on the n samples in pts; gradients into grads
-    int backward(int n) {
+    // one forward + backward on the n samples in pts; gradients into grads,
+    // the loss into *loss_dev (device)
+    int backward(int n, float* loss_dev) {
         SG_CK(cudaMemsetAsync(grads.p, 0, sizeof(float) * kParams, stream));
-        SG_CK(cudaMemsetAsync(loss.p, 0, sizeof(float), stream));
+        SG_CK(cudaMemsetAsync(loss_dev, 0, sizeof(float), stream));
         int rc = forward(n, true);
         if (rc) return rc;
-        k_head<<<std::min(1184, (n + 127) / 128), 128, 0, stream>>>(
+        k_head<<<std::min(num_sms * 4, n / kHeadRows), 32 * kHeadWarps, 0, stream>>>(
             X[kLayers].as<__nv_bfloat16>(), Z[kLayers - 1].as<float>(), pts.as<float4>(), n, params.as<float>(),
-            out_scale, nullptr, dZ[1].as<__nv_bfloat16>(), dZt[1].as<__nv_bfloat16>(), grads.as<float>(),
-            loss.as<float>());
+            out_scale, dZ[1].as<__nv_bfloat16>(), dZt[1].as<__nv_bfloat16>(), grads.as<float>(), loss_dev);
         SG_CK(cudaGetLastError());
         GemmArgs g;
         std::memset(&g, 0, sizeof(g));
@@ -1025,7 +1072,7 @@ void lvn_surrogate_destroy(lvn_surrogate* s) {
     if (!s) return;
     if (s->stream) cudaStreamSynchronize(s->stream);
     Buf* bufs[] = {&s->params, &s->grads, &s->adam_m, &s->adam_v, &s->wb, &s->wt, &s->loss, &s->status,
-                   &s->pts, &s->dZ[0], &s->dZ[1], &s->dZt[0], &s->dZt[1], &s->dens, &s->pool};
+                   &s->pts, &s->dZ[0], &s->dZ[1], &s->dZt[0], &s->dZt[1], &s->dens, &s->pool, &s->loss_hist};
     for (Buf* b : bufs) b->release();
     for (int l = 0; l <= kLayers; l++) {
         s->X[l].release();
@@ -1082,7 +1129,7 @@ int lvn_surrogate_grad(lvn_surrogate* s, const float* samples, int32_t n, float*
     if (!s || !samples || n <= 0 || n % kTile) return LVN_ERR_INVALID;
     int rc = upload_samples(s, samples, n);
     if (rc) return rc;
-    if ((rc = s->backward(n))) return rc;
+    if ((rc = s->backward(n, s->loss.as<float>()))) return rc;
     if ((rc = check_status(s))) return rc;
     if (grad_out) SG_CK(cudaMemcpy(grad_out, s->grads.p, 4ull * kParams, cudaMemcpyDeviceToHost));
     if (loss_out) SG_CK(cudaMemcpy(loss_out, s->loss.p, 4, cudaMemcpyDeviceToHost));
@@ -1095,6 +1142,9 @@ int lvn_surrogate_train(lvn_surrogate* s, int32_t steps, int32_t batch, float lr
     int rc = s->ensure_batch(batch);
     if (rc) return rc;
     const LayerMap lm = layer_map();
+    // the losses stay on the device until the end, so the host never waits
+    // on a step and the launches queue ahead of the GPU
+    if (steps > 0 && (rc = s->loss_hist.ensure(sizeof(float) * (size_t)steps))) return rc;
     for (int it = 0; it < steps; it++) {
         // the next `batch` samples of the pool (wrapping)
         const int64_t first = s->pool_next;
@@ -1105,7 +1155,7 @@ int lvn_surrogate_train(lvn_surrogate* s, int32_t steps, int32_t batch, float lr
             SG_CK(cudaMemcpyAsync(s->pts.as<float4>() + take, s->pool.p, sizeof(float4) * (batch - take),
                                   cudaMemcpyDeviceToDevice, s->stream));
         s->pool_next = (first + batch) % s->pool_n;
-        if ((rc = s->backward(batch))) return rc;
+        if ((rc = s->backward(batch, s->loss_hist.as<float>() + it))) return rc;
         s->step++;
         const float c1 = 1.f / (1.f - std::pow(0.9f, (float)s->step));
         const float c2 = 1.f / (1.f - std::pow(0.999f, (float)s->step));
@@ -1113,8 +1163,9 @@ int lvn_surrogate_train(lvn_surrogate* s, int32_t steps, int32_t batch, float lr
                                           s->adam_v.as<float>(), kParams, lr, c1, c2, s->wb.as<__nv_bfloat16>(),
                                           s->wt.as<__nv_bfloat16>(), lm);
         SG_CK(cudaGetLastError());
-        if (losses) SG_CK(cudaMemcpyAsync(losses + it, s->loss.p, 4, cudaMemcpyDeviceToHost, s->stream));
     }
+    if (losses && steps > 0)
+        SG_CK(cudaMemcpyAsync(losses, s->loss_hist.p, sizeof(float) * (size_t)steps, cudaMemcpyDeviceToHost, s->stream));
     return check_status(s);
 }
 

@@ -261,6 +261,7 @@ struct int4 {
     int4(int a, int b, int c, int d) : x(a), y(b), z(c), w(d) {}
 };
 inline int4 operator+(int4 a, const int4& b) { return int4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+inline int4 operator-(int4 a, const int4& b) { return int4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w); }
 inline int4 operator*(int s, const int4& a) { return int4(s * a.x, s * a.y, s * a.z, s * a.w); }
 inline int4& operator+=(int4& a, const int4& b) { a = a + b; return a; }
 inline int4& operator/=(int4& a, int s) {

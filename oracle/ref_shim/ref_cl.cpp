@@ -47,6 +47,11 @@ thread_local int clshim_gid[3];
 #define CUCKOO_MAX_ITERATIONS 32
 #define constant static const
 
+// ApplyCSGOperations through the reference's CSG kernels (ref_csg.cpp)
+int ref_csg_apply(const int32_t off[3], int scale, const void* ops, int num_ops, int32_t* materials,
+                  std::vector<int>& edge_keys, std::vector<float4>& edge_info);
+
+namespace refmesh {
 #include "cl/shared_constants.cl"
 #include "cl/simplex.cl"
 #include "cl/qef.cl"
@@ -55,8 +60,6 @@ thread_local int clshim_gid[3];
 #pragma GCC push_options
 #pragma GCC optimize("fp-contract=fast")
 #include "cl/noise.cl"
-
-namespace {
 
 // The density the field kernels evaluate: the reference's DensityFunc (mode
 // 0), or the benchmark's heightfield y - 48 BasicFractal(8, 1/256, 2, 0.5,
@@ -86,15 +89,16 @@ float HarnessDensity(const float4 position, image2d_t permTexture) {
     return base + 12.f * caves_fbm3(float3(position.x, position.y, position.z));
 }
 
-}  // namespace
 #pragma GCC pop_options
 
 #define DensityFunc HarnessDensity
 #include "cl/density_field.cl"
 #undef DensityFunc
 #include "cl/octree.cl"
+}  // namespace refmesh
 
 namespace {
+using namespace refmesh;
 
 // Cuckoo_InitialiseTable + the host insert loop (compute_cuckoo.cpp:49-139):
 // parameters from the generator until every key inserts.  The stash holds
@@ -202,10 +206,12 @@ float ref_qef_solve_points(const float* positions, const float* normals, int cou
     return err;
 }
 
-// One 64^3 chunk without CSG operations, through the reference's kernels in
-// the order generateChunkMesh runs them (compute_density_field.cpp:138-231,
+// One 64^3 chunk through the reference's kernels in the order
+// generateChunkMesh runs them (compute_density_field.cpp:138-274,
 // compute_octree.cpp:108-347): GenerateDefaultField, FindFieldEdges,
-// compaction, FindEdgeIntersectionInfo, FindActiveVoxels, compaction, the edge
+// compaction, FindEdgeIntersectionInfo, the stored CSG operations
+// (`num_ops` CSGOperation records, 48 bytes each, through ref_csg.cpp's
+// ApplyCSGOperations), FindActiveVoxels, compaction, the edge
 // table, CreateLeafNodes, SolveQEFs, the node table, GenerateMesh, compaction,
 // GenerateMeshVertexBuffer, FindSeamNodes, ExtractSeamNodeInfo.  Scans and
 // compactions are sequential here (stable, in index order).  Hash parameters
@@ -214,11 +220,13 @@ float ref_qef_solve_points(const float* positions, const float* normals, int cou
 // Outputs: materials[66^3]; edge keys and info; vertices (12 floats each);
 // triangle indices; seam records (12 words each).  counts[0..5] = edges,
 // leaves, triangle indices, seams, stash used (edge | node << 1), stash
-// entries past the reference's 101.  Returns 0, or -1 when an output array is
-// too small (counts are set).
+// entries past the reference's 101.  Returns 0, -1 when an output array is
+// too small (counts are set), -2 when CSG pruned every field edge (there the
+// reference keeps the unpruned list, compute_csg.cpp:156).
 int ref_mesh_chunk(const int32_t min[3], int32_t size, int32_t mode, uint32_t hash_seed, const float colour[3],
-                   int32_t* materials, int32_t* edge_keys, float* edge_info, int64_t edge_cap, float* vertices,
-                   int32_t* triangles, int32_t* seams, int64_t node_cap, int32_t counts[6]) {
+                   const void* ops, int32_t num_ops, int32_t* materials, int32_t* edge_keys, float* edge_info,
+                   int64_t edge_cap, float* vertices, int32_t* triangles, int32_t* seams, int64_t node_cap,
+                   int32_t counts[6]) {
     g_mode = mode;
     const int vpc = VOXELS_PER_CHUNK, fd = FIELD_DIM, hd = HERMITE_INDEX_SIZE;
     const int scale = size / (vpc * LEAF_SIZE_SCALE);
@@ -231,11 +239,16 @@ int ref_mesh_chunk(const int32_t min[3], int32_t size, int32_t mode, uint32_t ha
     std::vector<int> edges;
     for (size_t i = 0; i < occ.size(); i++)
         if (occ[i]) edges.push_back(idx[i]);
+    std::vector<float4> info(edges.size());
+    run_1d((int)edges.size(), [&] { FindEdgeIntersectionInfo(&g_perm, offset, scale, edges.data(), info.data()); });
+    // the stored operations replayed as one batch (compute_density_field.cpp:255-271)
+    if (num_ops > 0) {
+        const int32_t off[3] = {offset.x, offset.y, offset.z};
+        if (ref_csg_apply(off, scale, ops, num_ops, materials, edges, info) < 0) return -2;
+    }
     const int E = (int)edges.size();
     counts[0] = E;
     if (E > edge_cap) return -1;
-    std::vector<float4> info(std::max(E, 1));
-    run_1d(E, [&] { FindEdgeIntersectionInfo(&g_perm, offset, scale, edges.data(), info.data()); });
     for (int i = 0; i < E; i++) {
         edge_keys[i] = edges[i];
         std::memcpy(edge_info + 4 * i, &info[i], 16);

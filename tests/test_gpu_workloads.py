@@ -129,7 +129,7 @@ def test_tiled_csg_128_every_chunk(lvn_gpu):
 def test_clipmap_caves_1024_every_chunk(lvn_gpu):
     wl = W.clipmap_caves()
     res, checked, _ = check_workload(lvn_gpu, wl)
-    assert checked == 1024 and (res[:, 7] == 0).any() and res[:, 7].max() > 20000
+    assert checked == 1024 and (res[:, 7] == 0).any() and res[:, 7].max() > 10000
 
 
 def test_clipmap_caves_1024_simplified_every_chunk(lvn_gpu):

@@ -124,9 +124,11 @@ def test_qef_solve_bits(ref):
         assert np.array_equal(a[:3].view(np.int32), b[:3].view(np.int32)), (n, a, b)
 
 
-def ref_chunk(ref, mode, mn, size, colour):
-    ref.ref_mesh_chunk.argtypes = [C.c_int32 * 3, C.c_int32, C.c_int32, C.c_uint32, C.c_float * 3] + \
-        [C.c_void_p] * 3 + [C.c_int64] + [C.c_void_p] * 3 + [C.c_int64, C.c_int32 * 6]
+def ref_chunk(ref, mode, mn, size, colour, ops=()):
+    ref.ref_mesh_chunk.argtypes = [C.c_int32 * 3, C.c_int32, C.c_int32, C.c_uint32, C.c_float * 3, C.c_void_p,
+                                   C.c_int32] + [C.c_void_p] * 3 + [C.c_int64] + [C.c_void_p] * 3 + \
+        [C.c_int64, C.c_int32 * 6]
+    op_array = O.make_ops(list(ops))
     F = 66 ** 3
     ecap, ncap = 3 * 65 ** 3, 64 ** 3
     mats = np.zeros(F, np.int32)
@@ -136,7 +138,8 @@ def ref_chunk(ref, mode, mn, size, colour):
     tris = np.zeros(18 * ncap, np.int32)
     seams = np.zeros((ncap, 12), np.int32)
     counts = (C.c_int32 * 6)()
-    rc = ref.ref_mesh_chunk((C.c_int32 * 3)(*mn), size, mode, 5489, (C.c_float * 3)(*colour), mats.ctypes.data,
+    rc = ref.ref_mesh_chunk((C.c_int32 * 3)(*mn), size, mode, 5489, (C.c_float * 3)(*colour),
+                            C.cast(op_array, C.c_void_p), len(ops), mats.ctypes.data,
                             keys.ctypes.data, info.ctypes.data, ecap, verts.ctypes.data, tris.ctypes.data,
                             seams.ctypes.data, ncap, counts)
     assert rc == 0
@@ -171,3 +174,43 @@ def test_whole_chunk_through_the_reference_kernels(ref, mode, mn, size):
     assert np.array_equal(got["vertices"].view(np.int32), och.vertices().view(np.int32)), "vertices"
     assert np.array_equal(got["triangles"], och.triangles()), "triangle indices"
     assert np.array_equal(got["seams"], och.seams()), "seam nodes"
+
+
+def test_csg_chunks_through_the_reference_kernels(ref):
+    """Chunks of the tiled CSG workload with the stored operations replayed
+    through the reference's CSG kernels (CSG_HermiteIndices,
+    UpdateFieldMaterials, FindUpdatedEdges, RemoveInvalidIndices, the
+    RemoveDuplicates rounds of duplicate.cl, FilterValidEdges, PruneFieldEdges,
+    the CSG FindEdgeIntersectionInfo) under ApplyCSGOperations' host flow: the
+    field materials, the kept edges in order, the created edges as a set (the
+    reference orders them by a racy dedupe, duplicate.cl:40-51), every edge's
+    hermite data by key, and the vertices, triangles and seams all equal the
+    oracle's bit for bit."""
+    from leven_gb300 import workloads as W
+
+    O.set_seed(1)
+    image = O.perm_image_rgba()
+    ref.ref_set_perm_image(image.ctypes.data)
+    wl = W.tiled_csg()
+    by_ops = sorted(range(len(wl.chunks)), key=lambda c: -len(W.ops_for_chunk(wl.ops, *wl.chunks[c])))
+    checked = 0
+    for c in by_ops[:10]:
+        mn, size = wl.chunks[c]
+        ops = [op.as_tuple() for op in W.ops_for_chunk(wl.ops, mn, size)]
+        och = O.OracleChunk(O.density(mode=1), mn, size, vpc=64, ops=ops)
+        colour = och.vertices()[0, 8:11] if och.count(O.ORC_NODE_CODES) else np.zeros(3, np.float32)
+        got = ref_chunk(ref, 1, mn, size, [float(v) for v in colour], ops)
+        assert np.array_equal(got["materials"], och.materials()), "materials after CSG"
+        keys, okeys = got["keys"], och.edge_keys()
+        ncreated = och.count(O.ORC_CREATED_EDGE_KEYS)
+        nk = okeys.size - ncreated
+        assert keys.size == okeys.size and np.array_equal(keys[:nk], okeys[:nk]), "kept edges"
+        assert set(keys[nk:].tolist()) == set(okeys[nk:].tolist()), "created edges"
+        a, b = np.argsort(keys), np.argsort(okeys)
+        assert np.array_equal(got["info"][a].view(np.int32), och.edge_info()[b].view(np.int32)), "hermite by key"
+        assert got["stash"] == 0
+        assert np.array_equal(got["vertices"].view(np.int32), och.vertices().view(np.int32)), "vertices"
+        assert np.array_equal(got["triangles"], och.triangles()), "triangles"
+        assert np.array_equal(got["seams"], och.seams()), "seams"
+        checked += ncreated > 0
+    assert checked >= 5
