@@ -232,7 +232,19 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
         tc_fence_after();
     }
     if (!ok) {
+        // The MMAs this CTA committed did not signal within the poll limit.
+        // TMEM is freed below, and a later CTA on this SM may allocate the
+        // same columns, so first wait (bounded again) for the commit: once it
+        // arrives the MMAs are complete and nothing writes the columns.  If
+        // it still does not, the columns are freed all the same: a CTA that
+        // never frees them would stall every later allocation on this SM,
+        // and the status flag set here makes the host discard this call's
+        // results (LVN_ERR_DEVICE_STATUS), including anything a late MMA
+        // wrote.
         if (lane == 0) atomicExch(g.status, 1);
+        uint32_t polls = 0;
+        while (!mbar_try_wait(&bar, phase ^ 1u) && ++polls < 4 * kWaitLimit) {
+        }
     } else if (kb < ke) {
         const int row = warp * 32 + lane;  // D row = TMEM lane
         const int m = m0 + row;
@@ -721,7 +733,15 @@ __global__ void __launch_bounds__(128 * kInferWG, 1) k_mlp_infer(InferArgs a) {
         }
         if (ok && p < a.n) a.out[p] = fmaf(y, a.out_scale, y_out);
     }
-    if (!ok && (threadIdx.x & 127) == 0) atomicExch(a.status, 1);
+    if (!ok) {
+        // as in k_gemm: a second bounded wait for this warpgroup's pending
+        // commit before the columns are freed; the status flag makes the host
+        // discard the call's results either way
+        if ((threadIdx.x & 127) == 0) atomicExch(a.status, 1);
+        uint32_t polls = 0;
+        while (!mbar_try_wait(&bars[wg], phase ^ 1u) && ++polls < 4 * kWaitLimit) {
+        }
+    }
     tc_fence_before();
     __syncthreads();
     if (warp == 0) tmem_dealloc(tmem_base, 512);
