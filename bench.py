@@ -92,6 +92,8 @@ def parse():
                         "seams: the seam meshes of one camera's clipmap; collapse: the engine's edge-collapse "
                         "simplification of that clipmap's meshes")
     p.add_argument("--no-surrogate", action="store_true", help="sweep: skip the learned-density leg")
+    p.add_argument("--chunks", type=int, default=0,
+                   help="mesh only the workload's first N chunks (0 = all; for small profiler captures)")
     return p.parse_args()
 
 
@@ -157,6 +159,7 @@ class ClockSampler:
 
 
 WORKLOAD = "sweep"
+CHUNKS = 0
 
 
 def simplify_threshold(args):
@@ -170,6 +173,16 @@ def simp_name(thr):
 
 
 def workload():
+    wl = _workload()
+    if CHUNKS and CHUNKS < len(wl.chunks):
+        from leven_gb300 import workloads as W
+
+        wl = W.Workload(f"{wl.name}-first{CHUNKS}", wl.chunks[:CHUNKS], wl.ops, wl.density, wl.noise_seed,
+                        wl.voxels_per_chunk)
+    return wl
+
+
+def _workload():
     from leven_gb300 import workloads as W
 
     if WORKLOAD == "sweep":
@@ -1318,6 +1331,7 @@ def run_collapse(args):
 if __name__ == "__main__":
     a = parse()
     WORKLOAD = a.workload
+    CHUNKS = a.chunks
     if a.impl == "reference":
         run_reference(a)
     elif a.surrogate:

@@ -519,7 +519,7 @@ BatchPtrs make_ptrs(lvn_meshgen* m, int n) {
     b.num_sms = g.num_sms;
     b.density = g.density;
     b.default_material = g.default_material;
-    density_fields(g.density, g.default_material, &b.cave_band, b.dom_by_solid);
+    density_fields(g.density, g.default_material, &b.cave_band, b.cave_rem, b.dom_by_solid);
     b.desc = m->desc.as<ChunkDesc>();
     b.cs = m->cs.as<ChunkState>();
     b.bs = m->bs.as<BatchState>();
@@ -1891,8 +1891,32 @@ static float cave_band(const DensityParams& d) {
     return std::nextafter((float)band, INFINITY);
 }
 
-void density_fields(const DensityParams& d, int32_t default_material, float* band, int32_t dom_by_solid[9]) {
+// rem[s] = the same bound over fbm3's octaves 2s and up only (the octaves the
+// field kernel has not evaluated after s steps of two), plus 4e-3 for the
+// rounding of the partial sums the kernel compares against it; 0 once no
+// octave is left.
+static void cave_remainders(const DensityParams& d, float* rem) {
+    for (int s = 0; s <= kCaveSteps; s++) rem[s] = 0.f;
+    if (d.mode != LVN_DENSITY_CAVES) return;
+    float a = 1.f;
+    std::vector<double> amp;
+    for (int i = 0; i < d.octaves3; i++) {
+        amp.push_back(std::fabs((double)a));
+        a = a * d.gain3;
+    }
+    for (int s = 0; s <= kCaveSteps; s++) {
+        double sum = 0.0;
+        for (size_t i = 2 * (size_t)s; i < amp.size(); i++) sum += amp[i];
+        if (sum == 0.0) break;
+        const double r = std::fabs((double)d.amp3) * 1.2972 * sum * 1.001 + 4e-3;
+        rem[s] = r < 1e30 ? std::nextafter((float)r, INFINITY) : INFINITY;
+    }
+}
+
+void density_fields(const DensityParams& d, int32_t default_material, float* band, float* rem,
+                    int32_t dom_by_solid[9]) {
     *band = cave_band(d);
+    cave_remainders(d, rem);
     for (int n = 0; n <= 8; n++) {
         int mats[8];
         for (int i = 0; i < 8; i++) mats[i] = i < n ? default_material : MATERIAL_AIR;

@@ -607,8 +607,11 @@ __global__ void __launch_bounds__(96) k_field(BatchPtrs b) {
 // density is fma(amp3, fbm3, base) with base = y - amp2 h, and |amp3 fbm3| is
 // at most b.cave_band, so where |base| exceeds it the sign of the density,
 // which is all the field keeps, is the sign of base.  The other points go to a
-// shared list that all lanes then evaluate in full; their solid bits are
-// gathered into the row words with shared-memory atomics.
+// shared list that all lanes then evaluate, two octaves at a time, until the
+// octaves left cannot change the sign; their solid bits are gathered into the
+// row words with shared-memory atomics.
+constexpr int kCaveBatch = 1024;  // listed points per batch of the stepped evaluation
+
 template <int VPC>
 __global__ void __launch_bounds__(128) k_field_caves(BatchPtrs b) {
     using G = Geo<VPC>;
@@ -617,6 +620,9 @@ __global__ void __launch_bounds__(128) k_field_caves(BatchPtrs b) {
     __shared__ uint32_t words[3][G::FD];
     __shared__ uint16_t list[G::FD * G::FD];
     __shared__ int nlist;
+    __shared__ uint16_t bidx[2][kCaveBatch];  // the undecided points of a batch, ping-pong
+    __shared__ float bnoise[2][kCaveBatch];   // their fBm partial sums
+    __shared__ int bcount[2];
     if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
     if (threadIdx.x == 0) nlist = 0;
     for (int i = threadIdx.x; i < 3 * G::FD; i += blockDim.x) (&words[0][0])[i] = 0u;
@@ -659,14 +665,45 @@ __global__ void __launch_bounds__(128) k_field_caves(BatchPtrs b) {
         }
     }
     __syncthreads();
+    // The listed points, a batch at a time, two fBm octaves a step.  After a
+    // step, a point whose partial density fma(amp3, noise, base) exceeds the
+    // bound on the octaves still to come (b.cave_rem) in magnitude keeps that
+    // sign whatever they add, so it is decided; the others carry their partial
+    // sum (the exact float the full loop holds there) to the next step through
+    // a compacted batch list, and the last step decides by the full density.
     const int nl = nlist;
-    for (int k = threadIdx.x; k < nl; k += blockDim.x) {
-        const int i = list[k];
-        const int y = i / G::FD, x = i - G::FD * y;
-        const float dv = dens_h<LVN_DENSITY_CAVES>(nz, dp, hs[x], (float)(x * scale + ox), (float)(y * scale + oy), wz);
-        const int m = dv < 0.f ? dm : MATERIAL_AIR;
-        if (write_mats) mats[i] = (uint8_t)m;
-        if (m != MATERIAL_AIR) atomicOr(&words[x >> 5][y], 1u << (x & 31));
+    const int steps = dp.octaves3 > 0 ? (dp.octaves3 + 1) / 2 : 1;
+    for (int b0 = 0; b0 < nl; b0 += kCaveBatch) {
+        const int nb = min(kCaveBatch, nl - b0);
+        for (int st = 0; st < steps; st++) {
+            const int src = st & 1, dst = src ^ 1;
+            const int n_in = st == 0 ? nb : bcount[src];
+            __syncthreads();  // every thread has read n_in
+            if (threadIdx.x == 0) bcount[dst] = 0;
+            __syncthreads();
+            const bool last = st + 1 == steps;
+            const float rem = b.cave_rem[st + 1];
+            for (int k = threadIdx.x; k < n_in; k += blockDim.x) {
+                const int i = st == 0 ? list[b0 + k] : bidx[src][k];
+                const int y = i / G::FD, x = i - G::FD * y;
+                const float wy = (float)(y * scale + oy);
+                const float base = fmaf(-amp2, hs[x], wy);
+                const float noise = nz.fbm3_step(st, dp.octaves3, dp.freq3, dp.lacunarity3, dp.gain3,
+                                                 (float)(x * scale + ox), wy, wz, st == 0 ? 0.f : bnoise[src][k]);
+                const float v = fmaf(dp.amp3, noise, base);
+                if (last || !(fabsf(v) <= rem)) {
+                    const int m = v < 0.f ? dm : MATERIAL_AIR;
+                    if (write_mats) mats[i] = (uint8_t)m;
+                    if (m != MATERIAL_AIR) atomicOr(&words[x >> 5][y], 1u << (x & 31));
+                } else {
+                    const int slot = atomicAdd(&bcount[dst], 1);
+                    bidx[dst][slot] = (uint16_t)i;
+                    bnoise[dst][slot] = noise;
+                }
+            }
+            __syncthreads();
+            if (bcount[dst] == 0) break;
+        }
     }
     __syncthreads();
     const uint4 V = low_bits(G::FD);

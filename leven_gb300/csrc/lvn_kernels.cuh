@@ -23,6 +23,7 @@ struct BatchPtrs {
     int num_sms;
     DensityParams density;
     float cave_band;             // |y - amp2 h| above this: the cave term cannot change the density's sign
+    float cave_rem[kCaveSteps + 1];  // cave_rem[s]: bound on |amp3 * octaves 2s.. of fbm3| (0 past the last)
     float4* host_vertices;       // non-null: k_leaf also writes each vertex to this pinned host array
     int64_t host_vertex_cap;     //   (16-byte aligned), of this many vertices
     int4* host_seams;            // non-null: the seam pass of k_mesh_scatter also writes this pinned array

@@ -159,7 +159,7 @@ extern "C" int lvn_generate_chunk_mesh_noalloc(const int32_t min[3], int32_t siz
     b.num_sms = gv.num_sms;
     b.density = gv.density;
     b.default_material = gv.default_material;
-    density_fields(gv.density, gv.default_material, &b.cave_band, b.dom_by_solid);
+    density_fields(gv.density, gv.default_material, &b.cave_band, b.cave_rem, b.dom_by_solid);
     b.perm = gv.perm;
     b.perm_t3 = gv.perm_t3;
     b.grad = gv.grad;

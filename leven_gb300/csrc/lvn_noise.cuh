@@ -299,6 +299,31 @@ struct Noise {
         return noise;
     }
 
+    // Step s of fbm3: octaves 2s and 2s + 1 (the last one alone when
+    // `octaves` is odd) added to `noise`, at the coordinates and amplitude the
+    // full loop reaches there (the same products, in the same order), so that
+    // steps 0, 1, ... chained give fbm3's value bit for bit.
+    __device__ __forceinline__ float fbm3_step(int s, int octaves, float frequency, float lacunarity,
+                                               float persistence, float x, float y, float z, float noise) const {
+        if (2 * s >= octaves) return noise;
+        float px = x * frequency, py = y * frequency, pz = z * frequency;
+        float amplitude = 1.f;
+        for (int i = 0; i < s; i++) {
+            px = (px * lacunarity) * lacunarity;
+            py = (py * lacunarity) * lacunarity;
+            pz = (pz * lacunarity) * lacunarity;
+            amplitude = (amplitude * persistence) * persistence;
+        }
+        if (2 * s + 1 < octaves) {
+            const float qx = px * lacunarity, qy = py * lacunarity, qz = pz * lacunarity;
+            const float2 n = snoise3x2(make_float2(px, qx), make_float2(py, qy), make_float2(pz, qz));
+            noise = fmaf(n.x, amplitude, noise);
+            amplitude = amplitude * persistence;
+            return fmaf(n.y, amplitude, noise);
+        }
+        return fmaf(snoise3(px, py, pz), amplitude, noise);
+    }
+
     // RidgedMultiFractal (noise.cl:42-81), RIDGED_MULTI_H == 1
     __device__ __forceinline__ float ridged(int octaves, float lacunarity, float gain, float offset, float x,
                                             float y) const {

@@ -28,9 +28,12 @@ void draw_hash_params(uint32_t* p);
 void lod_colour_for(int min_leaf_size, float c[3]);
 // The batch fields derived from the density and the default material: the
 // cave band (|y - amp2 h| above it, the cave term cannot change the density's
-// sign; 0 without a 3D term) and the dominant material of 8 corners of which
-// n hold the default material and the rest AIR, for n = 0..8.
-void density_fields(const DensityParams& d, int32_t default_material, float* band, int32_t dom_by_solid[9]);
+// sign; 0 without a 3D term), the bounds rem[s] on |amp3 * (fbm3's octaves 2s
+// and up)| for s = 0..kCaveSteps (0 where no octave is left), and the dominant
+// material of 8 corners of which n hold the default material and the rest AIR,
+// for n = 0..8.
+void density_fields(const DensityParams& d, int32_t default_material, float* band, float* rem,
+                    int32_t dom_by_solid[9]);
 // Field-index box holding every point the operations can change.
 void csg_box_for(const Brush* ops, int n, const int32_t off[3], int scale, int fd, int32_t lo[3], int32_t hi[3]);
 

@@ -1132,9 +1132,9 @@ int lvn_surrogate_sample(lvn_surrogate* s, int64_t n, uint64_t seed, float* host
     if (!gv.initialised) return LVN_ERR_NOT_INITIALISED;
     int rc = s->pool.ensure(sizeof(float4) * (size_t)n);
     if (rc) return rc;
-    float band = 0.f;
+    float band = 0.f, rem[kCaveSteps + 1];
     int32_t dom_by_solid[9];
-    density_fields(gv.density, gv.default_material, &band, dom_by_solid);
+    density_fields(gv.density, gv.default_material, &band, rem, dom_by_solid);
     k_samples<<<gv.num_sms * 8, 256, 0, s->stream>>>(s->pool.as<float4>(), (int)n, seed, s->dom, gv.perm_t3,
                                                      gv.grad, gv.density, band);
     SG_CK(cudaGetLastError());

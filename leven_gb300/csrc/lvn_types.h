@@ -57,6 +57,11 @@ constexpr int CUCKOO_STASH_SIZE = 101;
 constexpr int CUCKOO_MAX_ITERATIONS = 32;
 constexpr uint32_t CUCKOO_MIN_TABLE_SIZE = 2048u;  // compute_cuckoo.cpp:15
 
+// fbm3 runs two octaves a step; the field kernel decides a point's sign after
+// each step when the octaves left cannot change it (bounds for at most
+// 2 kCaveSteps octaves)
+constexpr int kCaveSteps = 16;
+
 
 typedef lvn_density_params DensityParams;
 

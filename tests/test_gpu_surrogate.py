@@ -215,9 +215,11 @@ def test_trained_network_gain_over_the_method_without_it(lvn_gpu):
     network: the same 96 Fourier features with the best linear read-out, a
     float64 least-squares fit on the network's own training samples.  The
     trained network must cut the untrained one's RMS error 5-fold and beat the
-    linear read-out by 1.5x.  Then, meshing 16 chunks under a probe gate of 2
-    voxels, the trained network takes chunks off the plain noise path that the
-    untrained one cannot (it falls back everywhere)."""
+    linear read-out by 1.5x.  Then, meshing 16 chunks under a probe gate of 8
+    voxels (every one of a chunk's 512 probes within 8 density units of the
+    plain density), the trained network takes chunks off the plain noise path
+    that the untrained one cannot (it falls back everywhere), and the meshes
+    it makes index their own vertices."""
     lvn = lvn_gpu
     lvn.set_density(**W.FBM2D)
     lvn.clear_csg_operations()
@@ -231,14 +233,17 @@ def test_trained_network_gain_over_the_method_without_it(lvn_gpu):
         g = lvn.MeshGen(64)
         g.set_option(lvn.LVN_OPT_CACHE, 0)
         chunks = [((256 * i, 0, 256 * j), 256) for i in range(-2, 2) for j in range(-2, 2)]
-        g.set_surrogate(s, gate=2.0)
+        g.set_surrogate(s, gate=8.0)
         g.generate_chunks(chunks)
         used_untrained = int(g.surrogate_chunks(len(chunks)).sum())
         s.train(3000, batch=16384, lr=1e-3)
         rms_trained = float(np.sqrt(np.mean((s.eval(held) - held[:, 3]) ** 2)))
-        g.generate_chunks(chunks)
+        V, T, S, res = g.generate_chunks(chunks)
         used_trained = int(g.surrogate_chunks(len(chunks)).sum())
         g.close()
+        for r in res:
+            t = T[r[2]:r[2] + r[3]]
+            assert t.size == 0 or (t.min() >= 0 and t.max() < r[1])
     finally:
         s.close()
 
@@ -256,7 +261,7 @@ def test_trained_network_gain_over_the_method_without_it(lvn_gpu):
     coef, *_ = np.linalg.lstsq(feats(train), train[:, 3].astype(np.float64), rcond=None)
     rms_linear = float(np.sqrt(np.mean((feats(held) @ coef - held[:, 3]) ** 2)))
     print(f"density RMS error: untrained {rms_untrained:.3f}, linear Fourier read-out {rms_linear:.3f}, "
-          f"trained {rms_trained:.3f}; chunks on the surrogate at a 2-voxel gate: {used_untrained} -> {used_trained}")
+          f"trained {rms_trained:.3f}; chunks on the surrogate at an 8-voxel gate: {used_untrained} -> {used_trained}")
     assert rms_trained * 5.0 <= rms_untrained, (rms_trained, rms_untrained)
     assert rms_trained * 1.5 <= rms_linear, (rms_trained, rms_linear)
     assert used_untrained == 0 and used_trained > used_untrained
