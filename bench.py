@@ -546,17 +546,22 @@ def run_lvn(args):
 
 
 PROFILE_TAG = {"tiled": "tiled_csg_128", "clipmap": "clipmap_caves_1024", "one": "one_chunk",
-               "select": "select_4096", "seams": "clipmap_frame_428"}
+               "select": "select_4096", "seams": "clipmap_frame_428", "sweep": "clipmap_sweep_4096"}
 
 
 def committed_traffic(kernel):
-    """DRAM bytes per launch of `kernel` on this workload from the committed ncu
-    summary (profiles/<kernel>_<workload>.md, line `dram_bytes_per_launch`)."""
+    """DRAM bytes per launch of `kernel` on this workload as a committed ncu
+    summary states them (profiles/<kernel>_<workload>.md, the table row
+    `dram_bytes_per_launch`), with the file: a figure from an earlier capture,
+    not a measurement of this run."""
+    if CHUNKS:
+        return None
     path = ROOT / "profiles" / f"{kernel}_{PROFILE_TAG.get(WORKLOAD, WORKLOAD)}.md"
     try:
         for line in path.read_text().splitlines():
             if "dram_bytes_per_launch" in line:
-                return int(line.split("|")[2].strip())
+                return {"dram_bytes_per_launch": int(line.split("|")[2].strip()),
+                        "file": str(path.relative_to(ROOT))}
     except (OSError, ValueError, IndexError):
         pass
     return None
