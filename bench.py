@@ -682,6 +682,26 @@ def surrogate_leg(args, wl, mg, descs, results, plain_value, stream, flush, gpu_
                 e1.synchronize()
                 ts.append(e0.elapsed_time(e1))
         ms_sur = sum(ts) / len(ts)
+        # the gate swept: fallback rate against mesh Hausdorff distance (up to
+        # 256 surrogate chunks spread over those a gate lets through)
+        gate_sweep = []
+        for gate in (0.5, 1.0, 2.0, 4.0, 8.0, 16.0, 32.0):
+            mg.set_surrogate(sur, gate)
+            Vg, Tg, Sg, resg = mg.generate_chunks(wl.chunks)
+            ug = np.flatnonzero(mg.surrogate_chunks(n))
+            pick = ug[np.linspace(0, len(ug) - 1, min(len(ug), 256)).astype(int)] if len(ug) else ug
+            hg = []
+            for c in pick:
+                rp, rs = resp[c], resg[c]
+                h = hausdorff_voxels(Vp[rp[0]:rp[0] + rp[1], :3], Vg[rs[0]:rs[0] + rs[1], :3],
+                                     4.0 * wl.chunks[c][1] / 256)
+                if h is not None:
+                    hg.append(h)
+            gate_sweep.append({"gate_voxels": gate, "fallback_rate": round(1 - len(ug) / n, 4),
+                               "hausdorff_voxels_mean": round(float(np.mean(hg)), 4) if hg else None,
+                               "hausdorff_voxels_max": round(float(np.max(hg)), 4) if hg else None,
+                               "hausdorff_chunks": len(hg)})
+            del Vg, Tg, Sg
     finally:
         mg.set_surrogate(None)
     hd = []
@@ -721,7 +741,7 @@ def surrogate_leg(args, wl, mg, descs, results, plain_value, stream, flush, gpu_
                   "tensor_frac_of_sustained_bf16": round(train_tflops / sustained, 4) if sustained else None,
                   "loss_first": float(losses[0]) if len(losses) else None,
                   "loss_last100": float(np.mean(losses[-100:])) if len(losses) else None},
-        "domain": [lo, hi], "clocks": clocks.summary(),
+        "domain": [lo, hi], "clocks": clocks.summary(), "gate_sweep": gate_sweep,
     }
 
 
