@@ -198,6 +198,20 @@ int lvn_meshgen_generate_chunk_mesh(lvn_meshgen* ctx, const int32_t min[3], int3
 int lvn_meshgen_generate_chunks(lvn_meshgen* ctx, const lvn_chunk_desc* chunks, int32_t num_chunks,
                                 lvn_batch_out* out);
 
+/* New: lvn_meshgen_generate_chunks without waiting.  The call copies `chunks`
+ * and returns once the batch is handed to a host thread of the context's own,
+ * which runs the synchronous call; lvn_meshgen_wait(ctx) joins it and returns
+ * its result code, after which `out` holds the totals and per-chunk results.
+ * `out` and the arrays it points to must stay valid and untouched until then.
+ * One batch is in flight per context (a second call before the wait returns
+ * LVN_ERR_INVALID); two contexts, each with its own stream, keep two batches
+ * in flight, so that one batch's transfer to host arrays overlaps the next
+ * one's kernels.  A context must not be used by other calls between the two.
+ * lvn_meshgen_wait returns LVN_OK when nothing is in flight; destroying a
+ * context waits for its batch. */
+int lvn_meshgen_generate_chunks_async(lvn_meshgen* ctx, const lvn_chunk_desc* chunks, int32_t n, lvn_batch_out* out);
+int lvn_meshgen_wait(lvn_meshgen* ctx);
+
 /* new: execution control */
 int   lvn_meshgen_set_stream(lvn_meshgen* ctx, void* cuda_stream);
 void* lvn_meshgen_get_stream(lvn_meshgen* ctx);

@@ -105,6 +105,7 @@ EXPORTS = [
     "lvn_render_mesh_upload", "lvn_render_meshes_from_batch", "lvn_render_mesh_get", "lvn_render_mesh_download",
     "lvn_render_mesh_free",
     "lvn_render_pool_usage", "lvn_meshgen_qef_fp64_error", "lvn_debug_cuckoo", "lvn_debug_inject_fault",
+    "lvn_meshgen_generate_chunks_async", "lvn_meshgen_wait",
 ]
 
 _lib = None
@@ -136,6 +137,8 @@ def lib():
     L.lvn_meshgen_is_chunk_empty.argtypes = [C.c_void_p, i32p, C.c_int32, i32p]
     L.lvn_meshgen_generate_chunk_mesh.argtypes = [C.c_void_p, i32p, C.c_int32, C.POINTER(MeshOut)]
     L.lvn_meshgen_generate_chunks.argtypes = [C.c_void_p, C.POINTER(ChunkDesc), C.c_int32, C.POINTER(BatchOut)]
+    L.lvn_meshgen_generate_chunks_async.argtypes = [C.c_void_p, C.POINTER(ChunkDesc), C.c_int32, C.POINTER(BatchOut)]
+    L.lvn_meshgen_wait.argtypes = [C.c_void_p]
     L.lvn_meshgen_set_stream.argtypes = [C.c_void_p, C.c_void_p]
     L.lvn_meshgen_get_stream.argtypes = [C.c_void_p]
     L.lvn_meshgen_get_stream.restype = C.c_void_p
@@ -573,6 +576,15 @@ class MeshGen:
     def generate_chunks_raw(self, descs, n, batch_out):
         """Direct C-ABI call with caller-prepared ctypes structures."""
         return lib().lvn_meshgen_generate_chunks(self._h, descs, n, C.byref(batch_out))
+
+    def generate_chunks_async_raw(self, descs, n, batch_out):
+        """lvn_meshgen_generate_chunks_async: returns at once; batch_out and its
+        arrays must stay alive and untouched until wait()."""
+        return lib().lvn_meshgen_generate_chunks_async(self._h, descs, n, C.byref(batch_out))
+
+    def wait(self):
+        """lvn_meshgen_wait: the result code of the batch in flight (0 when none)."""
+        return lib().lvn_meshgen_wait(self._h)
 
     def qef_fp64_error(self):
         """(max, mean, leaves, leaves beyond 1e-3): the FP32 leaf solve's

@@ -15,7 +15,9 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <random>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -270,7 +272,12 @@ void lod_colour(int s, float c[3]) {
     }
 }
 
+// the shared parameter generator; contexts running batches on their own host
+// threads (lvn_meshgen_generate_chunks_async) draw from it concurrently
+std::mutex g_hash_gen_mutex;
+
 void draw_params(uint32_t* p) {
+    std::lock_guard<std::mutex> lock(g_hash_gen_mutex);
     std::uniform_int_distribution<uint32_t> dist(1u << 15, 1u << 30);
     for (int i = 0; i < CUCKOO_HASH_FN_COUNT * 2; i++) p[i] = dist(g.hash_gen);
     if (g_fault_hash_family > 0) {
@@ -326,6 +333,11 @@ struct OctreeEntry {  // the mesh a cached GPUOctree (compute_local.h:43-49) reg
 
 struct lvn_meshgen {
     int vpc = 64;
+    // a batch in flight on a host thread of its own (lvn_meshgen_generate_chunks_async)
+    std::thread async_thread;
+    bool async_active = false;
+    int async_rc = 0;
+    std::vector<lvn_chunk_desc> async_chunks;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int crossing_mode = 0;
@@ -1405,6 +1417,7 @@ lvn_meshgen* lvn_meshgen_create(int32_t voxels_per_chunk) {
 
 void lvn_meshgen_destroy(lvn_meshgen* m) {
     if (!m) return;
+    lvn_meshgen_wait(m);
     cudaStreamSynchronize(m->stream);
     DevBuf* bufs[] = {&m->desc,       &m->cs,         &m->bs,         &m->brushes,      &m->mats,  &m->planes, &m->hmap,
                       &m->edge_tiles, &m->vox_tiles,  &m->edge_keys,  &m->edge_chunk,   &m->edge_info, &m->edge_work,
@@ -1641,6 +1654,32 @@ int lvn_meshgen_generate_chunks(lvn_meshgen* m, const lvn_chunk_desc* chunks, in
         LVN_CK(cudaStreamSynchronize(m->stream));
     }
     return LVN_OK;
+}
+
+int lvn_meshgen_generate_chunks_async(lvn_meshgen* m, const lvn_chunk_desc* chunks, int32_t n, lvn_batch_out* out) {
+    if (!g.initialised) return LVN_ERR_NOT_INITIALISED;
+    if (!m || !out || n < 0 || (n > 0 && !chunks) || n > 65535) return LVN_ERR_INVALID;
+    if (m->async_active) return LVN_ERR_INVALID;  // one batch in flight per context
+    m->async_chunks.assign(chunks, chunks + n);
+    m->async_active = true;
+    m->async_rc = LVN_OK;
+    const int device = g.device;
+    m->async_thread = std::thread([m, out, device]() {
+        if (cudaSetDevice(device) != cudaSuccess) {
+            m->async_rc = LVN_ERR_CUDA;
+            return;
+        }
+        m->async_rc = lvn_meshgen_generate_chunks(m, m->async_chunks.data(), (int32_t)m->async_chunks.size(), out);
+    });
+    return LVN_OK;
+}
+
+int lvn_meshgen_wait(lvn_meshgen* m) {
+    if (!m) return LVN_ERR_INVALID;
+    if (!m->async_active) return LVN_OK;
+    m->async_thread.join();
+    m->async_active = false;
+    return m->async_rc;
 }
 
 int lvn_meshgen_generate_chunk_mesh(lvn_meshgen* m, const int32_t min[3], int32_t size, lvn_mesh_out* out) {
