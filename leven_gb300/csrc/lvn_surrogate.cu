@@ -497,19 +497,35 @@ __global__ void __launch_bounds__(32 * kHeadWarps) k_head(const __nv_bfloat16* X
     }
 }
 
-// bias gradient of layer l: sum over the batch of dZ (rows of dZ^T)
+// bias gradient of layer l: the sum over the batch of dZ, i.e. of each row of
+// dZ^T.  A row (n BF16 values, n a multiple of 8) is split over
+// gridDim.y CTAs; each thread reads 16-byte runs of 8 values, the CTA sums
+// them (warp shuffles, then shared memory) and adds its part to g[row].
+constexpr int kBiasSplits = 16;
+
 __global__ void __launch_bounds__(256) k_bias_grad(const __nv_bfloat16* dZt, int n, float* g) {
     __shared__ float red[8];
-    const __nv_bfloat16* row = dZt + (size_t)blockIdx.x * n;
+    const uint4* row = reinterpret_cast<const uint4*>(dZt + (size_t)blockIdx.x * n);
+    const int n8 = n / 8;
+    const int per = (n8 + gridDim.y - 1) / gridDim.y;
+    const int lo = blockIdx.y * per, hi = min(n8, lo + per);
     float s = 0.f;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) s += __bfloat162float(row[i]);
+    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        const uint4 v = row[i];
+        const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&v);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const float2 f = __bfloat1622float2(h[k]);
+            s += f.x + f.y;
+        }
+    }
     for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
     __syncthreads();
     if (threadIdx.x == 0) {
         float t = 0.f;
         for (int w = 0; w < 8; w++) t += red[w];
-        g[blockIdx.x] += t;
+        atomicAdd(&g[blockIdx.x], t);
     }
 }
 
@@ -981,8 +997,9 @@ struct lvn_surrogate {
         GemmArgs g;
         std::memset(&g, 0, sizeof(g));
         g.status = status.as<int>();
-        // split-K over the batch for the weight gradients: 128 samples per MMA stage
-        const int per_split = std::max(kKC, ((n / 148) + kKC - 1) / kKC * kKC);
+        // split-K over the batch for the weight gradients: 128 samples per MMA
+        // stage, about two CTAs per SM
+        const int per_split = std::max(kKC, ((n / (2 * num_sms)) + kKC - 1) / kKC * kKC);
         const int splits = (n + per_split - 1) / per_split;
         for (int l = kLayers - 1; l >= 0; l--) {
             // dZ of the last hidden layer is in buffer 1 (k_head), then the buffers alternate
@@ -997,7 +1014,8 @@ struct lvn_surrogate {
             g.G = grads.as<float>() + w_off(l);
             if (l == 0) SG_CK((gemm<EPI_DW, kIn>(g, splits, stream)));
             else SG_CK((gemm<EPI_DW, kHidden>(g, splits, stream)));
-            k_bias_grad<<<kHidden, 256, 0, stream>>>(dZt[buf].as<__nv_bfloat16>(), n, grads.as<float>() + b_off(l));
+            k_bias_grad<<<dim3(kHidden, kBiasSplits), 256, 0, stream>>>(dZt[buf].as<__nv_bfloat16>(), n,
+                                                                        grads.as<float>() + b_off(l));
             SG_CK(cudaGetLastError());
             if (l == 0) break;
             // dZ_{l-1} = (dZ_l W_l) * silu'(Z_{l-1})
