@@ -50,6 +50,10 @@ extern "C" {
 #define LVN_OPT_CACHE         2   /* 1 = keep density-field / octree caches (default) */
 #define LVN_OPT_PROFILE       3   /* 1 = record per-stage CUDA events                 */
 #define LVN_OPT_GRAPHS        4   /* 1 = run batches as one captured CUDA graph (default) */
+#define LVN_OPT_HOST_WRITES   5   /* pinned host outputs: 1 = written by the kernels over the
+                                     host link as they are made (default); 0 = meshed into
+                                     device pools, then moved by the copy engine, which leaves
+                                     the SMs to another context's batch in flight */
 
 /* CSGOperationInfo (leven/src/compute.h:16-24; apply_csg_operation.cl:5-14), 48 B */
 typedef struct lvn_csg_op {

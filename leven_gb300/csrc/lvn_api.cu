@@ -336,6 +336,7 @@ struct lvn_meshgen {
     // a batch in flight on a host thread of its own (lvn_meshgen_generate_chunks_async)
     std::thread async_thread;
     bool async_active = false;
+    bool host_writes = true;  // LVN_OPT_HOST_WRITES
     int async_rc = 0;
     std::vector<lvn_chunk_desc> async_chunks;
     cudaStream_t stream = nullptr;
@@ -1479,6 +1480,7 @@ int lvn_meshgen_set_option(lvn_meshgen* m, int32_t option, int32_t value) {
         case LVN_OPT_CACHE: m->cache = value != 0; return LVN_OK;
         case LVN_OPT_PROFILE: m->profile = value != 0; return LVN_OK;
         case LVN_OPT_GRAPHS: m->use_graphs = value != 0; return LVN_OK;
+        case LVN_OPT_HOST_WRITES: m->host_writes = value != 0; return LVN_OK;
         default: return LVN_ERR_INVALID;
     }
 }
@@ -1623,7 +1625,7 @@ int lvn_meshgen_generate_chunks(lvn_meshgen* m, const lvn_chunk_desc* chunks, in
     if (rc) return rc;
     const bool dev = out->memory == LVN_MEMORY_DEVICE;
     DirectOut direct;
-    const bool use_direct = !dev && direct_addresses(out, &direct);
+    const bool use_direct = !dev && m->host_writes && direct_addresses(out, &direct);
     if (use_direct && !m->side) {
         // exports take free SM slots ahead of the compute kernels they overlap
         int lo = 0, hi = 0;

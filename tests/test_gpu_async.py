@@ -20,7 +20,10 @@ def host_out(lvn, torch, cap_v, cap_t, cap_s, results):
     return bo, (hv, ht, hs)
 
 
-def test_two_batches_in_flight_match_the_synchronous_call(lvn_gpu):
+@pytest.mark.parametrize("host_writes", [1, 0])
+def test_two_batches_in_flight_match_the_synchronous_call(lvn_gpu, host_writes):
+    """host_writes 1: the kernels write the pinned arrays; 0: device pools and
+    a copy-engine transfer (LVN_OPT_HOST_WRITES)."""
     torch = pytest.importorskip("torch")
     lvn = lvn_gpu
     wl = W.tiled_csg(4, 2, 4, n_ops=16, seed=11)
@@ -37,6 +40,7 @@ def test_two_batches_in_flight_match_the_synchronous_call(lvn_gpu):
         keep = []
         for k, h in enumerate(halves):
             ctx[k].set_option(lvn.LVN_OPT_CACHE, 0)
+            ctx[k].set_option(lvn.LVN_OPT_HOST_WRITES, host_writes)
         for rnd in range(2):  # two rounds, so each context runs a second batch after its wait
             outs = []
             for k, h in enumerate(halves):
