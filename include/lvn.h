@@ -54,6 +54,11 @@ extern "C" {
                                      host link as they are made (default); 0 = meshed into
                                      device pools, then moved by the copy engine, which leaves
                                      the SMs to another context's batch in flight */
+#define LVN_OPT_COMPUTE_ORDER 6   /* 1 = the context's batches join a device-wide order: a
+                                      batch's kernels start after the kernels of the previous
+                                      ordered batch (any context) have ended; its copy-engine
+                                      transfers stay outside the order, so they overlap the next
+                                      batch's kernels (default 0) */
 
 /* CSGOperationInfo (leven/src/compute.h:16-24; apply_csg_operation.cl:5-14), 48 B */
 typedef struct lvn_csg_op {

@@ -337,6 +337,8 @@ struct lvn_meshgen {
     std::thread async_thread;
     bool async_active = false;
     bool host_writes = true;  // LVN_OPT_HOST_WRITES
+    bool compute_order = false;  // LVN_OPT_COMPUTE_ORDER
+    cudaEvent_t ev_order = nullptr;  // recorded after this context's last ordered batch's kernels
     int async_rc = 0;
     std::vector<lvn_chunk_desc> async_chunks;
     cudaStream_t stream = nullptr;
@@ -937,6 +939,33 @@ int surrogate_prologue(lvn_meshgen* m, const std::vector<ChunkDesc>& descs, size
     return LVN_OK;
 }
 
+// LVN_OPT_COMPUTE_ORDER: the ordered contexts' batches run their kernels one
+// batch after another.  A batch's stream waits for the event recorded after
+// the previous ordered batch's kernels (any context); the copy-engine
+// transfers a batch enqueues after its kernels are not covered by that event,
+// so they overlap the next batch's kernels instead of competing with them for
+// SMs and L2.  The mutex makes "wait for the last, then become the last" one
+// step across host threads.
+std::mutex g_order_mutex;
+cudaEvent_t g_order_last = nullptr;
+const lvn_meshgen* g_order_owner = nullptr;
+
+int order_begin(lvn_meshgen* m, std::unique_lock<std::mutex>& lock) {
+    if (!m->compute_order) return LVN_OK;
+    lock = std::unique_lock<std::mutex>(g_order_mutex);
+    if (g_order_last && g_order_owner != m) LVN_CK(cudaStreamWaitEvent(m->stream, g_order_last, 0));
+    return LVN_OK;
+}
+
+int order_end(lvn_meshgen* m) {  // the caller holds the lock order_begin took
+    if (!m->compute_order) return LVN_OK;
+    if (!m->ev_order) LVN_CK(cudaEventCreateWithFlags(&m->ev_order, cudaEventDisableTiming));
+    LVN_CK(cudaEventRecord(m->ev_order, m->stream));
+    g_order_last = m->ev_order;
+    g_order_owner = m;
+    return LVN_OK;
+}
+
 // Run fresh chunks end to end into the internal pools (or the caller's device
 // buffers when `dev_out` is given).  Grows the pools and reruns once when a
 // pool overflowed; retries the hash with new parameters when an insert failed.
@@ -1032,9 +1061,15 @@ int run_fresh_batch(lvn_meshgen* m, std::vector<ChunkDesc>& descs, const std::ve
                 LVN_CK(ie);
                 m->graph_key = key;
             }
+            std::unique_lock<std::mutex> order;
+            if ((rc = order_begin(m, order))) return rc;
             LVN_CK(cudaGraphLaunch(m->graph_exec, m->stream));
+            if ((rc = order_end(m))) return rc;
         } else {
+            std::unique_lock<std::mutex> order;
+            if ((rc = order_begin(m, order))) return rc;
             rc = enqueue_all();
+            if (!rc) rc = order_end(m);
             if (rc) return rc;
         }
         rc = finish_states(m, n);
@@ -1420,6 +1455,14 @@ void lvn_meshgen_destroy(lvn_meshgen* m) {
     if (!m) return;
     lvn_meshgen_wait(m);
     cudaStreamSynchronize(m->stream);
+    {
+        std::lock_guard<std::mutex> lock(g_order_mutex);
+        if (g_order_owner == m) {
+            g_order_last = nullptr;
+            g_order_owner = nullptr;
+        }
+    }
+    if (m->ev_order) cudaEventDestroy(m->ev_order);
     DevBuf* bufs[] = {&m->desc,       &m->cs,         &m->bs,         &m->brushes,      &m->mats,  &m->planes, &m->hmap,
                       &m->edge_tiles, &m->vox_tiles,  &m->edge_keys,  &m->edge_chunk,   &m->edge_info, &m->edge_work,
                       &m->node_codes, &m->node_info,  &m->node_chunk, &m->edge_slots,   &m->node_slots,
@@ -1481,6 +1524,7 @@ int lvn_meshgen_set_option(lvn_meshgen* m, int32_t option, int32_t value) {
         case LVN_OPT_PROFILE: m->profile = value != 0; return LVN_OK;
         case LVN_OPT_GRAPHS: m->use_graphs = value != 0; return LVN_OK;
         case LVN_OPT_HOST_WRITES: m->host_writes = value != 0; return LVN_OK;
+        case LVN_OPT_COMPUTE_ORDER: m->compute_order = value != 0; return LVN_OK;
         default: return LVN_ERR_INVALID;
     }
 }

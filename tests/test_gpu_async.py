@@ -20,10 +20,11 @@ def host_out(lvn, torch, cap_v, cap_t, cap_s, results):
     return bo, (hv, ht, hs)
 
 
-@pytest.mark.parametrize("host_writes", [1, 0])
-def test_two_batches_in_flight_match_the_synchronous_call(lvn_gpu, host_writes):
+@pytest.mark.parametrize("host_writes,order", [(1, 0), (0, 0), (0, 1), (1, 1)])
+def test_two_batches_in_flight_match_the_synchronous_call(lvn_gpu, host_writes, order):
     """host_writes 1: the kernels write the pinned arrays; 0: device pools and
-    a copy-engine transfer (LVN_OPT_HOST_WRITES)."""
+    a copy-engine transfer (LVN_OPT_HOST_WRITES).  order 1: both contexts'
+    kernels in the device-wide order (LVN_OPT_COMPUTE_ORDER)."""
     torch = pytest.importorskip("torch")
     lvn = lvn_gpu
     wl = W.tiled_csg(4, 2, 4, n_ops=16, seed=11)
@@ -41,6 +42,7 @@ def test_two_batches_in_flight_match_the_synchronous_call(lvn_gpu, host_writes):
         for k, h in enumerate(halves):
             ctx[k].set_option(lvn.LVN_OPT_CACHE, 0)
             ctx[k].set_option(lvn.LVN_OPT_HOST_WRITES, host_writes)
+            ctx[k].set_option(lvn.LVN_OPT_COMPUTE_ORDER, order)
         for rnd in range(2):  # two rounds, so each context runs a second batch after its wait
             outs = []
             for k, h in enumerate(halves):
@@ -65,6 +67,11 @@ def test_two_batches_in_flight_match_the_synchronous_call(lvn_gpu, host_writes):
                 got = np.ctypeslib.as_array(C.cast(results, C.POINTER(C.c_int32)), shape=(n, 8))
                 assert np.array_equal(got, res)
         assert ctx[0].wait() == 0  # nothing in flight
+        # a context closed while it was the last in the order leaves the order
+        # empty; the next ordered batch waits on nothing
+        ctx[1].close()
+        V, T, S, res = ctx[0].generate_chunks(halves[0])
+        assert np.array_equal(V.view(np.int32), want[0][0].view(np.int32))
     finally:
         ref.close()
         for c in ctx:
