@@ -764,6 +764,432 @@ __global__ void __launch_bounds__(128 * kInferWG, 1) k_mlp_infer(InferArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// Fused training: the forward, the loss, the backward and the weight and bias
+// gradients of 128-row tiles in one persistent kernel, one launch per step.
+//
+// Each CTA (8 warps) takes a run of tiles.  The four hidden layers' BF16
+// weights stay in shared memory, with two activation images and one dZ image
+// (216 KB).  Tensor memory holds the working accumulator (columns 0-127) and
+// the weight-gradient accumulators of layers 1-3 (128 l + 0-127), which add
+// up over the CTA's tiles for the whole step.  Layer 0's weight gradient
+// needs the features and dZ0 of every tile; those images wait in the CTA's
+// scratch (global memory, about 350 KB per CTA, in L2) and are contracted into
+// the working accumulator after the last tile.
+//
+// A thread owns TMEM lane / tile row 32 (warp & 3) + lane and the column half
+// 64 (warp >> 2) .. + 63.  Per tile:
+//   features -> XA (and the X0 image to scratch)
+//   layer l: acc = X_l W_l^T; z = acc + b_l -> BF16 z image (scratch);
+//            X_{l+1} = BF16 silu(z) -> the other image (X1 also to scratch)
+//   head:    y = X4 . w4 + b4 (two half sums), r = y - t / s, dy = 2 r / n,
+//            dZ3 = dy w4 silu'(z3) -> the dZ image
+//   l = 3, 2, 1: dW_l += dZ_l^T X_l and acc = dZ_l W_l in one commit;
+//            dZ_{l-1} = acc silu'(z_{l-1}) -> the dZ image (dZ0 to scratch)
+// The weight-gradient products read the dZ and X images as MN-major operands
+// (the same core matrices, K running over the tile's rows) and the input
+// gradient reads W_l as an MN-major B, so no transposed copy is ever made.
+// Bias and head-weight gradients are column sums over the tile's rows: a
+// warp's 32 rows are reduced by a butterfly that leaves column L's sum in
+// lane L, kept in registers across tiles.  The CTA writes its gradient and
+// loss to its own row of `partial`; k_adam_partials sums the rows in a fixed
+// order, so the step is deterministic.
+// ---------------------------------------------------------------------------
+
+constexpr uint32_t kCoreCol = (kTile / 8) * 128;  // bytes between core-matrix columns of a 128-row image
+constexpr int kTrainThreads = 256;
+constexpr int kX0Bytes = kTile * kIn * 2;       // 24 KB feature image
+constexpr int kImgBytes = kTile * kHidden * 2;  // 32 KB activation image
+constexpr int kTrainSmem = kWbBytes + 3 * kImgBytes;
+static_assert(kTrainSmem + 2 * kTile * 4 + 64 <= 227 * 1024, "one CTA per SM");
+constexpr size_t kSlotBytes = (size_t)kX0Bytes + kImgBytes;  // per tile: X0 and dZ0 images
+constexpr size_t kTransientBytes = 4 * (size_t)kImgBytes;    // z0, z1, z2 and X1 images of the tile in hand
+constexpr int kPartStride = (kParams + 1 + 3) / 4 * 4;       // gradient, then the loss; 16-byte rows
+constexpr uint32_t kIdescFwd = umma_idesc(kTile, kHidden);
+constexpr uint32_t kIdescDX = umma_idesc(kTile, kHidden) | (1u << 16);           // B MN-major
+constexpr uint32_t kIdescDW = umma_idesc(kHidden, kHidden) | (1u << 15) | (1u << 16);  // A and B MN-major
+constexpr uint32_t kIdescDW0 = umma_idesc(kHidden, kIn) | (1u << 15) | (1u << 16);
+
+struct TrainArgs {
+    const float4* pool;  // samples (x, y, z, density); row i of the batch is pool[(first + i) % pool_n]
+    int64_t pool_n, first;
+    int n;               // batch rows, a multiple of kTile
+    int tiles_per_cta;
+    const __nv_bfloat16* wb;
+    const float* params;
+    Domain dom;
+    FeatureFreqs ff;
+    float out_scale;
+    uint8_t* scratch;  // gridDim.x x (tiles_per_cta x kSlotBytes + kTransientBytes)
+    float* partial;    // gridDim.x x kPartStride
+    int* status;
+};
+
+// byte offset of core-matrix column c (8 elements), row r of a 128-row image
+__device__ __forceinline__ uint32_t img_off(int c, int r) { return (uint32_t)c * kCoreCol + (uint32_t)r * 16u; }
+
+__device__ __forceinline__ uint32_t bf2_bits(float a, float b) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+__device__ __forceinline__ uint4 pack8(const float* v) {
+    return make_uint4(bf2_bits(v[0], v[1]), bf2_bits(v[2], v[3]), bf2_bits(v[4], v[5]), bf2_bits(v[6], v[7]));
+}
+__device__ __forceinline__ void unpack8(uint4 u, float* v) {
+    const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w[i]));
+        v[2 * i] = f.x;
+        v[2 * i + 1] = f.y;
+    }
+}
+__device__ __forceinline__ float bf16_round(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+
+// Column sums of a warp's 32 rows: lane L holds row L's 32 values in v (which
+// this overwrites) and gets back the sum of column L over the 32 rows.  Each
+// of the five halvings keeps half of the remaining columns and adds the
+// partner lane's copy of them (31 shuffles in all).
+__device__ __forceinline__ float warp_column_sums(float (&v)[32], int lane) {
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) {
+        const bool up = (lane & off) != 0;
+#pragma unroll
+        for (int j = 0; j < off; j++) {
+            const float send = up ? v[j] : v[j + off];
+            const float keep = up ? v[j + off] : v[j];
+            v[j] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+        }
+    }
+    return v[0];
+}
+
+// every thread waits for the commit; false for the whole CTA when it did not
+// arrive within the poll limit
+__device__ __forceinline__ bool cta_wait(uint64_t* bar, uint32_t& phase) {
+    uint32_t polls = 0;
+    bool late = false;
+    while (!mbar_try_wait(bar, phase))
+        if (++polls == kWaitLimit) {
+            late = true;
+            break;
+        }
+    phase ^= 1u;
+    const bool ok = !__syncthreads_or(late);
+    tc_fence_after();
+    return ok;
+}
+
+// shared-memory writes of this CTA made visible to the tensor core, then one
+// barrier; thread 0 issues next
+__device__ __forceinline__ void to_tensor_core() {
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kTrainThreads, 1) k_mlp_train(TrainArgs a) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tmem_base;
+    __shared__ float ypart[2][kTile];
+    uint8_t* sW = smem;
+    uint8_t* sXA = smem + kWbBytes;
+    uint8_t* sXB = sXA + kImgBytes;
+    uint8_t* sDZ = sXB + kImgBytes;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int q = warp & 3, h = warp >> 2;
+    const int row = 32 * q + lane;  // tile row = TMEM lane; columns 64 h .. 64 h + 63
+    const uint32_t lane_base = (uint32_t)(32 * q) << 16;
+    for (int l = 0; l < kLayers; l++) {
+        const int in = in_dim(l), cores = in / 8;
+        uint8_t* dst = sW + 2 * wb_off(l);
+        for (int i = threadIdx.x; i < kHidden * cores; i += blockDim.x) {
+            const int r = i % kHidden, c = i / kHidden;
+            cp_async16(dst + img_off(c, r), a.wb + wb_off(l) + (size_t)r * in + 8 * c);
+        }
+    }
+    if (warp == 0) tmem_alloc(&tmem_base, 512);
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    cp_async_wait_all();
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+    const uint32_t w_addr = smem_u32(sW), xa_addr = smem_u32(sXA), xb_addr = smem_u32(sXB), dz_addr = smem_u32(sDZ);
+    uint8_t* scr = a.scratch + (size_t)blockIdx.x * ((size_t)a.tiles_per_cta * kSlotBytes + kTransientBytes);
+    auto zimg = [scr](int l) { return scr + (size_t)l * kImgBytes; };  // z_l, l = 0, 1, 2
+    uint8_t* x1img = scr + 3 * kImgBytes;
+    uint8_t* slots = scr + kTransientBytes;
+    const int ntiles = a.n / kTile;
+    const int t0 = blockIdx.x * a.tiles_per_cta, t1 = min(ntiles, t0 + a.tiles_per_cta);
+    const float b4 = a.params[kHeadB];
+    float db[kLayers][2] = {}, gw4[2] = {}, lsum = 0.f, gb4 = 0.f;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int t = t0; t < t1 && ok; t++) {
+        uint8_t* x0img = slots + (size_t)(t - t0) * kSlotBytes;
+        uint8_t* dz0img = x0img + kX0Bytes;
+        const float4 p = a.pool[(a.first + (int64_t)t * kTile + row) % a.pool_n];
+        const float target = p.w / a.out_scale;
+        // features: this thread's 8 of each axis' 16 frequencies, sin and cos
+        {
+            const float c[3] = {p.x, p.y, p.z};
+#pragma unroll
+            for (int ax = 0; ax < 3; ax++) {
+                const float u = 2.f * (c[ax] - a.dom.lo[ax]) / (a.dom.hi[ax] - a.dom.lo[ax]) - 1.f;
+                float sv[8], cv[8];
+#pragma unroll
+                for (int k = 0; k < 8; k++) sincos_pi(a.ff.f[ax][8 * h + k] * u, sv[k], cv[k]);
+                const uint4 us = pack8(sv), uc = pack8(cv);
+                const int cs = 4 * ax + h, cc = 4 * ax + 2 + h;
+                *reinterpret_cast<uint4*>(sXA + img_off(cs, row)) = us;
+                *reinterpret_cast<uint4*>(sXA + img_off(cc, row)) = uc;
+                *reinterpret_cast<uint4*>(x0img + img_off(cs, row)) = us;
+                *reinterpret_cast<uint4*>(x0img + img_off(cc, row)) = uc;
+            }
+        }
+        // forward
+        uint8_t* src = sXA;
+        uint8_t* dst = sXB;
+#pragma unroll 1
+        for (int l = 0; l < kLayers && ok; l++) {
+            to_tensor_core();
+            if (threadIdx.x == 0) {
+                tc_fence_after();
+                const uint32_t s_addr = smem_u32(src), wl = w_addr + 2 * wb_off(l);
+                for (int s = 0; s < in_dim(l) / 16; s++)
+                    umma_bf16(tmem, umma_desc(s_addr + 2 * s * kCoreCol, kCoreCol, 128),
+                              umma_desc(wl + 2 * s * kCoreCol, kCoreCol, 128), kIdescFwd, s > 0 ? 1u : 0u);
+                umma_commit(&bar);
+            }
+            ok = cta_wait(&bar, phase);
+            if (!ok) break;
+            const float* bias = a.params + b_off(l);
+            if (l < kLayers - 1) {
+#pragma unroll
+                for (int k = 0; k < 2; k++) {
+                    const int cc = 2 * h + k;
+                    float v[32];
+                    tmem_ld32(tmem + lane_base + (uint32_t)(32 * cc), v);
+#pragma unroll
+                    for (int j = 0; j < 32; j++) v[j] += __ldg(bias + 32 * cc + j);
+#pragma unroll
+                    for (int g = 0; g < 4; g++)
+                        *reinterpret_cast<uint4*>(zimg(l) + img_off(4 * cc + g, row)) = pack8(v + 8 * g);
+#pragma unroll
+                    for (int j = 0; j < 32; j++) v[j] = silu(v[j]);
+#pragma unroll
+                    for (int g = 0; g < 4; g++) {
+                        const uint4 u = pack8(v + 8 * g);
+                        *reinterpret_cast<uint4*>(dst + img_off(4 * cc + g, row)) = u;
+                        if (l == 0) *reinterpret_cast<uint4*>(x1img + img_off(4 * cc + g, row)) = u;
+                    }
+                }
+                uint8_t* tmp = src;
+                src = dst;
+                dst = tmp;
+            } else {
+                // head: y from the BF16 activations, as in inference
+                const float* w4 = a.params + kHeadW;
+                float y = 0.f;
+#pragma unroll
+                for (int k = 0; k < 2; k++) {
+                    const int cc = 2 * h + k;
+                    float v[32];
+                    tmem_ld32(tmem + lane_base + (uint32_t)(32 * cc), v);
+#pragma unroll
+                    for (int j = 0; j < 32; j++)
+                        y = fmaf(bf16_round(silu(v[j] + __ldg(bias + 32 * cc + j))), __ldg(w4 + 32 * cc + j), y);
+                }
+                ypart[h][row] = y;
+                __syncthreads();
+                const float r = ypart[0][row] + ypart[1][row] + b4 - target;
+                const float dy = 2.f * r / (float)a.n;
+                if (h == 0) {
+                    lsum = fmaf(r, r, lsum);
+                    gb4 += dy;
+                }
+#pragma unroll
+                for (int k = 0; k < 2; k++) {
+                    const int cc = 2 * h + k;
+                    float v[32], g4[32];
+                    tmem_ld32(tmem + lane_base + (uint32_t)(32 * cc), v);
+#pragma unroll
+                    for (int j = 0; j < 32; j++) {
+                        const float z = v[j] + __ldg(bias + 32 * cc + j);
+                        g4[j] = dy * bf16_round(silu(z));
+                        v[j] = bf16_round(dy * __ldg(w4 + 32 * cc + j) * silu_grad(z));
+                    }
+#pragma unroll
+                    for (int g = 0; g < 4; g++)
+                        *reinterpret_cast<uint4*>(sDZ + img_off(4 * cc + g, row)) = pack8(v + 8 * g);
+                    gw4[k] += warp_column_sums(g4, lane);
+                    db[kLayers - 1][k] += warp_column_sums(v, lane);
+                }
+            }
+        }
+        // backward: after the forward X2 is in XA and X3 in XB
+#pragma unroll
+        for (int l = kLayers - 1; l >= 1; l--) {
+            if (!ok) break;
+            if (l == 1) cp_async_wait_all();  // X1 back in XB
+            to_tensor_core();
+            if (threadIdx.x == 0) {
+                tc_fence_after();
+                // dW_l (+)= dZ_l^T X_l: M = 128 outputs, N = 128 inputs, K = the tile's rows
+                const uint32_t x_addr = l == 2 ? xa_addr : xb_addr;
+                for (int s = 0; s < kTile / 16; s++)
+                    umma_bf16(tmem + (uint32_t)(128 * l), umma_desc(dz_addr + 256 * s, 128, kCoreCol),
+                              umma_desc(x_addr + 256 * s, 128, kCoreCol), kIdescDW, (t > t0 || s > 0) ? 1u : 0u);
+                // dX = dZ_l W_l: M = the tile's rows, N = 128 inputs, K = 128 outputs
+                const uint32_t wl = w_addr + 2 * wb_off(l);
+                for (int s = 0; s < kHidden / 16; s++)
+                    umma_bf16(tmem, umma_desc(dz_addr + 2 * s * kCoreCol, kCoreCol, 128),
+                              umma_desc(wl + 256 * s, 128, kCoreCol), kIdescDX, s > 0 ? 1u : 0u);
+                umma_commit(&bar);
+            }
+            // this thread's z_{l-1} (64 BF16 values) while the products run
+            uint4 zr[8];
+#pragma unroll
+            for (int g = 0; g < 8; g++) zr[g] = *reinterpret_cast<const uint4*>(zimg(l - 1) + img_off(8 * h + g, row));
+            ok = cta_wait(&bar, phase);
+            if (!ok) break;
+            if (l == kLayers - 1) {
+                // X1 into XB (X3's products are done) for dW_1, two steps on
+                for (int i = threadIdx.x; i < kImgBytes / 16; i += kTrainThreads)
+                    cp_async16(sXB + 16 * i, x1img + 16 * i);
+            }
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                const int cc = 2 * h + k;
+                float v[32], z[32];
+                tmem_ld32(tmem + lane_base + (uint32_t)(32 * cc), v);
+#pragma unroll
+                for (int g = 0; g < 4; g++) unpack8(zr[4 * k + g], z + 8 * g);
+#pragma unroll
+                for (int j = 0; j < 32; j++) v[j] = bf16_round(v[j] * silu_grad(z[j]));
+                uint8_t* out = l > 1 ? sDZ : dz0img;
+#pragma unroll
+                for (int g = 0; g < 4; g++) *reinterpret_cast<uint4*>(out + img_off(4 * cc + g, row)) = pack8(v + 8 * g);
+                db[l - 1][k] += warp_column_sums(v, lane);
+            }
+        }
+    }
+    // dW_0 over the CTA's tiles, from the feature and dZ0 images in scratch
+    // (written by other threads of the CTA: the barrier orders their stores
+    // before these reads)
+    __syncthreads();
+    for (int t = t0; t < t1 && ok; t++) {
+        const uint8_t* x0img = slots + (size_t)(t - t0) * kSlotBytes;
+        const uint8_t* dz0img = x0img + kX0Bytes;
+        for (int i = threadIdx.x; i < kX0Bytes / 16; i += kTrainThreads) cp_async16(sXA + 16 * i, x0img + 16 * i);
+        for (int i = threadIdx.x; i < kImgBytes / 16; i += kTrainThreads) cp_async16(sDZ + 16 * i, dz0img + 16 * i);
+        cp_async_wait_all();
+        to_tensor_core();
+        if (threadIdx.x == 0) {
+            tc_fence_after();
+            for (int s = 0; s < kTile / 16; s++)
+                umma_bf16(tmem, umma_desc(dz_addr + 256 * s, 128, kCoreCol), umma_desc(xa_addr + 256 * s, 128, kCoreCol),
+                          kIdescDW0, (t > t0 || s > 0) ? 1u : 0u);
+            umma_commit(&bar);
+        }
+        ok = cta_wait(&bar, phase);
+    }
+    float* part = a.partial + (size_t)blockIdx.x * kPartStride;
+    if (ok) {
+        const bool any = t1 > t0;
+        // weight gradients: this thread's lane is output row `row` of each dW
+#pragma unroll 1
+        for (int l = 0; l < kLayers; l++) {
+            const int in = in_dim(l);
+            const uint32_t col0 = l == 0 ? 0u : (uint32_t)(128 * l);
+            for (int cc = h; cc < in / 32; cc += 2) {
+                float v[32];
+                if (any) tmem_ld32(tmem + col0 + lane_base + (uint32_t)(32 * cc), v);
+#pragma unroll
+                for (int j = 0; j < 32; j++) v[j] = any ? v[j] : 0.f;
+                float4* d4 = reinterpret_cast<float4*>(part + w_off(l) + (size_t)row * in + 32 * cc);
+#pragma unroll
+                for (int j = 0; j < 8; j++) d4[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+            }
+        }
+        // column sums over the four lane quarters: biases, then w4
+        float* red = reinterpret_cast<float*>(sXA);  // [kLayers + 1][4][kHidden]
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+            const int col = 64 * h + 32 * k + lane;
+#pragma unroll
+            for (int l = 0; l < kLayers; l++) red[(l * 4 + q) * kHidden + col] = db[l][k];
+            red[(kLayers * 4 + q) * kHidden + col] = gw4[k];
+        }
+        // loss and b4 (rows are summed by the h == 0 threads)
+        float ls = lsum, gb = gb4;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            ls += __shfl_xor_sync(0xffffffffu, ls, o);
+            gb += __shfl_xor_sync(0xffffffffu, gb, o);
+        }
+        if (h == 0 && lane == 0) {
+            ypart[0][q] = ls;
+            ypart[1][q] = gb;
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < (kLayers + 1) * kHidden; i += kTrainThreads) {
+            const int l = i / kHidden, col = i % kHidden;
+            float s = 0.f;
+#pragma unroll
+            for (int qq = 0; qq < 4; qq++) s += red[(l * 4 + qq) * kHidden + col];
+            part[(l < kLayers ? b_off(l) : kHeadW) + col] = s;
+        }
+        if (threadIdx.x == 0) {
+            part[kHeadB] = ((ypart[1][0] + ypart[1][1]) + ypart[1][2]) + ypart[1][3];
+            part[kParams] = (((ypart[0][0] + ypart[0][1]) + ypart[0][2]) + ypart[0][3]) / (float)a.n;
+        }
+    } else {
+        // as in k_gemm: a second bounded wait for the pending commit before
+        // the columns are freed; the status flag makes the host discard the
+        // step's results either way
+        if (threadIdx.x == 0) atomicExch(a.status, 1);
+        uint32_t polls = 0;
+        while (!mbar_try_wait(&bar, phase ^ 1u) && ++polls < 4 * kWaitLimit) {
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem_base, 512);
+}
+
+// The step's gradient: the sum of the CTAs' rows of `partial`, in CTA order.
+// With lr > 0, Adam (beta 0.9 / 0.999, eps 1e-8) on the FP32 master weights
+// and the BF16 copies refreshed; `grad` and `loss` receive the sums when not
+// null.
+__global__ void k_adam_partials(const float* partial, int parts, float* p, float* m, float* v, float lr, float c1,
+                                float c2, __nv_bfloat16* wb, LayerMap lm, float* grad, float* loss) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= kParams; i += gridDim.x * blockDim.x) {
+        float gi = 0.f;
+        for (int c = 0; c < parts; c++) gi += partial[(size_t)c * kPartStride + i];
+        if (i == kParams) {  // the loss
+            if (loss) *loss = gi;
+            continue;
+        }
+        if (grad) grad[i] = gi;
+        if (!(lr > 0.f)) continue;
+        const float mi = 0.9f * m[i] + 0.1f * gi;
+        const float vi = 0.999f * v[i] + 0.001f * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        const float pi = p[i] - lr * (mi * c1) / (sqrtf(vi * c2) + 1e-8f);
+        p[i] = pi;
+#pragma unroll
+        for (int l = 0; l < kLayers; l++) {
+            const int rel = i - lm.w[l];
+            if (rel >= 0 && rel < kHidden * lm.in[l]) wb[lm.wb[l] + rel] = __float2bfloat16_rn(pi);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // FP64 density: the 2D fBm heightfield (+ 3D fBm caves) in double precision,
 // with the exact simplex constants, over the same permutation image and
 // gradient table, as the reference the surrogate's and the FP32 density's
@@ -937,6 +1363,42 @@ struct lvn_surrogate {
     int64_t pool_n = 0;
     int64_t pool_next = 0;
     int step = 0;
+    Buf train_scratch, partial;  // k_mlp_train's per-CTA images and gradient rows
+
+    // one fused forward + backward over rows first .. first + n - 1 (mod
+    // pool_n) of pool_d; *parts = the rows of `partial` it writes
+    int train_launch(const float4* pool_d, int64_t pool_n_, int64_t first, int n, int* parts) {
+        static bool configured = false;
+        if (!configured) {
+            SG_CK(cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrainSmem));
+            configured = true;
+        }
+        const int ntiles = n / kTile;
+        const int tpc = (ntiles + num_sms - 1) / num_sms;
+        const int grid = (ntiles + tpc - 1) / tpc;
+        int rc;
+        if ((rc = train_scratch.ensure((size_t)grid * ((size_t)tpc * kSlotBytes + kTransientBytes)))) return rc;
+        if ((rc = partial.ensure(sizeof(float) * (size_t)grid * kPartStride))) return rc;
+        TrainArgs a;
+        std::memset(&a, 0, sizeof(a));
+        a.pool = pool_d;
+        a.pool_n = pool_n_;
+        a.first = first;
+        a.n = n;
+        a.tiles_per_cta = tpc;
+        a.wb = wb.as<__nv_bfloat16>();
+        a.params = params.as<float>();
+        a.dom = dom;
+        a.ff = ff;
+        a.out_scale = out_scale;
+        a.scratch = train_scratch.as<uint8_t>();
+        a.partial = partial.as<float>();
+        a.status = status.as<int>();
+        k_mlp_train<<<grid, kTrainThreads, kTrainSmem, stream>>>(a);
+        SG_CK(cudaGetLastError());
+        *parts = grid;
+        return LVN_OK;
+    }
 
     int ensure_batch(int n) {
         if (n <= cap) return LVN_OK;
@@ -1110,7 +1572,8 @@ void lvn_surrogate_destroy(lvn_surrogate* s) {
     if (!s) return;
     if (s->stream) cudaStreamSynchronize(s->stream);
     Buf* bufs[] = {&s->params, &s->grads, &s->adam_m, &s->adam_v, &s->wb, &s->wt, &s->loss, &s->status,
-                   &s->pts, &s->dZ[0], &s->dZ[1], &s->dZt[0], &s->dZt[1], &s->dens, &s->pool, &s->loss_hist};
+                   &s->pts, &s->dZ[0], &s->dZ[1], &s->dZt[0], &s->dZt[1], &s->dens, &s->pool, &s->loss_hist,
+                   &s->train_scratch, &s->partial};
     for (Buf* b : bufs) b->release();
     for (int l = 0; l <= kLayers; l++) {
         s->X[l].release();
@@ -1167,7 +1630,12 @@ int lvn_surrogate_grad(lvn_surrogate* s, const float* samples, int32_t n, float*
     if (!s || !samples || n <= 0 || n % kTile) return LVN_ERR_INVALID;
     int rc = upload_samples(s, samples, n);
     if (rc) return rc;
-    if ((rc = s->backward(n, s->loss.as<float>()))) return rc;
+    int parts = 0;
+    if ((rc = s->train_launch(s->pts.as<float4>(), n, 0, n, &parts))) return rc;
+    k_adam_partials<<<(kParams + 256) / 256, 256, 0, s->stream>>>(s->partial.as<float>(), parts, nullptr, nullptr,
+                                                                   nullptr, 0.f, 0.f, 0.f, nullptr, layer_map(),
+                                                                   s->grads.as<float>(), s->loss.as<float>());
+    SG_CK(cudaGetLastError());
     if ((rc = check_status(s))) return rc;
     if (grad_out) SG_CK(cudaMemcpy(grad_out, s->grads.p, 4ull * kParams, cudaMemcpyDeviceToHost));
     if (loss_out) SG_CK(cudaMemcpy(loss_out, s->loss.p, 4, cudaMemcpyDeviceToHost));
@@ -1177,29 +1645,23 @@ int lvn_surrogate_grad(lvn_surrogate* s, const float* samples, int32_t n, float*
 int lvn_surrogate_train(lvn_surrogate* s, int32_t steps, int32_t batch, float lr, float* losses) {
     if (!s || steps < 0 || batch <= 0 || batch % kTile || !(lr > 0.f)) return LVN_ERR_INVALID;
     if (s->pool_n < batch) return LVN_ERR_INVALID;  // lvn_surrogate_sample first
-    int rc = s->ensure_batch(batch);
-    if (rc) return rc;
+    int rc;
     const LayerMap lm = layer_map();
     // the losses stay on the device until the end, so the host never waits
     // on a step and the launches queue ahead of the GPU
     if (steps > 0 && (rc = s->loss_hist.ensure(sizeof(float) * (size_t)steps))) return rc;
     for (int it = 0; it < steps; it++) {
-        // the next `batch` samples of the pool (wrapping)
+        // the next `batch` samples of the pool (wrapping), read in place
         const int64_t first = s->pool_next;
-        const int64_t take = std::min<int64_t>(batch, s->pool_n - first);
-        SG_CK(cudaMemcpyAsync(s->pts.p, s->pool.as<float4>() + first, sizeof(float4) * take, cudaMemcpyDeviceToDevice,
-                              s->stream));
-        if (take < batch)
-            SG_CK(cudaMemcpyAsync(s->pts.as<float4>() + take, s->pool.p, sizeof(float4) * (batch - take),
-                                  cudaMemcpyDeviceToDevice, s->stream));
         s->pool_next = (first + batch) % s->pool_n;
-        if ((rc = s->backward(batch, s->loss_hist.as<float>() + it))) return rc;
+        int parts = 0;
+        if ((rc = s->train_launch(s->pool.as<float4>(), s->pool_n, first, batch, &parts))) return rc;
         s->step++;
         const float c1 = 1.f / (1.f - std::pow(0.9f, (float)s->step));
         const float c2 = 1.f / (1.f - std::pow(0.999f, (float)s->step));
-        k_adam<<<64, 256, 0, s->stream>>>(s->params.as<float>(), s->grads.as<float>(), s->adam_m.as<float>(),
-                                          s->adam_v.as<float>(), kParams, lr, c1, c2, s->wb.as<__nv_bfloat16>(),
-                                          s->wt.as<__nv_bfloat16>(), lm);
+        k_adam_partials<<<(kParams + 256) / 256, 256, 0, s->stream>>>(
+            s->partial.as<float>(), parts, s->params.as<float>(), s->adam_m.as<float>(), s->adam_v.as<float>(), lr, c1,
+            c2, s->wb.as<__nv_bfloat16>(), lm, nullptr, s->loss_hist.as<float>() + it);
         SG_CK(cudaGetLastError());
     }
     if (losses && steps > 0)

@@ -96,8 +96,12 @@ def test_forward_matches_float64(surrogate):
     assert np.linalg.norm(got - want) <= 0.05 * np.linalg.norm(want) + 1e-3, err.max()
 
 
-def test_gradient_matches_float64(surrogate):
-    pts = surrogate.sample(512, seed=7, fetch=True)
+@pytest.mark.parametrize("n", [512, 40960])
+def test_gradient_matches_float64(surrogate, n):
+    """512 rows: one 128-row tile per CTA of the fused training kernel;
+    40960 rows (320 tiles): several tiles per CTA, the weight gradients
+    accumulated over them in tensor memory, and a last CTA with fewer."""
+    pts = surrogate.sample(n, seed=7, fetch=True)
     g, loss = surrogate.grad(pts)
     rg, rloss = reference(surrogate.params(), pts, pts[:, 3])
     assert abs(loss - rloss) <= 0.02 * rloss
