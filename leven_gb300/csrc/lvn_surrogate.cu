@@ -6,14 +6,14 @@
 // 62,081 parameters.  Weights and activations are BF16, every product is
 // accumulated in FP32, the master weights and Adam moments are FP32.
 //
-// Every matrix product (the four hidden layers forward, their input gradients
-// and their weight gradients) runs on the 5th-generation tensor cores: one
-// elected thread issues tcgen05.mma (kind::f16, BF16 in, FP32 accumulator in
-// tensor memory) on 128-row tiles staged in shared memory, the CTA waits on
-// the MMA's mbarrier commit (bounded), and the epilogue reads the accumulator
-// back with tcgen05.ld and fuses bias + SiLU (forward), SiLU' (input
-// gradient) or the split-K reduction (weight gradient).  The 128 -> 1 head,
-// the Fourier features, the loss and Adam run on the CUDA cores.
+// Every matrix product runs on the 5th-generation tensor cores (tcgen05.mma,
+// kind::f16: BF16 in, FP32 accumulator in tensor memory), issued by one thread
+// per CTA on 128-row tiles staged in shared memory, with bounded waits on the
+// MMA's mbarrier commit:
+//   * training (k_mlp_train): one persistent kernel a step for the features,
+//     the forward, the loss, the backward and every gradient; Adam on the CUDA
+//     cores (k_adam_partials);
+//   * inference (k_mlp_infer): the whole network per 128-point tile.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -34,20 +34,23 @@ constexpr int kFreqs = 16;
 constexpr int kIn = 6 * kFreqs;  // 96
 constexpr int kLayers = 4;       // hidden layers
 constexpr int kTile = 128;       // rows per CTA tile (MMA M)
-constexpr int kKC = 128;         // K per shared-memory stage
 constexpr uint32_t kWaitLimit = 1u << 20;  // mbarrier polls before a CTA gives up
 
 // parameter offsets in the flat FP32 vector: W0 b0 W1 b1 W2 b2 W3 b3 w4 b4
 constexpr int kIn_[kLayers] = {kIn, kHidden, kHidden, kHidden};
 __host__ __device__ constexpr int in_dim(int l) { return l == 0 ? kIn : kHidden; }
-__host__ __device__ constexpr int w_off(int l) { return l == 0 ? 0 : w_off(l - 1) + kHidden * in_dim(l - 1) + kHidden; }
+// (closed forms: the kernels also call these with run-time layer indices)
+__host__ __device__ constexpr int w_off(int l) {
+    return l == 0 ? 0 : (kHidden * kIn + kHidden) + (l - 1) * (kHidden * kHidden + kHidden);
+}
 __host__ __device__ constexpr int b_off(int l) { return w_off(l) + kHidden * in_dim(l); }
 constexpr int kHeadW = w_off(kLayers);
 constexpr int kHeadB = kHeadW + kHidden;
 constexpr int kParams = kHeadB + 1;
+static_assert(w_off(2) == w_off(1) + kHidden * kHidden + kHidden && b_off(0) == kHidden * kIn, "layout");
 static_assert(kParams == 62081, "4 x 128 SiLU MLP on 96 features");
-// BF16 copies: W_l (out x in) and W_l^T (in x out) for l >= 1
-__host__ __device__ constexpr int wb_off(int l) { return l == 0 ? 0 : wb_off(l - 1) + kHidden * in_dim(l - 1); }
+// BF16 copies W_l (out x in)
+__host__ __device__ constexpr int wb_off(int l) { return l == 0 ? 0 : kHidden * kIn + (l - 1) * kHidden * kHidden; }
 constexpr int kWb = wb_off(kLayers);
 
 // ---------------------------------------------------------------------------
@@ -151,163 +154,7 @@ __device__ __forceinline__ void sincos_pi(float r, float& s, float& c) {
 }
 
 // ---------------------------------------------------------------------------
-// GEMM: D[M x N] = A[M x K] B[N x K]^T, A and B BF16 row-major (K contiguous),
-// one 128-row tile of D per CTA, K split over blockIdx.y.
-// ---------------------------------------------------------------------------
-
-enum Epilogue { EPI_FWD = 0, EPI_DX = 1, EPI_DW = 2 };
-
-struct GemmArgs {
-    const __nv_bfloat16* A;
-    const __nv_bfloat16* B;
-    int M, K, lda, ldb;
-    int k_per_split;
-    // EPI_FWD: z = acc + bias -> Z (fp32, optional), X = silu(z) (bf16), Xt (bf16, optional)
-    // EPI_DX : dz = acc * silu'(Zp)  -> X = dz (bf16), Xt (bf16)
-    // EPI_DW : G[row][col] += acc (fp32 atomics)
-    const float* bias;
-    const float* Zp;
-    float* Z;
-    __nv_bfloat16* X;
-    __nv_bfloat16* Xt;
-    float* G;
-    int* status;  // set to 1 when a CTA gave up waiting on its MMAs
-};
-
-constexpr int kGemmSmem = 2 * kTile * kKC * 2;  // A and B stages, 64 KB
-
-template <int EPI, int N>
-__global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
-    extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ uint64_t bar;
-    __shared__ uint32_t tmem_base;
-    uint8_t* sA = smem;
-    uint8_t* sB = smem + kTile * kKC * 2;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.x * kTile;
-    const int kb = blockIdx.y * g.k_per_split;
-    const int ke = min(g.K, kb + g.k_per_split);
-    if (warp == 0) tmem_alloc(&tmem_base, 128);
-    if (threadIdx.x == 0) mbar_init(&bar, 1);
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    const uint32_t tmem = tmem_base;
-    constexpr uint32_t kIdesc = umma_idesc(kTile, N);
-    uint32_t phase = 0;
-    bool ok = true;
-    for (int k0 = kb; k0 < ke && ok; k0 += kKC) {
-        const int kc = min(kKC, ke - k0);  // a multiple of 16
-        const int cores = kc / 8;          // 16-byte core-matrix columns along K
-        // core matrix (row group i, K column c) at c * lbo + i * 128, rows 16 B apart
-        const uint32_t lboA = (kTile / 8) * 128, lboB = (N / 8) * 128;
-        for (int i = threadIdx.x; i < kTile * cores; i += blockDim.x) {
-            const int r = i % kTile, c = i / kTile;
-            cp_async16(sA + c * lboA + r * 16, g.A + (size_t)(m0 + r) * g.lda + k0 + 8 * c);
-        }
-        for (int i = threadIdx.x; i < N * cores; i += blockDim.x) {
-            const int r = i % N, c = i / N;
-            cp_async16(sB + c * lboB + r * 16, g.B + (size_t)r * g.ldb + k0 + 8 * c);
-        }
-        cp_async_wait_all();
-        fence_proxy_async();
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            tc_fence_after();
-            const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
-            for (int s = 0; s < kc / 16; s++)
-                umma_bf16(tmem, umma_desc(a0 + 2 * s * lboA, lboA, 128), umma_desc(b0 + 2 * s * lboB, lboB, 128),
-                          kIdesc, (k0 > kb || s > 0) ? 1u : 0u);
-            umma_commit(&bar);
-        }
-        uint32_t polls = 0;
-        bool late = false;
-        while (!mbar_try_wait(&bar, phase))
-            if (++polls == kWaitLimit) {
-                late = true;
-                break;
-            }
-        phase ^= 1u;
-        ok = !__syncthreads_or(late);  // the whole CTA takes the same path
-        tc_fence_after();
-    }
-    if (!ok) {
-        // The MMAs this CTA committed did not signal within the poll limit.
-        // TMEM is freed below, and a later CTA on this SM may allocate the
-        // same columns, so first wait (bounded again) for the commit: once it
-        // arrives the MMAs are complete and nothing writes the columns.  If
-        // it still does not, the columns are freed all the same: a CTA that
-        // never frees them would stall every later allocation on this SM,
-        // and the status flag set here makes the host discard this call's
-        // results (LVN_ERR_DEVICE_STATUS), including anything a late MMA
-        // wrote.
-        if (lane == 0) atomicExch(g.status, 1);
-        uint32_t polls = 0;
-        while (!mbar_try_wait(&bar, phase ^ 1u) && ++polls < 4 * kWaitLimit) {
-        }
-    } else if (kb < ke) {
-        const int row = warp * 32 + lane;  // D row = TMEM lane
-        const int m = m0 + row;
-#pragma unroll 1
-        for (int cc = 0; cc < N / 32; cc++) {
-            float v[32];
-            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cc * 32), v);
-            const int n0 = cc * 32;
-            if (EPI == EPI_DW) {
-#pragma unroll
-                for (int j = 0; j < 32; j++) atomicAdd(g.G + (size_t)row * N + n0 + j, v[j]);
-            } else {
-                if (EPI == EPI_FWD) {
-#pragma unroll
-                    for (int j = 0; j < 32; j++) v[j] += __ldg(g.bias + n0 + j);
-                    if (g.Z) {
-                        float4* z4 = reinterpret_cast<float4*>(g.Z + (size_t)m * N + n0);
-#pragma unroll
-                        for (int j = 0; j < 8; j++) z4[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
-                    }
-#pragma unroll
-                    for (int j = 0; j < 32; j++) v[j] = silu(v[j]);
-                } else {
-                    const float4* z4 = reinterpret_cast<const float4*>(g.Zp + (size_t)m * N + n0);
-#pragma unroll
-                    for (int j = 0; j < 8; j++) {
-                        const float4 z = z4[j];
-                        v[4 * j] *= silu_grad(z.x);
-                        v[4 * j + 1] *= silu_grad(z.y);
-                        v[4 * j + 2] *= silu_grad(z.z);
-                        v[4 * j + 3] *= silu_grad(z.w);
-                    }
-                }
-                __nv_bfloat162* x2 = reinterpret_cast<__nv_bfloat162*>(g.X + (size_t)m * N + n0);
-#pragma unroll
-                for (int j = 0; j < 16; j++) x2[j] = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
-                if (g.Xt) {
-#pragma unroll
-                    for (int j = 0; j < 32; j++) g.Xt[(size_t)(n0 + j) * g.M + m] = __float2bfloat16_rn(v[j]);
-                }
-            }
-        }
-    }
-    tc_fence_before();
-    __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem, 128);
-}
-
-template <int EPI, int N>
-cudaError_t gemm(const GemmArgs& g, int splits, cudaStream_t s) {
-    static bool configured = false;
-    if (!configured) {
-        const cudaError_t e = cudaFuncSetAttribute(k_gemm<EPI, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
-    dim3 grid(EPI == EPI_DW ? 1 : g.M / kTile, splits);
-    k_gemm<EPI, N><<<grid, 128, kGemmSmem, s>>>(g);
-    return cudaGetLastError();
-}
-
-// ---------------------------------------------------------------------------
-// CUDA-core kernels: samples, features, head + loss, bias gradients, Adam
+// CUDA-core kernels: training samples, the BF16 weight copies
 // ---------------------------------------------------------------------------
 
 struct Domain {
@@ -368,205 +215,17 @@ struct FeatureFreqs {
     float f[3][kFreqs];
 };
 
-// Fourier features of a position normalised to [-1, 1] over the domain:
-// [sin(pi f u_x) x16, cos x16, then y, then z]
-__global__ void k_features(const float4* pts, int n, Domain dom, FeatureFreqs ff, __nv_bfloat16* X,
-                           __nv_bfloat16* Xt) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 p = pts[i];
-        const float c[3] = {p.x, p.y, p.z};
-        __nv_bfloat16* row = X + (size_t)i * kIn;
-#pragma unroll
-        for (int a = 0; a < 3; a++) {
-            const float u = 2.f * (c[a] - dom.lo[a]) / (dom.hi[a] - dom.lo[a]) - 1.f;
-#pragma unroll 4
-            for (int k = 0; k < kFreqs; k++) {
-                float s, co;
-                sincos_pi(ff.f[a][k] * u, s, co);
-                const __nv_bfloat16 bs = __float2bfloat16_rn(s), bc = __float2bfloat16_rn(co);
-                row[a * 2 * kFreqs + k] = bs;
-                row[a * 2 * kFreqs + kFreqs + k] = bc;
-                if (Xt) {
-                    Xt[(size_t)(a * 2 * kFreqs + k) * n + i] = bs;
-                    Xt[(size_t)(a * 2 * kFreqs + kFreqs + k) * n + i] = bc;
-                }
-            }
-        }
-    }
-}
-
-// Head and loss (training): y = X4 . w4 + b4 (density / out_scale),
-// r = y - t / s, loss += r^2 / n, dy = 2 r / n, dZ3 = dy w4 silu'(Z3),
-// gw4 += dy X4, gb4 += dy.  A CTA takes 64-row tiles; a warp takes a row at a
-// time, each lane 4 of its 128 columns, so every global access is a
-// contiguous row segment: X4 and dZ3 as 8-byte, Z3 as 16-byte lane loads and
-// stores.  y is a warp-shuffle sum.  Each lane keeps its 4 columns' gw4
-// partial sums in registers (no shared atomics); the CTA adds them up once at
-// the end.  dZ3^T (the weight gradient's operand) is staged through shared
-// memory and written 64 rows at a time, 128 bytes per column.
-constexpr int kHeadRows = 64;    // rows per tile
-constexpr int kHeadWarps = 8;    // 256 threads
-
-__global__ void __launch_bounds__(32 * kHeadWarps) k_head(const __nv_bfloat16* X4, const float* Z3, const float4* pts,
-                                                          int n, const float* params, float out_scale,
-                                                          __nv_bfloat16* dZ, __nv_bfloat16* dZt, float* grads,
-                                                          float* loss) {
-    __shared__ __align__(16) __nv_bfloat16 sT[kHidden][kHeadRows + 8];  // dZ3 transposed, padded rows
-    __shared__ float gsum[kHeadWarps][kHidden];
-    __shared__ float red[2][kHeadWarps];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int c0 = 4 * lane;  // this lane's columns c0 .. c0 + 3
-    const float4 w = *reinterpret_cast<const float4*>(params + kHeadW + c0);
-    const float b4 = params[kHeadB];
-    float gw0 = 0.f, gw1 = 0.f, gw2 = 0.f, gw3 = 0.f, l = 0.f, gb = 0.f;
-    const int tiles = n / kHeadRows;
-    for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
-        const int r0 = t * kHeadRows;
-        for (int rr = warp; rr < kHeadRows; rr += kHeadWarps) {
-            const int i = r0 + rr;
-            const uint2 xr = *reinterpret_cast<const uint2*>(X4 + (size_t)i * kHidden + c0);
-            const float2 xa = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&xr.x));
-            const float2 xb = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&xr.y));
-            float y = fmaf(xa.x, w.x, fmaf(xa.y, w.y, fmaf(xb.x, w.z, xb.y * w.w)));
-#pragma unroll
-            for (int o = 16; o; o >>= 1) y += __shfl_xor_sync(0xffffffffu, y, o);
-            y += b4;
-            const float r = y - pts[i].w / out_scale;
-            const float dy = 2.f * r / (float)n;
-            if (lane == 0) {
-                l += r * r;
-                gb += dy;
-            }
-            gw0 = fmaf(dy, xa.x, gw0);
-            gw1 = fmaf(dy, xa.y, gw1);
-            gw2 = fmaf(dy, xb.x, gw2);
-            gw3 = fmaf(dy, xb.y, gw3);
-            const float4 z = *reinterpret_cast<const float4*>(Z3 + (size_t)i * kHidden + c0);
-            const __nv_bfloat16 d0 = __float2bfloat16_rn(dy * w.x * silu_grad(z.x));
-            const __nv_bfloat16 d1 = __float2bfloat16_rn(dy * w.y * silu_grad(z.y));
-            const __nv_bfloat16 d2 = __float2bfloat16_rn(dy * w.z * silu_grad(z.z));
-            const __nv_bfloat16 d3 = __float2bfloat16_rn(dy * w.w * silu_grad(z.w));
-            __nv_bfloat162 p01, p23;
-            p01.x = d0;
-            p01.y = d1;
-            p23.x = d2;
-            p23.y = d3;
-            uint2 out;
-            out.x = *reinterpret_cast<uint32_t*>(&p01);
-            out.y = *reinterpret_cast<uint32_t*>(&p23);
-            *reinterpret_cast<uint2*>(dZ + (size_t)i * kHidden + c0) = out;
-            sT[c0][rr] = d0;
-            sT[c0 + 1][rr] = d1;
-            sT[c0 + 2][rr] = d2;
-            sT[c0 + 3][rr] = d3;
-        }
-        __syncthreads();
-        // dZ3^T: column j's 64 rows (128 bytes) by two threads, 4 x 16 bytes each
-        {
-            const int j = threadIdx.x >> 1, half = threadIdx.x & 1;
-            const uint4* src = reinterpret_cast<const uint4*>(&sT[j][32 * half]);
-            uint4* dst = reinterpret_cast<uint4*>(dZt + (size_t)j * n + r0 + 32 * half);
-#pragma unroll
-            for (int q = 0; q < 4; q++) dst[q] = src[q];
-        }
-        __syncthreads();
-    }
-    gsum[warp][c0] = gw0;
-    gsum[warp][c0 + 1] = gw1;
-    gsum[warp][c0 + 2] = gw2;
-    gsum[warp][c0 + 3] = gw3;
-    if (lane == 0) {
-        red[0][warp] = l;
-        red[1][warp] = gb;
-    }
-    __syncthreads();
-    if (threadIdx.x < kHidden) {
-        float s = 0.f;
-#pragma unroll
-        for (int k = 0; k < kHeadWarps; k++) s += gsum[k][threadIdx.x];
-        atomicAdd(&grads[kHeadW + threadIdx.x], s);
-    }
-    if (threadIdx.x == 0) {
-        float sl = 0.f, sg = 0.f;
-        for (int k = 0; k < kHeadWarps; k++) {
-            sl += red[0][k];
-            sg += red[1][k];
-        }
-        atomicAdd(loss, sl / (float)n);
-        atomicAdd(&grads[kHeadB], sg);
-    }
-}
-
-// bias gradient of layer l: the sum over the batch of dZ, i.e. of each row of
-// dZ^T.  A row (n BF16 values, n a multiple of 8) is split over
-// gridDim.y CTAs; each thread reads 16-byte runs of 8 values, the CTA sums
-// them (warp shuffles, then shared memory) and adds its part to g[row].
-constexpr int kBiasSplits = 16;
-
-__global__ void __launch_bounds__(256) k_bias_grad(const __nv_bfloat16* dZt, int n, float* g) {
-    __shared__ float red[8];
-    const uint4* row = reinterpret_cast<const uint4*>(dZt + (size_t)blockIdx.x * n);
-    const int n8 = n / 8;
-    const int per = (n8 + gridDim.y - 1) / gridDim.y;
-    const int lo = blockIdx.y * per, hi = min(n8, lo + per);
-    float s = 0.f;
-    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-        const uint4 v = row[i];
-        const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&v);
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const float2 f = __bfloat1622float2(h[k]);
-            s += f.x + f.y;
-        }
-    }
-    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float t = 0.f;
-        for (int w = 0; w < 8; w++) t += red[w];
-        atomicAdd(&g[blockIdx.x], t);
-    }
-}
-
 struct LayerMap {
     int w[kLayers], b[kLayers], in[kLayers], wb[kLayers];
 };
 
-// Adam (beta 0.9 / 0.999, eps 1e-8) on the FP32 master weights; refreshes the
-// BF16 copies W_l and W_l^T.
-__global__ void k_adam(float* p, const float* g, float* m, float* v, int n, float lr, float c1, float c2,
-                       __nv_bfloat16* wb, __nv_bfloat16* wt, LayerMap lm) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float gi = g[i];
-        const float mi = 0.9f * m[i] + 0.1f * gi;
-        const float vi = 0.999f * v[i] + 0.001f * gi * gi;
-        m[i] = mi;
-        v[i] = vi;
-        const float pi = p[i] - lr * (mi * c1) / (sqrtf(vi * c2) + 1e-8f);
-        p[i] = pi;
-#pragma unroll
-        for (int l = 0; l < kLayers; l++) {
-            const int rel = i - lm.w[l];
-            if (rel >= 0 && rel < kHidden * lm.in[l]) {
-                const int o = rel / lm.in[l], k = rel - o * lm.in[l];
-                wb[lm.wb[l] + rel] = __float2bfloat16_rn(pi);
-                wt[lm.wb[l] + k * kHidden + o] = __float2bfloat16_rn(pi);
-            }
-        }
-    }
-}
-
-__global__ void k_to_bf16(const float* p, int n, __nv_bfloat16* wb, __nv_bfloat16* wt, LayerMap lm) {
+// the BF16 copies W_l (out x in, row-major) of the FP32 hidden weights
+__global__ void k_to_bf16(const float* p, int n, __nv_bfloat16* wb, LayerMap lm) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
 #pragma unroll
         for (int l = 0; l < kLayers; l++) {
             const int rel = i - lm.w[l];
-            if (rel >= 0 && rel < kHidden * lm.in[l]) {
-                const int o = rel / lm.in[l], k = rel - o * lm.in[l];
-                wb[lm.wb[l] + rel] = __float2bfloat16_rn(p[i]);
-                wt[lm.wb[l] + k * kHidden + o] = __float2bfloat16_rn(p[i]);
-            }
+            if (rel >= 0 && rel < kHidden * lm.in[l]) wb[lm.wb[l] + rel] = __float2bfloat16_rn(p[i]);
         }
     }
 }
@@ -750,9 +409,14 @@ __global__ void __launch_bounds__(128 * kInferWG, 1) k_mlp_infer(InferArgs a) {
         if (ok && p < a.n) a.out[p] = fmaf(y, a.out_scale, y_out);
     }
     if (!ok) {
-        // as in k_gemm: a second bounded wait for this warpgroup's pending
-        // commit before the columns are freed; the status flag makes the host
-        // discard the call's results either way
+        // The MMAs this warpgroup committed did not signal within the poll
+        // limit.  TMEM is freed below, and a later CTA on this SM may allocate
+        // the same columns, so first wait (bounded again) for the commit:
+        // once it arrives the MMAs are complete and nothing writes the
+        // columns.  If it still does not, the columns are freed all the same
+        // (a CTA that never frees them would stall every later allocation on
+        // this SM), and the status flag makes the host discard the call's
+        // results (LVN_ERR_DEVICE_STATUS), including anything a late MMA wrote.
         if ((threadIdx.x & 127) == 0) atomicExch(a.status, 1);
         uint32_t polls = 0;
         while (!mbar_try_wait(&bars[wg], phase ^ 1u) && ++polls < 4 * kWaitLimit) {
@@ -767,47 +431,57 @@ __global__ void __launch_bounds__(128 * kInferWG, 1) k_mlp_infer(InferArgs a) {
 // Fused training: the forward, the loss, the backward and the weight and bias
 // gradients of 128-row tiles in one persistent kernel, one launch per step.
 //
-// Each CTA (8 warps) takes a run of tiles.  The four hidden layers' BF16
-// weights stay in shared memory, with two activation images and one dZ image
-// (216 KB).  Tensor memory holds the working accumulator (columns 0-127) and
-// the weight-gradient accumulators of layers 1-3 (128 l + 0-127), which add
-// up over the CTA's tiles for the whole step.  Layer 0's weight gradient
-// needs the features and dZ0 of every tile; those images wait in the CTA's
-// scratch (global memory, about 350 KB per CTA, in L2) and are contracted into
-// the working accumulator after the last tile.
+// Each CTA (16 warps) takes a run of tiles.  The four hidden layers' BF16
+// weights stay in shared memory, with two activation images, one dZ image and
+// a 128 x 16 image of ones (220 KB).  A thread owns TMEM lane / tile row
+// 32 (warp & 3) + lane and the 32-column chunk 32 (warp >> 2) .. + 31.
 //
-// A thread owns TMEM lane / tile row 32 (warp & 3) + lane and the column half
-// 64 (warp >> 2) .. + 63.  Per tile:
-//   features -> XA (and the X0 image to scratch)
+// Per tile:
+//   features -> XA (and the X0 image to the tile's slot in scratch)
 //   layer l: acc = X_l W_l^T; z = acc + b_l -> BF16 z image (scratch);
-//            X_{l+1} = BF16 silu(z) -> the other image (X1 also to scratch)
-//   head:    y = X4 . w4 + b4 (two half sums), r = y - t / s, dy = 2 r / n,
+//            X_{l+1} = BF16 silu(z) -> the other image (X1 also to the slot)
+//   head:    y = X4 . w4 + b4 (four chunk sums), r = y - t / s, dy = 2 r / n,
 //            dZ3 = dy w4 silu'(z3) -> the dZ image
-//   l = 3, 2, 1: dW_l += dZ_l^T X_l and acc = dZ_l W_l in one commit;
-//            dZ_{l-1} = acc silu'(z_{l-1}) -> the dZ image (dZ0 to scratch)
+//   l = 3, 2: dW_l += dZ_l^T X_l, db_l += dZ_l^T 1 and acc = dZ_l W_l in one
+//            commit; dZ_{l-1} = acc silu'(z_{l-1}) -> the dZ image (dZ1 also
+//            to the slot)
+//   l = 1:   acc = dZ1 W1; dZ0 = acc silu'(z0) -> the slot
+// dW_3, dW_2 and their bias sums accumulate in tensor memory over the CTA's
+// tiles.  After the last tile they are written out and the freed columns take
+// dW_1, dW_0 and their bias sums, contracted from the slots' X1 / dZ1 and
+// X0 / dZ0 images (about 480 KB of scratch per CTA, in L2).
+//
 // The weight-gradient products read the dZ and X images as MN-major operands
 // (the same core matrices, K running over the tile's rows) and the input
-// gradient reads W_l as an MN-major B, so no transposed copy is ever made.
-// Bias and head-weight gradients are column sums over the tile's rows: a
-// warp's 32 rows are reduced by a butterfly that leaves column L's sum in
-// lane L, kept in registers across tiles.  The CTA writes its gradient and
-// loss to its own row of `partial`; k_adam_partials sums the rows in a fixed
-// order, so the step is deterministic.
+// gradient reads W_l as an MN-major B, so no transposed copy is made.  A bias
+// gradient is the product of dZ^T with the ones image (column 0 of 16 kept).
+// The head's weight gradient is a column sum over rows on the CUDA cores (a
+// butterfly that leaves column L's sum of a warp's rows in lane L).  The CTA
+// writes its gradient and loss to its own row of `partial`; k_adam_partials
+// sums the rows in a fixed order, so a step is deterministic.
 // ---------------------------------------------------------------------------
 
 constexpr uint32_t kCoreCol = (kTile / 8) * 128;  // bytes between core-matrix columns of a 128-row image
-constexpr int kTrainThreads = 256;
+constexpr int kTrainThreads = 512;  // 16 warps: lane quarter warp & 3, column quarter warp >> 2
 constexpr int kX0Bytes = kTile * kIn * 2;       // 24 KB feature image
 constexpr int kImgBytes = kTile * kHidden * 2;  // 32 KB activation image
-constexpr int kTrainSmem = kWbBytes + 3 * kImgBytes;
-static_assert(kTrainSmem + 2 * kTile * 4 + 64 <= 227 * 1024, "one CTA per SM");
-constexpr size_t kSlotBytes = (size_t)kX0Bytes + kImgBytes;  // per tile: X0 and dZ0 images
-constexpr size_t kTransientBytes = 4 * (size_t)kImgBytes;    // z0, z1, z2 and X1 images of the tile in hand
-constexpr int kPartStride = (kParams + 1 + 3) / 4 * 4;       // gradient, then the loss; 16-byte rows
+constexpr int kOnesBytes = kTile * 16 * 2;      // 4 KB: 128 rows x 16 columns of 1.0
+constexpr int kTrainSmem = kWbBytes + 3 * kImgBytes + kOnesBytes;
+static_assert(kTrainSmem + 4 * kTile * 4 + 64 <= 227 * 1024, "one CTA per SM");
+// per tile slot: the X0, X1, dZ0 and dZ1 images, contracted after the last tile
+constexpr size_t kSlotBytes = (size_t)kX0Bytes + 3 * (size_t)kImgBytes;
+constexpr size_t kTransientBytes = 3 * (size_t)kImgBytes;  // z0, z1, z2 of the tile in hand
+constexpr int kPartStride = (kParams + 1 + 3) / 4 * 4;     // gradient, then the loss; 16-byte rows
+// tensor-memory columns
+constexpr uint32_t kTmWork = 0;    // forward and input-gradient accumulator
+constexpr uint32_t kTmDW2 = 128;   // dW_2 over the CTA's tiles; dW_1 after the last tile
+constexpr uint32_t kTmDW3 = 256;   // dW_3; dW_0 (96 columns) after the last tile
+constexpr uint32_t kTmDB = 384;    // db_2 / db_1 (16 columns), then db_3 / db_0 (16 columns)
 constexpr uint32_t kIdescFwd = umma_idesc(kTile, kHidden);
-constexpr uint32_t kIdescDX = umma_idesc(kTile, kHidden) | (1u << 16);           // B MN-major
+constexpr uint32_t kIdescDX = umma_idesc(kTile, kHidden) | (1u << 16);                 // B MN-major
 constexpr uint32_t kIdescDW = umma_idesc(kHidden, kHidden) | (1u << 15) | (1u << 16);  // A and B MN-major
 constexpr uint32_t kIdescDW0 = umma_idesc(kHidden, kIn) | (1u << 15) | (1u << 16);
+constexpr uint32_t kIdescDB = umma_idesc(kHidden, 16) | (1u << 15) | (1u << 16);
 
 struct TrainArgs {
     const float4* pool;  // samples (x, y, z, density); row i of the batch is pool[(first + i) % pool_n]
@@ -887,19 +561,33 @@ __device__ __forceinline__ void to_tensor_core() {
     __syncthreads();
 }
 
+// 32 consecutive floats (16-byte aligned, the same for every lane) into registers
+__device__ __forceinline__ void load32(const float* p, float (&v)[32]) {
+    const float4* p4 = reinterpret_cast<const float4*>(p);
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const float4 t = __ldg(p4 + i);
+        v[4 * i] = t.x;
+        v[4 * i + 1] = t.y;
+        v[4 * i + 2] = t.z;
+        v[4 * i + 3] = t.w;
+    }
+}
+
 __global__ void __launch_bounds__(kTrainThreads, 1) k_mlp_train(TrainArgs a) {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint64_t bar;
     __shared__ uint32_t tmem_base;
-    __shared__ float ypart[2][kTile];
+    __shared__ float ypart[4][kTile];
     uint8_t* sW = smem;
     uint8_t* sXA = smem + kWbBytes;
     uint8_t* sXB = sXA + kImgBytes;
     uint8_t* sDZ = sXB + kImgBytes;
+    uint8_t* sOnes = sDZ + kImgBytes;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int q = warp & 3, h = warp >> 2;
-    const int row = 32 * q + lane;  // tile row = TMEM lane; columns 64 h .. 64 h + 63
-    const uint32_t lane_base = (uint32_t)(32 * q) << 16;
+    const int q = warp & 3, cq = warp >> 2;
+    const int row = 32 * q + lane;  // tile row = TMEM lane; columns 32 cq .. 32 cq + 31
+    const uint32_t tl = ((uint32_t)(32 * q) << 16) + (uint32_t)(32 * cq);  // this thread's lane and chunk
     for (int l = 0; l < kLayers; l++) {
         const int in = in_dim(l), cores = in / 8;
         uint8_t* dst = sW + 2 * wb_off(l);
@@ -908,6 +596,8 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_mlp_train(TrainArgs a) {
             cp_async16(dst + img_off(c, r), a.wb + wb_off(l) + (size_t)r * in + 8 * c);
         }
     }
+    for (int i = threadIdx.x; i < kOnesBytes / 16; i += blockDim.x)
+        reinterpret_cast<uint4*>(sOnes)[i] = make_uint4(0x3F803F80u, 0x3F803F80u, 0x3F803F80u, 0x3F803F80u);
     if (warp == 0) tmem_alloc(&tmem_base, 512);
     if (threadIdx.x == 0) mbar_init(&bar, 1);
     cp_async_wait_all();
@@ -917,38 +607,58 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_mlp_train(TrainArgs a) {
     tc_fence_after();
     const uint32_t tmem = tmem_base;
     const uint32_t w_addr = smem_u32(sW), xa_addr = smem_u32(sXA), xb_addr = smem_u32(sXB), dz_addr = smem_u32(sDZ);
+    const uint32_t ones_addr = smem_u32(sOnes);
     uint8_t* scr = a.scratch + (size_t)blockIdx.x * ((size_t)a.tiles_per_cta * kSlotBytes + kTransientBytes);
     auto zimg = [scr](int l) { return scr + (size_t)l * kImgBytes; };  // z_l, l = 0, 1, 2
-    uint8_t* x1img = scr + 3 * kImgBytes;
-    uint8_t* slots = scr + kTransientBytes;
+    uint8_t* slots = scr + kTransientBytes;  // per tile: X0, X1, dZ0, dZ1
     const int ntiles = a.n / kTile;
     const int t0 = blockIdx.x * a.tiles_per_cta, t1 = min(ntiles, t0 + a.tiles_per_cta);
     const float b4 = a.params[kHeadB];
-    float db[kLayers][2] = {}, gw4[2] = {}, lsum = 0.f, gb4 = 0.f;
+    float gw4 = 0.f, lsum = 0.f, gb4 = 0.f;  // w4 column 32 cq + lane over the warp's rows; loss and b4 per row
     uint32_t phase = 0;
     bool ok = true;
+    // dW_l (+)= dZ^T X over one tile's rows (M = 128 outputs, N = `n_in` inputs,
+    // both operands MN-major) and db_l (+)= dZ^T 1, issued by thread 0
+    auto weight_grads = [&](uint32_t dw, uint32_t db, uint32_t x_addr, uint32_t idesc, bool acc) {
+        for (int s = 0; s < kTile / 16; s++) {
+            const uint64_t ad = umma_desc(dz_addr + 256 * s, 128, kCoreCol);
+            const uint32_t c = (acc || s > 0) ? 1u : 0u;
+            umma_bf16(tmem + dw, ad, umma_desc(x_addr + 256 * s, 128, kCoreCol), idesc, c);
+            umma_bf16(tmem + db, ad, umma_desc(ones_addr + 256 * s, 128, kCoreCol), kIdescDB, c);
+        }
+    };
+    // the features of tile t -> XA and its slot's X0 image; its targets
+    auto features = [&](int t, float& target) {
+        uint8_t* x0img = slots + (size_t)(t - t0) * kSlotBytes;
+        int64_t si = a.first + (int64_t)t * kTile + row;  // < 2 pool_n
+        if (si >= a.pool_n) si -= a.pool_n;
+        const float4 p = a.pool[si];
+        target = p.w / a.out_scale;
+        // core column cq + 4 ax of each axis: sin (cq < 2) or cos of
+        // frequencies 8 (cq & 1) .. + 7
+        const float c[3] = {p.x, p.y, p.z};
+#pragma unroll
+        for (int ax = 0; ax < 3; ax++) {
+            const float u = 2.f * (c[ax] - a.dom.lo[ax]) / (a.dom.hi[ax] - a.dom.lo[ax]) - 1.f;
+            float f8[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                float sv, cv;
+                sincos_pi(a.ff.f[ax][8 * (cq & 1) + k] * u, sv, cv);
+                f8[k] = cq < 2 ? sv : cv;
+            }
+            const uint4 u8 = pack8(f8);
+            *reinterpret_cast<uint4*>(sXA + img_off(4 * ax + cq, row)) = u8;
+            *reinterpret_cast<uint4*>(x0img + img_off(4 * ax + cq, row)) = u8;
+        }
+    };
+    float target = 0.f;
+    if (t0 < t1) features(t0, target);
     for (int t = t0; t < t1 && ok; t++) {
         uint8_t* x0img = slots + (size_t)(t - t0) * kSlotBytes;
-        uint8_t* dz0img = x0img + kX0Bytes;
-        const float4 p = a.pool[(a.first + (int64_t)t * kTile + row) % a.pool_n];
-        const float target = p.w / a.out_scale;
-        // features: this thread's 8 of each axis' 16 frequencies, sin and cos
-        {
-            const float c[3] = {p.x, p.y, p.z};
-#pragma unroll
-            for (int ax = 0; ax < 3; ax++) {
-                const float u = 2.f * (c[ax] - a.dom.lo[ax]) / (a.dom.hi[ax] - a.dom.lo[ax]) - 1.f;
-                float sv[8], cv[8];
-#pragma unroll
-                for (int k = 0; k < 8; k++) sincos_pi(a.ff.f[ax][8 * h + k] * u, sv[k], cv[k]);
-                const uint4 us = pack8(sv), uc = pack8(cv);
-                const int cs = 4 * ax + h, cc = 4 * ax + 2 + h;
-                *reinterpret_cast<uint4*>(sXA + img_off(cs, row)) = us;
-                *reinterpret_cast<uint4*>(sXA + img_off(cc, row)) = uc;
-                *reinterpret_cast<uint4*>(x0img + img_off(cs, row)) = us;
-                *reinterpret_cast<uint4*>(x0img + img_off(cc, row)) = uc;
-            }
-        }
+        uint8_t* x1img = x0img + kX0Bytes;
+        uint8_t* dz0img = x1img + kImgBytes;
+        uint8_t* dz1img = dz0img + kImgBytes;
         // forward
         uint8_t* src = sXA;
         uint8_t* dst = sXB;
@@ -959,197 +669,197 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_mlp_train(TrainArgs a) {
                 tc_fence_after();
                 const uint32_t s_addr = smem_u32(src), wl = w_addr + 2 * wb_off(l);
                 for (int s = 0; s < in_dim(l) / 16; s++)
-                    umma_bf16(tmem, umma_desc(s_addr + 2 * s * kCoreCol, kCoreCol, 128),
+                    umma_bf16(tmem + kTmWork, umma_desc(s_addr + 2 * s * kCoreCol, kCoreCol, 128),
                               umma_desc(wl + 2 * s * kCoreCol, kCoreCol, 128), kIdescFwd, s > 0 ? 1u : 0u);
                 umma_commit(&bar);
             }
+            float bv[32], w4c[32];
+            load32(a.params + b_off(l) + 32 * cq, bv);
+            if (l == kLayers - 1) load32(a.params + kHeadW + 32 * cq, w4c);
             ok = cta_wait(&bar, phase);
             if (!ok) break;
-            const float* bias = a.params + b_off(l);
+            float v[32];
+            tmem_ld32(tmem + kTmWork + tl, v);
+#pragma unroll
+            for (int j = 0; j < 32; j++) v[j] += bv[j];
             if (l < kLayers - 1) {
 #pragma unroll
-                for (int k = 0; k < 2; k++) {
-                    const int cc = 2 * h + k;
-                    float v[32];
-                    tmem_ld32(tmem + lane_base + (uint32_t)(32 * cc), v);
+                for (int g = 0; g < 4; g++)
+                    *reinterpret_cast<uint4*>(zimg(l) + img_off(4 * cq + g, row)) = pack8(v + 8 * g);
 #pragma unroll
-                    for (int j = 0; j < 32; j++) v[j] += __ldg(bias + 32 * cc + j);
+                for (int j = 0; j < 32; j++) v[j] = silu(v[j]);
 #pragma unroll
-                    for (int g = 0; g < 4; g++)
-                        *reinterpret_cast<uint4*>(zimg(l) + img_off(4 * cc + g, row)) = pack8(v + 8 * g);
-#pragma unroll
-                    for (int j = 0; j < 32; j++) v[j] = silu(v[j]);
-#pragma unroll
-                    for (int g = 0; g < 4; g++) {
-                        const uint4 u = pack8(v + 8 * g);
-                        *reinterpret_cast<uint4*>(dst + img_off(4 * cc + g, row)) = u;
-                        if (l == 0) *reinterpret_cast<uint4*>(x1img + img_off(4 * cc + g, row)) = u;
-                    }
+                for (int g = 0; g < 4; g++) {
+                    const uint4 u = pack8(v + 8 * g);
+                    *reinterpret_cast<uint4*>(dst + img_off(4 * cq + g, row)) = u;
+                    if (l == 0) *reinterpret_cast<uint4*>(x1img + img_off(4 * cq + g, row)) = u;
                 }
                 uint8_t* tmp = src;
                 src = dst;
                 dst = tmp;
             } else {
-                // head: y from the BF16 activations, as in inference
-                const float* w4 = a.params + kHeadW;
+                // head: y from the BF16 activations, as in inference; the
+                // four column quarters' sums meet in shared memory
                 float y = 0.f;
 #pragma unroll
-                for (int k = 0; k < 2; k++) {
-                    const int cc = 2 * h + k;
-                    float v[32];
-                    tmem_ld32(tmem + lane_base + (uint32_t)(32 * cc), v);
-#pragma unroll
-                    for (int j = 0; j < 32; j++)
-                        y = fmaf(bf16_round(silu(v[j] + __ldg(bias + 32 * cc + j))), __ldg(w4 + 32 * cc + j), y);
+                for (int j = 0; j < 32; j++) {
+                    const float sg = sigmoid(v[j]);
+                    const float x = bf16_round(v[j] * sg);
+                    y = fmaf(x, w4c[j], y);
+                    w4c[j] *= sg * (1.f + v[j] * (1.f - sg));  // dZ3 / dy = w4 silu'(z3)
+                    v[j] = x;                                  // X4
                 }
-                ypart[h][row] = y;
+                ypart[cq][row] = y;
                 __syncthreads();
-                const float r = ypart[0][row] + ypart[1][row] + b4 - target;
+                const float r = ((ypart[0][row] + ypart[1][row]) + (ypart[2][row] + ypart[3][row])) + b4 - target;
                 const float dy = 2.f * r / (float)a.n;
-                if (h == 0) {
+                if (cq == 0) {
                     lsum = fmaf(r, r, lsum);
                     gb4 += dy;
                 }
 #pragma unroll
-                for (int k = 0; k < 2; k++) {
-                    const int cc = 2 * h + k;
-                    float v[32], g4[32];
-                    tmem_ld32(tmem + lane_base + (uint32_t)(32 * cc), v);
-#pragma unroll
-                    for (int j = 0; j < 32; j++) {
-                        const float z = v[j] + __ldg(bias + 32 * cc + j);
-                        g4[j] = dy * bf16_round(silu(z));
-                        v[j] = bf16_round(dy * __ldg(w4 + 32 * cc + j) * silu_grad(z));
-                    }
-#pragma unroll
-                    for (int g = 0; g < 4; g++)
-                        *reinterpret_cast<uint4*>(sDZ + img_off(4 * cc + g, row)) = pack8(v + 8 * g);
-                    gw4[k] += warp_column_sums(g4, lane);
-                    db[kLayers - 1][k] += warp_column_sums(v, lane);
+                for (int j = 0; j < 32; j++) {
+                    v[j] *= dy;     // w4's gradient terms
+                    w4c[j] *= dy;   // dZ3
                 }
+#pragma unroll
+                for (int g = 0; g < 4; g++)
+                    *reinterpret_cast<uint4*>(sDZ + img_off(4 * cq + g, row)) = pack8(w4c + 8 * g);
+                gw4 += warp_column_sums(v, lane);
             }
         }
         // backward: after the forward X2 is in XA and X3 in XB
-#pragma unroll
-        for (int l = kLayers - 1; l >= 1; l--) {
-            if (!ok) break;
-            if (l == 1) cp_async_wait_all();  // X1 back in XB
+#pragma unroll 1
+        for (int l = kLayers - 1; l >= 1 && ok; l--) {
             to_tensor_core();
             if (threadIdx.x == 0) {
                 tc_fence_after();
-                // dW_l (+)= dZ_l^T X_l: M = 128 outputs, N = 128 inputs, K = the tile's rows
-                const uint32_t x_addr = l == 2 ? xa_addr : xb_addr;
-                for (int s = 0; s < kTile / 16; s++)
-                    umma_bf16(tmem + (uint32_t)(128 * l), umma_desc(dz_addr + 256 * s, 128, kCoreCol),
-                              umma_desc(x_addr + 256 * s, 128, kCoreCol), kIdescDW, (t > t0 || s > 0) ? 1u : 0u);
+                if (l >= 2)
+                    weight_grads(l == 3 ? kTmDW3 : kTmDW2, kTmDB + (l == 3 ? 16u : 0u), l == 3 ? xb_addr : xa_addr,
+                                 kIdescDW, t > t0);
                 // dX = dZ_l W_l: M = the tile's rows, N = 128 inputs, K = 128 outputs
                 const uint32_t wl = w_addr + 2 * wb_off(l);
                 for (int s = 0; s < kHidden / 16; s++)
-                    umma_bf16(tmem, umma_desc(dz_addr + 2 * s * kCoreCol, kCoreCol, 128),
+                    umma_bf16(tmem + kTmWork, umma_desc(dz_addr + 2 * s * kCoreCol, kCoreCol, 128),
                               umma_desc(wl + 256 * s, 128, kCoreCol), kIdescDX, s > 0 ? 1u : 0u);
                 umma_commit(&bar);
             }
-            // this thread's z_{l-1} (64 BF16 values) while the products run
-            uint4 zr[8];
+            // this thread's z_{l-1} (32 BF16 values) while the products run
+            uint4 zr[4];
 #pragma unroll
-            for (int g = 0; g < 8; g++) zr[g] = *reinterpret_cast<const uint4*>(zimg(l - 1) + img_off(8 * h + g, row));
+            for (int g = 0; g < 4; g++) zr[g] = *reinterpret_cast<const uint4*>(zimg(l - 1) + img_off(4 * cq + g, row));
+            // and the next tile's features into XA (X2's products are done)
+            if (l == 1 && t + 1 < t1) features(t + 1, target);
             ok = cta_wait(&bar, phase);
             if (!ok) break;
-            if (l == kLayers - 1) {
-                // X1 into XB (X3's products are done) for dW_1, two steps on
-                for (int i = threadIdx.x; i < kImgBytes / 16; i += kTrainThreads)
-                    cp_async16(sXB + 16 * i, x1img + 16 * i);
-            }
+            float v[32], z[32];
+            tmem_ld32(tmem + kTmWork + tl, v);
 #pragma unroll
-            for (int k = 0; k < 2; k++) {
-                const int cc = 2 * h + k;
-                float v[32], z[32];
-                tmem_ld32(tmem + lane_base + (uint32_t)(32 * cc), v);
+            for (int g = 0; g < 4; g++) unpack8(zr[g], z + 8 * g);
 #pragma unroll
-                for (int g = 0; g < 4; g++) unpack8(zr[4 * k + g], z + 8 * g);
+            for (int j = 0; j < 32; j++) v[j] *= silu_grad(z[j]);
 #pragma unroll
-                for (int j = 0; j < 32; j++) v[j] = bf16_round(v[j] * silu_grad(z[j]));
-                uint8_t* out = l > 1 ? sDZ : dz0img;
-#pragma unroll
-                for (int g = 0; g < 4; g++) *reinterpret_cast<uint4*>(out + img_off(4 * cc + g, row)) = pack8(v + 8 * g);
-                db[l - 1][k] += warp_column_sums(v, lane);
+            for (int g = 0; g < 4; g++) {
+                const uint4 u = pack8(v + 8 * g);
+                if (l > 1) *reinterpret_cast<uint4*>(sDZ + img_off(4 * cq + g, row)) = u;
+                if (l == 2) *reinterpret_cast<uint4*>(dz1img + img_off(4 * cq + g, row)) = u;
+                if (l == 1) *reinterpret_cast<uint4*>(dz0img + img_off(4 * cq + g, row)) = u;
             }
         }
     }
-    // dW_0 over the CTA's tiles, from the feature and dZ0 images in scratch
+    float* part = a.partial + (size_t)blockIdx.x * kPartStride;
+    const bool any = t1 > t0;
+    // this thread's lane is output row `row` of each dW, its chunk the
+    // columns 32 cq .. + 31 (layer 0 has three chunks); the bias sums are
+    // column 0 of their 16-column blocks
+    auto flush = [&](int l, uint32_t col0) {
+        const int in = in_dim(l);
+        if (32 * cq >= in) return;  // warp-uniform
+        float v[32];
+        if (any) tmem_ld32(tmem + col0 + tl, v);
+#pragma unroll
+        for (int j = 0; j < 32; j++) v[j] = any ? v[j] : 0.f;
+        float4* d4 = reinterpret_cast<float4*>(part + w_off(l) + (size_t)row * in + 32 * cq);
+#pragma unroll
+        for (int j = 0; j < 8; j++) d4[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+    };
+    auto flush_bias = [&](int la, int lb) {  // db_la in column kTmDB, db_lb in kTmDB + 16
+        if (cq != 0) return;
+        float v[32];
+        tmem_ld32(tmem + kTmDB + ((uint32_t)(32 * q) << 16), v);
+        part[b_off(la) + row] = any ? v[0] : 0.f;
+        part[b_off(lb) + row] = any ? v[16] : 0.f;
+    };
+    if (ok) {
+        flush(2, kTmDW2);
+        flush(3, kTmDW3);
+        flush_bias(2, 3);
+    }
+    // dW_1, db_1, dW_0, db_0 over the CTA's tiles from the slots' images
     // (written by other threads of the CTA: the barrier orders their stores
-    // before these reads)
+    // before these reads, and the TMEM reads above before the MMAs below)
+    tc_fence_before();
     __syncthreads();
     for (int t = t0; t < t1 && ok; t++) {
         const uint8_t* x0img = slots + (size_t)(t - t0) * kSlotBytes;
-        const uint8_t* dz0img = x0img + kX0Bytes;
-        for (int i = threadIdx.x; i < kX0Bytes / 16; i += kTrainThreads) cp_async16(sXA + 16 * i, x0img + 16 * i);
+        const uint8_t* x1img = x0img + kX0Bytes;
+        const uint8_t* dz0img = x1img + kImgBytes;
+        const uint8_t* dz1img = dz0img + kImgBytes;
+        for (int i = threadIdx.x; i < kImgBytes / 16; i += kTrainThreads) {
+            cp_async16(sXA + 16 * i, x1img + 16 * i);
+            cp_async16(sDZ + 16 * i, dz1img + 16 * i);
+        }
+        for (int i = threadIdx.x; i < kX0Bytes / 16; i += kTrainThreads) cp_async16(sXB + 16 * i, x0img + 16 * i);
+        cp_async_wait_all();
+        to_tensor_core();
+        if (threadIdx.x == 0) {
+            tc_fence_after();
+            weight_grads(kTmDW2, kTmDB, xa_addr, kIdescDW, t > t0);
+            umma_commit(&bar);
+        }
+        ok = cta_wait(&bar, phase);
+        if (!ok) break;
         for (int i = threadIdx.x; i < kImgBytes / 16; i += kTrainThreads) cp_async16(sDZ + 16 * i, dz0img + 16 * i);
         cp_async_wait_all();
         to_tensor_core();
         if (threadIdx.x == 0) {
             tc_fence_after();
-            for (int s = 0; s < kTile / 16; s++)
-                umma_bf16(tmem, umma_desc(dz_addr + 256 * s, 128, kCoreCol), umma_desc(xa_addr + 256 * s, 128, kCoreCol),
-                          kIdescDW0, (t > t0 || s > 0) ? 1u : 0u);
+            weight_grads(kTmDW3, kTmDB + 16, xb_addr, kIdescDW0, t > t0);
             umma_commit(&bar);
         }
         ok = cta_wait(&bar, phase);
     }
-    float* part = a.partial + (size_t)blockIdx.x * kPartStride;
     if (ok) {
-        const bool any = t1 > t0;
-        // weight gradients: this thread's lane is output row `row` of each dW
-#pragma unroll 1
-        for (int l = 0; l < kLayers; l++) {
-            const int in = in_dim(l);
-            const uint32_t col0 = l == 0 ? 0u : (uint32_t)(128 * l);
-            for (int cc = h; cc < in / 32; cc += 2) {
-                float v[32];
-                if (any) tmem_ld32(tmem + col0 + lane_base + (uint32_t)(32 * cc), v);
-#pragma unroll
-                for (int j = 0; j < 32; j++) v[j] = any ? v[j] : 0.f;
-                float4* d4 = reinterpret_cast<float4*>(part + w_off(l) + (size_t)row * in + 32 * cc);
-#pragma unroll
-                for (int j = 0; j < 8; j++) d4[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
-            }
-        }
-        // column sums over the four lane quarters: biases, then w4
-        float* red = reinterpret_cast<float*>(sXA);  // [kLayers + 1][4][kHidden]
-#pragma unroll
-        for (int k = 0; k < 2; k++) {
-            const int col = 64 * h + 32 * k + lane;
-#pragma unroll
-            for (int l = 0; l < kLayers; l++) red[(l * 4 + q) * kHidden + col] = db[l][k];
-            red[(kLayers * 4 + q) * kHidden + col] = gw4[k];
-        }
-        // loss and b4 (rows are summed by the h == 0 threads)
+        flush(1, kTmDW2);
+        flush(0, kTmDW3);
+        flush_bias(1, 0);
+        // w4: column sums over the four lane quarters
+        float* red = reinterpret_cast<float*>(sXA);  // [4][kHidden]
+        red[q * kHidden + 32 * cq + lane] = gw4;
+        // loss and b4 (rows are summed by the cq == 0 threads)
         float ls = lsum, gb = gb4;
 #pragma unroll
         for (int o = 16; o; o >>= 1) {
             ls += __shfl_xor_sync(0xffffffffu, ls, o);
             gb += __shfl_xor_sync(0xffffffffu, gb, o);
         }
-        if (h == 0 && lane == 0) {
+        if (cq == 0 && lane == 0) {
             ypart[0][q] = ls;
             ypart[1][q] = gb;
         }
         __syncthreads();
-        for (int i = threadIdx.x; i < (kLayers + 1) * kHidden; i += kTrainThreads) {
-            const int l = i / kHidden, col = i % kHidden;
-            float s = 0.f;
-#pragma unroll
-            for (int qq = 0; qq < 4; qq++) s += red[(l * 4 + qq) * kHidden + col];
-            part[(l < kLayers ? b_off(l) : kHeadW) + col] = s;
+        if (threadIdx.x < kHidden) {
+            const int c = threadIdx.x;
+            part[kHeadW + c] = ((red[c] + red[kHidden + c]) + red[2 * kHidden + c]) + red[3 * kHidden + c];
         }
         if (threadIdx.x == 0) {
             part[kHeadB] = ((ypart[1][0] + ypart[1][1]) + ypart[1][2]) + ypart[1][3];
             part[kParams] = (((ypart[0][0] + ypart[0][1]) + ypart[0][2]) + ypart[0][3]) / (float)a.n;
         }
     } else {
-        // as in k_gemm: a second bounded wait for the pending commit before
-        // the columns are freed; the status flag makes the host discard the
-        // step's results either way
+        // as in k_mlp_infer: a second bounded wait for the pending commit
+        // before the columns are freed; the status flag makes the host
+        // discard the step's results either way
         if (threadIdx.x == 0) atomicExch(a.status, 1);
         uint32_t polls = 0;
         while (!mbar_try_wait(&bar, phase ^ 1u) && ++polls < 4 * kWaitLimit) {
@@ -1326,11 +1036,11 @@ struct lvn_surrogate {
     FeatureFreqs ff;
     float out_scale = 8.f;  // the network predicts density / out_scale
     cudaStream_t stream = nullptr;
-    Buf params, grads, adam_m, adam_v, wb, wt, loss, status;
+    Buf params, grads, adam_m, adam_v, wb, loss, status;
     Buf loss_hist;  // one loss per training step, read back once per lvn_surrogate_train
-    // batch activations
+    // points and densities of host calls
     int cap = 0;
-    Buf pts, X[kLayers + 1], Xt[kLayers + 1], Z[kLayers], dZ[2], dZt[2], dens;
+    Buf pts, dens;
     Buf pool;  // training samples
     int num_sms = 0;
 
@@ -1404,97 +1114,8 @@ struct lvn_surrogate {
         if (n <= cap) return LVN_OK;
         int rc;
         if ((rc = pts.ensure(sizeof(float4) * n))) return rc;
-        for (int l = 0; l <= kLayers; l++) {
-            const int w = l == 0 ? kIn : kHidden;
-            if ((rc = X[l].ensure(2ull * n * w))) return rc;
-            if ((rc = Xt[l].ensure(2ull * n * w))) return rc;
-        }
-        for (int l = 0; l < kLayers; l++)
-            if ((rc = Z[l].ensure(4ull * n * kHidden))) return rc;
-        for (int i = 0; i < 2; i++) {
-            if ((rc = dZ[i].ensure(2ull * n * kHidden))) return rc;
-            if ((rc = dZt[i].ensure(2ull * n * kHidden))) return rc;
-        }
         if ((rc = dens.ensure(4ull * n))) return rc;
         cap = n;
-        return LVN_OK;
-    }
-
-    // forward through the hidden layers (transposes only when training)
-    int forward(int n, bool train) {
-        GemmArgs g;
-        std::memset(&g, 0, sizeof(g));
-        g.status = status.as<int>();
-        const int grid = std::min(1184, (n + 255) / 256);
-        k_features<<<grid, 256, 0, stream>>>(pts.as<float4>(), n, dom, ff, X[0].as<__nv_bfloat16>(),
-                                             train ? Xt[0].as<__nv_bfloat16>() : nullptr);
-        SG_CK(cudaGetLastError());
-        for (int l = 0; l < kLayers; l++) {
-            g.A = X[l].as<__nv_bfloat16>();
-            g.B = wb.as<__nv_bfloat16>() + wb_off(l);
-            g.M = n;
-            g.K = kIn_[l];
-            g.lda = g.ldb = kIn_[l];
-            g.k_per_split = kIn_[l];
-            g.bias = params.as<float>() + b_off(l);
-            g.Z = train ? Z[l].as<float>() : nullptr;
-            g.X = X[l + 1].as<__nv_bfloat16>();
-            g.Xt = train ? Xt[l + 1].as<__nv_bfloat16>() : nullptr;
-            SG_CK((gemm<EPI_FWD, kHidden>(g, 1, stream)));
-        }
-        return LVN_OK;
-    }
-
-    // one forward + backward on the n samples in pts; gradients into grads,
-    // the loss into *loss_dev (device)
-    int backward(int n, float* loss_dev) {
-        SG_CK(cudaMemsetAsync(grads.p, 0, sizeof(float) * kParams, stream));
-        SG_CK(cudaMemsetAsync(loss_dev, 0, sizeof(float), stream));
-        int rc = forward(n, true);
-        if (rc) return rc;
-        k_head<<<std::min(num_sms * 4, n / kHeadRows), 32 * kHeadWarps, 0, stream>>>(
-            X[kLayers].as<__nv_bfloat16>(), Z[kLayers - 1].as<float>(), pts.as<float4>(), n, params.as<float>(),
-            out_scale, dZ[1].as<__nv_bfloat16>(), dZt[1].as<__nv_bfloat16>(), grads.as<float>(), loss_dev);
-        SG_CK(cudaGetLastError());
-        GemmArgs g;
-        std::memset(&g, 0, sizeof(g));
-        g.status = status.as<int>();
-        // split-K over the batch for the weight gradients: 128 samples per MMA
-        // stage, about two CTAs per SM
-        const int per_split = std::max(kKC, ((n / (2 * num_sms)) + kKC - 1) / kKC * kKC);
-        const int splits = (n + per_split - 1) / per_split;
-        for (int l = kLayers - 1; l >= 0; l--) {
-            // dZ of the last hidden layer is in buffer 1 (k_head), then the buffers alternate
-            const int buf = ((kLayers - 1 - l) & 1) ? 0 : 1;
-            // dW_l = dZ_l^T X_l
-            g.A = dZt[buf].as<__nv_bfloat16>();
-            g.B = Xt[l].as<__nv_bfloat16>();
-            g.M = kHidden;
-            g.K = n;
-            g.lda = g.ldb = n;
-            g.k_per_split = per_split;
-            g.G = grads.as<float>() + w_off(l);
-            if (l == 0) SG_CK((gemm<EPI_DW, kIn>(g, splits, stream)));
-            else SG_CK((gemm<EPI_DW, kHidden>(g, splits, stream)));
-            k_bias_grad<<<dim3(kHidden, kBiasSplits), 256, 0, stream>>>(dZt[buf].as<__nv_bfloat16>(), n,
-                                                                        grads.as<float>() + b_off(l));
-            SG_CK(cudaGetLastError());
-            if (l == 0) break;
-            // dZ_{l-1} = (dZ_l W_l) * silu'(Z_{l-1})
-            GemmArgs d;
-            std::memset(&d, 0, sizeof(d));
-            d.status = status.as<int>();
-            d.A = dZ[buf].as<__nv_bfloat16>();
-            d.B = wt.as<__nv_bfloat16>() + wb_off(l);
-            d.M = n;
-            d.K = kHidden;
-            d.lda = d.ldb = kHidden;
-            d.k_per_split = kHidden;
-            d.Zp = Z[l - 1].as<float>();
-            d.X = dZ[buf ^ 1].as<__nv_bfloat16>();
-            d.Xt = dZt[buf ^ 1].as<__nv_bfloat16>();
-            SG_CK((gemm<EPI_DX, kHidden>(d, 1, stream)));
-        }
         return LVN_OK;
     }
 };
@@ -1539,7 +1160,7 @@ lvn_surrogate* lvn_surrogate_create(const float domain_min[3], const float domai
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, dev);
     bool ok = !s->params.ensure(4ull * kParams) && !s->grads.ensure(4ull * kParams) && !s->adam_m.ensure(4ull * kParams) &&
-              !s->adam_v.ensure(4ull * kParams) && !s->wb.ensure(2ull * kWb) && !s->wt.ensure(2ull * kWb) &&
+              !s->adam_v.ensure(4ull * kParams) && !s->wb.ensure(2ull * kWb) &&
               !s->loss.ensure(4) && !s->status.ensure(4);
     // PyTorch's Linear initialisation: U(-1/sqrt(fan_in), 1/sqrt(fan_in)), from splitmix64(seed)
     std::vector<float> h(kParams);
@@ -1571,15 +1192,9 @@ lvn_surrogate* lvn_surrogate_create(const float domain_min[3], const float domai
 void lvn_surrogate_destroy(lvn_surrogate* s) {
     if (!s) return;
     if (s->stream) cudaStreamSynchronize(s->stream);
-    Buf* bufs[] = {&s->params, &s->grads, &s->adam_m, &s->adam_v, &s->wb, &s->wt, &s->loss, &s->status,
-                   &s->pts, &s->dZ[0], &s->dZ[1], &s->dZt[0], &s->dZt[1], &s->dens, &s->pool, &s->loss_hist,
-                   &s->train_scratch, &s->partial};
+    Buf* bufs[] = {&s->params, &s->grads, &s->adam_m, &s->adam_v, &s->wb,   &s->loss,          &s->status,
+                   &s->pts,    &s->dens,  &s->pool,   &s->loss_hist, &s->train_scratch, &s->partial};
     for (Buf* b : bufs) b->release();
-    for (int l = 0; l <= kLayers; l++) {
-        s->X[l].release();
-        s->Xt[l].release();
-    }
-    for (int l = 0; l < kLayers; l++) s->Z[l].release();
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
 }
@@ -1592,8 +1207,7 @@ int lvn_surrogate_set_params(lvn_surrogate* s, const float* host, int64_t n) {
     SG_CK(cudaMemsetAsync(s->adam_m.p, 0, 4ull * kParams, s->stream));
     SG_CK(cudaMemsetAsync(s->adam_v.p, 0, 4ull * kParams, s->stream));
     SG_CK(cudaMemsetAsync(s->status.p, 0, 4, s->stream));
-    k_to_bf16<<<64, 256, 0, s->stream>>>(s->params.as<float>(), kParams, s->wb.as<__nv_bfloat16>(),
-                                         s->wt.as<__nv_bfloat16>(), layer_map());
+    k_to_bf16<<<64, 256, 0, s->stream>>>(s->params.as<float>(), kParams, s->wb.as<__nv_bfloat16>(), layer_map());
     SG_CK(cudaGetLastError());
     s->step = 0;
     SG_CK(cudaStreamSynchronize(s->stream));
