@@ -1931,34 +1931,29 @@ __global__ void __launch_bounds__(kNodeTile) k_mesh_count(BatchPtrs b) {
             int pos[3];
             position_for_code<VPC>(b.node_codes[i], pos[0], pos[1], pos[2]);
             const int corners = b.node_info[i] & 0xff;
-            // ProcessEdge (octree.cl:335-372) for the leaf's three edges: a
-            // quad needs the edge's sign change and all three neighbours
-            // (EDGE_NODE_OFFSETS, octree.cl:376-381).  The sign is tested
-            // first, so that the neighbour lookups run only for the edges it
-            // passes.  The nine lookups name six distinct leaves, at the
-            // offsets j = (ox oy oz) in binary, 1 .. 6; a leaf an earlier edge
-            // looked up is not looked up again.
-            //   x edge: 1, 2, 3    y edge: 4, 1, 5    z edge: 2, 4, 6
-            int nb[7];
-            bool have[7] = {false, false, false, false, false, false, false};
-            auto neighbour = [&](int j) {
-                if (!have[j]) {
-                    nb[j] = (int)hv.find(code_for_position<VPC>(pos[0] + (j >> 2), pos[1] + ((j >> 1) & 1), pos[2] + (j & 1)));
-                    have[j] = true;
-                }
-                return nb[j];
-            };
-            const int use[3][3] = {{1, 2, 3}, {4, 1, 5}, {2, 4, 6}};
             int quads = 0;
 #pragma unroll
             for (int axis = 0; axis < 3; axis++) {
                 int4 q = make_int4(-1, -1, -1, 0);
+                const int aa = pos[(axis + 1) % 3], bb = pos[(axis + 2) % 3];
+                // ProcessEdge (octree.cl:335-372): a quad needs the edge's sign
+                // change and all three neighbours; the sign is tested first, so
+                // that the neighbour lookups run only for the edges it passes
                 const int edge = axis * 4 + 3;
                 const int m1 = (corners >> edge_c0(edge)) & 1, m2 = (corners >> edge_c1(edge)) & 1;
-                if (pos[(axis + 1) % 3] != VPC - 1 && pos[(axis + 2) % 3] != VPC - 1 && m1 != m2) {
-                    const int n0 = neighbour(use[axis][0]), n1 = neighbour(use[axis][1]), n2 = neighbour(use[axis][2]);
-                    if (n0 != -1 && n1 != -1 && n2 != -1) {
-                        q = make_int4(n0, n1, n2, 1 | (m1 != 0 ? 2 : 0));
+                if (aa != VPC - 1 && bb != VPC - 1 && m1 != m2) {
+                    // EDGE_NODE_OFFSETS (octree.cl:376-381)
+                    int nb[3];
+#pragma unroll
+                    for (int k = 1; k < 4; k++) {
+                        int ox = 0, oy = 0, oz = 0;
+                        if (axis == 0) { oy = (k >> 1) & 1; oz = k & 1; }
+                        else if (axis == 1) { ox = k & 1; oz = (k >> 1) & 1; }
+                        else { oy = k & 1; ox = (k >> 1) & 1; }
+                        nb[k - 1] = (int)hv.find(code_for_position<VPC>(pos[0] + ox, pos[1] + oy, pos[2] + oz));
+                    }
+                    if (nb[0] != -1 && nb[1] != -1 && nb[2] != -1) {
+                        q = make_int4(nb[0], nb[1], nb[2], 1 | (m1 != 0 ? 2 : 0));
                         quads++;
                     }
                 }

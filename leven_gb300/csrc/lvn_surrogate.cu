@@ -99,13 +99,25 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint
 __host__ __device__ constexpr uint32_t umma_idesc(int m, int n) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
-__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                          uint32_t accumulate) {
-    asm volatile(
-        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem_d),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-        : "memory");
+// A chain of STEPS MMAs over K = 16 STEPS: the descriptors' start addresses
+// advance by a_step / b_step bytes a step (an immediate add to the low word:
+// shared-memory addresses are below 256 KB, so the 14-bit field never
+// carries).  The first MMA overwrites D unless `acc`.
+template <int STEPS>
+__device__ __forceinline__ void umma_chain(uint32_t tmem_d, uint64_t adesc, uint32_t a_step, uint64_t bdesc,
+                                           uint32_t b_step, uint32_t idesc, bool acc) {
+    const uint32_t alo = (uint32_t)adesc, ahi = (uint32_t)(adesc >> 32);
+    const uint32_t blo = (uint32_t)bdesc, bhi = (uint32_t)(bdesc >> 32);
+#pragma unroll
+    for (int s = 0; s < STEPS; s++) {
+        const uint32_t c = (acc || s > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n.reg .pred p;\n.reg .b64 da, db;\nsetp.ne.b32 p, %6, 0;\nmov.b64 da, {%1, %2};\nmov.b64 db, {%3, %4};\n"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], da, db, %5, p;\n}" ::"r"(tmem_d),
+            "r"(alo + (uint32_t)s * (a_step >> 4)), "r"(ahi), "r"(blo + (uint32_t)s * (b_step >> 4)), "r"(bhi), "r"(idesc),
+            "r"(c)
+            : "memory");
+    }
 }
 __device__ __forceinline__ void umma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
@@ -366,10 +378,9 @@ __global__ void __launch_bounds__(128 * kInferWG, 1) k_mlp_infer(InferArgs a) {
             wg_sync(wg);
             tc_fence_after();
             if (row == 0) {
-                const uint32_t wl = w_addr + 2 * wb_off(l);
-                for (int s = 0; s < in_dim(l) / 16; s++)
-                    umma_bf16(tmem, umma_desc(act_addr + 2 * s * kLbo, kLbo, 128),
-                              umma_desc(wl + 2 * s * kLbo, kLbo, 128), kIdesc, s > 0 ? 1u : 0u);
+                const uint64_t ad = umma_desc(act_addr, kLbo, 128), bd = umma_desc(w_addr + 2 * wb_off(l), kLbo, 128);
+                if (l == 0) umma_chain<kIn / 16>(tmem, ad, 2 * kLbo, bd, 2 * kLbo, kIdesc, false);
+                else umma_chain<kHidden / 16>(tmem, ad, 2 * kLbo, bd, 2 * kLbo, kIdesc, false);
                 umma_commit(&bars[wg]);
             }
             uint32_t polls = 0;
@@ -619,13 +630,10 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_mlp_train(TrainArgs a) {
     bool ok = true;
     // dW_l (+)= dZ^T X over one tile's rows (M = 128 outputs, N = `n_in` inputs,
     // both operands MN-major) and db_l (+)= dZ^T 1, issued by thread 0
+    const uint64_t dz_mn = umma_desc(dz_addr, 128, kCoreCol), ones_mn = umma_desc(ones_addr, 128, kCoreCol);
     auto weight_grads = [&](uint32_t dw, uint32_t db, uint32_t x_addr, uint32_t idesc, bool acc) {
-        for (int s = 0; s < kTile / 16; s++) {
-            const uint64_t ad = umma_desc(dz_addr + 256 * s, 128, kCoreCol);
-            const uint32_t c = (acc || s > 0) ? 1u : 0u;
-            umma_bf16(tmem + dw, ad, umma_desc(x_addr + 256 * s, 128, kCoreCol), idesc, c);
-            umma_bf16(tmem + db, ad, umma_desc(ones_addr + 256 * s, 128, kCoreCol), kIdescDB, c);
-        }
+        umma_chain<kTile / 16>(tmem + dw, dz_mn, 256, umma_desc(x_addr, 128, kCoreCol), 256, idesc, acc);
+        umma_chain<kTile / 16>(tmem + db, dz_mn, 256, ones_mn, 256, kIdescDB, acc);
     };
     // the features of tile t -> XA and its slot's X0 image; its targets
     auto features = [&](int t, float& target) {
@@ -667,10 +675,10 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_mlp_train(TrainArgs a) {
             to_tensor_core();
             if (threadIdx.x == 0) {
                 tc_fence_after();
-                const uint32_t s_addr = smem_u32(src), wl = w_addr + 2 * wb_off(l);
-                for (int s = 0; s < in_dim(l) / 16; s++)
-                    umma_bf16(tmem + kTmWork, umma_desc(s_addr + 2 * s * kCoreCol, kCoreCol, 128),
-                              umma_desc(wl + 2 * s * kCoreCol, kCoreCol, 128), kIdescFwd, s > 0 ? 1u : 0u);
+                const uint64_t ad = umma_desc(smem_u32(src), kCoreCol, 128);
+                const uint64_t bd = umma_desc(w_addr + 2 * wb_off(l), kCoreCol, 128);
+                if (l == 0) umma_chain<kIn / 16>(tmem + kTmWork, ad, 2 * kCoreCol, bd, 2 * kCoreCol, kIdescFwd, false);
+                else umma_chain<kHidden / 16>(tmem + kTmWork, ad, 2 * kCoreCol, bd, 2 * kCoreCol, kIdescFwd, false);
                 umma_commit(&bar);
             }
             float bv[32], w4c[32];
@@ -738,10 +746,8 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_mlp_train(TrainArgs a) {
                     weight_grads(l == 3 ? kTmDW3 : kTmDW2, kTmDB + (l == 3 ? 16u : 0u), l == 3 ? xb_addr : xa_addr,
                                  kIdescDW, t > t0);
                 // dX = dZ_l W_l: M = the tile's rows, N = 128 inputs, K = 128 outputs
-                const uint32_t wl = w_addr + 2 * wb_off(l);
-                for (int s = 0; s < kHidden / 16; s++)
-                    umma_bf16(tmem + kTmWork, umma_desc(dz_addr + 2 * s * kCoreCol, kCoreCol, 128),
-                              umma_desc(wl + 256 * s, 128, kCoreCol), kIdescDX, s > 0 ? 1u : 0u);
+                umma_chain<kHidden / 16>(tmem + kTmWork, umma_desc(dz_addr, kCoreCol, 128), 2 * kCoreCol,
+                                         umma_desc(w_addr + 2 * wb_off(l), 128, kCoreCol), 256, kIdescDX, false);
                 umma_commit(&bar);
             }
             // this thread's z_{l-1} (32 BF16 values) while the products run
