@@ -158,6 +158,15 @@ __device__ __forceinline__ float silu_grad(float z) {
     const float s = sigmoid(z);
     return s * (1.f + z * (1.f - s));
 }
+// the same on two values at once: the FP32 arithmetic in the two-lane forms
+// (one instruction for both), the hyperbolic tangent per lane
+__device__ __forceinline__ float2 sigmoid2(float2 z) {
+    const float2 h = mul2(z, v2(0.5f));
+    return fma2(v2(0.5f), make_float2(tanh_approx(h.x), tanh_approx(h.y)), v2(0.5f));
+}
+__device__ __forceinline__ float2 silu_grad2(float2 z, float2 s) {  // s = sigmoid2(z)
+    return mul2(s, fma2(z, sub2(v2(1.f), s), v2(1.f)));
+}
 // sin(pi r), cos(pi r): r reduced to [-1, 1] exactly (an even number of half
 // turns removed), then the fast intrinsics on a small argument
 __device__ __forceinline__ void sincos_pi(float r, float& s, float& c) {
@@ -689,13 +698,22 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_mlp_train(TrainArgs a) {
             float v[32];
             tmem_ld32(tmem + kTmWork + tl, v);
 #pragma unroll
-            for (int j = 0; j < 32; j++) v[j] += bv[j];
+            for (int j = 0; j < 32; j += 2) {
+                const float2 z = add2(make_float2(v[j], v[j + 1]), make_float2(bv[j], bv[j + 1]));
+                v[j] = z.x;
+                v[j + 1] = z.y;
+            }
             if (l < kLayers - 1) {
 #pragma unroll
                 for (int g = 0; g < 4; g++)
                     *reinterpret_cast<uint4*>(zimg(l) + img_off(4 * cq + g, row)) = pack8(v + 8 * g);
 #pragma unroll
-                for (int j = 0; j < 32; j++) v[j] = silu(v[j]);
+                for (int j = 0; j < 32; j += 2) {
+                    const float2 z = make_float2(v[j], v[j + 1]);
+                    const float2 x = mul2(z, sigmoid2(z));
+                    v[j] = x.x;
+                    v[j + 1] = x.y;
+                }
 #pragma unroll
                 for (int g = 0; g < 4; g++) {
                     const uint4 u = pack8(v + 8 * g);
@@ -708,16 +726,21 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_mlp_train(TrainArgs a) {
             } else {
                 // head: y from the BF16 activations, as in inference; the
                 // four column quarters' sums meet in shared memory
-                float y = 0.f;
+                float2 y2 = v2(0.f);
 #pragma unroll
-                for (int j = 0; j < 32; j++) {
-                    const float sg = sigmoid(v[j]);
-                    const float x = bf16_round(v[j] * sg);
-                    y = fmaf(x, w4c[j], y);
-                    w4c[j] *= sg * (1.f + v[j] * (1.f - sg));  // dZ3 / dy = w4 silu'(z3)
-                    v[j] = x;                                  // X4
+                for (int j = 0; j < 32; j += 2) {
+                    const float2 z = make_float2(v[j], v[j + 1]);
+                    const float2 sg = sigmoid2(z);
+                    const float2 x = __bfloat1622float2(__float22bfloat162_rn(mul2(z, sg)));  // X4
+                    const float2 w = make_float2(w4c[j], w4c[j + 1]);
+                    y2 = fma2(x, w, y2);
+                    const float2 d = mul2(w, silu_grad2(z, sg));  // dZ3 / dy = w4 silu'(z3)
+                    w4c[j] = d.x;
+                    w4c[j + 1] = d.y;
+                    v[j] = x.x;
+                    v[j + 1] = x.y;
                 }
-                ypart[cq][row] = y;
+                ypart[cq][row] = y2.x + y2.y;
                 __syncthreads();
                 const float r = ((ypart[0][row] + ypart[1][row]) + (ypart[2][row] + ypart[3][row])) + b4 - target;
                 const float dy = 2.f * r / (float)a.n;
@@ -726,9 +749,13 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_mlp_train(TrainArgs a) {
                     gb4 += dy;
                 }
 #pragma unroll
-                for (int j = 0; j < 32; j++) {
-                    v[j] *= dy;     // w4's gradient terms
-                    w4c[j] *= dy;   // dZ3
+                for (int j = 0; j < 32; j += 2) {
+                    const float2 g = mul2(make_float2(v[j], v[j + 1]), v2(dy));         // w4's gradient terms
+                    const float2 d = mul2(make_float2(w4c[j], w4c[j + 1]), v2(dy));     // dZ3
+                    v[j] = g.x;
+                    v[j + 1] = g.y;
+                    w4c[j] = d.x;
+                    w4c[j + 1] = d.y;
                 }
 #pragma unroll
                 for (int g = 0; g < 4; g++)
@@ -763,7 +790,12 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_mlp_train(TrainArgs a) {
 #pragma unroll
             for (int g = 0; g < 4; g++) unpack8(zr[g], z + 8 * g);
 #pragma unroll
-            for (int j = 0; j < 32; j++) v[j] *= silu_grad(z[j]);
+            for (int j = 0; j < 32; j += 2) {
+                const float2 zz = make_float2(z[j], z[j + 1]);
+                const float2 d = mul2(make_float2(v[j], v[j + 1]), silu_grad2(zz, sigmoid2(zz)));
+                v[j] = d.x;
+                v[j + 1] = d.y;
+            }
 #pragma unroll
             for (int g = 0; g < 4; g++) {
                 const uint4 u = pack8(v + 8 * g);
