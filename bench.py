@@ -641,17 +641,23 @@ def committed_traffic(kernel):
     return None
 
 
-# FP32 operations of the restated density arithmetic (an fma counts 2):
-# one simplex2 evaluation with its three corners inside the kernel radius 51,
-# one octave of fBm 51 + 5, an 8-octave height term 8 * 56 + 4 = 452;
-# one simplex3 evaluation 102, one octave of 3D fBm 108, the 6-octave cave
-# term 6 * 108 + 3 = 651 plus its fma.
+# FP32 operations of the restated density arithmetic, as the oracle counts
+# them (orc_flop_counts: add, sub, mul, div, sqrt and floor 1, an fma 2,
+# compares, min / max and abs free, every simplex corner taken;
+# tests/test_flop_counts.py holds these figures to that count):
+# one simplex2 evaluation 51, one octave of 2D fBm 56, the 8-octave height
+# term 8 * 56 + 4 = 452; one simplex3 evaluation 93, one octave of 3D fBm 99,
+# the 6-octave cave term 6 * 99 + 3 = 597 plus its fma; y - amp h is one fma.
 FLOP_HEIGHT8 = 452
-FLOP_CAVES6 = 651 + 2
+FLOP_CAVES6 = 597 + 2
+# FindEdgeIntersectionInfo outside its 23 density samples: the edge vector,
+# 17 search positions (3 fmas and the parameter step each), the crossing
+# (3 fmas), six normal offsets, three differences and the normalisation
+FLOP_EDGE_EXTRA = 146
 
 
 def density_flops(wl):
-    """(per-column height term, per-point rest) FP32 operations, or None."""
+    """(per-column height term, rest of a density sample) FP32 operations, or None."""
     d = wl.density
     if d["mode"] == 1 and d["octaves2"] == 8:
         return FLOP_HEIGHT8, 2
@@ -661,11 +667,14 @@ def density_flops(wl):
 
 
 def hermite_edge_flops(h, p):
-    """x / z edge: 17 search samples (height + point + 3 mix fmas) and 4
-    normal samples with their own height; y edge: the height once.  Both add
-    the y normal pair (shared height) and the normalisation (21)."""
-    xz = 17 * (h + p + 6) + 4 * (h + p + 3) + 2 * p + 21
-    y = h + 17 * (p + 6) + 4 * (h + p + 3) + 2 * p + 21
+    """The operations k_hermite performs for a plain edge: 23 density samples
+    (the rest p each) and the edge arithmetic, plus the height terms it
+    evaluates: an x or z edge 15 (its end points' heights come from the
+    field's height map) and 4 for the x and z normal samples; a y edge the 4
+    normal heights only (its own height is the map's, and the y normal pair
+    shares it)."""
+    xz = 19 * h + 23 * p + FLOP_EDGE_EXTRA
+    y = 4 * h + 23 * p + FLOP_EDGE_EXTRA
     return xz, y
 
 

@@ -134,12 +134,61 @@ inline int texel(int row, int col) { return ((row & 255) << 8) | (col & 255); }
 inline int alpha_column(int a) { return a == 255 ? 0 : a; }
 
 // ---------------------------------------------------------------------------
+// Operation counting.  The density and edge arithmetic below is written once
+// for a scalar R: float for the restatement, Counted to count its FP32
+// operations (the FLOP figures of the roofline): add, sub, mul, div, sqrt
+// and floor count 1, an fma counts 2 (its two source operations);
+// comparisons, min / max, abs and negation are free.  A Counted run takes
+// every simplex corner and every normalisation, as the branch-free kernels
+// execute them; the values it computes are not used.
+// ---------------------------------------------------------------------------
+
+struct Counted {
+    float v = 0.f;
+    static thread_local uint64_t ops;
+    Counted() = default;
+    Counted(float f) : v(f) {}  // literals and constants: free
+    explicit operator int() const { return (int)v; }
+};
+thread_local uint64_t Counted::ops = 0;
+inline Counted operator+(Counted a, Counted b) { ++Counted::ops; return Counted(a.v + b.v); }
+inline Counted operator-(Counted a, Counted b) { ++Counted::ops; return Counted(a.v - b.v); }
+inline Counted operator*(Counted a, Counted b) { ++Counted::ops; return Counted(a.v * b.v); }
+inline Counted operator/(Counted a, Counted b) { ++Counted::ops; return Counted(a.v / b.v); }
+inline Counted operator-(Counted a) { return Counted(-a.v); }
+inline Counted& operator+=(Counted& a, Counted b) { return a = a + b; }
+inline bool operator<(Counted a, Counted b) { return a.v < b.v; }
+inline bool operator>(Counted a, Counted b) { return a.v > b.v; }
+inline bool operator<=(Counted a, Counted b) { return a.v <= b.v; }
+inline bool operator>=(Counted a, Counted b) { return a.v >= b.v; }
+inline bool operator==(Counted a, Counted b) { return a.v == b.v; }
+inline bool operator!=(Counted a, Counted b) { return a.v != b.v; }
+
+template <class R> constexpr bool kCounting = false;
+template <> constexpr bool kCounting<Counted> = true;
+
+inline float r_fma(float a, float b, float c) { return std::fmaf(a, b, c); }
+inline Counted r_fma(Counted a, Counted b, Counted c) {
+    Counted::ops += 2;
+    return Counted(std::fmaf(a.v, b.v, c.v));
+}
+inline float r_floor(float x) { return std::floor(x); }
+inline Counted r_floor(Counted x) { ++Counted::ops; return Counted(std::floor(x.v)); }
+inline float r_sqrt(float x) { return std::sqrt(x); }
+inline Counted r_sqrt(Counted x) { ++Counted::ops; return Counted(std::sqrt(x.v)); }
+inline float r_abs(float x) { return std::fabs(x); }
+inline Counted r_abs(Counted x) { return Counted(std::fabs(x.v)); }
+template <class R> inline R r_clamp01(R x) { return x < R(0.f) ? R(0.f) : (x > R(1.f) ? R(1.f) : x); }
+
+// ---------------------------------------------------------------------------
 // Simplex noise: simplex.cl:158-289 (Gustavson, public domain)
 // ---------------------------------------------------------------------------
 
-inline float dot2(float ax, float ay, float bx, float by) { return std::fmaf(ay, by, ax * bx); }
+template <class R> inline R dot2_t(R ax, R ay, R bx, R by) { return r_fma(ay, by, ax * bx); }
+template <class R> inline R dot3_t(R ax, R ay, R az, R bx, R by, R bz) { return r_fma(az, bz, r_fma(ay, by, ax * bx)); }
+inline float dot2(float ax, float ay, float bx, float by) { return dot2_t<float>(ax, ay, bx, by); }
 inline float dot3(float ax, float ay, float az, float bx, float by, float bz) {
-    return std::fmaf(az, bz, std::fmaf(ay, by, ax * bx));
+    return dot3_t<float>(ax, ay, az, bx, by, bz);
 }
 
 const float F2 = 0.366025403784f;
@@ -147,50 +196,52 @@ const float G2 = 0.211324865405f;
 const float F3 = 0.333333333333f;
 const float G3 = 0.166666666667f;
 
-float snoise2(float px, float py, const PermLut& L) {
+template <class R>
+R snoise2_t(R px, R py, const PermLut& L) {
     const float c2 = 1.f - 2.f * G2;
-    const float s = (px + py) * F2;
-    const float pix = std::floor(px + s);
-    const float piy = std::floor(py + s);
-    const float t = (pix + piy) * G2;
-    const float x0 = px - (pix - t);
-    const float y0 = py - (piy - t);
+    const R s = (px + py) * R(F2);
+    const R pix = r_floor(px + s);
+    const R piy = r_floor(py + s);
+    const R t = (pix + piy) * R(G2);
+    const R x0 = px - (pix - t);
+    const R y0 = py - (piy - t);
     const int ix = (int)pix, iy = (int)piy;
     const int o1x = x0 > y0 ? 1 : 0;
     const int o1y = 1 - o1x;
 
-    float n0 = 0.f, n1 = 0.f, n2 = 0.f;
+    R n0 = 0.f, n1 = 0.f, n2 = 0.f;
     {
         const float* g = L.g[L.v[texel(iy, ix)] & 15];
-        float t0 = 0.5f - dot2(x0, y0, x0, y0);
-        if (!(t0 < 0.f)) { t0 = t0 * t0; n0 = (t0 * t0) * dot2(g[0], g[1], x0, y0); }
+        R t0 = R(0.5f) - dot2_t<R>(x0, y0, x0, y0);
+        if (kCounting<R> || !(t0 < R(0.f))) { t0 = t0 * t0; n0 = (t0 * t0) * dot2_t<R>(g[0], g[1], x0, y0); }
     }
-    const float x1 = (x0 - (float)o1x) + G2, y1 = (y0 - (float)o1y) + G2;
+    const R x1 = (x0 - R((float)o1x)) + R(G2), y1 = (y0 - R((float)o1y)) + R(G2);
     {
         const float* g = L.g[L.v[texel(iy + o1y, ix + o1x)] & 15];
-        float t1 = 0.5f - dot2(x1, y1, x1, y1);
-        if (!(t1 < 0.f)) { t1 = t1 * t1; n1 = (t1 * t1) * dot2(g[0], g[1], x1, y1); }
+        R t1 = R(0.5f) - dot2_t<R>(x1, y1, x1, y1);
+        if (kCounting<R> || !(t1 < R(0.f))) { t1 = t1 * t1; n1 = (t1 * t1) * dot2_t<R>(g[0], g[1], x1, y1); }
     }
-    const float x2 = x0 - c2, y2 = y0 - c2;
+    const R x2 = x0 - R(c2), y2 = y0 - R(c2);
     {
         const float* g = L.g[L.v[texel(iy + 1, ix + 1)] & 15];
-        float t2 = 0.5f - dot2(x2, y2, x2, y2);
-        if (!(t2 < 0.f)) { t2 = t2 * t2; n2 = (t2 * t2) * dot2(g[0], g[1], x2, y2); }
+        R t2 = R(0.5f) - dot2_t<R>(x2, y2, x2, y2);
+        if (kCounting<R> || !(t2 < R(0.f))) { t2 = t2 * t2; n2 = (t2 * t2) * dot2_t<R>(g[0], g[1], x2, y2); }
     }
-    return 70.f * ((n0 + n1) + n2);
+    return R(70.f) * ((n0 + n1) + n2);
 }
 
-float snoise3(float px, float py, float pz, const PermLut& L) {
+template <class R>
+R snoise3_t(R px, R py, R pz, const PermLut& L) {
     const float c2 = 2.f * G3;
     const float c3 = 1.f - 3.f * G3;
-    const float s = ((px + py) + pz) * F3;
-    const float pix = std::floor(px + s);
-    const float piy = std::floor(py + s);
-    const float piz = std::floor(pz + s);
-    const float t = ((pix + piy) + piz) * G3;
-    const float x0 = px - (pix - t);
-    const float y0 = py - (piy - t);
-    const float z0 = pz - (piz - t);
+    const R s = ((px + py) + pz) * R(F3);
+    const R pix = r_floor(px + s);
+    const R piy = r_floor(py + s);
+    const R piz = r_floor(pz + s);
+    const R t = ((pix + piy) + piz) * R(G3);
+    const R x0 = px - (pix - t);
+    const R y0 = py - (piy - t);
+    const R z0 = pz - (piz - t);
     const int ix = (int)pix, iy = (int)piy, iz = (int)piz;
 
     // simplex() (simplex.cl:133-156): rank the components of Pf0
@@ -205,38 +256,41 @@ float snoise3(float px, float py, float pz, const PermLut& L) {
     const int o1x = std::min(std::max(off_x - 1, 0), 1), o1y = std::min(std::max(off_y - 1, 0), 1),
               o1z = std::min(std::max(off_z - 1, 0), 1);
 
-    auto corner = [&](int dx, int dy, int dz, float x, float y, float z) -> float {
+    auto corner = [&](int dx, int dy, int dz, R x, R y, R z) -> R {
         const int a = L.v[texel(iy + dy, ix + dx)];
         const float* g = L.g[L.v[texel(iz + dz, alpha_column(a))] & 15];
-        float tt = 0.6f - dot3(x, y, z, x, y, z);
-        if (tt < 0.f) return 0.f;
+        R tt = R(0.6f) - dot3_t<R>(x, y, z, x, y, z);
+        if (!kCounting<R> && tt < R(0.f)) return R(0.f);
         tt = tt * tt;
-        return (tt * tt) * dot3(g[0], g[1], g[2], x, y, z);
+        return (tt * tt) * dot3_t<R>(g[0], g[1], g[2], x, y, z);
     };
 
-    const float n0 = corner(0, 0, 0, x0, y0, z0);
-    const float x1 = (x0 - (float)o1x) + G3, y1 = (y0 - (float)o1y) + G3, z1 = (z0 - (float)o1z) + G3;
-    const float n1 = corner(o1x, o1y, o1z, x1, y1, z1);
-    const float x2 = (x0 - (float)o2x) + c2, y2 = (y0 - (float)o2y) + c2, z2 = (z0 - (float)o2z) + c2;
-    const float n2 = corner(o2x, o2y, o2z, x2, y2, z2);
-    const float x3 = x0 - c3, y3 = y0 - c3, z3 = z0 - c3;
-    const float n3 = corner(1, 1, 1, x3, y3, z3);
-    return 32.f * (((n0 + n1) + n2) + n3);
+    const R n0 = corner(0, 0, 0, x0, y0, z0);
+    const R x1 = (x0 - R((float)o1x)) + R(G3), y1 = (y0 - R((float)o1y)) + R(G3), z1 = (z0 - R((float)o1z)) + R(G3);
+    const R n1 = corner(o1x, o1y, o1z, x1, y1, z1);
+    const R x2 = (x0 - R((float)o2x)) + R(c2), y2 = (y0 - R((float)o2y)) + R(c2), z2 = (z0 - R((float)o2z)) + R(c2);
+    const R n2 = corner(o2x, o2y, o2z, x2, y2, z2);
+    const R x3 = x0 - R(c3), y3 = y0 - R(c3), z3 = z0 - R(c3);
+    const R n3 = corner(1, 1, 1, x3, y3, z3);
+    return R(32.f) * (((n0 + n1) + n2) + n3);
 }
+
+inline float snoise2(float px, float py, const PermLut& L) { return snoise2_t<float>(px, py, L); }
+inline float snoise3(float px, float py, float pz, const PermLut& L) { return snoise3_t<float>(px, py, pz, L); }
 
 // ---------------------------------------------------------------------------
 // Fractals and density: noise.cl:8-81, 205-268
 // ---------------------------------------------------------------------------
 
 // BasicFractal (noise.cl:8-36); NOISE_SCALE == 1
-float basic_fractal(int octaves, float frequency, float lacunarity, float persistence, float x, float y,
-                    const PermLut& L) {
-    float px = x * 1.f, py = y * 1.f;
-    float noise = 0.f, amplitude = 1.f;
+template <class R>
+R basic_fractal_t(int octaves, R frequency, R lacunarity, R persistence, R x, R y, const PermLut& L) {
+    R px = x * R(1.f), py = y * R(1.f);
+    R noise = 0.f, amplitude = 1.f;
     px = px * frequency;
     py = py * frequency;
     for (int i = 0; i < octaves; i++) {
-        noise = std::fmaf(snoise2(px, py, L), amplitude, noise);
+        noise = r_fma(snoise2_t<R>(px, py, L), amplitude, noise);
         px = px * lacunarity;
         py = py * lacunarity;
         amplitude = amplitude * persistence;
@@ -245,12 +299,12 @@ float basic_fractal(int octaves, float frequency, float lacunarity, float persis
 }
 
 // 3D analogue of BasicFractal for the cave term of the caves density mode
-float basic_fractal3(int octaves, float frequency, float lacunarity, float persistence, float x, float y,
-                     float z, const PermLut& L) {
-    float px = x * frequency, py = y * frequency, pz = z * frequency;
-    float noise = 0.f, amplitude = 1.f;
+template <class R>
+R basic_fractal3_t(int octaves, R frequency, R lacunarity, R persistence, R x, R y, R z, const PermLut& L) {
+    R px = x * frequency, py = y * frequency, pz = z * frequency;
+    R noise = 0.f, amplitude = 1.f;
     for (int i = 0; i < octaves; i++) {
-        noise = std::fmaf(snoise3(px, py, pz, L), amplitude, noise);
+        noise = r_fma(snoise3_t<R>(px, py, pz, L), amplitude, noise);
         px = px * lacunarity;
         py = py * lacunarity;
         pz = pz * lacunarity;
@@ -260,62 +314,78 @@ float basic_fractal3(int octaves, float frequency, float lacunarity, float persi
 }
 
 // RidgedMultiFractal (noise.cl:42-81) with RIDGED_MULTI_H == 1
-float ridged_multi_fractal(int octaves, float lacunarity, float gain, float offset, float x, float y,
-                           const PermLut& L) {
-    float px = x * 1.f, py = y * 1.f;
-    float signal = snoise2(px, py, L);
-    signal = std::fabs(signal);
+template <class R>
+R ridged_multi_fractal_t(int octaves, R lacunarity, R gain, R offset, R x, R y, const PermLut& L) {
+    R px = x * R(1.f), py = y * R(1.f);
+    R signal = snoise2_t<R>(px, py, L);
+    signal = r_abs(signal);
     signal = offset - signal;
     signal = signal * signal;
-    float noise = signal;
-    float weight = 1.f;
-    float frequency = 1.f;
+    R noise = signal;
+    R weight = 1.f;
+    R frequency = 1.f;
     for (int i = 0; i < octaves; i++) {
         px = px * lacunarity;
         py = py * lacunarity;
         weight = signal * gain;
-        weight = std::min(std::max(weight, 0.f), 1.f);
-        signal = snoise2(px, py, L);
-        signal = std::fabs(signal);
+        weight = r_clamp01(weight);
+        signal = snoise2_t<R>(px, py, L);
+        signal = r_abs(signal);
         signal = offset - signal;
         signal = signal * weight;
-        const float exponent = 1.f / frequency;
+        const R exponent = R(1.f) / frequency;
         frequency = frequency * lacunarity;
-        noise = std::fmaf(signal, exponent, noise);
+        noise = r_fma(signal, exponent, noise);
     }
-    noise = noise * (1.f / (float)octaves);
+    noise = noise * R(1.f / (float)octaves);
     return noise;
 }
 
 // Terrain (noise.cl:205-223)
-float terrain(float x, float z, const PermLut& L) {
-    const float px = x * (1.f / 2000.f);
-    const float pz = z * (1.f / 2000.f);
-    float ridged = 0.8f * ridged_multi_fractal(7, 2.114352f, 1.5241f, 1.f, px, pz, L);
-    ridged = std::min(std::max(ridged, 0.f), 1.f);
-    float billow = 0.6f * basic_fractal(4, 0.24f, 1.8754f, 0.433f, -4.33f * px, 7.98f * pz, L);
-    billow = std::fmaf(0.5f, billow, 0.5f);
-    float b2 = 0.6f * basic_fractal(2, 0.63f, 2.2f, 0.15f, px, pz, L);
-    b2 = std::fmaf(b2, 0.5f, 0.5f);
-    return std::fmaf(billow, ridged, b2);
+template <class R>
+R terrain_t(R x, R z, const PermLut& L) {
+    const R px = x * R(1.f / 2000.f);
+    const R pz = z * R(1.f / 2000.f);
+    R ridged = R(0.8f) * ridged_multi_fractal_t<R>(7, 2.114352f, 1.5241f, 1.f, px, pz, L);
+    ridged = r_clamp01(ridged);
+    R billow = R(0.6f) * basic_fractal_t<R>(4, 0.24f, 1.8754f, 0.433f, R(-4.33f) * px, R(7.98f) * pz, L);
+    billow = r_fma(R(0.5f), billow, R(0.5f));
+    R b2 = R(0.6f) * basic_fractal_t<R>(2, 0.63f, 2.2f, 0.15f, px, pz, L);
+    b2 = r_fma(b2, R(0.5f), R(0.5f));
+    return r_fma(billow, ridged, b2);
+}
+
+// the height term h(x, z) of a heightfield mode (density = y - amp2 h [+ caves])
+template <class R>
+R height_t(const orc_density& d, R x, R z, const PermLut& L) {
+    return basic_fractal_t<R>(d.octaves2, d.freq2, d.lacunarity2, d.gain2, x, z, L);
 }
 
 // DensityFunc (noise.cl:225-268) and the two heightfield modes
-float density(const orc_density& d, float x, float y, float z, const PermLut& L) {
+template <class R>
+R density_t(const orc_density& d, R x, R y, R z, const PermLut& L) {
     switch (d.mode) {
         case 0:
-            return std::fmaf(-900.f, terrain(x, z, L), y);  // MAX_TERRAIN_HEIGHT = 900
+            return r_fma(R(-900.f), terrain_t<R>(x, z, L), y);  // MAX_TERRAIN_HEIGHT = 900
         case 1: {
-            const float h = basic_fractal(d.octaves2, d.freq2, d.lacunarity2, d.gain2, x, z, L);
-            return std::fmaf(-d.amp2, h, y);
+            const R h = height_t<R>(d, x, z, L);
+            return r_fma(-R(d.amp2), h, y);
         }
         default: {
-            const float h = basic_fractal(d.octaves2, d.freq2, d.lacunarity2, d.gain2, x, z, L);
-            const float base = std::fmaf(-d.amp2, h, y);
-            const float c = basic_fractal3(d.octaves3, d.freq3, d.lacunarity3, d.gain3, x, y, z, L);
-            return std::fmaf(d.amp3, c, base);
+            const R h = height_t<R>(d, x, z, L);
+            const R base = r_fma(-R(d.amp2), h, y);
+            const R c = basic_fractal3_t<R>(d.octaves3, d.freq3, d.lacunarity3, d.gain3, x, y, z, L);
+            return r_fma(R(d.amp3), c, base);
         }
     }
+}
+
+inline float basic_fractal(int octaves, float frequency, float lacunarity, float persistence, float x, float y,
+                           const PermLut& L) {
+    return basic_fractal_t<float>(octaves, frequency, lacunarity, persistence, x, y, L);
+}
+inline float density(const orc_density& d, float x, float y, float z, const PermLut& L) {
+    return density_t<float>(d, x, y, z, L);
 }
 
 // ---------------------------------------------------------------------------
@@ -930,44 +1000,66 @@ inline void decode_edge(const Dims& D, int key, int p[3], int* axis) {
     p[2] = (h >> (2 * D.shift)) & D.mask;
 }
 
+// normalize(v) = v / sqrt(dot(v, v)); a zero vector stays zero
+template <class R>
+inline void normalize3_t(R& x, R& y, R& z) {
+    const R len = r_sqrt(dot3_t<R>(x, y, z, x, y, z));
+    if (!kCounting<R> && len == R(0.f)) { x = y = z = R(0.f); return; }
+    x = x / len;
+    y = y / len;
+    z = z / len;
+}
+
 // FindEdgeIntersectionInfo (density_field.cl:96-151); crossing_mode 1
 // replaces the 17-sample search by linear interpolation of the end densities.
-F4 edge_info_density(const Dims& D, const orc_density& dn, const PermLut& L, int key, const int off[3],
-                     int scale, int crossing_mode) {
+template <class R>
+void edge_info_density_t(const Dims& D, const orc_density& dn, const PermLut& L, int key, const int off[3], int scale,
+                         int crossing_mode, R out[4]) {
     int lp[3], axis;
     decode_edge(D, key, lp, &axis);
     const int wx = scale * lp[0] + off[0], wy = scale * lp[1] + off[1], wz = scale * lp[2] + off[2];
-    const F4 p0{(float)wx, (float)wy, (float)wz, 0.f};
-    const F4 p1{(float)(wx + scale * kAxisOffset[axis][0]), (float)(wy + scale * kAxisOffset[axis][1]),
-                (float)(wz + scale * kAxisOffset[axis][2]), 0.f};
-    float t = 0.f;
+    const R p0x = (float)wx, p0y = (float)wy, p0z = (float)wz;
+    const R p1x = (float)(wx + scale * kAxisOffset[axis][0]), p1y = (float)(wy + scale * kAxisOffset[axis][1]),
+            p1z = (float)(wz + scale * kAxisOffset[axis][2]);
+    const R ex = p1x - p0x, ey = p1y - p0y, ez = p1z - p0z;  // the edge vector, once
+    R t = 0.f;
     if (crossing_mode == 0) {
-        float min_value = FLT_MAX;
-        float current = 0.f;
+        R min_value = FLT_MAX;
+        R current = 0.f;
         for (int i = 0; i <= 16; i++) {
-            const float px = std::fmaf(p1.x - p0.x, current, p0.x);
-            const float py = std::fmaf(p1.y - p0.y, current, p0.y);
-            const float pz = std::fmaf(p1.z - p0.z, current, p0.z);
-            const float d = std::fabs(density(dn, px, py, pz, L));
+            const R px = r_fma(ex, current, p0x);
+            const R py = r_fma(ey, current, p0y);
+            const R pz = r_fma(ez, current, p0z);
+            const R d = r_abs(density_t<R>(dn, px, py, pz, L));
             if (d < min_value) { t = current; min_value = d; }
-            current += 0.0625f;
+            current += R(0.0625f);
         }
     } else {
-        const float d0 = density(dn, p0.x, p0.y, p0.z, L);
-        const float d1 = density(dn, p1.x, p1.y, p1.z, L);
-        const float den = d0 - d1;
-        t = den != 0.f ? d0 / den : 0.5f;
-        t = std::min(std::max(t, 0.f), 1.f);
+        const R d0 = density_t<R>(dn, p0x, p0y, p0z, L);
+        const R d1 = density_t<R>(dn, p1x, p1y, p1z, L);
+        const R den = d0 - d1;
+        t = den != R(0.f) ? d0 / den : R(0.5f);
+        t = r_clamp01(t);
     }
-    const float px = std::fmaf(p1.x - p0.x, t, p0.x);
-    const float py = std::fmaf(p1.y - p0.y, t, p0.y);
-    const float pz = std::fmaf(p1.z - p0.z, t, p0.z);
-    const float h = 0.001f;
-    float nx = density(dn, px + h, py, pz, L) - density(dn, px - h, py, pz, L);
-    float ny = density(dn, px, py + h, pz, L) - density(dn, px, py - h, pz, L);
-    float nz = density(dn, px, py, pz + h, L) - density(dn, px, py, pz - h, L);
-    normalize3(nx, ny, nz);
-    return F4{nx, ny, nz, t};
+    const R px = r_fma(ex, t, p0x);
+    const R py = r_fma(ey, t, p0y);
+    const R pz = r_fma(ez, t, p0z);
+    const R h = 0.001f;
+    R nx = density_t<R>(dn, px + h, py, pz, L) - density_t<R>(dn, px - h, py, pz, L);
+    R ny = density_t<R>(dn, px, py + h, pz, L) - density_t<R>(dn, px, py - h, pz, L);
+    R nz = density_t<R>(dn, px, py, pz + h, L) - density_t<R>(dn, px, py, pz - h, L);
+    normalize3_t<R>(nx, ny, nz);
+    out[0] = nx;
+    out[1] = ny;
+    out[2] = nz;
+    out[3] = t;
+}
+
+F4 edge_info_density(const Dims& D, const orc_density& dn, const PermLut& L, int key, const int off[3],
+                     int scale, int crossing_mode) {
+    float o[4];
+    edge_info_density_t<float>(D, dn, L, key, off, scale, crossing_mode, o);
+    return F4{o[0], o[1], o[2], o[3]};
 }
 
 // CSG FindEdgeIntersectionInfo (apply_csg_operation.cl:443-477)
@@ -1628,6 +1720,25 @@ void orc_perm_image_rgba(uint8_t* out) {
 float orc_density_at(const orc_density* d, float x, float y, float z) { return density(*d, x, y, z, g_lut); }
 float orc_snoise2(float x, float y) { return snoise2(x, y, g_lut); }
 float orc_snoise3(float x, float y, float z) { return snoise3(x, y, z, g_lut); }
+
+int orc_flop_counts(const orc_density* d, int64_t* out) {
+    if (!d || !out) return -1;
+    Counted::ops = 0;
+    if (d->mode != 0) (void)height_t<Counted>(*d, 37.25f, -81.5f, g_lut);
+    out[0] = (int64_t)Counted::ops;
+    Counted::ops = 0;
+    (void)density_t<Counted>(*d, 37.25f, 12.75f, -81.5f, g_lut);
+    out[1] = (int64_t)Counted::ops - out[0];
+    const Dims D(64);
+    const int off[3] = {0, 0, 0};
+    for (int axis = 0; axis < 3; axis++) {
+        Counted o[4];
+        Counted::ops = 0;
+        edge_info_density_t<Counted>(D, *d, g_lut, edge_key(D, 5, 6, 7, axis), off, 1, 0, o);
+        out[2 + axis] = (int64_t)Counted::ops;
+    }
+    return 0;
+}
 int orc_find_next_prime(int32_t n) { return find_next_prime(n); }
 
 float orc_qef_solve_points(const float* positions, const float* normals, int32_t count, float* out) {

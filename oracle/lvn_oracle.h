@@ -84,6 +84,13 @@ void  orc_perm_image_rgba(uint8_t* out);
 float orc_density_at(const orc_density* d, float x, float y, float z);
 float orc_snoise2(float x, float y);
 float orc_snoise3(float x, float y, float z);
+/* FP32 operation counts of the restated arithmetic (add, sub, mul, div,
+ * sqrt, floor 1; fma 2; compares, min / max, abs free; every simplex corner
+ * taken): out[0] the height term of a heightfield mode (0 for the reference
+ * terrain), out[1] the rest of one density sample, out[2..4] the whole
+ * FindEdgeIntersectionInfo of an x, y and z edge (17-sample search, 23
+ * density samples, each with its own height term) */
+int   orc_flop_counts(const orc_density* d, int64_t* out);
 int   orc_find_next_prime(int32_t n);
 /* qef_create_from_points + qef_solve (qef.cl:239-303) over `count` (<= 12)
  * points and normals (4 floats each); out[4] = the solved position */

@@ -59,6 +59,7 @@ def lib():
         L.orc_snoise3.argtypes = [C.c_float, C.c_float, C.c_float]
         L.orc_snoise3.restype = C.c_float
         L.orc_find_next_prime.argtypes = [C.c_int32]
+        L.orc_flop_counts.argtypes = [C.POINTER(Density), C.c_void_p]
         L.orc_chunk_new.restype = C.c_void_p
         L.orc_chunk_free.argtypes = [C.c_void_p]
         L.orc_chunk_run.argtypes = [C.c_void_p, C.POINTER(Density), C.POINTER(ChunkArgs)]
@@ -362,3 +363,11 @@ def uniform_draws(hi, n):
     out = np.zeros(max(1, n), np.int32)
     lib().orc_uniform_draws(int(hi), int(n), out.ctypes.data)
     return out[:n]
+
+
+def flop_counts(d):
+    """The oracle's FP32 operation counts for density d: (height term, rest of
+    a density sample, x edge, y edge, z edge), see orc_flop_counts."""
+    out = (C.c_int64 * 5)()
+    assert lib().orc_flop_counts(C.byref(d), out) == 0
+    return tuple(int(v) for v in out)
