@@ -1557,28 +1557,39 @@ int lvn_meshgen_autotune(lvn_meshgen* m, const lvn_chunk_desc* chunks, int32_t n
     std::memcpy(saved_launches, m->stage_launches, sizeof(saved_launches));
     m->profile = true;
     static const int kCandidates[] = {2, 4, 8, 16, 32};
-    std::array<double, ST_COUNT> best_ms;
-    std::array<int, ST_COUNT> best{};
-    best_ms.fill(1e30);
-    for (int cand : kCandidates) {
+    constexpr int kCand = sizeof(kCandidates) / sizeof(kCandidates[0]);
+    constexpr int kRounds = 3;
+    auto shape_of = [](int cand) {
         std::array<int, ST_COUNT> shape{};
         for (int st = 0; st < ST_COUNT; st++) shape[st] = stage_has_persistent_grid(st) ? cand : 0;
-        m->tunes[key] = shape;
-        std::array<double, ST_COUNT> ms;
-        ms.fill(1e30);
-        for (int rep = 0; rep < 3 && rc == LVN_OK; rep++) {  // the first run also sizes the pools
+        return shape;
+    };
+    // Warm-up runs size the pools and bring the SM clock up before anything is
+    // timed.  The candidates are then timed in turn, round after round, and
+    // each keeps its fastest run: a clock ramp or a cache warming up during the
+    // tuning spreads over every candidate instead of favouring the last ones.
+    m->tunes[key] = shape_of(kCandidates[0]);
+    for (int rep = 0; rep < 3 && rc == LVN_OK; rep++) rc = run_fresh_batch(m, descs, brushes, nullptr);
+    std::array<std::array<double, ST_COUNT>, kCand> ms;
+    for (auto& a : ms) a.fill(1e30);
+    for (int round = 0; round < kRounds && rc == LVN_OK; round++) {
+        for (int k = 0; k < kCand && rc == LVN_OK; k++) {
+            m->tunes[key] = shape_of(kCandidates[k]);
             for (int st = 0; st < ST_COUNT; st++) m->stage_ms[st] = 0.0, m->stage_launches[st] = 0;
             rc = run_fresh_batch(m, descs, brushes, nullptr);
             for (int st = 0; st < ST_COUNT; st++)
-                if (m->stage_launches[st]) ms[st] = std::min(ms[st], m->stage_ms[st]);
+                if (m->stage_launches[st]) ms[k][st] = std::min(ms[k][st], m->stage_ms[st]);
         }
-        if (rc) break;
-        for (int st = 0; st < ST_COUNT; st++)
-            if (stage_has_persistent_grid(st) && ms[st] < best_ms[st]) {
-                best_ms[st] = ms[st];
-                best[st] = cand;
-            }
     }
+    std::array<double, ST_COUNT> best_ms;
+    std::array<int, ST_COUNT> best{};
+    best_ms.fill(1e30);
+    for (int k = 0; k < kCand && rc == LVN_OK; k++)
+        for (int st = 0; st < ST_COUNT; st++)
+            if (stage_has_persistent_grid(st) && ms[k][st] < best_ms[st]) {
+                best_ms[st] = ms[k][st];
+                best[st] = kCandidates[k];
+            }
     m->profile = profile;
     std::memcpy(m->stage_ms, saved_ms, sizeof(saved_ms));
     std::memcpy(m->stage_launches, saved_launches, sizeof(saved_launches));
@@ -1588,24 +1599,29 @@ int lvn_meshgen_autotune(lvn_meshgen* m, const lvn_chunk_desc* chunks, int32_t n
     }
     m->tunes[key] = best;
     // hermite shares the GPU with the voxel / hash / quad chain in the batch
-    // DAG: its grid is chosen by the time of the whole batch graph
-    double best_total = 1e30;
-    int best_h = 0;
-    for (int cand : kCandidates) {
-        m->dag_tunes[key] = cand;
-        double t = 1e30;
-        for (int rep = 0; rep < 3 && rc == LVN_OK; rep++) {  // the first run captures the graph
+    // DAG: its grid is chosen by the time of the whole batch graph.  A change
+    // of shape re-captures the graph, so each candidate's first run in a round
+    // (the capture) is not timed; candidates again take turns, round by round.
+    std::array<double, kCand> total;
+    total.fill(1e30);
+    for (int round = 0; round < kRounds && rc == LVN_OK; round++) {
+        for (int k = 0; k < kCand && rc == LVN_OK; k++) {
+            m->dag_tunes[key] = kCandidates[k];
+            rc = run_fresh_batch(m, descs, brushes, nullptr);
+            if (rc) break;
             const auto t0 = std::chrono::steady_clock::now();
             rc = run_fresh_batch(m, descs, brushes, nullptr);
             const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-            if (rep > 0) t = std::min(t, dt);
-        }
-        if (rc) break;
-        if (t < best_total) {
-            best_total = t;
-            best_h = cand;
+            total[k] = std::min(total[k], dt);
         }
     }
+    double best_total = 1e30;
+    int best_h = 0;
+    for (int k = 0; k < kCand && rc == LVN_OK; k++)
+        if (total[k] < best_total) {
+            best_total = total[k];
+            best_h = kCandidates[k];
+        }
     if (rc) {
         m->dag_tunes.erase(key);
         return rc;

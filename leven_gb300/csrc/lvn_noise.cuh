@@ -207,24 +207,30 @@ struct Noise {
         const float2 z0 = sub2(pz, sub2(piz, t));
         const int b1a = ((int)piy.x & 255) * kT3Row + ((int)pix.x & 255), b2a = ((int)piz.x & 255) * kT3Row;
         const int b1b = ((int)piy.y & 255) * kT3Row + ((int)pix.y & 255), b2b = ((int)piz.y & 255) * kT3Row;
-        const bool xya = x0.x >= y0.x, xza = x0.x >= z0.x, yza = y0.x >= z0.x;
-        const bool xyb = x0.y >= y0.y, xzb = x0.y >= z0.y, yzb = y0.y >= z0.y;
-        const bool o1xa = xya && xza, o1ya = !xya && yza, o1za = !xza && !yza;
-        const bool o2xa = xya || xza, o2ya = !xya || yza, o2za = !xza || !yza;
-        const bool o1xb = xyb && xzb, o1yb = !xyb && yzb, o1zb = !xzb && !yzb;
-        const bool o2xb = xyb || xzb, o2yb = !xyb || yzb, o2zb = !xzb || !yzb;
-        auto f = [](bool o) { return o ? 1.f : 0.f; };
+        // simplex() (simplex.cl:74-100) in exact 0 / 1 float arithmetic, both
+        // lanes at once: with fxy = (x0 >= y0) etc., the axis of rank 2 steps
+        // first (o1 = the product of its two comparisons) and the axes of rank
+        // >= 1 step second (o2 = a + b - ab, their "or").  The texel offsets of
+        // those corners are the same 0 / 1 values times the row stride, exact in
+        // float and converted once per lane.
+        auto ge = [](float a, float b) { return a >= b ? 1.f : 0.f; };
+        const float2 fxy = make_float2(ge(x0.x, y0.x), ge(x0.y, y0.y));
+        const float2 fxz = make_float2(ge(x0.x, z0.x), ge(x0.y, z0.y));
+        const float2 fyz = make_float2(ge(y0.x, z0.x), ge(y0.y, z0.y));
+        const float2 nxy = sub2(v2(1.f), fxy), nxz = sub2(v2(1.f), fxz), nyz = sub2(v2(1.f), fyz);
+        const float2 o1x = mul2(fxy, fxz), o2x = sub2(add2(fxy, fxz), o1x);
+        const float2 o1y = mul2(nxy, fyz), o2y = sub2(add2(nxy, fyz), o1y);
+        const float2 o1z = mul2(nxz, nyz), o2z = sub2(add2(nxz, nyz), o1z);
+        const float R = (float)kT3Row;
+        const float2 r1 = fma2(o1y, v2(R), o1x), r2 = fma2(o2y, v2(R), o2x);
+        const float2 s1 = mul2(o1z, v2(R)), s2 = mul2(o2z, v2(R));
         const float2 n0 = corner3x2(grad3(b1a, b2a), grad3(b1b, b2b), x0, y0, z0);
-        const float2 n1 = corner3x2(grad3(b1a + (o1ya ? kT3Row : 0) + o1xa, b2a + (o1za ? kT3Row : 0)),
-                                    grad3(b1b + (o1yb ? kT3Row : 0) + o1xb, b2b + (o1zb ? kT3Row : 0)),
-                                    add2(sub2(x0, make_float2(f(o1xa), f(o1xb))), v2(G3)),
-                                    add2(sub2(y0, make_float2(f(o1ya), f(o1yb))), v2(G3)),
-                                    add2(sub2(z0, make_float2(f(o1za), f(o1zb))), v2(G3)));
-        const float2 n2 = corner3x2(grad3(b1a + (o2ya ? kT3Row : 0) + o2xa, b2a + (o2za ? kT3Row : 0)),
-                                    grad3(b1b + (o2yb ? kT3Row : 0) + o2xb, b2b + (o2zb ? kT3Row : 0)),
-                                    add2(sub2(x0, make_float2(f(o2xa), f(o2xb))), v2(C2)),
-                                    add2(sub2(y0, make_float2(f(o2ya), f(o2yb))), v2(C2)),
-                                    add2(sub2(z0, make_float2(f(o2za), f(o2zb))), v2(C2)));
+        const float2 n1 = corner3x2(grad3(b1a + (int)r1.x, b2a + (int)s1.x), grad3(b1b + (int)r1.y, b2b + (int)s1.y),
+                                    add2(sub2(x0, o1x), v2(G3)), add2(sub2(y0, o1y), v2(G3)),
+                                    add2(sub2(z0, o1z), v2(G3)));
+        const float2 n2 = corner3x2(grad3(b1a + (int)r2.x, b2a + (int)s2.x), grad3(b1b + (int)r2.y, b2b + (int)s2.y),
+                                    add2(sub2(x0, o2x), v2(C2)), add2(sub2(y0, o2y), v2(C2)),
+                                    add2(sub2(z0, o2z), v2(C2)));
         const float2 n3 = corner3x2(grad3(b1a + kT3Row + 1, b2a + kT3Row), grad3(b1b + kT3Row + 1, b2b + kT3Row),
                                     sub2(x0, v2(C3)), sub2(y0, v2(C3)), sub2(z0, v2(C3)));
         return mul2(v2(32.f), add2(add2(add2(n0, n1), n2), n3));
