@@ -549,6 +549,8 @@ def run_lvn(args):
         "metric": METRIC, "value": round(value, 2), "unit": "chunks/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "step_ms": {"min": round(min(t_dev), 4), "median": round(statistics.median(t_dev), 4),
+                    "max": round(max(t_dev), 4)},
         "config": {"workload": wl.name, "chunks_per_step": n, "voxels_per_chunk": wl.voxels_per_chunk,
                    "csg_ops": len(wl.ops), "density": density_name(wl), "lod": lod_range(wl),
                    "simplify": simp_name(simp), "leaf_vertices": int(res_np[:, 7].sum()),

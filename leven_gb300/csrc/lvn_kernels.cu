@@ -602,30 +602,31 @@ __global__ void __launch_bounds__(96) k_field(BatchPtrs b) {
 // rows there get their final-air and changed bits rewritten.
 // ---------------------------------------------------------------------------
 
-// Field of a density with a 3D term (the cave fBm).  One CTA per z slice;
-// the slice's 66 column heights are computed once into shared memory.  The
-// density is fma(amp3, fbm3, base) with base = y - amp2 h, and |amp3 fbm3| is
-// at most b.cave_band, so where |base| exceeds it the sign of the density,
-// which is all the field keeps, is the sign of base.  The other points go to a
-// shared list that all lanes then evaluate, two octaves at a time, until the
-// octaves left cannot change the sign; their solid bits are gathered into the
-// row words with shared-memory atomics.
+// Field of a density with a 3D term (the cave fBm).  One CTA per z slice,
+// one thread per x column.  The density is fma(amp3, fbm3, base) with
+// base = y - amp2 h, and |amp3 fbm3| is at most b.cave_band, so where |base|
+// exceeds it the sign of the density, which is all the field keeps, is the
+// sign of base.  base rounds monotonically in y, so each column is solid below
+// a first row ya (base < -band) and air from a first row yb (base > band),
+// both found by bisection like the heightfield's crossing; only the rows
+// [ya, yb) between them need the 3D term.  Those points go to a shared list
+// that all lanes then evaluate, two octaves at a time, until the octaves left
+// cannot change the sign; their solid bits are gathered into the row words
+// with shared-memory atomics.
 constexpr int kCaveBatch = 1024;  // listed points per batch of the stepped evaluation
 
 template <int VPC>
-__global__ void __launch_bounds__(128) k_field_caves(BatchPtrs b) {
+__global__ void __launch_bounds__(96) k_field_caves(BatchPtrs b) {
     using G = Geo<VPC>;
     __shared__ __align__(16) float sg[64];
     __shared__ float hs[G::FD];
     __shared__ uint32_t words[3][G::FD];
     __shared__ uint16_t list[G::FD * G::FD];
-    __shared__ int nlist;
+    __shared__ int wsum[3];
     __shared__ uint16_t bidx[2][kCaveBatch];  // the undecided points of a batch, ping-pong
     __shared__ float bnoise[2][kCaveBatch];   // their fBm partial sums
     __shared__ int bcount[2];
     if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
-    if (threadIdx.x == 0) nlist = 0;
-    for (int i = threadIdx.x; i < 3 * G::FD; i += blockDim.x) (&words[0][0])[i] = 0u;
     const int c = blockIdx.y, z = blockIdx.x;
     if (b.s_on && b.sslot[c] >= 0) return;  // the surrogate's field (k_field_sdens)
     const int scale = b.desc[c].scale;
@@ -634,36 +635,73 @@ __global__ void __launch_bounds__(128) k_field_caves(BatchPtrs b) {
     const float wz = (float)(z * scale + oz);
     __syncthreads();
     const Noise nz{b.perm_t3, sg};
-    const int tx = (int)threadIdx.x;  // signed: chunk offsets may be negative
-    if (tx < G::FD) {
-        const float h = height_m<LVN_DENSITY_CAVES>(nz, dp, (float)(tx * scale + ox), wz);
-        hs[tx] = h;
-        if (b.hmap) b.hmap[(size_t)c * G::FD * G::FD + tx + G::FD * z] = h;
-    }
-    __syncthreads();
+    const int x = threadIdx.x;
+    const bool valid = x < G::FD;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int dm = b.default_material;
-    const bool write_mats = b.need_mats != 0;
-    uint8_t* mats = b.mats + (size_t)c * G::F + G::FD * G::FD * z;
     const float amp2 = dp.amp2, band = b.cave_band;
-    const int lane = threadIdx.x & 31;
-    // the whole CTA runs every round, so that each ballot has all 32 lanes
-    for (int i0 = 0; i0 < G::FD * G::FD; i0 += blockDim.x) {
-        const int i = i0 + threadIdx.x;
-        const bool valid = i < G::FD * G::FD;
-        const int y = i / G::FD, x = i - G::FD * y;
-        const float base = valid ? fmaf(-amp2, hs[x], (float)(y * scale + oy)) : 0.f;
-        const bool decided = valid && fabsf(base) > band;  // false for a NaN band or base
-        const unsigned need = __ballot_sync(0xffffffffu, valid && !decided);
-        int slot = 0;
-        if (lane == 0 && need) slot = atomicAdd(&nlist, __popc(need));
-        slot = __shfl_sync(0xffffffffu, slot, 0);
-        if (valid && !decided) list[slot + __popc(need & ((1u << lane) - 1u))] = (uint16_t)i;
-        if (decided) {
-            const int m = base < 0.f ? dm : MATERIAL_AIR;
-            if (write_mats) mats[i] = (uint8_t)m;
-            if (m != MATERIAL_AIR) atomicOr(&words[x >> 5][y], 1u << (x & 31));
+    const float h = valid ? height_m<LVN_DENSITY_CAVES>(nz, dp, (float)(x * scale + ox), wz) : 0.f;
+    if (valid) {
+        hs[x] = h;
+        if (b.hmap) b.hmap[(size_t)c * G::FD * G::FD + x + G::FD * z] = h;
+    }
+    // ya: the first row whose base is not below -band; yb: the first row from
+    // ya up whose base is above band (G::FD where there is none).  A NaN base
+    // or band decides nothing: ya = 0, yb = G::FD, every row evaluated.  An AIR
+    // default material makes every point air: no rows at all.
+    int ya = 0, yb = 0;
+    if (valid && dm != MATERIAL_AIR) {
+        int lo = 0, hi = G::FD;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (fmaf(-amp2, h, (float)(mid * scale + oy)) < -band) lo = mid + 1;
+            else hi = mid;
+        }
+        ya = lo;
+        hi = G::FD;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (!(fmaf(-amp2, h, (float)(mid * scale + oy)) > band)) lo = mid + 1;
+            else hi = mid;
+        }
+        yb = lo;
+    }
+    // the warp's row words of the rows decided solid: every valid column is
+    // solid below the warp's lowest ya and none from its highest, so only the
+    // rows between need a ballot.  Lane l keeps rows l, l + 32 and l + 64.
+    {
+        const unsigned vmask = __ballot_sync(FULL, valid);
+        const int ymin = __reduce_min_sync(FULL, valid ? ya : G::FD);
+        const int ymax = __reduce_max_sync(FULL, valid ? ya : 0);
+        uint32_t w0 = 0, w1 = 0, w2 = 0;
+        for (int y = ymin; y < ymax; y++) {
+            const unsigned sb = __ballot_sync(FULL, y < ya);
+            if ((y & 31) == lane) {
+                w0 = y < 32 ? sb : w0;
+                w1 = y >= 32 && y < 64 ? sb : w1;
+                w2 = y >= 64 ? sb : w2;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const int y = lane + 32 * k;
+            if (y < G::FD) words[warp][y] = y < ymin ? vmask : y >= ymax ? 0u : k == 0 ? w0 : k == 1 ? w1 : w2;
         }
     }
+    // list the band rows of every column: an exclusive scan of the counts
+    const int cnt = valid ? yb - ya : 0;
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    int off = incl - cnt;
+    for (int w = 0; w < warp; w++) off += wsum[w];
+    const int nl = wsum[0] + wsum[1] + wsum[2];
+    for (int k = 0; k < cnt; k++) list[off + k] = (uint16_t)(x + G::FD * (ya + k));
     __syncthreads();
     // The listed points, a batch at a time, two fBm octaves a step.  After a
     // step, a point whose partial density fma(amp3, noise, base) exceeds the
@@ -671,7 +709,6 @@ __global__ void __launch_bounds__(128) k_field_caves(BatchPtrs b) {
     // sign whatever they add, so it is decided; the others carry their partial
     // sum (the exact float the full loop holds there) to the next step through
     // a compacted batch list, and the last step decides by the full density.
-    const int nl = nlist;
     const int steps = dp.octaves3 > 0 ? (dp.octaves3 + 1) / 2 : 1;
     for (int b0 = 0; b0 < nl; b0 += kCaveBatch) {
         const int nb = min(kCaveBatch, nl - b0);
@@ -685,16 +722,14 @@ __global__ void __launch_bounds__(128) k_field_caves(BatchPtrs b) {
             const float rem = b.cave_rem[st + 1];
             for (int k = threadIdx.x; k < n_in; k += blockDim.x) {
                 const int i = st == 0 ? list[b0 + k] : bidx[src][k];
-                const int y = i / G::FD, x = i - G::FD * y;
+                const int y = i / G::FD, px = i - G::FD * y;
                 const float wy = (float)(y * scale + oy);
-                const float base = fmaf(-amp2, hs[x], wy);
+                const float base = fmaf(-amp2, hs[px], wy);
                 const float noise = nz.fbm3_step(st, dp.octaves3, dp.freq3, dp.lacunarity3, dp.gain3,
-                                                 (float)(x * scale + ox), wy, wz, st == 0 ? 0.f : bnoise[src][k]);
+                                                 (float)(px * scale + ox), wy, wz, st == 0 ? 0.f : bnoise[src][k]);
                 const float v = fmaf(dp.amp3, noise, base);
                 if (last || !(fabsf(v) <= rem)) {
-                    const int m = v < 0.f ? dm : MATERIAL_AIR;
-                    if (write_mats) mats[i] = (uint8_t)m;
-                    if (m != MATERIAL_AIR) atomicOr(&words[x >> 5][y], 1u << (x & 31));
+                    if (v < 0.f) atomicOr(&words[px >> 5][y], 1u << (px & 31));
                 } else {
                     const int slot = atomicAdd(&bcount[dst], 1);
                     bidx[dst][slot] = (uint16_t)i;
@@ -715,6 +750,14 @@ __global__ void __launch_bounds__(128) k_field_caves(BatchPtrs b) {
         P[y] = p;
         A[y] = and4(not4(p), V);
         X[y] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    // byte materials, where the batch keeps them: the default material where
+    // the point is solid, AIR elsewhere
+    if (b.need_mats && valid) {
+        uint8_t* mats = b.mats + (size_t)c * G::F + x + G::FD * G::FD * z;
+        const uint32_t* wc = &words[x >> 5][0];
+        const uint32_t bit = 1u << (x & 31);
+        for (int y = 0; y < G::FD; y++) mats[G::FD * y] = (uint8_t)((wc[y] & bit) ? dm : MATERIAL_AIR);
     }
 }
 
@@ -2519,7 +2562,7 @@ cudaError_t launch_field(const BatchPtrs& b, cudaStream_t s) {
     switch (b.density.mode) {
         case LVN_DENSITY_REFERENCE: LVN_VPC_DISPATCH(b.vpc, (k_field<V, LVN_DENSITY_REFERENCE><<<grid, 96, 0, s>>>(b))); break;
         case LVN_DENSITY_FBM2D: LVN_VPC_DISPATCH(b.vpc, (k_field<V, LVN_DENSITY_FBM2D><<<grid, 96, 0, s>>>(b))); break;
-        default: LVN_VPC_DISPATCH(b.vpc, (k_field_caves<V><<<grid, 128, 0, s>>>(b))); break;
+        default: LVN_VPC_DISPATCH(b.vpc, (k_field_caves<V><<<grid, 96, 0, s>>>(b))); break;
     }
     if (b.s_on) LVN_VPC_DISPATCH(b.vpc, (k_field_sdens<V><<<grid, 128, 0, s>>>(b)));
     return cudaGetLastError();
