@@ -270,6 +270,29 @@ def test_cave_field_band(lvn_gpu, mg):
     assert solid >= 1 and air >= 1, (solid, air)
 
 
+@pytest.mark.parametrize("amp3", [0.0, -12.0, 300.0])
+def test_cave_field_band_edges(lvn_gpu, mg, amp3):
+    """The field kernel's band rows at their limits: no cave term (a band of
+    width 0, only points with y - amp2 h == 0 evaluated), a negative cave
+    amplitude (the band uses |amp3|), and a band wider than the chunks (every
+    row of every column evaluated).  Materials and meshes match the oracle."""
+    lvn = lvn_gpu
+    dens = dict(W.CAVES, amp3=amp3)
+    lvn.set_density(**dens)
+    chunks = [((0, -256, 0), 256), ((256, 0, 0), 256), ((0, -1024, 1024), 1024)]
+    V, T, S, res = mg.generate_chunks(chunks)
+    O.set_seed(1)
+    od = O.density(**{k: v for k, v in dens.items() if k not in ("lacunarity2", "lacunarity3")},
+                   lac2=dens["lacunarity2"], lac3=dens["lacunarity3"])
+    for c, (mn, size) in enumerate(chunks):
+        ref = O.OracleChunk(od, mn, size, vpc=64)
+        scale = size // 256
+        compare_stages(lvn, mg, c, ref, 64, scale)
+        r = res[c]
+        compare_mesh(V[r[0]:r[0] + r[1]], T[r[2]:r[2] + r[3]], S[r[4]:r[4] + r[5]], ref, scale)
+    lvn.set_density(**W.CAVES)
+
+
 def test_empty_chunks(lvn_gpu, mg):
     lvn = lvn_gpu
     lvn.set_density(**W.FBM2D)
