@@ -92,6 +92,8 @@ def parse():
                         "seams: the seam meshes of one camera's clipmap; collapse: the engine's edge-collapse "
                         "simplification of that clipmap's meshes")
     p.add_argument("--no-surrogate", action="store_true", help="sweep: skip the learned-density leg")
+    p.add_argument("--inflight", type=int, default=3,
+                   help="batches in flight on as many contexts for the pipelined end-to-end figure (>= 2)")
     p.add_argument("--chunks", type=int, default=0,
                    help="mesh only the workload's first N chunks (0 = all; for small profiler captures)")
     return p.parse_args()
@@ -411,38 +413,43 @@ def run_lvn(args):
             torch.distributed.barrier()
         return times, bo
 
-    # end to end with two batches in flight: a second context with its own
+    # end to end with batches in flight: further contexts, each with its own
     # stream and pinned host arrays; while one batch's outputs cross to the
-    # host, the other's kernels run (lvn_meshgen_generate_chunks_async)
-    mg2 = lvn.MeshGen(wl.voxels_per_chunk)
-    mg2.set_option(lvn.LVN_OPT_CACHE, 0)
-    # copy-engine transfers, so that one batch's transfer leaves the SMs to the other's kernels
-    mg2.set_option(lvn.LVN_OPT_HOST_WRITES, 0)
-    # the two contexts' kernels run batch after batch; only transfers overlap kernels
-    mg2.set_option(lvn.LVN_OPT_COMPUTE_ORDER, 1)
-    if simp >= 0:
-        mg2.set_simplify(simp)
-    if tuned:
-        mg2.autotune(wl.chunks)
-    stream2 = torch.cuda.ExternalStream(mg2.stream(), device=dev)
-    results2 = (lvn.ChunkResult * n)()
-    h_vert2 = torch.empty(cap_v * 12, dtype=torch.float32).pin_memory()
-    h_tri2 = torch.empty(cap_t * 3, dtype=torch.int32).pin_memory()
-    h_seam2 = torch.empty(cap_s * 12, dtype=torch.int32).pin_memory()
-    bo_pipe = [batch_out(False),
-               lvn.BatchOut(lvn.LVN_MEMORY_HOST, h_vert2.data_ptr(), cap_v, 0, h_tri2.data_ptr(), cap_t, 0,
-                            h_seam2.data_ptr(), cap_s, 0, C.cast(results2, C.POINTER(lvn.ChunkResult)))]
-    ctxs = [(mg, stream), (mg2, stream2)]
+    # host, the next batches' kernels run (lvn_meshgen_generate_chunks_async).
+    # With three in flight a batch's transfer may take up to twice a batch's
+    # kernel time before the next submission on its context waits for it.
+    extra = []
+    for _ in range(max(2, args.inflight) - 1):
+        mgx = lvn.MeshGen(wl.voxels_per_chunk)
+        mgx.set_option(lvn.LVN_OPT_CACHE, 0)
+        # copy-engine transfers, so that a batch's transfer leaves the SMs to the others' kernels
+        mgx.set_option(lvn.LVN_OPT_HOST_WRITES, 0)
+        # the contexts' kernels run batch after batch; only transfers overlap kernels
+        mgx.set_option(lvn.LVN_OPT_COMPUTE_ORDER, 1)
+        if simp >= 0:
+            mgx.set_simplify(simp)
+        if tuned:
+            mgx.autotune(wl.chunks)
+        resx = (lvn.ChunkResult * n)()
+        hv = torch.empty(cap_v * 12, dtype=torch.float32).pin_memory()
+        ht = torch.empty(cap_t * 3, dtype=torch.int32).pin_memory()
+        hs = torch.empty(cap_s * 12, dtype=torch.int32).pin_memory()
+        bo = lvn.BatchOut(lvn.LVN_MEMORY_HOST, hv.data_ptr(), cap_v, 0, ht.data_ptr(), cap_t, 0,
+                          hs.data_ptr(), cap_s, 0, C.cast(resx, C.POINTER(lvn.ChunkResult)))
+        extra.append((mgx, torch.cuda.ExternalStream(mgx.stream(), device=dev), bo, (resx, hv, ht, hs)))
+    ctxs = [(mg, stream)] + [(x[0], x[1]) for x in extra]
+    bo_pipe = [batch_out(False)] + [x[2] for x in extra]
+    inflight = len(ctxs)
 
     def pipelined(steps, warmup):
         def run(count):
             for k in range(count):
-                c, _ = ctxs[k % 2]
-                if k >= 2:
-                    r = ctxs[k % 2][0].wait()
+                c, _ = ctxs[k % inflight]
+                if k >= inflight:
+                    r = c.wait()
                     if r != 0:
                         raise lvn.LvnError(r, "generate_chunks_async")
-                r = c.generate_chunks_async_raw(descs, n, bo_pipe[k % 2])
+                r = c.generate_chunks_async_raw(descs, n, bo_pipe[k % inflight])
                 if r != 0:
                     raise lvn.LvnError(r, "generate_chunks_async")
             for c, _ in ctxs:
@@ -455,13 +462,15 @@ def run_lvn(args):
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
-        e0, e1, eb = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
-                      torch.cuda.Event())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        stream2.wait_event(e0)
+        for _, sx in ctxs[1:]:
+            sx.wait_event(e0)
         run(steps)
-        eb.record(stream2)
-        stream.wait_event(eb)
+        for _, sx in ctxs[1:]:
+            eb = torch.cuda.Event()
+            eb.record(sx)
+            stream.wait_event(eb)
         e1.record(stream)
         e1.synchronize()
         torch.cuda.synchronize()
@@ -477,7 +486,8 @@ def run_lvn(args):
         ms_pipe = pipelined(args.steps, max(3, args.warmup // 2))
     ms = sum(t_dev) / len(t_dev)
     ms_single = sum(t_e2e) / len(t_e2e)
-    mg2.close()
+    for x in extra:
+        x[0].close()
     if world > 1:
         t = torch.tensor([ms, ms_single, ms_pipe], dtype=torch.float64, device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -562,11 +572,12 @@ def run_lvn(args):
                    "edges": E, "seams": int(bo.total_seams)},
         "e2e": {"value": round(e2e, 2), "unit": "chunks/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": round(ms_e2e, 4),
-                "mode": "pinned host outputs moved by the copy engine (LVN_OPT_HOST_WRITES 0); two contexts, "
-                        "a batch in flight on each (lvn_meshgen_generate_chunks_async), their kernels in one "
-                        "device-wide order (LVN_OPT_COMPUTE_ORDER 1) so that one batch's transfer overlaps the "
-                        "next batch's kernels; CUDA events from the first batch's start to the last one's end "
-                        "over both streams",
+                "mode": f"pinned host outputs moved by the copy engine (LVN_OPT_HOST_WRITES 0); {inflight} "
+                        "contexts, a batch in flight on each (lvn_meshgen_generate_chunks_async), their kernels in "
+                        "one device-wide order (LVN_OPT_COMPUTE_ORDER 1) so that one batch's transfer overlaps the "
+                        "next batches' kernels; CUDA events from the first batch's start to the last one's end "
+                        "over all the streams",
+                "batches_in_flight": inflight,
                 "single_call": {"value": round(e2e_single, 2), "ms_per_step": round(ms_single, 4),
                                 "mode": "one synchronous lvn_meshgen_generate_chunks call per step, the kernels "
                                         "writing the pinned host arrays (LVN_OPT_HOST_WRITES 1)"}},
