@@ -99,6 +99,15 @@ def parse():
     return p.parse_args()
 
 
+def interval_summary(stamps):
+    """min / median / max of the host-clock gaps between consecutive batch
+    completions of the pipelined run (a diagnostic of its steadiness)."""
+    gaps = [1e3 * (b - a) for a, b in zip(stamps, stamps[1:])]
+    if not gaps:
+        return None
+    return {"min": round(min(gaps), 3), "median": round(statistics.median(gaps), 3), "max": round(max(gaps), 3)}
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -428,8 +437,8 @@ def run_lvn(args):
         mgx.set_option(lvn.LVN_OPT_COMPUTE_ORDER, 1)
         if simp >= 0:
             mgx.set_simplify(simp)
-        if tuned:
-            mgx.autotune(wl.chunks)
+        # the tuned shapes are process-wide: every context runs those the
+        # first context's autotuning chose
         resx = (lvn.ChunkResult * n)()
         hv = torch.empty(cap_v * 12, dtype=torch.float32).pin_memory()
         ht = torch.empty(cap_t * 3, dtype=torch.int32).pin_memory()
@@ -441,21 +450,28 @@ def run_lvn(args):
     bo_pipe = [batch_out(False)] + [x[2] for x in extra]
     inflight = len(ctxs)
 
+    done_at = []  # host clock when each timed batch's wait returned (diagnostics only)
+
     def pipelined(steps, warmup):
-        def run(count):
+        def run(count, stamps=None):
             for k in range(count):
                 c, _ = ctxs[k % inflight]
                 if k >= inflight:
                     r = c.wait()
                     if r != 0:
                         raise lvn.LvnError(r, "generate_chunks_async")
+                    if stamps is not None:
+                        stamps.append(time.perf_counter())
                 r = c.generate_chunks_async_raw(descs, n, bo_pipe[k % inflight])
                 if r != 0:
                     raise lvn.LvnError(r, "generate_chunks_async")
-            for c, _ in ctxs:
+            for j in range(inflight):
+                c, _ = ctxs[(count + j) % inflight]
                 r = c.wait()
                 if r != 0:
                     raise lvn.LvnError(r, "generate_chunks_async")
+                if stamps is not None:
+                    stamps.append(time.perf_counter())
         mg.set_option(lvn.LVN_OPT_HOST_WRITES, 0)
         mg.set_option(lvn.LVN_OPT_COMPUTE_ORDER, 1)
         run(warmup)
@@ -466,7 +482,7 @@ def run_lvn(args):
         e0.record(stream)
         for _, sx in ctxs[1:]:
             sx.wait_event(e0)
-        run(steps)
+        run(steps, done_at)
         for _, sx in ctxs[1:]:
             eb = torch.cuda.Event()
             eb.record(sx)
@@ -578,6 +594,7 @@ def run_lvn(args):
                         "next batches' kernels; CUDA events from the first batch's start to the last one's end "
                         "over all the streams",
                 "batches_in_flight": inflight,
+                "completion_interval_ms": interval_summary(done_at),
                 "single_call": {"value": round(e2e_single, 2), "ms_per_step": round(ms_single, 4),
                                 "mode": "one synchronous lvn_meshgen_generate_chunks call per step, the kernels "
                                         "writing the pinned host arrays (LVN_OPT_HOST_WRITES 1)"}},

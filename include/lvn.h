@@ -246,7 +246,9 @@ int lvn_meshgen_set_simplify(lvn_meshgen* ctx, float threshold);
  * lvn_meshgen_generate_chunks would, outputs discarded) with each stage's
  * persistent grid at 2, 4, 8, 16 and 32 CTAs per SM, and keeps the fastest
  * shape of every stage for later batches with the same density mode,
- * crossing mode, simplification setting and power-of-two batch size.  The
+ * crossing mode, simplification setting and power-of-two batch size, on
+ * every context of the process (tune once, then keep batches in flight on
+ * several contexts that all run the tuned shapes).  The
  * hermite stage, which a batch runs beside the voxel / hash / quad stages, is
  * then tuned again by the time of the whole batch.  The chosen CTAs per SM,
  * indexed by stage (0 = built-in default), go to
@@ -300,13 +302,18 @@ int lvn_debug_cuckoo(const uint32_t* keys, int32_t n, uint32_t prime, int32_t fl
  * meshing calls.  LVN_FAULT_DEVICE_ALLOC makes the next `count` device
  * allocations fail as cudaMalloc's out-of-memory does (the call returns
  * LVN_ERR_OUT_OF_MEMORY); LVN_FAULT_HASH_FAMILY makes the next `count` cuckoo
- * parameter draws a degenerate family under which no table holds three keys
- * (the call returns LVN_ERR_HASH after its bounded retries, where the
- * reference's loop at compute_cuckoo.cpp:86-132 retries without bound);
- * LVN_FAULT_NONE clears both.  No GPU fault is involved. */
-#define LVN_FAULT_NONE         0
-#define LVN_FAULT_DEVICE_ALLOC 1
-#define LVN_FAULT_HASH_FAMILY  2
+ * parameter draws a degenerate family under which no table holds three keys,
+ * and the batch's device-side table repair degenerate as well (the call
+ * returns LVN_ERR_HASH after its bounded retries, where the reference's loop
+ * at compute_cuckoo.cpp:86-132 retries without bound);
+ * LVN_FAULT_HASH_FAMILY_HOST makes the next `count` host draws degenerate
+ * but leaves the device-side repair its own parameters, so that a batch
+ * meshes only through that repair; LVN_FAULT_NONE clears them all.  No GPU
+ * fault is involved. */
+#define LVN_FAULT_NONE              0
+#define LVN_FAULT_DEVICE_ALLOC      1
+#define LVN_FAULT_HASH_FAMILY       2
+#define LVN_FAULT_HASH_FAMILY_HOST  3
 int lvn_debug_inject_fault(int32_t what, int32_t count);
 
 /* No counterpart in the reference.  Meshes one chunk exactly as

@@ -676,7 +676,7 @@ class Surrogate:
 
 
 LVN_CUCKOO_REFERENCE_FIND = 1
-LVN_FAULT_NONE, LVN_FAULT_DEVICE_ALLOC, LVN_FAULT_HASH_FAMILY = 0, 1, 2
+LVN_FAULT_NONE, LVN_FAULT_DEVICE_ALLOC, LVN_FAULT_HASH_FAMILY, LVN_FAULT_HASH_FAMILY_HOST = 0, 1, 2, 3
 
 
 def debug_cuckoo(keys, prime=0, reference_find=False, with_table=False):

@@ -46,6 +46,7 @@ namespace {
 // return a degenerate family.  Test hooks; both stay 0 in normal use.
 int g_fault_device_alloc = 0;
 int g_fault_hash_family = 0;
+bool g_fault_hash_host_only = false;  // the degenerate draws spare the device-side repair
 
 struct DevBuf {
     void* p = nullptr;
@@ -388,10 +389,12 @@ struct lvn_meshgen {
     cudaEvent_t ev_fork = nullptr, ev_herm = nullptr, ev_hash = nullptr, ev_mesh = nullptr;
     int dag_hermite_per_sm = 0;
 
-    // autotuned persistent-grid shapes (CTAs per SM per stage), keyed by
-    // density mode, crossing mode, simplification on/off and log2(batch size)
+    // the shapes an autotuning in progress on this context is trying (CTAs
+    // per SM per stage, and hermite's inside the batch DAG); the results are
+    // published process-wide (g_tunes) when the tuning ends
+    bool tuning = false;
     std::map<std::array<int, 4>, std::array<int, ST_COUNT>> tunes;
-    std::map<std::array<int, 4>, int> dag_tunes;  // hermite's CTAs per SM inside the batch DAG
+    std::map<std::array<int, 4>, int> dag_tunes;
 
     // profiling
     cudaEvent_t ev[ST_COUNT + 1] = {};
@@ -513,6 +516,40 @@ Capacity default_capacity(const lvn_meshgen* m, int n) {
                     (int64_t)n * (int64_t)std::min(C, 24 * 1024) + (int64_t)C};
 }
 
+// Autotuned launch shapes, keyed by density mode, crossing mode,
+// simplification on/off and log2(batch size), shared by every context of the
+// process: the best shapes are a property of the device and the kind of
+// batch, and contexts that keep batches in flight side by side should run
+// them alike.
+struct Tuned {
+    std::array<int, ST_COUNT> shape;  // CTAs per SM per stage (0 = built-in)
+    int dag_hermite;                  // hermite's CTAs per SM inside the batch DAG
+};
+std::mutex g_tune_mutex;
+std::map<std::array<int, 4>, Tuned> g_tunes;
+
+// The shapes for batches of kind `key` on context m: those its own tuning
+// is trying, else the published ones.  False when there are none.
+bool stage_shapes(const lvn_meshgen* m, const std::array<int, 4>& key, std::array<int, ST_COUNT>* shape,
+                  int* dag_hermite) {
+    if (m->tuning) {
+        const auto t = m->tunes.find(key);
+        const auto d = m->dag_tunes.find(key);
+        if (shape && t != m->tunes.end()) *shape = t->second;
+        if (dag_hermite) *dag_hermite = d != m->dag_tunes.end() ? d->second : 0;
+        return t != m->tunes.end();
+    }
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    const auto t = g_tunes.find(key);
+    if (t == g_tunes.end()) {
+        if (dag_hermite) *dag_hermite = 0;
+        return false;
+    }
+    if (shape) *shape = t->second.shape;
+    if (dag_hermite) *dag_hermite = t->second.dag_hermite;
+    return true;
+}
+
 std::array<int, 4> tune_key(const lvn_meshgen* m, int n) {
     int bucket = 0;
     while ((2 << bucket) <= n) bucket++;
@@ -522,9 +559,9 @@ std::array<int, 4> tune_key(const lvn_meshgen* m, int n) {
 BatchPtrs make_ptrs(lvn_meshgen* m, int n) {
     BatchPtrs b;
     std::memset(&b, 0, sizeof(b));
-    auto tuned = m->tunes.find(tune_key(m, n));
-    if (tuned != m->tunes.end())
-        for (int st = 0; st < ST_COUNT; st++) b.grid_per_sm[st] = tuned->second[st];
+    std::array<int, ST_COUNT> shape{};
+    if (stage_shapes(m, tune_key(m, n), &shape, nullptr))
+        for (int st = 0; st < ST_COUNT; st++) b.grid_per_sm[st] = shape[st];
     b.n = n;
     b.vpc = m->vpc;
     b.crossing_mode = m->crossing_mode;
@@ -532,6 +569,7 @@ BatchPtrs make_ptrs(lvn_meshgen* m, int n) {
     b.derive_mats = 1;
     b.need_mats = 0;
     b.num_sms = g.num_sms;
+    b.hash_fault = device_hash_fault();
     b.density = g.density;
     b.default_material = g.default_material;
     density_fields(g.density, g.default_material, &b.cave_band, b.cave_rem, b.dom_by_solid);
@@ -975,8 +1013,9 @@ int run_fresh_batch(lvn_meshgen* m, std::vector<ChunkDesc>& descs, const std::ve
     Capacity cap = default_capacity(m, n);
     cap.ecap = std::max(cap.ecap, m->ecap);
     cap.vcap = std::max(cap.vcap, m->vcap);
-    const auto dag = m->dag_tunes.find(tune_key(m, n));
-    m->dag_hermite_per_sm = dag != m->dag_tunes.end() ? dag->second : 0;
+    int dag_hermite = 0;
+    stage_shapes(m, tune_key(m, n), nullptr, &dag_hermite);
+    m->dag_hermite_per_sm = dag_hermite;
     for (int attempt = 0; attempt < kMaxHashRetries + 2; attempt++) {
         int rc = ensure_pools(m, n, cap);
         if (rc) return rc;
@@ -1040,6 +1079,7 @@ int run_fresh_batch(lvn_meshgen* m, std::vector<ChunkDesc>& descs, const std::ve
             key.push_back(thr_bits);
             for (int st = 0; st < ST_COUNT; st++) key.push_back((uintptr_t)b.grid_per_sm[st]);
             key.push_back((uintptr_t)m->dag_hermite_per_sm);
+            key.push_back((uintptr_t)b.hash_fault);
             const uint32_t* dk = reinterpret_cast<const uint32_t*>(&g.density);
             for (size_t i = 0; i < sizeof(g.density) / 4; i++) key.push_back(dk[i]);
             if (!m->graph_exec || key != m->graph_key) {
@@ -1556,6 +1596,9 @@ int lvn_meshgen_autotune(lvn_meshgen* m, const lvn_chunk_desc* chunks, int32_t n
     std::memcpy(saved_ms, m->stage_ms, sizeof(saved_ms));
     std::memcpy(saved_launches, m->stage_launches, sizeof(saved_launches));
     m->profile = true;
+    m->tuning = true;
+    m->tunes.clear();
+    m->dag_tunes.clear();
     static const int kCandidates[] = {2, 4, 8, 16, 32};
     constexpr int kCand = sizeof(kCandidates) / sizeof(kCandidates[0]);
     constexpr int kRounds = 3;
@@ -1594,7 +1637,7 @@ int lvn_meshgen_autotune(lvn_meshgen* m, const lvn_chunk_desc* chunks, int32_t n
     std::memcpy(m->stage_ms, saved_ms, sizeof(saved_ms));
     std::memcpy(m->stage_launches, saved_launches, sizeof(saved_launches));
     if (rc) {
-        m->tunes.erase(key);
+        m->tuning = false;
         return rc;
     }
     m->tunes[key] = best;
@@ -1622,11 +1665,12 @@ int lvn_meshgen_autotune(lvn_meshgen* m, const lvn_chunk_desc* chunks, int32_t n
             best_total = total[k];
             best_h = kCandidates[k];
         }
-    if (rc) {
-        m->dag_tunes.erase(key);
-        return rc;
+    m->tuning = false;
+    if (rc) return rc;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        g_tunes[key] = Tuned{best, best_h};
     }
-    m->dag_tunes[key] = best_h;
     if (grid_per_sm) {
         for (int st = 0; st < ST_COUNT; st++) grid_per_sm[st] = best[st];
         grid_per_sm[ST_HERMITE] = best_h;  // the shape used in batches
@@ -1909,9 +1953,20 @@ int lvn_meshgen_qef_fp64_error(lvn_meshgen* m, double out[4]) {
 int lvn_debug_inject_fault(int32_t what, int32_t count) {
     if (count < 0) return LVN_ERR_INVALID;
     switch (what) {
-        case LVN_FAULT_NONE: g_fault_device_alloc = 0; g_fault_hash_family = 0; return LVN_OK;
+        case LVN_FAULT_NONE:
+            g_fault_device_alloc = 0;
+            g_fault_hash_family = 0;
+            g_fault_hash_host_only = false;
+            return LVN_OK;
         case LVN_FAULT_DEVICE_ALLOC: g_fault_device_alloc = count; return LVN_OK;
-        case LVN_FAULT_HASH_FAMILY: g_fault_hash_family = count; return LVN_OK;
+        case LVN_FAULT_HASH_FAMILY:
+            g_fault_hash_family = count;
+            g_fault_hash_host_only = false;
+            return LVN_OK;
+        case LVN_FAULT_HASH_FAMILY_HOST:
+            g_fault_hash_family = count;
+            g_fault_hash_host_only = true;
+            return LVN_OK;
         default: return LVN_ERR_INVALID;
     }
 }
@@ -2051,6 +2106,7 @@ int stored_ops_for_chunk(const int32_t min[3], int32_t size, Brush* out, int cap
 }
 
 void draw_hash_params(uint32_t* p) { draw_params(p); }
+int device_hash_fault() { return g_fault_hash_family > 0 && !g_fault_hash_host_only ? 1 : 0; }
 
 void lod_colour_for(int s, float c[3]) { lod_colour(s, c); }
 

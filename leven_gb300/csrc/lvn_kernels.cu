@@ -826,52 +826,79 @@ __global__ void __launch_bounds__(kProbes) k_gate(BatchPtrs b) {
     if (p == 0) b.gate_ok[c] = bad ? 0 : 1;
 }
 
-// One CTA per (z slice, chunk): 96 threads along x (three warps, one per
-// plane word) times kCsgRows rows of y taken together.
+// A persistent grid over the batch's (chunk, z slice) pairs, pair w to CTA
+// w % gridDim.x.  On a large batch few slices have work (the chunks an
+// operation touches, inside their operation boxes), so a CTA first tests a
+// block of its pairs with one thread each and lists those with work, then
+// takes the listed slices one at a time: 96 threads along x (three warps,
+// one per plane word) times kCsgRows rows of y taken together.  One CTA per
+// pair instead launched n * 66 CTAs, nearly all of them empty on a clipmap
+// batch.
 constexpr int kCsgRows = 8;
+constexpr int kCsgThreads = 96 * kCsgRows;
 
 template <int VPC>
-__global__ void __launch_bounds__(96 * kCsgRows) k_csg(BatchPtrs b) {
+__global__ void __launch_bounds__(kCsgThreads) k_csg(BatchPtrs b) {
     using G = Geo<VPC>;
-    const int c = blockIdx.y, z = blockIdx.x;
-    const ChunkDesc d = b.desc[c];  // a copy: the byte stores below may alias the descriptor
-    const int nops = d.op_count;
-    if (nops == 0 || z < d.csg_lo[2] || z > d.csg_hi[2]) return;
-    const int x = threadIdx.x;
-    const bool inx = x < G::FD && x >= d.csg_lo[0] && x <= d.csg_hi[0];
-    const Brush* ops = b.brushes + d.op_begin;
-    uint8_t* mats = b.mats + (size_t)c * G::F + G::FD * G::FD * z;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    uint32_t* A = reinterpret_cast<uint32_t*>(plane_ptr<VPC>(b, c, 1) + G::FD * z);
-    uint32_t* X = reinterpret_cast<uint32_t*>(plane_ptr<VPC>(b, c, 2) + G::FD * z);
-    const float wx = (float)(d.off[0] + d.scale * x);
-    const float wz = (float)(d.off[2] + d.scale * z);
-    for (int y = d.csg_lo[1] + (int)threadIdx.y; y <= d.csg_hi[1]; y += kCsgRows) {  // uniform per warp
-        bool air = false, changed = false;
-        if (x < G::FD) {
-            // a fresh field's materials are the default or AIR, given by its
-            // plain-solid bits; a cached field's are in the byte array
-            const int m = b.need_mats ? mats[x + G::FD * y]
-                                      : (bit4(plane_ptr<VPC>(b, c, 0)[y + G::FD * z], x) ? b.default_material
-                                                                                        : MATERIAL_AIR);
-            int nm = m;
-            if (inx) {
-                const float wy = (float)(d.off[1] + d.scale * y);
-                for (int i = 0; i < nops; i++) {
-                    const Brush& br = ops[i];
-                    if (brush_density(br, wx, wy, wz) <= 0.f) nm = br.type == 0 ? br.material : MATERIAL_AIR;
+    __shared__ int active[kCsgThreads];
+    __shared__ int nact;
+    const int tid = threadIdx.x + 96 * threadIdx.y;
+    const int items = b.n * G::FD;
+    const int mine = (items - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;  // this CTA's pairs
+    for (int base = 0; base < mine; base += kCsgThreads) {
+        if (tid == 0) nact = 0;
+        __syncthreads();
+        const int k = base + tid;
+        const int w = (int)blockIdx.x + k * (int)gridDim.x;
+        if (k < mine) {
+            const int c = w / G::FD, z = w - G::FD * c;
+            const ChunkDesc& dd = b.desc[c];
+            if (dd.op_count > 0 && z >= dd.csg_lo[2] && z <= dd.csg_hi[2]) active[atomicAdd(&nact, 1)] = w;
+        }
+        __syncthreads();
+        const int na = nact;
+        for (int a = 0; a < na; a++) {
+            const int c = active[a] / G::FD, z = active[a] - G::FD * (active[a] / G::FD);
+            const ChunkDesc d = b.desc[c];  // a copy: the byte stores below may alias the descriptor
+            const int nops = d.op_count;
+            const int x = threadIdx.x;
+            const bool inx = x < G::FD && x >= d.csg_lo[0] && x <= d.csg_hi[0];
+            const Brush* ops = b.brushes + d.op_begin;
+            uint8_t* mats = b.mats + (size_t)c * G::F + G::FD * G::FD * z;
+            const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+            uint32_t* A = reinterpret_cast<uint32_t*>(plane_ptr<VPC>(b, c, 1) + G::FD * z);
+            uint32_t* X = reinterpret_cast<uint32_t*>(plane_ptr<VPC>(b, c, 2) + G::FD * z);
+            const float wx = (float)(d.off[0] + d.scale * x);
+            const float wz = (float)(d.off[2] + d.scale * z);
+            for (int y = d.csg_lo[1] + (int)threadIdx.y; y <= d.csg_hi[1]; y += kCsgRows) {  // uniform per warp
+                bool air = false, changed = false;
+                if (x < G::FD) {
+                    // a fresh field's materials are the default or AIR, given by its
+                    // plain-solid bits; a cached field's are in the byte array
+                    const int m = b.need_mats ? mats[x + G::FD * y]
+                                              : (bit4(plane_ptr<VPC>(b, c, 0)[y + G::FD * z], x) ? b.default_material
+                                                                                                : MATERIAL_AIR);
+                    int nm = m;
+                    if (inx) {
+                        const float wy = (float)(d.off[1] + d.scale * y);
+                        for (int i = 0; i < nops; i++) {
+                            const Brush& br = ops[i];
+                            if (brush_density(br, wx, wy, wz) <= 0.f) nm = br.type == 0 ? br.material : MATERIAL_AIR;
+                        }
+                        // inside the box the byte array holds the final material
+                        if (nm != m || !b.need_mats) mats[x + G::FD * y] = (uint8_t)nm;
+                    }
+                    air = nm == MATERIAL_AIR;
+                    changed = nm != m;
                 }
-                // inside the box the byte array holds the final material
-                if (nm != m || !b.need_mats) mats[x + G::FD * y] = (uint8_t)nm;
+                const unsigned aw = __ballot_sync(FULL, air), cw = __ballot_sync(FULL, changed);
+                if (lane == 0) {
+                    A[4 * y + warp] = aw;
+                    X[4 * y + warp] = cw;
+                }
             }
-            air = nm == MATERIAL_AIR;
-            changed = nm != m;
         }
-        const unsigned aw = __ballot_sync(FULL, air), cw = __ballot_sync(FULL, changed);
-        if (lane == 0) {
-            A[4 * y + warp] = aw;
-            X[4 * y + warp] = cw;
-        }
+        __syncthreads();  // every thread is done with the list before the next block resets it
     }
 }
 
@@ -1025,63 +1052,111 @@ __global__ void __launch_bounds__(256) k_primes(BatchPtrs b) {
     }
 }
 
-// Single CTA: per-chunk tile offsets, per-chunk edge offsets, edge-table plan.
+// The edge plan in two launches: per-chunk tile offsets (many CTAs), then the
+// batch's per-chunk edge offsets and edge-table plan (one CTA).
+// Each chunk's edge tiles: exclusive offsets of the three edge classes within
+// the chunk and the chunk's counts.  One warp per chunk, eight chunks a CTA.
 template <int VPC>
-__global__ void __launch_bounds__(1024) k_edge_plan(BatchPtrs b) {
+__global__ void __launch_bounds__(256) k_edge_tiles(BatchPtrs b) {
     using G = Geo<VPC>;
-    __shared__ int sm[1024 / 32 + 1];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int c = warp; c < b.n; c += 32) {
-        int4* t = b.edge_tiles + (size_t)c * G::NBE;
-        int cx = 0, cy = 0, cc = 0;
-        for (int base = 0; base < G::NBE; base += 32) {
-            const int i = base + lane;
-            const int4 v = i < G::NBE ? t[i] : make_int4(0, 0, 0, 0);
-            const int ix = warp_inclusive(v.x), iy = warp_inclusive(v.y), ic = warp_inclusive(v.z);
-            if (i < G::NBE) t[i] = make_int4(cx + ix - v.x, cy + iy - v.y, cc + ic - v.z, 0);
-            cx += __shfl_sync(FULL, ix, 31);
-            cy += __shfl_sync(FULL, iy, 31);
-            cc += __shfl_sync(FULL, ic, 31);
-        }
-        if (lane == 0) {
-            // edges kept from a cached field precede the plain class
-            const int cp = b.cs[c].kept_edges + cx + cy;
-            b.cs[c].edges_xz = cx;
-            b.cs[c].edges_y = cy;
-            b.cs[c].plain_edges = cp;
-            b.cs[c].created_edges = cc;
-            b.cs[c].num_edges = cp + cc;
+    const int lane = threadIdx.x & 31;
+    const int c = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (c >= b.n) return;  // the warp's own chunk: the exit is warp-uniform
+    int4* t = b.edge_tiles + (size_t)c * G::NBE;
+    int cx = 0, cy = 0, cc = 0;
+    for (int base = 0; base < G::NBE; base += 32) {
+        const int i = base + lane;
+        const int4 v = i < G::NBE ? t[i] : make_int4(0, 0, 0, 0);
+        const int ix = warp_inclusive(v.x), iy = warp_inclusive(v.y), ic = warp_inclusive(v.z);
+        if (i < G::NBE) t[i] = make_int4(cx + ix - v.x, cy + iy - v.y, cc + ic - v.z, 0);
+        cx += __shfl_sync(FULL, ix, 31);
+        cy += __shfl_sync(FULL, iy, 31);
+        cc += __shfl_sync(FULL, ic, 31);
+    }
+    if (lane == 0) {
+        // edges kept from a cached field precede the plain class
+        const int cp = b.cs[c].kept_edges + cx + cy;
+        b.cs[c].edges_xz = cx;
+        b.cs[c].edges_y = cy;
+        b.cs[c].plain_edges = cp;
+        b.cs[c].created_edges = cc;
+        b.cs[c].num_edges = cp + cc;
+    }
+}
+
+// Exclusive scans of K values a thread over the CTA, side by side with one
+// set of barriers; `sm` holds K * (NT / 32 + 1) ints.
+template <int NT, int K>
+__device__ __forceinline__ void block_exclusive_k(const int (&v)[K], int (&ex)[K], int (&total)[K], int* sm) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int W = NT / 32;
+    int inc[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        inc[k] = warp_inclusive(v[k]);
+        if (lane == 31) sm[k * (W + 1) + warp] = inc[k];
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const int w = lane < W ? sm[k * (W + 1) + lane] : 0;
+            const int wi = warp_inclusive(w);
+            if (lane < W) sm[k * (W + 1) + lane] = wi - w;
+            if (lane == W - 1) sm[k * (W + 1) + W] = wi;
         }
     }
     __syncthreads();
-    const long long total = cta_scan(
-        b.n, [&](int c) { return b.cs[c].num_edges; }, [&](int c, long long ex) { b.cs[c].edge_off = (int)ex; },
-        nullptr, sm);
-    // table slots are reserved for the largest prime the chunk can need; the
-    // prime itself is found later by k_primes
-    const long long slots = cta_scan(
-        b.n, [&](int c) { return table_slot_bound(b.cs[c].num_edges); },
-        [&](int c, long long ex) { b.cs[c].edge_table_off = (int)ex; }, nullptr, sm);
-    const long long txz = cta_scan(
-        b.n, [&](int c) { return b.cs[c].edges_xz; }, [&](int c, long long ex) { b.cs[c].wl_xz_off = (int)ex; },
-        nullptr, sm);
-    const long long ty = cta_scan(
-        b.n, [&](int c) { return b.cs[c].edges_y; }, [&](int c, long long ex) { b.cs[c].wl_y_off = (int)ex; },
-        nullptr, sm);
-    const long long tcr = cta_scan(
-        b.n, [&](int c) { return b.cs[c].created_edges; }, [&](int c, long long ex) { b.cs[c].wl_c_off = (int)ex; },
-        nullptr, sm);
-    if (threadIdx.x == 0) {
-        b.bs->total_xz = (int)txz;
-        b.bs->total_y = (int)ty;
-        b.bs->total_created = (int)tcr;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        ex[k] = inc[k] - v[k] + sm[k * (W + 1) + warp];
+        total[k] = sm[k * (W + 1) + W];
+    }
+    __syncthreads();
+}
+
+// The batch's edge offsets: five exclusive scans over the chunks in one pass
+// (edges, hash-table slots, and the work-list segments of plain x / z, plain
+// y and created edges), then the totals and the capacity checks.
+template <int VPC>
+__global__ void __launch_bounds__(1024) k_edge_plan(BatchPtrs b) {
+    __shared__ int sm[5 * (1024 / 32 + 1)];
+    long long carry[5] = {0, 0, 0, 0, 0};
+    for (int base = 0; base < b.n; base += 1024) {
+        const int c = base + threadIdx.x;
+        int v[5] = {0, 0, 0, 0, 0};
+        if (c < b.n) {
+            const ChunkState& cs = b.cs[c];
+            v[0] = cs.num_edges;
+            // table slots are reserved for the largest prime the chunk can
+            // need; the prime itself is found later by k_primes
+            v[1] = table_slot_bound(cs.num_edges);
+            v[2] = cs.edges_xz;
+            v[3] = cs.edges_y;
+            v[4] = cs.created_edges;
+        }
+        int ex[5], tot[5];
+        block_exclusive_k<1024, 5>(v, ex, tot, sm);
+        if (c < b.n) {
+            ChunkState& cs = b.cs[c];
+            cs.edge_off = (int)(carry[0] + ex[0]);
+            cs.edge_table_off = (int)(carry[1] + ex[1]);
+            cs.wl_xz_off = (int)(carry[2] + ex[2]);
+            cs.wl_y_off = (int)(carry[3] + ex[3]);
+            cs.wl_c_off = (int)(carry[4] + ex[4]);
+        }
+#pragma unroll
+        for (int k = 0; k < 5; k++) carry[k] += tot[k];
     }
     if (threadIdx.x == 0) {
-        b.bs->total_edges = (int)total;
-        b.bs->total_edge_slots = slots;
+        b.bs->total_xz = (int)carry[2];
+        b.bs->total_y = (int)carry[3];
+        b.bs->total_created = (int)carry[4];
+        b.bs->total_edges = (int)carry[0];
+        b.bs->total_edge_slots = carry[1];
         int ovf = 0;
-        if (total > b.ecap) ovf |= OVF_EDGES;
-        if (slots > b.edge_slot_cap) ovf |= OVF_EDGE_SLOTS;
+        if (carry[0] > b.ecap) ovf |= OVF_EDGES;
+        if (carry[1] > b.edge_slot_cap) ovf |= OVF_EDGE_SLOTS;
         b.bs->overflow |= ovf;
     }
 }
@@ -1577,6 +1652,84 @@ __global__ void __launch_bounds__(kThreads) k_node_insert(BatchPtrs b) {
                                     (uint32_t)(i - st->node_off));
         if (r == 1) st->node_stash_used = 1;
         if (r < 0) st->node_insert_failed = 1;
+    }
+}
+
+// Device-side repair of a chunk's cuckoo table after a failed insert (a key
+// whose eviction chain ran out and whose stash slot was taken).  The host
+// would redraw that chunk's parameters and rerun the whole batch; instead one
+// CTA draws new parameters from the old ones, clears the table and inserts
+// the chunk's keys again, up to kRepairAttempts times, within the batch.  The
+// new parameters go to the chunk's descriptor, where the lookups read them.
+// A chunk still failing after that keeps its flag, and the host reruns.
+constexpr int kRepairAttempts = 8;
+constexpr int kRepairThreads = 256;
+
+// a parameter word from the previous one and a salt, in the host's draw
+// range [2^15, 2^30] (a 32-bit finaliser of the two)
+__device__ __forceinline__ uint32_t repair_param(uint32_t prev, uint32_t salt) {
+    uint32_t x = prev ^ (salt * 0x9E3779B9u);
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return (1u << 15) + x % ((1u << 30) - (1u << 15) + 1u);
+}
+
+template <bool NODES>
+__global__ void __launch_bounds__(kRepairThreads) k_hash_repair(BatchPtrs b) {
+    __shared__ int list[kRepairThreads];
+    __shared__ int nl, failed, stashed;
+    if (b.bs->overflow) return;  // the same for every thread
+    if (threadIdx.x == 0) nl = 0;
+    __syncthreads();
+    const int c = blockIdx.x * kRepairThreads + threadIdx.x;
+    if (c < b.n && (NODES ? b.cs[c].node_insert_failed : b.cs[c].edge_insert_failed)) list[atomicAdd(&nl, 1)] = c;
+    __syncthreads();
+    for (int a = 0; a < nl; a++) {
+        const int ch = list[a];
+        ChunkState* st = b.cs + ch;
+        // the descriptors are this batch's device copy: writable
+        uint32_t* params = const_cast<uint32_t*>(NODES ? b.desc[ch].node_params : b.desc[ch].edge_params);
+        const uint32_t prime = NODES ? st->node_prime : st->edge_prime;
+        const uint32_t magic = NODES ? st->node_magic : st->edge_magic;
+        unsigned long long* table = NODES ? b.node_slots + st->node_table_off : b.edge_slots + st->edge_table_off;
+        const int first = NODES ? st->node_off : st->edge_off;
+        const int count = NODES ? st->nodes : st->num_edges;
+        for (int attempt = 0; attempt < kRepairAttempts; attempt++) {
+            uint32_t p[10];
+#pragma unroll
+            for (int k = 0; k < 10; k++)  // an injected fault makes these degenerate too (a = 0)
+                p[k] = b.hash_fault ? ((k & 1) ? 1u << 15 : 0u)
+                                    : repair_param(params[k], (uint32_t)(ch * 10 + k) * 31u + (uint32_t)attempt);
+            __syncthreads();  // every thread has read the previous parameters
+            if (threadIdx.x < 10) params[threadIdx.x] = p[threadIdx.x];
+            if (threadIdx.x == 0) {
+                failed = 0;
+                stashed = 0;
+            }
+            for (uint32_t i = threadIdx.x; i < prime + CUCKOO_STASH_SIZE; i += kRepairThreads) table[i] = CUCKOO_EMPTY;
+            __syncthreads();
+            for (int i = threadIdx.x; i < count; i += kRepairThreads) {
+                const uint32_t key = NODES ? b.node_codes[first + i] : (uint32_t)b.edge_keys[first + i];
+                const int r = cuckoo_insert(table, table + prime, prime, magic, p, key, (uint32_t)i);
+                if (r == 1) stashed = 1;
+                if (r < 0) failed = 1;
+            }
+            __syncthreads();
+            if (!failed) break;
+        }
+        if (threadIdx.x == 0) {
+            if (NODES) {
+                st->node_stash_used = stashed;
+                st->node_insert_failed = failed;
+            } else {
+                st->edge_stash_used = stashed;
+                st->edge_insert_failed = failed;
+            }
+        }
+        __syncthreads();  // the flags are read before the next chunk resets them
     }
 }
 
@@ -2579,7 +2732,8 @@ cudaError_t launch_gate(const BatchPtrs& b, cudaStream_t s) {
 }
 
 cudaError_t launch_csg(const BatchPtrs& b, cudaStream_t s) {
-    dim3 grid(b.vpc + 2, b.n);
+    // two CTAs per SM, no more than the batch has pairs
+    const int grid = std::max(1, std::min(2 * b.num_sms, b.n * (b.vpc + 2)));
     LVN_VPC_DISPATCH(b.vpc, (k_csg<V><<<grid, dim3(96, kCsgRows), 0, s>>>(b)));
     return cudaGetLastError();
 }
@@ -2596,6 +2750,7 @@ cudaError_t launch_edge_count(const BatchPtrs& b, cudaStream_t s) {
 }
 
 cudaError_t launch_edge_plan(const BatchPtrs& b, cudaStream_t s) {
+    LVN_VPC_DISPATCH(b.vpc, (k_edge_tiles<V><<<(b.n + 7) / 8, 256, 0, s>>>(b)));
     LVN_VPC_DISPATCH(b.vpc, (k_edge_plan<V><<<1, 1024, 0, s>>>(b)));
     return cudaGetLastError();
 }
@@ -2645,6 +2800,7 @@ cudaError_t launch_hash_fill(const BatchPtrs& b, cudaStream_t s) {
 
 cudaError_t launch_edge_insert(const BatchPtrs& b, cudaStream_t s) {
     k_edge_insert<<<persistent_grid(b, ST_EDGE_INSERT, 8), kThreads, 0, s>>>(b);
+    k_hash_repair<false><<<(b.n + kRepairThreads - 1) / kRepairThreads, kRepairThreads, 0, s>>>(b);
     return cudaGetLastError();
 }
 
@@ -2660,6 +2816,7 @@ cudaError_t launch_leaf(const BatchPtrs& b, cudaStream_t s) {
 
 cudaError_t launch_node_insert(const BatchPtrs& b, cudaStream_t s) {
     k_node_insert<<<persistent_grid(b, ST_NODE_INSERT, 8), kThreads, 0, s>>>(b);
+    k_hash_repair<true><<<(b.n + kRepairThreads - 1) / kRepairThreads, kRepairThreads, 0, s>>>(b);
     return cudaGetLastError();
 }
 

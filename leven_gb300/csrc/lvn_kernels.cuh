@@ -21,6 +21,7 @@ struct BatchPtrs {
                                  //    elsewhere they are the default material or AIR by the solid bits
     int need_mats;               // 1: the field kernel writes every byte material (cached fields)
     int num_sms;
+    int hash_fault;              // 1: a table repair draws degenerate parameters too (host fault injection)
     DensityParams density;
     float cave_band;             // |y - amp2 h| above this: the cave term cannot change the density's sign
     float cave_rem[kCaveSteps + 1];  // cave_rem[s]: bound on |amp3 * octaves 2s.. of fbm3| (0 past the last)

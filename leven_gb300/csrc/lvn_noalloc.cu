@@ -152,6 +152,7 @@ extern "C" int lvn_generate_chunk_mesh_noalloc(const int32_t min[3], int32_t siz
     BatchPtrs b;
     std::memset(&b, 0, sizeof(b));
     b.n = 1;
+    b.hash_fault = device_hash_fault();
     b.vpc = vpc;
     b.crossing_mode = 0;
     b.plain_class = 1;

@@ -24,6 +24,9 @@ GlobalView global_view();
 int stored_ops_for_chunk(const int32_t min[3], int32_t size, Brush* out, int cap);
 // Draws one cuckoo parameter set (10 words) from the shared generator.
 void draw_hash_params(uint32_t* p);
+// 1 while injected degenerate draws also apply to the device-side table
+// repair (BatchPtrs::hash_fault), 0 in normal use.
+int device_hash_fault();
 // ColourForMinLeafSize (clipmap.cpp:329-353)
 void lod_colour_for(int min_leaf_size, float c[3]);
 // The batch fields derived from the density and the default material: the

@@ -142,3 +142,37 @@ def test_injected_allocation_failure(lvn_gpu):
     finally:
         lvn.inject_fault(lvn.LVN_FAULT_NONE, 0)
         mg.close()
+
+
+def test_device_table_repair(lvn_gpu):
+    """A failed cuckoo insert is repaired inside the batch: with every host
+    draw of parameters degenerate (no table holds three keys) and the batch's
+    device-side repair left its own draws, each chunk's edge and leaf tables
+    are rebuilt on the device, and the meshes equal the oracle's bit for bit,
+    through the batch call and the single-chunk call.  Without the repair the
+    call could only end in LVN_ERR_HASH (previous test)."""
+    lvn = lvn_gpu
+    lvn.set_density(**W.FBM2D)
+    lvn.clear_csg_operations()
+    chunks = [((0, 128, 0), 256), ((256, 128, 0), 256), ((0, -128, 256), 256), ((256, 0, 256), 256)]
+    mg = lvn.MeshGen(64)
+    try:
+        mg.set_option(lvn.LVN_OPT_CACHE, 0)
+        lvn.inject_fault(lvn.LVN_FAULT_HASH_FAMILY_HOST, 1 << 20)
+        V, T, S, res = mg.generate_chunks(chunks)
+        one = mg.generate_chunk_mesh(chunks[0][0], chunks[0][1])
+        lvn.inject_fault(lvn.LVN_FAULT_NONE, 0)
+        O.set_seed(1)
+        for c, (mn, size) in enumerate(chunks):
+            ref = O.OracleChunk(O.density(mode=1), mn, size, vpc=64)
+            r = res[c]
+            nv = ref.mesh_vertex_count()
+            assert r[1] == nv > 0
+            assert np.array_equal(V[r[0]:r[0] + nv].view(np.int32), ref.vertices()[:nv].view(np.int32)), c
+            assert np.array_equal(T[r[2]:r[2] + r[3]], ref.triangles()), c
+            assert np.array_equal(S[r[4]:r[4] + r[5]][:, :4], ref.seams()[:, :4]), c
+            if c == 0:
+                assert np.array_equal(one.triangles, ref.triangles())
+    finally:
+        lvn.inject_fault(lvn.LVN_FAULT_NONE, 0)
+        mg.close()
