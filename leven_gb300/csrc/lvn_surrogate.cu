@@ -537,7 +537,6 @@ __device__ __forceinline__ void unpack8(uint4 u, float* v) {
         v[2 * i + 1] = f.y;
     }
 }
-__device__ __forceinline__ float bf16_round(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
 
 // Column sums of a warp's 32 rows: lane L holds row L's 32 values in v (which
 // this overwrites) and gets back the sum of column L over the 32 rows.  Each
