@@ -154,10 +154,6 @@ __device__ __forceinline__ float tanh_approx(float x) {
 }
 __device__ __forceinline__ float sigmoid(float z) { return fmaf(0.5f, tanh_approx(0.5f * z), 0.5f); }
 __device__ __forceinline__ float silu(float z) { return z * sigmoid(z); }
-__device__ __forceinline__ float silu_grad(float z) {
-    const float s = sigmoid(z);
-    return s * (1.f + z * (1.f - s));
-}
 // the same on two values at once: the FP32 arithmetic in the two-lane forms
 // (one instruction for both), the hyperbolic tangent per lane
 __device__ __forceinline__ float2 sigmoid2(float2 z) {
