@@ -105,7 +105,8 @@ def interval_summary(stamps):
     gaps = [1e3 * (b - a) for a, b in zip(stamps, stamps[1:])]
     if not gaps:
         return None
-    return {"min": round(min(gaps), 3), "median": round(statistics.median(gaps), 3), "max": round(max(gaps), 3)}
+    return {"min": round(min(gaps), 3), "median": round(statistics.median(gaps), 3), "max": round(max(gaps), 3),
+            "all": [round(g, 2) for g in gaps]}
 
 
 def dist_env():
