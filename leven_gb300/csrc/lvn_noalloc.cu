@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdio>
+#include <mutex>
 #include <cstring>
 
 #include "lvn_kernels.cuh"
@@ -77,9 +78,12 @@ static_assert(OFF_END <= (size_t)LVN_NOALLOC_SCRATCH_BYTES, "scratch layout exce
 static __device__ __align__(256) unsigned char g_noalloc_scratch[LVN_NOALLOC_SCRATCH_BYTES];
 
 // The scratch array's device address, looked up on the first call (with the
-// init device current) and kept for the device it was looked up on.
+// init device current) and kept for the device it was looked up on; the
+// lookup is under a lock, so that threads whose first calls meet do not race
+// on it (the calls themselves must still not overlap, as they share the array).
 int g_scratch_dev = -1;
 unsigned char* g_scratch_ptr = nullptr;
+std::mutex g_scratch_mutex;
 
 int scratch_for_init_device(int init_device, unsigned char** out) {
     int dev = 0;
@@ -89,6 +93,7 @@ int scratch_for_init_device(int init_device, unsigned char** out) {
                      init_device);
         return LVN_ERR_INVALID;
     }
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
     if (g_scratch_dev != dev || !g_scratch_ptr) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
