@@ -1408,6 +1408,7 @@ int lvn_initialise(int32_t noise_seed, uint32_t default_material, int32_t num_cs
     if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return LVN_ERR_NO_DEVICE;
     LVN_CK(cudaGetDevice(&g.device));
     LVN_CK(cudaDeviceGetAttribute(&g.num_sms, cudaDevAttrMultiProcessorCount, g.device));
+    LVN_CK(set_kernel_attributes());
     g.default_material = (int32_t)default_material;
     g.hash_gen = std::mt19937();
     const int rc = upload_perm(noise_seed);

@@ -38,6 +38,8 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 constexpr int kThreads = 256;
+constexpr int kHermiteSmemThreads = 1024;   // k_hermite_smem: one CTA per SM
+constexpr int kHermiteSmemMinChunks = 2048;  // batches at least this large take k_hermite_smem
 
 // ---------------------------------------------------------------------------
 // geometry
@@ -503,13 +505,13 @@ __device__ __forceinline__ uint4 low_bits(int n) {
 
 // Height term and density for a density mode fixed at compile time, so a
 // kernel carries one density's code (DensityFunc, noise.cl:225-268).
-template <int MODE>
-__device__ __forceinline__ float height_m(const Noise& nz, const DensityParams& dp, float x, float z) {
+template <int MODE, class N>
+__device__ __forceinline__ float height_m(const N& nz, const DensityParams& dp, float x, float z) {
     if (MODE == LVN_DENSITY_REFERENCE) return nz.terrain(x, z);
     return nz.fbm2(dp.octaves2, dp.freq2, dp.lacunarity2, dp.gain2, x, z);
 }
-template <int MODE>
-__device__ __forceinline__ float dens_h(const Noise& nz, const DensityParams& dp, float h, float x, float y, float z) {
+template <int MODE, class N>
+__device__ __forceinline__ float dens_h(const N& nz, const DensityParams& dp, float h, float x, float y, float z) {
     const float amp = MODE == LVN_DENSITY_REFERENCE ? 900.f : dp.amp2;  // MAX_TERRAIN_HEIGHT
     const float base = fmaf(-amp, h, y);
     if (MODE != LVN_DENSITY_CAVES) return base;
@@ -1245,8 +1247,8 @@ __global__ void __launch_bounds__(kThreads) k_edge_scatter(BatchPtrs b) {
 // `hm` is the chunk's height map (the field kernel's height term per column),
 // or null: the height at an edge's end points is then read, not recomputed,
 // with the same arguments and so the same value.
-template <int VPC, int MODE>
-__device__ __forceinline__ float4 hermite_density(const BatchPtrs& b, const Noise& nz, const ChunkDesc& d, int key,
+template <int VPC, int MODE, class N>
+__device__ __forceinline__ float4 hermite_density(const BatchPtrs& b, const N& nz, const ChunkDesc& d, int key,
                                                   const float* hm) {
     using G = Geo<VPC>;
     const int axis = key & 3;
@@ -1408,15 +1410,10 @@ __device__ __forceinline__ float4 hermite_sdens(const BatchPtrs& b, int slot, in
     return make_float4(nx, ny, nzv, t);
 }
 
-template <int VPC, int MODE>
-__global__ void __launch_bounds__(kThreads) k_hermite(BatchPtrs b) {
-    __shared__ __align__(16) float sg[64];
-    if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
-    __syncthreads();
-    if (b.bs->overflow) return;
-    const Noise nz{b.perm_t3, sg};
-    // work list segments: plain x/z edges, plain y edges, CSG-created edges, so
-    // that a warp's 32 edges take the same path
+// The hermite work list, grid-stride: plain x/z edges, plain y edges,
+// CSG-created edges, in segments, so that a warp's 32 edges take the same path.
+template <int VPC, int MODE, class N>
+__device__ __forceinline__ void hermite_list(const BatchPtrs& b, const N& nz) {
     const int nplain = b.bs->total_xz + b.bs->total_y;
     const int total = nplain + b.bs->total_created;
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < total; w += gridDim.x * blockDim.x) {
@@ -1430,6 +1427,34 @@ __global__ void __launch_bounds__(kThreads) k_hermite(BatchPtrs b) {
                          : slot >= 0 ? hermite_sdens<VPC>(b, slot, key)
                                      : hermite_density<VPC, MODE>(b, nz, d, key, hm);
     }
+}
+
+template <int VPC, int MODE>
+__global__ void __launch_bounds__(kThreads) k_hermite(BatchPtrs b) {
+    __shared__ __align__(16) float sg[64];
+    if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
+    __syncthreads();
+    if (b.bs->overflow) return;
+    hermite_list<VPC, MODE>(b, Noise{b.perm_t3, sg});
+}
+
+// The same for large batches: one 1024-thread CTA per SM holds the two
+// simplex lookup tables (kT3Bytes) in shared memory, so a table read is a
+// shared load with a 32-bit address instead of a read-only global load with
+// a 64-bit one (9% fewer instructions a 3D fBm).  Such a CTA takes an SM's
+// registers and most of its shared memory, leaving the stages beside hermite
+// in the batch DAG no room; on a large batch hermite's share of the step
+// outweighs that, on a small one it does not.
+template <int VPC, int MODE>
+__global__ void __launch_bounds__(kHermiteSmemThreads, 1) k_hermite_smem(BatchPtrs b) {
+    extern __shared__ __align__(16) uint8_t stab[];  // the lookup tables
+    __shared__ __align__(16) float sg[64];
+    if (b.bs->overflow) return;  // the same for every thread
+    if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
+    const uint4* src = reinterpret_cast<const uint4*>(b.perm_t3);
+    for (int i = threadIdx.x; i < kT3Bytes / 16; i += blockDim.x) reinterpret_cast<uint4*>(stab)[i] = __ldg(src + i);
+    __syncthreads();
+    hermite_list<VPC, MODE>(b, NoiseT<true>{stab, sg});
 }
 
 // ---------------------------------------------------------------------------
@@ -2762,6 +2787,19 @@ cudaError_t launch_edge_scatter(const BatchPtrs& b, cudaStream_t s) {
 }
 
 cudaError_t launch_hermite(const BatchPtrs& b, cudaStream_t s) {
+    if (b.n >= kHermiteSmemMinChunks) {
+        // the tuned grid in 256-thread units per SM, as for the other stages:
+        // 4 units are one 1024-thread CTA per SM, 2 leave half the SMs free
+        const int per_sm = b.grid_per_sm[ST_HERMITE] > 0 ? b.grid_per_sm[ST_HERMITE] : 4;
+        const int g = std::max(1, b.num_sms * per_sm / (kHermiteSmemThreads / kThreads));
+        const int T = kHermiteSmemThreads, smem = kT3Bytes;
+        switch (b.density.mode) {
+            case LVN_DENSITY_REFERENCE: LVN_VPC_DISPATCH(b.vpc, (k_hermite_smem<V, LVN_DENSITY_REFERENCE><<<g, T, smem, s>>>(b))); break;
+            case LVN_DENSITY_FBM2D: LVN_VPC_DISPATCH(b.vpc, (k_hermite_smem<V, LVN_DENSITY_FBM2D><<<g, T, smem, s>>>(b))); break;
+            default: LVN_VPC_DISPATCH(b.vpc, (k_hermite_smem<V, LVN_DENSITY_CAVES><<<g, T, smem, s>>>(b))); break;
+        }
+        return cudaGetLastError();
+    }
     const int g = persistent_grid(b, ST_HERMITE, 8);
     switch (b.density.mode) {
         case LVN_DENSITY_REFERENCE: LVN_VPC_DISPATCH(b.vpc, (k_hermite<V, LVN_DENSITY_REFERENCE><<<g, kThreads, 0, s>>>(b))); break;
@@ -2769,6 +2807,25 @@ cudaError_t launch_hermite(const BatchPtrs& b, cudaStream_t s) {
         default: LVN_VPC_DISPATCH(b.vpc, (k_hermite<V, LVN_DENSITY_CAVES><<<g, kThreads, 0, s>>>(b))); break;
     }
     return cudaGetLastError();
+}
+
+// Kernel attributes set once per device: the shared-memory hermite kernels'
+// lookup tables are above the default dynamic shared-memory limit.
+cudaError_t set_kernel_attributes() {
+    cudaError_t e = cudaSuccess;
+    auto set = [&](const void* f) {
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, kT3Bytes);
+    };
+#define LVN_HERMITE_ATTR(V)                                        \
+    set((const void*)k_hermite_smem<V, LVN_DENSITY_REFERENCE>);    \
+    set((const void*)k_hermite_smem<V, LVN_DENSITY_FBM2D>);        \
+    set((const void*)k_hermite_smem<V, LVN_DENSITY_CAVES>);
+    LVN_HERMITE_ATTR(8)
+    LVN_HERMITE_ATTR(16)
+    LVN_HERMITE_ATTR(32)
+    LVN_HERMITE_ATTR(64)
+#undef LVN_HERMITE_ATTR
+    return e;
 }
 
 cudaError_t launch_vox_count(const BatchPtrs& b, cudaStream_t s) {

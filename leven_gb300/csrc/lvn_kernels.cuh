@@ -177,6 +177,7 @@ cudaError_t launch_edge_count(const BatchPtrs& b, cudaStream_t stream);
 cudaError_t launch_edge_plan(const BatchPtrs& b, cudaStream_t stream);
 cudaError_t launch_edge_scatter(const BatchPtrs& b, cudaStream_t stream);
 cudaError_t launch_hermite(const BatchPtrs& b, cudaStream_t stream);
+cudaError_t set_kernel_attributes();  // once per device, at initialisation
 cudaError_t launch_vox_count(const BatchPtrs& b, cudaStream_t stream);
 cudaError_t launch_vox_plan(const BatchPtrs& b, cudaStream_t stream);
 cudaError_t launch_vox_scatter(const BatchPtrs& b, cudaStream_t stream);

@@ -58,14 +58,23 @@ __device__ __forceinline__ float2 mul2s(float2 a, float2 b) { return make_float2
 __device__ __forceinline__ float2 floor2(float2 a) { return make_float2(floorf(a.x), floorf(a.y)); }
 __device__ __forceinline__ float2 max02(float2 a) { return make_float2(fmaxf(a.x, 0.f), fmaxf(a.y, 0.f)); }
 
-struct Noise {
+// kSharedTables: the kernel staged the two lookup tables in shared memory
+// (plain loads); otherwise they are read from global memory through the
+// read-only path.
+template <bool kSharedTables>
+struct NoiseT {
     const uint8_t* __restrict__ t3;   // the two simplex lookup tables (kT3Row x kT3Row texels each)
     const float* __restrict__ g;      // 16 x 4 gradient table, staged in shared memory
+
+    __device__ __forceinline__ int tab(int i) const {
+        if (kSharedTables) return t3[i];
+        return __ldg(t3 + i);
+    }
 
     // the 2D gradient of texel b of the padded tables (row * kT3Row + column):
     // the second table holds (alpha & 15) * 16, the byte offset of its float4
     __device__ __forceinline__ float2 grad2(int b) const {
-        const int kb = __ldg(t3 + kT3Second + b);
+        const int kb = tab(kT3Second + b);
         return *reinterpret_cast<const float2*>(reinterpret_cast<const char*>(g) + kb);
     }
 
@@ -142,8 +151,8 @@ struct Noise {
     // offset of iz (rows and columns in [0, 256], so a corner adds its 0/1
     // steps without a wrap).
     __device__ __forceinline__ float4 grad3(int b1, int b2) const {
-        const int a = __ldg(t3 + b1);
-        const int kb = __ldg(t3 + kT3Second + b2 + a);
+        const int a = tab(b1);
+        const int kb = tab(kT3Second + b2 + a);
         return *reinterpret_cast<const float4*>(reinterpret_cast<const char*>(g) + kb);  // one 16-byte shared load
     }
 
@@ -389,6 +398,7 @@ struct Noise {
         return density_h(d, height(d, x, z), x, y, z);
     }
 };
+using Noise = NoiseT<false>;
 
 // ---------------------------------------------------------------------------
 // CSG brushes: apply_csg_operation.cl:42-175, hg_sdf.glsl fBox (218-221), pR (460-463)
