@@ -96,6 +96,9 @@ def parse():
                    help="batches in flight on as many contexts for the pipelined end-to-end figure (>= 2)")
     p.add_argument("--chunks", type=int, default=0,
                    help="mesh only the workload's first N chunks (0 = all; for small profiler captures)")
+    p.add_argument("--hermite-form", type=int, default=0, choices=[0, 1, 2],
+                   help="LVN_OPT_HERMITE_FORM: 0 = by batch size, 1 = shared-memory tables, 2 = global tables "
+                        "(so that a small capture can profile the form a large batch takes)")
     return p.parse_args()
 
 
@@ -361,6 +364,7 @@ def run_lvn(args):
         lvn.store_csg_operation(lvn.make_op(op.type, op.brush_shape, op.material, op.origin, op.dimensions))
     mg = lvn.MeshGen(wl.voxels_per_chunk)
     mg.set_option(lvn.LVN_OPT_CACHE, 0)
+    mg.set_option(lvn.LVN_OPT_HERMITE_FORM, args.hermite_form)
     simp = simplify_threshold(args)
     if simp >= 0:
         mg.set_simplify(simp)
@@ -432,6 +436,7 @@ def run_lvn(args):
     for _ in range(max(2, args.inflight) - 1):
         mgx = lvn.MeshGen(wl.voxels_per_chunk)
         mgx.set_option(lvn.LVN_OPT_CACHE, 0)
+        mgx.set_option(lvn.LVN_OPT_HERMITE_FORM, args.hermite_form)
         # copy-engine transfers, so that a batch's transfer leaves the SMs to the others' kernels
         mgx.set_option(lvn.LVN_OPT_HOST_WRITES, 0)
         # the contexts' kernels run batch after batch; only transfers overlap kernels
@@ -583,6 +588,7 @@ def run_lvn(args):
                    "csg_ops": len(wl.ops), "density": density_name(wl), "lod": lod_range(wl),
                    "simplify": simp_name(simp), "leaf_vertices": int(res_np[:, 7].sum()),
                    "launch_shapes": {"autotuned_ctas_per_sm": tuned} if tuned else "built-in",
+                   "hermite_form": ["by batch size", "shared-memory tables", "global tables"][args.hermite_form],
                    "parallelism": f"replicas x{world}",
                    "l2": "flushed between steps (256 MiB write) for value and the single-call e2e; the pipelined "
                          "e2e's batches touch far more than L2 (several GB each)",

@@ -59,6 +59,12 @@ extern "C" {
                                       ordered batch (any context) have ended; its copy-engine
                                       transfers stay outside the order, so they overlap the next
                                       batch's kernels (default 0) */
+#define LVN_OPT_HERMITE_FORM  7   /* new: the hermite kernel's form.  0 = by batch size (default):
+                                      batches of 2048 chunks and more stage the noise lookup
+                                      tables in shared memory (one 1024-thread CTA per SM), smaller
+                                      ones read them from global memory; 1 = shared-memory tables
+                                      for every batch; 2 = global tables for every batch.  The
+                                      results are the same bits in every form */
 
 /* CSGOperationInfo (leven/src/compute.h:16-24; apply_csg_operation.cl:5-14), 48 B */
 typedef struct lvn_csg_op {

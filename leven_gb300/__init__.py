@@ -31,7 +31,7 @@ LVN_MEMORY_HOST = 0
 LVN_MEMORY_DEVICE = 1
 LVN_DENSITY_REFERENCE, LVN_DENSITY_FBM2D, LVN_DENSITY_CAVES = 0, 1, 2
 LVN_OPT_CROSSING_MODE, LVN_OPT_CACHE, LVN_OPT_PROFILE, LVN_OPT_GRAPHS, LVN_OPT_HOST_WRITES = 1, 2, 3, 4, 5
-LVN_OPT_COMPUTE_ORDER = 6
+LVN_OPT_COMPUTE_ORDER, LVN_OPT_HERMITE_FORM = 6, 7
 (DEBUG_MATERIALS, DEBUG_EDGE_KEYS, DEBUG_EDGE_INFO, DEBUG_NODE_CODES, DEBUG_NODE_INFO, DEBUG_EDGE_TABLE,
  DEBUG_EDGE_STASH, DEBUG_NODE_TABLE, DEBUG_NODE_STASH, DEBUG_PLAIN_EDGES, DEBUG_SIMP_REPS) = range(11)
 

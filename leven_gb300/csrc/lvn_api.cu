@@ -338,6 +338,7 @@ struct lvn_meshgen {
     std::thread async_thread;
     bool async_active = false;
     bool host_writes = true;  // LVN_OPT_HOST_WRITES
+    int hermite_form = 0;     // LVN_OPT_HERMITE_FORM
     bool compute_order = false;  // LVN_OPT_COMPUTE_ORDER
     cudaEvent_t ev_order = nullptr;  // recorded after this context's last ordered batch's kernels
     int async_rc = 0;
@@ -570,6 +571,7 @@ BatchPtrs make_ptrs(lvn_meshgen* m, int n) {
     b.need_mats = 0;
     b.num_sms = g.num_sms;
     b.hash_fault = device_hash_fault();
+    b.hermite_form = m->hermite_form;
     b.density = g.density;
     b.default_material = g.default_material;
     density_fields(g.density, g.default_material, &b.cave_band, b.cave_rem, b.dom_by_solid);
@@ -1080,6 +1082,7 @@ int run_fresh_batch(lvn_meshgen* m, std::vector<ChunkDesc>& descs, const std::ve
             for (int st = 0; st < ST_COUNT; st++) key.push_back((uintptr_t)b.grid_per_sm[st]);
             key.push_back((uintptr_t)m->dag_hermite_per_sm);
             key.push_back((uintptr_t)b.hash_fault);
+            key.push_back((uintptr_t)b.hermite_form);
             const uint32_t* dk = reinterpret_cast<const uint32_t*>(&g.density);
             for (size_t i = 0; i < sizeof(g.density) / 4; i++) key.push_back(dk[i]);
             if (!m->graph_exec || key != m->graph_key) {
@@ -1566,6 +1569,10 @@ int lvn_meshgen_set_option(lvn_meshgen* m, int32_t option, int32_t value) {
         case LVN_OPT_GRAPHS: m->use_graphs = value != 0; return LVN_OK;
         case LVN_OPT_HOST_WRITES: m->host_writes = value != 0; return LVN_OK;
         case LVN_OPT_COMPUTE_ORDER: m->compute_order = value != 0; return LVN_OK;
+        case LVN_OPT_HERMITE_FORM:
+            if (value < 0 || value > 2) return LVN_ERR_INVALID;
+            m->hermite_form = value;
+            return LVN_OK;
         default: return LVN_ERR_INVALID;
     }
 }

@@ -2787,7 +2787,8 @@ cudaError_t launch_edge_scatter(const BatchPtrs& b, cudaStream_t s) {
 }
 
 cudaError_t launch_hermite(const BatchPtrs& b, cudaStream_t s) {
-    if (b.n >= kHermiteSmemMinChunks) {
+    const bool shared_tables = b.hermite_form == 1 || (b.hermite_form == 0 && b.n >= kHermiteSmemMinChunks);
+    if (shared_tables) {
         // the tuned grid in 256-thread units per SM, as for the other stages:
         // 4 units are one 1024-thread CTA per SM, 2 leave half the SMs free
         const int per_sm = b.grid_per_sm[ST_HERMITE] > 0 ? b.grid_per_sm[ST_HERMITE] : 4;

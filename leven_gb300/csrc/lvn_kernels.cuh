@@ -22,6 +22,7 @@ struct BatchPtrs {
     int need_mats;               // 1: the field kernel writes every byte material (cached fields)
     int num_sms;
     int hash_fault;              // 1: a table repair draws degenerate parameters too (host fault injection)
+    int hermite_form;            // LVN_OPT_HERMITE_FORM: 0 by batch size, 1 shared-memory tables, 2 global
     DensityParams density;
     float cave_band;             // |y - amp2 h| above this: the cave term cannot change the density's sign
     float cave_rem[kCaveSteps + 1];  // cave_rem[s]: bound on |amp3 * octaves 2s.. of fbm3| (0 past the last)

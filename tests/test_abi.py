@@ -33,6 +33,18 @@ def test_exports_every_declared_symbol(lib):
     assert sorted(lvn.EXPORTS) == names
 
 
+def test_constants_match_header():
+    """Every option, fault and memory-kind constant the Python binding defines
+    has the value include/lvn.h gives it, and every option the header
+    declares is bound."""
+    text = (ROOT / "include" / "lvn.h").read_text()
+    defines = {k: int(v) for k, v in re.findall(r"#define\s+(LVN_[A-Z0-9_]+)\s+(-?\d+)\b", text)}
+    bound = {k: getattr(lvn, k) for k in defines if hasattr(lvn, k)}
+    assert bound and all(bound[k] == defines[k] for k in bound), {k: (bound[k], defines[k]) for k in bound}
+    missing = [k for k in defines if k.startswith(("LVN_OPT_", "LVN_FAULT_", "LVN_MEMORY_")) and k not in bound]
+    assert not missing, missing
+
+
 def test_struct_layouts():
     # byte-identical to CSGOperationInfo, MeshVertex, MeshTriangle, SeamNodeInfo
     assert C.sizeof(lvn.CsgOp) == 48

@@ -498,3 +498,39 @@ def test_graph_and_stream_paths_agree(lvn_gpu):
         a.close()
         b.close()
         lvn.clear_csg_operations()
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_hermite_forms_agree(lvn_gpu, mode):
+    """LVN_OPT_HERMITE_FORM: the hermite kernel with its noise lookup tables in
+    shared memory (the form batches of 2048 chunks and more take) and the one
+    reading them from global memory give the same bits on the same batch, and
+    the shared-memory form matches the oracle on chunks with CSG operations."""
+    lvn = lvn_gpu
+    lvn.set_density(**density_args(mode))
+    lvn.clear_csg_operations()
+    sx, sy, sz = surface_min(mode, 64)
+    chunks = [((sx + 256 * i, sy, sz + 256 * k), 256) for i in range(3) for k in range(2)]
+    chunks.append(((sx, sy - 256, sz), 512))
+    gens = [lvn.MeshGen(64) for _ in range(3)]
+    try:
+        outs = []
+        for form, g in enumerate(gens):
+            g.set_option(lvn.LVN_OPT_CACHE, 0)
+            g.set_option(lvn.LVN_OPT_HERMITE_FORM, form)
+            outs.append(g.generate_chunks(chunks))
+        assert outs[0][3][:, 3].sum() > 0
+        for other in outs[1:]:
+            for x, y in zip(outs[0], other):
+                assert np.array_equal(np.asarray(x).view(np.uint8), np.asarray(y).view(np.uint8))
+        with pytest.raises(lvn.LvnError):
+            gens[0].set_option(lvn.LVN_OPT_HERMITE_FORM, 3)
+        if mode == 2:
+            wl = W.tiled_csg(2, 2, 2, n_ops=8, seed=5)
+            wl = W.Workload(wl.name, wl.chunks, wl.ops, W.CAVES)
+            res, checked = run_batch_vs_oracle(lvn, gens[1], wl)
+            assert checked == 8 and res[:, 3].sum() > 0
+    finally:
+        for g in gens:
+            g.close()
+        lvn.clear_csg_operations()
