@@ -180,7 +180,7 @@ int upload_perm(int seed) {
         for (int c = 0; c < kT3Row; c++) {
             const uint8_t a = v[(r & 255) * 256 + (c & 255)];
             t3[r * kT3Row + c] = a == 255 ? 0 : a;
-            t3[kT3Second + r * kT3Row + c] = (uint8_t)((a & 15) * 16);
+            t3[kT3Second + r * kT3Row + c] = (uint8_t)((a & 15) * 8);
         }
     LVN_CK(g.perm_t3.ensure(kT3Bytes));
     LVN_CK(cudaMemcpy(g.perm_t3.p, t3.data(), kT3Bytes, cudaMemcpyHostToDevice));

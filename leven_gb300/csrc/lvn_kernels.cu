@@ -530,7 +530,7 @@ __global__ void __launch_bounds__(96) k_field(BatchPtrs b) {
     using G = Geo<VPC>;
     __shared__ __align__(16) float sg[64];
     __shared__ uint32_t words[3][G::FD];  // solid-bit word of each warp, per row y
-    if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
+    stage_gradients(sg, b.grad);
     __syncthreads();
     const int c = blockIdx.y, z = blockIdx.x;
     if (b.s_on && b.sslot[c] >= 0) return;  // the surrogate's field (k_field_sdens)
@@ -628,7 +628,7 @@ __global__ void __launch_bounds__(96) k_field_caves(BatchPtrs b) {
     __shared__ uint16_t bidx[2][kCaveBatch];  // the undecided points of a batch, ping-pong
     __shared__ float bnoise[2][kCaveBatch];   // their fBm partial sums
     __shared__ int bcount[2];
-    if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
+    stage_gradients(sg, b.grad);
     const int c = blockIdx.y, z = blockIdx.x;
     if (b.s_on && b.sslot[c] >= 0) return;  // the surrogate's field (k_field_sdens)
     const int scale = b.desc[c].scale;
@@ -803,7 +803,7 @@ template <int VPC>
 __global__ void __launch_bounds__(kProbes) k_probe(BatchPtrs b) {
     using G = Geo<VPC>;
     __shared__ __align__(16) float sg[64];
-    if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
+    stage_gradients(sg, b.grad);
     __syncthreads();
     const int c = blockIdx.x, p = threadIdx.x;
     const ChunkDesc& d = b.desc[c];
@@ -1432,7 +1432,7 @@ __device__ __forceinline__ void hermite_list(const BatchPtrs& b, const N& nz) {
 template <int VPC, int MODE>
 __global__ void __launch_bounds__(kThreads) k_hermite(BatchPtrs b) {
     __shared__ __align__(16) float sg[64];
-    if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
+    stage_gradients(sg, b.grad);
     __syncthreads();
     if (b.bs->overflow) return;
     hermite_list<VPC, MODE>(b, Noise{b.perm_t3, sg});
@@ -1450,7 +1450,7 @@ __global__ void __launch_bounds__(kHermiteSmemThreads, 1) k_hermite_smem(BatchPt
     extern __shared__ __align__(16) uint8_t stab[];  // the lookup tables
     __shared__ __align__(16) float sg[64];
     if (b.bs->overflow) return;  // the same for every thread
-    if (threadIdx.x < 64) sg[threadIdx.x] = b.grad[threadIdx.x];
+    stage_gradients(sg, b.grad);
     const uint4* src = reinterpret_cast<const uint4*>(b.perm_t3);
     for (int i = threadIdx.x; i < kT3Bytes / 16; i += blockDim.x) reinterpret_cast<uint4*>(stab)[i] = __ldg(src + i);
     __syncthreads();

@@ -25,6 +25,22 @@ namespace lvn {
 __device__ __forceinline__ int texel(int row, int col) { return ((row & 255) << 8) | (col & 255); }
 __device__ __forceinline__ int alpha_column(int a) { return a == 255 ? 0 : a; }
 
+// The gradient table as the noise code reads it from shared memory (64
+// floats, 16-byte aligned), staged from the 16 x float4 table `grad` by the
+// block's first 64 threads: the 16 (x, y) pairs in bytes 0-127, then the 16
+// (z, 0) pairs in bytes 128-255.  A texel's second-table byte (alpha & 15) * 8
+// addresses both halves.  Across a warp an (x, y) load touches each of the 32
+// banks at most once per half-warp and a z load 16 distinct banks, so neither
+// conflicts; one float4 load from a 256-byte table conflicts wherever entries
+// k and k + 8 meet in one quarter-warp.
+__device__ __forceinline__ void stage_gradients(float* sg, const float* grad) {
+    const int t = threadIdx.x;
+    if (t < 64) {
+        const int k = t >> 2, c = t & 3;
+        sg[(c < 2 ? 0 : 30) + 2 * k + c] = grad[t];
+    }
+}
+
 __device__ __forceinline__ float dot2(float ax, float ay, float bx, float by) { return fmaf(ay, by, ax * bx); }
 __device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, float by, float bz) {
     return fmaf(az, bz, fmaf(ay, by, ax * bx));
@@ -72,7 +88,8 @@ struct NoiseT {
     }
 
     // the 2D gradient of texel b of the padded tables (row * kT3Row + column):
-    // the second table holds (alpha & 15) * 16, the byte offset of its float4
+    // the second table holds (alpha & 15) * 8, the byte offset of its (x, y)
+    // pair in the staged gradient table (stage_gradients)
     __device__ __forceinline__ float2 grad2(int b) const {
         const int kb = tab(kT3Second + b);
         return *reinterpret_cast<const float2*>(reinterpret_cast<const char*>(g) + kb);
@@ -153,7 +170,11 @@ struct NoiseT {
     __device__ __forceinline__ float4 grad3(int b1, int b2) const {
         const int a = tab(b1);
         const int kb = tab(kT3Second + b2 + a);
-        return *reinterpret_cast<const float4*>(reinterpret_cast<const char*>(g) + kb);  // one 16-byte shared load
+        // the (x, y) pair and, 128 bytes on, z (stage_gradients): two
+        // conflict-free shared loads
+        const char* e = reinterpret_cast<const char*>(g) + kb;
+        const float2 xy = *reinterpret_cast<const float2*>(e);
+        return make_float4(xy.x, xy.y, *reinterpret_cast<const float*>(e + 128), 0.f);
     }
 
     // one corner of snoise3 with its gradient

@@ -197,7 +197,7 @@ __device__ __forceinline__ float unit(uint64_t h) { return (float)(h >> 40) * (1
 __global__ void k_samples(float4* out, int n, uint64_t seed, Domain dom, const uint8_t* perm_t3,
                           const float* grad, DensityParams dp, float band) {
     __shared__ __align__(16) float sg[64];
-    if (threadIdx.x < 64) sg[threadIdx.x] = grad[threadIdx.x];
+    stage_gradients(sg, grad);
     __syncthreads();
     const Noise nz{perm_t3, sg};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {

@@ -69,9 +69,10 @@ typedef lvn_density_params DensityParams;
 // texels: row r, column c holds texel (r & 255, c & 255), so a corner's +x, +y
 // or +z neighbour needs no wrap.  The first table holds snoise3's first
 // lookup's result (the alpha read as a column, 255 as 0).  The second, from
-// byte kT3Second, holds a texel's gradient as a byte offset ((alpha & 15) * 16)
-// into the 16 x float4 gradient table: snoise3's second lookup and snoise2's
-// three corners read it.
+// byte kT3Second, holds a texel's gradient as a byte offset ((alpha & 15) * 8)
+// into the gradient table as the kernels stage it in shared memory (the 16
+// (x, y) pairs, then the 16 z components at the same 8-byte stride):
+// snoise3's second lookup and snoise2's three corners read it.
 constexpr int kT3Row = 257;
 constexpr int kT3Second = 66064;  // 257 * 257 rounded up to 16 bytes
 constexpr int kT3Bytes = 2 * kT3Second;
