@@ -60,9 +60,10 @@ extern "C" {
                                       transfers stay outside the order, so they overlap the next
                                       batch's kernels (default 0) */
 #define LVN_OPT_HERMITE_FORM  7   /* new: the hermite kernel's form.  0 = by batch size (default):
-                                      batches of 2048 chunks and more stage the noise lookup
-                                      tables in shared memory (one 1024-thread CTA per SM), smaller
-                                      ones read them from global memory; 1 = shared-memory tables
+                                      batches of 256 chunks and more with the caves density, of
+                                      2048 and more with the others, stage the noise lookup tables
+                                      in shared memory (one 1024-thread CTA per SM), smaller ones
+                                      read them from global memory; 1 = shared-memory tables
                                       for every batch; 2 = global tables for every batch.  The
                                       results are the same bits in every form */
 

@@ -39,7 +39,12 @@ namespace {
 constexpr unsigned FULL = 0xffffffffu;
 constexpr int kThreads = 256;
 constexpr int kHermiteSmemThreads = 1024;   // k_hermite_smem: one CTA per SM
-constexpr int kHermiteSmemMinChunks = 2048;  // batches at least this large take k_hermite_smem
+// batches at least this large take k_hermite_smem: with the caves density,
+// whose 3D fBm reads the tables most, from 256 chunks (the sweep's first 256,
+// 512 and 1024 chunks ran 5%, 4% and 4% faster a step than with k_hermite);
+// with a heightfield alone from 2048 (a 128-chunk batch ran 8% slower)
+constexpr int kHermiteSmemMinChunks = 2048;
+constexpr int kHermiteSmemMinChunksCaves = 256;
 
 // ---------------------------------------------------------------------------
 // geometry
@@ -2787,7 +2792,8 @@ cudaError_t launch_edge_scatter(const BatchPtrs& b, cudaStream_t s) {
 }
 
 cudaError_t launch_hermite(const BatchPtrs& b, cudaStream_t s) {
-    const bool shared_tables = b.hermite_form == 1 || (b.hermite_form == 0 && b.n >= kHermiteSmemMinChunks);
+    const int min_chunks = b.density.mode == LVN_DENSITY_CAVES ? kHermiteSmemMinChunksCaves : kHermiteSmemMinChunks;
+    const bool shared_tables = b.hermite_form == 1 || (b.hermite_form == 0 && b.n >= min_chunks);
     if (shared_tables) {
         // the tuned grid in 256-thread units per SM, as for the other stages:
         // 4 units are one 1024-thread CTA per SM, 2 leave half the SMs free

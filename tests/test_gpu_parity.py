@@ -503,7 +503,7 @@ def test_graph_and_stream_paths_agree(lvn_gpu):
 @pytest.mark.parametrize("mode", [0, 1, 2])
 def test_hermite_forms_agree(lvn_gpu, mode):
     """LVN_OPT_HERMITE_FORM: the hermite kernel with its noise lookup tables in
-    shared memory (the form batches of 2048 chunks and more take) and the one
+    shared memory (the form large batches take by default) and the one
     reading them from global memory give the same bits on the same batch, and
     the shared-memory form matches the oracle on chunks with CSG operations."""
     lvn = lvn_gpu
