@@ -119,6 +119,25 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(values, world, device):
+    """Each figure's maximum over the ranks (an all-reduce MAX over the
+    process group; the identity for one rank): the replicas' step time is the
+    slowest rank's."""
+    if world <= 1:
+        return [float(v) for v in values]
+    import torch
+
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return t.tolist()
+
+
+def replicas_rate(world, chunks_per_rank, ms):
+    """Whole-job chunks/s of `world` independent replicas, each meshing
+    `chunks_per_rank` chunks a step, from the slowest rank's step time."""
+    return world * chunks_per_rank / (ms / 1e3)
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -511,14 +530,11 @@ def run_lvn(args):
     ms_single = sum(t_e2e) / len(t_e2e)
     for x in extra:
         x[0].close()
-    if world > 1:
-        t = torch.tensor([ms, ms_single, ms_pipe], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms, ms_single, ms_pipe = t.tolist()
-    value = world * n / (ms / 1e3)
+    ms, ms_single, ms_pipe = max_over_ranks([ms, ms_single, ms_pipe], world, dev)
+    value = replicas_rate(world, n, ms)
     ms_e2e = ms_pipe
-    e2e = world * n / (ms_e2e / 1e3)
-    e2e_single = world * n / (ms_single / 1e3)
+    e2e = replicas_rate(world, n, ms_e2e)
+    e2e_single = replicas_rate(world, n, ms_single)
 
     # per-stage device times (profiled pass, synchronising between stages)
     mg.reset_stage_times()
